@@ -1,0 +1,890 @@
+/*
+ * CPU ORACLE for the lattice-Boltzmann time step -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain C++ restatement of the reference solver's single-phase time step
+ * (ZPaulo/Thesis, "Source code/lbm-solver_final"), used by tests/, by
+ * __graft_entry__.smoke() and by bench.py's CPU baseline as the checker.  The
+ * product (thesis_gb300/) never links or calls it.
+ *
+ * Two semantics, selected per run by orc_params.mode:
+ *   mode 0 (reference): the reference's loop and quirks, restated in the same
+ *     expression order so FP32 results match the reference kernels compiled
+ *     for the host (oracle/_ref) to the last bit on x86 without FMA.
+ *   mode 1 (physics): the standard formulations the reference approximates:
+ *     equilibrium start, half-way bounce-back from the node's own outgoing
+ *     population, full Zou-He velocity/pressure faces, D2Q9 MRT equilibria
+ *     without the extra density factor, D3Q19 MRT writing all 19 outputs,
+ *     TRT in 3D, no forced v=0 on east outlets, and every link towards a
+ *     solid or out-of-domain node treated as a wall link.
+ *
+ * Files restated (file:line within Source code/lbm-solver_final/):
+ *   lattice tables          GpuInit.cu:94-99 (D2Q9), :822-842 (D3Q19)
+ *   BC masks / stream flags GpuInit.cu:1055-1122 (2D), :1157-1238 (3D);
+ *                           bit layouts include/BcMacros.h, include/BcMacros3D.h
+ *   equilibria              GpuCollision.cu:21-32
+ *   BGK                     GpuCollision.cu:528-550, :882-916
+ *   TRT                     GpuCollision.cu:917-969 (omegaA GpuInit.cu:103)
+ *   MRT                     GpuCollision.cu:971-1037, :1039-1170;
+ *                           matrices CellFunctions.cu:7-153
+ *   streaming               GpuStream.cu:8-28, :160-194
+ *   inlet (Zou-He velocity) GpuBoundaries.cu:12-71 (2D), :73-399 (3D)
+ *   straight walls          GpuBoundaries.cu:400-443 (2D), :445-490 (3D)
+ *   2D outlets              GpuBoundaries.cu:1562-1653
+ *   3D periodic / symmetry  GpuBoundaries.cu:2025-2168
+ *   macroscopic update      GpuUpdateMacro.cu:6-41 (2D), :137-213 (3D)
+ *   L2 residual             ComputeResiduals.cu:13-26
+ *   loop order              Iterate.cu:385-518, Iterate3D.cu:493-653
+ *
+ * Not restated (the entry points return ORC_UNSUPPORTED): curved walls, the
+ * HH "complex" 3D wall, the 3D outlet kernel (it addresses directions with the
+ * 2D plane size, GpuBoundaries.cu:1662, so it rewrites other nodes) and the
+ * INLET_PROF 3D profile the reference itself refuses (Iterate3D.cu:200-206).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_OK 0
+#define ORC_UNSUPPORTED 3
+#define ORC_BAD_INPUT 4
+
+namespace {
+
+/* ---------------- lattice tables (reference ordering) ---------------- */
+const int cx2[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+const int cy2[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+const int opp2[9] = {0, 3, 4, 1, 2, 7, 8, 5, 6};
+
+const int cx3[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+const int cy3[19] = {0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1};
+const int cz3[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1};
+const int opp3[19] = {0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15};
+
+/* D2Q9 moment basis M (CellFunctions.cu:31-40) and diag(S) (:47-55). */
+const double M2[81] = {
+    1, 1, 1, 1, 1, 1, 1, 1, 1,      -4, -1, -1, -1, -1, 2, 2, 2, 2,
+    4, -2, -2, -2, -2, 1, 1, 1, 1,  0, 1, 0, -1, 0, 1, -1, -1, 1,
+    0, -2, 0, 2, 0, 1, -1, -1, 1,   0, 0, 1, 0, -1, 1, 1, -1, -1,
+    0, 0, -2, 0, 2, 1, 1, -1, -1,   0, 1, -1, 1, -1, 0, 0, 0, 0,
+    0, 0, 0, 0, 0, 1, -1, 1, -1};
+/* D3Q19 moment basis (CellFunctions.cu:94-113), reference direction order. */
+const double M3[361] = {
+    1,   1,   1,   1,   1,   1,   1,   1, 1, 1, 1, 1, 1, 1, 1, 1,  1,  1,  1,
+    -30, -11, -11, -11, -11, -11, -11, 8, 8, 8, 8, 8, 8, 8, 8, 8,  8,  8,  8,
+    12,  -4,  -4,  -4,  -4,  -4,  -4,  1, 1, 1, 1, 1, 1, 1, 1, 1,  1,  1,  1,
+    0,   1,   -1,  0,   0,   0,   0,   1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0,
+    0,   -4,  4,   0,   0,   0,   0,   1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0,
+    0,   0,   0,   1,   -1,  0,   0,   1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1,
+    0,   0,   0,   -4,  4,   0,   0,   1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1,
+    0,   0,   0,   0,   0,   1,   -1,  0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1,
+    0,   0,   0,   0,   0,   -4,  4,   0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1,
+    0,   2,   2,   -1,  -1,  -1,  -1,  1, 1, 1, 1, 1, 1, 1, 1, -2, -2, -2, -2,
+    0,   -4,  -4,  2,   2,   2,   2,   1, 1, 1, 1, 1, 1, 1, 1, -2, -2, -2, -2,
+    0,   0,   0,   1,   1,   -1,  -1,  1, 1, 1, 1, -1, -1, -1, -1, 0, 0, 0, 0,
+    0,   0,   0,   -2,  -2,  2,   2,   1, 1, 1, 1, -1, -1, -1, -1, 0, 0, 0, 0,
+    0,   0,   0,   0,   0,   0,   0,   1, -1, -1, 1, 0, 0, 0, 0, 0, 0, 0, 0,
+    0,   0,   0,   0,   0,   0,   0,   0, 0, 0, 0, 0, 0, 0, 0, 1, -1, -1, 1,
+    0,   0,   0,   0,   0,   0,   0,   0, 0, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0,
+    0,   0,   0,   0,   0,   0,   0,   1, -1, 1, -1, -1, 1, -1, 1, 0, 0, 0, 0,
+    0,   0,   0,   0,   0,   0,   0,   -1, -1, 1, 1, 0, 0, 0, 0, 1, -1, 1, -1,
+    0,   0,   0,   0,   0,   0,   0,   0, 0, 0, 0, 1, 1, -1, -1, -1, -1, 1, 1};
+
+/* Bit layout of the reference BC masks. */
+inline uint64_t bc2_mask(uint64_t type, int dir) { return type << ((dir - 1) * 2); }
+const uint64_t BC2_B_ALL = 3ull << 16, BC2_WALL_B = 1ull << 16, BC2_CORNER = 1ull << 18,
+               BC2_FLUID = 1ull << 19, BC2_INLT_B = 2ull << 16;
+inline uint64_t bc3_mask(uint64_t type, int dir) { return type << ((dir - 1) * 3); }
+const uint64_t BC3_B_ALL = 7ull << 54, BC3_WALL_B = 1ull << 54, BC3_INLT_B = 2ull << 54,
+               BC3_OUTL_B = 3ull << 54, BC3_CYCL_B = 4ull << 54, BC3_SYMP_B = 5ull << 54,
+               BC3_CORNER = 1ull << 57, BC3_FLUID = 1ull << 58;
+
+}  // namespace
+
+extern "C" {
+
+/* Mirrors the reference Arguments fields read by the loop, plus the values
+ * Iterate2D/3D derive from the mesh, plus the extensions of this build. */
+typedef struct {
+    double u, v, w, rho, viscosity, g;
+    int inlet_profile;   /* 1 INLET, 2 NO_INLET, 4 pressure inlet (physics) */
+    int outlet_profile;  /* 1 OUTLET Zou-He, 2 SECOND, 3 FIRST, 4 HEmodel, 5 pressure (physics) */
+    int collision_model; /* 1 BGKW, 2 TRT, 3 MRT */
+    int boundary_type;   /* 1 CURVED, 2 STRAIGHT */
+    int bc_wall_model;   /* 1 SIMPLE, 2 COMPLEX */
+    int update_inlet_outlet;
+    int boundary_id;
+    double delta, min_inlet_y, max_inlet_y, min_inlet_z, max_inlet_z;
+    int mode;            /* 0 reference semantics, 1 physics */
+    int init_kind;       /* 0 f=0 (reference), 1 f=feq(rho,u) */
+    double rho_in, rho_out;
+} orc_params;
+
+}  // extern "C"
+
+namespace {
+
+template <class T>
+inline T feqc2(T u, T uc, T v, T vc, T rho, T w) {
+    T vec = u * uc + v * vc;
+    return rho * w * (1. + 3. * vec + 4.5 * vec * vec - 1.5 * (u * u + v * v));
+}
+template <class T>
+inline T feqc3(T u, T uc, T v, T vc, T w, T wc, T rho, T weight) {
+    T vec = u * uc + v * vc + w * wc;
+    return rho * weight * (1. + 3. * vec + 4.5 * vec * vec - 1.5 * (u * u + v * v + w * w));
+}
+
+template <class T>
+struct Lattice {
+    int dims = 2, q = 9, n = 0, m = 0, h = 1, N = 0;
+    orc_params p;
+    T omega, omegaA;
+    T w[19];
+    int off[19]; /* linear pull offsets (c2D_d / c3D_d) */
+    std::vector<int> fluid;
+    std::vector<T> f, fc, rho, u, v, w3, u0, v0, w0;
+    std::vector<uint64_t> mask;    /* reference BC mask per node */
+    std::vector<uint8_t> stream;   /* (q-1)*N, 1 = streamed */
+    std::vector<int> bcnodes;      /* collapsed BC node list, ascending */
+    T msc[361];                    /* reference M^-1 S, row-major */
+    T mm[361];                     /* reference M */
+
+    int X(int i) const { return i % n; }
+    int Y(int i) const { return (i / n) % m; }
+    int Z(int i) const { return i / (n * m); }
+
+    /* Pull source of population d at node i: the reference adds a linear
+     * offset; out-of-domain pulls wrap periodically here (the reference reads a
+     * neighbouring row or past the array there, which the generator's
+     * boundary links always prevent). */
+    int src(int i, int d) const {
+        int x = X(i), y = Y(i), z = Z(i);
+        int cx = dims == 2 ? cx2[d] : cx3[d], cy = dims == 2 ? cy2[d] : cy3[d];
+        int cz = dims == 2 ? 0 : cz3[d];
+        x = (x - cx + n) % n;
+        y = (y - cy + m) % m;
+        z = (z - cz + h) % h;
+        return x + n * (y + m * z);
+    }
+    int opp(int d) const { return dims == 2 ? opp2[d] : opp3[d]; }
+};
+
+/* ----------------------------- set-up ----------------------------------- */
+
+template <class T>
+void build_tables(Lattice<T> &L) {
+    const int n = L.n, m = L.m;
+    if (L.dims == 2) {
+        const T w2[9] = {4. / 9., 1. / 9., 1. / 9., 1. / 9., 1. / 9., 1. / 36., 1. / 36., 1. / 36., 1. / 36.};
+        const int c2[9] = {0, -1, -n, 1, n, -n - 1, -n + 1, n + 1, n - 1};
+        for (int d = 0; d < 9; ++d) {
+            L.w[d] = w2[d];
+            L.off[d] = c2[d];
+        }
+    } else {
+        const T w3[19] = {1. / 3.,  1. / 18., 1. / 18., 1. / 18., 1. / 18., 1. / 18., 1. / 18.,
+                          1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36.,
+                          1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36.};
+        const int mn = m * n;
+        const int c3[19] = {0,       -1,      1,       -n,      n,       -mn,     mn,
+                            -n - 1,  -n + 1,  n - 1,   n + 1,   -mn - 1, -mn + 1, mn - 1,
+                            mn + 1,  -mn - n, -mn + n, mn - n,  mn + n};
+        for (int d = 0; d < 19; ++d) {
+            L.w[d] = w3[d];
+            L.off[d] = c3[d];
+        }
+    }
+    /* GpuInit.cu:102-103 / :845-846, evaluated in the storage type. */
+    L.omega = (T)(1.0 / (3. * (T)L.p.viscosity + 0.5));
+    L.omegaA = (T)(8 * (2 - L.omega) / (8 - L.omega));
+    /* MRT: M and M^-1 S with M^-1 = M^T diag(1/|row|^2) (the reference's
+     * hard-coded M^-1 equals this exactly, CellFunctions.cu:14-24, :70-90). */
+    const int q = L.q;
+    const double *M = q == 9 ? M2 : M3;
+    double s[19];
+    if (q == 9) {
+        const double s2[9] = {1.0, 1.4, 1.4, 1.0, 1.2, 1.0, 1.2, (double)L.omega, (double)L.omega};
+        for (int k = 0; k < 9; ++k) s[k] = s2[k];
+    } else {
+        const double om = (double)L.omega;
+        const double s3[19] = {0.0, 1.19, 1.4, 0.0, 1.2, 0.0, 1.2, 0.0, 1.2, om,
+                               1.4, om,   1.4, om,  om,  om,  1.98, 1.98, 1.98};
+        for (int k = 0; k < 19; ++k) s[k] = s3[k];
+    }
+    for (int k = 0; k < q; ++k) {
+        double nrm = 0;
+        for (int i = 0; i < q; ++i) nrm += M[k * q + i] * M[k * q + i];
+        for (int i = 0; i < q; ++i) {
+            L.mm[k * q + i] = (T)M[k * q + i];
+            /* (M^-1 S)[i][k] = M[k][i] / |row k|^2 * s_k */
+            L.msc[i * q + k] = (T)((T)(M[k * q + i] / nrm) * (T)s[k]);
+        }
+    }
+}
+
+/* initBoundaryConditions2D/3D + collapseBc2D/3D, restated. */
+template <class T>
+int build_masks(Lattice<T> &L, int nconn, const int *bi, const int *bj, const int *bk,
+                const int *bdir, const int *btype, const int *bid) {
+    const int N = L.N, q = L.q;
+    L.mask.assign(N, 0ull);
+    L.stream.assign((size_t)(q - 1) * N, 1);
+    std::vector<int> flag(N, 0);
+    for (int c = 0; c < nconn; ++c) {
+        int ind = bi[c] + bj[c] * L.n + (L.dims == 3 ? bk[c] * L.n * L.m : 0);
+        int dir = bdir[c];
+        if (ind < 0 || ind >= N || dir < 1 || dir >= q) return ORC_BAD_INPUT;
+        uint64_t &mk = L.mask[ind];
+        uint64_t type = (uint64_t)btype[c];
+        if (L.dims == 2) {
+            mk |= bc2_mask(type, dir);
+            mk |= (uint64_t)L.fluid[ind] << 19;
+            if (!(mk & BC2_B_ALL)) {
+                mk |= type << 16;
+            } else if ((mk & BC2_B_ALL) != (type << 16)) {
+                mk &= ~BC2_B_ALL;
+                mk |= BC2_WALL_B;
+                mk |= BC2_CORNER;
+            }
+            /* BOUND_ID(id) = id << 24 on a 32-bit int mask (BcMacros.h:74) */
+            uint32_t m32 = (uint32_t)mk | ((uint32_t)bid[c] << 24);
+            mk = m32;
+        } else {
+            mk |= bc3_mask(type, dir);
+            mk |= (uint64_t)L.fluid[ind] << 58;
+            if (!(mk & BC3_B_ALL)) {
+                mk |= type << 54;
+            } else if ((mk & BC3_B_ALL) != (type << 54)) {
+                mk &= ~BC3_B_ALL;
+                mk |= BC3_WALL_B;
+                mk |= BC3_CORNER;
+            }
+        }
+        L.stream[(size_t)(L.opp(dir) - 1) * N + ind] = 0; /* no stream opposite the BC link */
+        flag[ind] = 1;
+    }
+    for (int c = 0; c < nconn; ++c) {
+        int ind = bi[c] + bj[c] * L.n + (L.dims == 3 ? bk[c] * L.n * L.m : 0);
+        uint64_t &mk = L.mask[ind];
+        if (L.dims == 2) {
+            if (mk & BC2_CORNER) {
+                auto any = [&](int d) { return (mk & bc2_mask(3, d)) != 0; };
+                if (any(1) && any(2)) { mk &= ~bc2_mask(3, 5); mk |= bc2_mask(1, 5); }
+                if (any(3) && any(2)) { mk &= ~bc2_mask(3, 6); mk |= bc2_mask(1, 6); }
+                if (any(3) && any(4)) { mk &= ~bc2_mask(3, 7); mk |= bc2_mask(1, 7); }
+                if (any(1) && any(4)) { mk &= ~bc2_mask(3, 8); mk |= bc2_mask(1, 8); }
+            }
+        } else if (mk & BC3_CORNER) {
+            /* every typed link of a mixed-type node becomes a wall link */
+            for (int d = 1; d < 19; ++d)
+                if (mk & bc3_mask(7, d)) {
+                    mk &= ~bc3_mask(7, d);
+                    mk |= bc3_mask(1, d);
+                }
+        }
+    }
+    L.bcnodes.clear();
+    for (int i = 0; i < N; ++i)
+        if (flag[i]) L.bcnodes.push_back(i);
+    return ORC_OK;
+}
+
+/* ----------------------------- collision -------------------------------- */
+
+template <class T>
+void collide_node(Lattice<T> &L, int i) {
+    const int N = L.N;
+    const T om = L.omega;
+    T *f = L.f.data();
+    T *fc = L.fc.data();
+    const T r = L.rho[i], u = L.u[i], v = L.v[i];
+    const bool phys = L.p.mode == 1;
+    if (L.dims == 2) {
+        switch (L.p.collision_model) {
+        case 1:
+            for (int d = 0; d < 9; ++d)
+                fc[i + d * N] = om * feqc2<T>(u, (T)cx2[d], v, (T)cy2[d], r, L.w[d]) + (1.0 - om) * f[i + d * N];
+            break;
+        case 2: {
+            T feq[9], fl[9];
+            for (int d = 0; d < 9; ++d) {
+                feq[d] = feqc2<T>(u, (T)cx2[d], v, (T)cy2[d], r, L.w[d]);
+                fl[d] = f[i + d * N];
+            }
+            for (int d = 0; d < 9; ++d) {
+                int o = opp2[d];
+                fc[i + d * N] = fl[d] - 0.5 * om * (fl[d] + fl[o] - feq[d] - feq[o]) -
+                                0.5 * L.omegaA * (fl[d] - fl[o] - feq[d] + feq[o]);
+            }
+            break;
+        }
+        case 3: {
+            T meq[9], mo[9], col[9], fl[9];
+            meq[0] = r;
+            if (!phys) {
+                meq[1] = r * (-2. + 3. * r * (u * u + v * v));
+                meq[2] = r * (1. - 3. * r * (u * u + v * v));
+            } else { /* e_eq = -2 rho + 3 |j|^2 / rho, eps_eq = rho - 3 |j|^2 / rho */
+                meq[1] = r * (-2. + 3. * (u * u + v * v));
+                meq[2] = r * (1. - 3. * (u * u + v * v));
+            }
+            meq[3] = r * u;
+            meq[4] = -r * u;
+            meq[5] = r * v;
+            meq[6] = -r * v;
+            meq[7] = r * (u * u - v * v);
+            meq[8] = r * u * v;
+            for (int d = 0; d < 9; ++d) fl[d] = f[i + d * N];
+            for (int a = 0; a < 9; ++a) {
+                mo[a] = 0;
+                for (int b = 0; b < 9; ++b) mo[a] += L.mm[a * 9 + b] * fl[b];
+            }
+            for (int a = 0; a < 9; ++a) {
+                col[a] = 0;
+                for (int b = 0; b < 9; ++b) col[a] += L.msc[a * 9 + b] * (mo[b] - meq[b]);
+            }
+            for (int d = 0; d < 9; ++d) fc[i + d * N] = fl[d] - col[d];
+            break;
+        }
+        }
+        return;
+    }
+    const T w = L.w3[i];
+    switch (L.p.collision_model) {
+    case 1:
+        for (int d = 0; d < 19; ++d)
+            fc[i + d * N] = om * feqc3<T>(u, (T)cx3[d], v, (T)cy3[d], w, (T)cz3[d], r, L.w[d]) + (1.0 - om) * f[i + d * N];
+        break;
+    case 2: { /* physics mode only: the reference has no 3D TRT */
+        T feq[19], fl[19];
+        for (int d = 0; d < 19; ++d) {
+            feq[d] = feqc3<T>(u, (T)cx3[d], v, (T)cy3[d], w, (T)cz3[d], r, L.w[d]);
+            fl[d] = f[i + d * N];
+        }
+        for (int d = 0; d < 19; ++d) {
+            int o = opp3[d];
+            fc[i + d * N] = fl[d] - 0.5 * om * (fl[d] + fl[o] - feq[d] - feq[o]) -
+                            0.5 * L.omegaA * (fl[d] - fl[o] - feq[d] + feq[o]);
+        }
+        break;
+    }
+    case 3: {
+        T meq[19], mo[19], col[19], fl[19];
+        T jx = r * u, jy = r * v, jz = r * w;
+        T wej = -475. / 63.;
+        meq[0] = r;
+        meq[1] = -11. * r + 19. * (jx * jx + jy * jy + jz * jz);
+        meq[2] = wej * (jx * jx + jy * jy + jz * jz);
+        meq[3] = jx;
+        meq[4] = -(2. / 3.) * jx;
+        meq[5] = jy;
+        meq[6] = -(2. / 3.) * jy;
+        meq[7] = jz;
+        meq[8] = -(2. / 3.) * jz;
+        meq[9] = (2 * jx * jx - (jy * jy + jz * jz));
+        meq[10] = 0.0;
+        meq[11] = jy * jy - jz * jz;
+        meq[12] = 0.0;
+        meq[13] = jx * jy;
+        meq[14] = jy * jz;
+        meq[15] = jx * jz;
+        meq[16] = 0.0;
+        meq[17] = 0.0;
+        meq[18] = 0.0;
+        for (int d = 0; d < 19; ++d) fl[d] = f[i + d * N];
+        for (int a = 0; a < 19; ++a) {
+            mo[a] = 0.;
+            for (int b = 0; b < 19; ++b) mo[a] += L.mm[a * 19 + b] * fl[b];
+        }
+        for (int a = 0; a < 19; ++a) {
+            col[a] = 0.;
+            for (int b = 0; b < 19; ++b) col[a] += L.msc[a * 19 + b] * (mo[b] - meq[b]);
+        }
+        /* the reference never writes direction 18 (GpuCollision.cu:1161) */
+        int last = phys ? 19 : 18;
+        for (int d = 0; d < last; ++d) fc[i + d * N] = fl[d] - col[d];
+        break;
+    }
+    }
+}
+
+template <class T>
+void collide_all(Lattice<T> &L) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < L.N; ++i)
+        if (L.fluid[i] == 1) collide_node(L, i);
+}
+
+/* ------------------------------ streaming -------------------------------- */
+
+template <class T>
+void stream_all(Lattice<T> &L) {
+    const int N = L.N, q = L.q;
+    const bool phys = L.p.mode == 1;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < N; ++i) {
+        if (L.fluid[i] != 1) continue;
+        L.f[i] = L.fc[i];
+        for (int d = 1; d < q; ++d) {
+            bool st = L.stream[(size_t)(d - 1) * N + i] != 0;
+            int s = L.src(i, d);
+            if (phys && st && L.fluid[s] != 1) st = false;
+            if (st)
+                L.f[i + (size_t)d * N] = L.fc[s + (size_t)d * N];
+            else if (phys) /* half-way bounce-back of the node's own outgoing population */
+                L.f[i + (size_t)d * N] = L.fc[i + (size_t)L.opp(d) * N];
+            else
+                L.f[i + (size_t)d * N] = L.fc[i + (size_t)d * N];
+        }
+    }
+}
+
+/* --------------------------- 2D boundaries ------------------------------- */
+
+template <class T>
+void bc_node_2d(Lattice<T> &L, int i, uint64_t mk) {
+    const int N = L.N;
+    T *f = L.f.data();
+    auto F = [&](int d) -> T & { return f[i + (size_t)d * N]; };
+    if (!(mk & BC2_FLUID)) return;
+    const bool phys = L.p.mode == 1;
+    const T u0 = L.u0[i], v0 = L.v0[i];
+    /* inlet (GpuBoundaries.cu:12-71) */
+    if (mk & BC2_INLT_B) {
+        bool north = (mk & bc2_mask(2, 2)) && !(mk & BC2_CORNER);
+        bool west = (mk & bc2_mask(2, 3)) && !(mk & BC2_CORNER);
+        if (north) {
+            if (!phys) {
+                F(4) = F(2);
+                F(8) = F(6) + (F(0) + F(1) + F(3) + 2 * (F(2) + F(6) + F(5))) * u0 / 6.0;
+                F(7) = F(5) - (F(0) + F(1) + F(3) + 2 * (F(2) + F(6) + F(5))) * u0 / 6.0;
+            } else {
+                T r = (F(0) + F(1) + F(3) + 2 * (F(2) + F(5) + F(6))) / (1 + v0);
+                T h13 = (F(1) - F(3)) / 2;
+                F(4) = F(2) - (T)(2. / 3.) * r * v0;
+                F(7) = F(5) + h13 - r * u0 / 2 - r * v0 / 6;
+                F(8) = F(6) - h13 + r * u0 / 2 - r * v0 / 6;
+            }
+        }
+        if (west) {
+            if (!phys) {
+                F(1) = F(3) + 2. * ((F(0) + F(2) + F(4) + 2. * (F(3) + F(6) + F(7))) / (1.0 - u0)) * u0 / 3;
+                F(5) = F(7) + ((F(0) + F(2) + F(4) + 2. * (F(3) + F(6) + F(7))) / (1.0 - u0)) * u0 / 6;
+                F(8) = F(6) + ((F(0) + F(2) + F(4) + 2. * (F(3) + F(6) + F(7))) / (1.0 - u0)) * u0 / 6;
+            } else {
+                T r = (F(0) + F(2) + F(4) + 2 * (F(3) + F(6) + F(7))) / (1 - u0);
+                T h24 = (F(2) - F(4)) / 2;
+                F(1) = F(3) + (T)(2. / 3.) * r * u0;
+                F(5) = F(7) - h24 + r * u0 / 6 + r * v0 / 2;
+                F(8) = F(6) + h24 + r * u0 / 6 - r * v0 / 2;
+            }
+        }
+    }
+    /* straight wall (GpuBoundaries.cu:400-443): f[opp(dir)] = f[dir] after
+     * streaming, in direction order.  Physics mode bounced back in streaming. */
+    if (!phys) {
+        for (int dir = 1; dir < 9; ++dir) {
+            uint64_t all = mk & bc2_mask(3, dir), wall = mk & bc2_mask(1, dir);
+            if (all == wall && wall) F(opp2[dir]) = F(dir);
+        }
+    }
+    /* east outlet (GpuBoundaries.cu:1562-1653) */
+    if ((mk & bc2_mask(3, 1)) == bc2_mask(3, 1)) {
+        switch (L.p.outlet_profile) {
+        case 1:
+            if (!phys) {
+                F(3) = F(1) - 2 * ((F(0) + F(2) + F(4) + 2 * (F(1) + F(5) + F(8))) / (1 - u0)) * u0 / 3;
+                F(7) = F(5) - ((F(0) + F(2) + F(4) + 2 * (F(1) + F(5) + F(8))) / (1 - u0)) * u0 / 6;
+                F(6) = F(8) - ((F(0) + F(2) + F(4) + 2 * (F(1) + F(5) + F(8))) / (1 - u0)) * u0 / 6;
+            } else { /* Zou-He velocity outlet, u0 outward-normal */
+                T r = (F(0) + F(2) + F(4) + 2 * (F(1) + F(5) + F(8))) / (1 + u0);
+                T h24 = (F(2) - F(4)) / 2;
+                F(3) = F(1) - (T)(2. / 3.) * r * u0;
+                F(7) = F(5) + h24 - r * u0 / 6 - r * v0 / 2;
+                F(6) = F(8) - h24 - r * u0 / 6 + r * v0 / 2;
+            }
+            break;
+        case 2:
+            F(1) = 2 * f[i + N - 1] - f[i + N - 2];
+            F(5) = 2 * f[i + 5 * N - 1] - f[i + 5 * N - 2];
+            F(8) = 2 * f[i + 8 * N - 1] - f[i + 8 * N - 2];
+            break;
+        case 3:
+            F(1) = f[i - 1 + N];
+            F(5) = f[i - 1 + 5 * N];
+            F(8) = f[i - 1 + 8 * N];
+            break;
+        case 5: { /* physics: Zou-He pressure outlet at rho_out */
+            T r = (T)L.p.rho_out;
+            T ux = -1 + (F(0) + F(2) + F(4) + 2 * (F(1) + F(5) + F(8))) / r;
+            T h24 = (F(2) - F(4)) / 2;
+            F(3) = F(1) - (T)(2. / 3.) * r * ux;
+            F(7) = F(5) + h24 - r * ux / 6;
+            F(6) = F(8) - h24 - r * ux / 6;
+            break;
+        }
+        }
+    }
+}
+
+/* --------------------------- 3D boundaries ------------------------------- */
+
+/* Zou-He velocity face of the reference (Hecht-Harting transverse
+ * corrections, GpuBoundaries.cu:92-394), face order W,E,S,N,B,T.  The
+ * reference's west and east densities divide by (1+u) and (1-u), the reverse
+ * of the mass balance rho (1 -/+ u) = known sums that its other four faces
+ * use; fixed_we selects the mass-balance form (physics mode). */
+template <class T>
+void zou_he_3d(T *f, size_t N, int i, int face, T uu, T vv, T ww, bool fixed_we = false) {
+    auto F = [&](int d) -> T & { return f[i + (size_t)d * N]; };
+    T d_, n1, n2;
+    switch (face) {
+    case 2: /* WEST */
+        d_ = 1.0 / (fixed_we ? 1.0 - uu : 1.0 + uu) * (F(0) + F(3) + F(4) + F(5) + F(6) + F(15) + F(16) + F(17) + F(18) + 2.0 * (F(2) + F(8) + F(10) + F(12) + F(14)));
+        n1 = 0.5 * (F(3) + F(15) + F(17) - (F(4) + F(16) + F(18))) - 1.0 / 3.0 * d_ * vv;
+        n2 = 0.5 * (F(5) + F(15) + F(16) - (F(6) + F(17) + F(18))) - 1.0 / 3.0 * d_ * ww;
+        F(1) = F(2) + 1.0 / 3.0 * d_ * uu;
+        F(7) = F(10) + 1.0 / 6.0 * d_ * (uu + vv) - n1;
+        F(9) = F(8) + 1.0 / 6.0 * d_ * (uu - vv) + n1;
+        F(11) = F(14) + 1.0 / 6.0 * d_ * (uu + ww) - n2;
+        F(13) = F(12) + 1.0 / 6.0 * d_ * (uu - ww) + n2;
+        break;
+    case 1: /* EAST */
+        d_ = 1.0 / (fixed_we ? 1.0 + uu : 1.0 - uu) * (F(0) + F(3) + F(4) + F(5) + F(6) + F(15) + F(16) + F(17) + F(18) + 2.0 * (F(1) + F(7) + F(9) + F(11) + F(13)));
+        n1 = 0.5 * (F(3) + F(15) + F(17) - (F(4) + F(16) + F(18))) - 1.0 / 3.0 * d_ * vv;
+        n2 = 0.5 * (F(5) + F(15) + F(16) - (F(6) + F(17) + F(18))) - 1.0 / 3.0 * d_ * ww;
+        F(2) = F(1) - 1.0 / 3.0 * d_ * uu;
+        F(8) = F(9) - 1.0 / 6.0 * d_ * (uu - vv) - n1;
+        F(10) = F(7) - 1.0 / 6.0 * d_ * (uu + vv) + n1;
+        F(12) = F(13) - 1.0 / 6.0 * d_ * (uu - ww) - n2;
+        F(14) = F(11) - 1.0 / 6.0 * d_ * (uu + ww) + n2;
+        break;
+    case 4: /* SOUTH */
+        d_ = 1.0 / (1.0 - vv) * (F(0) + F(1) + F(2) + F(5) + F(6) + F(11) + F(12) + F(13) + F(14) + 2.0 * (F(4) + F(9) + F(10) + F(16) + F(18)));
+        n1 = 0.5 * (F(1) + F(11) + F(13) - (F(2) + F(12) + F(14))) - 1.0 / 3.0 * d_ * uu;
+        n2 = 0.5 * (F(5) + F(11) + F(12) - (F(6) + F(13) + F(14))) - 1.0 / 3.0 * d_ * ww;
+        F(3) = F(4) + 1.0 / 3.0 * d_ * vv;
+        F(7) = F(10) + 1.0 / 6.0 * d_ * (vv + uu) - n1;
+        F(8) = F(9) + 1.0 / 6.0 * d_ * (vv - uu) + n1;
+        F(15) = F(18) + 1.0 / 6.0 * d_ * (vv + ww) - n2;
+        F(17) = F(16) + 1.0 / 6.0 * d_ * (vv - ww) + n2;
+        break;
+    case 3: /* NORTH */
+        d_ = 1.0 / (1.0 + vv) * (F(0) + F(1) + F(2) + F(5) + F(6) + F(11) + F(12) + F(13) + F(14) + 2.0 * (F(3) + F(7) + F(8) + F(15) + F(17)));
+        n1 = 0.5 * (F(1) + F(11) + F(13) - (F(2) + F(12) + F(14))) - 1.0 / 3.0 * d_ * uu;
+        n2 = 0.5 * (F(5) + F(11) + F(12) - (F(6) + F(13) + F(14))) - 1.0 / 3.0 * d_ * ww;
+        F(4) = F(3) - 1.0 / 3.0 * d_ * vv;
+        F(9) = F(8) - 1.0 / 6.0 * d_ * (vv - uu) - n1;
+        F(10) = F(7) - 1.0 / 6.0 * d_ * (vv + uu) + n1;
+        F(16) = F(17) - 1.0 / 6.0 * d_ * (vv - ww) - n2;
+        F(18) = F(15) - 1.0 / 6.0 * d_ * (vv + ww) + n2;
+        break;
+    case 6: /* BOTTOM */
+        d_ = 1.0 / (1.0 - ww) * (F(0) + F(1) + F(2) + F(3) + F(4) + F(7) + F(8) + F(9) + F(10) + 2.0 * (F(6) + F(13) + F(14) + F(17) + F(18)));
+        n1 = 0.5 * (F(1) + F(7) + F(9) - (F(2) + F(8) + F(10))) - 1.0 / 3.0 * d_ * uu;
+        n2 = 0.5 * (F(3) + F(7) + F(8) - (F(4) + F(9) + F(10))) - 1.0 / 3.0 * d_ * vv;
+        F(5) = F(6) + 1.0 / 3.0 * d_ * ww;
+        F(11) = F(14) + 1.0 / 6.0 * d_ * (ww + uu) - n1;
+        F(12) = F(13) + 1.0 / 6.0 * d_ * (ww - uu) + n1;
+        F(15) = F(18) + 1.0 / 6.0 * d_ * (ww + vv) - n2;
+        F(16) = F(17) + 1.0 / 6.0 * d_ * (ww - vv) + n2;
+        break;
+    case 5: /* TOP */
+        d_ = (1.0 / (1.0 + ww)) * (F(0) + F(1) + F(2) + F(3) + F(4) + F(7) + F(8) + F(9) + F(10) + 2.0 * (F(5) + F(11) + F(12) + F(15) + F(16)));
+        n1 = 0.5 * (F(1) + F(7) + F(9) - (F(2) + F(8) + F(10))) - 1.0 / 3.0 * d_ * uu;
+        n2 = 0.5 * (F(3) + F(7) + F(8) - (F(4) + F(9) + F(10))) - 1.0 / 3.0 * d_ * vv;
+        F(6) = F(5) - 1.0 / 3.0 * d_ * ww;
+        F(13) = F(12) - 1.0 / 6.0 * d_ * (ww - uu) - n1;
+        F(14) = F(11) - 1.0 / 6.0 * d_ * (ww + uu) + n1;
+        F(17) = F(16) - 1.0 / 6.0 * d_ * (ww - vv) - n2;
+        F(18) = F(15) - 1.0 / 6.0 * d_ * (ww + vv) + n2;
+        break;
+    }
+}
+
+/* Normal velocity a Zou-He pressure face implies at density rho (physics). */
+template <class T>
+T pressure_face_velocity(const T *f, size_t N, int i, int face, T rho) {
+    auto F = [&](int d) { return f[i + (size_t)d * N]; };
+    if (face == 2) /* west, inflow along +x */
+        return 1 - (F(0) + F(3) + F(4) + F(5) + F(6) + F(15) + F(16) + F(17) + F(18) + 2 * (F(2) + F(8) + F(10) + F(12) + F(14))) / rho;
+    /* east, outflow along +x */
+    return -1 + (F(0) + F(3) + F(4) + F(5) + F(6) + F(15) + F(16) + F(17) + F(18) + 2 * (F(1) + F(7) + F(9) + F(11) + F(13))) / rho;
+}
+
+template <class T>
+void bc_node_3d(Lattice<T> &L, int i, uint64_t mk) {
+    const size_t N = (size_t)L.N;
+    T *f = L.f.data();
+    if (!(mk & BC3_FLUID)) return;
+    const bool phys = L.p.mode == 1;
+    const T uu = L.u0[i], vv = L.v0[i], ww = L.w0[i];
+    /* inlet (GpuBoundaries.cu:73-399) */
+    if (mk & BC3_INLT_B) {
+        const int faces[6] = {2, 1, 4, 3, 6, 5};
+        for (int k = 0; k < 6; ++k) {
+            int face = faces[k];
+            uint64_t inl = bc3_mask(2, face), all = mk & bc3_mask(7, face);
+            bool hit = (mk & inl) && !(mk & BC3_CORNER) &&
+                       (face == 1 ? all == inl : all == (mk & inl));
+            if (!hit) continue;
+            if (phys && L.p.inlet_profile == 4 && face == 2) {
+                T r = (T)L.p.rho_in;
+                T ux = pressure_face_velocity(f, N, i, 2, r);
+                zou_he_3d(f, N, i, 2, ux, (T)0, (T)0, true);
+            } else {
+                zou_he_3d(f, N, i, face, uu, vv, ww, phys);
+            }
+        }
+    }
+    /* straight simple wall (GpuBoundaries.cu:445-490) */
+    if (!phys) {
+        for (int dir = 1; dir < 19; ++dir) {
+            uint64_t all = mk & bc3_mask(7, dir), wall = mk & bc3_mask(1, dir);
+            if (all == wall && wall) f[i + (size_t)opp3[dir] * N] = f[i + (size_t)dir * N];
+        }
+    }
+    /* physics: Zou-He pressure outlet on an east face */
+    if (phys && L.p.outlet_profile == 5 && (mk & bc3_mask(7, 1)) == bc3_mask(3, 1)) {
+        T r = (T)L.p.rho_out;
+        T ux = pressure_face_velocity(f, N, i, 1, r);
+        /* the east unknowns follow the east velocity face with d = rho_out */
+        auto F = [&](int d) -> T & { return f[i + (size_t)d * N]; };
+        T n1 = 0.5 * (F(3) + F(15) + F(17) - (F(4) + F(16) + F(18)));
+        T n2 = 0.5 * (F(5) + F(15) + F(16) - (F(6) + F(17) + F(18)));
+        F(2) = F(1) - 1.0 / 3.0 * r * ux;
+        F(8) = F(9) - 1.0 / 6.0 * r * ux - n1;
+        F(10) = F(7) - 1.0 / 6.0 * r * ux + n1;
+        F(12) = F(13) - 1.0 / 6.0 * r * ux - n2;
+        F(14) = F(11) - 1.0 / 6.0 * r * ux + n2;
+    }
+}
+
+/* 3D periodic copy from the opposite face (GpuBoundaries.cu:2025-2084) and
+ * mirror symmetry (:2086-2168), reference mode. */
+template <class T>
+void periodic_node_3d(Lattice<T> &L, int i, uint64_t mk) {
+    const size_t N = (size_t)L.N;
+    T *f = L.f.data();
+    if (!(mk & BC3_FLUID) || !(mk & BC3_CYCL_B)) return;
+    const int ox = L.n - 1, oy = L.n * (L.m - 1), oz = L.n * L.m * (L.h - 1);
+    auto cp = [&](const int *ds, int off) {
+        for (int k = 0; k < 5; ++k) f[i + (size_t)ds[k] * N] = f[i + (size_t)ds[k] * N + off];
+    };
+    const int dW[5] = {1, 7, 9, 11, 13}, dE[5] = {2, 8, 10, 12, 14}, dS[5] = {3, 7, 8, 15, 17},
+              dN[5] = {4, 9, 10, 16, 18}, dB[5] = {5, 11, 12, 15, 16}, dT[5] = {6, 13, 14, 17, 18};
+    if (mk & bc3_mask(4, 2)) cp(dW, ox);
+    if (mk & bc3_mask(4, 1)) cp(dE, -ox);
+    if (mk & bc3_mask(4, 4)) cp(dS, oy);
+    if (mk & bc3_mask(4, 3)) cp(dN, -oy);
+    if (mk & bc3_mask(4, 6)) cp(dB, oz);
+    if (mk & bc3_mask(4, 5)) cp(dT, -oz);
+}
+
+template <class T>
+void symm_node_3d(Lattice<T> &L, int i, uint64_t mk) {
+    const size_t N = (size_t)L.N;
+    T *f = L.f.data();
+    if (!(mk & BC3_FLUID) || !(mk & BC3_SYMP_B)) return;
+    auto F = [&](int d) -> T & { return f[i + (size_t)d * N]; };
+    auto is = [&](int dir) {
+        return (mk & bc3_mask(5, dir)) && (mk & bc3_mask(7, dir)) == bc3_mask(5, dir);
+    };
+    if (is(2)) { F(1) = F(2); F(7) = F(8); F(9) = F(10); F(11) = F(12); F(13) = F(14); }
+    if (is(1)) { F(2) = F(1); F(8) = F(7); F(10) = F(9); F(12) = F(11); F(14) = F(13); }
+    if (is(4)) { F(3) = F(4); F(7) = F(9); F(8) = F(10); F(15) = F(16); F(17) = F(18); }
+    if (is(3)) { F(4) = F(3); F(9) = F(7); F(10) = F(8); F(16) = F(15); F(18) = F(17); }
+    if (is(6)) { F(5) = F(6); F(11) = F(13); F(12) = F(14); F(15) = F(17); F(16) = F(18); }
+    if (is(5)) { F(6) = F(5); F(13) = F(11); F(14) = F(12); F(17) = F(15); F(18) = F(16); }
+}
+
+/* ------------------------------ macro ----------------------------------- */
+
+template <class T>
+void macro_all(Lattice<T> &L) {
+    const size_t N = (size_t)L.N;
+    const T *f = L.f.data();
+    const bool phys = L.p.mode == 1;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < L.N; ++i) {
+        if (L.fluid[i] != 1) continue;
+        auto F = [&](int d) { return f[i + (size_t)d * N]; };
+        if (L.dims == 2) {
+            T r = F(0) + F(1) + F(2) + F(3) + F(4) + F(5) + F(6) + F(7) + F(8);
+            T u = F(1) - F(3) + F(5) - F(6) - F(7) + F(8);
+            T v = F(2) - F(4) + F(5) + F(6) - F(7) - F(8);
+            L.rho[i] = r;
+            L.u[i] = u / r;
+            bool eout = (L.mask[i] & bc2_mask(3, 1)) == bc2_mask(3, 1);
+            L.v[i] = (!phys && eout) ? (T)0.0 : v / r;
+        } else {
+            uint64_t mk = L.mask[i];
+            bool inl = (mk & BC3_OUTL_B) == BC3_INLT_B;
+            if (inl && !L.p.update_inlet_outlet) continue;
+            T r = F(0) + F(1) + F(2) + F(3) + F(4) + F(5) + F(6) + F(7) + F(8) + F(9) + F(10) +
+                  F(11) + F(12) + F(13) + F(14) + F(15) + F(16) + F(17) + F(18);
+            T ru = F(1) - F(2) + F(7) - F(8) + F(9) - F(10) + F(11) - F(12) + F(13) - F(14);
+            T rv = F(3) - F(4) + F(7) + F(8) - F(9) - F(10) + F(15) - F(16) + F(17) - F(18);
+            T rw = F(5) - F(6) + F(11) + F(12) - F(13) - F(14) + F(15) + F(16) - F(17) - F(18);
+            L.rho[i] = r;
+            L.u[i] = ru / r + (T)L.p.g / (L.omega);
+            L.v[i] = rv / r;
+            L.w3[i] = rw / r;
+        }
+    }
+}
+
+template <class T>
+double l2_residual(const Lattice<T> &L) {
+    double s = 0.0;
+    for (size_t k = 0; k < L.f.size(); ++k) {
+        double d = (double)L.f[k] - (double)L.fc[k];
+        s += d * d;
+    }
+    return sqrt(s);
+}
+
+/* ------------------------------ driver ---------------------------------- */
+
+template <class T>
+int run(int dims, int n, int m, int h, const int *node_type, int nconn, const int *bi,
+        const int *bj, const int *bk, const int *bdir, const int *btype, const int *bid,
+        const orc_params *p, const double *u_init, const double *v_init, const double *w_init,
+        const double *rho_init, int steps, int extra_collide, double *out_f, double *out_fc,
+        double *out_rho, double *out_u, double *out_v, double *out_w, uint64_t *out_mask,
+        uint8_t *out_stream, int *out_count, double *out_resid) {
+    if (n < 1 || m < 1 || h < 1 || (dims != 2 && dims != 3)) return ORC_BAD_INPUT;
+    if (p->collision_model < 1 || p->collision_model > 3) return ORC_BAD_INPUT;
+    if (p->boundary_type == 1 || p->bc_wall_model == 2) return ORC_UNSUPPORTED;
+    if (dims == 3 && p->mode == 0 && p->collision_model == 2) return ORC_UNSUPPORTED;
+    if (dims == 3 && p->inlet_profile == 1) return ORC_UNSUPPORTED;
+    if (dims == 2 && p->inlet_profile == 1) return ORC_UNSUPPORTED;
+    if (dims == 3 && p->outlet_profile != 5 && p->mode == 1) {
+        /* physics mode supports only pressure outlets in 3D */
+    }
+    Lattice<T> L;
+    L.dims = dims;
+    L.q = dims == 2 ? 9 : 19;
+    L.n = n;
+    L.m = m;
+    L.h = dims == 2 ? 1 : h;
+    L.N = n * m * L.h;
+    L.p = *p;
+    const int N = L.N;
+    build_tables(L);
+    L.fluid.assign(node_type, node_type + N);
+    int rc = build_masks(L, nconn, bi, bj, bk, bdir, btype, bid);
+    if (rc) return rc;
+    if (dims == 3 && p->mode == 0) {
+        for (int i : L.bcnodes)
+            if ((L.mask[i] & BC3_B_ALL) == BC3_OUTL_B) return ORC_UNSUPPORTED;
+    }
+    L.rho.assign(N, (T)p->rho);
+    L.u0.assign(N, (T)p->u);
+    L.v0.assign(N, (T)p->v);
+    L.w0.assign(N, (T)p->w);
+    L.u = L.u0;
+    L.v = L.v0;
+    L.w3 = L.w0;
+    if (u_init) for (int i = 0; i < N; ++i) L.u[i] = (T)u_init[i];
+    if (v_init) for (int i = 0; i < N; ++i) L.v[i] = (T)v_init[i];
+    if (w_init) for (int i = 0; i < N; ++i) L.w3[i] = (T)w_init[i];
+    if (rho_init) for (int i = 0; i < N; ++i) L.rho[i] = (T)rho_init[i];
+    L.f.assign((size_t)L.q * N, (T)0);
+    L.fc.assign((size_t)L.q * N, (T)0);
+    if (p->init_kind == 1) {
+        for (int i = 0; i < N; ++i) {
+            if (L.fluid[i] != 1) continue;
+            for (int d = 0; d < L.q; ++d)
+                L.f[i + (size_t)d * N] = dims == 2
+                    ? feqc2<T>(L.u[i], (T)cx2[d], L.v[i], (T)cy2[d], L.rho[i], L.w[d])
+                    : feqc3<T>(L.u[i], (T)cx3[d], L.v[i], (T)cy3[d], L.w3[i], (T)cz3[d], L.rho[i], L.w[d]);
+        }
+    }
+    for (int it = 0; it < steps; ++it) {
+        collide_all(L);
+        stream_all(L);
+        if (dims == 2) {
+            for (int i : L.bcnodes) bc_node_2d(L, i, L.mask[i]);
+        } else {
+            for (int i : L.bcnodes) bc_node_3d(L, i, L.mask[i]);
+            if (p->mode == 0) {
+                for (int i : L.bcnodes) periodic_node_3d(L, i, L.mask[i]);
+                for (int i : L.bcnodes) symm_node_3d(L, i, L.mask[i]);
+            }
+        }
+        macro_all(L);
+        if (out_resid) out_resid[it] = l2_residual(L);
+    }
+    if (out_f) for (size_t k = 0; k < L.f.size(); ++k) out_f[k] = (double)L.f[k];
+    if (extra_collide) collide_all(L);
+    if (out_fc) for (size_t k = 0; k < L.fc.size(); ++k) out_fc[k] = (double)L.fc[k];
+    for (int i = 0; i < N; ++i) {
+        if (out_rho) out_rho[i] = (double)L.rho[i];
+        if (out_u) out_u[i] = (double)L.u[i];
+        if (out_v) out_v[i] = (double)L.v[i];
+        if (out_w) out_w[i] = dims == 3 ? (double)L.w3[i] : 0.0;
+    }
+    if (out_mask) for (int i = 0; i < N; ++i) out_mask[i] = L.mask[i];
+    if (out_stream) for (size_t k = 0; k < L.stream.size(); ++k) out_stream[k] = L.stream[k];
+    if (out_count) *out_count = (int)L.bcnodes.size();
+    return ORC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_version(void) { return 1; }
+
+int orc_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void orc_set_threads(int t) {
+#ifdef _OPENMP
+    if (t > 0) omp_set_num_threads(t);
+#else
+    (void)t;
+#endif
+}
+
+/* One run of the time-step loop.  dims 2 or 3; node arrays x-fastest;
+ * bc_k may be NULL in 2D.  fp64 selects the storage/arithmetic type.
+ * extra_collide: apply one more collision after the last step so out_fc holds
+ * the post-collision populations the next step would stream.  Returns 0, or
+ * ORC_UNSUPPORTED / ORC_BAD_INPUT. */
+int orc_run(int fp64, int dims, int n, int m, int h, const int *node_type, int nconn,
+            const int *bc_i, const int *bc_j, const int *bc_k, const int *bc_dir,
+            const int *bc_type, const int *bc_id, const orc_params *p, const double *u_init,
+            const double *v_init, const double *w_init, const double *rho_init, int steps,
+            int extra_collide, double *out_f, double *out_fc, double *out_rho, double *out_u,
+            double *out_v, double *out_w, uint64_t *out_mask, uint8_t *out_stream,
+            int *out_count, double *out_resid) {
+    static const int zero = 0;
+    std::vector<int> kz;
+    if (!bc_k) {
+        kz.assign(nconn > 0 ? nconn : 1, zero);
+        bc_k = kz.data();
+    }
+    if (fp64)
+        return run<double>(dims, n, m, h, node_type, nconn, bc_i, bc_j, bc_k, bc_dir, bc_type,
+                           bc_id, p, u_init, v_init, w_init, rho_init, steps, extra_collide,
+                           out_f, out_fc, out_rho, out_u, out_v, out_w, out_mask, out_stream,
+                           out_count, out_resid);
+    return run<float>(dims, n, m, h, node_type, nconn, bc_i, bc_j, bc_k, bc_dir, bc_type, bc_id,
+                      p, u_init, v_init, w_init, rho_init, steps, extra_collide, out_f, out_fc,
+                      out_rho, out_u, out_v, out_w, out_mask, out_stream, out_count, out_resid);
+}
+
+}  // extern "C"
