@@ -1,0 +1,342 @@
+#!/usr/bin/env python3
+"""Benchmark: D3Q19 MRT pressure-driven duct packed with spheres.
+
+Workload: 256x256x512 lattice, spheres with radii uniform in [6, 14] inserted
+until porosity 0.70 (seed 0), Zou-He pressure faces rho_in = 1.005 at z = 0
+and rho_out = 1.0 at z = 511, bounce-back on spheres and side walls,
+tau = 0.8, D3Q19 MRT, populations stored as FP16 deviations from the rest
+weights (FP32 arithmetic).  A step is one fused stream-collide launch over
+the whole lattice; the metric is fluid-node updates per second (GLUPS).
+
+Arms:
+  --impl ours (default): value = GLUPS with the state resident in HBM, timed
+    with CUDA events on the launch stream; e2e = a full run through the C ABI
+    from host buffers (lattice upload, init, steps, macroscopic read-back).
+  --impl reference: the reference's CPU path for this time step -- the oracle
+    restatement of its kernels (oracle/lbm_oracle.cpp; the reference has no
+    CPU implementation of the single-phase 3D loop) on all host cores, on a
+    bounded sample of the same workload.
+Multi-GPU (torchrun, --gpus N): independent replicas (one duct per rank, seed
+= rank), no collective on the data path; value = all ranks' updates / max
+time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(n=256, m=256, h=512, porosity=0.70, rmin=6.0, rmax=14.0, tau=0.8,
+                rho_in=1.005, rho_out=1.0)
+METRIC = "GLUPS (fluid-node updates/s / 1e9), D3Q19 MRT sphere-packed duct"
+STORAGE_NAMES = {"f16s": 1, "f32": 0, "f64": 2}
+B_LU = {0: 152, 1: 76, 2: 304}   # algorithmic population bytes per fluid-node update
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--storage", default="f16s", choices=list(STORAGE_NAMES))
+    ap.add_argument("--size", default=None, help="n,m,h (default 256,256,512)")
+    ap.add_argument("--e2e-steps", type=int, default=5000, help="steps of the end-to-end run")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", default="64,64,128", help="n,m,h of the CPU-baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=10)
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload_config(args, n, m, h):
+    return {"workload": "D3Q19 MRT pressure-driven duct, sphere packing porosity %.2f, radii [%g,%g], "
+                        "%dx%dx%d, tau %.1f, rho_in %.3f / rho_out %.3f"
+                        % (WORKLOAD["porosity"], WORKLOAD["rmin"], WORKLOAD["rmax"], n, m, h,
+                           WORKLOAD["tau"], WORKLOAD["rho_in"], WORKLOAD["rho_out"]),
+            "lattice": [n, m, h], "collision": "MRT", "storage": args.storage,
+            "boundaries": "Zou-He pressure z faces, half-way bounce-back",
+            "l2_policy": "inputs larger than L2 (population buffers 2 x %.2f GB vs 129 MB L2)"
+                         % (19 * n * m * h * (2 if args.storage == "f16s" else 4) / 1e9)}
+
+
+def make_lattice(n, m, h, seed):
+    from thesis_gb300 import lattice
+    return lattice.sphere_duct(n, m, h, WORKLOAD["porosity"], WORKLOAD["rmin"], WORKLOAD["rmax"], seed)
+
+
+def solver_args(storage):
+    from thesis_gb300 import native as N
+    from thesis_gb300.solver import Arguments
+    return Arguments(viscosity=(WORKLOAD["tau"] - 0.5) / 3.0, collision_model=N.MRT,
+                     mode=N.MODE_PHYSICS, storage=storage, init_equilibrium=1,
+                     inlet_profile=N.INLET_PRESSURE, outlet_profile=N.OUTLET_PRESSURE,
+                     rho_in=WORKLOAD["rho_in"], rho_out=WORKLOAD["rho_out"])
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(storage, n, m, h):
+    """DRAM bytes per launch from the committed ncu summary, scaled to this
+    lattice by node count (None when no summary covers this storage)."""
+    path = os.path.join(ROOT, "profiles", "step_kernel_d3q19_mrt_%s_sphere_duct.txt" % storage)
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    vals = {}
+    for line in text.splitlines():
+        if ":" in line:
+            k, v = line.split(":", 1)
+            vals[k.strip()] = v.strip()
+    try:
+        per_node = float(vals["dram_bytes_per_node"])
+    except (KeyError, ValueError):
+        return None
+    return per_node * n * m * h
+
+
+def cpu_baseline_run(sample, steps, threads=None):
+    """Oracle restatement of the reference kernels (physics mode, FP32) on a
+    bounded sample of the workload; returns (GLUPS, threads, description)."""
+    from oracle import pyoracle
+    L = pyoracle.oracle_lib()
+    if threads:
+        L.orc_set_threads(int(threads))
+    nthreads = L.orc_threads()
+    n, m, h = sample
+    lat = make_lattice(n, m, h, 0)
+    kw = dict(viscosity=(WORKLOAD["tau"] - 0.5) / 3.0, collision_model=3, inlet_profile=4, outlet_profile=5)
+    nn = lat.num_nodes
+    init = (np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
+    pyoracle.run_oracle(lat, 1, mode=1, init_kind=1, rho_in=WORKLOAD["rho_in"],
+                        rho_out=WORKLOAD["rho_out"], init=init, **kw)  # warm the page cache / pools
+    t0 = time.perf_counter()
+    r = pyoracle.run_oracle(lat, steps, mode=1, init_kind=1, rho_in=WORKLOAD["rho_in"],
+                            rho_out=WORKLOAD["rho_out"], init=init, **kw)
+    t1 = time.perf_counter()
+    assert r.rc == 0
+    glups = lat.num_fluid * steps / (t1 - t0) / 1e9
+    desc = ("oracle restatement of the reference kernels (physics mode, FP32, OpenMP) on a %dx%dx%d "
+            "duct of the same packing, %d steps, %.1f s" % (n, m, h, steps, t1 - t0))
+    return glups, nthreads, desc
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return 0
+    sample = tuple(int(x) for x in args.cpu_sample.split(","))
+    n, m, h = (int(x) for x in args.size.split(",")) if args.size else (WORKLOAD["n"], WORKLOAD["m"], WORKLOAD["h"])
+    per = []
+    for _ in range(max(args.warmup and 1, 0)):
+        cpu_baseline_run(sample, 2)
+    for _ in range(max(args.steps // 100, 1)):
+        g, threads, desc = cpu_baseline_run(sample, args.cpu_steps)
+        per.append(g)
+    value = statistics.median(per)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GLUPS",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config(args, n, m, h),
+            "cpu_baseline": {"value": value, "unit": "GLUPS", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        return run_reference_arm(args, rank, world)
+
+    import torch
+    import torch.distributed as dist
+    from thesis_gb300 import build as native_build
+    from thesis_gb300 import native as N
+    from thesis_gb300.solver import Solver
+
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    native_build.build()
+    storage = STORAGE_NAMES[args.storage]
+    n, m, h = (int(x) for x in args.size.split(",")) if args.size else (WORKLOAD["n"], WORKLOAD["m"], WORKLOAD["h"])
+    lat = make_lattice(n, m, h, rank)
+    sargs = solver_args(storage)
+    nn = lat.num_nodes
+    rho0 = np.ones(nn, np.float32)
+    zero = np.zeros(nn, np.float32)
+
+    # ---- value: state resident in HBM, CUDA events on the launch stream ----
+    s = Solver(lat, sargs)
+    s.init(rho0, zero, zero, zero)
+    fluid = s.fluid_nodes
+    stream = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(stream):
+        s.step(args.warmup, write_macro=False, stream=stream.cuda_stream)
+    stream.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.step(args.steps, write_macro=False, stream=stream.cuda_stream)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    ms_max = float(t.item())
+    total_updates = fluid * args.steps * world
+    value = total_updates / (ms_max / 1e3) / 1e9
+    # sanity: the run is finite and the residual norms are computable
+    s.step(1, write_macro=True)
+    norms, rc = s.norms()
+    status = "ok" if rc == N.LBM_OK else "diverged"
+    s.close()
+
+    per_launch_s = ms / 1e3 / args.steps
+    alg_bytes = B_LU[storage] * fluid
+    peak, peak_kind = measured_peak()
+    achieved = alg_bytes / per_launch_s / 1e9
+    traffic = profiled_traffic(args.storage, n, m, h)
+
+    # ---- e2e: whole run through the C ABI from host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        host = [torch.from_numpy(a).pin_memory().numpy() for a in (rho0, zero, zero, zero)]
+        outs = [torch.empty(nn, dtype=torch.float32).pin_memory().numpy() for _ in range(4)]
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        t0 = time.perf_counter()
+        s2 = Solver(lat, sargs)
+        s2.init(*host)
+        s2.step(args.e2e_steps, write_macro=True)
+        rho, u, v, w = s2.macro()
+        for dst, src in zip(outs, (rho, u, v, w)):
+            dst[:] = src
+        t1 = time.perf_counter()
+        s2.close()
+        tt = torch.tensor([t1 - t0], dtype=torch.float64, device=dev)
+        if world > 1:
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        h2d = nn * 4 * (1 + 4) + lat.bc.shape[0] * 4 * 6  # node flags + initial macro + BC links
+        d2h = nn * 4 * 4
+        e2e = {"value": fluid * args.e2e_steps * world / float(tt.item()) / 1e9, "unit": "GLUPS",
+               "h2d_bytes_per_step": int(h2d / args.e2e_steps), "d2h_bytes_per_step": int(d2h / args.e2e_steps),
+               "steps": args.e2e_steps, "seconds": float(tt.item()),
+               "includes": "lbm_create (host flag build + upload), lbm_init, steps, macro read-back"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        sample = tuple(int(x) for x in args.cpu_sample.split(","))
+        g, threads, desc = cpu_baseline_run(sample, args.cpu_steps)
+        cpu = {"value": g, "unit": "GLUPS", "cores": threads, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "GLUPS", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic (seeded sphere packing)",
+                "config": workload_config(args, n, m, h),
+                "fluid_nodes_per_gpu": fluid, "status": status,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "peak_kind": peak_kind,
+                             "traffic": traffic,
+                             "algorithmic_bytes_per_launch": alg_bytes,
+                             "bytes_per_fluid_update": B_LU[storage]},
+                "clocks": clk, "gpu_launches": args.steps,
+                "e2e": e2e, "cpu_baseline": cpu}
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,177 @@
+/*
+ * thesis_lbm.h -- C ABI of the GB300 lattice-Boltzmann time-step engine.
+ *
+ * Drop-in for the time-step loop of the reference solver
+ * (ZPaulo/Thesis, "Source code/lbm-solver_final"):
+ *
+ *   int Iterate2D(InputFilenames*, Arguments*)   include/Iterate.h:64
+ *   int Iterate3D(InputFilenames*, Arguments*)   include/Iterate.h:65
+ *
+ * The reference runs collision, streaming, boundary and macroscopic kernels
+ * per step (Iterate3D.cu:493-653) on state it allocates itself.  This library
+ * keeps the same inputs -- the columns of the Node and BC lattice files and the
+ * Arguments fields the loop reads -- and runs one fused CUDA kernel per step.
+ *
+ * Conventions: plain pointers and sizes only; host buffers are owned by the
+ * caller, device buffers by the handle; every call returns a status code
+ * (never exits the process); one handle per host thread.
+ */
+#ifndef THESIS_LBM_H
+#define THESIS_LBM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  1 and 2 keep the meaning of Iterate2D/3D's return values
+ * (Iterate.cu:563, Iterate3D.cu:89-105). */
+#define LBM_OK 0
+#define LBM_DIVERGED 1
+#define LBM_ERR_FILE 2
+#define LBM_ERR_UNSUPPORTED 3
+#define LBM_ERR_INVALID 4
+#define LBM_ERR_CUDA 5
+#define LBM_ERR_NOMEM 6
+
+/* Population storage in HBM.  Arithmetic is FP32 for F32 and F16S, FP64 for
+ * F64.  F16S stores (f_i - w_i) * scale as IEEE half. */
+#define LBM_STORE_F32 0
+#define LBM_STORE_F16S 1
+#define LBM_STORE_F64 2
+
+/* Semantics.  REFERENCE reproduces the reference loop including its quirks
+ * (zero initial populations, post-stream wall copies, the lid Zou-He with
+ * rho*u/6, D3Q19 MRT without direction 18, ...).  PHYSICS uses the standard
+ * forms: half-way bounce-back, mass-balanced Zou-He velocity and pressure
+ * faces, all 19 MRT outputs, TRT in 3D. */
+#define LBM_MODE_REFERENCE 0
+#define LBM_MODE_PHYSICS 1
+
+/* Values of the reference's enums (include/Arguments.h:14-56). */
+#define LBM_BGKW 1
+#define LBM_TRT 2
+#define LBM_MRT 3
+#define LBM_INLET 1            /* InletProfile INLET (parabolic, 2D)        */
+#define LBM_NO_INLET 2         /* InletProfile NO_INLET (constant u, v, w)  */
+#define LBM_INLET_PRESSURE 4   /* extension: Zou-He pressure inlet, rho_in  */
+#define LBM_OUTLET_ZOUHE 1     /* OutletProfile OUTLET                      */
+#define LBM_OUTLET_SECOND 2
+#define LBM_OUTLET_FIRST 3
+#define LBM_OUTLET_HEMODEL 4
+#define LBM_OUTLET_PRESSURE 5  /* extension: Zou-He pressure outlet, rho_out */
+#define LBM_CURVED 1
+#define LBM_STRAIGHT 2
+#define LBM_WALL_SIMPLE 1
+#define LBM_WALL_COMPLEX 2
+
+/* BC file link types (latticegen: WALL/INLE/OUTL/CYCL/SYMP -> 1..5). */
+#define LBM_BC_WALL 1
+#define LBM_BC_INLET 2
+#define LBM_BC_OUTLET 3
+#define LBM_BC_PERIODIC 4
+#define LBM_BC_SYMMETRY 5
+
+typedef struct lbm_handle_s *lbm_handle;
+
+/* A lattice as the reference reads it: the Node file columns (i, j, [k,]
+ * fluid) laid out x fastest, and the BC file columns (i, j, [k,] dir, type,
+ * id) -- FilesReading.cu:270-347. */
+typedef struct lbm_lattice_desc {
+    int dims;                 /* 2 or 3 */
+    int n, m, h;              /* nodes along x, y, z (h = 1 in 2D) */
+    const int *node_type;     /* n*m*h entries: 1 fluid, 0 solid */
+    int num_conns;            /* number of BC links */
+    const int *bc_i, *bc_j;   /* node of each link */
+    const int *bc_k;          /* NULL in 2D */
+    const int *bc_dir;        /* lattice direction from the node into the boundary */
+    const int *bc_type;       /* LBM_BC_* */
+    const int *bc_id;         /* boundary id (2D drag/lift), may be NULL */
+} lbm_lattice_desc;
+
+/* The Arguments fields the time-step loop reads (include/Arguments.h:86-135),
+ * plus this engine's options. */
+typedef struct lbm_params {
+    double u, v, w;           /* inlet / initial velocity */
+    double rho;               /* initial density */
+    double viscosity;         /* omega = 1 / (3 nu + 0.5) */
+    double g;                 /* 3D body force, applied as u += g / omega */
+    int inlet_profile;        /* LBM_NO_INLET, LBM_INLET_PRESSURE */
+    int outlet_profile;       /* LBM_OUTLET_* */
+    int collision_model;      /* LBM_BGKW, LBM_TRT, LBM_MRT */
+    int boundary_type;        /* LBM_STRAIGHT (LBM_CURVED unsupported) */
+    int bc_wall_model;        /* LBM_WALL_SIMPLE (COMPLEX unsupported) */
+    int update_inlet_outlet;  /* UpdateInltOutl */
+    int mode;                 /* LBM_MODE_REFERENCE or LBM_MODE_PHYSICS */
+    int storage;              /* LBM_STORE_* */
+    double rho_in, rho_out;   /* pressure faces */
+    double f16_scale;         /* F16S scale; 0 selects 1024 */
+    int periodic[3];          /* physics mode: periodic x, y, z */
+    int init_equilibrium;     /* 0: f starts at 0 (reference); 1: f_eq(rho, u) */
+} lbm_params;
+
+/* Build a solver from a lattice description.  Computes the reference's BC
+ * masks and streaming flags (GpuInit.cu:1055-1277), derives the per-node flag
+ * words, allocates device state and uploads it. */
+int lbm_create(const lbm_lattice_desc *lattice, const lbm_params *params, lbm_handle *out);
+
+/* Per-node inlet/outlet velocity field (the reference's u0/u1 arrays); any
+ * NULL component keeps the constant from params.  Host arrays of n*m*h. */
+int lbm_set_inlet_velocity(lbm_handle h, const float *u, const float *v, const float *w);
+
+/* Initial macroscopic state (NULL = constant from params) and the first
+ * collision, which produces the state lbm_step advances. */
+int lbm_init(lbm_handle h, const float *rho, const float *u, const float *v, const float *w);
+
+/* Advance nsteps time steps on `stream` (a cudaStream_t; NULL = the
+ * handle's own stream).  write_macro_last: store rho, u on the last step. */
+int lbm_step(lbm_handle h, int nsteps, int write_macro_last, void *stream);
+
+/* Wait for queued steps, then copy the macroscopic fields written by the
+ * last step that stored them into host arrays of n*m*h (any may be NULL). */
+int lbm_get_macro(lbm_handle h, float *rho, float *u, float *v, float *w);
+
+/* Copy the post-collision populations into a host array of Q*n*m*h doubles,
+ * SoA f[d*n*m*h + node] in the reference's direction order. */
+int lbm_get_populations(lbm_handle h, double *f);
+
+/* FP64 norms over fluid nodes of the last stored macroscopic fields:
+ * out[0] = sum |u - u_prev|^2, out[1] = sum |u|^2, out[2] = sum rho,
+ * out[3] = number of fluid nodes, out[4] = sum rho*ux.  u_prev is the field
+ * at the previous call (zero before the first).  Deterministic.  Returns
+ * LBM_DIVERGED when a sum is not finite. */
+#define LBM_NORMS 5
+int lbm_macro_norms(lbm_handle h, double *out);
+
+/* Sticky status of the handle (LBM_OK, LBM_DIVERGED, LBM_ERR_CUDA). */
+int lbm_status(lbm_handle h);
+
+/* Number of fluid nodes (the lattice updates one step performs). */
+long long lbm_fluid_nodes(lbm_handle h);
+
+/* Bytes of HBM one step moves per fluid node for the populations alone. */
+int lbm_bytes_per_update(lbm_handle h);
+
+/* Message of the last failing call on this thread. */
+const char *lbm_last_error(void);
+
+void lbm_destroy(lbm_handle h);
+
+/* Host only, needs no GPU: the reference's BC masks (one uint64 per node; 2D
+ * masks in the low 32 bits), this engine's flag words (one uint32 per node:
+ * bit 0 fluid, bit d blocked pull of direction d, bit 19 boundary slot) and
+ * slot indices (int32 per node, -1 for none), and the number of nodes with BC
+ * links.  Any output pointer may be NULL. */
+int lbm_build_flags(const lbm_lattice_desc *lattice, const lbm_params *params, uint64_t *mask,
+                    uint32_t *word, int32_t *slot, int *num_bc_nodes);
+
+/* Library version, for load checks. */
+int lbm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* THESIS_LBM_H */

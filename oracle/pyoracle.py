@@ -1,0 +1,163 @@
+"""ctypes binding of the oracle restatement (oracle/lbm_oracle.cpp) and of the
+reference kernels run on the host (oracle/_ref/libreflbm_*.so, built here from
+the reference tree by oracle/build_ref.sh; absent on machines without it).
+
+TEST INFRASTRUCTURE ONLY.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+ORACLE_SO = os.path.join(BUILD, "liboracle_lbm.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+ORC_OK, ORC_UNSUPPORTED, ORC_BAD_INPUT = 0, 3, 4
+
+_RP = ["u", "v", "w", "rho", "viscosity", "g"]
+_RI = ["inlet_profile", "outlet_profile", "collision_model", "boundary_type", "bc_wall_model",
+       "update_inlet_outlet", "boundary_id"]
+_RD = ["delta", "min_inlet_y", "max_inlet_y", "min_inlet_z", "max_inlet_z"]
+
+
+class RefParams(C.Structure):
+    _fields_ = [(k, C.c_double) for k in _RP] + [(k, C.c_int) for k in _RI] + [(k, C.c_double) for k in _RD]
+
+
+class OrcParams(C.Structure):
+    _fields_ = RefParams._fields_ + [("mode", C.c_int), ("init_kind", C.c_int),
+                                     ("rho_in", C.c_double), ("rho_out", C.c_double)]
+
+
+def build_oracle(force=False):
+    """Compile the oracle with g++ (OpenMP, no FMA contraction)."""
+    src = os.path.join(HERE, "lbm_oracle.cpp")
+    if not force and os.path.exists(ORACLE_SO) and os.path.getmtime(ORACLE_SO) >= os.path.getmtime(src):
+        return ORACLE_SO
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = ORACLE_SO + ".tmp"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp",
+                    src, "-o", tmp], check=True)
+    os.replace(tmp, ORACLE_SO)
+    return ORACLE_SO
+
+
+_orc = None
+
+
+def oracle_lib():
+    global _orc
+    if _orc is None:
+        _orc = C.CDLL(build_oracle())
+    return _orc
+
+
+def ref_lib(fp64=False):
+    path = os.path.join(REF_DIR, "libreflbm_f64.so" if fp64 else "libreflbm_f32.so")
+    if not os.path.exists(path):
+        return None
+    return C.CDLL(path)
+
+
+def _vp(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _params(cls, kw):
+    p = cls()
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def default_params(**kw):
+    base = dict(u=0.0, v=0.0, w=0.0, rho=1.0, viscosity=0.1, g=0.0, inlet_profile=2,
+                outlet_profile=2, collision_model=1, boundary_type=2, bc_wall_model=1,
+                update_inlet_outlet=1, boundary_id=0, delta=1.0, min_inlet_y=0.0,
+                max_inlet_y=0.0, min_inlet_z=0.0, max_inlet_z=0.0)
+    base.update(kw)
+    return base
+
+
+def _cols(lat):
+    return [np.ascontiguousarray(lat.bc[:, k], dtype=np.int32) for k in range(6)]
+
+
+class Result:
+    pass
+
+
+def run_oracle(lat, steps, fp64=False, mode=0, init_kind=0, rho_in=1.0, rho_out=1.0,
+               extra_collide=False, init=None, **kw):
+    """Run the oracle restatement; returns a Result with f, fc (q, N), rho,
+    u, v, w (N), mask, stream, count, resid, rc."""
+    L = oracle_lib()
+    q = lat.q
+    nn = lat.num_nodes
+    p = _params(OrcParams, dict(default_params(**kw), mode=mode, init_kind=init_kind,
+                                rho_in=rho_in, rho_out=rho_out))
+    cols = _cols(lat)
+    r = Result()
+    r.f, r.fc = np.zeros(q * nn), np.zeros(q * nn)
+    r.rho, r.u, r.v, r.w = (np.zeros(nn) for _ in range(4))
+    r.mask = np.zeros(nn, np.uint64)
+    r.stream = np.zeros((q - 1) * nn, np.uint8)
+    r.resid = np.zeros(max(steps, 1))
+    cnt = C.c_int(0)
+    ini = [None] * 4
+    if init is not None:
+        ini = [None if a is None else np.ascontiguousarray(a, np.float64) for a in init]
+    r.rc = L.orc_run(int(fp64), lat.dims, lat.n, lat.m, lat.h, _vp(lat.node_type), int(lat.bc.shape[0]),
+                     _vp(cols[0]), _vp(cols[1]), _vp(cols[2]) if lat.dims == 3 else None,
+                     _vp(cols[3]), _vp(cols[4]), _vp(cols[5]), C.byref(p),
+                     _vp(ini[1]), _vp(ini[2]), _vp(ini[3]), _vp(ini[0]), int(steps), int(extra_collide),
+                     _vp(r.f), _vp(r.fc), _vp(r.rho), _vp(r.u), _vp(r.v), _vp(r.w), _vp(r.mask),
+                     _vp(r.stream), C.byref(cnt), _vp(r.resid))
+    r.count = cnt.value
+    r.f, r.fc = r.f.reshape(q, nn), r.fc.reshape(q, nn)
+    return r
+
+
+def run_reference(lat, steps, fp64=False, **kw):
+    """Run the reference's own kernels on the host (oracle/_ref).  Returns
+    None when oracle/_ref has not been built on this machine."""
+    L = ref_lib(fp64)
+    if L is None:
+        return None
+    q = lat.q
+    nn = lat.num_nodes
+    p = _params(RefParams, default_params(**kw))
+    cols = _cols(lat)
+    x, y, z = lat.coords(kw.get("delta", 1.0))
+    x, y, z = (np.ascontiguousarray(a, np.float64) for a in (x, y, z))
+    bx = np.ascontiguousarray(x[cols[0] + lat.n * (cols[1] + lat.m * cols[2])] if len(cols[0]) else np.zeros(0))
+    by = np.ascontiguousarray(y[cols[0] + lat.n * (cols[1] + lat.m * cols[2])] if len(cols[0]) else np.zeros(0))
+    bz = np.ascontiguousarray(z[cols[0] + lat.n * (cols[1] + lat.m * cols[2])] if len(cols[0]) else np.zeros(0))
+    r = Result()
+    r.f, r.fc = np.zeros(q * nn), np.zeros(q * nn)
+    r.rho, r.u, r.v, r.w = (np.zeros(nn) for _ in range(4))
+    r.resid = np.zeros(max(steps, 1))
+    cnt = C.c_int(0)
+    if lat.dims == 2:
+        r.mask32 = np.zeros(nn, np.int32)
+        r.stream32 = np.zeros(8 * nn, np.int32)
+        r.rc = L.ref_run2d(lat.n, lat.m, _vp(lat.node_type), _vp(x), _vp(y), int(lat.bc.shape[0]),
+                           _vp(cols[0]), _vp(cols[1]), _vp(cols[3]), _vp(cols[4]), _vp(cols[5]),
+                           _vp(bx), _vp(by), C.byref(p), int(steps), _vp(r.f), _vp(r.fc), _vp(r.rho),
+                           _vp(r.u), _vp(r.v), _vp(r.mask32), _vp(r.stream32), C.byref(cnt), _vp(r.resid))
+        r.mask = r.mask32.astype(np.uint32).astype(np.uint64)
+        r.stream = r.stream32.astype(np.uint8)
+    else:
+        r.mask = np.zeros(nn, np.uint64)
+        r.stream = np.zeros(18 * nn, np.uint8)
+        r.rc = L.ref_run3d(lat.n, lat.m, lat.h, _vp(lat.node_type), _vp(x), _vp(y), _vp(z),
+                           int(lat.bc.shape[0]), *[_vp(c) for c in cols[:5]], _vp(cols[5]),
+                           _vp(bx), _vp(by), _vp(bz), C.byref(p), int(steps), _vp(r.f), _vp(r.fc),
+                           _vp(r.rho), _vp(r.u), _vp(r.v), _vp(r.w), _vp(r.mask), _vp(r.stream),
+                           C.byref(cnt), _vp(r.resid))
+    r.count = cnt.value
+    r.f, r.fc = r.f.reshape(q, nn), r.fc.reshape(q, nn)
+    return r

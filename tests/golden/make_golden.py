@@ -1,0 +1,67 @@
+"""Generate tests/golden/reference_runs.npz from the reference's own kernels.
+
+Runs the reference solver's kernels compiled for the host (oracle/_ref, built
+by oracle/build_ref.sh from the reference tree) on lattices from
+thesis_gb300.lattice and stores their outputs, so machines without the
+reference tree can still pin the oracle.  Usage:
+    oracle/build_ref.sh && python tests/golden/make_golden.py
+"""
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import pyoracle  # noqa: E402
+from thesis_gb300 import lattice  # noqa: E402
+
+
+def cases():
+    """(name, lattice builder args, run kwargs, steps)."""
+    out = []
+    for coll, tag in ((1, "bgk"), (2, "trt"), (3, "mrt")):
+        out.append(("cav2d_16_" + tag, ("cavity2d", (16, 16)),
+                    dict(u=0.1, viscosity=0.128, collision_model=coll, outlet_profile=1), 25))
+    for coll, tag in ((1, "bgk"), (3, "mrt")):
+        out.append(("cav3d_10x9x8_" + tag, ("cavity3d", (10, 9, 8)),
+                    dict(u=0.05, viscosity=0.1, collision_model=coll), 12))
+    out.append(("cav2d_40x24_bgk_long", ("cavity2d", (40, 24)),
+                dict(u=0.1, viscosity=0.05, collision_model=1, outlet_profile=1), 200))
+    return out
+
+
+def make_lattice(spec):
+    name, args = spec
+    return getattr(lattice, name)(*args)
+
+
+def bc_hash(lat):
+    return hashlib.sha256(np.ascontiguousarray(lat.bc).tobytes() + lat.node_type.tobytes()).hexdigest()
+
+
+def main():
+    if pyoracle.ref_lib() is None:
+        sys.exit("oracle/_ref not built; run oracle/build_ref.sh first")
+    store = {}
+    for name, spec, kw, steps in cases():
+        lat = make_lattice(spec)
+        r = pyoracle.run_reference(lat, steps, fp64=False, **kw)
+        assert r.rc == 0, name
+        store[name + "/f"] = r.f.astype(np.float32)
+        store[name + "/fc"] = r.fc.astype(np.float32)
+        for k in ("rho", "u", "v", "w"):
+            store[name + "/" + k] = getattr(r, k).astype(np.float32)
+        store[name + "/mask"] = r.mask
+        store[name + "/stream"] = r.stream
+        store[name + "/resid"] = r.resid[:steps]
+        store[name + "/lattice_sha256"] = np.frombuffer(bc_hash(lat).encode(), np.uint8)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_runs.npz")
+    np.savez_compressed(path, **store)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()

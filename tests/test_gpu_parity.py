@@ -1,0 +1,202 @@
+"""CUDA time step (through the C ABI) against the CPU oracle on the same
+seeded inputs.
+
+Tolerances (stated per storage type):
+  * F64 storage vs the FP64 oracle: 1e-10 absolute on populations and
+    macroscopic fields (FP64 arithmetic in a different operation order).
+  * F32 storage vs the FP32 oracle: 2e-5 absolute on populations, density and
+    velocity (FP32 with fused multiply-adds and another summation order; the
+    oracle follows the reference's expression order without contraction).
+  * F16S storage vs the FP32 oracle: 2e-3 relative to the field's range
+    (half precision keeps ~11 bits of the deviation from the rest weights).
+The GPU state after k steps is the post-collision field the next step
+streams, i.e. the oracle's state after k steps followed by one collision.
+"""
+import numpy as np
+import pytest
+
+from thesis_gb300 import lattice
+from thesis_gb300 import native as N
+from thesis_gb300.solver import Arguments, Solver
+
+pytestmark = pytest.mark.gpu
+
+TOL = {N.STORE_F64: 1e-10, N.STORE_F32: 2e-5}
+
+
+def run_pair(oracle, lat, args, steps, init=None):
+    """Run GPU and oracle; return (gpu dict, oracle Result)."""
+    fluid = lat.node_type == 1
+    with Solver(lat, args) as s:
+        if init is not None:
+            s.init(*init)
+        else:
+            s.init()
+        s.step(steps, write_macro=True)
+        rho, u, v, w = s.macro()
+        f = s.populations()
+    okw = dict(u=args.u, v=args.v, w=args.w, rho=args.rho, viscosity=args.viscosity, g=args.g,
+               inlet_profile=args.inlet_profile, outlet_profile=args.outlet_profile,
+               collision_model=args.collision_model, update_inlet_outlet=args.update_inlet_outlet)
+    r = oracle.run_oracle(lat, steps, fp64=args.storage == N.STORE_F64, mode=args.mode,
+                          init_kind=args.init_equilibrium, rho_in=args.rho_in, rho_out=args.rho_out,
+                          extra_collide=True, init=init, **okw)
+    assert r.rc == 0
+    g = dict(rho=rho.astype(np.float64), u=u.astype(np.float64), v=v.astype(np.float64),
+             w=w.astype(np.float64), f=f)
+    return g, r, fluid
+
+
+def compare(g, r, fluid, storage, dims):
+    errs = {}
+    keys = ["rho", "u", "v"] + (["w"] if dims == 3 else [])
+    for k in keys:
+        a, b = g[k][fluid], getattr(r, k)[fluid]
+        errs[k] = float(np.abs(a - b).max())
+    errs["f"] = float(np.abs(g["f"][:, fluid] - r.fc[:, fluid]).max())
+    if storage == N.STORE_F16S:
+        scale = {k: max(1e-3, float(np.ptp(getattr(r, k)[fluid]))) for k in keys}
+        scale["f"] = max(1e-3, float(np.abs(r.fc[:, fluid]).max()))
+        bad = {k: v for k, v in errs.items() if v > 2e-3 * scale[k]}
+    else:
+        bad = {k: v for k, v in errs.items() if v > TOL[storage]}
+    assert not bad, (bad, errs)
+    return errs
+
+
+@pytest.mark.parametrize("coll", [N.BGKW, N.TRT, N.MRT])
+def test_reference_cavity2d(oracle, coll):
+    lat = lattice.cavity2d(32, 24)
+    args = Arguments(u=0.1, viscosity=0.128, collision_model=coll, outlet_profile=N.OUTLET_ZOUHE)
+    g, r, fl = run_pair(oracle, lat, args, 60)
+    compare(g, r, fl, N.STORE_F32, 2)
+
+
+@pytest.mark.parametrize("coll", [N.BGKW, N.MRT])
+def test_reference_cavity2d_fp64(oracle, coll):
+    lat = lattice.cavity2d(20)
+    args = Arguments(u=0.1, viscosity=0.128, collision_model=coll, storage=N.STORE_F64,
+                     outlet_profile=N.OUTLET_ZOUHE)
+    g, r, fl = run_pair(oracle, lat, args, 40)
+    compare(g, r, fl, N.STORE_F64, 2)
+
+
+@pytest.mark.parametrize("coll", [N.BGKW, N.MRT])
+def test_reference_cavity3d(oracle, coll):
+    lat = lattice.cavity3d(12, 10, 9)
+    args = Arguments(u=0.05, viscosity=0.1, collision_model=coll)
+    g, r, fl = run_pair(oracle, lat, args, 25)
+    compare(g, r, fl, N.STORE_F32, 3)
+
+
+def test_reference_cavity3d_gravity_no_inlet_update(oracle):
+    lat = lattice.cavity3d(9, 8, 7)
+    args = Arguments(u=0.05, viscosity=0.1, collision_model=N.BGKW, g=1e-5, update_inlet_outlet=0)
+    g, r, fl = run_pair(oracle, lat, args, 15)
+    compare(g, r, fl, N.STORE_F32, 3)
+
+
+@pytest.mark.parametrize("coll", [N.BGKW, N.TRT, N.MRT])
+@pytest.mark.parametrize("storage", [N.STORE_F32, N.STORE_F64])
+def test_physics_cavity2d(oracle, coll, storage):
+    lat = lattice.cavity2d(32)
+    args = Arguments(u=0.1, viscosity=0.128, collision_model=coll, mode=N.MODE_PHYSICS,
+                     storage=storage, init_equilibrium=1, outlet_profile=N.OUTLET_ZOUHE)
+    nn = lat.num_nodes
+    init = (np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
+    g, r, fl = run_pair(oracle, lat, args, 80, init=init)
+    compare(g, r, fl, storage, 2)
+
+
+@pytest.mark.parametrize("coll", [N.BGKW, N.TRT, N.MRT])
+@pytest.mark.parametrize("storage", [N.STORE_F32, N.STORE_F64, N.STORE_F16S])
+def test_physics_sphere_duct(oracle, coll, storage):
+    lat = lattice.sphere_duct(24, 20, 48, porosity=0.75, rmin=3, rmax=5, seed=7)
+    args = Arguments(viscosity=(0.8 - 0.5) / 3, collision_model=coll, mode=N.MODE_PHYSICS,
+                     storage=storage, init_equilibrium=1, inlet_profile=N.INLET_PRESSURE,
+                     outlet_profile=N.OUTLET_PRESSURE, rho_in=1.005, rho_out=1.0)
+    nn = lat.num_nodes
+    init = (np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
+    g, r, fl = run_pair(oracle, lat, args, 40, init=init)
+    compare(g, r, fl, storage, 3)
+
+
+def test_physics_channel2d_velocity_inlet_pressure_outlet(oracle):
+    lat = lattice.channel2d(160, 48, seed=5)
+    args = Arguments(u=0.05, viscosity=0.05, collision_model=N.TRT, mode=N.MODE_PHYSICS,
+                     init_equilibrium=1, outlet_profile=N.OUTLET_PRESSURE, rho_out=1.0)
+    nn = lat.num_nodes
+    init = (np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
+    g, r, fl = run_pair(oracle, lat, args, 60, init=init)
+    compare(g, r, fl, N.STORE_F32, 2)
+
+
+def test_macro_norms_fp64(oracle):
+    lat = lattice.sphere_duct(20, 16, 32, porosity=0.8, rmin=3, rmax=4, seed=3)
+    args = Arguments(viscosity=0.1, collision_model=N.MRT, mode=N.MODE_PHYSICS, init_equilibrium=1,
+                     inlet_profile=N.INLET_PRESSURE, outlet_profile=N.OUTLET_PRESSURE,
+                     rho_in=1.01, rho_out=1.0)
+    nn = lat.num_nodes
+    fl = lat.node_type == 1
+    with Solver(lat, args) as s:
+        s.init(np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
+        s.step(10, write_macro=True)
+        n0, rc = s.norms()
+        assert rc == N.LBM_OK
+        rho, u, v, w = [a.astype(np.float64) for a in s.macro()]
+        assert n0[3] == fl.sum()
+        np.testing.assert_allclose(n0[2], rho[fl].sum(), rtol=1e-12)
+        np.testing.assert_allclose(n0[1], (u[fl] ** 2 + v[fl] ** 2 + w[fl] ** 2).sum(), rtol=1e-12)
+        s.step(10, write_macro=True)
+        n1, _ = s.norms()
+        rho2, u2, v2, w2 = [a.astype(np.float64) for a in s.macro()]
+        du = ((u2 - u)[fl] ** 2 + (v2 - v)[fl] ** 2 + (w2 - w)[fl] ** 2).sum()
+        np.testing.assert_allclose(n1[0], du, rtol=1e-10)
+        # deterministic: same inputs, same bits
+        s.step(0, write_macro=False)
+    with Solver(lat, args) as s2:
+        s2.init(np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
+        s2.step(10, write_macro=True)
+        m0, _ = s2.norms()
+    assert np.array_equal(m0, n0)
+
+
+def test_divergence_is_reported_not_fatal(oracle):
+    """A blown-up run (host-seeded NaN in the initial density) is reported as
+    LBM_DIVERGED by the FP64 norms and the handle stays usable."""
+    lat = lattice.cavity2d(16)
+    args = Arguments(u=0.1, viscosity=0.1, collision_model=N.BGKW, mode=N.MODE_PHYSICS, init_equilibrium=1)
+    nn = lat.num_nodes
+    rho = np.ones(nn)
+    rho[nn // 2] = np.nan
+    with Solver(lat, args) as s:
+        s.init(rho, np.zeros(nn), np.zeros(nn), np.zeros(nn))
+        s.step(5, write_macro=True)
+        _, rc = s.norms()
+        assert rc == N.LBM_DIVERGED
+        assert s.status == N.LBM_DIVERGED
+        s.init(np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
+        s.step(5, write_macro=True)
+        _, rc = s.norms()
+        assert rc == N.LBM_OK
+        assert s.status == N.LBM_OK
+
+
+def test_graph_path_matches_single_launches(oracle):
+    """lbm_step replays a captured two-step graph for long runs; the result
+    must equal step-by-step launches bit for bit."""
+    lat = lattice.cavity2d(24)
+    args = Arguments(u=0.1, viscosity=0.1, collision_model=N.MRT, mode=N.MODE_PHYSICS, init_equilibrium=1)
+    nn = lat.num_nodes
+    init = (np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
+    with Solver(lat, args) as a:
+        a.init(*init)
+        a.step(41, write_macro=True)
+        fa = a.populations()
+    with Solver(lat, args) as b:
+        b.init(*init)
+        for _ in range(40):
+            b.step(1, write_macro=False)
+        b.step(1, write_macro=True)
+        fb = b.populations()
+    assert np.array_equal(fa, fb)

@@ -1,0 +1,80 @@
+"""The oracle restatement against the reference's own kernels run on the
+host (oracle/_ref, built from the reference tree by oracle/build_ref.sh).
+
+Only runs where oracle/_ref exists (the build container); the committed
+golden fixtures in tests/golden/ carry the same pin to other machines.
+"""
+import numpy as np
+import pytest
+
+from thesis_gb300 import lattice
+
+pytestmark = pytest.mark.skipif(
+    __import__("oracle.pyoracle", fromlist=["x"]).ref_lib() is None,
+    reason="oracle/_ref (reference kernels built for the host) not present")
+
+CASES_2D = [(16, 16, 1), (16, 16, 2), (16, 16, 3), (24, 12, 1)]
+
+
+@pytest.mark.parametrize("n,m,coll", CASES_2D)
+@pytest.mark.parametrize("fp64", [False, True])
+def test_cavity2d_bit_exact(oracle, n, m, coll, fp64):
+    lat = lattice.cavity2d(n, m)
+    kw = dict(u=0.1, viscosity=0.128, collision_model=coll, outlet_profile=1)
+    ref = oracle.run_reference(lat, 25, fp64=fp64, **kw)
+    orc = oracle.run_oracle(lat, 25, fp64=fp64, **kw)
+    assert ref.rc == 0 and orc.rc == 0
+    np.testing.assert_array_equal(ref.mask, orc.mask)
+    np.testing.assert_array_equal(ref.stream, orc.stream)
+    assert ref.count == orc.count
+    tol = 0.0 if not fp64 else 1e-14
+    for a, b in ((ref.f, orc.f), (ref.fc, orc.fc), (ref.rho, orc.rho), (ref.u, orc.u), (ref.v, orc.v)):
+        assert np.abs(a - b).max() <= tol
+    np.testing.assert_allclose(ref.resid[:25], orc.resid[:25], rtol=1e-12)
+
+
+@pytest.mark.parametrize("coll", [1, 3])
+@pytest.mark.parametrize("fp64", [False, True])
+def test_cavity3d_bit_exact(oracle, coll, fp64):
+    lat = lattice.cavity3d(10, 9, 8)
+    kw = dict(u=0.05, viscosity=0.1, collision_model=coll)
+    ref = oracle.run_reference(lat, 12, fp64=fp64, **kw)
+    orc = oracle.run_oracle(lat, 12, fp64=fp64, **kw)
+    assert ref.rc == 0 and orc.rc == 0
+    np.testing.assert_array_equal(ref.mask, orc.mask)
+    np.testing.assert_array_equal(ref.stream, orc.stream)
+    tol = 0.0 if not fp64 else 1e-12
+    for a, b in ((ref.f, orc.f), (ref.fc, orc.fc), (ref.rho, orc.rho), (ref.u, orc.u), (ref.w, orc.w)):
+        assert np.abs(a - b).max() <= tol * max(1.0, np.abs(a).max())
+
+
+def test_symmetry_and_gravity_3d(oracle):
+    """Symmetry planes (GpuBoundaries.cu:2086-2168) and the g/omega force."""
+    lat = lattice.cavity3d(8, 8, 10)
+    bc = lat.bc.copy()
+    # make the y- face a symmetry plane
+    sel = (bc[:, 1] == 0) & (bc[:, 4] == 1)
+    bc[sel, 4] = 5
+    lat = lattice.Lattice(3, lat.n, lat.m, lat.h, lat.node_type, bc)
+    kw = dict(u=0.05, viscosity=0.1, collision_model=1, g=1e-5)
+    ref = oracle.run_reference(lat, 8, **kw)
+    orc = oracle.run_oracle(lat, 8, **kw)
+    np.testing.assert_array_equal(ref.mask, orc.mask)
+    assert np.abs(ref.f - orc.f).max() == 0.0
+    assert np.abs(ref.u - orc.u).max() == 0.0
+
+
+def test_reference_lid_cavity_golden_mesh(oracle):
+    """The 30^3 lid cavity the reference generator ships (latticegen2_W8/
+    lidvalidation_{Node,BC}.dat): masks, stream flags and 5 MRT steps."""
+    import os
+    g = "/root/reference/Source code/latticegen2_W8/"
+    if not os.path.exists(g + "lidvalidation_Node.dat"):
+        pytest.skip("reference tree not mounted")
+    lat = lattice.from_files(g + "lidvalidation_Node.dat", g + "lidvalidation_BC.dat")
+    kw = dict(u=0.05, viscosity=0.1, collision_model=3, delta=1 / 29)
+    ref = oracle.run_reference(lat, 5, **kw)
+    orc = oracle.run_oracle(lat, 5, **kw)
+    np.testing.assert_array_equal(ref.mask, orc.mask)
+    np.testing.assert_array_equal(ref.stream, orc.stream)
+    assert np.abs(ref.f - orc.f).max() == 0.0

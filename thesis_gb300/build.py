@@ -1,0 +1,74 @@
+"""Build recipe for the native library (sm_103a CUDA kernels + C ABI).
+
+Compiles thesis_gb300/csrc/*.cu and *.cpp with nvcc for sm_103a only, in
+parallel, into thesis_gb300/_lib/libthesis_lbm.so.  Objects are rebuilt only
+when a source or header is newer than the library.
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+LIBDIR = os.path.join(HERE, "_lib")
+OBJDIR = os.path.join(LIBDIR, "obj")
+LIBNAME = "libthesis_lbm.so"
+LIB_PATH = os.path.join(LIBDIR, LIBNAME)
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc():
+    home = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    cand = os.path.join(home, "bin", "nvcc")
+    return cand if os.path.exists(cand) else "nvcc"
+
+
+def sources():
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
+
+
+def _newest_input():
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    files.append(os.path.join(ROOT, "include", "thesis_lbm.h"))
+    files.append(os.path.abspath(__file__))
+    return max(os.path.getmtime(f) for f in files)
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s" % (" ".join(cmd), r.stdout))
+    return r.stdout
+
+
+def build(force=False, verbose=False):
+    """Compile the library if needed; return its path."""
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= _newest_input():
+        return LIB_PATH
+    os.makedirs(OBJDIR, exist_ok=True)
+    common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
+              "-I" + os.path.join(ROOT, "include"), "-I" + CSRC] + ARCH
+
+    def compile_one(src):
+        obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
+        cmd = [nvcc()] + common + ["-c", src, "-o", obj]
+        if src.endswith(".cpp"):
+            cmd = [nvcc(), "-x", "c++"] + common + ["-c", src, "-o", obj]
+        out = _run(cmd)
+        if verbose and out:
+            sys.stdout.write(out)
+        return obj
+
+    srcs = sources()
+    with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    tmp = LIB_PATH + ".tmp"
+    _run([nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart"])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,278 @@
+// Host-side lattice set-up: the reference's boundary masks and streaming flags
+// and, from them, this engine's per-node flag words and boundary slots.
+//
+// Reference masks (restated from GpuInit.cu:1055-1122 and :1157-1238):
+//   per BC link (node, dir, type):
+//     mask |= type << (dir-1)*B             (B = 2 bits in 2D, 3 in 3D)
+//     mask |= fluid << F                    (F = 19 / 58)
+//     main type (bits 16 / 54): set to type if unset; if a different type was
+//       set, main := WALL and the CORNER bit (18 / 57) is set
+//     2D: mask |= boundary id << 24
+//     stream flag of direction opp(dir) cleared
+//   corner pass: 2D -- a corner node's diagonal links between two typed faces
+//     become walls (NE, NW, SW, SE); 3D -- every typed link becomes a wall.
+#include "lbm_flags.h"
+
+#include <string.h>
+
+#include <thread>
+
+namespace lbm {
+
+namespace {
+const int CX2[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+const int CY2[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+const int OPP2[9] = {0, 3, 4, 1, 2, 7, 8, 5, 6};
+const int CX3[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+const int CY3[19] = {0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1};
+const int CZ3[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1};
+const int OPP3[19] = {0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15};
+}  // namespace
+
+int lattice_cx(int q, int d) { return q == 9 ? CX2[d] : CX3[d]; }
+int lattice_cy(int q, int d) { return q == 9 ? CY2[d] : CY3[d]; }
+int lattice_cz(int q, int d) { return q == 9 ? 0 : CZ3[d]; }
+int lattice_opp(int q, int d) { return q == 9 ? OPP2[d] : OPP3[d]; }
+
+uint64_t ref_type(const RefMasks &r, int node, int dir) {
+    const int b = r.q == 9 ? 2 : 3;
+    return (r.mask[node] >> ((dir - 1) * b)) & (r.q == 9 ? 3ull : 7ull);
+}
+
+uint64_t ref_main_type(const RefMasks &r, int node) {
+    return r.q == 9 ? (r.mask[node] >> 16) & 3ull : (r.mask[node] >> 54) & 7ull;
+}
+
+bool ref_corner(const RefMasks &r, int node) {
+    return r.q == 9 ? (r.mask[node] >> 18) & 1ull : (r.mask[node] >> 57) & 1ull;
+}
+
+int build_ref_masks(const lbm_lattice_desc &L, RefMasks &r, std::string &err) {
+    const int q = L.dims == 2 ? 9 : 19;
+    const long long N = (long long)L.n * L.m * (L.dims == 2 ? 1 : L.h);
+    r.q = q;
+    r.mask.assign((size_t)N, 0ull);
+    r.blocked.assign((size_t)N, 0u);
+    r.linked.assign((size_t)N, 0u);
+    std::vector<uint8_t> seen((size_t)N, 0);
+    const int h = L.dims == 2 ? 1 : L.h;
+    for (int c = 0; c < L.num_conns; ++c) {
+        const int i = L.bc_i[c], j = L.bc_j[c], k = L.bc_k ? L.bc_k[c] : 0;
+        const int dir = L.bc_dir[c];
+        if (i < 0 || i >= L.n || j < 0 || j >= L.m || k < 0 || k >= h || dir < 1 || dir >= q) {
+            err = "BC link " + std::to_string(c) + " out of range";
+            return LBM_ERR_INVALID;
+        }
+        const long long ind = i + (long long)L.n * (j + (long long)L.m * k);
+        const uint64_t type = (uint64_t)L.bc_type[c];
+        uint64_t &mk = r.mask[(size_t)ind];
+        const uint64_t fluid = (uint64_t)(L.node_type[ind] & 1);
+        if (q == 9) {
+            mk |= type << ((dir - 1) * 2);
+            mk |= fluid << 19;
+            const uint64_t all = 3ull << 16;
+            if (!(mk & all)) {
+                mk |= type << 16;
+            } else if ((mk & all) != (type << 16)) {
+                mk &= ~all;
+                mk |= 1ull << 16;
+                mk |= 1ull << 18;
+            }
+            const uint32_t id = L.bc_id ? (uint32_t)L.bc_id[c] : 0u;
+            mk = (uint64_t)((uint32_t)mk | (id << 24));
+        } else {
+            mk |= type << ((dir - 1) * 3);
+            mk |= fluid << 58;
+            const uint64_t all = 7ull << 54;
+            if (!(mk & all)) {
+                mk |= type << 54;
+            } else if ((mk & all) != (type << 54)) {
+                mk &= ~all;
+                mk |= 1ull << 54;
+                mk |= 1ull << 57;
+            }
+        }
+        r.blocked[(size_t)ind] |= 1u << lattice_opp(q, dir);
+        r.linked[(size_t)ind] |= 1u << dir;
+        seen[(size_t)ind] = 1;
+    }
+    for (long long ind = 0; ind < N; ++ind) {
+        if (!seen[(size_t)ind]) continue;
+        uint64_t &mk = r.mask[(size_t)ind];
+        if (q == 9) {
+            if (!((mk >> 18) & 1ull)) continue;
+            auto any = [&](int d) { return ((mk >> ((d - 1) * 2)) & 3ull) != 0; };
+            auto wall = [&](int d) {
+                mk &= ~(3ull << ((d - 1) * 2));
+                mk |= 1ull << ((d - 1) * 2);
+            };
+            if (any(1) && any(2)) wall(5);
+            if (any(3) && any(2)) wall(6);
+            if (any(3) && any(4)) wall(7);
+            if (any(1) && any(4)) wall(8);
+        } else {
+            if (!((mk >> 57) & 1ull)) continue;
+            for (int d = 1; d < 19; ++d)
+                if ((mk >> ((d - 1) * 3)) & 7ull) {
+                    mk &= ~(7ull << ((d - 1) * 3));
+                    mk |= 1ull << ((d - 1) * 3);
+                }
+        }
+    }
+    r.bc_nodes.clear();
+    for (long long ind = 0; ind < N; ++ind)
+        if (seen[(size_t)ind]) r.bc_nodes.push_back(ind);
+    return LBM_OK;
+}
+
+// Face id (inward normal) of an axis link direction pointing out of the domain.
+static int face_of_link(int q, int dir) {
+    const int cx = lattice_cx(q, dir), cy = lattice_cy(q, dir), cz = lattice_cz(q, dir);
+    if (cx == -1 && cy == 0 && cz == 0) return 0;  // link to x-: inward +x
+    if (cx == 1 && cy == 0 && cz == 0) return 1;
+    if (cy == -1 && cx == 0 && cz == 0) return 2;
+    if (cy == 1 && cx == 0 && cz == 0) return 3;
+    if (cz == -1 && cx == 0 && cy == 0) return 4;
+    if (cz == 1 && cx == 0 && cy == 0) return 5;
+    return -1;
+}
+
+int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const RefMasks &r,
+                       DeviceFlags &out, std::string &err) {
+    const int q = r.q;
+    const int n = L.n, m = L.m, h = L.dims == 2 ? 1 : L.h;
+    const long long N = (long long)n * m * h;
+    const bool phys = P.mode == LBM_MODE_PHYSICS;
+    out.word.assign((size_t)N, 0u);
+    out.slot.assign((size_t)N, -1);
+    out.mask.clear();
+    out.kind.clear();
+    out.slot_node.clear();
+
+    if (P.boundary_type == LBM_CURVED) {
+        err = "curved (q-interpolated) walls are not supported";
+        return LBM_ERR_UNSUPPORTED;
+    }
+    if (P.bc_wall_model == LBM_WALL_COMPLEX) {
+        err = "the HH complex wall model is not supported";
+        return LBM_ERR_UNSUPPORTED;
+    }
+
+    // fluid bit and blocked pulls, in parallel over node ranges
+    auto word_range = [&](long long lo, long long hi) {
+        for (long long ind = lo; ind < hi; ++ind) {
+            if (!(L.node_type[ind] & 1)) continue;
+            uint32_t w = W_FLUID | r.blocked[(size_t)ind];
+            if (phys) {
+                const int x = (int)(ind % n), y = (int)((ind / n) % m), z = (int)(ind / ((long long)n * m));
+                uint32_t b = 0;
+                for (int d = 1; d < q; ++d) {
+                    const int opp = lattice_opp(q, d);
+                    // a periodic-type link on the opposite direction streams by wrapping
+                    const bool periodic_link = ((r.linked[(size_t)ind] >> opp) & 1u) &&
+                                               ref_type(r, (int)ind, opp) == LBM_BC_PERIODIC;
+                    if (((w >> d) & 1u) && !periodic_link) b |= 1u << d;
+                    int sx = x - lattice_cx(q, d), sy = y - lattice_cy(q, d), sz = z - lattice_cz(q, d);
+                    bool outside = false;
+                    if (sx < 0 || sx >= n) { if (P.periodic[0] || periodic_link) sx = (sx + n) % n; else outside = true; }
+                    if (sy < 0 || sy >= m) { if (P.periodic[1] || periodic_link) sy = (sy + m) % m; else outside = true; }
+                    if (sz < 0 || sz >= h) { if (P.periodic[2] || periodic_link) sz = (sz + h) % h; else outside = true; }
+                    if (outside) {
+                        b |= 1u << d;
+                        continue;
+                    }
+                    const long long s = sx + (long long)n * (sy + (long long)m * sz);
+                    if (!(L.node_type[s] & 1)) b |= 1u << d;
+                }
+                w = W_FLUID | b;
+            }
+            out.word[(size_t)ind] = w;
+        }
+    };
+    {
+        unsigned nt = std::thread::hardware_concurrency();
+        nt = nt == 0 ? 1 : (nt > 32 ? 32 : nt);
+        if (N < (1 << 16)) nt = 1;
+        std::vector<std::thread> pool;
+        const long long chunk = (N + nt - 1) / nt;
+        for (unsigned t = 0; t < nt; ++t) {
+            const long long lo = t * chunk, hi = lo + chunk < N ? lo + chunk : N;
+            if (lo < hi) pool.emplace_back(word_range, lo, hi);
+        }
+        for (auto &th : pool) th.join();
+    }
+
+    // special nodes
+    for (long long ind : r.bc_nodes) {
+        if (!(L.node_type[ind] & 1)) continue;
+        const int node = (int)ind;
+        bool special = false;
+        int kind = 0;
+        if (!phys) {
+            bool simple = ref_main_type(r, node) == LBM_BC_WALL;
+            for (int d = 1; d < q && simple; ++d) {
+                const uint64_t t = ref_type(r, node, d);
+                const bool wall = t == LBM_BC_WALL;
+                const bool blocked_opp = (r.blocked[(size_t)ind] >> lattice_opp(q, d)) & 1u;
+                if (t > LBM_BC_WALL || wall != blocked_opp) simple = false;
+            }
+            special = !simple;
+            if (special) {
+                for (int d = 1; d < q; ++d) {
+                    const uint64_t t = ref_type(r, node, d);
+                    if (t == LBM_BC_PERIODIC && q == 19 && !ref_corner(r, node)) {
+                        err = "reference-mode 3D periodic copies are not supported (use physics mode)";
+                        return LBM_ERR_UNSUPPORTED;
+                    }
+                }
+                const uint64_t mt = ref_main_type(r, node);
+                if (q == 19 && mt == LBM_BC_OUTLET) {
+                    err = "the reference's 3D outlet kernel addresses populations with the 2D plane "
+                          "size; 3D outlets are supported in physics mode only";
+                    return LBM_ERR_UNSUPPORTED;
+                }
+                if (q == 9 && ref_type(r, node, 1) == LBM_BC_OUTLET &&
+                    P.outlet_profile != LBM_OUTLET_ZOUHE) {
+                    err = "extrapolation outlets read neighbouring boundary nodes; only the Zou-He "
+                          "outlet is supported";
+                    return LBM_ERR_UNSUPPORTED;
+                }
+            }
+        } else {
+            if (ref_corner(r, node)) continue;  // mixed faces: walls only
+            const uint64_t mt = ref_main_type(r, node);
+            if (mt == LBM_BC_SYMMETRY) {
+                err = "symmetry planes are supported in reference mode only";
+                return LBM_ERR_UNSUPPORTED;
+            }
+            if (mt != LBM_BC_INLET && mt != LBM_BC_OUTLET) continue;
+            int face = -1;
+            for (int d = 1; d < q && face < 0; ++d)
+                if (((r.linked[(size_t)ind] >> d) & 1u) && ref_type(r, node, d) == mt)
+                    face = face_of_link(q, d);
+            if (face < 0) continue;
+            kind = face | BCK_ACTIVE;
+            if (mt == LBM_BC_INLET) {
+                if (P.inlet_profile == LBM_INLET_PRESSURE) kind |= BCK_PRESSURE;
+            } else {
+                kind |= BCK_OUTLET;
+                if (P.outlet_profile == LBM_OUTLET_PRESSURE)
+                    kind |= BCK_PRESSURE;
+                else if (P.outlet_profile != LBM_OUTLET_ZOUHE) {
+                    err = "physics-mode outlets must be Zou-He velocity or pressure faces";
+                    return LBM_ERR_UNSUPPORTED;
+                }
+            }
+            special = true;
+        }
+        if (!special) continue;
+        out.slot[(size_t)ind] = (int32_t)out.slot_node.size();
+        out.slot_node.push_back(ind);
+        out.mask.push_back(r.mask[(size_t)ind]);
+        out.kind.push_back(kind);
+        out.word[(size_t)ind] |= W_SPECIAL;
+    }
+    return LBM_OK;
+}
+
+}  // namespace lbm

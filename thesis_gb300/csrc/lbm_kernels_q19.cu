@@ -1,0 +1,46 @@
+// Instantiations of the fused step, init and decode kernels for D3Q19.
+#include "lbm_step.cuh"
+
+namespace lbm {
+
+static dim3 node_grid(const StepParams &p) {
+    return dim3((unsigned)((p.nx + STEP_BLOCK - 1) / STEP_BLOCK), (unsigned)p.ny, (unsigned)p.nz);
+}
+
+#define LBM_FOR_ALL(M)                                                                      \
+    M(1, 0, false) M(1, 1, false) M(1, 2, false) M(2, 0, false) M(2, 1, false) M(2, 2, false) \
+    M(3, 0, false) M(3, 1, false) M(3, 2, false) M(1, 0, true) M(1, 1, true) M(1, 2, true)   \
+    M(2, 0, true) M(2, 1, true) M(2, 2, true) M(3, 0, true) M(3, 1, true) M(3, 2, true)
+
+int launch_step_q19(const StepParams &p, int coll, int st, int phys, cudaStream_t s) {
+#define STEP_CASE(C, S, P)                                                         \
+    if (coll == C && st == S && (phys != 0) == P) {                                \
+        step_kernel<19, C, S, P><<<node_grid(p), STEP_BLOCK, 0, s>>>(p);           \
+        return 0;                                                                  \
+    }
+    LBM_FOR_ALL(STEP_CASE)
+#undef STEP_CASE
+    return -1;
+}
+
+int launch_init_q19(const StepParams &p, const StepParams &o, int coll, int st, int phys, int eq,
+                    cudaStream_t s) {
+#define INIT_CASE(C, S, P)                                                         \
+    if (coll == C && st == S && (phys != 0) == P) {                                \
+        init_kernel<19, C, S, P><<<node_grid(p), STEP_BLOCK, 0, s>>>(p, o, eq);    \
+        return 0;                                                                  \
+    }
+    LBM_FOR_ALL(INIT_CASE)
+#undef INIT_CASE
+    return -1;
+}
+
+int launch_decode_q19(const StepParams &p, int st, double *out, long long n, cudaStream_t s) {
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    if (st == LBM_STORE_F32) decode_kernel<19, LBM_STORE_F32><<<blocks, 256, 0, s>>>(p, out, n);
+    else if (st == LBM_STORE_F16S) decode_kernel<19, LBM_STORE_F16S><<<blocks, 256, 0, s>>>(p, out, n);
+    else decode_kernel<19, LBM_STORE_F64><<<blocks, 256, 0, s>>>(p, out, n);
+    return 0;
+}
+
+}  // namespace lbm

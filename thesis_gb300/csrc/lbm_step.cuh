@@ -1,0 +1,210 @@
+// Fused lattice-Boltzmann time step: one launch per step does what the
+// reference does in four (collision, streaming, boundary and macroscopic
+// kernels with a host synchronisation after each, Iterate3D.cu:493-653):
+//
+//   for every fluid node, in registers:
+//     f_d  <- post-collision population d of the neighbour x - c_d   (pull)
+//             or, across a blocked link, the node's own population
+//             (reference: f_d itself; physics: f_opp(d), half-way bounce-back)
+//     boundary conditions (reference wall copies / Zou-He faces)
+//     rho, u <- moments of f  (+ g/omega body-force shift in 3D)
+//     f <- collide(f, rho, u)  and store to the other buffer
+//
+// The state between launches is the post-collision population field in a
+// pull double buffer, SoA by direction (one contiguous array per direction,
+// x fastest), so a warp's loads and stores are 32 consecutive nodes of one
+// direction.  Per node the kernel reads one 32-bit flag word and Q
+// populations and writes Q populations; macroscopic fields are written only
+// on steps that need them (residuals, output).
+#pragma once
+#include "lbm_bc.cuh"
+
+namespace lbm {
+
+struct StepParams {
+    const void *fin[19];
+    void *fout[19];
+    const uint32_t *word;
+    const int32_t *slot;
+    const unsigned long long *bc_mask;
+    const int32_t *bc_kind;
+    const float *bc_uvw;
+    float *rho, *ux, *uy, *uz;
+    int nx, ny, nz;
+    int write_macro;
+    float omega, omega_m, gshift;
+    float rho_in, rho_out;
+    float scale, inv_scale;
+    int outlet_profile;
+    int update_inlet_outlet;
+};
+
+constexpr int STEP_BLOCK = 128;
+
+template <int Q, int COLL, int ST, bool PHYS>
+__device__ __forceinline__ void collide(typename Store<ST>::R (&f)[Q], typename Store<ST>::R rho,
+                                        typename Store<ST>::R ux, typename Store<ST>::R uy,
+                                        typename Store<ST>::R uz, const StepParams &p) {
+    using R = typename Store<ST>::R;
+    if (COLL == LBM_BGKW) {
+        collide_bgk<Q, R>(f, rho, ux, uy, uz, (R)p.omega);
+    } else if (COLL == LBM_TRT) {
+        collide_trt<Q, R>(f, rho, ux, uy, uz, (R)p.omega, (R)p.omega_m);
+    } else {
+        if constexpr (Q == 9)
+            collide_mrt9<!PHYS, R>(f, rho, ux, uy, (R)p.omega);
+        else
+            collide_mrt19<!PHYS, R>(f, rho, ux, uy, uz, (R)p.omega);
+    }
+}
+
+template <int Q, int COLL, int ST, bool PHYS>
+__global__ void __launch_bounds__(STEP_BLOCK) step_kernel(const StepParams p) {
+    using S = Store<ST>;
+    using T = typename S::T;
+    using R = typename S::R;
+    using L = Lat<Q>;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= p.nx) return;
+    const int y = blockIdx.y, z = blockIdx.z;
+    const int node = x + p.nx * (y + p.ny * z);
+    const uint32_t w = __ldg(p.word + node);
+    if (!(w & W_FLUID)) return;
+
+    // Neighbour coordinates wrap periodically; links that must not wrap are
+    // blocked in the flag word, so a wrapped address is only read where the
+    // lattice is periodic.
+    const int xm = x == 0 ? p.nx - 1 : x - 1, xp = x == p.nx - 1 ? 0 : x + 1;
+    const int ym = y == 0 ? p.ny - 1 : y - 1, yp = y == p.ny - 1 ? 0 : y + 1;
+    const int zm = z == 0 ? p.nz - 1 : z - 1, zp = z == p.nz - 1 ? 0 : z + 1;
+
+    R f[Q];
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+        if (d == 0) {
+            f[0] = S::load((const T *)p.fin[0] + node, L::w(0), p.inv_scale);
+            continue;
+        }
+        const int sx = L::cx(d) == 1 ? xm : (L::cx(d) == -1 ? xp : x);
+        const int sy = L::cy(d) == 1 ? ym : (L::cy(d) == -1 ? yp : y);
+        const int sz = L::cz(d) == 1 ? zm : (L::cz(d) == -1 ? zp : z);
+        const int src = sx + p.nx * (sy + p.ny * sz);
+        const bool blocked = (w >> d) & 1u;
+        const T *base = (const T *)p.fin[(blocked && PHYS) ? L::opp(d) : d];
+        f[d] = S::load(base + (blocked ? node : src), L::w(d), p.inv_scale);
+    }
+
+    bool keep_macro = false, zero_v = false;
+    if (w & W_SPECIAL) {
+        const int sl = __ldg(p.slot + node);
+        const R u0 = (R)__ldg(p.bc_uvw + 3 * sl), v0 = (R)__ldg(p.bc_uvw + 3 * sl + 1),
+                w0 = (R)__ldg(p.bc_uvw + 3 * sl + 2);
+        if constexpr (!PHYS) {
+            const unsigned long long mk = __ldg(p.bc_mask + sl);
+            if constexpr (Q == 9)
+                bc_ref_d2q9<R>(f, (uint32_t)mk, u0, p.outlet_profile, zero_v);
+            else
+                bc_ref_d3q19<R>(f, mk, u0, v0, w0, p.update_inlet_outlet, keep_macro);
+        } else {
+            const int kind = __ldg(p.bc_kind + sl);
+            if (kind & BCK_ACTIVE) {
+                const bool pressure = (kind & BCK_PRESSURE) != 0;
+                const R rset = (kind & BCK_OUTLET) ? (R)p.rho_out : (R)p.rho_in;
+                bc_phys<Q, R>(f, kind & BCK_FACE_MASK, pressure, rset, u0, v0, w0);
+            }
+        }
+    } else if constexpr (!PHYS) {
+        // reference straight walls: f[opp(dir)] = f[dir] for every wall link
+        // dir in direction order (GpuBoundaries.cu:436, :483); on a plain wall
+        // node the wall links are exactly the opposites of the blocked pulls.
+#pragma unroll
+        for (int dir = 1; dir < Q; ++dir)
+            if ((w >> L::opp(dir)) & 1u) f[L::opp(dir)] = f[dir];
+    }
+
+    R rho = 0, jx = 0, jy = 0, jz = 0;
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+        rho += f[d];
+        if (L::cx(d)) jx += (R)L::cx(d) * f[d];
+        if (L::cy(d)) jy += (R)L::cy(d) * f[d];
+        if (L::cz(d)) jz += (R)L::cz(d) * f[d];
+    }
+    R ux, uy, uz;
+    if (keep_macro) {
+        rho = (R)p.rho[node];
+        ux = (R)p.ux[node];
+        uy = (R)p.uy[node];
+        uz = (R)p.uz[node];
+    } else {
+        const R inv = (R)1 / rho;
+        ux = jx * inv + (R)p.gshift;
+        uy = zero_v ? (R)0 : jy * inv;
+        uz = jz * inv;
+        if (p.write_macro) {
+            p.rho[node] = (float)rho;
+            p.ux[node] = (float)ux;
+            p.uy[node] = (float)uy;
+            p.uz[node] = (float)uz;
+        }
+    }
+
+    collide<Q, COLL, ST, PHYS>(f, rho, ux, uy, uz, p);
+
+#pragma unroll
+    for (int d = 0; d < Q; ++d) S::store((T *)p.fout[d] + node, f[d], L::w(d), p.scale);
+}
+
+// First post-collision field: f0 = 0 (the reference's start, Iterate.cu:244)
+// or f0 = f_eq(rho0, u0), collided with rho0, u0 read from the macro arrays.
+// Solid nodes get f = 0 in both buffers, which is what a fluid node pulls
+// from a solid neighbour when no boundary link blocks it (the reference never
+// writes solid nodes).
+template <int Q, int COLL, int ST, bool PHYS>
+__global__ void __launch_bounds__(STEP_BLOCK) init_kernel(const StepParams p, const StepParams other,
+                                                          int equilibrium_start) {
+    using S = Store<ST>;
+    using T = typename S::T;
+    using R = typename S::R;
+    using L = Lat<Q>;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= p.nx) return;
+    const int node = x + p.nx * (blockIdx.y + p.ny * blockIdx.z);
+    const uint32_t w = p.word[node];
+    if (!(w & W_FLUID)) {
+#pragma unroll
+        for (int d = 0; d < Q; ++d) {
+            ((T *)p.fout[d])[node] = S::encode((R)0, L::w(d), p.scale);
+            ((T *)other.fout[d])[node] = S::encode((R)0, L::w(d), p.scale);
+        }
+        return;
+    }
+    const R rho = (R)p.rho[node], ux = (R)p.ux[node], uy = (R)p.uy[node], uz = (R)p.uz[node];
+    R f[Q];
+    const R usq15 = (R)1.5 * (ux * ux + uy * uy + uz * uz);
+#pragma unroll
+    for (int d = 0; d < Q; ++d) f[d] = equilibrium_start ? feq<Q, R>(d, rho, ux, uy, uz, usq15) : (R)0;
+    collide<Q, COLL, ST, PHYS>(f, rho, ux, uy, uz, p);
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+        S::store((T *)p.fout[d] + node, f[d], L::w(d), p.scale);
+        // The other buffer's fluid entries are overwritten by the first step
+        // before anything reads them; give them the same finite values.
+        S::store((T *)other.fout[d] + node, f[d], L::w(d), p.scale);
+    }
+}
+
+// Decode a population field to double (host read-back of the state).
+template <int Q, int ST>
+__global__ void decode_kernel(const StepParams p, double *out, long long n) {
+    using S = Store<ST>;
+    using T = typename S::T;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+#pragma unroll
+    for (int d = 0; d < Q; ++d)
+        out[d * n + i] = (double)S::load((const T *)p.fin[d] + i, Lat<Q>::w(d), p.inv_scale);
+}
+
+}  // namespace lbm
+

@@ -1,0 +1,32 @@
+// Internal constants shared by host and device code.
+#pragma once
+#include <stdint.h>
+
+#include "thesis_lbm.h"
+
+namespace lbm {
+
+// Per-node flag word, one uint32 per lattice node:
+//   bit 0        fluid node (the reference's fluid_d == 1)
+//   bits 1..18   pull of population d is blocked (the reference's stream flag
+//                for direction d cleared, or, in physics mode, x - c_d is
+//                solid or outside a non-periodic domain)
+//   bit 19       special node: boundary handling needs its slot record
+constexpr uint32_t W_FLUID = 1u;
+constexpr uint32_t W_SPECIAL = 1u << 19;
+
+// Physics-mode slot kinds (bc_kind): face id in bits 0..2 (inward normal
+// 0 +x, 1 -x, 2 +y, 3 -y, 4 +z, 5 -z), pressure face, outlet face, active.
+constexpr int BCK_FACE_MASK = 7;
+constexpr int BCK_PRESSURE = 8;
+constexpr int BCK_OUTLET = 16;
+constexpr int BCK_ACTIVE = 32;
+
+struct StepParams;
+// Kernel launchers (lbm_kernels_q9.cu / lbm_kernels_q19.cu).
+int launch_step(int q, const StepParams &p, int coll, int storage, int phys, void *stream);
+int launch_init(int q, const StepParams &p, const StepParams &other, int coll, int storage,
+                int phys, int equilibrium_start, void *stream);
+int launch_decode(int q, const StepParams &p, int storage, double *out, long long n, void *stream);
+
+}  // namespace lbm

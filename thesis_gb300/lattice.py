@@ -1,0 +1,268 @@
+"""Lattices in the reference's file layout, built from geometry.
+
+A lattice is what the reference's solver reads from its Node and BC files
+(Source code/lbm-solver_final/FilesReading.cu:270-347): a fluid/solid flag per
+node (x fastest) and a list of boundary links (i, j, k, dir, type, id), where
+`dir` is the lattice direction from a fluid node into the boundary and `type`
+is 1 wall, 2 inlet, 3 outlet, 4 periodic, 5 symmetry.
+
+Builders here emit the workloads this engine is measured on:
+
+* cavity2d / cavity3d -- lid-driven cavities: every node fluid, a link for each
+  direction leaving the domain, inlet-typed where it leaves through the lid.
+* sphere_duct -- a duct packed with non-overlapping spheres of random radii
+  until a target porosity, pressure faces at both ends of the long axis.
+* channel2d -- a 2D channel with circular and rectangular obstacles.
+"""
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# Reference direction order (GpuInit.cu:97-98, :835-837).
+CX2 = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1])
+CY2 = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1])
+CX3 = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0])
+CY3 = np.array([0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1])
+CZ3 = np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1])
+W2 = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
+W3 = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+
+
+@dataclass
+class Lattice:
+    dims: int
+    n: int
+    m: int
+    h: int
+    node_type: np.ndarray                      # int32, n*m*h, x fastest
+    bc: np.ndarray = field(default=None)       # int32 (num_conns, 6): i, j, k, dir, type, id
+
+    def __post_init__(self):
+        self.node_type = np.ascontiguousarray(self.node_type.reshape(-1), dtype=np.int32)
+        if self.bc is None:
+            self.bc = np.zeros((0, 6), np.int32)
+        self.bc = np.ascontiguousarray(self.bc, dtype=np.int32)
+
+    @property
+    def q(self):
+        return 9 if self.dims == 2 else 19
+
+    @property
+    def num_nodes(self):
+        return self.n * self.m * self.h
+
+    @property
+    def num_fluid(self):
+        return int(self.node_type.sum())
+
+    def coords(self, delta=None):
+        """Node coordinates as the generator writes them: index * spacing."""
+        d = delta if delta is not None else 1.0 / max(self.n - 1, 1)
+        idx = np.arange(self.num_nodes)
+        x = (idx % self.n) * d
+        y = ((idx // self.n) % self.m) * d
+        z = (idx // (self.n * self.m)) * d
+        return x, y, z
+
+
+def _boundary_links(dims, n, m, h, fluid, face_type):
+    """Links of fluid nodes whose direction leaves the domain.
+
+    face_type(axis, side) -> BC type for a link leaving through that face, or
+    0 for none.  A link leaving through several faces takes the first non-zero
+    type in the order x-, x+, y-, y+, z-, z+.
+    """
+    if dims == 2:
+        cxs, cys, czs = CX2, CY2, np.zeros(9, int)
+    else:
+        cxs, cys, czs = CX3, CY3, CZ3
+    q = len(cxs)
+    idx = np.nonzero(fluid)[0]
+    x = idx % n
+    y = (idx // n) % m
+    z = idx // (n * m)
+    on_edge = (x == 0) | (x == n - 1) | (y == 0) | (y == m - 1)
+    if dims == 3:
+        on_edge |= (z == 0) | (z == h - 1)
+    idx, x, y, z = idx[on_edge], x[on_edge], y[on_edge], z[on_edge]
+    out = []
+    for d in range(1, q):
+        tx, ty, tz = x + cxs[d], y + cys[d], z + czs[d]
+        t = np.zeros(idx.shape, np.int32)
+        for axis, coord, size in ((0, tx, n), (1, ty, m), (2, tz, h)):
+            for side, sel in ((0, coord < 0), (1, coord > size - 1)):
+                ft = face_type(axis, side)
+                if ft:
+                    t = np.where((t == 0) & sel, ft, t)
+        leave = (tx < 0) | (tx > n - 1) | (ty < 0) | (ty > m - 1) | (tz < 0) | (tz > h - 1)
+        sel = leave & (t > 0)
+        if sel.any():
+            k = np.count_nonzero(sel)
+            out.append(np.stack([x[sel], y[sel], z[sel], np.full(k, d), t[sel], np.zeros(k, int)], 1))
+    if not out:
+        return np.zeros((0, 6), np.int32)
+    bc = np.concatenate(out).astype(np.int32)
+    # node-major order, as a generator sweeping the lattice would write them
+    order = np.lexsort((bc[:, 3], bc[:, 0] + n * (bc[:, 1] + m * bc[:, 2])))
+    return bc[order]
+
+
+def cavity2d(n, m=None):
+    """Lid-driven cavity: all nodes fluid, walls on three sides, the lid
+    (links leaving through y = m-1) an inlet."""
+    m = n if m is None else m
+    fluid = np.ones(n * m, np.int32)
+
+    def ft(axis, side):
+        return 2 if (axis == 1 and side == 1) else 1
+    return Lattice(2, n, m, 1, fluid, _boundary_links(2, n, m, 1, fluid, ft))
+
+
+def cavity3d(n, m=None, h=None):
+    """3D lid-driven cavity with the lid at z = h-1."""
+    m = n if m is None else m
+    h = n if h is None else h
+    fluid = np.ones(n * m * h, np.int32)
+
+    def ft(axis, side):
+        return 2 if (axis == 2 and side == 1) else 1
+    return Lattice(3, n, m, h, fluid, _boundary_links(3, n, m, h, fluid, ft))
+
+
+def pack_spheres(shape, porosity=0.70, rmin=6.0, rmax=14.0, seed=0, margin_axis=2, margin=2,
+                 max_attempts=2_000_000):
+    """Random sequential insertion of non-overlapping spheres.
+
+    Radii uniform in [rmin, rmax], centres uniform in the box (kept `margin`
+    nodes plus a radius away from both ends of `margin_axis`, so the pressure
+    faces stay fluid); spheres are added until the solid fraction reaches
+    1 - porosity.  Returns (solid mask (z, y, x) bool, spheres (k, 4)).
+    """
+    n, m, h = shape
+    rng = np.random.default_rng(seed)
+    target = (1.0 - porosity) * n * m * h
+    solid = np.zeros((h, m, n), bool)
+    centres = np.zeros((0, 3))
+    radii = np.zeros(0)
+    solid_count = 0
+    attempts = 0
+    batch = 256
+    while solid_count < target and attempts < max_attempts:
+        r = rng.uniform(rmin, rmax, batch)
+        c = rng.uniform(0, 1, (batch, 3)) * np.array([n - 1, m - 1, h - 1], float)
+        lo = margin + r
+        hi = np.array([n - 1, m - 1, h - 1], float)[margin_axis] - margin - r
+        c[:, margin_axis] = lo + rng.uniform(0, 1, batch) * np.maximum(hi - lo, 0)
+        attempts += batch
+        for k in range(batch):
+            if centres.shape[0]:
+                d2 = ((centres - c[k]) ** 2).sum(1)
+                if np.any(d2 < (radii + r[k]) ** 2):
+                    continue
+            centres = np.vstack([centres, c[k]])
+            radii = np.append(radii, r[k])
+            x0, y0, z0 = c[k]
+            rr = r[k]
+            xs = slice(max(int(np.floor(x0 - rr)), 0), min(int(np.ceil(x0 + rr)) + 1, n))
+            ys = slice(max(int(np.floor(y0 - rr)), 0), min(int(np.ceil(y0 + rr)) + 1, m))
+            zs = slice(max(int(np.floor(z0 - rr)), 0), min(int(np.ceil(z0 + rr)) + 1, h))
+            zz, yy, xx = np.meshgrid(np.arange(zs.start, zs.stop), np.arange(ys.start, ys.stop),
+                                     np.arange(xs.start, xs.stop), indexing="ij")
+            inside = (xx - x0) ** 2 + (yy - y0) ** 2 + (zz - z0) ** 2 <= rr * rr
+            sub = solid[zs, ys, xs]
+            solid_count += int(np.count_nonzero(inside & ~sub))
+            sub |= inside
+            if solid_count >= target:
+                break
+    spheres = np.concatenate([centres, radii[:, None]], 1) if radii.size else np.zeros((0, 4))
+    return solid, spheres
+
+
+def sphere_duct(n=256, m=256, h=512, porosity=0.70, rmin=6.0, rmax=14.0, seed=0):
+    """Pressure-driven duct along z packed with spheres: inlet face z = 0,
+    outlet face z = h-1, the four side faces and the spheres are walls (in
+    physics mode, links into solid or out of the domain bounce back, so only
+    the two pressure faces need BC links)."""
+    solid, spheres = pack_spheres((n, m, h), porosity, rmin, rmax, seed, margin_axis=2)
+    fluid = (~solid).astype(np.int32).reshape(-1)
+
+    def ft(axis, side):
+        if axis == 2:
+            return 2 if side == 0 else 3
+        return 0
+    lat = Lattice(3, n, m, h, fluid, _boundary_links(3, n, m, h, fluid, ft))
+    lat.spheres = spheres
+    return lat
+
+
+def channel2d(n=1024, m=256, seed=0, n_obstacles=None):
+    """2D channel along x with 1-6 circles (radius 8-32) and rectangles
+    (sides 10-60), non-overlapping and clear of the inlet and outlet; walls at
+    y = 0 and y = m-1, inlet x = 0, outlet x = n-1."""
+    rng = np.random.default_rng(seed)
+    k = n_obstacles if n_obstacles is not None else int(rng.integers(1, 7))
+    solid = np.zeros((m, n), bool)
+    boxes = []
+    yy, xx = np.mgrid[0:m, 0:n]
+    placed = 0
+    tries = 0
+    while placed < k and tries < 10_000:
+        tries += 1
+        rmax = min(32.0, (m - 8) / 2.0, n * 0.3)
+        smax = min(60.0, m - 8.0, n * 0.5)
+        if rng.uniform() < 0.5:
+            r = rng.uniform(min(8.0, rmax), rmax)
+            cx = rng.uniform(n * 0.1 + r, n * 0.85 - r)
+            cy = rng.uniform(r + 3, m - 4 - r)
+            bb = (cx - r, cy - r, cx + r, cy + r)
+            shape = ("circle", cx, cy, r)
+        else:
+            w, hh = rng.uniform(min(10.0, smax), smax, 2)
+            x0 = rng.uniform(n * 0.1, n * 0.85 - w)
+            y0 = rng.uniform(3, m - 4 - hh)
+            bb = (x0, y0, x0 + w, y0 + hh)
+            shape = ("rect", x0, y0, w, hh)
+        if any(not (bb[2] + 2 < b[0] or b[2] + 2 < bb[0] or bb[3] + 2 < b[1] or b[3] + 2 < bb[1]) for b in boxes):
+            continue
+        boxes.append(bb)
+        if shape[0] == "circle":
+            solid |= (xx - shape[1]) ** 2 + (yy - shape[2]) ** 2 <= shape[3] ** 2
+        else:
+            solid |= (xx >= shape[1]) & (xx <= shape[1] + shape[3]) & (yy >= shape[2]) & (yy <= shape[2] + shape[4])
+        placed += 1
+    fluid = (~solid).astype(np.int32).reshape(-1)
+
+    def ft(axis, side):
+        if axis == 0:
+            return 2 if side == 0 else 3
+        return 1
+    return Lattice(2, n, m, 1, fluid, _boundary_links(2, n, m, 1, fluid, ft))
+
+
+def read_node_file(path, dims):
+    """Node file (FilesReading.cu:270-305): `i j x y fluid` (2D, spaces) or
+    `i<TAB>j<TAB>k<TAB>x<TAB>y<TAB>z<TAB>fluid` (3D).  Returns columns."""
+    a = np.loadtxt(path, ndmin=2)
+    return a
+
+
+def read_bc_file(path, dims):
+    """BC file (FilesReading.cu:307-347): `i j dir bc x y id` (2D) or
+    `i j k dir bc x y z id` (3D)."""
+    return np.loadtxt(path, ndmin=2)
+
+
+def from_files(node_path, bc_path):
+    """Build a Lattice from reference-format Node and BC files."""
+    nodes = np.loadtxt(node_path, ndmin=2)
+    dims = 3 if nodes.shape[1] == 7 else 2
+    bcs = np.loadtxt(bc_path, ndmin=2)
+    if dims == 3:
+        n, m, h = int(nodes[-1, 0]) + 1, int(nodes[-1, 1]) + 1, int(nodes[-1, 2]) + 1
+        fluid = nodes[:, 6]
+        bc = np.stack([bcs[:, 0], bcs[:, 1], bcs[:, 2], bcs[:, 3], bcs[:, 4], bcs[:, 8]], 1)
+    else:
+        n, m, h = int(nodes[-1, 0]) + 1, int(nodes[-1, 1]) + 1, 1
+        fluid = nodes[:, 4]
+        bc = np.stack([bcs[:, 0], bcs[:, 1], np.zeros(len(bcs)), bcs[:, 2], bcs[:, 3], bcs[:, 6]], 1)
+    return Lattice(dims, n, m, h, fluid.astype(np.int32), bc.astype(np.int32))

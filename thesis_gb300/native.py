@@ -1,0 +1,98 @@
+"""ctypes binding of libthesis_lbm.so (include/thesis_lbm.h).
+
+The library is required: there is no CPU fallback.  If it has not been built,
+every call raises with the command that builds it.
+"""
+import ctypes as C
+import os
+
+from . import build as _build
+
+LBM_OK, LBM_DIVERGED, LBM_ERR_FILE, LBM_ERR_UNSUPPORTED, LBM_ERR_INVALID, LBM_ERR_CUDA, LBM_ERR_NOMEM = range(7)
+STORE_F32, STORE_F16S, STORE_F64 = 0, 1, 2
+MODE_REFERENCE, MODE_PHYSICS = 0, 1
+BGKW, TRT, MRT = 1, 2, 3
+INLET, NO_INLET, INLET_PRESSURE = 1, 2, 4
+OUTLET_ZOUHE, OUTLET_SECOND, OUTLET_FIRST, OUTLET_HEMODEL, OUTLET_PRESSURE = 1, 2, 3, 4, 5
+CURVED, STRAIGHT = 1, 2
+WALL_SIMPLE, WALL_COMPLEX = 1, 2
+BC_WALL, BC_INLET, BC_OUTLET, BC_PERIODIC, BC_SYMMETRY = 1, 2, 3, 4, 5
+NORMS = 5
+
+_IP = C.POINTER(C.c_int)
+
+
+class LatticeDesc(C.Structure):
+    _fields_ = [("dims", C.c_int), ("n", C.c_int), ("m", C.c_int), ("h", C.c_int),
+                ("node_type", _IP), ("num_conns", C.c_int),
+                ("bc_i", _IP), ("bc_j", _IP), ("bc_k", _IP),
+                ("bc_dir", _IP), ("bc_type", _IP), ("bc_id", _IP)]
+
+
+class Params(C.Structure):
+    _fields_ = [("u", C.c_double), ("v", C.c_double), ("w", C.c_double), ("rho", C.c_double),
+                ("viscosity", C.c_double), ("g", C.c_double),
+                ("inlet_profile", C.c_int), ("outlet_profile", C.c_int),
+                ("collision_model", C.c_int), ("boundary_type", C.c_int),
+                ("bc_wall_model", C.c_int), ("update_inlet_outlet", C.c_int),
+                ("mode", C.c_int), ("storage", C.c_int),
+                ("rho_in", C.c_double), ("rho_out", C.c_double), ("f16_scale", C.c_double),
+                ("periodic", C.c_int * 3), ("init_equilibrium", C.c_int)]
+
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB_PATH
+
+
+def lib():
+    """Load the native library (raises if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        raise RuntimeError("libthesis_lbm.so is not built (%s); run "
+                           "`python -c 'import __graft_entry__ as g; g.build()'`" % path)
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    fp = C.POINTER(C.c_float)
+    dp = C.POINTER(C.c_double)
+    sig = {
+        "lbm_version": (C.c_int, []),
+        "lbm_last_error": (C.c_char_p, []),
+        "lbm_create": (C.c_int, [C.POINTER(LatticeDesc), C.POINTER(Params), C.POINTER(vp)]),
+        "lbm_set_inlet_velocity": (C.c_int, [vp, fp, fp, fp]),
+        "lbm_init": (C.c_int, [vp, fp, fp, fp, fp]),
+        "lbm_step": (C.c_int, [vp, C.c_int, C.c_int, vp]),
+        "lbm_get_macro": (C.c_int, [vp, fp, fp, fp, fp]),
+        "lbm_get_populations": (C.c_int, [vp, dp]),
+        "lbm_macro_norms": (C.c_int, [vp, dp]),
+        "lbm_status": (C.c_int, [vp]),
+        "lbm_fluid_nodes": (C.c_longlong, [vp]),
+        "lbm_bytes_per_update": (C.c_int, [vp]),
+        "lbm_destroy": (None, [vp]),
+        "lbm_build_flags": (C.c_int, [C.POINTER(LatticeDesc), C.POINTER(Params),
+                                      C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
+                                      C.POINTER(C.c_int32), C.POINTER(C.c_int)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+class LbmError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("lbm error %d: %s" % (code, msg))
+        self.code = code
+
+
+def check(rc):
+    if rc != LBM_OK:
+        raise LbmError(rc, lib().lbm_last_error().decode(errors="replace"))
+    return rc

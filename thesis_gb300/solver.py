@@ -1,0 +1,175 @@
+"""Python host mirror of the reference's time-step entry points.
+
+`Arguments` carries the fields of the reference's Arguments struct
+(Source code/lbm-solver_final/include/Arguments.h:86-135) that the time-step
+loop reads; `Solver` wraps one libthesis_lbm handle.  All compute runs in the
+CUDA library; this module only marshals arrays.
+"""
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import native as N
+from .lattice import Lattice
+
+
+@dataclass
+class Arguments:
+    u: float = 0.0
+    v: float = 0.0
+    w: float = 0.0
+    rho: float = 1.0
+    viscosity: float = 0.1
+    g: float = 0.0
+    inlet_profile: int = N.NO_INLET
+    outlet_profile: int = N.OUTLET_SECOND
+    collision_model: int = N.BGKW
+    boundary_type: int = N.STRAIGHT
+    bc_wall_model: int = N.WALL_SIMPLE
+    update_inlet_outlet: int = 1
+    # engine options
+    mode: int = N.MODE_REFERENCE
+    storage: int = N.STORE_F32
+    rho_in: float = 1.0
+    rho_out: float = 1.0
+    f16_scale: float = 0.0
+    periodic: tuple = (0, 0, 0)
+    init_equilibrium: int = 0
+
+    def to_c(self):
+        p = N.Params()
+        for k in ("u", "v", "w", "rho", "viscosity", "g", "rho_in", "rho_out", "f16_scale"):
+            setattr(p, k, float(getattr(self, k)))
+        for k in ("inlet_profile", "outlet_profile", "collision_model", "boundary_type",
+                  "bc_wall_model", "update_inlet_outlet", "mode", "storage", "init_equilibrium"):
+            setattr(p, k, int(getattr(self, k)))
+        for i in range(3):
+            p.periodic[i] = int(self.periodic[i])
+        return p
+
+    @property
+    def omega(self):
+        return 1.0 / (3.0 * self.viscosity + 0.5)
+
+
+def _iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _fptr(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def lattice_desc(lat: Lattice):
+    """Fill an lbm_lattice_desc; the returned tuple keeps the arrays alive."""
+    bc = lat.bc
+    cols = [np.ascontiguousarray(bc[:, k], dtype=np.int32) for k in range(6)]
+    d = N.LatticeDesc()
+    d.dims, d.n, d.m, d.h = lat.dims, lat.n, lat.m, lat.h
+    d.node_type = _iptr(lat.node_type)
+    d.num_conns = int(bc.shape[0])
+    d.bc_i, d.bc_j = _iptr(cols[0]), _iptr(cols[1])
+    d.bc_k = _iptr(cols[2]) if lat.dims == 3 else None
+    d.bc_dir, d.bc_type, d.bc_id = _iptr(cols[3]), _iptr(cols[4]), _iptr(cols[5])
+    return d, cols
+
+
+def build_flags(lat: Lattice, args: Arguments):
+    """Reference masks, flag words and slots computed by the library on the
+    host (no GPU).  Returns (mask uint64, word uint32, slot int32, n_bc)."""
+    L = N.lib()
+    d, keep = lattice_desc(lat)
+    p = args.to_c()
+    nn = lat.num_nodes
+    mask = np.zeros(nn, np.uint64)
+    word = np.zeros(nn, np.uint32)
+    slot = np.zeros(nn, np.int32)
+    nbc = C.c_int(0)
+    N.check(L.lbm_build_flags(C.byref(d), C.byref(p), mask.ctypes.data_as(C.POINTER(C.c_uint64)),
+                              word.ctypes.data_as(C.POINTER(C.c_uint32)),
+                              slot.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(nbc)))
+    del keep
+    return mask, word, slot, nbc.value
+
+
+class Solver:
+    """One lattice on the GPU.  Usage: s = Solver(lat, args); s.init();
+    s.step(100, write_macro=True); rho, u, v, w = s.macro()."""
+
+    def __init__(self, lat: Lattice, args: Arguments):
+        self.lat = lat
+        self.args = args
+        self._lib = N.lib()
+        d, keep = lattice_desc(lat)
+        p = args.to_c()
+        h = C.c_void_p()
+        N.check(self._lib.lbm_create(C.byref(d), C.byref(p), C.byref(h)))
+        del keep
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.lbm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_inlet_velocity(self, u=None, v=None, w=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float32).reshape(-1) for a in (u, v, w)]
+        N.check(self._lib.lbm_set_inlet_velocity(self._h, *[_fptr(a) for a in arrs]))
+
+    def init(self, rho=None, u=None, v=None, w=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float32).reshape(-1) for a in (rho, u, v, w)]
+        N.check(self._lib.lbm_init(self._h, *[_fptr(a) for a in arrs]))
+
+    def step(self, nsteps, write_macro=True, stream=None):
+        N.check(self._lib.lbm_step(self._h, int(nsteps), int(bool(write_macro)),
+                                   None if stream is None else C.c_void_p(stream)))
+
+    def macro(self):
+        nn = self.lat.num_nodes
+        out = [np.empty(nn, np.float32) for _ in range(4)]
+        N.check(self._lib.lbm_get_macro(self._h, *[_fptr(a) for a in out]))
+        return out
+
+    def populations(self):
+        q = self.lat.q
+        f = np.empty(q * self.lat.num_nodes, np.float64)
+        N.check(self._lib.lbm_get_populations(self._h, f.ctypes.data_as(C.POINTER(C.c_double))))
+        return f.reshape(q, -1)
+
+    def norms(self):
+        out = np.zeros(N.NORMS, np.float64)
+        rc = self._lib.lbm_macro_norms(self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc not in (N.LBM_OK, N.LBM_DIVERGED):
+            N.check(rc)
+        return out, rc
+
+    def residual(self):
+        """Velocity residual sqrt(sum|u - u_prev|^2) / sqrt(sum|u|^2) over
+        fluid nodes (FP64), relative to the field at the previous call."""
+        nm, rc = self.norms()
+        return (np.sqrt(nm[0]) / np.sqrt(nm[1]) if nm[1] > 0 else np.inf), rc
+
+    @property
+    def fluid_nodes(self):
+        return int(self._lib.lbm_fluid_nodes(self._h))
+
+    @property
+    def bytes_per_update(self):
+        return int(self._lib.lbm_bytes_per_update(self._h))
+
+    @property
+    def status(self):
+        return int(self._lib.lbm_status(self._h))
