@@ -167,6 +167,18 @@ void lbm_destroy(lbm_handle h);
 int lbm_build_flags(const lbm_lattice_desc *lattice, const lbm_params *params, uint64_t *mask,
                     uint32_t *word, int32_t *slot, int *num_bc_nodes);
 
+/* Lattice generator: STAR-CD geometry (.vrt vertices, .bnd quadrilateral
+ * boundary faces) to the Node and BC files the solver reads, byte-identical to
+ * the reference generator `latticegen <geom> <n> <xseed> <yseed> <zseed>
+ * <out> <1|2>` (latticegen2_W8/main.cpp:19-66, FluidTracking.cpp:24-236).
+ * n_x: nodes along x; seed: a point inside the fluid; complexity 1 writes a
+ * boundary link when first met, 2 after the flood fill.  out_dims (may be
+ * NULL) receives n, m, h. */
+int lbm_latticegen(const char *vrt_path, const char *bnd_path, int n_x, double xseed, double yseed,
+                   double zseed, int complexity, const char *node_path, const char *bc_path,
+                   int *out_dims);
+const char *lbm_latticegen_error(void);
+
 /* Library version, for load checks. */
 int lbm_version(void);
 

@@ -123,6 +123,7 @@ typedef struct {
     int mode;            /* 0 reference semantics, 1 physics */
     int init_kind;       /* 0 f=0 (reference), 1 f=feq(rho,u) */
     double rho_in, rho_out;
+    int periodic[3];     /* physics mode: axes whose out-of-domain pulls wrap */
 } orc_params;
 
 }  // extern "C"
@@ -434,7 +435,24 @@ void stream_all(Lattice<T> &L) {
         for (int d = 1; d < q; ++d) {
             bool st = L.stream[(size_t)(d - 1) * N + i] != 0;
             int s = L.src(i, d);
-            if (phys && st && L.fluid[s] != 1) st = false;
+            if (phys) {
+                /* physics: a link is a wall link when the reference's stream
+                 * flag is cleared by a non-periodic BC link, or when x - c_d is
+                 * solid or outside a non-periodic domain */
+                const int od = L.opp(d);
+                const int b = L.dims == 2 ? 2 : 3;
+                const uint64_t lt = (L.mask[i] >> ((od - 1) * b)) & (L.dims == 2 ? 3ull : 7ull);
+                const bool periodic_link = !st && lt == 4;
+                if (periodic_link) st = true;
+                const int cx = L.dims == 2 ? cx2[d] : cx3[d], cy = L.dims == 2 ? cy2[d] : cy3[d];
+                const int cz = L.dims == 2 ? 0 : cz3[d];
+                const int sx = L.X(i) - cx, sy = L.Y(i) - cy, sz = L.Z(i) - cz;
+                if (!periodic_link && ((!L.p.periodic[0] && (sx < 0 || sx >= L.n)) ||
+                                       (!L.p.periodic[1] && (sy < 0 || sy >= L.m)) ||
+                                       (!L.p.periodic[2] && (sz < 0 || sz >= L.h))))
+                    st = false;
+                if (st && L.fluid[s] != 1) st = false;
+            }
             if (st)
                 L.f[i + (size_t)d * N] = L.fc[s + (size_t)d * N];
             else if (phys) /* half-way bounce-back of the node's own outgoing population */
@@ -453,62 +471,35 @@ void bc_node_2d(Lattice<T> &L, int i, uint64_t mk) {
     T *f = L.f.data();
     auto F = [&](int d) -> T & { return f[i + (size_t)d * N]; };
     if (!(mk & BC2_FLUID)) return;
-    const bool phys = L.p.mode == 1;
-    const T u0 = L.u0[i], v0 = L.v0[i];
+    const T u0 = L.u0[i];
     /* inlet (GpuBoundaries.cu:12-71) */
     if (mk & BC2_INLT_B) {
         bool north = (mk & bc2_mask(2, 2)) && !(mk & BC2_CORNER);
         bool west = (mk & bc2_mask(2, 3)) && !(mk & BC2_CORNER);
         if (north) {
-            if (!phys) {
-                F(4) = F(2);
-                F(8) = F(6) + (F(0) + F(1) + F(3) + 2 * (F(2) + F(6) + F(5))) * u0 / 6.0;
-                F(7) = F(5) - (F(0) + F(1) + F(3) + 2 * (F(2) + F(6) + F(5))) * u0 / 6.0;
-            } else {
-                T r = (F(0) + F(1) + F(3) + 2 * (F(2) + F(5) + F(6))) / (1 + v0);
-                T h13 = (F(1) - F(3)) / 2;
-                F(4) = F(2) - (T)(2. / 3.) * r * v0;
-                F(7) = F(5) + h13 - r * u0 / 2 - r * v0 / 6;
-                F(8) = F(6) - h13 + r * u0 / 2 - r * v0 / 6;
-            }
+            F(4) = F(2);
+            F(8) = F(6) + (F(0) + F(1) + F(3) + 2 * (F(2) + F(6) + F(5))) * u0 / 6.0;
+            F(7) = F(5) - (F(0) + F(1) + F(3) + 2 * (F(2) + F(6) + F(5))) * u0 / 6.0;
         }
         if (west) {
-            if (!phys) {
-                F(1) = F(3) + 2. * ((F(0) + F(2) + F(4) + 2. * (F(3) + F(6) + F(7))) / (1.0 - u0)) * u0 / 3;
-                F(5) = F(7) + ((F(0) + F(2) + F(4) + 2. * (F(3) + F(6) + F(7))) / (1.0 - u0)) * u0 / 6;
-                F(8) = F(6) + ((F(0) + F(2) + F(4) + 2. * (F(3) + F(6) + F(7))) / (1.0 - u0)) * u0 / 6;
-            } else {
-                T r = (F(0) + F(2) + F(4) + 2 * (F(3) + F(6) + F(7))) / (1 - u0);
-                T h24 = (F(2) - F(4)) / 2;
-                F(1) = F(3) + (T)(2. / 3.) * r * u0;
-                F(5) = F(7) - h24 + r * u0 / 6 + r * v0 / 2;
-                F(8) = F(6) + h24 + r * u0 / 6 - r * v0 / 2;
-            }
+            F(1) = F(3) + 2. * ((F(0) + F(2) + F(4) + 2. * (F(3) + F(6) + F(7))) / (1.0 - u0)) * u0 / 3;
+            F(5) = F(7) + ((F(0) + F(2) + F(4) + 2. * (F(3) + F(6) + F(7))) / (1.0 - u0)) * u0 / 6;
+            F(8) = F(6) + ((F(0) + F(2) + F(4) + 2. * (F(3) + F(6) + F(7))) / (1.0 - u0)) * u0 / 6;
         }
     }
     /* straight wall (GpuBoundaries.cu:400-443): f[opp(dir)] = f[dir] after
-     * streaming, in direction order.  Physics mode bounced back in streaming. */
-    if (!phys) {
-        for (int dir = 1; dir < 9; ++dir) {
-            uint64_t all = mk & bc2_mask(3, dir), wall = mk & bc2_mask(1, dir);
-            if (all == wall && wall) F(opp2[dir]) = F(dir);
-        }
+     * streaming, in direction order */
+    for (int dir = 1; dir < 9; ++dir) {
+        uint64_t all = mk & bc2_mask(3, dir), wall = mk & bc2_mask(1, dir);
+        if (all == wall && wall) F(opp2[dir]) = F(dir);
     }
     /* east outlet (GpuBoundaries.cu:1562-1653) */
     if ((mk & bc2_mask(3, 1)) == bc2_mask(3, 1)) {
         switch (L.p.outlet_profile) {
         case 1:
-            if (!phys) {
-                F(3) = F(1) - 2 * ((F(0) + F(2) + F(4) + 2 * (F(1) + F(5) + F(8))) / (1 - u0)) * u0 / 3;
-                F(7) = F(5) - ((F(0) + F(2) + F(4) + 2 * (F(1) + F(5) + F(8))) / (1 - u0)) * u0 / 6;
-                F(6) = F(8) - ((F(0) + F(2) + F(4) + 2 * (F(1) + F(5) + F(8))) / (1 - u0)) * u0 / 6;
-            } else { /* Zou-He velocity outlet, u0 outward-normal */
-                T r = (F(0) + F(2) + F(4) + 2 * (F(1) + F(5) + F(8))) / (1 + u0);
-                T h24 = (F(2) - F(4)) / 2;
-                F(3) = F(1) - (T)(2. / 3.) * r * u0;
-                F(7) = F(5) + h24 - r * u0 / 6 - r * v0 / 2;
-                F(6) = F(8) - h24 - r * u0 / 6 + r * v0 / 2;
-            }
+            F(3) = F(1) - 2 * ((F(0) + F(2) + F(4) + 2 * (F(1) + F(5) + F(8))) / (1 - u0)) * u0 / 3;
+            F(7) = F(5) - ((F(0) + F(2) + F(4) + 2 * (F(1) + F(5) + F(8))) / (1 - u0)) * u0 / 6;
+            F(6) = F(8) - ((F(0) + F(2) + F(4) + 2 * (F(1) + F(5) + F(8))) / (1 - u0)) * u0 / 6;
             break;
         case 2:
             F(1) = 2 * f[i + N - 1] - f[i + N - 2];
@@ -520,15 +511,6 @@ void bc_node_2d(Lattice<T> &L, int i, uint64_t mk) {
             F(5) = f[i - 1 + 5 * N];
             F(8) = f[i - 1 + 8 * N];
             break;
-        case 5: { /* physics: Zou-He pressure outlet at rho_out */
-            T r = (T)L.p.rho_out;
-            T ux = -1 + (F(0) + F(2) + F(4) + 2 * (F(1) + F(5) + F(8))) / r;
-            T h24 = (F(2) - F(4)) / 2;
-            F(3) = F(1) - (T)(2. / 3.) * r * ux;
-            F(7) = F(5) + h24 - r * ux / 6;
-            F(6) = F(8) - h24 - r * ux / 6;
-            break;
-        }
         }
     }
 }
@@ -539,14 +521,14 @@ void bc_node_2d(Lattice<T> &L, int i, uint64_t mk) {
  * corrections, GpuBoundaries.cu:92-394), face order W,E,S,N,B,T.  The
  * reference's west and east densities divide by (1+u) and (1-u), the reverse
  * of the mass balance rho (1 -/+ u) = known sums that its other four faces
- * use; fixed_we selects the mass-balance form (physics mode). */
+ * use; physics mode uses zou_he_face instead. */
 template <class T>
-void zou_he_3d(T *f, size_t N, int i, int face, T uu, T vv, T ww, bool fixed_we = false) {
+void zou_he_3d(T *f, size_t N, int i, int face, T uu, T vv, T ww) {
     auto F = [&](int d) -> T & { return f[i + (size_t)d * N]; };
     T d_, n1, n2;
     switch (face) {
     case 2: /* WEST */
-        d_ = 1.0 / (fixed_we ? 1.0 - uu : 1.0 + uu) * (F(0) + F(3) + F(4) + F(5) + F(6) + F(15) + F(16) + F(17) + F(18) + 2.0 * (F(2) + F(8) + F(10) + F(12) + F(14)));
+        d_ = 1.0 / (1.0 + uu) * (F(0) + F(3) + F(4) + F(5) + F(6) + F(15) + F(16) + F(17) + F(18) + 2.0 * (F(2) + F(8) + F(10) + F(12) + F(14)));
         n1 = 0.5 * (F(3) + F(15) + F(17) - (F(4) + F(16) + F(18))) - 1.0 / 3.0 * d_ * vv;
         n2 = 0.5 * (F(5) + F(15) + F(16) - (F(6) + F(17) + F(18))) - 1.0 / 3.0 * d_ * ww;
         F(1) = F(2) + 1.0 / 3.0 * d_ * uu;
@@ -556,7 +538,7 @@ void zou_he_3d(T *f, size_t N, int i, int face, T uu, T vv, T ww, bool fixed_we 
         F(13) = F(12) + 1.0 / 6.0 * d_ * (uu - ww) + n2;
         break;
     case 1: /* EAST */
-        d_ = 1.0 / (fixed_we ? 1.0 + uu : 1.0 - uu) * (F(0) + F(3) + F(4) + F(5) + F(6) + F(15) + F(16) + F(17) + F(18) + 2.0 * (F(1) + F(7) + F(9) + F(11) + F(13)));
+        d_ = 1.0 / (1.0 - uu) * (F(0) + F(3) + F(4) + F(5) + F(6) + F(15) + F(16) + F(17) + F(18) + 2.0 * (F(1) + F(7) + F(9) + F(11) + F(13)));
         n1 = 0.5 * (F(3) + F(15) + F(17) - (F(4) + F(16) + F(18))) - 1.0 / 3.0 * d_ * vv;
         n2 = 0.5 * (F(5) + F(15) + F(16) - (F(6) + F(17) + F(18))) - 1.0 / 3.0 * d_ * ww;
         F(2) = F(1) - 1.0 / 3.0 * d_ * uu;
@@ -608,22 +590,11 @@ void zou_he_3d(T *f, size_t N, int i, int face, T uu, T vv, T ww, bool fixed_we 
     }
 }
 
-/* Normal velocity a Zou-He pressure face implies at density rho (physics). */
-template <class T>
-T pressure_face_velocity(const T *f, size_t N, int i, int face, T rho) {
-    auto F = [&](int d) { return f[i + (size_t)d * N]; };
-    if (face == 2) /* west, inflow along +x */
-        return 1 - (F(0) + F(3) + F(4) + F(5) + F(6) + F(15) + F(16) + F(17) + F(18) + 2 * (F(2) + F(8) + F(10) + F(12) + F(14))) / rho;
-    /* east, outflow along +x */
-    return -1 + (F(0) + F(3) + F(4) + F(5) + F(6) + F(15) + F(16) + F(17) + F(18) + 2 * (F(1) + F(7) + F(9) + F(11) + F(13))) / rho;
-}
-
 template <class T>
 void bc_node_3d(Lattice<T> &L, int i, uint64_t mk) {
     const size_t N = (size_t)L.N;
     T *f = L.f.data();
     if (!(mk & BC3_FLUID)) return;
-    const bool phys = L.p.mode == 1;
     const T uu = L.u0[i], vv = L.v0[i], ww = L.w0[i];
     /* inlet (GpuBoundaries.cu:73-399) */
     if (mk & BC3_INLT_B) {
@@ -633,36 +604,13 @@ void bc_node_3d(Lattice<T> &L, int i, uint64_t mk) {
             uint64_t inl = bc3_mask(2, face), all = mk & bc3_mask(7, face);
             bool hit = (mk & inl) && !(mk & BC3_CORNER) &&
                        (face == 1 ? all == inl : all == (mk & inl));
-            if (!hit) continue;
-            if (phys && L.p.inlet_profile == 4 && face == 2) {
-                T r = (T)L.p.rho_in;
-                T ux = pressure_face_velocity(f, N, i, 2, r);
-                zou_he_3d(f, N, i, 2, ux, (T)0, (T)0, true);
-            } else {
-                zou_he_3d(f, N, i, face, uu, vv, ww, phys);
-            }
+            if (hit) zou_he_3d(f, N, i, face, uu, vv, ww);
         }
     }
     /* straight simple wall (GpuBoundaries.cu:445-490) */
-    if (!phys) {
-        for (int dir = 1; dir < 19; ++dir) {
-            uint64_t all = mk & bc3_mask(7, dir), wall = mk & bc3_mask(1, dir);
-            if (all == wall && wall) f[i + (size_t)opp3[dir] * N] = f[i + (size_t)dir * N];
-        }
-    }
-    /* physics: Zou-He pressure outlet on an east face */
-    if (phys && L.p.outlet_profile == 5 && (mk & bc3_mask(7, 1)) == bc3_mask(3, 1)) {
-        T r = (T)L.p.rho_out;
-        T ux = pressure_face_velocity(f, N, i, 1, r);
-        /* the east unknowns follow the east velocity face with d = rho_out */
-        auto F = [&](int d) -> T & { return f[i + (size_t)d * N]; };
-        T n1 = 0.5 * (F(3) + F(15) + F(17) - (F(4) + F(16) + F(18)));
-        T n2 = 0.5 * (F(5) + F(15) + F(16) - (F(6) + F(17) + F(18)));
-        F(2) = F(1) - 1.0 / 3.0 * r * ux;
-        F(8) = F(9) - 1.0 / 6.0 * r * ux - n1;
-        F(10) = F(7) - 1.0 / 6.0 * r * ux + n1;
-        F(12) = F(13) - 1.0 / 6.0 * r * ux - n2;
-        F(14) = F(11) - 1.0 / 6.0 * r * ux + n2;
+    for (int dir = 1; dir < 19; ++dir) {
+        uint64_t all = mk & bc3_mask(7, dir), wall = mk & bc3_mask(1, dir);
+        if (all == wall && wall) f[i + (size_t)opp3[dir] * N] = f[i + (size_t)dir * N];
     }
 }
 
@@ -702,6 +650,94 @@ void symm_node_3d(Lattice<T> &L, int i, uint64_t mk) {
     if (is(3)) { F(4) = F(3); F(9) = F(7); F(10) = F(8); F(16) = F(15); F(18) = F(17); }
     if (is(6)) { F(5) = F(6); F(11) = F(13); F(12) = F(14); F(15) = F(17); F(16) = F(18); }
     if (is(5)) { F(6) = F(5); F(13) = F(11); F(14) = F(12); F(17) = F(15); F(18) = F(16); }
+}
+
+
+/* Physics mode: mass-balanced Zou-He face with Hecht-Harting transverse
+ * terms for any lattice face.  face = inward normal: 0 +x (west), 1 -x (east),
+ * 2 +y (south), 3 -y (north), 4 +z (bottom), 5 -z (top).  With e the inward
+ * normal: rho (1 - u.e) = S0 + 2 S- over the c.e = 0 and c.e = -1 populations;
+ * the c.e = +1 unknowns are f_opp + rho (c.u)/3 (axis, D3Q19) or 2 rho (c.u)/3
+ * (axis, D2Q9), and f_opp + rho (u.e)/6 + rho (u.t)/2 - (1/2) sum_{c.e=0}
+ * (c.t) f_c for a diagonal c = e + t. */
+template <class T>
+void zou_he_face(Lattice<T> &L, int i, int face, bool pressure, T rho_set, T ux, T uy, T uz) {
+    const size_t N = (size_t)L.N;
+    T *f = L.f.data();
+    const int q = L.q;
+    const int *cx = q == 9 ? cx2 : cx3, *cy = q == 9 ? cy2 : cy3;
+    static const int zero9[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int *cz = q == 9 ? zero9 : cz3;
+    int e[3] = {0, 0, 0};
+    e[face / 2] = (face % 2 == 0) ? 1 : -1;
+    T s0 = 0, sm = 0;
+    for (int d = 0; d < q; ++d) {
+        const int ce = cx[d] * e[0] + cy[d] * e[1] + cz[d] * e[2];
+        if (ce == 0) s0 += f[i + d * N];
+        else if (ce == -1) sm += f[i + d * N];
+    }
+    T rho, un;
+    T u[3] = {ux, uy, uz};
+    if (pressure) {
+        rho = rho_set;
+        un = 1 - (s0 + 2 * sm) / rho;
+        for (int a = 0; a < 3; ++a) u[a] = un * e[a];
+    } else {
+        un = u[0] * e[0] + u[1] * e[1] + u[2] * e[2];
+        rho = (s0 + 2 * sm) / (1 - un);
+    }
+    for (int d = 1; d < q; ++d) {
+        const int ce = cx[d] * e[0] + cy[d] * e[1] + cz[d] * e[2];
+        if (ce != 1) continue;
+        const int t[3] = {cx[d] - e[0], cy[d] - e[1], cz[d] - e[2]};
+        const int o = L.opp(d);
+        if (!t[0] && !t[1] && !t[2]) {
+            f[i + d * N] = f[i + o * N] + (T)(q == 9 ? 2.0 / 3.0 : 1.0 / 3.0) * rho * un;
+            continue;
+        }
+        T st = 0;
+        for (int c = 0; c < q; ++c) {
+            const int cce = cx[c] * e[0] + cy[c] * e[1] + cz[c] * e[2];
+            const int ct = cx[c] * t[0] + cy[c] * t[1] + cz[c] * t[2];
+            if (cce == 0 && ct) st += (T)ct * f[i + c * N];
+        }
+        const T ut = u[0] * t[0] + u[1] * t[1] + u[2] * t[2];
+        f[i + d * N] = f[i + o * N] + rho * un / 6 + rho * ut / 2 - st / 2;
+    }
+}
+
+/* Physics-mode boundary node: an inlet or outlet node (not a corner) gets a
+ * Zou-He face normal to its first axis link of the node's type. */
+template <class T>
+int phys_face_kind(const Lattice<T> &L, uint64_t mk, int &face, bool &pressure, bool &outlet) {
+    const int q = L.q;
+    const bool d2 = q == 9;
+    const uint64_t corner = d2 ? BC2_CORNER : BC3_CORNER;
+    if (mk & corner) return 0;
+    const uint64_t mt = d2 ? (mk >> 16) & 3ull : (mk >> 54) & 7ull;
+    if (mt != 2 && mt != 3) return 0;
+    face = -1;
+    for (int d = 1; d < q && face < 0; ++d) {
+        const uint64_t t = d2 ? (mk >> ((d - 1) * 2)) & 3ull : (mk >> ((d - 1) * 3)) & 7ull;
+        if (t != mt) continue;
+        const int cxd = d2 ? cx2[d] : cx3[d], cyd = d2 ? cy2[d] : cy3[d], czd = d2 ? 0 : cz3[d];
+        if (cxd == -1 && !cyd && !czd) face = 0;
+        else if (cxd == 1 && !cyd && !czd) face = 1;
+        else if (cyd == -1 && !cxd && !czd) face = 2;
+        else if (cyd == 1 && !cxd && !czd) face = 3;
+        else if (czd == -1 && !cxd && !cyd) face = 4;
+        else if (czd == 1 && !cxd && !cyd) face = 5;
+    }
+    if (face < 0) return 0;
+    outlet = mt == 3;
+    if (!outlet) {
+        pressure = L.p.inlet_profile == 4;
+    } else {
+        if (L.p.outlet_profile == 5) pressure = true;
+        else if (L.p.outlet_profile == 1) pressure = false;
+        else return -1;
+    }
+    return 1;
 }
 
 /* ------------------------------ macro ----------------------------------- */
@@ -785,6 +821,13 @@ int run(int dims, int n, int m, int h, const int *node_type, int nconn, const in
         for (int i : L.bcnodes)
             if ((L.mask[i] & BC3_B_ALL) == BC3_OUTL_B) return ORC_UNSUPPORTED;
     }
+    if (p->mode == 1) {
+        for (int i : L.bcnodes) {
+            int face;
+            bool pr = false, ou = false;
+            if (L.fluid[i] && phys_face_kind(L, L.mask[i], face, pr, ou) < 0) return ORC_UNSUPPORTED;
+        }
+    }
     L.rho.assign(N, (T)p->rho);
     L.u0.assign(N, (T)p->u);
     L.v0.assign(N, (T)p->v);
@@ -810,7 +853,15 @@ int run(int dims, int n, int m, int h, const int *node_type, int nconn, const in
     for (int it = 0; it < steps; ++it) {
         collide_all(L);
         stream_all(L);
-        if (dims == 2) {
+        if (p->mode == 1) {
+            for (int i : L.bcnodes) {
+                int face;
+                bool pressure = false, outlet = false;
+                if (!L.fluid[i] || phys_face_kind(L, L.mask[i], face, pressure, outlet) != 1) continue;
+                const T rset = (T)(outlet ? p->rho_out : p->rho_in);
+                zou_he_face(L, i, face, pressure, rset, L.u0[i], L.v0[i], dims == 3 ? L.w0[i] : (T)0);
+            }
+        } else if (dims == 2) {
             for (int i : L.bcnodes) bc_node_2d(L, i, L.mask[i]);
         } else {
             for (int i : L.bcnodes) bc_node_3d(L, i, L.mask[i]);

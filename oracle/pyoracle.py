@@ -29,7 +29,8 @@ class RefParams(C.Structure):
 
 class OrcParams(C.Structure):
     _fields_ = RefParams._fields_ + [("mode", C.c_int), ("init_kind", C.c_int),
-                                     ("rho_in", C.c_double), ("rho_out", C.c_double)]
+                                     ("rho_in", C.c_double), ("rho_out", C.c_double),
+                                     ("periodic", C.c_int * 3)]
 
 
 def build_oracle(force=False):
@@ -91,7 +92,7 @@ class Result:
 
 
 def run_oracle(lat, steps, fp64=False, mode=0, init_kind=0, rho_in=1.0, rho_out=1.0,
-               extra_collide=False, init=None, **kw):
+               extra_collide=False, init=None, periodic=(0, 0, 0), **kw):
     """Run the oracle restatement; returns a Result with f, fc (q, N), rho,
     u, v, w (N), mask, stream, count, resid, rc."""
     L = oracle_lib()
@@ -99,6 +100,8 @@ def run_oracle(lat, steps, fp64=False, mode=0, init_kind=0, rho_in=1.0, rho_out=
     nn = lat.num_nodes
     p = _params(OrcParams, dict(default_params(**kw), mode=mode, init_kind=init_kind,
                                 rho_in=rho_in, rho_out=rho_out))
+    for a in range(3):
+        p.periodic[a] = int(periodic[a])
     cols = _cols(lat)
     r = Result()
     r.f, r.fc = np.zeros(q * nn), np.zeros(q * nn)

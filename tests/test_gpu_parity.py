@@ -2,8 +2,9 @@
 seeded inputs.
 
 Tolerances (stated per storage type):
-  * F64 storage vs the FP64 oracle: 1e-10 absolute on populations and
-    macroscopic fields (FP64 arithmetic in a different operation order).
+  * F64 storage vs the FP64 oracle: 1e-10 absolute on populations (FP64
+    arithmetic in a different operation order); the macroscopic fields are
+    returned as FP32, so 3e-7 absolute on them.
   * F32 storage vs the FP32 oracle: 2e-5 absolute on populations, density and
     velocity (FP32 with fused multiply-adds and another summation order; the
     oracle follows the reference's expression order without contraction).
@@ -40,7 +41,7 @@ def run_pair(oracle, lat, args, steps, init=None):
                collision_model=args.collision_model, update_inlet_outlet=args.update_inlet_outlet)
     r = oracle.run_oracle(lat, steps, fp64=args.storage == N.STORE_F64, mode=args.mode,
                           init_kind=args.init_equilibrium, rho_in=args.rho_in, rho_out=args.rho_out,
-                          extra_collide=True, init=init, **okw)
+                          extra_collide=True, init=init, periodic=args.periodic, **okw)
     assert r.rc == 0
     g = dict(rho=rho.astype(np.float64), u=u.astype(np.float64), v=v.astype(np.float64),
              w=w.astype(np.float64), f=f)
@@ -58,6 +59,8 @@ def compare(g, r, fluid, storage, dims):
         scale = {k: max(1e-3, float(np.ptp(getattr(r, k)[fluid]))) for k in keys}
         scale["f"] = max(1e-3, float(np.abs(r.fc[:, fluid]).max()))
         bad = {k: v for k, v in errs.items() if v > 2e-3 * scale[k]}
+    elif storage == N.STORE_F64:
+        bad = {k: v for k, v in errs.items() if v > (TOL[storage] if k == "f" else 3e-7)}
     else:
         bad = {k: v for k, v in errs.items() if v > TOL[storage]}
     assert not bad, (bad, errs)

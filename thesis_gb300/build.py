@@ -25,12 +25,21 @@ def nvcc():
     return cand if os.path.exists(cand) else "nvcc"
 
 
+CLI_DIR = os.path.join(CSRC, "cli")
+TOOLS = {"latticegen": "latticegen_main.cpp"}
+
+
 def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
+def tool_path(name):
+    return os.path.join(LIBDIR, name)
+
+
 def _newest_input():
-    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if os.path.isfile(os.path.join(CSRC, f))]
+    files += [os.path.join(CLI_DIR, f) for f in os.listdir(CLI_DIR)]
     files.append(os.path.join(ROOT, "include", "thesis_lbm.h"))
     files.append(os.path.abspath(__file__))
     return max(os.path.getmtime(f) for f in files)
@@ -45,7 +54,9 @@ def _run(cmd):
 
 def build(force=False, verbose=False):
     """Compile the library if needed; return its path."""
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= _newest_input():
+    newest = _newest_input()
+    if not force and all(os.path.exists(p) and os.path.getmtime(p) >= newest
+                         for p in [LIB_PATH] + [tool_path(t) for t in TOOLS]):
         return LIB_PATH
     os.makedirs(OBJDIR, exist_ok=True)
     common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
@@ -67,6 +78,11 @@ def build(force=False, verbose=False):
     tmp = LIB_PATH + ".tmp"
     _run([nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart"])
     os.replace(tmp, LIB_PATH)
+    for name, src in TOOLS.items():
+        out = tool_path(name)
+        _run(["g++", "-O2", "-std=c++17", os.path.join(CLI_DIR, src), "-o", out + ".tmp",
+              "-L" + LIBDIR, "-lthesis_lbm", "-Wl,-rpath,$ORIGIN"])
+        os.replace(out + ".tmp", out)
     return LIB_PATH
 
 

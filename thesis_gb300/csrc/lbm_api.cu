@@ -51,7 +51,7 @@ struct lbm_handle_s {
     int32_t *slot = nullptr;
     unsigned long long *mask = nullptr;
     int32_t *kind = nullptr;
-    float *uvw = nullptr;
+    double *uvw = nullptr;
     float *rho = nullptr, *ux = nullptr, *uy = nullptr, *uz = nullptr;
     float *pux = nullptr, *puy = nullptr, *puz = nullptr;
     double *partial = nullptr, *norms = nullptr;
@@ -62,7 +62,8 @@ struct lbm_handle_s {
     cudaGraphExec_t pair[2] = {nullptr, nullptr};
     int status = LBM_OK;
     bool initialised = false;
-    float omega = 1, omega_m = 1, gshift = 0, scale = 1024.f;
+    double omega = 1, omega_m = 1, gshift = 0;
+    float scale = 1024.f;
 };
 
 static StepParams make_params(const lbm_handle_s *H, int from, int write_macro) {
@@ -88,8 +89,8 @@ static StepParams make_params(const lbm_handle_s *H, int from, int write_macro) 
     p.omega = H->omega;
     p.omega_m = H->omega_m;
     p.gshift = H->gshift;
-    p.rho_in = (float)H->P.rho_in;
-    p.rho_out = (float)H->P.rho_out;
+    p.rho_in = H->P.rho_in;
+    p.rho_out = H->P.rho_out;
     p.scale = H->scale;
     p.inv_scale = 1.0f / H->scale;
     p.outlet_profile = H->P.outlet_profile;
@@ -161,9 +162,9 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     H->elem = P->storage == LBM_STORE_F32 ? 4 : (P->storage == LBM_STORE_F16S ? 2 : 8);
     H->scale = P->f16_scale > 0 ? (float)P->f16_scale : 1024.0f;
     // omega as the reference computes it (GpuInit.cu:102-103)
-    H->omega = (float)(1.0 / (3.0 * P->viscosity + 0.5));
-    H->omega_m = (float)(8.0 * (2.0 - H->omega) / (8.0 - H->omega));
-    H->gshift = L->dims == 3 ? (float)(P->g / H->omega) : 0.0f;
+    H->omega = 1.0 / (3.0 * P->viscosity + 0.5);
+    H->omega_m = 8.0 * (2.0 - H->omega) / (8.0 - H->omega);
+    H->gshift = L->dims == 3 ? P->g / H->omega : 0.0;
     long long fl = 0;
     for (long long i = 0; i < N; ++i) fl += (L->node_type[i] & 1);
     H->fluid = fl;
@@ -185,7 +186,7 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     ALLOC(H->slot, sizeof(int32_t) * N);
     ALLOC(H->mask, sizeof(unsigned long long) * H->nslots);
     ALLOC(H->kind, sizeof(int32_t) * H->nslots);
-    ALLOC(H->uvw, sizeof(float) * 3 * H->nslots);
+    ALLOC(H->uvw, sizeof(double) * 3 * H->nslots);
     ALLOC(H->rho, sizeof(float) * N);
     ALLOC(H->ux, sizeof(float) * N);
     ALLOC(H->uy, sizeof(float) * N);
@@ -204,14 +205,14 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
         e = cudaMemcpy(H->mask, mk.data(), sizeof(unsigned long long) * H->nslots, cudaMemcpyHostToDevice);
         if (e == cudaSuccess)
             e = cudaMemcpy(H->kind, flags.kind.data(), sizeof(int32_t) * H->nslots, cudaMemcpyHostToDevice);
-        std::vector<float> uvw((size_t)3 * H->nslots);
+        std::vector<double> uvw((size_t)3 * H->nslots);
         for (int s = 0; s < H->nslots; ++s) {
-            uvw[3 * s] = (float)P->u;
-            uvw[3 * s + 1] = (float)P->v;
-            uvw[3 * s + 2] = (float)P->w;
+            uvw[3 * s] = P->u;
+            uvw[3 * s + 1] = P->v;
+            uvw[3 * s + 2] = P->w;
         }
         if (e == cudaSuccess)
-            e = cudaMemcpy(H->uvw, uvw.data(), sizeof(float) * 3 * H->nslots, cudaMemcpyHostToDevice);
+            e = cudaMemcpy(H->uvw, uvw.data(), sizeof(double) * 3 * H->nslots, cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) e = cudaMemset(H->pux, 0, sizeof(float) * N);
     if (e == cudaSuccess) e = cudaMemset(H->puy, 0, sizeof(float) * N);
@@ -227,14 +228,14 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
 int lbm_set_inlet_velocity(lbm_handle H, const float *u, const float *v, const float *w) {
     if (!H) return fail(LBM_ERR_INVALID, "null handle");
     if (!H->nslots) return LBM_OK;
-    std::vector<float> uvw((size_t)3 * H->nslots);
+    std::vector<double> uvw((size_t)3 * H->nslots);
     for (int s = 0; s < H->nslots; ++s) {
         const long long node = H->slot_node[s];
-        uvw[3 * s] = u ? u[node] : (float)H->P.u;
-        uvw[3 * s + 1] = v ? v[node] : (float)H->P.v;
-        uvw[3 * s + 2] = w ? w[node] : (float)H->P.w;
+        uvw[3 * s] = u ? (double)u[node] : H->P.u;
+        uvw[3 * s + 1] = v ? (double)v[node] : H->P.v;
+        uvw[3 * s + 2] = w ? (double)w[node] : H->P.w;
     }
-    CUDA_TRY(cudaMemcpyAsync(H->uvw, uvw.data(), sizeof(float) * 3 * H->nslots, cudaMemcpyHostToDevice, H->stream));
+    CUDA_TRY(cudaMemcpyAsync(H->uvw, uvw.data(), sizeof(double) * 3 * H->nslots, cudaMemcpyHostToDevice, H->stream));
     CUDA_TRY(cudaStreamSynchronize(H->stream));
     return LBM_OK;
 }
@@ -260,8 +261,13 @@ int lbm_init(lbm_handle H, const float *rho, const float *u, const float *v, con
     CUDA_TRY(cudaMemsetAsync(H->pux, 0, sizeof(float) * H->N, H->stream));
     CUDA_TRY(cudaMemsetAsync(H->puy, 0, sizeof(float) * H->N, H->stream));
     CUDA_TRY(cudaMemsetAsync(H->puz, 0, sizeof(float) * H->N, H->stream));
-    const StepParams p = make_params(H, 1, 0);  // fout = buffer 0
+    StepParams p = make_params(H, 1, 0);  // fout = buffer 0
     const StepParams o = make_params(H, 0, 0);  // fout = buffer 1
+    p.init_rho = H->P.rho;
+    p.init_ux = H->P.u;
+    p.init_uy = H->P.v;
+    p.init_uz = H->dims == 3 ? H->P.w : 0.0;
+    p.init_from_arrays = (rho ? 1 : 0) | (u ? 2 : 0) | (v ? 4 : 0) | (w ? 8 : 0);
     const int phys = H->P.mode == LBM_MODE_PHYSICS;
     rc = H->q == 9 ? launch_init_q9(p, o, H->P.collision_model, H->P.storage, phys, H->P.init_equilibrium, H->stream)
                    : launch_init_q19(p, o, H->P.collision_model, H->P.storage, phys, H->P.init_equilibrium, H->stream);

@@ -28,15 +28,19 @@ struct StepParams {
     const int32_t *slot;
     const unsigned long long *bc_mask;
     const int32_t *bc_kind;
-    const float *bc_uvw;
+    const double *bc_uvw;
     float *rho, *ux, *uy, *uz;
     int nx, ny, nz;
     int write_macro;
-    float omega, omega_m, gshift;
-    float rho_in, rho_out;
+    double omega, omega_m, gshift;
+    double rho_in, rho_out;
     float scale, inv_scale;
     int outlet_profile;
     int update_inlet_outlet;
+    // initial state (init kernel only): constants for the fields not given as
+    // arrays (bit 0 rho, 1 ux, 2 uy, 3 uz set = read the array)
+    double init_rho, init_ux, init_uy, init_uz;
+    int init_from_arrays;
 };
 
 constexpr int STEP_BLOCK = 128;
@@ -65,18 +69,30 @@ __global__ void __launch_bounds__(STEP_BLOCK) step_kernel(const StepParams p) {
     using R = typename S::R;
     using L = Lat<Q>;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= p.nx) return;
     const int y = blockIdx.y, z = blockIdx.z;
+    const bool in_row = x < p.nx;
     const int node = x + p.nx * (y + p.ny * z);
-    const uint32_t w = __ldg(p.word + node);
-    if (!(w & W_FLUID)) return;
+    const uint32_t w = in_row ? __ldg(p.word + node) : 0u;
+    const bool fluid = (w & W_FLUID) != 0;
+    // Solid lanes of a warp that also holds fluid nodes store the zero
+    // encoding, so the warp's stores cover whole 32-byte sectors instead of
+    // forcing a read-modify-write of partly written ones in L2/DRAM.
+    const unsigned warp_fluid = __ballot_sync(0xffffffffu, fluid);
+    if (!fluid) {
+        if (in_row && warp_fluid) {
+#pragma unroll
+            for (int d = 0; d < Q; ++d) ((T *)p.fout[d])[node] = S::encode((R)0, L::w(d), p.scale);
+        }
+        return;
+    }
 
-    // Neighbour coordinates wrap periodically; links that must not wrap are
-    // blocked in the flag word, so a wrapped address is only read where the
-    // lattice is periodic.
-    const int xm = x == 0 ? p.nx - 1 : x - 1, xp = x == p.nx - 1 ? 0 : x + 1;
-    const int ym = y == 0 ? p.ny - 1 : y - 1, yp = y == p.ny - 1 ? 0 : y + 1;
-    const int zm = z == 0 ? p.nz - 1 : z - 1, zp = z == p.nz - 1 ? 0 : z + 1;
+    // Pull offsets to the six face neighbours; coordinates wrap periodically
+    // and links that must not wrap are blocked in the flag word, so a wrapped
+    // address is only read where the lattice is periodic.
+    const int plane = p.nx * p.ny;
+    const int oxm = x == 0 ? p.nx - 1 : -1, oxp = x == p.nx - 1 ? 1 - p.nx : 1;
+    const int oym = y == 0 ? (p.ny - 1) * p.nx : -p.nx, oyp = y == p.ny - 1 ? (1 - p.ny) * p.nx : p.nx;
+    const int ozm = z == 0 ? (p.nz - 1) * plane : -plane, ozp = z == p.nz - 1 ? (1 - p.nz) * plane : plane;
 
     R f[Q];
 #pragma unroll
@@ -85,10 +101,9 @@ __global__ void __launch_bounds__(STEP_BLOCK) step_kernel(const StepParams p) {
             f[0] = S::load((const T *)p.fin[0] + node, L::w(0), p.inv_scale);
             continue;
         }
-        const int sx = L::cx(d) == 1 ? xm : (L::cx(d) == -1 ? xp : x);
-        const int sy = L::cy(d) == 1 ? ym : (L::cy(d) == -1 ? yp : y);
-        const int sz = L::cz(d) == 1 ? zm : (L::cz(d) == -1 ? zp : z);
-        const int src = sx + p.nx * (sy + p.ny * sz);
+        const int src = node + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
+                        (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
+                        (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
         const bool blocked = (w >> d) & 1u;
         const T *base = (const T *)p.fin[(blocked && PHYS) ? L::opp(d) : d];
         f[d] = S::load(base + (blocked ? node : src), L::w(d), p.inv_scale);
@@ -179,7 +194,11 @@ __global__ void __launch_bounds__(STEP_BLOCK) init_kernel(const StepParams p, co
         }
         return;
     }
-    const R rho = (R)p.rho[node], ux = (R)p.ux[node], uy = (R)p.uy[node], uz = (R)p.uz[node];
+    const int m = p.init_from_arrays;
+    const R rho = (m & 1) ? (R)p.rho[node] : (R)p.init_rho;
+    const R ux = (m & 2) ? (R)p.ux[node] : (R)p.init_ux;
+    const R uy = (m & 4) ? (R)p.uy[node] : (R)p.init_uy;
+    const R uz = (m & 8) ? (R)p.uz[node] : (R)p.init_uz;
     R f[Q];
     const R usq15 = (R)1.5 * (ux * ux + uy * uy + uz * uz);
 #pragma unroll

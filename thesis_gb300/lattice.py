@@ -266,3 +266,51 @@ def from_files(node_path, bc_path):
         fluid = nodes[:, 4]
         bc = np.stack([bcs[:, 0], bcs[:, 1], np.zeros(len(bcs)), bcs[:, 2], bcs[:, 3], bcs[:, 6]], 1)
     return Lattice(dims, n, m, h, fluid.astype(np.int32), bc.astype(np.int32))
+
+
+def write_starcd(prefix, vertices, faces):
+    """Write STAR-CD geometry in the generator's input layout: `<prefix>.vrt`
+    lines `id x y z` and `<prefix>.bnd` lines `id p1 p2 p3 p4 bcid 0 TYPE`
+    with TYPE one of WALL, INLE, OUTL, CYCL, SYMP (GeomRead.cpp:40-99)."""
+    with open(prefix + ".vrt", "w") as f:
+        for i, (x, y, z) in enumerate(vertices, 1):
+            f.write("%9d      %+.9e%+.9e%+.9e\n" % (i, x, y, z))
+    with open(prefix + ".bnd", "w") as f:
+        for i, (pts, bcid, kind) in enumerate(faces, 1):
+            f.write("%8d %14d %8d %8d %8d %6d %6d      %s\n" % (i, pts[0], pts[1], pts[2], pts[3], bcid, 0, kind))
+
+
+def box_geometry(lo, hi, kinds, first_vertex=1, first_bcid=1):
+    """Vertices and faces of an axis-aligned box.  kinds: dict face -> TYPE
+    for faces 'x-','x+','y-','y+','z-','z+'."""
+    (x0, y0, z0), (x1, y1, z1) = lo, hi
+    v = [(x0, y0, z0), (x1, y0, z0), (x1, y1, z0), (x0, y1, z0),
+         (x0, y0, z1), (x1, y0, z1), (x1, y1, z1), (x0, y1, z1)]
+    b = first_vertex
+    quads = {"z-": (0, 1, 2, 3), "z+": (4, 5, 6, 7), "y-": (0, 1, 5, 4),
+             "y+": (3, 2, 6, 7), "x-": (0, 3, 7, 4), "x+": (1, 2, 6, 5)}
+    faces = []
+    for k, name in enumerate(("x-", "x+", "y-", "y+", "z-", "z+")):
+        q = quads[name]
+        faces.append(((b + q[0], b + q[1], b + q[2], b + q[3]), first_bcid + k, kinds.get(name, "WALL")))
+    return v, faces
+
+
+def generate(vrt, bnd, n, seed, complexity=1, out_prefix="lattice"):
+    """Run the library's lattice generator (bit-identical to the reference
+    latticegen); returns (node path, bc path, (n, m, h))."""
+    import ctypes as C
+    from . import native as N
+    L = N.lib()
+    fn = L.lbm_latticegen
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
+                   C.c_char_p, C.c_char_p, C.POINTER(C.c_int)]
+    dims = (C.c_int * 3)()
+    node, bc = out_prefix + "_Node.dat", out_prefix + "_BC.dat"
+    rc = fn(vrt.encode(), bnd.encode(), int(n), float(seed[0]), float(seed[1]), float(seed[2]),
+            int(complexity), node.encode(), bc.encode(), dims)
+    if rc != 0:
+        L.lbm_latticegen_error.restype = C.c_char_p
+        raise N.LbmError(rc, L.lbm_latticegen_error().decode())
+    return node, bc, tuple(dims)
