@@ -145,6 +145,26 @@ int lbm_get_populations(lbm_handle h, double *f);
 #define LBM_NORMS 5
 int lbm_macro_norms(lbm_handle h, double *out);
 
+/* The same FP64 norms as lbm_macro_norms, for callers that must not allocate
+ * device memory while they run (for example a host framework that owns a
+ * fixed device arena and forbids cudaMalloc/cudaFree inside its step
+ * callback, where allocation would synchronise the device or could fail).
+ * This function has no counterpart in the reference.  All pointers are
+ * device pointers the caller owns: the flag words and macroscopic fields of
+ * n nodes, the previous-velocity arrays (read, then overwritten with u, v, w)
+ * and `out`, LBM_NORMS doubles.  It allocates nothing: its per-block partial
+ * sums live in a static device array (160 KiB per device context, kept until
+ * the process exits), so n is limited to lbm_noalloc_max_nodes() (67,108,864)
+ * and larger calls return LBM_ERR_INVALID.  Calls share that array, so calls
+ * that overlap on the GPU race and must be serialised.  The first call on a
+ * device looks up the array's address; make it before any stream capture.
+ * Work is queued on `stream` (a cudaStream_t, NULL = legacy default). */
+int lbm_fluid_norms_noalloc(const uint32_t *word, const float *rho, const float *u, const float *v,
+                            const float *w, float *u_prev, float *v_prev, float *w_prev, long long n,
+                            double *out, void *stream);
+long long lbm_noalloc_max_nodes(void);
+const char *lbm_noalloc_last_error(void);
+
 /* Sticky status of the handle (LBM_OK, LBM_DIVERGED, LBM_ERR_CUDA). */
 int lbm_status(lbm_handle h);
 
