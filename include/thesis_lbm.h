@@ -171,6 +171,11 @@ int lbm_status(lbm_handle h);
 /* Number of fluid nodes (the lattice updates one step performs). */
 long long lbm_fluid_nodes(lbm_handle h);
 
+/* Nodes one thread of the step kernel advances: 2 for the pair kernel (even
+ * n, F32/F16S storage), 1 otherwise (or when THESIS_LBM_KERNEL=scalar is set
+ * in the environment at lbm_create). */
+int lbm_kernel_variant(lbm_handle h);
+
 /* Bytes of HBM one step moves per fluid node for the populations alone. */
 int lbm_bytes_per_update(lbm_handle h);
 
@@ -198,6 +203,51 @@ int lbm_latticegen(const char *vrt_path, const char *bnd_path, int n_x, double x
                    double zseed, int complexity, const char *node_path, const char *bc_path,
                    int *out_dims);
 const char *lbm_latticegen_error(void);
+
+/* ---- Colour-gradient two-phase D2Q9 on a periodic lattice ----------------
+ * The reference's multiphase 2D step (Iterate.cu:393-491): colour gradient
+ * of (rho_r - rho_b)/rho over the 3x3 stencil or, with high_order, the
+ * 24-point stencil (GpuCollision.cu:112-281), one BGK collision with the
+ * harmonic-mean viscosity, phase-dependent rest weights, surface-tension
+ * perturbation and recolouring (gpuCollBgkwGC2D, gpuCollEnhancedBgkwGC2D,
+ * GpuCollision.cu:552-707), streaming of both colours (gpuStreaming2DCG,
+ * GpuStream.cu:30-158) and the colour densities (gpuUpdateMacro2DCG,
+ * GpuUpdateMacro.cu:43-135).  Both axes wrap periodically. */
+typedef struct lbm_cg_handle_s *lbm_cg_handle;
+
+typedef struct lbm_cg_params {
+    double r_alpha, b_alpha;         /* rest-weight parameters of each colour */
+    double r_viscosity, b_viscosity; /* kinematic viscosities */
+    double beta;                     /* recolouring strength */
+    double A;                        /* surface-tension perturbation amplitude */
+    double g_limit;                  /* |colour gradient| above which a node is interface */
+    double control_param;            /* |phi| threshold of the Laplace-law sums */
+    int high_order;                  /* 1: 24-point gradient stencil */
+    int enhanced;                    /* 1: enhanced equilibrium (GpuCollision.cu:630-707) */
+    int storage;                     /* LBM_STORE_F32 */
+} lbm_cg_params;
+
+/* n x m periodic lattice, n, m >= 5. */
+int lbm_cg_create(int n, int m, const lbm_cg_params *params, lbm_cg_handle *out);
+/* Post-streaming red and blue populations, host arrays of 9*n*m floats in
+ * SoA order f[d*n*m + x + n*y]; performs the first collision. */
+int lbm_cg_init(lbm_cg_handle h, const float *r_f, const float *b_f);
+/* nsteps of stream + densities + collide on `stream` (NULL = own stream);
+ * write_macro_last stores rho, u, v on the last step. */
+int lbm_cg_step(lbm_cg_handle h, int nsteps, int write_macro_last, void *stream);
+/* Colour densities of the last step and the velocity of the last step that
+ * stored it, host arrays of n*m (any may be NULL). */
+int lbm_cg_get_macro(lbm_cg_handle h, float *r_rho, float *b_rho, float *u, float *v);
+/* Post-collision red and blue populations, 9*n*m floats each. */
+int lbm_cg_get_populations(lbm_cg_handle h, float *r_f, float *b_f);
+/* FP64 Laplace-law sums (Iterate.cu:496-499): out[0] = sum rho_r where
+ * phi >= control_param, out[1] = their count, out[2] = sum rho_b where
+ * phi <= -control_param, out[3] = their count, out[4] = max |u|.
+ * Returns LBM_DIVERGED when a sum is not finite. */
+int lbm_cg_laplace(lbm_cg_handle h, double *out);
+long long lbm_cg_nodes(lbm_cg_handle h);
+const char *lbm_cg_last_error(void);
+void lbm_cg_destroy(lbm_cg_handle h);
 
 /* Library version, for load checks. */
 int lbm_version(void);

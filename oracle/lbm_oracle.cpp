@@ -41,6 +41,7 @@
  * INLET_PROF 3D profile the reference itself refuses (Iterate3D.cu:200-206).
  */
 #include <math.h>
+#include <cmath>
 #include <stdint.h>
 #include <string.h>
 
@@ -939,3 +940,245 @@ int orc_run(int fp64, int dims, int n, int m, int h, const int *node_type, int n
 }
 
 }  // extern "C"
+
+/* =====================================================================
+ * Colour-gradient two-phase D2Q9 (restated from GpuCollision.cu:112-707,
+ * GpuStream.cu:30-158, GpuUpdateMacro.cu:43-135, constants GpuInit.cu:144-203).
+ *
+ * One step, as the reference orders it (Iterate.cu:393-491):
+ *   collide: colour gradient of phi = (rho_r - rho_b)/rho from the 3x3
+ *     (cg_w = 4/12, 1/12) or 24-point (weights /5040) stencil, one BGK with
+ *     omega_eff from the harmonic mean viscosity, phase-dependent rest weights
+ *     phi_k + theta_k alpha_mean, perturbation A|g|(w_k (c.g)^2/|g|^2 - B_k)
+ *     and recolouring +/- beta rho_r rho_b/rho cos(phi_k)(phi_k + theta_k alpha);
+ *   stream both colours; macroscopic densities, f = r + b, u.
+ * The lattice is periodic by index wrap in both axes (the reference copies
+ * across a one-node overlap and uses one-sided gradients on its edges; its
+ * interior formulas are what this follows).  Test infrastructure only.
+ * ===================================================================== */
+extern "C" {
+typedef struct {
+    double r_density, b_density, r_alpha, b_alpha, r_viscosity, b_viscosity;
+    double beta, A, g_limit, control_param, g;
+    int high_order, enhanced, external_force;
+} orc_cg_params;
+}
+
+namespace {
+
+const double CG_PHI[9] = {0.0, 0.2, 0.2, 0.2, 0.2, 0.05, 0.05, 0.05, 0.05};
+const double CG_TETA[9] = {1.0, -0.2, -0.2, -0.2, -0.2, -0.05, -0.05, -0.05, -0.05};
+const double CG_CHI[9] = {-8.0 / 3.0, -1.0 / 6.0, -1.0 / 6.0, -1.0 / 6.0, -1.0 / 6.0, 1.0 / 12.0, 1.0 / 12.0, 1.0 / 12.0, 1.0 / 12.0};
+const double CG_PSI[9] = {0.0, 0.5, 0.5, 0.5, 0.5, 0.125, 0.125, 0.125, 0.125};
+const double CG_WPERT[9] = {-4.0 / 27.0, 2.0 / 27.0, 2.0 / 27.0, 2.0 / 27.0, 2.0 / 27.0, 5.0 / 108.0, 5.0 / 108.0, 5.0 / 108.0, 5.0 / 108.0};
+const double CG_W[9] = {0., 4. / 12., 4. / 12., 4. / 12., 4. / 12., 1. / 12., 1. / 12., 1. / 12., 1. / 12.};
+const int HO_CX[25] = {0, 1, 0, -1, 0, 1, -1, -1, 1, 0, 1, 2, 2, 2, 2, 2, 1, 0, -1, -2, -2, -2, -2, -2, -1};
+const int HO_CY[25] = {0, 0, 1, 0, -1, 1, 1, -1, -1, 2, 2, 2, 1, 0, -1, -2, -2, -2, -2, -2, -1, 0, 1, 2, 2};
+const double HO_W[25] = {0., 960., 960., 960., 960., 448., 448., 448., 448., 84., 32., 1., 32., 84., 32., 1., 32., 84., 32., 1., 32., 84., 32., 1., 32.};
+
+template <class T>
+struct CgState {
+    int n, m, N;
+    orc_cg_params p;
+    std::vector<T> rf, bf, rfc, bfc, rr, br, rho, u, v;
+    int wrap(int x, int y) const { return ((x % n + n) % n) + n * ((y % m + m) % m); }
+};
+
+template <class T>
+void cg_macro(CgState<T> &S) {
+    const size_t N = (size_t)S.N;
+    for (int i = 0; i < S.N; ++i) {
+        T r = 0, b = 0, ju = 0, jv = 0;
+        for (int d = 0; d < 9; ++d) {
+            const T fd = S.rf[i + d * N] + S.bf[i + d * N];
+            r += S.rf[i + d * N];
+            b += S.bf[i + d * N];
+            ju += (T)cx2[d] * fd;
+            jv += (T)cy2[d] * fd;
+        }
+        const T rho = r + b;
+        S.rr[i] = r;
+        S.br[i] = b;
+        S.rho[i] = rho;
+        S.u[i] = ju / rho;
+        S.v[i] = jv / rho;
+    }
+}
+
+template <class T>
+void cg_collide(CgState<T> &S) {
+    const size_t N = (size_t)S.N;
+    const orc_cg_params &p = S.p;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < S.N; ++i) {
+        const int x = i % S.n, y = i / S.n;
+        T cgx = 0, cgy = 0, grx = 0, gry = 0;
+        if (p.high_order) {
+            for (int k = 1; k < 25; ++k) {
+                const int j = S.wrap(x + HO_CX[k], y + HO_CY[k]);
+                const T w = (T)(HO_W[k] / 5040.0);
+                const T a1 = w * (S.rr[j] - S.br[j]) / S.rho[j], a2 = w * S.rho[j];
+                grx += a2 * (T)HO_CX[k];
+                gry += a2 * (T)HO_CY[k];
+                cgx += a1 * (T)HO_CX[k];
+                cgy += a1 * (T)HO_CY[k];
+            }
+        } else {
+            for (int k = 1; k < 9; ++k) {
+                const int j = S.wrap(x + cx2[k], y + cy2[k]);
+                const T a1 = (T)CG_W[k] * (S.rr[j] - S.br[j]) / S.rho[j], a2 = (T)CG_W[k] * S.rho[j];
+                grx += a2 * (T)cx2[k];
+                gry += a2 * (T)cy2[k];
+                cgx += a1 * (T)cx2[k];
+                cgy += a1 * (T)cy2[k];
+            }
+        }
+        const T r_r = S.rr[i], b_r = S.br[i], r = S.rho[i], u = S.u[i], v = S.v[i];
+        const T mean_nu = (T)1.0 / (r_r / (r * (T)p.r_viscosity) + b_r / (r * (T)p.b_viscosity));
+        const T omega_eff = (T)1.0 / ((T)3.0 * mean_nu + (T)0.5);
+        const T mean_alpha = (T)p.r_alpha * r_r / r + (T)p.b_alpha * b_r / r;
+        const T gnorm = std::sqrt(cgx * cgx + cgy * cgy);
+        const T k_r = r_r / r, k_b = b_r / r, k_k = (T)p.beta * r_r * b_r / r;
+        const T cu1 = u * u + v * v;
+        const T G1 = (T)2.0 * u * grx, G2 = u * gry + v * grx, G4 = (T)2.0 * v * gry;
+        const T ugr = u * grx + v * gry;
+        for (int k = 0; k < 9; ++k) {
+            T pert = 0, cosin = 0;
+            if (gnorm > (T)p.g_limit) {
+                const T pcg = (T)cx2[k] * cgx + (T)cy2[k] * cgy;
+                const T cn = k == 0 ? (T)0 : (k <= 4 ? (T)1 : (T)std::sqrt(2.0));
+                cosin = k != 0 ? pcg / (gnorm * cn) : (T)0;
+                const T wk = k == 0 ? (T)(4. / 9.) : (k <= 4 ? (T)(1. / 9.) : (T)(1. / 36.));
+                pert = (T)p.A * gnorm * (wk * (pcg * pcg) / (gnorm * gnorm) - (T)CG_WPERT[k]);
+            }
+            const T wk = k == 0 ? (T)(4. / 9.) : (k <= 4 ? (T)(1. / 9.) : (T)(1. / 36.));
+            const T cu2 = u * (T)cx2[k] + v * (T)cy2[k];
+            const T rest = (T)CG_PHI[k] + (T)CG_TETA[k] * mean_alpha;
+            T feq = r * (rest + wk * ((T)3. * cu2 + (T)4.5 * cu2 * cu2 - (T)1.5 * cu1));
+            if (p.enhanced) {
+                const T TC = G1 * (T)(cx2[k] * cx2[k]) + (T)2 * G2 * (T)(cx2[k] * cy2[k]) + G4 * (T)(cy2[k] * cy2[k]);
+                feq += mean_nu * ((T)CG_CHI[k] * ugr + (T)CG_PSI[k] * TC);
+            }
+            const T fk = S.rf[i + k * N] + S.bf[i + k * N];
+            const T fp = omega_eff * feq + ((T)1 - omega_eff) * fk + pert;
+            S.rfc[i + k * N] = k_r * fp + k_k * cosin * rest;
+            S.bfc[i + k * N] = k_b * fp - k_k * cosin * rest;
+        }
+    }
+}
+
+template <class T>
+void cg_stream(CgState<T> &S) {
+    const size_t N = (size_t)S.N;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < S.N; ++i) {
+        const int x = i % S.n, y = i / S.n;
+        for (int d = 0; d < 9; ++d) {
+            const int j = S.wrap(x - cx2[d], y - cy2[d]);
+            S.rf[i + d * N] = S.rfc[j + d * N];
+            S.bf[i + d * N] = S.bfc[j + d * N];
+        }
+    }
+}
+
+template <class T>
+int run_cg(int n, int m, const orc_cg_params *p, const double *r0, const double *b0, int steps,
+           int extra_collide, double *out_rf, double *out_bf, double *out_rfc, double *out_bfc,
+           double *out_rr, double *out_br, double *out_u, double *out_v, double *out_laplace) {
+    CgState<T> S;
+    S.n = n;
+    S.m = m;
+    S.N = n * m;
+    S.p = *p;
+    const size_t Q = 9 * (size_t)S.N;
+    S.rf.assign(r0, r0 + Q);
+    S.bf.assign(b0, b0 + Q);
+    S.rfc.assign(Q, (T)0);
+    S.bfc.assign(Q, (T)0);
+    S.rr.assign(S.N, 0);
+    S.br.assign(S.N, 0);
+    S.rho.assign(S.N, 0);
+    S.u.assign(S.N, 0);
+    S.v.assign(S.N, 0);
+    cg_macro(S);
+    for (int it = 0; it < steps; ++it) {
+        cg_collide(S);
+        cg_stream(S);
+        cg_macro(S);
+    }
+    if (extra_collide) cg_collide(S);
+    for (size_t k = 0; k < Q; ++k) {
+        if (out_rf) out_rf[k] = S.rf[k];
+        if (out_bf) out_bf[k] = S.bf[k];
+        if (out_rfc) out_rfc[k] = S.rfc[k];
+        if (out_bfc) out_bfc[k] = S.bfc[k];
+    }
+    double pin = 0, pout = 0, nin = 0, nout = 0, umax = 0;
+    for (int i = 0; i < S.N; ++i) {
+        if (out_rr) out_rr[i] = S.rr[i];
+        if (out_br) out_br[i] = S.br[i];
+        if (out_u) out_u[i] = S.u[i];
+        if (out_v) out_v[i] = S.v[i];
+        const double chi = ((double)S.rr[i] - (double)S.br[i]) / (double)S.rho[i];
+        if (chi >= p->control_param) { pin += S.rr[i]; nin += 1; }
+        else if (chi <= -p->control_param) { pout += S.br[i]; nout += 1; }
+        const double um = sqrt((double)S.u[i] * S.u[i] + (double)S.v[i] * S.v[i]);
+        if (um > umax) umax = um;
+    }
+    if (out_laplace) {
+        out_laplace[0] = pin;
+        out_laplace[1] = nin;
+        out_laplace[2] = pout;
+        out_laplace[3] = nout;
+        out_laplace[4] = umax;
+    }
+    return ORC_OK;
+}
+
+}  // namespace
+
+extern "C" int orc_run_cg2d(int fp64, int n, int m, const orc_cg_params *p, const double *r0,
+                            const double *b0, int steps, int extra_collide, double *out_rf,
+                            double *out_bf, double *out_rfc, double *out_bfc, double *out_rr,
+                            double *out_br, double *out_u, double *out_v, double *out_laplace) {
+    if (n < 3 || m < 3 || !p || !r0 || !b0) return ORC_BAD_INPUT;
+    if (p->g != 0.0) return ORC_UNSUPPORTED; /* body-force variants not restated */
+    if (fp64)
+        return run_cg<double>(n, m, p, r0, b0, steps, extra_collide, out_rf, out_bf, out_rfc, out_bfc,
+                              out_rr, out_br, out_u, out_v, out_laplace);
+    return run_cg<float>(n, m, p, r0, b0, steps, extra_collide, out_rf, out_bf, out_rfc, out_bfc, out_rr,
+                         out_br, out_u, out_v, out_laplace);
+}
+
+/* One colour-gradient collision from given macroscopic fields and summed
+ * populations (the inputs of gpuCollBgkwGC2D), for pinning against the
+ * reference kernel. */
+extern "C" int orc_cg2d_collide(int fp64, int n, int m, const orc_cg_params *p, const double *rho,
+                                const double *r_rho, const double *b_rho, const double *u,
+                                const double *v, const double *f, double *out_rfc, double *out_bfc) {
+    auto go = [&](auto tag) {
+        using T = decltype(tag);
+        CgState<T> S;
+        S.n = n;
+        S.m = m;
+        S.N = n * m;
+        S.p = *p;
+        const size_t Q = 9 * (size_t)S.N;
+        S.rf.assign(f, f + Q);
+        S.bf.assign(Q, (T)0);
+        S.rfc.assign(Q, (T)0);
+        S.bfc.assign(Q, (T)0);
+        S.rr.assign(r_rho, r_rho + S.N);
+        S.br.assign(b_rho, b_rho + S.N);
+        S.rho.assign(rho, rho + S.N);
+        S.u.assign(u, u + S.N);
+        S.v.assign(v, v + S.N);
+        cg_collide(S);
+        for (size_t k = 0; k < Q; ++k) {
+            out_rfc[k] = S.rfc[k];
+            out_bfc[k] = S.bfc[k];
+        }
+        return ORC_OK;
+    };
+    return fp64 ? go(0.0) : go(0.0f);
+}

@@ -164,3 +164,70 @@ def run_reference(lat, steps, fp64=False, **kw):
     r.count = cnt.value
     r.f, r.fc = r.f.reshape(q, nn), r.fc.reshape(q, nn)
     return r
+
+
+class CgParams(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("r_density", "b_density", "r_alpha", "b_alpha", "r_viscosity",
+                                          "b_viscosity", "beta", "A", "g_limit", "control_param", "g")] + \
+               [(k, C.c_int) for k in ("high_order", "enhanced", "external_force")]
+
+
+def cg_params(**kw):
+    base = dict(r_density=1.0, b_density=1.0, r_alpha=4 / 9, b_alpha=4 / 9, r_viscosity=1 / 6,
+                b_viscosity=1 / 6, beta=0.7, A=0.005, g_limit=0.0, control_param=0.9, g=0.0,
+                high_order=0, enhanced=0, external_force=0)
+    base.update(kw)
+    return _params(CgParams, base)
+
+
+def cg_rest_populations(alpha, density):
+    """Colour populations of a fluid at rest (GpuInit.cu:323-360):
+    density * (alpha, (1-alpha)/5 x4, (1-alpha)/20 x4)."""
+    return density * np.array([alpha] + [(1 - alpha) / 5] * 4 + [(1 - alpha) / 20] * 4)
+
+
+def droplet(n, m, radius, p, centre=None):
+    """Red droplet in blue at rest: per-colour populations (9, N) each."""
+    cx, cy = centre if centre is not None else ((n - 1) / 2, (m - 1) / 2)
+    idx = np.arange(n * m)
+    x, y = idx % n, idx // n
+    inside = (x - cx) ** 2 + (y - cy) ** 2 <= radius ** 2
+    r = np.where(inside[None, :], cg_rest_populations(p.r_alpha, p.r_density)[:, None], 0.0)
+    b = np.where(~inside[None, :], cg_rest_populations(p.b_alpha, p.b_density)[:, None], 0.0)
+    return np.ascontiguousarray(r), np.ascontiguousarray(b)
+
+
+def run_oracle_cg(n, m, p, r0, b0, steps, fp64=False, extra_collide=False):
+    L = oracle_lib()
+    nn = n * m
+    r = Result()
+    r.rf, r.bf, r.rfc, r.bfc = (np.zeros(9 * nn) for _ in range(4))
+    r.rr, r.br, r.u, r.v = (np.zeros(nn) for _ in range(4))
+    r.laplace = np.zeros(5)
+    r0 = np.ascontiguousarray(r0, np.float64).reshape(-1)
+    b0 = np.ascontiguousarray(b0, np.float64).reshape(-1)
+    r.rc = L.orc_run_cg2d(int(fp64), n, m, C.byref(p), _vp(r0), _vp(b0), int(steps), int(extra_collide),
+                          _vp(r.rf), _vp(r.bf), _vp(r.rfc), _vp(r.bfc), _vp(r.rr), _vp(r.br), _vp(r.u),
+                          _vp(r.v), _vp(r.laplace))
+    for k in ("rf", "bf", "rfc", "bfc"):
+        setattr(r, k, getattr(r, k).reshape(9, nn))
+    return r
+
+
+def cg_collide_pair(n, m, p, rho, r_rho, b_rho, u, v, f, fp64=False):
+    """One colour-gradient collision by the oracle and, where oracle/_ref
+    exists, by the reference kernel; returns (oracle (rfc, bfc), reference
+    (rfc, bfc, cg_dir) or None)."""
+    arrs = [np.ascontiguousarray(a, np.float64).reshape(-1) for a in (rho, r_rho, b_rho, u, v, f)]
+    nn = n * m
+    orc = (np.zeros(9 * nn), np.zeros(9 * nn))
+    rc = oracle_lib().orc_cg2d_collide(int(fp64), n, m, C.byref(p), *[_vp(a) for a in arrs],
+                                       _vp(orc[0]), _vp(orc[1]))
+    assert rc == 0
+    ref = None
+    L = ref_lib(fp64)
+    if L is not None:
+        rr, bb, cd = np.zeros(9 * nn), np.zeros(9 * nn), np.zeros(nn, np.int32)
+        L.ref_cg2d_collide(n, m, C.byref(p), *[_vp(a) for a in arrs], _vp(rr), _vp(bb), _vp(cd))
+        ref = (rr.reshape(9, nn), bb.reshape(9, nn), cd)
+    return (orc[0].reshape(9, nn), orc[1].reshape(9, nn)), ref

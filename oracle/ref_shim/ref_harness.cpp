@@ -336,6 +336,72 @@ int ref_run3d(int n, int m, int h, const int *node_type, const double *node_x,
     return 0;
 }
 
+/* Colour-gradient parameters (the multiphase fields of Arguments,
+ * include/Arguments.h:113-128). */
+typedef struct {
+    double r_density, b_density, r_alpha, b_alpha, r_viscosity, b_viscosity;
+    double beta, A, g_limit, control_param, g;
+    int high_order, enhanced, external_force;
+} ref_cg_params;
+
+/* One call of the reference's gpuCollBgkwGC2D / gpuCollEnhancedBgkwGC2D
+ * (GpuCollision.cu:552-707) on given fields; out_cgdir receives the
+ * reference's gradient-direction map (GpuInit.cu:206-260). */
+int ref_cg2d_collide(int n, int m, const ref_cg_params *cp, const double *rho, const double *r_rho,
+                     const double *b_rho, const double *u, const double *v, const double *f,
+                     double *out_rfc, double *out_bfc, int *out_cgdir) {
+    const int ms = n * m;
+    Arguments args;
+    memset(&args, 0, sizeof(args));
+    args.viscosity = (FLOAT_TYPE)0.1;
+    args.multiPhase = 1;
+    args.r_density = (FLOAT_TYPE)cp->r_density;
+    args.b_density = (FLOAT_TYPE)cp->b_density;
+    args.r_alpha = (FLOAT_TYPE)cp->r_alpha;
+    args.b_alpha = (FLOAT_TYPE)cp->b_alpha;
+    args.r_viscosity = (FLOAT_TYPE)cp->r_viscosity;
+    args.b_viscosity = (FLOAT_TYPE)cp->b_viscosity;
+    args.beta = (FLOAT_TYPE)cp->beta;
+    args.A = (FLOAT_TYPE)cp->A;
+    args.g_limit = (FLOAT_TYPE)cp->g_limit;
+    args.control_param = (FLOAT_TYPE)cp->control_param;
+    args.g = (FLOAT_TYPE)cp->g;
+    args.external_force = cp->external_force != 0;
+    args.bubble_radius = (FLOAT_TYPE)1.0;
+    initConstants2D(&args, 0, 0, 1, m, n);
+    std::vector<int> cgdir(ms, 0);
+    if (cp->high_order)
+        initHOColorGradient(cgdir.data(), n, m);
+    else
+        initColorGradient(cgdir.data(), n, m);
+    std::vector<FLOAT_TYPE> R(ms), RR(ms), BR(ms), U(ms), V(ms), F(9 * (size_t)ms), RC(9 * (size_t)ms, 0),
+        BC(9 * (size_t)ms, 0);
+    for (int i = 0; i < ms; ++i) {
+        R[i] = (FLOAT_TYPE)rho[i];
+        RR[i] = (FLOAT_TYPE)r_rho[i];
+        BR[i] = (FLOAT_TYPE)b_rho[i];
+        U[i] = (FLOAT_TYPE)u[i];
+        V[i] = (FLOAT_TYPE)v[i];
+    }
+    for (size_t k = 0; k < 9 * (size_t)ms; ++k) F[k] = (FLOAT_TYPE)f[k];
+    shim_dim3 tpb{THREADS, 1, 1};
+    shim_dim3 bpg1{(unsigned)(ms / THREADS) + 1, 1, 1};
+    launch(bpg1, tpb, [&] {
+        if (cp->enhanced)
+            gpuCollEnhancedBgkwGC2D(R.data(), RR.data(), BR.data(), U.data(), V.data(), F.data(), RC.data(),
+                                    BC.data(), cgdir.data(), cp->high_order != 0);
+        else
+            gpuCollBgkwGC2D(R.data(), RR.data(), BR.data(), U.data(), V.data(), F.data(), RC.data(), BC.data(),
+                            cgdir.data(), cp->high_order != 0);
+    });
+    for (size_t k = 0; k < 9 * (size_t)ms; ++k) {
+        out_rfc[k] = RC[k];
+        out_bfc[k] = BC[k];
+    }
+    if (out_cgdir) memcpy(out_cgdir, cgdir.data(), sizeof(int) * (size_t)ms);
+    return 0;
+}
+
 /* The reference's MRT matrices (CellFunctions.cu:7-153) for a given omega. */
 void ref_mrt_matrices(int q, double omega, double *vel_mom_map, double *mom_coll_mtx) {
     int n = q * q;

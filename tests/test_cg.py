@@ -1,0 +1,171 @@
+"""Colour-gradient two-phase D2Q9: the oracle pinned against the reference's
+collision kernel, oracle invariants, the host helpers, and the CUDA path
+(lbm_cg_*) against the oracle.
+
+The reference computes the colour gradient one-sided on the lattice edges
+(GpuCollision.cu:112-281) while this path wraps periodically, so the pin
+compares nodes at least two away from every edge."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from thesis_gb300 import multiphase as mp
+
+COMBOS = [(ho, enh) for ho in (0, 1) for enh in (0, 1)]
+
+
+def _collide_inputs(n, m, seed):
+    rng = np.random.default_rng(seed)
+    nn = n * m
+    j, i = np.divmod(np.arange(nn), n)
+    # a smooth interface plus noise, so gradients are non-trivial everywhere
+    phi = np.tanh((np.hypot(i - n / 2, j - m / 2) - n / 4) / 2.0)
+    r_rho = 0.5 * (1 - phi) + 0.01 * rng.random(nn)
+    b_rho = 0.5 * (1 + phi) + 0.01 * rng.random(nn)
+    rho = r_rho + b_rho
+    u = 0.02 * rng.standard_normal(nn)
+    v = 0.02 * rng.standard_normal(nn)
+    f = rng.random((9, nn)) * rho[None, :] / 4.5
+    return rho, r_rho, b_rho, u, v, f
+
+
+@pytest.mark.parametrize("ho,enh", COMBOS)
+@pytest.mark.parametrize("fp64", [True, False])
+def test_cg_collision_pinned_to_reference(ho, enh, fp64):
+    if po.ref_lib(fp64) is None:
+        pytest.skip("reference kernels not built (oracle/_ref)")
+    n, m = 24, 20
+    p = po.cg_params(high_order=ho, enhanced=enh, r_viscosity=0.5, b_viscosity=0.2, beta=0.99, A=0.01,
+                     r_alpha=0.5, b_alpha=4 / 9)
+    orc, ref = po.cg_collide_pair(n, m, p, *_collide_inputs(n, m, 7 + ho + 2 * enh), fp64=fp64)
+    j, i = np.divmod(np.arange(n * m), n)
+    e = 2 if ho else 1
+    interior = (i >= e) & (i < n - e) & (j >= e) & (j < m - e)
+    for a, b in ((orc[0], ref[0]), (orc[1], ref[1])):
+        d = np.abs(a[:, interior] - b[:, interior]).max()
+        if fp64:
+            assert d == 0.0, d
+        else:
+            # FP32: the reference's expression trees differ from the oracle's
+            # in a few places; values are O(1), so 2 ulp is 2.4e-7
+            assert d <= 2.4e-7, d
+
+
+def test_cg_oracle_conserves_colour_mass():
+    a = mp.CgArguments(bubble_radius=0.25, A=0.005, beta=0.99)
+    n, m = 32, 28
+    r0, b0 = mp.create_bubble(n, m, a)
+    p = po.cg_params(A=a.A, beta=a.beta, high_order=1)
+    r = po.run_oracle_cg(n, m, p, r0, b0, 100, fp64=True)
+    assert r.rc == 0
+    assert abs(r.rf.sum() - r0.sum()) < 1e-10 * r0.sum()
+    assert abs(r.bf.sum() - b0.sum()) < 1e-10 * b0.sum()
+    assert np.all(r.rr + r.br > 0)
+
+
+def test_create_bubble_and_prediction():
+    a = mp.CgArguments(bubble_radius=0.25, r_density=1.0, b_density=0.5, r_alpha=0.6, b_alpha=0.2)
+    r, b = mp.create_bubble(17, 17, a)
+    assert r.shape == (9, 289) and b.shape == (9, 289)
+    centre = 8 + 17 * 8
+    np.testing.assert_allclose(r[:, centre], mp.rest_weights(0.6))
+    assert np.all(b[:, centre] == 0)
+    np.testing.assert_allclose(b[:, 0], 0.5 * mp.rest_weights(0.2))
+    np.testing.assert_allclose(mp.rest_weights(0.3).sum(), 1.0)
+    # omega_eff = 1 when the mean viscosity is 1/6
+    a2 = mp.CgArguments(r_viscosity=1 / 6, b_viscosity=1 / 6, A=0.009)
+    assert abs(mp.predicted_surface_tension(a2) - 0.004) < 1e-15
+    lap = np.array([10.0, 10.0, 9.0, 10.0, 0.0])
+    err = mp.surface_tension_error(lap, a2, 10.0)
+    st = 10.0 * (3 / 5 * (1 - a2.r_alpha) * 1.0 - 3 / 5 * (1 - a2.b_alpha) * 0.9)
+    assert abs(err - abs(0.004 - st) / 0.004 * 100) < 1e-9
+
+
+def _gpu_case(n, m, ho, enh, seed=3):
+    a = mp.CgArguments(bubble_radius=0.3, A=0.01, beta=0.99, r_viscosity=0.3, b_viscosity=0.1,
+                       r_alpha=0.5, b_alpha=4 / 9, high_order=bool(ho), enhanced_distrib=bool(enh),
+                       control_param=0.9)
+    r0, b0 = mp.create_bubble(n, m, a)
+    rng = np.random.default_rng(seed)
+    # a 1% random density perturbation sets the fluid in motion, so every term
+    # of the collision is active
+    r0 = r0 * (1 + 0.01 * rng.random(r0.shape))
+    b0 = b0 * (1 + 0.01 * rng.random(b0.shape))
+    p = po.cg_params(r_density=a.r_density, b_density=a.b_density, r_alpha=a.r_alpha, b_alpha=a.b_alpha,
+                     r_viscosity=a.r_viscosity, b_viscosity=a.b_viscosity, beta=a.beta, A=a.A,
+                     g_limit=a.g_limit, control_param=a.control_param, high_order=ho, enhanced=enh)
+    return a, p, r0.astype(np.float32).astype(np.float64), b0.astype(np.float32).astype(np.float64)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ho,enh", COMBOS)
+def test_cg_gpu_matches_oracle(ho, enh):
+    n, m, steps = 48, 40, 40
+    a, p, r0, b0 = _gpu_case(n, m, ho, enh)
+    orc = po.run_oracle_cg(n, m, p, r0, b0, steps, fp64=False, extra_collide=True)
+    assert orc.rc == 0
+    with mp.CgSolver(n, m, a) as s:
+        s.init(r0, b0)
+        s.step(steps, write_macro=True)
+        rf, bf = s.populations()
+        rr, br, u, v = s.macro()
+        lap, rc = s.laplace()
+    assert rc == 0
+    # FP32 with different operation order (FMA contraction on the GPU):
+    # differences stay at a few ulps of O(1) values over 40 steps
+    tol = 2e-5
+    assert np.abs(rf - orc.rfc).max() < tol
+    assert np.abs(bf - orc.bfc).max() < tol
+    assert np.abs(rr - orc.rr).max() < tol
+    assert np.abs(br - orc.br).max() < tol
+    assert np.abs(u - orc.u).max() < tol
+    assert np.abs(v - orc.v).max() < tol
+    # Laplace-law sums: counts can flip only where phi sits at the threshold
+    assert abs(lap[1] - orc.laplace[1]) <= 2 and abs(lap[3] - orc.laplace[3]) <= 2
+    np.testing.assert_allclose(lap[0], orc.laplace[0], rtol=0, atol=2.5)
+    np.testing.assert_allclose(lap[2], orc.laplace[2], rtol=0, atol=2.5)
+    np.testing.assert_allclose(lap[4], orc.laplace[4], rtol=1e-3, atol=1e-6)
+
+
+@pytest.mark.gpu
+def test_cg_gpu_laplace_sums_exact_counts():
+    """After one step of a sharp bubble no node sits near the phase threshold,
+    so the phase counts must equal the oracle's exactly."""
+    n, m = 64, 64
+    a = mp.CgArguments(bubble_radius=0.25, control_param=0.9)
+    r0, b0 = mp.create_bubble(n, m, a)
+    p = po.cg_params(control_param=0.9)
+    orc = po.run_oracle_cg(n, m, p, r0, b0, 0, fp64=False)
+    with mp.CgSolver(n, m, a) as s:
+        s.init(r0, b0)
+        s.step(1, write_macro=True)
+        lap0, _ = s.laplace()
+    orc1 = po.run_oracle_cg(n, m, p, r0, b0, 1, fp64=False)
+    assert lap0[1] == orc1.laplace[1] and lap0[3] == orc1.laplace[3]
+    assert orc.laplace[1] > 0 and orc.laplace[3] > 0
+
+
+@pytest.mark.gpu
+def test_cg_gpu_mass_conservation_large():
+    n, m, steps = 512, 384, 1000
+    a = mp.CgArguments(bubble_radius=0.2, A=0.005, beta=0.99, high_order=True)
+    r0, b0 = mp.create_bubble(n, m, a)
+    with mp.CgSolver(n, m, a) as s:
+        s.init(r0, b0)
+        s.step(steps, write_macro=True)
+        rf, bf = s.populations()
+        lap, rc = s.laplace()
+    assert rc == 0
+    # FP32 accumulation over 2e5 nodes x 1000 steps: relative drift 1e-4
+    assert abs(rf.astype(np.float64).sum() - r0.sum()) < 1e-4 * r0.sum()
+    assert abs(bf.astype(np.float64).sum() - b0.sum()) < 1e-4 * b0.sum()
+    assert lap[4] < 0.05  # a bubble at rest stays near rest
+
+
+@pytest.mark.gpu
+def test_cg_gpu_refusals():
+    from thesis_gb300 import native as N
+    with pytest.raises(N.LbmError):
+        mp.CgSolver(4, 16, mp.CgArguments())
+    with pytest.raises(N.LbmError):
+        mp.CgSolver(16, 16, mp.CgArguments(r_viscosity=0.0))

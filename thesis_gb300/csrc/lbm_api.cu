@@ -3,18 +3,22 @@
 // captured two-step CUDA graph for short steps) and read-back.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <new>
 #include <string>
 #include <vector>
 
 #include "lbm_flags.h"
-#include "lbm_step.cuh"
+#include "lbm_step_tma.cuh"
 
 namespace lbm {
 int launch_step_q9(const StepParams &p, int coll, int st, int phys, cudaStream_t s);
 int launch_step_q19(const StepParams &p, int coll, int st, int phys, cudaStream_t s);
+int launch_step_x2_q9(const StepParams &p, int coll, int st, int phys, cudaStream_t s);
+int launch_step_x2_q19(const StepParams &p, int coll, int st, int phys, cudaStream_t s);
 int launch_init_q9(const StepParams &p, const StepParams &o, int coll, int st, int phys, int eq, cudaStream_t s);
 int launch_init_q19(const StepParams &p, const StepParams &o, int coll, int st, int phys, int eq, cudaStream_t s);
 int launch_decode_q9(const StepParams &p, int st, double *out, long long n, cudaStream_t s);
@@ -23,6 +27,10 @@ int launch_norms(const uint32_t *word, const float *rho, const float *ux, const 
                  const float *uz, float *pux, float *puy, float *puz, long long n,
                  double *partial, double *out, cudaStream_t s);
 int norm_partial_count();
+int tma_prepare(int q, int coll, int st, size_t smem, int *blocks_per_sm);
+int launch_step_tma(int q, const StepParams &p, const TmaRows &rows, int coll, int st, int grid, size_t smem,
+                    cudaStream_t s);
+unsigned tma_stage_size(int q, int nx, int elem);
 }  // namespace lbm
 
 using namespace lbm;
@@ -62,6 +70,13 @@ struct lbm_handle_s {
     cudaGraphExec_t pair[2] = {nullptr, nullptr};
     int status = LBM_OK;
     bool initialised = false;
+    bool pair_kernel = false;  // two nodes per thread (even nx, F32/F16S)
+    bool tma_kernel = false;   // row-staged bulk-copy kernel
+    int32_t *tma_row = nullptr;
+    uint32_t *tma_lmask = nullptr, *tma_omask = nullptr;
+    unsigned int *tma_err = nullptr;
+    int tma_nrows = 0, tma_stages = 0, tma_grid = 0;
+    size_t tma_smem = 0;
     double omega = 1, omega_m = 1, gshift = 0;
     float scale = 1024.f;
 };
@@ -93,6 +108,8 @@ static StepParams make_params(const lbm_handle_s *H, int from, int write_macro) 
     p.rho_out = H->P.rho_out;
     p.scale = H->scale;
     p.inv_scale = 1.0f / H->scale;
+    for (int d = 0; d < H->q; ++d)
+        p.shift[d] = H->P.storage == LBM_STORE_F16S ? (float)rest_shift(H->q, H->P.collision_model, d) : 0.0f;
     p.outlet_profile = H->P.outlet_profile;
     p.update_inlet_outlet = H->P.update_inlet_outlet;
     return p;
@@ -103,11 +120,105 @@ static void free_handle(lbm_handle_s *H) {
     for (int c = 0; c < 2; ++c)
         if (H->pair[c]) cudaGraphExecDestroy(H->pair[c]);
     void *ptrs[] = {H->fbuf[0], H->fbuf[1], H->word, H->slot, H->mask, H->kind, H->uvw,
-                    H->rho, H->ux, H->uy, H->uz, H->pux, H->puy, H->puz, H->partial, H->norms};
+                    H->rho, H->ux, H->uy, H->uz, H->pux, H->puy, H->puz, H->partial, H->norms,
+                    H->tma_row, H->tma_lmask, H->tma_omask, H->tma_err};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (H->stream) cudaStreamDestroy(H->stream);
     delete H;
+}
+
+// Per row (y + ny z) holding fluid nodes: the directions whose pull row the
+// row-staged kernel must copy (those some fluid node of the row pulls across
+// an open link) and the arrays whose own row it must copy (opp(d) for every
+// d that some fluid node of the row cannot pull).
+template <int Q>
+static void tma_row_tables(const std::vector<uint32_t> &word, int nx, long long nrows_all,
+                           std::vector<int32_t> &rows, std::vector<uint32_t> &lm, std::vector<uint32_t> &om) {
+    using L = Lat<Q>;
+    const uint32_t dirs = (1u << Q) - 1u;
+    for (long long r = 0; r < nrows_all; ++r) {
+        const uint32_t *w = word.data() + (size_t)r * nx;
+        uint32_t any_blocked = 0, all_blocked = dirs;
+        bool fluid = false;
+        for (int x = 0; x < nx; ++x) {
+            if (!(w[x] & W_FLUID)) continue;
+            fluid = true;
+            const uint32_t b = w[x] & dirs & ~1u;
+            any_blocked |= b;
+            all_blocked &= b;
+        }
+        if (!fluid) continue;
+        uint32_t o = 0;
+        for (int d = 1; d < Q; ++d)
+            if ((any_blocked >> d) & 1u) o |= 1u << L::opp(d);
+        rows.push_back((int32_t)r);
+        lm.push_back(dirs & ~all_blocked);
+        om.push_back(o);
+    }
+}
+
+// Decide whether the row-staged kernel can run this lattice and set it up:
+// physics mode, F32/F16S storage, rows a multiple of 16 bytes and at least
+// two stages in shared memory.  Returns LBM_OK with H->tma_kernel false when
+// it cannot.
+static int setup_tma(lbm_handle_s *H, const std::vector<uint32_t> &word) {
+    H->tma_kernel = false;
+    if (H->P.mode != LBM_MODE_PHYSICS) return LBM_OK;
+    if (H->P.storage != LBM_STORE_F32 && H->P.storage != LBM_STORE_F16S) return LBM_OK;
+    if (((size_t)H->n * H->elem) % 16 != 0) return LBM_OK;
+    int dev = 0, sms = 0, smem_sm = 0, smem_blk = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&smem_blk, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const long long stage = tma_stage_size(H->q, H->n, (int)H->elem);
+    int stages = 0;
+    for (int blocks = 2; blocks >= 1; --blocks) {
+        const long long per_block = std::min<long long>(smem_blk, smem_sm / blocks - 1024);
+        stages = (int)std::min<long long>(8, (per_block - TMA_BARRIER_BYTES) / stage);
+        if (stages >= (blocks == 2 ? 3 : 2)) break;
+    }
+    if (stages < 2) return LBM_OK;
+    std::vector<int32_t> rows;
+    std::vector<uint32_t> lm, om;
+    const long long nrows_all = (long long)H->m * H->h;
+    if (H->q == 9) tma_row_tables<9>(word, H->n, nrows_all, rows, lm, om);
+    else tma_row_tables<19>(word, H->n, nrows_all, rows, lm, om);
+    if (rows.empty()) return LBM_OK;
+    const size_t smem = TMA_BARRIER_BYTES + (size_t)stages * stage;
+    int bps = 0;
+    const int e = tma_prepare(H->q, H->P.collision_model, H->P.storage, smem, &bps);
+    if (e != 0 || bps < 1) return LBM_OK;
+    const size_t nr = rows.size();
+    CUDA_TRY(cudaMalloc((void **)&H->tma_row, sizeof(int32_t) * nr));
+    CUDA_TRY(cudaMalloc((void **)&H->tma_lmask, sizeof(uint32_t) * nr));
+    CUDA_TRY(cudaMalloc((void **)&H->tma_omask, sizeof(uint32_t) * nr));
+    CUDA_TRY(cudaMalloc((void **)&H->tma_err, sizeof(unsigned int)));
+    CUDA_TRY(cudaMemcpy(H->tma_row, rows.data(), sizeof(int32_t) * nr, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(H->tma_lmask, lm.data(), sizeof(uint32_t) * nr, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(H->tma_omask, om.data(), sizeof(uint32_t) * nr, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemset(H->tma_err, 0, sizeof(unsigned int)));
+    H->tma_nrows = (int)nr;
+    H->tma_stages = stages;
+    H->tma_smem = smem;
+    H->tma_grid = (int)std::min<long long>((long long)nr, (long long)sms * bps);
+    H->tma_kernel = true;
+    return LBM_OK;
+}
+
+// A bounded wait inside the row-staged kernel that gave up leaves a code in
+// tma_err; report it once the stream is idle.
+static int check_tma(lbm_handle_s *H) {
+    if (!H->tma_kernel) return LBM_OK;
+    unsigned int err = 0;
+    CUDA_TRY(cudaMemcpy(&err, H->tma_err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err) {
+        H->status = LBM_ERR_CUDA;
+        return fail(LBM_ERR_CUDA, "row-staged step: a shared-memory pipeline wait timed out (code " +
+                                      std::to_string(err) + ")");
+    }
+    return LBM_OK;
 }
 
 extern "C" {
@@ -168,8 +279,28 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     long long fl = 0;
     for (long long i = 0; i < N; ++i) fl += (L->node_type[i] & 1);
     H->fluid = fl;
+    bool want_tma = false;
+    {
+        // Two nodes per thread pays where the packed FP32x2 arithmetic
+        // outweighs its higher register count: F32 storage.  For F16S the
+        // one-node kernel keeps more warps resident and is faster.
+        // THESIS_LBM_KERNEL=scalar|pair overrides the choice.
+        const char *kv = getenv("THESIS_LBM_KERNEL");
+        const bool can_pair = (L->n % 2 == 0) && P->storage != LBM_STORE_F64;
+        if (kv && strcmp(kv, "scalar") == 0) H->pair_kernel = false;
+        else if (kv && strcmp(kv, "pair") == 0) H->pair_kernel = can_pair;
+        else H->pair_kernel = can_pair && P->storage == LBM_STORE_F32;
+        want_tma = kv && strcmp(kv, "tma") == 0;
+    }
     H->nslots = (int)flags.slot_node.size();
     H->slot_node = flags.slot_node;
+    if (want_tma) {
+        rc = setup_tma(H, flags.word);
+        if (rc) {
+            free_handle(H);
+            return rc;
+        }
+    }
 
 #define ALLOC(ptr, bytes)                                                               \
     do {                                                                                \
@@ -283,8 +414,22 @@ int lbm_init(lbm_handle H, const float *rho, const float *u, const float *v, con
 static int launch(lbm_handle_s *H, int from, int write_macro, cudaStream_t s) {
     const StepParams p = make_params(H, from, write_macro);
     const int phys = H->P.mode == LBM_MODE_PHYSICS;
-    const int rc = H->q == 9 ? launch_step_q9(p, H->P.collision_model, H->P.storage, phys, s)
-                             : launch_step_q19(p, H->P.collision_model, H->P.storage, phys, s);
+    int rc;
+    if (H->tma_kernel) {
+        TmaRows rows;
+        rows.row = H->tma_row;
+        rows.lmask = H->tma_lmask;
+        rows.omask = H->tma_omask;
+        rows.nrows = H->tma_nrows;
+        rows.stages = H->tma_stages;
+        rows.err = H->tma_err;
+        rc = launch_step_tma(H->q, p, rows, H->P.collision_model, H->P.storage, H->tma_grid, H->tma_smem, s);
+    } else if (H->pair_kernel)
+        rc = H->q == 9 ? launch_step_x2_q9(p, H->P.collision_model, H->P.storage, phys, s)
+                       : launch_step_x2_q19(p, H->P.collision_model, H->P.storage, phys, s);
+    else
+        rc = H->q == 9 ? launch_step_q9(p, H->P.collision_model, H->P.storage, phys, s)
+                       : launch_step_q19(p, H->P.collision_model, H->P.storage, phys, s);
     return rc ? fail(LBM_ERR_UNSUPPORTED, "no kernel for this configuration") : LBM_OK;
 }
 
@@ -339,6 +484,7 @@ int lbm_step(lbm_handle H, int nsteps, int write_macro_last, void *stream) {
 int lbm_get_macro(lbm_handle H, float *rho, float *u, float *v, float *w) {
     if (!H) return fail(LBM_ERR_INVALID, "null handle");
     CUDA_TRY(cudaDeviceSynchronize());
+    if (int rc = check_tma(H)) return rc;
     const size_t b = sizeof(float) * H->N;
     if (rho) CUDA_TRY(cudaMemcpy(rho, H->rho, b, cudaMemcpyDeviceToHost));
     if (u) CUDA_TRY(cudaMemcpy(u, H->ux, b, cudaMemcpyDeviceToHost));
@@ -350,6 +496,7 @@ int lbm_get_macro(lbm_handle H, float *rho, float *u, float *v, float *w) {
 int lbm_get_populations(lbm_handle H, double *f) {
     if (!H || !f) return fail(LBM_ERR_INVALID, "null argument");
     CUDA_TRY(cudaDeviceSynchronize());
+    if (int rc = check_tma(H)) return rc;
     double *tmp = nullptr;
     const size_t bytes = sizeof(double) * (size_t)H->q * H->N;
     CUDA_TRY(cudaMalloc((void **)&tmp, bytes));
@@ -373,6 +520,7 @@ int lbm_macro_norms(lbm_handle H, double *out) {
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(out, H->norms, sizeof(double) * LBM_NORMS, cudaMemcpyDeviceToHost, H->stream));
     CUDA_TRY(cudaStreamSynchronize(H->stream));
+    if (int rc = check_tma(H)) return rc;
     for (int k = 0; k < LBM_NORMS; ++k)
         if (!isfinite(out[k])) {
             H->status = LBM_DIVERGED;
@@ -402,6 +550,8 @@ int lbm_build_flags(const lbm_lattice_desc *L, const lbm_params *P, uint64_t *ma
 int lbm_status(lbm_handle H) { return H ? H->status : LBM_ERR_INVALID; }
 
 long long lbm_fluid_nodes(lbm_handle H) { return H ? H->fluid : -1; }
+
+int lbm_kernel_variant(lbm_handle H) { return H ? (H->tma_kernel ? 3 : (H->pair_kernel ? 2 : 1)) : -1; }
 
 int lbm_bytes_per_update(lbm_handle H) { return H ? (int)(2 * H->q * H->elem) : -1; }
 

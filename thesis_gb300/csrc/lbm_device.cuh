@@ -61,6 +61,9 @@ template <> struct Lat<19> {
     }
 };
 
+// Rest-state populations of a collision model, the F16S storage shift.
+__host__ __device__ constexpr double rest_shift(int q, int coll, int d);
+
 // D2Q9 and D3Q19 moment bases of the reference MRT (CellFunctions.cu:31-40,
 // :94-113).  Rows are orthogonal, so M^-1 = M^T diag(1/|row|^2).
 __host__ __device__ constexpr int mrt2(int k, int i) {
@@ -103,38 +106,54 @@ __host__ __device__ constexpr int mrt3_norm(int k) {
     return N[k];
 }
 
+// w_d for BGK/TRT and the D2Q9 MRT (whose rest state is w); for the D3Q19
+// MRT, w_d minus the eps-moment part 3/252 * M_eps,d that its zero-density
+// eps equilibrium removes (w -> 4/21, 13/126, 1/63).
+__host__ __device__ constexpr double rest_shift(int q, int coll, int d) {
+    return q == 9 ? Lat<9>::w(d)
+                  : (coll == LBM_MRT ? Lat<19>::w(d) - 3.0 / 252.0 * mrt3(2, d) : Lat<19>::w(d));
+}
+
 // ---------------------------------------------------------------------------
 // Population storage.  F32 and F64 hold f itself; F16S holds the scaled
-// deviation from the rest-state weight, h = (f - w_d) * scale, so the few
-// significant digits of a slow flow land in FP16's normal range.
+// deviation from the collision model's rest state, h = (f - shift_d) * scale,
+// so the few significant digits of a slow flow land in FP16's normal range.
+// The shift is the lattice weights w_d, except for the D3Q19 MRT whose
+// incompressible energy-square equilibrium (eps_eq = -475/63 j^2, no density
+// term) puts its rest state at w_d - (3/252) M_eps,d (rest_shift below).
 // ---------------------------------------------------------------------------
 template <int ST> struct Store;
 template <> struct Store<LBM_STORE_F32> {
     using T = float;   // element type in HBM
     using R = float;   // arithmetic type
-    __device__ static __forceinline__ R load(const T *p, double, float) { return __ldg(p); }
-    __device__ static __forceinline__ void store(T *p, R v, double, float) { *p = v; }
-    __device__ static __forceinline__ T encode(R v, double, float) { return v; }
+    __device__ static __forceinline__ R load(const T *p, float, float) { return __ldg(p); }
+    __device__ static __forceinline__ R decode(T v, float, float) { return v; }
+    __device__ static __forceinline__ void store(T *p, R v, float, float) { *p = v; }
+    __device__ static __forceinline__ T encode(R v, float, float) { return v; }
 };
 template <> struct Store<LBM_STORE_F16S> {
     using T = __half;
     using R = float;
-    __device__ static __forceinline__ R load(const T *p, double w, float inv_scale) {
-        return fmaf(__half2float(__ldg(p)), inv_scale, (float)w);
+    __device__ static __forceinline__ R load(const T *p, float w, float inv_scale) {
+        return fmaf(__half2float(__ldg(p)), inv_scale, w);
     }
-    __device__ static __forceinline__ T encode(R v, double w, float scale) {
-        return __float2half_rn((v - (float)w) * scale);
+    __device__ static __forceinline__ R decode(T v, float w, float inv_scale) {
+        return fmaf(__half2float(v), inv_scale, w);
     }
-    __device__ static __forceinline__ void store(T *p, R v, double w, float scale) {
+    __device__ static __forceinline__ T encode(R v, float w, float scale) {
+        return __float2half_rn((v - w) * scale);
+    }
+    __device__ static __forceinline__ void store(T *p, R v, float w, float scale) {
         *p = encode(v, w, scale);
     }
 };
 template <> struct Store<LBM_STORE_F64> {
     using T = double;
     using R = double;
-    __device__ static __forceinline__ R load(const T *p, double, float) { return __ldg(p); }
-    __device__ static __forceinline__ void store(T *p, R v, double, float) { *p = v; }
-    __device__ static __forceinline__ T encode(R v, double, float) { return v; }
+    __device__ static __forceinline__ R load(const T *p, float, float) { return __ldg(p); }
+    __device__ static __forceinline__ R decode(T v, float, float) { return v; }
+    __device__ static __forceinline__ void store(T *p, R v, float, float) { *p = v; }
+    __device__ static __forceinline__ T encode(R v, float, float) { return v; }
 };
 
 // ---------------------------------------------------------------------------

@@ -1,5 +1,5 @@
 // Instantiations of the fused step, init and decode kernels for D2Q9.
-#include "lbm_step.cuh"
+#include "lbm_step_x2.cuh"
 
 namespace lbm {
 
@@ -20,6 +20,25 @@ int launch_step_q9(const StepParams &p, int coll, int st, int phys, cudaStream_t
     }
     LBM_FOR_ALL(STEP_CASE)
 #undef STEP_CASE
+    return -1;
+}
+
+static dim3 pair_grid(const StepParams &p) {
+    const int pairs = p.nx / 2;
+    return dim3((unsigned)((pairs + X2_BLOCK - 1) / X2_BLOCK), (unsigned)p.ny, (unsigned)p.nz);
+}
+
+// Two-node kernel (F32 / F16S storage, even nx).
+int launch_step_x2_q9(const StepParams &p, int coll, int st, int phys, cudaStream_t s) {
+#define X2_CASE(C, S, P)                                                              \
+    if (coll == C && st == S && (phys != 0) == P) {                                  \
+        step_kernel_x2<9, C, S, P><<<pair_grid(p), X2_BLOCK, 0, s>>>(p);           \
+        return 0;                                                                     \
+    }
+    X2_CASE(1, 0, false) X2_CASE(1, 1, false) X2_CASE(2, 0, false) X2_CASE(2, 1, false)
+    X2_CASE(3, 0, false) X2_CASE(3, 1, false) X2_CASE(1, 0, true) X2_CASE(1, 1, true)
+    X2_CASE(2, 0, true) X2_CASE(2, 1, true) X2_CASE(3, 0, true) X2_CASE(3, 1, true)
+#undef X2_CASE
     return -1;
 }
 

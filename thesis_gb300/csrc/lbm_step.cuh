@@ -35,6 +35,9 @@ struct StepParams {
     double omega, omega_m, gshift;
     double rho_in, rho_out;
     float scale, inv_scale;
+    // F16S storage holds (f_d - shift_d) * scale: shift is the collision
+    // model's rest-state equilibrium (0 for F32/F64 storage)
+    float shift[19];
     int outlet_profile;
     int update_inlet_outlet;
     // initial state (init kernel only): constants for the fields not given as
@@ -62,53 +65,13 @@ __device__ __forceinline__ void collide(typename Store<ST>::R (&f)[Q], typename 
     }
 }
 
+// Everything a fluid node does after its populations are gathered: boundary
+// conditions, macroscopic moments (stored when p.write_macro), collision.
 template <int Q, int COLL, int ST, bool PHYS>
-__global__ void __launch_bounds__(STEP_BLOCK) step_kernel(const StepParams p) {
-    using S = Store<ST>;
-    using T = typename S::T;
-    using R = typename S::R;
+__device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], uint32_t w, int node,
+                                            const StepParams &p) {
+    using R = typename Store<ST>::R;
     using L = Lat<Q>;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
-    const bool in_row = x < p.nx;
-    const int node = x + p.nx * (y + p.ny * z);
-    const uint32_t w = in_row ? __ldg(p.word + node) : 0u;
-    const bool fluid = (w & W_FLUID) != 0;
-    // Solid lanes of a warp that also holds fluid nodes store the zero
-    // encoding, so the warp's stores cover whole 32-byte sectors instead of
-    // forcing a read-modify-write of partly written ones in L2/DRAM.
-    const unsigned warp_fluid = __ballot_sync(0xffffffffu, fluid);
-    if (!fluid) {
-        if (in_row && warp_fluid) {
-#pragma unroll
-            for (int d = 0; d < Q; ++d) ((T *)p.fout[d])[node] = S::encode((R)0, L::w(d), p.scale);
-        }
-        return;
-    }
-
-    // Pull offsets to the six face neighbours; coordinates wrap periodically
-    // and links that must not wrap are blocked in the flag word, so a wrapped
-    // address is only read where the lattice is periodic.
-    const int plane = p.nx * p.ny;
-    const int oxm = x == 0 ? p.nx - 1 : -1, oxp = x == p.nx - 1 ? 1 - p.nx : 1;
-    const int oym = y == 0 ? (p.ny - 1) * p.nx : -p.nx, oyp = y == p.ny - 1 ? (1 - p.ny) * p.nx : p.nx;
-    const int ozm = z == 0 ? (p.nz - 1) * plane : -plane, ozp = z == p.nz - 1 ? (1 - p.nz) * plane : plane;
-
-    R f[Q];
-#pragma unroll
-    for (int d = 0; d < Q; ++d) {
-        if (d == 0) {
-            f[0] = S::load((const T *)p.fin[0] + node, L::w(0), p.inv_scale);
-            continue;
-        }
-        const int src = node + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
-                        (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
-                        (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
-        const bool blocked = (w >> d) & 1u;
-        const T *base = (const T *)p.fin[(blocked && PHYS) ? L::opp(d) : d];
-        f[d] = S::load(base + (blocked ? node : src), L::w(d), p.inv_scale);
-    }
-
     bool keep_macro = false, zero_v = false;
     if (w & W_SPECIAL) {
         const int sl = __ldg(p.slot + node);
@@ -165,9 +128,59 @@ __global__ void __launch_bounds__(STEP_BLOCK) step_kernel(const StepParams p) {
     }
 
     collide<Q, COLL, ST, PHYS>(f, rho, ux, uy, uz, p);
+}
+
+template <int Q, int COLL, int ST, bool PHYS>
+__global__ void __launch_bounds__(STEP_BLOCK) step_kernel(const StepParams p) {
+    using S = Store<ST>;
+    using T = typename S::T;
+    using R = typename S::R;
+    using L = Lat<Q>;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    const bool in_row = x < p.nx;
+    const int node = x + p.nx * (y + p.ny * z);
+    const uint32_t w = in_row ? __ldg(p.word + node) : 0u;
+    const bool fluid = (w & W_FLUID) != 0;
+    // Solid lanes of a warp that also holds fluid nodes store the zero
+    // encoding, so the warp's stores cover whole 32-byte sectors instead of
+    // forcing a read-modify-write of partly written ones in L2/DRAM.
+    const unsigned warp_fluid = __ballot_sync(0xffffffffu, fluid);
+    if (!fluid) {
+        if (in_row && warp_fluid) {
+#pragma unroll
+            for (int d = 0; d < Q; ++d) ((T *)p.fout[d])[node] = S::encode((R)0, p.shift[d], p.scale);
+        }
+        return;
+    }
+
+    // Pull offsets to the six face neighbours; coordinates wrap periodically
+    // and links that must not wrap are blocked in the flag word, so a wrapped
+    // address is only read where the lattice is periodic.
+    const int plane = p.nx * p.ny;
+    const int oxm = x == 0 ? p.nx - 1 : -1, oxp = x == p.nx - 1 ? 1 - p.nx : 1;
+    const int oym = y == 0 ? (p.ny - 1) * p.nx : -p.nx, oyp = y == p.ny - 1 ? (1 - p.ny) * p.nx : p.nx;
+    const int ozm = z == 0 ? (p.nz - 1) * plane : -plane, ozp = z == p.nz - 1 ? (1 - p.nz) * plane : plane;
+
+    R f[Q];
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+        if (d == 0) {
+            f[0] = S::load((const T *)p.fin[0] + node, p.shift[0], p.inv_scale);
+            continue;
+        }
+        const int src = node + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
+                        (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
+                        (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
+        const bool blocked = (w >> d) & 1u;
+        const T *base = (const T *)p.fin[(blocked && PHYS) ? L::opp(d) : d];
+        f[d] = S::load(base + (blocked ? node : src), p.shift[d], p.inv_scale);
+    }
+
+    update_node<Q, COLL, ST, PHYS>(f, w, node, p);
 
 #pragma unroll
-    for (int d = 0; d < Q; ++d) S::store((T *)p.fout[d] + node, f[d], L::w(d), p.scale);
+    for (int d = 0; d < Q; ++d) S::store((T *)p.fout[d] + node, f[d], p.shift[d], p.scale);
 }
 
 // First post-collision field: f0 = 0 (the reference's start, Iterate.cu:244)
@@ -189,8 +202,8 @@ __global__ void __launch_bounds__(STEP_BLOCK) init_kernel(const StepParams p, co
     if (!(w & W_FLUID)) {
 #pragma unroll
         for (int d = 0; d < Q; ++d) {
-            ((T *)p.fout[d])[node] = S::encode((R)0, L::w(d), p.scale);
-            ((T *)other.fout[d])[node] = S::encode((R)0, L::w(d), p.scale);
+            ((T *)p.fout[d])[node] = S::encode((R)0, p.shift[d], p.scale);
+            ((T *)other.fout[d])[node] = S::encode((R)0, p.shift[d], p.scale);
         }
         return;
     }
@@ -206,10 +219,10 @@ __global__ void __launch_bounds__(STEP_BLOCK) init_kernel(const StepParams p, co
     collide<Q, COLL, ST, PHYS>(f, rho, ux, uy, uz, p);
 #pragma unroll
     for (int d = 0; d < Q; ++d) {
-        S::store((T *)p.fout[d] + node, f[d], L::w(d), p.scale);
+        S::store((T *)p.fout[d] + node, f[d], p.shift[d], p.scale);
         // The other buffer's fluid entries are overwritten by the first step
         // before anything reads them; give them the same finite values.
-        S::store((T *)other.fout[d] + node, f[d], L::w(d), p.scale);
+        S::store((T *)other.fout[d] + node, f[d], p.shift[d], p.scale);
     }
 }
 
@@ -222,7 +235,7 @@ __global__ void decode_kernel(const StepParams p, double *out, long long n) {
     if (i >= n) return;
 #pragma unroll
     for (int d = 0; d < Q; ++d)
-        out[d * n + i] = (double)S::load((const T *)p.fin[d] + i, Lat<Q>::w(d), p.inv_scale);
+        out[d * n + i] = (double)S::load((const T *)p.fin[d] + i, p.shift[d], p.inv_scale);
 }
 
 }  // namespace lbm

@@ -1,0 +1,430 @@
+// Two-node fused step for sm_100-class GPUs (sm_103a here).
+//
+// Each thread owns the x-adjacent node pair (x, x+1), x even.  Populations of
+// the pair travel as one 4-byte half2 (F16S) or 8-byte float2 (F32) per
+// direction, and all arithmetic runs on packed FP32x2 (FFMA2/FADD2/FMUL2), so a
+// warp instruction advances two lattice nodes.  Pulls with cx = 0 are one
+// aligned pair load; pulls with cx = +/-1 take the source row's aligned pair
+// and its left or right neighbour pair and pick the shifted elements.
+//
+// Arithmetic runs in storage space: h = (f - sigma w) * S, with sigma = 1 and
+// S = scale for F16S (FP16 deviation from the rest weights) and sigma = 0,
+// S = 1 for F32.  Every collision operator is linear in f except through the
+// equilibria, so it is applied to h directly with equilibria expressed in the
+// same units; a load is one half2->float2 convert and a store one float2->half2
+// convert, with no per-population shift and scale.  Boundary nodes convert to f
+// and reuse the scalar boundary code.
+#pragma once
+#include "lbm_step.cuh"
+
+namespace lbm {
+
+struct f2 {
+    float2 v;
+    __device__ __forceinline__ f2() {}
+    __device__ __forceinline__ f2(float s) : v(make_float2(s, s)) {}
+    __device__ __forceinline__ f2(float a, float b) : v(make_float2(a, b)) {}
+    __device__ __forceinline__ f2(float2 x) : v(x) {}
+};
+__device__ __forceinline__ f2 operator+(f2 a, f2 b) { return f2(__fadd2_rn(a.v, b.v)); }
+__device__ __forceinline__ f2 operator*(f2 a, f2 b) { return f2(__fmul2_rn(a.v, b.v)); }
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return f2(__ffma2_rn(a.v, b.v, c.v)); }
+__device__ __forceinline__ f2 operator-(f2 a, f2 b) { return f2(__ffma2_rn(b.v, make_float2(-1.f, -1.f), a.v)); }
+__device__ __forceinline__ f2 operator-(f2 a) { return f2(__fmul2_rn(a.v, make_float2(-1.f, -1.f))); }
+__device__ __forceinline__ f2 &operator+=(f2 &a, f2 b) { return a = a + b; }
+__device__ __forceinline__ f2 &operator-=(f2 &a, f2 b) { return a = a - b; }
+
+// Pair storage: element type of a pair in HBM and its conversion to h.
+template <int ST> struct Pair;
+template <> struct Pair<LBM_STORE_F32> {
+    using T = float2;
+    __device__ static __forceinline__ f2 load(const float *p) { return f2(__ldg((const float2 *)p)); }
+    __device__ static __forceinline__ float load1(const float *p) { return __ldg(p); }
+    __device__ static __forceinline__ void store(float *p, f2 h) { *(float2 *)p = h.v; }
+};
+template <> struct Pair<LBM_STORE_F16S> {
+    using T = __half2;
+    __device__ static __forceinline__ f2 load(const __half *p) { return f2(__half22float2(__ldg((const __half2 *)p))); }
+    __device__ static __forceinline__ float load1(const __half *p) { return __half2float(__ldg(p)); }
+    __device__ static __forceinline__ void store(__half *p, f2 h) { *(__half2 *)p = __float22half2_rn(h.v); }
+};
+
+// Moments of the storage shift that h carries: D2Q9 shift w has
+// (rho, e, eps) = (1, -2, 1); the D3Q19 BGK/TRT shift w has rho = 1 and the
+// D3Q19 MRT shift w~ has (rho, e, eps) = (1, -11, 0); the other moments
+// vanish by isotropy.
+
+// BGK / TRT in h units: h_eq,d = S w_d [(rho - sigma) + rho (3 cu + 4.5 cu^2 - 1.5 u^2)].
+template <int Q>
+__device__ __forceinline__ f2 heq(int d, f2 rho_m_sigma, f2 rho, f2 ux, f2 uy, f2 uz, f2 usq15, float S) {
+    using L = Lat<Q>;
+    f2 cu = 0.f;
+    if (L::cx(d)) cu = L::cx(d) > 0 ? ux : -ux;
+    if (L::cy(d)) cu = L::cy(d) > 0 ? cu + uy : cu - uy;
+    if (L::cz(d)) cu = L::cz(d) > 0 ? cu + uz : cu - uz;
+    // rho (3 cu + 4.5 cu^2 - 1.5 u^2) = rho (cu (3 + 4.5 cu) - usq15)
+    const f2 poly = fma2(cu, fma2(cu, f2(4.5f), f2(3.f)), -usq15);
+    return f2((float)(L::w(d)) * S) * fma2(rho, poly, rho_m_sigma);
+}
+
+template <int Q>
+__device__ __forceinline__ void collide_bgk_x2(f2 (&h)[Q], f2 rho, f2 ux, f2 uy, f2 uz, float omega, float sigma,
+                                               float S) {
+    const f2 usq15 = f2(1.5f) * fma2(ux, ux, fma2(uy, uy, uz * uz));
+    const f2 rms = rho - f2(sigma);
+    const f2 om(omega);
+#pragma unroll
+    for (int d = 0; d < Q; ++d) h[d] = fma2(-om, h[d] - heq<Q>(d, rms, rho, ux, uy, uz, usq15, S), h[d]);
+}
+
+template <int Q>
+__device__ __forceinline__ void collide_trt_x2(f2 (&h)[Q], f2 rho, f2 ux, f2 uy, f2 uz, float omega,
+                                               float omega_m, float sigma, float S) {
+    using L = Lat<Q>;
+    const f2 usq15 = f2(1.5f) * fma2(ux, ux, fma2(uy, uy, uz * uz));
+    const f2 rms = rho - f2(sigma);
+    f2 e[Q];
+#pragma unroll
+    for (int d = 0; d < Q; ++d) e[d] = heq<Q>(d, rms, rho, ux, uy, uz, usq15, S);
+    f2 out[Q];
+    const f2 hp(0.5f * omega), hm(0.5f * omega_m);
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+        const int o = L::opp(d);
+        const f2 nd = h[d] - e[d], no = h[o] - e[o];
+        out[d] = h[d] - fma2(hp, nd + no, hm * (nd - no));
+    }
+#pragma unroll
+    for (int d = 0; d < Q; ++d) h[d] = out[d];
+}
+
+// D3Q19 MRT in h units, in the pair-sum form of collide_mrt19 (lbm_device.cuh):
+// d_k = s_k/|m_k|^2 (m_k(h) - S (m_eq,k - sigma m_k(w~))), with w~ the
+// model's rest state (rest_shift): m(w~) = (1, -11, 0, 0, ...).
+template <bool REF>
+__device__ __forceinline__ void collide_mrt19_x2(f2 (&h)[19], f2 rho, f2 ux, f2 uy, f2 uz, float omega,
+                                                 float sigma, float S) {
+    const f2 sX = h[1] + h[2], aX = h[1] - h[2];
+    const f2 sY = h[3] + h[4], aY = h[3] - h[4];
+    const f2 sZ = h[5] + h[6], aZ = h[5] - h[6];
+    const f2 sA = h[7] + h[10], aA = h[7] - h[10];
+    const f2 sB = h[8] + h[9], aB = h[8] - h[9];
+    const f2 sC = h[11] + h[14], aC = h[11] - h[14];
+    const f2 sD = h[12] + h[13], aD = h[12] - h[13];
+    const f2 sE = h[15] + h[18], aE = h[15] - h[18];
+    const f2 sF = h[16] + h[17], aF = h[16] - h[17];
+    const f2 sAxis = sX + sY + sZ;
+    const f2 sAB = sA + sB, sCD = sC + sD, sEF = sE + sF;
+    const f2 sABCD = sAB + sCD, sDiag = sABCD + sEF;
+    const f2 h0 = h[0];
+    const f2 tx = (aA - aB) + (aC - aD), ty = (aA + aB) + (aE - aF), tz = (aC + aD) + (aE + aF);
+    const f2 m1 = fma2(f2(-30.f), h0, fma2(f2(-11.f), sAxis, f2(8.f) * sDiag));
+    const f2 m2 = fma2(f2(12.f), h0, fma2(f2(-4.f), sAxis, sDiag));
+    const f2 m4 = fma2(f2(-4.f), aX, tx);
+    const f2 m6 = fma2(f2(-4.f), aY, ty);
+    const f2 m8 = fma2(f2(-4.f), aZ, tz);
+    const f2 sYZ = sY + sZ;
+    const f2 m9 = fma2(f2(2.f), sX - sEF, sABCD - sYZ);
+    const f2 m10 = fma2(f2(2.f), sYZ - sEF, fma2(f2(-4.f), sX, sABCD));
+    const f2 m11 = (sY - sZ) + (sAB - sCD);
+    const f2 m12 = fma2(f2(2.f), sZ - sY, sAB - sCD);
+    const f2 m13 = sA - sB, m14 = sE - sF, m15 = sC - sD;
+    const f2 m16 = (aA - aB) - (aC - aD);
+    const f2 m17 = (aE - aF) - (aA + aB);
+    const f2 m18 = (aC + aD) - (aE + aF);
+    const f2 jx = rho * ux, jy = rho * uy, jz = rho * uz;
+    const f2 jx2 = jx * jx, jy2 = jy * jy, jz2 = jz * jz;
+    const f2 jsq = jx2 + jy2 + jz2;
+    const f2 Sv(S);
+    // S (m_eq,k - sigma m_k(w)) for the non-conserved moments
+    const f2 E1 = Sv * fma2(f2(-11.f), rho - f2(sigma), f2(19.f) * jsq);
+    // the storage shift is this model's rest state, whose eps moment is 0
+    const f2 E2 = Sv * (f2((float)(-475.0 / 63.0)) * jsq);
+    const f2 c23 = f2((float)(-2.0 / 3.0) * S);
+    const f2 d1 = f2((float)(1.19 / 2394.0)) * (m1 - E1);
+    const f2 d2 = f2((float)(1.4 / 252.0)) * (m2 - E2);
+    const f2 d4 = f2((float)(1.2 / 40.0)) * (m4 - c23 * jx);
+    const f2 d6 = f2((float)(1.2 / 40.0)) * (m6 - c23 * jy);
+    const f2 d8 = f2((float)(1.2 / 40.0)) * (m8 - c23 * jz);
+    const f2 d9 = f2(omega / 36.f) * (m9 - Sv * (fma2(f2(2.f), jx2, -jy2) - jz2));
+    const f2 d10 = f2((float)(1.4 / 72.0)) * m10;
+    const f2 d11 = f2(omega / 12.f) * (m11 - Sv * (jy2 - jz2));
+    const f2 d12 = f2((float)(1.4 / 24.0)) * m12;
+    const f2 w4(0.25f * omega);
+    const f2 d13 = w4 * (m13 - Sv * (jx * jy));
+    const f2 d14 = w4 * (m14 - Sv * (jy * jz));
+    const f2 d15 = w4 * (m15 - Sv * (jx * jz));
+    const f2 g16(1.98f / 8.f);
+    const f2 d16 = g16 * m16, d17 = g16 * m17, d18 = g16 * m18;
+    const f2 P = fma2(f2(-11.f), d1, f2(-4.f) * d2);
+    const f2 EX = fma2(f2(2.f), d9, fma2(f2(-4.f), d10, P));
+    const f2 EYZb = fma2(f2(2.f), d10, P - d9);
+    const f2 K2 = fma2(f2(-2.f), d12, d11);
+    const f2 EY = EYZb + K2, EZ = EYZb - K2;
+    const f2 G = fma2(f2(8.f), d1, d2), H = d9 + d10, K = d11 + d12;
+    const f2 GH = G + H;
+    const f2 GHp = GH + K, GHm = GH - K, G2H = fma2(f2(-2.f), H, G);
+    const f2 OA = (d4 + d6) + (d16 - d17), OB = (d6 - d4) - (d16 + d17);
+    const f2 OC = (d4 + d8) + (d18 - d16), OD = (d8 - d4) + (d16 + d18);
+    const f2 OE = (d6 + d8) + (d17 - d18), OF = (d8 - d6) - (d17 + d18);
+    const f2 m4d4 = f2(-4.f) * d4, m4d6 = f2(-4.f) * d6, m4d8 = f2(-4.f) * d8;
+    h[0] = h0 - fma2(f2(-30.f), d1, f2(12.f) * d2);
+    h[1] -= EX + m4d4;
+    h[2] -= EX - m4d4;
+    h[3] -= EY + m4d6;
+    h[4] -= EY - m4d6;
+    h[5] -= EZ + m4d8;
+    h[6] -= EZ - m4d8;
+    const f2 eA = GHp + d13, eB = GHp - d13, eC = GHm + d15, eD = GHm - d15, eE = G2H + d14, eF = G2H - d14;
+    h[7] -= eA + OA;
+    h[10] -= eA - OA;
+    h[8] -= eB + OB;
+    h[9] -= eB - OB;
+    h[11] -= eC + OC;
+    h[14] -= eC - OC;
+    h[12] -= eD + OD;
+    h[13] -= eD - OD;
+    h[15] -= eE + OE;
+    h[18] -= eE - OE;
+    h[16] -= eF + OF;
+    h[17] -= eF - OF;
+    if (REF) h[18] = f2((float)(-sigma * rest_shift(19, LBM_MRT, 18)) * S);  // f18 = 0
+}
+
+// D2Q9 MRT in h units (CellFunctions.cu:7-63 basis and rates); REF keeps the
+// reference's energy equilibria with the extra density factor.
+template <bool REF>
+__device__ __forceinline__ void collide_mrt9_x2(f2 (&h)[9], f2 rho, f2 ux, f2 uy, float omega, float sigma,
+                                                float S) {
+    const f2 usq = fma2(ux, ux, uy * uy);
+    const f2 ef = REF ? rho : f2(1.f);
+    const f2 Sv(S);
+    const f2 rs = rho * usq * ef;
+    f2 E[9];
+    E[0] = 0.f;
+    E[1] = Sv * fma2(f2(3.f), rs, f2(-2.f) * (rho - f2(sigma)));
+    E[2] = Sv * fma2(f2(-3.f), rs, rho - f2(sigma));
+    E[3] = Sv * (rho * ux);
+    E[4] = -E[3];
+    E[5] = Sv * (rho * uy);
+    E[6] = -E[5];
+    E[7] = Sv * (rho * (ux * ux - uy * uy));
+    E[8] = Sv * (rho * (ux * uy));
+    const float s[9] = {0.f, 1.4f, 1.4f, 0.f, 1.2f, 0.f, 1.2f, omega, omega};
+    f2 dm[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        if (s[k] == 0.f) {
+            dm[k] = 0.f;
+            continue;
+        }
+        f2 m = 0.f;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const int c = mrt2(k, i);
+            if (c == 1) m += h[i];
+            else if (c == -1) m -= h[i];
+            else if (c != 0) m = fma2(f2((float)c), h[i], m);
+        }
+        dm[k] = f2(s[k] / (float)mrt2_norm(k)) * (m - E[k]);
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        f2 c = 0.f;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const int mk = mrt2(k, i);
+            if (s[k] == 0.f || mk == 0) continue;
+            if (mk == 1) c += dm[k];
+            else if (mk == -1) c -= dm[k];
+            else c = fma2(f2((float)mk), dm[k], c);
+        }
+        h[i] -= c;
+    }
+}
+
+template <int Q, int COLL, bool PHYS>
+__device__ __forceinline__ void collide_x2(f2 (&h)[Q], f2 rho, f2 ux, f2 uy, f2 uz, const StepParams &p,
+                                           float sigma, float S) {
+    if (COLL == LBM_BGKW) {
+        collide_bgk_x2<Q>(h, rho, ux, uy, uz, (float)p.omega, sigma, S);
+    } else if (COLL == LBM_TRT) {
+        collide_trt_x2<Q>(h, rho, ux, uy, uz, (float)p.omega, (float)p.omega_m, sigma, S);
+    } else {
+        if constexpr (Q == 9)
+            collide_mrt9_x2<!PHYS>(h, rho, ux, uy, (float)p.omega, sigma, S);
+        else
+            collide_mrt19_x2<!PHYS>(h, rho, ux, uy, uz, (float)p.omega, sigma, S);
+    }
+}
+
+constexpr int X2_BLOCK = 128;
+
+template <int Q, int COLL, int ST, bool PHYS>
+__global__ void __launch_bounds__(X2_BLOCK) step_kernel_x2(const StepParams p) {
+    using L = Lat<Q>;
+    using T = typename Store<ST>::T;
+    using PS = Pair<ST>;
+    constexpr bool F16 = ST == LBM_STORE_F16S;
+    const float sigma = F16 ? 1.f : 0.f;
+    const float S = F16 ? p.scale : 1.f;
+    const float invS = F16 ? p.inv_scale : 1.f;
+
+    const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = blockIdx.y, z = blockIdx.z;
+    const bool in_row = x0 < p.nx;
+    const int node = x0 + p.nx * (y + p.ny * z);
+    uint2 wp = make_uint2(0u, 0u);
+    if (in_row) wp = __ldg((const uint2 *)(p.word + node));
+    const bool fl0 = (wp.x & W_FLUID) != 0, fl1 = (wp.y & W_FLUID) != 0;
+    const unsigned warp_fluid = __ballot_sync(0xffffffffu, fl0 || fl1);
+    if (!fl0 && !fl1) {
+        if (in_row && warp_fluid) {
+#pragma unroll
+            for (int d = 0; d < Q; ++d)
+                PS::store((T *)p.fout[d] + node, f2(-p.shift[d] * S));
+        }
+        return;
+    }
+
+    const int plane = p.nx * p.ny;
+    const int oym = y == 0 ? (p.ny - 1) * p.nx : -p.nx, oyp = y == p.ny - 1 ? (1 - p.ny) * p.nx : p.nx;
+    const int ozm = z == 0 ? (p.nz - 1) * plane : -plane, ozp = z == p.nz - 1 ? (1 - p.nz) * plane : plane;
+    // x offsets of the pair's pulls: from x - 1 and from x + 1 (wrapped)
+    const int oxm0 = x0 == 0 ? p.nx - 1 : -1;              // node x0 pulling from x0 - 1
+    const int oxp1 = x0 + 2 >= p.nx ? 1 - p.nx + 0 : 1;     // node x0 + 1 pulling from x0 + 2
+
+    // All loads first, none of their values used before the last is issued:
+    // each element's address already selects the pull source or, across a
+    // blocked link, the node's own population (direction d in reference
+    // mode, opp(d) for half-way bounce-back), so there is no branch between
+    // loads and the memory system sees every request of the thread at once.
+    float hx[Q], hy[Q];
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+        const int oyz = (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
+                        (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
+        const int s0 = node + oyz + (L::cx(d) == 1 ? oxm0 : (L::cx(d) == -1 ? 1 : 0));
+        const int s1 = node + 1 + oyz + (L::cx(d) == 1 ? -1 : (L::cx(d) == -1 ? oxp1 : 0));
+        const T *pull = (const T *)p.fin[d];
+        if (d == 0) {
+            hx[0] = PS::load1(pull + node);
+            hy[0] = PS::load1(pull + node + 1);
+            continue;
+        }
+        const T *own = (const T *)p.fin[PHYS ? L::opp(d) : d];
+        const bool b0 = (wp.x >> d) & 1u, b1 = (wp.y >> d) & 1u;
+        hx[d] = PS::load1(b0 ? own + node : pull + s0);
+        hy[d] = PS::load1(b1 ? own + node + 1 : pull + s1);
+    }
+    const unsigned warp_blocked = __reduce_or_sync(0xffffffffu, (wp.x | wp.y) & 0x7FFFEu);
+    f2 h[Q];
+#pragma unroll
+    for (int d = 0; d < Q; ++d) h[d] = f2(hx[d], hy[d]);
+
+    bool keep0 = false, keep1 = false, zv0 = false, zv1 = false;
+    if (((wp.x | wp.y) & W_SPECIAL) != 0) {
+        // boundary nodes: to f, scalar boundary code, back to h
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const uint32_t we = e ? wp.y : wp.x;
+            if (!(we & W_SPECIAL) || !(we & W_FLUID)) continue;
+            float f[Q];
+#pragma unroll
+            for (int d = 0; d < Q; ++d)
+                f[d] = fmaf(e ? h[d].v.y : h[d].v.x, invS, p.shift[d]);
+            const int nd = node + e;
+            const int sl = __ldg(p.slot + nd);
+            const float u0 = (float)__ldg(p.bc_uvw + 3 * sl), v0 = (float)__ldg(p.bc_uvw + 3 * sl + 1),
+                        w0 = (float)__ldg(p.bc_uvw + 3 * sl + 2);
+            bool keep = false, zv = false;
+            if constexpr (!PHYS) {
+                const unsigned long long mk = __ldg(p.bc_mask + sl);
+                if constexpr (Q == 9)
+                    bc_ref_d2q9<float>(f, (uint32_t)mk, u0, p.outlet_profile, zv);
+                else
+                    bc_ref_d3q19<float>(f, mk, u0, v0, w0, p.update_inlet_outlet, keep);
+            } else {
+                const int kind = __ldg(p.bc_kind + sl);
+                if (kind & BCK_ACTIVE) {
+                    const float rset = (kind & BCK_OUTLET) ? (float)p.rho_out : (float)p.rho_in;
+                    bc_phys<Q, float>(f, kind & BCK_FACE_MASK, (kind & BCK_PRESSURE) != 0, rset, u0, v0, w0);
+                }
+            }
+#pragma unroll
+            for (int d = 0; d < Q; ++d) {
+                const float hv = (f[d] - p.shift[d]) * S;
+                if (e) h[d].v.y = hv; else h[d].v.x = hv;
+            }
+            if (e) { keep1 = keep; zv1 = zv; } else { keep0 = keep; zv0 = zv; }
+        }
+        if constexpr (!PHYS) {
+            // reference straight walls of the plain wall node of the pair
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const uint32_t we = e ? wp.y : wp.x;
+                if ((we & W_SPECIAL) || !(we & W_FLUID)) continue;
+#pragma unroll
+                for (int dir = 1; dir < Q; ++dir)
+                    if ((we >> L::opp(dir)) & 1u) {
+                        if (e) h[L::opp(dir)].v.y = h[dir].v.y; else h[L::opp(dir)].v.x = h[dir].v.x;
+                    }
+            }
+        }
+    } else if constexpr (!PHYS) {
+        if (warp_blocked) {
+#pragma unroll
+            for (int dir = 1; dir < Q; ++dir) {
+                const int o = L::opp(dir);
+                const bool b0 = (wp.x >> o) & 1u, b1 = (wp.y >> o) & 1u;
+                h[o] = f2(b0 ? h[dir].v.x : h[o].v.x, b1 ? h[dir].v.y : h[o].v.y);
+            }
+        }
+    }
+
+    // macroscopic moments: rho = sigma + sum(h)/S, j = sum(c h)/S
+    f2 sum = h[0], jx = 0.f, jy = 0.f, jz = 0.f;
+#pragma unroll
+    for (int d = 1; d < Q; ++d) {
+        sum += h[d];
+        if (L::cx(d) == 1) jx += h[d]; else if (L::cx(d) == -1) jx -= h[d];
+        if (L::cy(d) == 1) jy += h[d]; else if (L::cy(d) == -1) jy -= h[d];
+        if (L::cz(d) == 1) jz += h[d]; else if (L::cz(d) == -1) jz -= h[d];
+    }
+    f2 rho = fma2(sum, f2(invS), f2(sigma));
+    const f2 irho(1.f / rho.v.x, 1.f / rho.v.y);
+    const f2 sc = irho * f2(invS);
+    f2 ux = fma2(jx, sc, f2((float)p.gshift)), uy = jy * sc, uz = jz * sc;
+    if (zv0) uy.v.x = 0.f;
+    if (zv1) uy.v.y = 0.f;
+    if (keep0 || keep1) {
+        if (keep0) {
+            rho.v.x = p.rho[node]; ux.v.x = p.ux[node]; uy.v.x = p.uy[node]; uz.v.x = p.uz[node];
+        }
+        if (keep1) {
+            rho.v.y = p.rho[node + 1]; ux.v.y = p.ux[node + 1]; uy.v.y = p.uy[node + 1]; uz.v.y = p.uz[node + 1];
+        }
+    }
+    if (p.write_macro) {
+        if (!keep0 && fl0) { p.rho[node] = rho.v.x; p.ux[node] = ux.v.x; p.uy[node] = uy.v.x; p.uz[node] = uz.v.x; }
+        if (!keep1 && fl1) {
+            p.rho[node + 1] = rho.v.y; p.ux[node + 1] = ux.v.y; p.uy[node + 1] = uy.v.y; p.uz[node + 1] = uz.v.y;
+        }
+    }
+
+    collide_x2<Q, COLL, PHYS>(h, rho, ux, uy, uz, p, sigma, S);
+
+    // a solid node of a mixed pair keeps the zero encoding
+    if (!fl0 || !fl1) {
+#pragma unroll
+        for (int d = 0; d < Q; ++d) {
+            const float z0 = -p.shift[d] * S;
+            if (!fl0) h[d].v.x = z0;
+            if (!fl1) h[d].v.y = z0;
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < Q; ++d) PS::store((T *)p.fout[d] + node, h[d]);
+}
+
+}  // namespace lbm

@@ -1,0 +1,144 @@
+"""Host side of the colour-gradient two-phase D2Q9 path.
+
+Mirrors the reference's multiphase 2D driver pieces around the time step:
+`create_bubble` is createBubble test case 1 (Multiphase.cu:325-356),
+`predicted_surface_tension` the prediction of Iterate.cu:163-168 and
+`surface_tension_error` calculateSurfaceTension (Multiphase.cu:1082-1091)
+applied to the Laplace-law sums (Iterate.cu:496-499).  The step itself runs
+in the CUDA library (`lbm_cg_*` in include/thesis_lbm.h); this module only
+marshals arrays.
+"""
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import native as N
+
+
+@dataclass
+class CgArguments:
+    """The multiphase fields of the reference's Arguments
+    (include/Arguments.h:112-131)."""
+    r_density: float = 1.0
+    b_density: float = 1.0
+    r_alpha: float = 4.0 / 9.0
+    b_alpha: float = 4.0 / 9.0
+    r_viscosity: float = 1.0 / 6.0
+    b_viscosity: float = 1.0 / 6.0
+    beta: float = 0.7
+    A: float = 0.005
+    g_limit: float = 0.0
+    control_param: float = 0.9
+    high_order: bool = False
+    enhanced_distrib: bool = False
+    bubble_radius: float = 0.2
+
+    def to_c(self):
+        return N.CgParams(self.r_alpha, self.b_alpha, self.r_viscosity, self.b_viscosity, self.beta,
+                          self.A, self.g_limit, self.control_param, int(bool(self.high_order)),
+                          int(bool(self.enhanced_distrib)), N.STORE_F32)
+
+
+def rest_weights(alpha):
+    """phi_k of a colour at rest (GpuInit.cu:323-360): alpha, (1-alpha)/5 on
+    the axes, (1-alpha)/20 on the diagonals."""
+    return np.array([alpha] + [(1 - alpha) / 5] * 4 + [(1 - alpha) / 20] * 4)
+
+
+def create_bubble(n, m, args: CgArguments, x=None, y=None):
+    """Red bubble of radius `args.bubble_radius` (in the node coordinates'
+    units) centred at (0.5, 0.5), blue around it, both at rest.  x, y default
+    to i/(n-1), j/(m-1).  Returns post-streaming red and blue populations,
+    (9, n*m) float64 each, in SoA order."""
+    if x is None or y is None:
+        j, i = np.divmod(np.arange(n * m), n)
+        x, y = i / (n - 1), j / (m - 1)
+    inside = np.sqrt((np.asarray(x) - 0.5) ** 2 + (np.asarray(y) - 0.5) ** 2) <= args.bubble_radius
+    r = np.where(inside[None, :], (args.r_density * rest_weights(args.r_alpha))[:, None], 0.0)
+    b = np.where(~inside[None, :], (args.b_density * rest_weights(args.b_alpha))[:, None], 0.0)
+    return np.ascontiguousarray(r), np.ascontiguousarray(b)
+
+
+def predicted_surface_tension(args: CgArguments):
+    """sigma = 4 A / (9 omega_eff) with omega_eff from the density-weighted
+    harmonic mean viscosity (Iterate.cu:163-168)."""
+    rd, bd = args.r_density, args.b_density
+    mean_nu = 1.0 / (rd / ((rd + bd) * args.r_viscosity) + bd / ((rd + bd) * args.b_viscosity))
+    omega_eff = 1.0 / (3.0 * mean_nu + 0.5)
+    return 4.0 * args.A / 9.0 / omega_eff
+
+
+def surface_tension_error(laplace, args: CgArguments, radius_nodes):
+    """Percent error of the Laplace-law surface tension R (p_in - p_out),
+    p = (3/5)(1 - alpha) rho_colour averaged over each phase
+    (Multiphase.cu:1082-1091), against the prediction."""
+    p_in = laplace[0] / laplace[1] if laplace[1] > 0 else 0.0
+    p_out = laplace[2] / laplace[3] if laplace[3] > 0 else 0.0
+    p_in *= 3.0 / 5.0 * (1.0 - args.r_alpha)
+    p_out *= 3.0 / 5.0 * (1.0 - args.b_alpha)
+    st = radius_nodes * (p_in - p_out)
+    pred = predicted_surface_tension(args)
+    return abs(pred - st) / pred * 100.0
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class CgSolver:
+    """One periodic n x m colour-gradient lattice on the GPU."""
+
+    def __init__(self, n, m, args: CgArguments):
+        self.n, self.m, self.args = n, m, args
+        self._lib = N.lib()
+        h = C.c_void_p()
+        p = args.to_c()
+        N.check_cg(self._lib.lbm_cg_create(n, m, C.byref(p), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.lbm_cg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def init(self, r_f, b_f):
+        r = np.ascontiguousarray(r_f, np.float32).reshape(-1)
+        b = np.ascontiguousarray(b_f, np.float32).reshape(-1)
+        if r.size != 9 * self.n * self.m or b.size != r.size:
+            raise ValueError("populations must hold 9*n*m values per colour")
+        N.check_cg(self._lib.lbm_cg_init(self._h, _fp(r), _fp(b)))
+
+    def step(self, nsteps, write_macro=True, stream=None):
+        N.check_cg(self._lib.lbm_cg_step(self._h, int(nsteps), int(bool(write_macro)),
+                                         None if stream is None else C.c_void_p(stream)))
+
+    def macro(self):
+        out = [np.empty(self.n * self.m, np.float32) for _ in range(4)]
+        N.check_cg(self._lib.lbm_cg_get_macro(self._h, *[_fp(a) for a in out]))
+        return out
+
+    def populations(self):
+        r = np.empty(9 * self.n * self.m, np.float32)
+        b = np.empty_like(r)
+        N.check_cg(self._lib.lbm_cg_get_populations(self._h, _fp(r), _fp(b)))
+        return r.reshape(9, -1), b.reshape(9, -1)
+
+    def laplace(self):
+        out = np.zeros(5, np.float64)
+        rc = self._lib.lbm_cg_laplace(self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc not in (N.LBM_OK, N.LBM_DIVERGED):
+            N.check_cg(rc)
+        return out, rc

@@ -40,6 +40,14 @@ class Params(C.Structure):
                 ("periodic", C.c_int * 3), ("init_equilibrium", C.c_int)]
 
 
+class CgParams(C.Structure):
+    _fields_ = [("r_alpha", C.c_double), ("b_alpha", C.c_double),
+                ("r_viscosity", C.c_double), ("b_viscosity", C.c_double),
+                ("beta", C.c_double), ("A", C.c_double), ("g_limit", C.c_double),
+                ("control_param", C.c_double), ("high_order", C.c_int), ("enhanced", C.c_int),
+                ("storage", C.c_int)]
+
+
 _lib = None
 
 
@@ -73,10 +81,20 @@ def lib():
         "lbm_status": (C.c_int, [vp]),
         "lbm_fluid_nodes": (C.c_longlong, [vp]),
         "lbm_bytes_per_update": (C.c_int, [vp]),
+        "lbm_kernel_variant": (C.c_int, [vp]),
         "lbm_destroy": (None, [vp]),
         "lbm_build_flags": (C.c_int, [C.POINTER(LatticeDesc), C.POINTER(Params),
                                       C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
                                       C.POINTER(C.c_int32), C.POINTER(C.c_int)]),
+        "lbm_cg_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(CgParams), C.POINTER(vp)]),
+        "lbm_cg_init": (C.c_int, [vp, fp, fp]),
+        "lbm_cg_step": (C.c_int, [vp, C.c_int, C.c_int, vp]),
+        "lbm_cg_get_macro": (C.c_int, [vp, fp, fp, fp, fp]),
+        "lbm_cg_get_populations": (C.c_int, [vp, fp, fp]),
+        "lbm_cg_laplace": (C.c_int, [vp, dp]),
+        "lbm_cg_nodes": (C.c_longlong, [vp]),
+        "lbm_cg_last_error": (C.c_char_p, []),
+        "lbm_cg_destroy": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -95,4 +113,10 @@ class LbmError(RuntimeError):
 def check(rc):
     if rc != LBM_OK:
         raise LbmError(rc, lib().lbm_last_error().decode(errors="replace"))
+    return rc
+
+
+def check_cg(rc):
+    if rc != LBM_OK:
+        raise LbmError(rc, lib().lbm_cg_last_error().decode(errors="replace"))
     return rc
