@@ -53,7 +53,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", default="64,64,128", help="n,m,h of the CPU-baseline sample")
-    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                    help="target CPU time of one CPU-baseline sample (steps are chosen to fill it)")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "jit", "tma", "pair", "scalar"],
+                    help="step kernel (auto: the library's default for the storage)")
     return ap.parse_args()
 
 
@@ -150,10 +153,14 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(storage, n, m, h):
-    """DRAM bytes per launch from the committed ncu summary, scaled to this
-    lattice by node count (None when no summary covers this storage)."""
-    path = os.path.join(ROOT, "profiles", "step_kernel_d3q19_mrt_%s_sphere_duct.txt" % storage)
+KERNEL_NAMES = {1: "step_kernel", 2: "step_kernel_x2", 3: "step_kernel_tma", 4: "step_kernel_fixed"}
+
+
+def profiled_traffic(kernel, storage, n, m, h):
+    """DRAM bytes per launch from the committed ncu summary of this kernel and
+    storage, scaled to this lattice by node count (None when no summary
+    covers them)."""
+    path = os.path.join(ROOT, "profiles", "%s_d3q19_mrt_%s_sphere_duct.txt" % (kernel, storage))
     try:
         text = open(path).read()
     except OSError:
@@ -170,9 +177,11 @@ def profiled_traffic(storage, n, m, h):
     return per_node * n * m * h
 
 
-def cpu_baseline_run(sample, steps, threads=None):
+def cpu_baseline_run(sample, seconds, threads=None):
     """Oracle restatement of the reference kernels (physics mode, FP32) on a
-    bounded sample of the workload; returns (GLUPS, threads, description)."""
+    bounded sample of the workload: a few steps estimate the step time, then
+    enough steps to fill about `seconds` are timed.  Returns (GLUPS, threads,
+    description)."""
     from oracle import pyoracle
     L = pyoracle.oracle_lib()
     if threads:
@@ -183,8 +192,11 @@ def cpu_baseline_run(sample, steps, threads=None):
     kw = dict(viscosity=(WORKLOAD["tau"] - 0.5) / 3.0, collision_model=3, inlet_profile=4, outlet_profile=5)
     nn = lat.num_nodes
     init = (np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
-    pyoracle.run_oracle(lat, 1, mode=1, init_kind=1, rho_in=WORKLOAD["rho_in"],
-                        rho_out=WORKLOAD["rho_out"], init=init, **kw)  # warm the page cache / pools
+    t0 = time.perf_counter()
+    pyoracle.run_oracle(lat, 3, mode=1, init_kind=1, rho_in=WORKLOAD["rho_in"],
+                        rho_out=WORKLOAD["rho_out"], init=init, **kw)  # estimate; warms pools
+    est = (time.perf_counter() - t0) / 3
+    steps = int(min(max(seconds / max(est, 1e-6), 3), 100000))
     t0 = time.perf_counter()
     r = pyoracle.run_oracle(lat, steps, mode=1, init_kind=1, rho_in=WORKLOAD["rho_in"],
                             rho_out=WORKLOAD["rho_out"], init=init, **kw)
@@ -202,10 +214,9 @@ def run_reference_arm(args, rank, world):
     sample = tuple(int(x) for x in args.cpu_sample.split(","))
     n, m, h = (int(x) for x in args.size.split(",")) if args.size else (WORKLOAD["n"], WORKLOAD["m"], WORKLOAD["h"])
     per = []
-    for _ in range(max(args.warmup and 1, 0)):
-        cpu_baseline_run(sample, 2)
-    for _ in range(max(args.steps // 100, 1)):
-        g, threads, desc = cpu_baseline_run(sample, args.cpu_steps)
+    # every sample is about args.cpu_seconds / 3 of CPU work, at most 5 samples
+    for _ in range(min(max(args.steps // 100, 1), 5)):
+        g, threads, desc = cpu_baseline_run(sample, args.cpu_seconds / 3)
         per.append(g)
     value = statistics.median(per)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GLUPS",
@@ -231,6 +242,8 @@ def main():
     from thesis_gb300 import native as N
     from thesis_gb300.solver import Solver
 
+    if args.kernel != "auto":
+        os.environ["THESIS_LBM_KERNEL"] = args.kernel
     if world > 1:
         torch.cuda.set_device(local)
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
@@ -247,8 +260,11 @@ def main():
 
     # ---- value: state resident in HBM, CUDA events on the launch stream ----
     s = Solver(lat, sargs)
+    variant = N.lib().lbm_kernel_variant(s._h)
+    knobs = s.autotune(20) if variant == 4 else s.kernel_config()
     s.init(rho0, zero, zero, zero)
     fluid = s.fluid_nodes
+    kernel = KERNEL_NAMES.get(variant, "?")
     stream = torch.cuda.Stream(device=dev)
     with torch.cuda.stream(stream):
         s.step(args.warmup, write_macro=False, stream=stream.cuda_stream)
@@ -283,7 +299,7 @@ def main():
     alg_bytes = B_LU[storage] * fluid
     peak, peak_kind = measured_peak()
     achieved = alg_bytes / per_launch_s / 1e9
-    traffic = profiled_traffic(args.storage, n, m, h)
+    traffic = profiled_traffic(kernel, args.storage, n, m, h)
 
     # ---- e2e: whole run through the C ABI from host buffers ----
     e2e = None
@@ -315,7 +331,7 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         sample = tuple(int(x) for x in args.cpu_sample.split(","))
-        g, threads, desc = cpu_baseline_run(sample, args.cpu_steps)
+        g, threads, desc = cpu_baseline_run(sample, args.cpu_seconds)
         cpu = {"value": g, "unit": "GLUPS", "cores": threads, "kind": "port", "sample": desc}
 
     if rank == 0:
@@ -323,7 +339,9 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic (seeded sphere packing)",
-                "config": workload_config(args, n, m, h),
+                "config": dict(workload_config(args, n, m, h), kernel=kernel,
+                               kernel_knobs={"block": knobs[0], "l2_256B_loads": knobs[1],
+                                             "predicated_bounce_back": knobs[2]}),
                 "fluid_nodes_per_gpu": fluid, "status": status,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind,

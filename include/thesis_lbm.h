@@ -74,6 +74,10 @@ extern "C" {
 #define LBM_BC_PERIODIC 4
 #define LBM_BC_SYMMETRY 5
 
+/* The constants above are shared with the CUDA kernels, which the library
+ * also compiles at run time (NVRTC), where host declarations are not allowed. */
+#ifndef __CUDACC_RTC__
+
 typedef struct lbm_handle_s *lbm_handle;
 
 /* A lattice as the reference reads it: the Node file columns (i, j, [k,]
@@ -145,6 +149,13 @@ int lbm_get_populations(lbm_handle h, double *f);
 #define LBM_NORMS 5
 int lbm_macro_norms(lbm_handle h, double *out);
 
+/* The reference's MaxMacroDiff residual (Iterate3D.cu:696-735): out[0..3] =
+ * max over all nodes of |u - u_prev|, |v - v_prev|, |w - w_prev|,
+ * |rho - rho_prev| for the last stored macroscopic fields, where _prev is the
+ * field at the previous call (the initial fields before the first); out[4] =
+ * number of non-finite differences.  Returns LBM_DIVERGED when out[4] > 0. */
+int lbm_macro_diff(lbm_handle h, double *out);
+
 /* The same FP64 norms as lbm_macro_norms, for callers that must not allocate
  * device memory while they run (for example a host framework that owns a
  * fixed device arena and forbids cudaMalloc/cudaFree inside its step
@@ -171,10 +182,33 @@ int lbm_status(lbm_handle h);
 /* Number of fluid nodes (the lattice updates one step performs). */
 long long lbm_fluid_nodes(lbm_handle h);
 
-/* Nodes one thread of the step kernel advances: 2 for the pair kernel (even
- * n, F32/F16S storage), 1 otherwise (or when THESIS_LBM_KERNEL=scalar is set
- * in the environment at lbm_create). */
+/* Step kernel of the handle, chosen at lbm_create: 4 (the default) the
+ * one-node kernel specialised for this lattice's extents at run time, 1 the
+ * compiled-in one-node kernel (used when the run-time build is unavailable),
+ * 2 two nodes per thread (even n, F32/F16S), 3 the row-staged bulk-copy
+ * kernel.  THESIS_LBM_KERNEL=scalar|pair|tma|jit in the environment at
+ * lbm_create selects one; a variant the lattice does not admit falls back to
+ * 1, except jit, whose build failure lbm_create reports. */
 int lbm_kernel_variant(lbm_handle h);
+
+/* Autotuner of the run-time specialised kernel: builds its variants (block
+ * of 128 or 256 threads along x; plain or L2-256-byte-prefetching loads;
+ * bounce-back by selected address or by predicated loads), times
+ * trial_steps steps of each on the handle's stream and keeps the fastest,
+ * also for handles created later in the process on the same lattice and
+ * parameters.  The trial steps leave the populations undefined: call
+ * lbm_init afterwards.  The chosen knobs go to block, hint, pred (may be
+ * NULL).  This function has no counterpart in the reference. */
+int lbm_autotune(lbm_handle h, int trial_steps, int *block, int *hint, int *pred);
+/* The knobs of the handle's step kernel (defaults 128, 0, 0). */
+int lbm_kernel_config(lbm_handle h, int *block, int *hint, int *pred);
+
+/* Compile (no GPU needed, nothing is loaded) the run-time specialised step
+ * kernel for the given template arguments and knobs (as lbm_autotune): a
+ * build check of the sources the library embeds.  Returns LBM_OK or LBM_ERR_CUDA with the compiler log in
+ * lbm_last_error(). */
+int lbm_jit_check(int q, int coll, int storage, int phys, int wrap, int nx, int ny, int nz, int block, int hint,
+                  int pred);
 
 /* Bytes of HBM one step moves per fluid node for the populations alone. */
 int lbm_bytes_per_update(lbm_handle h);
@@ -251,6 +285,8 @@ void lbm_cg_destroy(lbm_cg_handle h);
 
 /* Library version, for load checks. */
 int lbm_version(void);
+
+#endif /* __CUDACC_RTC__ */
 
 #ifdef __cplusplus
 }

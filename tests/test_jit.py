@@ -1,0 +1,125 @@
+"""Run-time specialised step kernel (THESIS_LBM_KERNEL=jit): the embedded
+sources compile with NVRTC (CPU, no GPU needed), and on the GPU the kernel
+matches the oracle with the tolerances of test_gpu_parity."""
+import numpy as np
+import pytest
+
+from thesis_gb300 import lattice
+from thesis_gb300 import native as N
+from thesis_gb300.solver import Arguments, Solver
+
+
+@pytest.mark.parametrize("q,coll,storage,phys,wrap,dims,knobs", [
+    (19, N.MRT, N.STORE_F16S, 1, 0, (256, 256, 512), (128, 0, 0)),
+    (19, N.MRT, N.STORE_F16S, 1, 0, (256, 256, 512), (256, 1, 1)),
+    (19, N.BGKW, N.STORE_F64, 0, 1, (12, 10, 9), (128, 1, 0)),
+    (9, N.TRT, N.STORE_F32, 1, 1, (160, 48, 1), (256, 0, 1)),
+    (9, N.MRT, N.STORE_F32, 0, 1, (32, 24, 1), (128, 0, 0)),
+])
+def test_jit_sources_compile(native_lib, q, coll, storage, phys, wrap, dims, knobs):
+    rc = native_lib.lbm_jit_check(q, coll, storage, phys, wrap, *dims, *knobs)
+    assert rc == N.LBM_OK, native_lib.lbm_last_error().decode()
+
+
+@pytest.fixture
+def jit(monkeypatch):
+    monkeypatch.setenv("THESIS_LBM_KERNEL", "jit")
+    yield
+    monkeypatch.delenv("THESIS_LBM_KERNEL", raising=False)
+
+
+def _rest(nn):
+    return (np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
+
+
+def _check(oracle, lat, args, steps, init, dims, storage):
+    from test_gpu_parity import compare, run_pair
+    with Solver(lat, args) as s:
+        assert N.lib().lbm_kernel_variant(s._h) == 4
+    g, r, fl = run_pair(oracle, lat, args, steps, init=init)
+    compare(g, r, fl, storage, dims)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("coll", [N.BGKW, N.TRT, N.MRT])
+@pytest.mark.parametrize("storage", [N.STORE_F32, N.STORE_F16S, N.STORE_F64])
+def test_jit_sphere_duct(oracle, jit, coll, storage):
+    lat = lattice.sphere_duct(24, 20, 48, porosity=0.75, rmin=3, rmax=5, seed=7)
+    args = Arguments(viscosity=(0.8 - 0.5) / 3, collision_model=coll, mode=N.MODE_PHYSICS, storage=storage,
+                     init_equilibrium=1, inlet_profile=N.INLET_PRESSURE, outlet_profile=N.OUTLET_PRESSURE,
+                     rho_in=1.005, rho_out=1.0)
+    _check(oracle, lat, args, 40, _rest(lat.num_nodes), 3, storage)
+
+
+@pytest.mark.gpu
+def test_jit_periodic_duct(oracle, jit):
+    lat = lattice.sphere_duct(32, 24, 40, porosity=0.8, rmin=3, rmax=5, seed=4)
+    args = Arguments(viscosity=0.1, collision_model=N.MRT, mode=N.MODE_PHYSICS, init_equilibrium=1,
+                     inlet_profile=N.INLET_PRESSURE, outlet_profile=N.OUTLET_PRESSURE, rho_in=1.005,
+                     periodic=(1, 1, 0))
+    _check(oracle, lat, args, 40, _rest(lat.num_nodes), 3, N.STORE_F32)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("coll", [N.BGKW, N.MRT])
+def test_jit_reference_cavities(oracle, jit, coll):
+    lat = lattice.cavity2d(32, 24)
+    args = Arguments(u=0.1, viscosity=0.128, collision_model=coll, outlet_profile=N.OUTLET_ZOUHE)
+    _check(oracle, lat, args, 60, None, 2, N.STORE_F32)
+    lat = lattice.cavity3d(12, 10, 9)
+    args = Arguments(u=0.05, viscosity=0.1, collision_model=coll)
+    _check(oracle, lat, args, 25, None, 3, N.STORE_F32)
+
+
+@pytest.mark.gpu
+def test_jit_channel2d(oracle, jit):
+    lat = lattice.channel2d(160, 48, seed=5)
+    args = Arguments(u=0.05, viscosity=0.05, collision_model=N.TRT, mode=N.MODE_PHYSICS,
+                     init_equilibrium=1, outlet_profile=N.OUTLET_PRESSURE, rho_out=1.0)
+    _check(oracle, lat, args, 60, _rest(lat.num_nodes), 2, N.STORE_F32)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", [N.STORE_F32, N.STORE_F16S, N.STORE_F64])
+def test_compiled_in_kernel_sphere_duct(oracle, monkeypatch, storage):
+    """The compiled-in one-node kernel (the fallback when the run-time build
+    is unavailable) against the oracle."""
+    monkeypatch.setenv("THESIS_LBM_KERNEL", "scalar")
+    lat = lattice.sphere_duct(24, 20, 48, porosity=0.75, rmin=3, rmax=5, seed=7)
+    args = Arguments(viscosity=(0.8 - 0.5) / 3, collision_model=N.MRT, mode=N.MODE_PHYSICS, storage=storage,
+                     init_equilibrium=1, inlet_profile=N.INLET_PRESSURE, outlet_profile=N.OUTLET_PRESSURE,
+                     rho_in=1.005, rho_out=1.0)
+    from test_gpu_parity import compare, run_pair
+    with Solver(lat, args) as s:
+        assert N.lib().lbm_kernel_variant(s._h) == 1
+    g, r, fl = run_pair(oracle, lat, args, 40, init=_rest(lat.num_nodes))
+    compare(g, r, fl, storage, 3)
+
+
+@pytest.mark.gpu
+def test_autotune_then_parity(oracle):
+    """lbm_autotune keeps one of its variants; after lbm_init the run matches
+    the oracle, and a second handle on the same lattice reuses the choice."""
+    from test_gpu_parity import compare
+    lat = lattice.sphere_duct(32, 24, 40, porosity=0.75, rmin=3, rmax=5, seed=9)
+    args = Arguments(viscosity=0.1, collision_model=N.MRT, mode=N.MODE_PHYSICS, storage=N.STORE_F32,
+                     init_equilibrium=1, inlet_profile=N.INLET_PRESSURE, outlet_profile=N.OUTLET_PRESSURE,
+                     rho_in=1.005)
+    nn = lat.num_nodes
+    with Solver(lat, args) as s:
+        knobs = s.autotune(6)
+        assert knobs[0] in (128, 256) and knobs[1] in (0, 1) and knobs[2] in (0, 1)
+        with pytest.raises(N.LbmError):
+            s.step(1)  # populations undefined until init
+        s.init(*_rest(nn))
+        s.step(30, write_macro=True)
+        rho, u, v, w = s.macro()
+        f = s.populations()
+        with Solver(lat, args) as s2:
+            assert s2.kernel_config() == knobs
+    r = oracle.run_oracle(lat, 30, mode=N.MODE_PHYSICS, init_kind=1, rho_in=1.005, rho_out=1.0,
+                          extra_collide=True, init=_rest(nn), viscosity=0.1, collision_model=N.MRT,
+                          inlet_profile=N.INLET_PRESSURE, outlet_profile=N.OUTLET_PRESSURE)
+    g = dict(rho=rho.astype(np.float64), u=u.astype(np.float64), v=v.astype(np.float64),
+             w=w.astype(np.float64), f=f)
+    compare(g, r, lat.node_type == 1, N.STORE_F32, 3)

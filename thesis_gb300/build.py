@@ -25,8 +25,17 @@ def nvcc():
     return cand if os.path.exists(cand) else "nvcc"
 
 
+def cuda_include():
+    """Toolkit include directory (cuda_fp16.h for the run-time kernel build)."""
+    home = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    path = os.path.join(home, "include")
+    if not os.path.exists(os.path.join(path, "cuda_fp16.h")):
+        path = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "include")
+    return path
+
+
 CLI_DIR = os.path.join(CSRC, "cli")
-TOOLS = {"latticegen": "latticegen_main.cpp"}
+TOOLS = {"latticegen": "latticegen_main.cpp", "thesis_lbm_run": "lbm_run_main.cpp"}
 
 
 def sources():
@@ -45,6 +54,32 @@ def _newest_input():
     return max(os.path.getmtime(f) for f in files)
 
 
+# Headers the run-time specialised step kernel is compiled from (lbm_jit.cpp).
+JIT_HEADERS = [os.path.join(ROOT, "include", "thesis_lbm.h")] + [
+    os.path.join(CSRC, f) for f in ("lbm_types.h", "lbm_device.cuh", "lbm_bc.cuh", "lbm_step.cuh")]
+
+
+def write_jit_sources(path):
+    """Embed the kernel headers as C++ raw strings for NVRTC."""
+    delim = "LBMSRC"
+    parts, names = [], []
+    for h in JIT_HEADERS:
+        text = open(h).read()
+        if ")" + delim + '"' in text:
+            raise RuntimeError("raw-string delimiter found in " + h)
+        parts.append('R"%s(%s)%s"' % (delim, text, delim))
+        names.append('"%s"' % os.path.basename(h))
+    out = ["// generated by thesis_gb300/build.py: kernel headers for NVRTC",
+           "#pragma once",
+           "static const char *const kJitHeaders[] = {" + ",\n".join(parts) + "};",
+           "static const char *const kJitHeaderNames[] = {" + ", ".join(names) + "};",
+           "static const int kJitHeaderCount = %d;" % len(names)]
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        f.write("\n".join(out) + "\n")
+    os.replace(tmp, path)
+
+
 def _run(cmd):
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
@@ -59,8 +94,10 @@ def build(force=False, verbose=False):
                          for p in [LIB_PATH] + [tool_path(t) for t in TOOLS]):
         return LIB_PATH
     os.makedirs(OBJDIR, exist_ok=True)
+    write_jit_sources(os.path.join(OBJDIR, "jit_sources.h"))
     common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
-              "-I" + os.path.join(ROOT, "include"), "-I" + CSRC] + ARCH
+              "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-I" + OBJDIR,
+              '-DTHESIS_CUDA_INCLUDE="%s"' % cuda_include()] + ARCH
 
     def compile_one(src):
         obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
@@ -76,11 +113,14 @@ def build(force=False, verbose=False):
     with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB_PATH + ".tmp"
-    _run([nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart"])
+    cuda_lib = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "lib64")
+    _run([nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs +
+         ["-lcudart", "-lnvrtc", "-Xlinker", "-rpath," + cuda_lib])
     os.replace(tmp, LIB_PATH)
     for name, src in TOOLS.items():
         out = tool_path(name)
-        _run(["g++", "-O2", "-std=c++17", os.path.join(CLI_DIR, src), "-o", out + ".tmp",
+        _run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), os.path.join(CLI_DIR, src),
+              "-o", out + ".tmp",
               "-L" + LIBDIR, "-lthesis_lbm", "-Wl,-rpath,$ORIGIN"])
         os.replace(out + ".tmp", out)
     return LIB_PATH

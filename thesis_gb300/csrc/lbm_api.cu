@@ -7,11 +7,15 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <new>
+#include <thread>
 #include <string>
 #include <vector>
 
 #include "lbm_flags.h"
+#include "lbm_jit.h"
 #include "lbm_step_tma.cuh"
 
 namespace lbm {
@@ -27,6 +31,8 @@ int launch_norms(const uint32_t *word, const float *rho, const float *ux, const 
                  const float *uz, float *pux, float *puy, float *puz, long long n,
                  double *partial, double *out, cudaStream_t s);
 int norm_partial_count();
+int launch_macro_diff(const float *ux, const float *uy, const float *uz, const float *rho, float *pux, float *puy,
+                      float *puz, float *prho, long long n, double *partial, double *out, cudaStream_t s);
 int tma_prepare(int q, int coll, int st, size_t smem, int *blocks_per_sm);
 int launch_step_tma(int q, const StepParams &p, const TmaRows &rows, int coll, int st, int grid, size_t smem,
                     cudaStream_t s);
@@ -62,6 +68,7 @@ struct lbm_handle_s {
     double *uvw = nullptr;
     float *rho = nullptr, *ux = nullptr, *uy = nullptr, *uz = nullptr;
     float *pux = nullptr, *puy = nullptr, *puz = nullptr;
+    float *mdiff_prev = nullptr;  // u, v, w, rho at the last lbm_macro_diff (4 N floats)
     double *partial = nullptr, *norms = nullptr;
     int nslots = 0;
     std::vector<long long> slot_node;
@@ -72,6 +79,9 @@ struct lbm_handle_s {
     bool initialised = false;
     bool pair_kernel = false;  // two nodes per thread (even nx, F32/F16S)
     bool tma_kernel = false;   // row-staged bulk-copy kernel
+    bool jit_kernel = false;   // step kernel specialised for this lattice at run time
+    cudaKernel_t jit_fn = nullptr;
+    JitStepKey jit_key{};
     int32_t *tma_row = nullptr;
     uint32_t *tma_lmask = nullptr, *tma_omask = nullptr;
     unsigned int *tma_err = nullptr;
@@ -85,8 +95,9 @@ static StepParams make_params(const lbm_handle_s *H, int from, int write_macro) 
     StepParams p;
     memset(&p, 0, sizeof(p));
     for (int d = 0; d < H->q; ++d) {
-        p.fin[d] = (const char *)H->fbuf[from] + (size_t)d * H->stride * H->elem;
-        p.fout[d] = (char *)H->fbuf[1 - from] + (size_t)d * H->stride * H->elem;
+        // row layout: direction d of row r starts at (r * q + d) * n
+        p.fin[d] = (const char *)H->fbuf[from] + (size_t)d * H->n * H->elem;
+        p.fout[d] = (char *)H->fbuf[1 - from] + (size_t)d * H->n * H->elem;
     }
     p.word = H->word;
     p.slot = H->slot;
@@ -100,6 +111,7 @@ static StepParams make_params(const lbm_handle_s *H, int from, int write_macro) 
     p.nx = H->n;
     p.ny = H->m;
     p.nz = H->h;
+    p.pitch = H->q * H->n;
     p.write_macro = write_macro;
     p.omega = H->omega;
     p.omega_m = H->omega_m;
@@ -121,7 +133,7 @@ static void free_handle(lbm_handle_s *H) {
         if (H->pair[c]) cudaGraphExecDestroy(H->pair[c]);
     void *ptrs[] = {H->fbuf[0], H->fbuf[1], H->word, H->slot, H->mask, H->kind, H->uvw,
                     H->rho, H->ux, H->uy, H->uz, H->pux, H->puy, H->puz, H->partial, H->norms,
-                    H->tma_row, H->tma_lmask, H->tma_omask, H->tma_err};
+                    H->tma_row, H->tma_lmask, H->tma_omask, H->tma_err, H->mdiff_prev};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (H->stream) cudaStreamDestroy(H->stream);
@@ -207,6 +219,67 @@ static int setup_tma(lbm_handle_s *H, const std::vector<uint32_t> &word) {
     return LBM_OK;
 }
 
+// True when some fluid node pulls across an out-of-domain link that is not
+// blocked: the step must then wrap coordinates at the faces.
+template <int Q>
+static bool open_outside_links(const std::vector<uint32_t> &word, int n, int m, int h) {
+    using L = Lat<Q>;
+    for (int z = 0; z < h; ++z)
+        for (int y = 0; y < m; ++y) {
+            const bool face_row = y == 0 || y == m - 1 || z == 0 || z == h - 1;
+            for (int x = 0; x < n; x = (face_row || x == n - 1) ? x + 1 : n - 1) {
+                const uint32_t w = word[(size_t)x + (size_t)n * (y + (size_t)m * z)];
+                if (!(w & W_FLUID)) continue;
+                for (int d = 1; d < Q; ++d) {
+                    const int sx = x - L::cx(d), sy = y - L::cy(d), sz = z - L::cz(d);
+                    const bool outside = sx < 0 || sx >= n || sy < 0 || sy >= m || sz < 0 || sz >= h;
+                    if (outside && !((w >> d) & 1u)) return true;
+                }
+            }
+        }
+    return false;
+}
+
+// Knobs of the specialised kernel chosen by lbm_autotune, remembered per
+// lattice configuration for the rest of the process.
+struct TunedKnobs {
+    int block, hint;
+    bool pred;
+};
+static std::mutex g_tuned_mutex;
+static std::map<std::string, TunedKnobs> g_tuned;
+
+static std::string tune_key(const JitStepKey &k) {
+    char b[160];
+    snprintf(b, sizeof(b), "%d/%d/%d/%d/%d/%d/%d/%d", k.q, k.coll, k.storage, (int)k.phys, (int)k.wrap, k.nx,
+             k.ny, k.nz);
+    return b;
+}
+
+// Build the run-time specialised step kernel for this lattice.
+static int setup_jit(lbm_handle_s *H, const std::vector<uint32_t> &word) {
+    const bool periodic = H->P.mode == LBM_MODE_PHYSICS &&
+                          (H->P.periodic[0] || H->P.periodic[1] || (H->dims == 3 && H->P.periodic[2]));
+    const bool wrap = periodic || (H->q == 9 ? open_outside_links<9>(word, H->n, H->m, H->h)
+                                             : open_outside_links<19>(word, H->n, H->m, H->h));
+    JitStepKey k{H->q, H->P.collision_model, H->P.storage, H->P.mode == LBM_MODE_PHYSICS, wrap,
+                 H->n, H->m, H->h, STEP_BLOCK, 0, false, false};
+    {
+        std::lock_guard<std::mutex> lock(g_tuned_mutex);
+        auto it = g_tuned.find(tune_key(k));
+        if (it != g_tuned.end()) {
+            k.block = it->second.block;
+            k.hint = it->second.hint;
+            k.pred = it->second.pred;
+        }
+    }
+    std::string err;
+    if (jit_step_kernel(k, &H->jit_fn, err)) return fail(LBM_ERR_CUDA, "run-time kernel build: " + err);
+    H->jit_key = k;
+    H->jit_kernel = true;
+    return LBM_OK;
+}
+
 // A bounded wait inside the row-staged kernel that gave up leaves a code in
 // tma_err; report it once the stream is idle.
 static int check_tma(lbm_handle_s *H) {
@@ -238,7 +311,8 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     if (L->dims == 3 && (L->m > 65535 || h > 65535)) return fail(LBM_ERR_INVALID, "m or h exceeds 65535");
     const long long N = (long long)L->n * L->m * h;
     const int q = L->dims == 2 ? 9 : 19;
-    if ((long long)q * N >= (1ll << 31) * 8ll) return fail(LBM_ERR_INVALID, "lattice too large");
+    // population offsets inside one z-plane (q * n * m elements) are 32-bit
+    if ((long long)q * L->n * L->m >= (1ll << 31)) return fail(LBM_ERR_INVALID, "lattice plane too large");
     if (N >= (1ll << 31)) return fail(LBM_ERR_INVALID, "more than 2^31 nodes");
     if (L->num_conns > 0 && (!L->bc_i || !L->bc_j || !L->bc_dir || !L->bc_type || (L->dims == 3 && !L->bc_k)))
         return fail(LBM_ERR_INVALID, "missing BC columns");
@@ -279,24 +353,32 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     long long fl = 0;
     for (long long i = 0; i < N; ++i) fl += (L->node_type[i] & 1);
     H->fluid = fl;
-    bool want_tma = false;
+    bool want_tma = false, want_jit = false, jit_required = false;
     {
-        // Two nodes per thread pays where the packed FP32x2 arithmetic
-        // outweighs its higher register count: F32 storage.  For F16S the
-        // one-node kernel keeps more warps resident and is faster.
-        // THESIS_LBM_KERNEL=scalar|pair overrides the choice.
+        // Default: the one-node kernel specialised at run time for this
+        // lattice (all population offsets become immediates; fastest for
+        // every storage), falling back to the compiled-in one-node kernel if
+        // the run-time build is unavailable.  THESIS_LBM_KERNEL=scalar|pair|
+        // tma|jit selects a variant explicitly (jit then fails loudly).
         const char *kv = getenv("THESIS_LBM_KERNEL");
         const bool can_pair = (L->n % 2 == 0) && P->storage != LBM_STORE_F64;
-        if (kv && strcmp(kv, "scalar") == 0) H->pair_kernel = false;
-        else if (kv && strcmp(kv, "pair") == 0) H->pair_kernel = can_pair;
-        else H->pair_kernel = can_pair && P->storage == LBM_STORE_F32;
+        H->pair_kernel = kv && strcmp(kv, "pair") == 0 && can_pair;
         want_tma = kv && strcmp(kv, "tma") == 0;
+        want_jit = !kv || !*kv || strcmp(kv, "jit") == 0;
+        jit_required = kv && strcmp(kv, "jit") == 0;
     }
     H->nslots = (int)flags.slot_node.size();
     H->slot_node = flags.slot_node;
     if (want_tma) {
         rc = setup_tma(H, flags.word);
         if (rc) {
+            free_handle(H);
+            return rc;
+        }
+    }
+    if (want_jit) {
+        rc = setup_jit(H, flags.word);
+        if (rc && jit_required) {
             free_handle(H);
             return rc;
         }
@@ -325,7 +407,8 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     ALLOC(H->pux, sizeof(float) * N);
     ALLOC(H->puy, sizeof(float) * N);
     ALLOC(H->puz, sizeof(float) * N);
-    ALLOC(H->partial, sizeof(double) * norm_partial_count());
+    ALLOC(H->partial, sizeof(double) * std::max(norm_partial_count(), 304 * 5));
+    ALLOC(H->mdiff_prev, sizeof(float) * 4 * N);
     ALLOC(H->norms, sizeof(double) * LBM_NORMS);
 #undef ALLOC
     cudaError_t e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking);
@@ -392,6 +475,12 @@ int lbm_init(lbm_handle H, const float *rho, const float *u, const float *v, con
     CUDA_TRY(cudaMemsetAsync(H->pux, 0, sizeof(float) * H->N, H->stream));
     CUDA_TRY(cudaMemsetAsync(H->puy, 0, sizeof(float) * H->N, H->stream));
     CUDA_TRY(cudaMemsetAsync(H->puz, 0, sizeof(float) * H->N, H->stream));
+    // MaxMacroDiff compares against the initial fields first (Iterate3D.cu:208-213)
+    const size_t fb = sizeof(float) * (size_t)H->N;
+    CUDA_TRY(cudaMemcpyAsync(H->mdiff_prev, H->ux, fb, cudaMemcpyDeviceToDevice, H->stream));
+    CUDA_TRY(cudaMemcpyAsync(H->mdiff_prev + H->N, H->uy, fb, cudaMemcpyDeviceToDevice, H->stream));
+    CUDA_TRY(cudaMemcpyAsync(H->mdiff_prev + 2 * H->N, H->uz, fb, cudaMemcpyDeviceToDevice, H->stream));
+    CUDA_TRY(cudaMemcpyAsync(H->mdiff_prev + 3 * H->N, H->rho, fb, cudaMemcpyDeviceToDevice, H->stream));
     StepParams p = make_params(H, 1, 0);  // fout = buffer 0
     const StepParams o = make_params(H, 0, 0);  // fout = buffer 1
     p.init_rho = H->P.rho;
@@ -415,6 +504,13 @@ static int launch(lbm_handle_s *H, int from, int write_macro, cudaStream_t s) {
     const StepParams p = make_params(H, from, write_macro);
     const int phys = H->P.mode == LBM_MODE_PHYSICS;
     int rc;
+    if (H->jit_kernel) {
+        const int bx = H->jit_key.block;
+        const dim3 grid((unsigned)((H->n + bx - 1) / bx), (unsigned)H->m, (unsigned)H->h);
+        void *args[] = {(void *)&p};
+        cudaError_t e = cudaLaunchKernel((const void *)H->jit_fn, grid, dim3((unsigned)bx), args, 0, s);
+        return e == cudaSuccess ? LBM_OK : fail(LBM_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
+    }
     if (H->tma_kernel) {
         TmaRows rows;
         rows.row = H->tma_row;
@@ -529,6 +625,22 @@ int lbm_macro_norms(lbm_handle H, double *out) {
     return LBM_OK;
 }
 
+int lbm_macro_diff(lbm_handle H, double *out) {
+    if (!H || !out) return fail(LBM_ERR_INVALID, "null argument");
+    const long long N = H->N;
+    launch_macro_diff(H->ux, H->uy, H->uz, H->rho, H->mdiff_prev, H->mdiff_prev + N, H->mdiff_prev + 2 * N,
+                      H->mdiff_prev + 3 * N, N, H->partial, H->norms, H->stream);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(out, H->norms, sizeof(double) * 5, cudaMemcpyDeviceToHost, H->stream));
+    CUDA_TRY(cudaStreamSynchronize(H->stream));
+    if (int rc = check_tma(H)) return rc;
+    if (out[4] != 0.0) {
+        H->status = LBM_DIVERGED;
+        return fail(LBM_DIVERGED, "non-finite macroscopic field (divergence)");
+    }
+    return LBM_OK;
+}
+
 int lbm_build_flags(const lbm_lattice_desc *L, const lbm_params *P, uint64_t *mask, uint32_t *word,
                     int32_t *slot, int *num_bc_nodes) {
     if (!L || !P) return fail(LBM_ERR_INVALID, "null argument");
@@ -551,7 +663,96 @@ int lbm_status(lbm_handle H) { return H ? H->status : LBM_ERR_INVALID; }
 
 long long lbm_fluid_nodes(lbm_handle H) { return H ? H->fluid : -1; }
 
-int lbm_kernel_variant(lbm_handle H) { return H ? (H->tma_kernel ? 3 : (H->pair_kernel ? 2 : 1)) : -1; }
+int lbm_kernel_variant(lbm_handle H) {
+    return H ? (H->jit_kernel ? 4 : (H->tma_kernel ? 3 : (H->pair_kernel ? 2 : 1))) : -1;
+}
+
+int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred) {
+    if (!H) return fail(LBM_ERR_INVALID, "null handle");
+    if (!H->jit_kernel) return fail(LBM_ERR_UNSUPPORTED, "autotuning needs the run-time specialised kernel");
+    if (trial_steps < 2) trial_steps = 2;
+    std::vector<JitStepKey> cand;
+    for (int b : {128, 256})
+        for (int hi : {0, 1})
+            for (int pr : {0, 1}) {
+                JitStepKey k = H->jit_key;
+                k.block = b;
+                k.hint = hi;
+                k.pred = pr != 0;
+                cand.push_back(k);
+            }
+    std::vector<cudaKernel_t> fn(cand.size(), nullptr);
+    std::vector<std::string> errs(cand.size());
+    {
+        std::vector<std::thread> th;
+        for (size_t i = 0; i < cand.size(); ++i)
+            th.emplace_back([&, i] { jit_step_kernel(cand[i], &fn[i], errs[i]); });
+        for (auto &t : th) t.join();
+    }
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    const JitStepKey keep = H->jit_key;
+    const cudaKernel_t keep_fn = H->jit_fn;
+    float best = 1e30f;
+    int best_i = -1;
+    for (size_t i = 0; i < cand.size(); ++i) {
+        if (!fn[i]) continue;
+        H->jit_key = cand[i];
+        H->jit_fn = fn[i];
+        int rc = launch(H, H->cur, 0, H->stream);  // warm-up
+        if (!rc) rc = launch(H, 1 - H->cur, 0, H->stream);
+        CUDA_TRY(cudaEventRecord(e0, H->stream));
+        for (int sI = 0; sI < trial_steps && !rc; ++sI) rc = launch(H, (H->cur + sI) & 1, 0, H->stream);
+        CUDA_TRY(cudaEventRecord(e1, H->stream));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0;
+        CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        if (!rc && ms < best) {
+            best = ms;
+            best_i = (int)i;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best_i < 0) {
+        H->jit_key = keep;
+        H->jit_fn = keep_fn;
+        return fail(LBM_ERR_CUDA, "autotune: no candidate ran: " + errs[0]);
+    }
+    H->jit_key = cand[best_i];
+    H->jit_fn = fn[best_i];
+    for (int c = 0; c < 2; ++c)
+        if (H->pair[c]) {
+            cudaGraphExecDestroy(H->pair[c]);
+            H->pair[c] = nullptr;
+        }
+    {
+        std::lock_guard<std::mutex> lock(g_tuned_mutex);
+        g_tuned[tune_key(H->jit_key)] = TunedKnobs{H->jit_key.block, H->jit_key.hint, H->jit_key.pred};
+    }
+    H->initialised = false;  // the trial steps leave the populations undefined
+    if (block) *block = H->jit_key.block;
+    if (hint) *hint = H->jit_key.hint;
+    if (pred) *pred = H->jit_key.pred ? 1 : 0;
+    return LBM_OK;
+}
+
+int lbm_kernel_config(lbm_handle H, int *block, int *hint, int *pred) {
+    if (!H) return fail(LBM_ERR_INVALID, "null handle");
+    if (block) *block = H->jit_kernel ? H->jit_key.block : STEP_BLOCK;
+    if (hint) *hint = H->jit_kernel ? H->jit_key.hint : 0;
+    if (pred) *pred = H->jit_kernel && H->jit_key.pred ? 1 : 0;
+    return LBM_OK;
+}
+
+int lbm_jit_check(int q, int coll, int storage, int phys, int wrap, int nx, int ny, int nz, int block, int hint,
+                  int pred) {
+    JitStepKey k{q, coll, storage, phys != 0, wrap != 0, nx, ny, nz, block, hint, pred != 0, true};
+    std::string err;
+    if (jit_step_kernel(k, nullptr, err)) return fail(LBM_ERR_CUDA, err);
+    return LBM_OK;
+}
 
 int lbm_bytes_per_update(lbm_handle H) { return H ? (int)(2 * H->q * H->elem) : -1; }
 

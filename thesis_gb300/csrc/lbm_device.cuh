@@ -122,6 +122,37 @@ __host__ __device__ constexpr double rest_shift(int q, int coll, int d) {
 // incompressible energy-square equilibrium (eps_eq = -475/63 j^2, no density
 // term) puts its rest state at w_d - (3/252) M_eps,d (rest_shift below).
 // ---------------------------------------------------------------------------
+// Read-only population load.  HINT 1 asks L2 to fetch the whole 256-byte
+// block around the address from DRAM (ld.global.nc.L2::256B), so the
+// neighbouring warps that read the rest of the block hit L2.
+template <int HINT>
+__device__ __forceinline__ __half ld_pop(const __half *p) {
+    if (HINT == 1) {
+        unsigned short v;
+        asm("ld.global.nc.L2::256B.b16 %0, [%1];" : "=h"(v) : "l"(p));
+        return __ushort_as_half(v);
+    }
+    return __ldg(p);
+}
+template <int HINT>
+__device__ __forceinline__ float ld_pop(const float *p) {
+    if (HINT == 1) {
+        float v;
+        asm("ld.global.nc.L2::256B.f32 %0, [%1];" : "=f"(v) : "l"(p));
+        return v;
+    }
+    return __ldg(p);
+}
+template <int HINT>
+__device__ __forceinline__ double ld_pop(const double *p) {
+    if (HINT == 1) {
+        double v;
+        asm("ld.global.nc.L2::256B.f64 %0, [%1];" : "=d"(v) : "l"(p));
+        return v;
+    }
+    return __ldg(p);
+}
+
 template <int ST> struct Store;
 template <> struct Store<LBM_STORE_F32> {
     using T = float;   // element type in HBM

@@ -1,0 +1,24 @@
+// Run-time specialisation of the step kernel (lbm_jit.cpp).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+namespace lbm {
+
+struct JitStepKey {
+    int q, coll, storage;
+    bool phys, wrap;
+    int nx, ny, nz;
+    int block;          // threads per block along x
+    int hint;           // population load form (ld_pop)
+    bool pred;          // blocked links by predicated loads
+    bool compile_only;  // compile to a cubin and stop (no GPU needed)
+};
+
+// Compile (or fetch from the process cache) step_kernel_fixed for `k` and
+// return its handle; launch it with cudaLaunchKernel((const void *)kernel,
+// ...) and a StepParams argument.  Returns 0 or -1 with `err` set.
+int jit_step_kernel(const JitStepKey &k, cudaKernel_t *out, std::string &err);
+
+}  // namespace lbm

@@ -72,4 +72,57 @@ int launch_norms(const uint32_t *word, const float *rho, const float *ux, const 
 
 int norm_partial_count() { return NORM_BLOCKS * LBM_NORMS; }
 
+// The reference's MaxMacroDiff residual (Iterate3D.cu:696-735, gpu_abs_sub +
+// gpu_max_h, GpuSum.cu:10-23, 241-264): max |x - x_prev| over all nodes for
+// u, v, w, rho, then x_prev <- x.  out[4] counts non-finite differences (the
+// reference's divergence flag).  Max is order-independent, so the result is
+// deterministic.
+__global__ void __launch_bounds__(NORM_THREADS)
+macro_diff_partial(const float *__restrict__ ux, const float *__restrict__ uy, const float *__restrict__ uz,
+                   const float *__restrict__ rho, float *pux, float *puy, float *puz, float *prho, long long n,
+                   double *partial) {
+    double acc[5] = {0, 0, 0, 0, 0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float cur[4] = {ux[i], uy[i], uz[i], rho[i]};
+        float *prev[4] = {pux, puy, puz, prho};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const double d = fabs((double)cur[k] - (double)prev[k][i]);
+            if (!isfinite(d)) acc[4] += 1.0;
+            else acc[k] = d > acc[k] ? d : acc[k];
+            prev[k][i] = cur[k];
+        }
+    }
+    __shared__ double sm[NORM_THREADS][5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) sm[threadIdx.x][k] = acc[k];
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        double r = 0;
+        for (int t = 0; t < NORM_THREADS; ++t) {
+            const double v = sm[t][threadIdx.x];
+            r = threadIdx.x == 4 ? r + v : (v > r ? v : r);
+        }
+        partial[blockIdx.x * 5 + threadIdx.x] = r;
+    }
+}
+
+__global__ void macro_diff_final(const double *partial, int nblocks, double *out) {
+    if (threadIdx.x >= 5) return;
+    double r = 0;
+    for (int b = 0; b < nblocks; ++b) {
+        const double v = partial[b * 5 + threadIdx.x];
+        r = threadIdx.x == 4 ? r + v : (v > r ? v : r);
+    }
+    out[threadIdx.x] = r;
+}
+
+int launch_macro_diff(const float *ux, const float *uy, const float *uz, const float *rho, float *pux, float *puy,
+                      float *puz, float *prho, long long n, double *partial, double *out, cudaStream_t s) {
+    macro_diff_partial<<<NORM_BLOCKS, NORM_THREADS, 0, s>>>(ux, uy, uz, rho, pux, puy, puz, prho, n, partial);
+    macro_diff_final<<<1, 32, 0, s>>>(partial, NORM_BLOCKS, out);
+    return 0;
+}
+
 }  // namespace lbm

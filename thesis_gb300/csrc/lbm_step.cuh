@@ -11,9 +11,12 @@
 //     f <- collide(f, rho, u)  and store to the other buffer
 //
 // The state between launches is the post-collision population field in a
-// pull double buffer, SoA by direction (one contiguous array per direction,
-// x fastest), so a warp's loads and stores are 32 consecutive nodes of one
-// direction.  Per node the kernel reads one 32-bit flag word and Q
+// pull double buffer laid out as rows: for every lattice row (y, z) the Q
+// directions follow each other, each a run of nx values (x fastest), so
+// population d of node (x, y, z) sits at d*nx + x + pitch*(y + ny*z) with
+// pitch = Q*nx.  A warp's loads and stores are 32 consecutive nodes of one
+// direction, one row of one direction is contiguous (a single bulk copy),
+// and all populations of a node are at fixed offsets from one base.  Per node the kernel reads one 32-bit flag word and Q
 // populations and writes Q populations; macroscopic fields are written only
 // on steps that need them (residuals, output).
 #pragma once
@@ -31,6 +34,7 @@ struct StepParams {
     const double *bc_uvw;
     float *rho, *ux, *uy, *uz;
     int nx, ny, nz;
+    int pitch;  // elements from one row of a direction to the next (Q * nx)
     int write_macro;
     double omega, omega_m, gshift;
     double rho_in, rho_out;
@@ -130,18 +134,37 @@ __device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], uint3
     collide<Q, COLL, ST, PHYS>(f, rho, ux, uy, uz, p);
 }
 
-template <int Q, int COLL, int ST, bool PHYS>
-__global__ void __launch_bounds__(STEP_BLOCK) step_kernel(const StepParams p) {
+// Lattice extents seen by the step: read from the parameters (DynGeom) or
+// fixed at compile time (FixedGeom, the build specialised for one lattice,
+// where every population offset becomes an immediate).
+struct DynGeom {
+    int nx, ny, nz, pitch;
+};
+template <int NX, int NY, int NZ, int PITCH>
+struct FixedGeom {
+    static constexpr int nx = NX, ny = NY, nz = NZ, pitch = PITCH;
+};
+
+// One node of the fused step.  WRAP: coordinates wrap at the lattice faces
+// (periodic lattices, or any out-of-domain link left open); without it the
+// pull offsets are constants and every out-of-domain link must be blocked.
+// HINT: population load form (ld_pop).  PRED: a blocked link is read by a
+// second, predicated load instead of a selected address.
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, int HINT = 0, bool PRED = false>
+__device__ __forceinline__ void step_node(const StepParams &p, const G &g, int x, int y, int z) {
     using S = Store<ST>;
     using T = typename S::T;
     using R = typename S::R;
     using L = Lat<Q>;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
-    const bool in_row = x < p.nx;
-    const int node = x + p.nx * (y + p.ny * z);
+    const bool in_row = x < g.nx;
+    const int row = y + g.ny * z;
+    const int node = x + g.nx * row;    // flag words and macroscopic fields
+    const long long idx = x + (long long)g.pitch * row;  // populations
     const uint32_t w = in_row ? __ldg(p.word + node) : 0u;
     const bool fluid = (w & W_FLUID) != 0;
+    // Every population of the node is at a fixed offset from these bases.
+    const T *in = (const T *)p.fin[0] + idx;
+    T *out = (T *)p.fout[0] + idx;
     // Solid lanes of a warp that also holds fluid nodes store the zero
     // encoding, so the warp's stores cover whole 32-byte sectors instead of
     // forcing a read-modify-write of partly written ones in L2/DRAM.
@@ -149,38 +172,68 @@ __global__ void __launch_bounds__(STEP_BLOCK) step_kernel(const StepParams p) {
     if (!fluid) {
         if (in_row && warp_fluid) {
 #pragma unroll
-            for (int d = 0; d < Q; ++d) ((T *)p.fout[d])[node] = S::encode((R)0, p.shift[d], p.scale);
+            for (int d = 0; d < Q; ++d) out[d * g.nx] = S::encode((R)0, p.shift[d], p.scale);
         }
         return;
     }
 
-    // Pull offsets to the six face neighbours; coordinates wrap periodically
+    // Pull offsets to the six face neighbours.  With WRAP, coordinates wrap
     // and links that must not wrap are blocked in the flag word, so a wrapped
     // address is only read where the lattice is periodic.
-    const int plane = p.nx * p.ny;
-    const int oxm = x == 0 ? p.nx - 1 : -1, oxp = x == p.nx - 1 ? 1 - p.nx : 1;
-    const int oym = y == 0 ? (p.ny - 1) * p.nx : -p.nx, oyp = y == p.ny - 1 ? (1 - p.ny) * p.nx : p.nx;
-    const int ozm = z == 0 ? (p.nz - 1) * plane : -plane, ozp = z == p.nz - 1 ? (1 - p.nz) * plane : plane;
+    const int plane = g.pitch * g.ny;
+    int oxm = -1, oxp = 1, oym = -g.pitch, oyp = g.pitch, ozm = -plane, ozp = plane;
+    if (WRAP) {
+        oxm = x == 0 ? g.nx - 1 : -1;
+        oxp = x == g.nx - 1 ? 1 - g.nx : 1;
+        oym = y == 0 ? (g.ny - 1) * g.pitch : -g.pitch;
+        oyp = y == g.ny - 1 ? (1 - g.ny) * g.pitch : g.pitch;
+        ozm = z == 0 ? (g.nz - 1) * plane : -plane;
+        ozp = z == g.nz - 1 ? (1 - g.nz) * plane : plane;
+    }
 
     R f[Q];
+    f[0] = S::decode(ld_pop<HINT>(in), p.shift[0], p.inv_scale);
 #pragma unroll
-    for (int d = 0; d < Q; ++d) {
-        if (d == 0) {
-            f[0] = S::load((const T *)p.fin[0] + node, p.shift[0], p.inv_scale);
-            continue;
-        }
-        const int src = node + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
-                        (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
-                        (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
+    for (int d = 1; d < Q; ++d) {
+        const int pull = d * g.nx + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
+                         (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
+                         (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
+        // across a blocked link: the node's own population, opp(d) for
+        // half-way bounce-back, d itself in the reference's wall model
+        const int own = (PHYS ? L::opp(d) : d) * g.nx;
         const bool blocked = (w >> d) & 1u;
-        const T *base = (const T *)p.fin[(blocked && PHYS) ? L::opp(d) : d];
-        f[d] = S::load(base + (blocked ? node : src), p.shift[d], p.inv_scale);
+        T v;
+        if (PRED) {
+            if (blocked) v = ld_pop<HINT>(in + own);
+            else v = ld_pop<HINT>(in + pull);
+        } else {
+            v = ld_pop<HINT>(in + (blocked ? own : pull));
+        }
+        f[d] = S::decode(v, p.shift[d], p.inv_scale);
     }
 
     update_node<Q, COLL, ST, PHYS>(f, w, node, p);
 
 #pragma unroll
-    for (int d = 0; d < Q; ++d) S::store((T *)p.fout[d] + node, f[d], p.shift[d], p.scale);
+    for (int d = 0; d < Q; ++d) S::store(out + d * g.nx, f[d], p.shift[d], p.scale);
+}
+
+template <int Q, int COLL, int ST, bool PHYS>
+__global__ void __launch_bounds__(STEP_BLOCK) step_kernel(const StepParams p) {
+    const DynGeom g{p.nx, p.ny, p.nz, p.pitch};
+    step_node<Q, COLL, ST, PHYS, true>(p, g, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// The same step with the lattice extents fixed at compile time: built at run
+// time for one lattice (lbm_jit.cpp), so pull, bounce-back and store offsets
+// are immediates of the loads and stores.
+// BLOCK threads along x, HINT and PRED as in step_node: the knobs the
+// autotuner (lbm_autotune) chooses among.
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, int NX, int NY, int NZ, int BLOCK, int HINT, bool PRED>
+__global__ void __launch_bounds__(BLOCK) step_kernel_fixed(const StepParams p) {
+    const FixedGeom<NX, NY, NZ, Q * NX> g;
+    step_node<Q, COLL, ST, PHYS, WRAP, FixedGeom<NX, NY, NZ, Q * NX>, HINT, PRED>(
+        p, g, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // First post-collision field: f0 = 0 (the reference's start, Iterate.cu:244)
@@ -197,13 +250,15 @@ __global__ void __launch_bounds__(STEP_BLOCK) init_kernel(const StepParams p, co
     using L = Lat<Q>;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= p.nx) return;
-    const int node = x + p.nx * (blockIdx.y + p.ny * blockIdx.z);
+    const int row = blockIdx.y + p.ny * blockIdx.z;
+    const int node = x + p.nx * row;
+    const long long idx = x + (long long)p.pitch * row;
     const uint32_t w = p.word[node];
     if (!(w & W_FLUID)) {
 #pragma unroll
         for (int d = 0; d < Q; ++d) {
-            ((T *)p.fout[d])[node] = S::encode((R)0, p.shift[d], p.scale);
-            ((T *)other.fout[d])[node] = S::encode((R)0, p.shift[d], p.scale);
+            ((T *)p.fout[d])[idx] = S::encode((R)0, p.shift[d], p.scale);
+            ((T *)other.fout[d])[idx] = S::encode((R)0, p.shift[d], p.scale);
         }
         return;
     }
@@ -219,23 +274,25 @@ __global__ void __launch_bounds__(STEP_BLOCK) init_kernel(const StepParams p, co
     collide<Q, COLL, ST, PHYS>(f, rho, ux, uy, uz, p);
 #pragma unroll
     for (int d = 0; d < Q; ++d) {
-        S::store((T *)p.fout[d] + node, f[d], p.shift[d], p.scale);
+        S::store((T *)p.fout[d] + idx, f[d], p.shift[d], p.scale);
         // The other buffer's fluid entries are overwritten by the first step
         // before anything reads them; give them the same finite values.
-        S::store((T *)other.fout[d] + node, f[d], p.shift[d], p.scale);
+        S::store((T *)other.fout[d] + idx, f[d], p.shift[d], p.scale);
     }
 }
 
-// Decode a population field to double (host read-back of the state).
+// Decode a population field to double in the reference's SoA order
+// out[d*n + node] (host read-back of the state).
 template <int Q, int ST>
 __global__ void decode_kernel(const StepParams p, double *out, long long n) {
     using S = Store<ST>;
     using T = typename S::T;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const long long idx = i % p.nx + (long long)p.pitch * (i / p.nx);
 #pragma unroll
     for (int d = 0; d < Q; ++d)
-        out[d * n + i] = (double)S::load((const T *)p.fin[d] + i, p.shift[d], p.inv_scale);
+        out[d * n + i] = (double)S::load((const T *)p.fin[d] + idx, p.shift[d], p.inv_scale);
 }
 
 }  // namespace lbm

@@ -142,13 +142,15 @@ __global__ void __launch_bounds__(TMA_THREADS) step_kernel_tma(const StepParams 
                 sy = sy < 0 ? sy + p.ny : (sy >= p.ny ? sy - p.ny : sy);
                 sz = sz < 0 ? sz + p.nz : (sz >= p.nz ? sz - p.nz : sz);
                 const size_t src_row = (size_t)sy + (size_t)p.ny * sz;
-                bulk_copy_g2s(smem_addr(pull + (size_t)d * rowb), (const T *)p.fin[d] + src_row * nx, rowb, full);
+                bulk_copy_g2s(smem_addr(pull + (size_t)d * rowb), (const T *)p.fin[d] + src_row * p.pitch, rowb,
+                              full);
             }
             unsigned char *own = pull + (size_t)Q * rowb;
 #pragma unroll
             for (int e = 0; e < Q; ++e) {
                 if (!((om >> e) & 1u)) continue;
-                bulk_copy_g2s(smem_addr(own + (size_t)e * rowb), (const T *)p.fin[e] + (size_t)r * nx, rowb, full);
+                bulk_copy_g2s(smem_addr(own + (size_t)e * rowb), (const T *)p.fin[e] + (size_t)r * p.pitch, rowb,
+                              full);
             }
         }
         // Copies still in flight must land before the block's shared memory
@@ -166,8 +168,10 @@ __global__ void __launch_bounds__(TMA_THREADS) step_kernel_tma(const StepParams 
     for (int k = blockIdx.x; k < rows.nrows; k += gridDim.x, ++used) {
         const int s = used % nst;
         const uint32_t use = (uint32_t)(used / nst);
-        if (!mbar_wait(smem_addr(bars + s), use & 1u)) {
-            atomicExch(rows.err, 2u);
+        // every lane waits; the warp leaves together if any lane gave up
+        const bool ok = mbar_wait(smem_addr(bars + s), use & 1u);
+        if (!__all_sync(0xffffffffu, ok)) {
+            if (lane == 0) atomicExch(rows.err, 2u);
             return;
         }
         const unsigned char *st = stage0 + (size_t)s * stage_bytes;
@@ -177,12 +181,13 @@ __global__ void __launch_bounds__(TMA_THREADS) step_kernel_tma(const StepParams 
         const int r = rows.row[k];
         for (int x = ct; x < nx; x += TMA_CONSUMERS) {
             const uint32_t w = wrow[x];
-            const int node = r * nx + x;
+            const int node = r * nx + x;       // flag words and macroscopic fields
+            const long long idx = (long long)r * p.pitch + x;  // populations
             if (!(w & W_FLUID)) {
                 // solid nodes keep the zero encoding; writing it keeps the
                 // warp's stores sector-complete
 #pragma unroll
-                for (int d = 0; d < Q; ++d) ((T *)p.fout[d])[node] = S::encode((R)0, p.shift[d], p.scale);
+                for (int d = 0; d < Q; ++d) ((T *)p.fout[d])[idx] = S::encode((R)0, p.shift[d], p.scale);
                 continue;
             }
             const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
@@ -196,7 +201,7 @@ __global__ void __launch_bounds__(TMA_THREADS) step_kernel_tma(const StepParams 
             }
             update_node<Q, COLL, ST, true>(f, w, node, p);
 #pragma unroll
-            for (int d = 0; d < Q; ++d) S::store((T *)p.fout[d] + node, f[d], p.shift[d], p.scale);
+            for (int d = 0; d < Q; ++d) S::store((T *)p.fout[d] + idx, f[d], p.shift[d], p.scale);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_addr(bars + nst + s));

@@ -273,7 +273,9 @@ __global__ void __launch_bounds__(X2_BLOCK) step_kernel_x2(const StepParams p) {
     const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int y = blockIdx.y, z = blockIdx.z;
     const bool in_row = x0 < p.nx;
-    const int node = x0 + p.nx * (y + p.ny * z);
+    const int row = y + p.ny * z;
+    const int node = x0 + p.nx * row;   // flag words and macroscopic fields
+    const long long idx = x0 + (long long)p.pitch * row;  // populations
     uint2 wp = make_uint2(0u, 0u);
     if (in_row) wp = __ldg((const uint2 *)(p.word + node));
     const bool fl0 = (wp.x & W_FLUID) != 0, fl1 = (wp.y & W_FLUID) != 0;
@@ -282,13 +284,13 @@ __global__ void __launch_bounds__(X2_BLOCK) step_kernel_x2(const StepParams p) {
         if (in_row && warp_fluid) {
 #pragma unroll
             for (int d = 0; d < Q; ++d)
-                PS::store((T *)p.fout[d] + node, f2(-p.shift[d] * S));
+                PS::store((T *)p.fout[d] + idx, f2(-p.shift[d] * S));
         }
         return;
     }
 
-    const int plane = p.nx * p.ny;
-    const int oym = y == 0 ? (p.ny - 1) * p.nx : -p.nx, oyp = y == p.ny - 1 ? (1 - p.ny) * p.nx : p.nx;
+    const int plane = p.pitch * p.ny;
+    const int oym = y == 0 ? (p.ny - 1) * p.pitch : -p.pitch, oyp = y == p.ny - 1 ? (1 - p.ny) * p.pitch : p.pitch;
     const int ozm = z == 0 ? (p.nz - 1) * plane : -plane, ozp = z == p.nz - 1 ? (1 - p.nz) * plane : plane;
     // x offsets of the pair's pulls: from x - 1 and from x + 1 (wrapped)
     const int oxm0 = x0 == 0 ? p.nx - 1 : -1;              // node x0 pulling from x0 - 1
@@ -304,18 +306,18 @@ __global__ void __launch_bounds__(X2_BLOCK) step_kernel_x2(const StepParams p) {
     for (int d = 0; d < Q; ++d) {
         const int oyz = (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
                         (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
-        const int s0 = node + oyz + (L::cx(d) == 1 ? oxm0 : (L::cx(d) == -1 ? 1 : 0));
-        const int s1 = node + 1 + oyz + (L::cx(d) == 1 ? -1 : (L::cx(d) == -1 ? oxp1 : 0));
+        const long long s0 = idx + oyz + (L::cx(d) == 1 ? oxm0 : (L::cx(d) == -1 ? 1 : 0));
+        const long long s1 = idx + 1 + oyz + (L::cx(d) == 1 ? -1 : (L::cx(d) == -1 ? oxp1 : 0));
         const T *pull = (const T *)p.fin[d];
         if (d == 0) {
-            hx[0] = PS::load1(pull + node);
-            hy[0] = PS::load1(pull + node + 1);
+            hx[0] = PS::load1(pull + idx);
+            hy[0] = PS::load1(pull + idx + 1);
             continue;
         }
         const T *own = (const T *)p.fin[PHYS ? L::opp(d) : d];
         const bool b0 = (wp.x >> d) & 1u, b1 = (wp.y >> d) & 1u;
-        hx[d] = PS::load1(b0 ? own + node : pull + s0);
-        hy[d] = PS::load1(b1 ? own + node + 1 : pull + s1);
+        hx[d] = PS::load1(b0 ? own + idx : pull + s0);
+        hy[d] = PS::load1(b1 ? own + idx + 1 : pull + s1);
     }
     const unsigned warp_blocked = __reduce_or_sync(0xffffffffu, (wp.x | wp.y) & 0x7FFFEu);
     f2 h[Q];
@@ -424,7 +426,7 @@ __global__ void __launch_bounds__(X2_BLOCK) step_kernel_x2(const StepParams p) {
         }
     }
 #pragma unroll
-    for (int d = 0; d < Q; ++d) PS::store((T *)p.fout[d] + node, h[d]);
+    for (int d = 0; d < Q; ++d) PS::store((T *)p.fout[d] + idx, h[d]);
 }
 
 }  // namespace lbm

@@ -22,11 +22,4 @@ constexpr int BCK_PRESSURE = 8;
 constexpr int BCK_OUTLET = 16;
 constexpr int BCK_ACTIVE = 32;
 
-struct StepParams;
-// Kernel launchers (lbm_kernels_q9.cu / lbm_kernels_q19.cu).
-int launch_step(int q, const StepParams &p, int coll, int storage, int phys, void *stream);
-int launch_init(int q, const StepParams &p, const StepParams &other, int coll, int storage,
-                int phys, int equilibrium_start, void *stream);
-int launch_decode(int q, const StepParams &p, int storage, double *out, long long n, void *stream);
-
 }  // namespace lbm

@@ -268,6 +268,33 @@ def from_files(node_path, bc_path):
     return Lattice(dims, n, m, h, fluid.astype(np.int32), bc.astype(np.int32))
 
 
+def write_files(lat, node_path, bc_path, delta=None):
+    """Write a Lattice as reference-format Node and BC files (the layout
+    readNodeFile/readConnFile read, FilesReading.cu:270-347): 2D
+    `i j x y fluid` and `i j dir type x y id`; 3D tab-separated
+    `i j k x y z fluid` and `i j k<TAB><TAB>dir type x y z id`.  Coordinates
+    are index * delta (default 1/(n-1)); a BC line's coordinates are those of
+    its node."""
+    x, y, z = lat.coords(delta)
+    idx = np.arange(lat.num_nodes)
+    i, j, k = idx % lat.n, (idx // lat.n) % lat.m, idx // (lat.n * lat.m)
+    with open(node_path, "w") as f:
+        if lat.dims == 2:
+            for r in range(lat.num_nodes):
+                f.write("%d %d %.6f %.6f %d\n" % (i[r], j[r], x[r], y[r], lat.node_type[r]))
+        else:
+            for r in range(lat.num_nodes):
+                f.write("%d\t%d\t%d\t%.6f\t%.6f\t%.6f\t%d\n" % (i[r], j[r], k[r], x[r], y[r], z[r],
+                                                                lat.node_type[r]))
+    with open(bc_path, "w") as f:
+        for bi, bj, bk, d, t, bid in lat.bc:
+            r = bi + lat.n * (bj + lat.m * bk)
+            if lat.dims == 2:
+                f.write("%d %d %d %d %.6f %.6f %d\n" % (bi, bj, d, t, x[r], y[r], bid))
+            else:
+                f.write("%d\t%d\t%d\t\t%d\t%d\t%.6f\t%.6f\t%.6f\t%d\n" % (bi, bj, bk, d, t, x[r], y[r], z[r], bid))
+
+
 def write_starcd(prefix, vertices, faces):
     """Write STAR-CD geometry in the generator's input layout: `<prefix>.vrt`
     lines `id x y z` and `<prefix>.bnd` lines `id p1 p2 p3 p4 bcid 0 TYPE`

@@ -48,6 +48,20 @@ class CgParams(C.Structure):
                 ("storage", C.c_int)]
 
 
+class RunConfig(C.Structure):
+    """lbm_run_config (include/thesis_lbm_io.h)."""
+    _fields_ = [("problem_name", C.c_char * 512),
+                ("u", C.c_double), ("v", C.c_double), ("w", C.c_double), ("rho", C.c_double),
+                ("viscosity", C.c_double),
+                ("inlet_profile", C.c_int), ("collision_model", C.c_int), ("boundary_type", C.c_int),
+                ("bc_wall_model", C.c_int), ("outlet_profile", C.c_int), ("iterations", C.c_int),
+                ("autosave_after", C.c_int), ("autosave_every", C.c_int),
+                ("stop_condition", C.c_double * 4), ("output_format", C.c_int),
+                ("use_initial_conditions_file", C.c_int), ("initial_conditions_name", C.c_char * 512),
+                ("residual_model", C.c_int), ("show_macro_diff", C.c_int), ("g", C.c_double),
+                ("boundary_id", C.c_int), ("update_inlet_outlet", C.c_int), ("unparsed_lines", C.c_int)]
+
+
 _lib = None
 
 
@@ -82,10 +96,27 @@ def lib():
         "lbm_fluid_nodes": (C.c_longlong, [vp]),
         "lbm_bytes_per_update": (C.c_int, [vp]),
         "lbm_kernel_variant": (C.c_int, [vp]),
+        "lbm_jit_check": (C.c_int, [C.c_int] * 11),
+        "lbm_autotune": (C.c_int, [vp, C.c_int, _IP, _IP, _IP]),
+        "lbm_kernel_config": (C.c_int, [vp, _IP, _IP, _IP]),
         "lbm_destroy": (None, [vp]),
         "lbm_build_flags": (C.c_int, [C.POINTER(LatticeDesc), C.POINTER(Params),
                                       C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
                                       C.POINTER(C.c_int32), C.POINTER(C.c_int)]),
+        "lbm_macro_diff": (C.c_int, [vp, dp]),
+        "lbm_read_init_file": (C.c_int, [C.c_char_p, C.POINTER(RunConfig)]),
+        "lbm_count_lines": (C.c_longlong, [C.c_char_p]),
+        "lbm_node_file_dims": (C.c_int, [C.c_char_p]),
+        "lbm_read_node_file": (C.c_int, [C.c_char_p, C.c_int, C.c_longlong, _IP, _IP, _IP, fp, fp, fp, _IP]),
+        "lbm_read_bc_file": (C.c_int, [C.c_char_p, C.c_int, C.c_longlong, _IP, _IP, _IP, _IP, _IP, fp, fp, fp,
+                                       _IP]),
+        "lbm_write_results": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, fp, fp, fp, fp, fp, fp,
+                                        fp]),
+        "lbm_read_results": (C.c_longlong, [C.c_char_p, C.c_longlong, dp]),
+        "lbm_read_initial_conditions": (C.c_int, [C.c_char_p, C.c_longlong, C.c_int, C.c_int, C.c_int, fp, fp, fp,
+                                                  fp]),
+        "lbm_compare_results": (C.c_int, [C.c_char_p, C.c_char_p, dp, dp]),
+        "lbm_io_last_error": (C.c_char_p, []),
         "lbm_cg_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(CgParams), C.POINTER(vp)]),
         "lbm_cg_init": (C.c_int, [vp, fp, fp]),
         "lbm_cg_step": (C.c_int, [vp, C.c_int, C.c_int, vp]),

@@ -129,6 +129,19 @@ class Solver:
         arrs = [None if a is None else np.ascontiguousarray(a, np.float32).reshape(-1) for a in (u, v, w)]
         N.check(self._lib.lbm_set_inlet_velocity(self._h, *[_fptr(a) for a in arrs]))
 
+    def autotune(self, trial_steps=20):
+        """Pick the fastest variant of the specialised step kernel (block size,
+        load form, bounce-back form); leaves the populations undefined, so
+        call init() afterwards.  Returns (block, hint, pred)."""
+        b, h, p = C.c_int(), C.c_int(), C.c_int()
+        N.check(self._lib.lbm_autotune(self._h, int(trial_steps), C.byref(b), C.byref(h), C.byref(p)))
+        return b.value, h.value, p.value
+
+    def kernel_config(self):
+        b, h, p = C.c_int(), C.c_int(), C.c_int()
+        N.check(self._lib.lbm_kernel_config(self._h, C.byref(b), C.byref(h), C.byref(p)))
+        return b.value, h.value, p.value
+
     def init(self, rho=None, u=None, v=None, w=None):
         arrs = [None if a is None else np.ascontiguousarray(a, np.float32).reshape(-1) for a in (rho, u, v, w)]
         N.check(self._lib.lbm_init(self._h, *[_fptr(a) for a in arrs]))
@@ -152,6 +165,16 @@ class Solver:
     def norms(self):
         out = np.zeros(N.NORMS, np.float64)
         rc = self._lib.lbm_macro_norms(self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc not in (N.LBM_OK, N.LBM_DIVERGED):
+            N.check(rc)
+        return out, rc
+
+    def macro_diff(self):
+        """The reference's MaxMacroDiff residual: (max|du|, max|dv|, max|dw|,
+        max|drho|, non-finite count) against the previous call (the initial
+        fields before the first), and the status code."""
+        out = np.zeros(5, np.float64)
+        rc = self._lib.lbm_macro_diff(self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
         if rc not in (N.LBM_OK, N.LBM_DIVERGED):
             N.check(rc)
         return out, rc
