@@ -149,6 +149,22 @@ int lbm_get_populations(lbm_handle h, double *f);
 #define LBM_NORMS 5
 int lbm_macro_norms(lbm_handle h, double *out);
 
+/* The reference's L2 residual (computeResidual2D/3D, ComputeResiduals.cu:13-26,
+ * used when ResidualModel = L2): sqrt(sum over all populations of
+ * (f - fColl)^2), fColl the post-collision state the last step left and f the
+ * post-stream, post-boundary field the next step will pull from it.  Summed
+ * in FP64 (the reference sums in FP32).  LBM_DIVERGED when not finite. */
+int lbm_residual_l2(lbm_handle h, double *out);
+
+/* Drag and lift by momentum exchange (physics mode): the force on the solid
+ * nodes inside box = {x0, x1, y0, y1, z0, z1} (inclusive node indices), from
+ * every bounced-back link of a fluid node into one of them, 2 c f* per link
+ * and step, f* the post-collision state the last step left; force[0..2] in
+ * lattice units, FP64 sums.  The reference's drag/lift (GpuUpdateMacro.cu:
+ * 33-38) integrates a hard-wired pressure expression over the nodes of a
+ * boundary id instead; this is the standard link-based force. */
+int lbm_momentum_exchange(lbm_handle h, const int *box, double *force);
+
 /* The reference's MaxMacroDiff residual (Iterate3D.cu:696-735): out[0..3] =
  * max over all nodes of |u - u_prev|, |v - v_prev|, |w - w_prev|,
  * |rho - rho_prev| for the last stored macroscopic fields, where _prev is the
@@ -183,29 +199,40 @@ int lbm_status(lbm_handle h);
 long long lbm_fluid_nodes(lbm_handle h);
 
 /* Step kernel of the handle, chosen at lbm_create: 4 (the default) the
- * one-node kernel specialised for this lattice's extents at run time, 1 the
+ * one-node kernel specialised for this lattice's extents at run time (in
+ * physics mode computing in storage units, deviations from the rest state;
+ * THESIS_LBM_KERNEL=jith|jitf forces storage-unit or f-space), 1 the
  * compiled-in one-node kernel (used when the run-time build is unavailable),
  * 2 two nodes per thread (even n, F32/F16S), 3 the row-staged bulk-copy
- * kernel.  THESIS_LBM_KERNEL=scalar|pair|tma|jit in the environment at
- * lbm_create selects one; a variant the lattice does not admit falls back to
- * 1, except jit, whose build failure lbm_create reports. */
+ * kernel.  THESIS_LBM_KERNEL=scalar|pair|tma|jit|jit2 in the environment at
+ * lbm_create selects one (jit2: the run-time specialised two-node kernel); a
+ * variant the lattice does not admit falls back to 1, except jit and jit2,
+ * whose build failure lbm_create reports. */
 int lbm_kernel_variant(lbm_handle h);
 
-/* Autotuner of the run-time specialised kernel: builds its variants (block
- * of 128 or 256 threads along x; plain or L2-256-byte-prefetching loads;
- * bounce-back by selected address or by predicated loads), times
- * trial_steps steps of each on the handle's stream and keeps the fastest,
- * also for handles created later in the process on the same lattice and
- * parameters.  The trial steps leave the populations undefined: call
- * lbm_init afterwards.  The chosen knobs go to block, hint, pred (may be
- * NULL).  This function has no counterpart in the reference. */
+/* Autotuner of the run-time specialised kernel: builds its variants (one
+ * node per thread with blocks of 128 or 256 threads along x, plain or
+ * L2-256-byte-prefetching loads, bounce-back by selected address or by
+ * predicated loads; and, for even n with F32/F16S storage, two nodes per
+ * thread with blocks of 64 or 128), times trial_steps steps of each on the
+ * handle's stream and keeps the fastest, also for handles created later in
+ * the process on the same lattice and parameters.  The trial steps leave the
+ * populations undefined: call lbm_init afterwards.  The chosen knobs go to
+ * block, hint (bit 0 L2-256-byte loads, bit 1 arithmetic in storage units,
+ * one node per thread) and pred (bit 0 predicated bounce-back, bit 1 two
+ * nodes per thread, bits 2 and up the minimum resident blocks per SM asked of
+ * the register allocator, 0 for none); each may be NULL.  In physics mode with
+ * F32 storage only storage-unit variants are candidates (their moments come
+ * from deviations from the rest state).  This function has no
+ * counterpart in the reference. */
 int lbm_autotune(lbm_handle h, int trial_steps, int *block, int *hint, int *pred);
 /* The knobs of the handle's step kernel (defaults 128, 0, 0). */
 int lbm_kernel_config(lbm_handle h, int *block, int *hint, int *pred);
 
 /* Compile (no GPU needed, nothing is loaded) the run-time specialised step
- * kernel for the given template arguments and knobs (as lbm_autotune): a
- * build check of the sources the library embeds.  Returns LBM_OK or LBM_ERR_CUDA with the compiler log in
+ * kernel for the given template arguments and knobs (as lbm_autotune; pred
+ * bit 1 selects the two-node kernel): a build check of the sources the
+ * library embeds.  Returns LBM_OK or LBM_ERR_CUDA with the compiler log in
  * lbm_last_error(). */
 int lbm_jit_check(int q, int coll, int storage, int phys, int wrap, int nx, int ny, int nz, int block, int hint,
                   int pred);
@@ -237,6 +264,41 @@ int lbm_latticegen(const char *vrt_path, const char *bnd_path, int n_x, double x
                    double zseed, int complexity, const char *node_path, const char *bc_path,
                    int *out_dims);
 const char *lbm_latticegen_error(void);
+
+/* ---- Batched independent domains -------------------------------------------
+ * Many lattices of uneven sizes (a sweep over geometry and Reynolds number)
+ * advanced together: one persistent launch per step over a packed table of
+ * row tiles of all active domains, long runs replayed from a captured CUDA
+ * graph, per-domain FP64 residuals, converged domains retired from the table.
+ * The reference runs one lattice per process; this has no counterpart there.
+ * All domains share dims, collision model and storage (F32 or F16S) and run
+ * in physics mode; each has its own extents, viscosity, velocities and
+ * boundary links. */
+typedef struct lbm_batch_s *lbm_batch;
+int lbm_batch_create(const lbm_lattice_desc *const *lattices, const lbm_params *params, int count,
+                     lbm_batch *out);
+/* Equilibrium start of every domain from its params' rho, u, v, w. */
+int lbm_batch_init(lbm_batch b);
+/* nsteps steps of every active domain (stream NULL = the batch's own). */
+int lbm_batch_step(lbm_batch b, int nsteps, int write_macro_last, void *stream);
+/* res[d]: sqrt(sum |u - u_prev|^2) / sqrt(sum |u|^2) over fluid nodes of the
+ * last stored fields against those at the previous call (FP64; zero fields
+ * before the first call).  LBM_DIVERGED when an active domain is not finite. */
+int lbm_batch_residuals(lbm_batch b, double *res);
+/* Retire (0) or re-activate (1) domains; retired domains keep their state. */
+int lbm_batch_set_active(lbm_batch b, const int *active);
+/* Step all active domains in chunks of check_every steps, retire each domain
+ * whose residual falls below tol, until none is active or max_steps steps
+ * ran.  steps[d] and res[d] (may be NULL) receive each domain's step count
+ * and last residual. */
+int lbm_batch_run_to_tolerance(lbm_batch b, double tol, int check_every, long long max_steps, long long *steps,
+                               double *res);
+int lbm_batch_get_macro(lbm_batch b, int domain, float *rho, float *u, float *v, float *w);
+int lbm_batch_get_populations(lbm_batch b, int domain, double *f);
+int lbm_batch_info(lbm_batch b, int *domains, long long *nodes, long long *fluid_nodes, int *active_tiles);
+long long lbm_batch_active_fluid_nodes(lbm_batch b);
+const char *lbm_batch_last_error(void);
+void lbm_batch_destroy(lbm_batch b);
 
 /* ---- Colour-gradient two-phase D2Q9 on a periodic lattice ----------------
  * The reference's multiphase 2D step (Iterate.cu:393-491): colour gradient

@@ -105,6 +105,20 @@ int lbm_read_initial_conditions(const char *path, long long nodes, int n, int m,
  * line counts differ or a file is unreadable. */
 int lbm_compare_results(const char *f1, const char *f2, double *diff_sum, double *diff_max);
 
+/* Cavity centre lines (WriteLidDrivenCavityMidLines3D, FilesWriting.cu:
+ * 260-302): 3D — for the nodes at y = m/2, u/Ulid and z along the line
+ * x = n/2, and x and w/Ulid along the line z = h/2, one row per pair,
+ * "%.8f\t%.8f\t%.8f\t%.8f"; 2D (the same layout for the 2D cavity) — u/Ulid
+ * and y along x = n/2, x and v/Ulid along y = m/2.  Header lines
+ * "CASE: Ulid = %f Nx = %d" and the column names. */
+int lbm_write_midlines(const char *path, int dims, int n, int m, int h, const float *x, const float *y,
+                       const float *z, const float *u, const float *v, const float *w, double ulid);
+
+/* Channel cross-section (WriteChannelCrossSection3D, FilesWriting.cu:304-336):
+ * every node of the plane x = (3/4) n, "x y z u v w". */
+int lbm_write_cross_section(const char *path, int n, int m, int h, const float *x, const float *y,
+                            const float *z, const float *u, const float *v, const float *w, double uin);
+
 /* Message of the last failing call on this thread. */
 const char *lbm_io_last_error(void);
 

@@ -4,7 +4,7 @@ Runs the reference solver's kernels compiled for the host (oracle/_ref, built
 by oracle/build_ref.sh from the reference tree) on lattices from
 thesis_gb300.lattice and stores their outputs, so machines without the
 reference tree can still pin the oracle.  Usage:
-    oracle/build_ref.sh && python tests/golden/make_golden.py
+    oracle/build_ref.sh && python tests/golden/make_golden.py [--cavity128]
 """
 import hashlib
 import os
@@ -63,5 +63,25 @@ def main():
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
+def main_cavity128():
+    """configs[0]: D2Q9 BGK lid-driven cavity 128x128, u_lid 0.1, Re 100
+    (nu = 0.128), 20,000 steps, FP32, by the reference's kernels; the final
+    rho, u, v and the centre lines go to cavity128_bgk_20000.npz."""
+    if pyoracle.ref_lib() is None:
+        sys.exit("oracle/_ref not built; run oracle/build_ref.sh first")
+    lat = lattice.cavity2d(128)
+    steps = 20000
+    r = pyoracle.run_reference(lat, steps, fp64=False, u=0.1, viscosity=0.128, collision_model=1, outlet_profile=1)
+    assert r.rc == 0
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "cavity128_bgk_20000.npz")
+    np.savez_compressed(path, rho=r.rho.astype(np.float32), u=r.u.astype(np.float32), v=r.v.astype(np.float32),
+                        resid=r.resid[-100:], steps=np.int64(steps),
+                        lattice_sha256=np.frombuffer(bc_hash(lat).encode(), np.uint8))
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
 if __name__ == "__main__":
-    main()
+    if "--cavity128" in sys.argv:
+        main_cavity128()
+    else:
+        main()

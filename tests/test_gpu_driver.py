@@ -1,0 +1,129 @@
+"""The file-driven drop-in (thesis_lbm_run): init file + Mesh/ files in the
+reference's formats in, FinalData and MacroDiffs out, on the GPU; and the
+MaxMacroDiff residual."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from thesis_gb300 import build, lattice
+from thesis_gb300 import native as N
+from thesis_gb300.solver import Arguments, Solver
+
+pytestmark = pytest.mark.gpu
+
+INIT = """Lattice = "cav"
+U= 0.1
+V= 0.0
+W= 0.0
+Density = 1.0
+viscosity = 0.128
+InletProfile = INLET_CTE
+CollisionModel = {coll}
+Walls = STRAIGHT
+BCwallModel = BBack
+BCoutlet = Vout
+Number of iterations = {iters}
+AutosaveAfter = 0
+AutosaveEach = 0
+MinMacroDiffs(u_v_w_rho)(StopCond) = {stop}
+OutputFormat = {fmt}
+InitialConditionFromFile = {ic}
+InitialFile = "{icfile}"
+ResidualModel = MaxMacroDiff
+ResidualsAndMacroDiffsAfter = 100
+Force = 0
+DragAndLift = 0
+UpdateInltOutl = yes
+"""
+
+
+def _setup(tmp_path, lat, **kw):
+    (tmp_path / "Mesh").mkdir(exist_ok=True)
+    lattice.write_files(lat, str(tmp_path / "Mesh" / "cav_Node.dat"), str(tmp_path / "Mesh" / "cav_BC.dat"))
+    d = dict(coll="SRT", iters=400, stop="0 0 0 0", fmt="CSV", ic="no", icfile="none")
+    d.update(kw)
+    (tmp_path / "SetUpData.ini").write_text(INIT.format(**d))
+
+
+def _run(tmp_path, *args):
+    build.build()
+    exe = build.tool_path("thesis_lbm_run")
+    return subprocess.run([exe] + list(args), cwd=str(tmp_path), capture_output=True, text=True, timeout=600)
+
+
+def test_driver_matches_api_run(tmp_path):
+    lat = lattice.cavity2d(40, 32)
+    _setup(tmp_path, lat)
+    r = _run(tmp_path)
+    assert r.returncode == 0, r.stderr
+    out = tmp_path / "Results" / "FinalData.csv"
+    rows = np.loadtxt(out, delimiter=",", skiprows=1)
+    assert rows.shape == (lat.num_nodes, 9)
+    # the init file's values are parsed into FP32, as the reference does
+    f32 = lambda v: float(np.float32(v))
+    with Solver(lat, Arguments(u=f32(0.1), viscosity=f32(0.128), collision_model=N.BGKW, outlet_profile=1)) as s:
+        s.init()
+        s.step(400, write_macro=True)
+        rho, u, v, w = s.macro()
+    # same library, same steps: equal up to the %.10f formatting of the file
+    np.testing.assert_allclose(rows[:, 3], u, atol=6e-11)
+    np.testing.assert_allclose(rows[:, 7], rho, atol=6e-11)
+    md = (tmp_path / "Results" / "MacroDiffs.txt").read_text().splitlines()
+    assert md[0].startswith("iteration") and len(md) == 1 + 4  # checks at 100, 200, 300, 400
+    # compare subcommand: identical files agree, an edited one does not
+    assert _run(tmp_path, "compare", str(out), str(out)).returncode == 0
+    edited = tmp_path / "edited.csv"
+    lines = out.read_text().splitlines()
+    parts = lines[5].split(", ")
+    parts[3] = "%.10f" % (float(parts[3]) + 0.01)
+    lines[5] = ", ".join(parts)
+    edited.write_text("\n".join(lines) + "\n")
+    assert _run(tmp_path, "compare", str(out), str(edited)).returncode == 1
+
+
+def test_driver_stop_condition_and_restart(tmp_path):
+    lat = lattice.cavity2d(24)
+    # changes per 100 steps below 1e-6 (physics mode: the lid is a moving
+    # wall, which conserves mass, so the density settles too)
+    stop = "1e-6 1e-6 1e-6 1e-6"
+    _setup(tmp_path, lat, iters=100000, stop=stop, coll="MRT")
+    r = _run(tmp_path, "--physics")
+    md = (tmp_path / "Results" / "MacroDiffs.txt").read_text().splitlines()
+    assert r.returncode == 0 and "converged" in r.stdout, (r.stderr, md[-3:])
+    last = [float(x) for x in md[-1].split()[1:]]
+    assert len(md) < 1000 and max(last) < 1e-6
+    # restart from the converged field (physics mode starts from f_eq of the
+    # given fields): far fewer checks until the stop test holds
+    (tmp_path / "Restart").mkdir()
+    os.replace(tmp_path / "Results" / "FinalData.csv", tmp_path / "Restart" / "s.csv")
+    _setup(tmp_path, lat, iters=100000, stop=stop, coll="MRT", ic="yes", icfile="Restart/s.csv")
+    r = _run(tmp_path, "-o", "Run2", "--physics")
+    assert r.returncode == 0, r.stderr
+    md2 = (tmp_path / "Run2" / "MacroDiffs.txt").read_text().splitlines()
+    assert len(md2) < len(md)
+
+
+def test_driver_missing_lattice(tmp_path):
+    (tmp_path / "SetUpData.ini").write_text(INIT.format(coll="SRT", iters=10, stop="0 0 0 0", fmt="CSV", ic="no",
+                                                        icfile="x"))
+    assert _run(tmp_path).returncode == 2
+
+
+def test_macro_diff_semantics():
+    lat = lattice.cavity2d(20)
+    with Solver(lat, Arguments(u=0.1, viscosity=0.1, collision_model=N.BGKW, mode=N.MODE_PHYSICS,
+                               init_equilibrium=1)) as s:
+        s.init()
+        s.step(10, write_macro=True)
+        _, u0, v0, _ = [a.astype(np.float64) for a in s.macro()]
+        d, rc = s.macro_diff()
+        assert rc == N.LBM_OK
+        # first call: against the initial fields (u = 0.1 everywhere, from params)
+        assert abs(d[0] - np.abs(u0 - np.float32(0.1)).max()) < 1e-7
+        assert abs(d[1] - np.abs(v0).max()) < 1e-7
+        s.step(10, write_macro=True)
+        _, u1, v1, _ = [a.astype(np.float64) for a in s.macro()]
+        d, rc = s.macro_diff()
+        assert abs(d[0] - np.abs(u1 - u0).max()) < 1e-7 and d[4] == 0

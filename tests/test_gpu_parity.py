@@ -237,3 +237,92 @@ def test_pair_kernel_matches_single_node_kernel(oracle, monkeypatch, storage):
     assert np.abs(out["pair"][0] - out["scalar"][0]).max() < tol
     for a, b in zip(out["pair"][1], out["scalar"][1]):
         assert np.abs(a - b).max() < tol
+
+
+@pytest.mark.parametrize("case", ["cavity2d_ref", "cavity3d_ref", "duct_phys"])
+def test_reference_l2_residual(oracle, case):
+    """lbm_residual_l2 (the reference's sqrt(sum (f - fColl)^2)) against the
+    oracle's per-iteration residual, which follows computeResidual2D/3D."""
+    if case == "cavity2d_ref":
+        lat = lattice.cavity2d(32, 24)
+        args = Arguments(u=0.1, viscosity=0.128, collision_model=N.MRT, outlet_profile=N.OUTLET_ZOUHE)
+        init = None
+    elif case == "cavity3d_ref":
+        lat = lattice.cavity3d(12, 10, 9)
+        args = Arguments(u=0.05, viscosity=0.1, collision_model=N.BGKW)
+        init = None
+    else:
+        lat = lattice.sphere_duct(24, 20, 40, porosity=0.8, rmin=3, rmax=5, seed=3)
+        args = Arguments(viscosity=0.1, collision_model=N.MRT, mode=N.MODE_PHYSICS, init_equilibrium=1,
+                         inlet_profile=N.INLET_PRESSURE, outlet_profile=N.OUTLET_PRESSURE, rho_in=1.01)
+        nn = lat.num_nodes
+        init = (np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
+    k = 30
+    with Solver(lat, args) as s:
+        s.init(*init) if init is not None else s.init()
+        s.step(k, write_macro=True)
+        r_gpu, rc = s.residual_l2()
+        assert rc == N.LBM_OK
+    okw = dict(u=args.u, v=args.v, w=args.w, rho=args.rho, viscosity=args.viscosity,
+               inlet_profile=args.inlet_profile, outlet_profile=args.outlet_profile,
+               collision_model=args.collision_model)
+    r = oracle.run_oracle(lat, k + 1, mode=args.mode, init_kind=args.init_equilibrium, rho_in=args.rho_in,
+                          rho_out=args.rho_out, init=init, **okw)
+    assert r.rc == 0
+    assert abs(r_gpu - r.resid[k]) <= 1e-4 * r.resid[k] + 1e-6, (r_gpu, r.resid[k])
+
+
+def test_momentum_exchange_matches_host_sum(oracle):
+    """lbm_momentum_exchange against the same link sum evaluated on the host
+    from the read-back populations and flag words; drag along the flow."""
+    from thesis_gb300.solver import build_flags
+    lat = lattice.channel2d(160, 48, seed=5)
+    args = Arguments(u=0.05, viscosity=0.05, collision_model=N.TRT, mode=N.MODE_PHYSICS, init_equilibrium=1,
+                     outlet_profile=N.OUTLET_PRESSURE, rho_out=1.0)
+    nn = lat.num_nodes
+    box = (10, 150, 1, 46, 0, 0)  # the obstacles, not the channel walls (out-of-domain links)
+    with Solver(lat, args) as s:
+        s.init(np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
+        s.step(300, write_macro=True)
+        F = s.momentum_exchange(box)
+        f = s.populations()
+    _, word, _, _ = build_flags(lat, args)
+    n, m = lat.n, lat.m
+    idx = np.arange(nn)
+    x, y = idx % n, idx // n
+    host = np.zeros(2)
+    for d in range(1, 9):
+        o = lattice.OPP2[d] if hasattr(lattice, "OPP2") else [0, 3, 4, 1, 2, 7, 8, 5, 6][d]
+        sx, sy = x - lattice.CX2[d], y - lattice.CY2[d]
+        sel = ((word & 1) == 1) & (((word >> d) & 1) == 1) & (sx >= box[0]) & (sx <= box[1]) & \
+              (sy >= box[2]) & (sy <= box[3]) & (sx >= 0) & (sx < n) & (sy >= 0) & (sy < m)
+        host[0] += 2 * lattice.CX2[o] * f[o, sel].sum()
+        host[1] += 2 * lattice.CY2[o] * f[o, sel].sum()
+    np.testing.assert_allclose(F[:2], host, rtol=1e-9, atol=1e-12)
+    assert F[2] == 0.0 and F[0] > 0  # obstacles are dragged downstream
+
+
+def test_full_cavity128_against_reference_golden():
+    """The BGK lid-driven cavity of the plain-method configuration (128x128,
+    u_lid 0.1, Re 100, 20,000 steps, FP32, reference semantics) against the
+    reference's own kernels' result (tests/golden/cavity128_bgk_20000.npz,
+    made by tests/golden/make_golden.py --cavity128).  FP32 in a different
+    operation order over 20,000 steps: 5e-5 absolute on u, v, rho and the
+    centre lines."""
+    import hashlib
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cavity128_bgk_20000.npz"))
+    lat = lattice.cavity2d(128)
+    sha = hashlib.sha256(np.ascontiguousarray(lat.bc).tobytes() + lat.node_type.tobytes()).hexdigest()
+    assert sha == bytes(g["lattice_sha256"]).decode()
+    args = Arguments(u=0.1, viscosity=0.128, collision_model=N.BGKW, outlet_profile=N.OUTLET_ZOUHE)
+    with Solver(lat, args) as s:
+        s.init()
+        s.step(int(g["steps"]), write_macro=True)
+        rho, u, v, _ = s.macro()
+    for a, b in ((rho, g["rho"]), (u, g["u"]), (v, g["v"])):
+        assert np.abs(a.astype(np.float64) - b).max() < 5e-5
+    U = u.reshape(128, 128)[:, 64]  # vertical centre line
+    V = v.reshape(128, 128)[64, :]  # horizontal centre line
+    np.testing.assert_allclose(U, g["u"].reshape(128, 128)[:, 64], atol=5e-5)
+    np.testing.assert_allclose(V, g["v"].reshape(128, 128)[64, :], atol=5e-5)

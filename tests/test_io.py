@@ -176,3 +176,38 @@ def test_compare_line_mismatch(native_lib, tmp_path):
     a.write_text("x,y,z,u,v,w,vel_mag,rho,press\n0, 0, 0, 0, 0, 0, 0, 1, 0.3\n")
     b.write_text("x,y,z,u,v,w,vel_mag,rho,press\n")
     assert native_lib.lbm_compare_results(str(a).encode(), str(b).encode(), None, None) == N.LBM_ERR_FILE
+
+
+def test_midlines_and_cross_section(native_lib, tmp_path):
+    n, m, h = 9, 7, 5
+    lat = lattice.cavity3d(n, m, h)
+    x, y, z = (a.astype(np.float32) for a in lat.coords())
+    u, v, w, _ = _fields(n, m, h, 3)
+    p = str(tmp_path / "midLines.txt")
+    assert native_lib.lbm_write_midlines(p.encode(), 3, n, m, h, _fp(x), _fp(y), _fp(z), _fp(u), _fp(v), _fp(w),
+                                         0.1) == 0
+    lines = open(p).read().splitlines()
+    assert lines[0] == "CASE: Ulid = 0.100000 Nx = %d" % n and lines[1] == "U/Ulid\tZ\tX\tW/Ulid"
+    rows = np.array([[float(c) for c in ln.split("\t")] for ln in lines[2:]])
+    assert rows.shape == (h, 4)
+    ids = (n // 2) + n * ((m // 2) + m * np.arange(h))
+    np.testing.assert_allclose(rows[:, 0], u[ids] / np.float32(0.1), atol=1e-7)
+    np.testing.assert_allclose(rows[:, 1], z[ids], atol=1e-7)
+    # 2D: u along x = n/2, v along y = m/2
+    lat2 = lattice.cavity2d(8, 6)
+    x2, y2, z2 = (a.astype(np.float32) for a in lat2.coords())
+    u2, v2, w2, _ = _fields(8, 6, 1, 4)
+    p2 = str(tmp_path / "mid2d.txt")
+    assert native_lib.lbm_write_midlines(p2.encode(), 2, 8, 6, 1, _fp(x2), _fp(y2), _fp(z2), _fp(u2), _fp(v2),
+                                         _fp(w2), 0.1) == 0
+    r2 = np.array([[float(c) for c in ln.split("\t")] for ln in open(p2).read().splitlines()[2:]])
+    np.testing.assert_allclose(r2[:6, 0], u2[4 + 8 * np.arange(6)] / np.float32(0.1), atol=1e-7)
+    np.testing.assert_allclose(r2[:8, 3], v2[np.arange(8) + 8 * 3] / np.float32(0.1), atol=1e-7)
+    # cross-section at x = 3n/4
+    p3 = str(tmp_path / "channelPlane.txt")
+    assert native_lib.lbm_write_cross_section(p3.encode(), n, m, h, _fp(x), _fp(y), _fp(z), _fp(u), _fp(v),
+                                              _fp(w), 0.05) == 0
+    l3 = open(p3).read().splitlines()
+    assert l3[1] == "X\tY\tZ\tU\tV\tW" and len(l3) == 2 + m * h
+    first = [float(c) for c in l3[2].split()]
+    assert abs(first[3] - u[int(0.75 * n)]) < 1e-9

@@ -56,7 +56,8 @@ def _newest_input():
 
 # Headers the run-time specialised step kernel is compiled from (lbm_jit.cpp).
 JIT_HEADERS = [os.path.join(ROOT, "include", "thesis_lbm.h")] + [
-    os.path.join(CSRC, f) for f in ("lbm_types.h", "lbm_device.cuh", "lbm_bc.cuh", "lbm_step.cuh")]
+    os.path.join(CSRC, f) for f in ("lbm_types.h", "lbm_device.cuh", "lbm_bc.cuh", "lbm_step.cuh",
+                                    "lbm_step_x2.cuh")]
 
 
 def write_jit_sources(path):

@@ -31,6 +31,14 @@ int launch_norms(const uint32_t *word, const float *rho, const float *ux, const 
                  const float *uz, float *pux, float *puy, float *puz, long long n,
                  double *partial, double *out, cudaStream_t s);
 int norm_partial_count();
+int launch_resid_l2_q9(const StepParams &p, int st, int phys, double *partial, double *out, cudaStream_t s);
+int launch_resid_l2_q19(const StepParams &p, int st, int phys, double *partial, double *out, cudaStream_t s);
+long long resid_l2_partials_q9(const StepParams &p);
+int launch_momentum_exchange_q9(const StepParams &p, int st, const int *box, double *partial, double *out,
+                                cudaStream_t s);
+int launch_momentum_exchange_q19(const StepParams &p, int st, const int *box, double *partial, double *out,
+                                 cudaStream_t s);
+long long resid_l2_partials_q19(const StepParams &p);
 int launch_macro_diff(const float *ux, const float *uy, const float *uz, const float *rho, float *pux, float *puy,
                       float *puz, float *prho, long long n, double *partial, double *out, cudaStream_t s);
 int tma_prepare(int q, int coll, int st, size_t smem, int *blocks_per_sm);
@@ -74,6 +82,9 @@ struct lbm_handle_s {
     std::vector<long long> slot_node;
     int cur = 0;
     cudaStream_t stream = nullptr;
+    // recorded after the steps of every lbm_step, on the stream they ran on;
+    // the handle's own stream waits for it before reductions and read-back
+    cudaEvent_t stepped = nullptr;
     cudaGraphExec_t pair[2] = {nullptr, nullptr};
     int status = LBM_OK;
     bool initialised = false;
@@ -118,10 +129,16 @@ static StepParams make_params(const lbm_handle_s *H, int from, int write_macro) 
     p.gshift = H->gshift;
     p.rho_in = H->P.rho_in;
     p.rho_out = H->P.rho_out;
+    p.rho0 = H->P.rho;
     p.scale = H->scale;
     p.inv_scale = 1.0f / H->scale;
-    for (int d = 0; d < H->q; ++d)
-        p.shift[d] = H->P.storage == LBM_STORE_F16S ? (float)rest_shift(H->q, H->P.collision_model, d) : 0.0f;
+    // populations stored as deviations from the rest state: F16S always, F32
+    // in physics mode (moments then come from small numbers, without the
+    // cancellation that limits an FP32 steady state to a ~1e-6 residual)
+    const bool shifted = H->P.storage == LBM_STORE_F16S ||
+                         (H->P.storage == LBM_STORE_F32 && H->P.mode == LBM_MODE_PHYSICS);
+    for (int d = 0; d < H->q; ++d) p.shift[d] = shifted ? (float)rest_shift(H->q, H->P.collision_model, d) : 0.0f;
+    p.sigma = shifted ? 1.f : 0.f;
     p.outlet_profile = H->P.outlet_profile;
     p.update_inlet_outlet = H->P.update_inlet_outlet;
     return p;
@@ -136,6 +153,7 @@ static void free_handle(lbm_handle_s *H) {
                     H->tma_row, H->tma_lmask, H->tma_omask, H->tma_err, H->mdiff_prev};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    if (H->stepped) cudaEventDestroy(H->stepped);
     if (H->stream) cudaStreamDestroy(H->stream);
     delete H;
 }
@@ -244,7 +262,9 @@ static bool open_outside_links(const std::vector<uint32_t> &word, int n, int m, 
 // lattice configuration for the rest of the process.
 struct TunedKnobs {
     int block, hint;
-    bool pred;
+    bool pred, pair;
+    int minb;
+    bool hspace;
 };
 static std::mutex g_tuned_mutex;
 static std::map<std::string, TunedKnobs> g_tuned;
@@ -257,20 +277,27 @@ static std::string tune_key(const JitStepKey &k) {
 }
 
 // Build the run-time specialised step kernel for this lattice.
-static int setup_jit(lbm_handle_s *H, const std::vector<uint32_t> &word) {
+static int setup_jit(lbm_handle_s *H, const std::vector<uint32_t> &word, bool pair, int hspace) {
     const bool periodic = H->P.mode == LBM_MODE_PHYSICS &&
                           (H->P.periodic[0] || H->P.periodic[1] || (H->dims == 3 && H->P.periodic[2]));
     const bool wrap = periodic || (H->q == 9 ? open_outside_links<9>(word, H->n, H->m, H->h)
                                              : open_outside_links<19>(word, H->n, H->m, H->h));
     JitStepKey k{H->q, H->P.collision_model, H->P.storage, H->P.mode == LBM_MODE_PHYSICS, wrap,
-                 H->n, H->m, H->h, STEP_BLOCK, 0, false, false};
+                 H->n, H->m, H->h, pair ? 64 : STEP_BLOCK, 0, false, false, pair};
+    // storage-unit arithmetic by default in physics mode (accuracy of the
+    // moments); reference mode keeps the f-space form of the reference
+    k.hspace = !pair && (hspace > 0 || (hspace < 0 && H->P.mode == LBM_MODE_PHYSICS &&
+                                        H->P.storage != LBM_STORE_F64));
     {
         std::lock_guard<std::mutex> lock(g_tuned_mutex);
         auto it = g_tuned.find(tune_key(k));
-        if (it != g_tuned.end()) {
+        if (it != g_tuned.end() && !pair) {
             k.block = it->second.block;
             k.hint = it->second.hint;
             k.pred = it->second.pred;
+            k.pair = it->second.pair;
+            k.minb = it->second.minb;
+            k.hspace = it->second.hspace;
         }
     }
     std::string err;
@@ -353,7 +380,8 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     long long fl = 0;
     for (long long i = 0; i < N; ++i) fl += (L->node_type[i] & 1);
     H->fluid = fl;
-    bool want_tma = false, want_jit = false, jit_required = false;
+    bool want_tma = false, want_jit = false, jit_required = false, jit_pair = false;
+    int jit_hspace = -1;
     {
         // Default: the one-node kernel specialised at run time for this
         // lattice (all population offsets become immediates; fastest for
@@ -364,8 +392,11 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
         const bool can_pair = (L->n % 2 == 0) && P->storage != LBM_STORE_F64;
         H->pair_kernel = kv && strcmp(kv, "pair") == 0 && can_pair;
         want_tma = kv && strcmp(kv, "tma") == 0;
-        want_jit = !kv || !*kv || strcmp(kv, "jit") == 0;
-        jit_required = kv && strcmp(kv, "jit") == 0;
+        want_jit = !kv || !*kv || strcmp(kv, "jit") == 0 || strcmp(kv, "jit2") == 0 || strcmp(kv, "jith") == 0 ||
+                   strcmp(kv, "jitf") == 0;
+        jit_required = kv && *kv && want_jit;
+        jit_pair = kv && strcmp(kv, "jit2") == 0 && can_pair;
+        jit_hspace = kv && strcmp(kv, "jith") == 0 ? 1 : (kv && strcmp(kv, "jitf") == 0 ? 0 : -1);
     }
     H->nslots = (int)flags.slot_node.size();
     H->slot_node = flags.slot_node;
@@ -377,7 +408,7 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
         }
     }
     if (want_jit) {
-        rc = setup_jit(H, flags.word);
+        rc = setup_jit(H, flags.word, jit_pair, jit_hspace);
         if (rc && jit_required) {
             free_handle(H);
             return rc;
@@ -412,6 +443,7 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     ALLOC(H->norms, sizeof(double) * LBM_NORMS);
 #undef ALLOC
     cudaError_t e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&H->stepped, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMemcpy(H->word, flags.word.data(), sizeof(uint32_t) * N, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(H->slot, flags.slot.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && H->nslots) {
@@ -506,7 +538,8 @@ static int launch(lbm_handle_s *H, int from, int write_macro, cudaStream_t s) {
     int rc;
     if (H->jit_kernel) {
         const int bx = H->jit_key.block;
-        const dim3 grid((unsigned)((H->n + bx - 1) / bx), (unsigned)H->m, (unsigned)H->h);
+        const int units = H->jit_key.pair ? H->n / 2 : H->n;  // threads along x (h-space: one node each)
+        const dim3 grid((unsigned)((units + bx - 1) / bx), (unsigned)H->m, (unsigned)H->h);
         void *args[] = {(void *)&p};
         cudaError_t e = cudaLaunchKernel((const void *)H->jit_fn, grid, dim3((unsigned)bx), args, 0, s);
         return e == cudaSuccess ? LBM_OK : fail(LBM_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
@@ -570,6 +603,7 @@ int lbm_step(lbm_handle H, int nsteps, int write_macro_last, void *stream) {
         H->cur ^= 1;
     }
     cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventRecord(H->stepped, s);
     if (e != cudaSuccess) {
         H->status = LBM_ERR_CUDA;
         return fail(LBM_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
@@ -611,6 +645,7 @@ int lbm_get_populations(lbm_handle H, double *f) {
 
 int lbm_macro_norms(lbm_handle H, double *out) {
     if (!H || !out) return fail(LBM_ERR_INVALID, "null argument");
+    CUDA_TRY(cudaStreamWaitEvent(H->stream, H->stepped, 0));
     launch_norms(H->word, H->rho, H->ux, H->uy, H->uz, H->pux, H->puy, H->puz, H->N, H->partial,
                  H->norms, H->stream);
     CUDA_TRY(cudaGetLastError());
@@ -625,8 +660,54 @@ int lbm_macro_norms(lbm_handle H, double *out) {
     return LBM_OK;
 }
 
+int lbm_residual_l2(lbm_handle H, double *out) {
+    if (!H || !out) return fail(LBM_ERR_INVALID, "null argument");
+    if (!H->initialised) return fail(LBM_ERR_INVALID, "lbm_init has not been called");
+    CUDA_TRY(cudaStreamWaitEvent(H->stream, H->stepped, 0));
+    const StepParams p = make_params(H, H->cur, 0);
+    const long long nb = H->q == 9 ? resid_l2_partials_q9(p) : resid_l2_partials_q19(p);
+    double *partial = nullptr;
+    CUDA_TRY(cudaMallocAsync((void **)&partial, sizeof(double) * (nb + 1), H->stream));
+    if (H->q == 9) launch_resid_l2_q9(p, H->P.storage, H->P.mode == LBM_MODE_PHYSICS, partial, partial + nb, H->stream);
+    else launch_resid_l2_q19(p, H->P.storage, H->P.mode == LBM_MODE_PHYSICS, partial, partial + nb, H->stream);
+    cudaError_t e = cudaGetLastError();
+    double s = 0.0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&s, partial + nb, sizeof(double), cudaMemcpyDeviceToHost, H->stream);
+    cudaFreeAsync(partial, H->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("L2 residual: ") + cudaGetErrorString(e));
+    *out = sqrt(s);
+    if (!(*out == *out)) {
+        H->status = LBM_DIVERGED;
+        return fail(LBM_DIVERGED, "non-finite populations (divergence)");
+    }
+    return LBM_OK;
+}
+
+int lbm_momentum_exchange(lbm_handle H, const int *box, double *force) {
+    if (!H || !box || !force) return fail(LBM_ERR_INVALID, "null argument");
+    if (!H->initialised) return fail(LBM_ERR_INVALID, "lbm_init has not been called");
+    if (H->P.mode != LBM_MODE_PHYSICS)
+        return fail(LBM_ERR_UNSUPPORTED, "momentum exchange needs physics mode's half-way bounce-back");
+    CUDA_TRY(cudaStreamWaitEvent(H->stream, H->stepped, 0));
+    const StepParams p = make_params(H, H->cur, 0);
+    const long long nb = H->q == 9 ? resid_l2_partials_q9(p) : resid_l2_partials_q19(p);
+    double *partial = nullptr;
+    CUDA_TRY(cudaMallocAsync((void **)&partial, sizeof(double) * (3 * nb + 3), H->stream));
+    if (H->q == 9) launch_momentum_exchange_q9(p, H->P.storage, box, partial, partial + 3 * nb, H->stream);
+    else launch_momentum_exchange_q19(p, H->P.storage, box, partial, partial + 3 * nb, H->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(force, partial + 3 * nb, sizeof(double) * 3, cudaMemcpyDeviceToHost, H->stream);
+    cudaFreeAsync(partial, H->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("momentum exchange: ") + cudaGetErrorString(e));
+    return LBM_OK;
+}
+
 int lbm_macro_diff(lbm_handle H, double *out) {
     if (!H || !out) return fail(LBM_ERR_INVALID, "null argument");
+    CUDA_TRY(cudaStreamWaitEvent(H->stream, H->stepped, 0));
     const long long N = H->N;
     launch_macro_diff(H->ux, H->uy, H->uz, H->rho, H->mdiff_prev, H->mdiff_prev + N, H->mdiff_prev + 2 * N,
                       H->mdiff_prev + 3 * N, N, H->partial, H->norms, H->stream);
@@ -671,16 +752,44 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
     if (!H) return fail(LBM_ERR_INVALID, "null handle");
     if (!H->jit_kernel) return fail(LBM_ERR_UNSUPPORTED, "autotuning needs the run-time specialised kernel");
     if (trial_steps < 2) trial_steps = 2;
+    // one node per thread: block, load form, bounce-back form, and a register
+    // cap that buys occupancy; two nodes per thread: block and register cap
+    // one node per thread in f space: block, load form, bounce-back form and a
+    // register cap that buys occupancy; in storage units (h): block and
+    // register cap; two nodes per thread (storage units): block and cap.
+    // Physics-mode F32 keeps to the storage-unit kernels, whose moments come
+    // from deviations: an f-space kernel would bring back the ~1e-6 residual
+    // floor of cancelling FP32 sums.
+    struct V {
+        int block, hint, pred, pair, minb, hs;
+    };
+    const bool fspace_ok = !(H->P.mode == LBM_MODE_PHYSICS && H->P.storage == LBM_STORE_F32);
+    const bool hs_ok = H->P.storage != LBM_STORE_F64;
+    std::vector<V> vs;
+    if (fspace_ok) {
+        const V fv[] = {{128, 0, 0, 0, 1, 0}, {128, 1, 0, 0, 1, 0}, {128, 0, 1, 0, 1, 0}, {128, 1, 1, 0, 1, 0},
+                        {256, 0, 0, 0, 1, 0}, {256, 1, 1, 0, 1, 0}, {128, 1, 1, 0, 12, 0}};
+        vs.insert(vs.end(), fv, fv + 7);
+    }
+    if (hs_ok) {
+        const V hv[] = {{128, 0, 0, 0, 1, 1}, {128, 0, 0, 0, 10, 1}, {256, 0, 0, 0, 1, 1}, {256, 0, 0, 0, 5, 1}};
+        vs.insert(vs.end(), hv, hv + 4);
+    }
+    if (H->n % 2 == 0 && hs_ok) {
+        const V pv[] = {{64, 0, 0, 1, 1, 0}, {128, 0, 0, 1, 1, 0}, {64, 0, 0, 1, 12, 0}, {128, 0, 0, 1, 6, 0}};
+        vs.insert(vs.end(), pv, pv + 4);
+    }
     std::vector<JitStepKey> cand;
-    for (int b : {128, 256})
-        for (int hi : {0, 1})
-            for (int pr : {0, 1}) {
-                JitStepKey k = H->jit_key;
-                k.block = b;
-                k.hint = hi;
-                k.pred = pr != 0;
-                cand.push_back(k);
-            }
+    for (const V &v : vs) {
+        JitStepKey k = H->jit_key;
+        k.block = v.block;
+        k.hint = v.hint;
+        k.pred = v.pred != 0;
+        k.pair = v.pair != 0;
+        k.minb = v.minb;
+        k.hspace = v.hs != 0;
+        cand.push_back(k);
+    }
     std::vector<cudaKernel_t> fn(cand.size(), nullptr);
     std::vector<std::string> errs(cand.size());
     {
@@ -729,26 +838,32 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
         }
     {
         std::lock_guard<std::mutex> lock(g_tuned_mutex);
-        g_tuned[tune_key(H->jit_key)] = TunedKnobs{H->jit_key.block, H->jit_key.hint, H->jit_key.pred};
+        g_tuned[tune_key(H->jit_key)] = TunedKnobs{H->jit_key.block, H->jit_key.hint, H->jit_key.pred,
+                                                   H->jit_key.pair, H->jit_key.minb, H->jit_key.hspace};
     }
     H->initialised = false;  // the trial steps leave the populations undefined
     if (block) *block = H->jit_key.block;
-    if (hint) *hint = H->jit_key.hint;
-    if (pred) *pred = H->jit_key.pred ? 1 : 0;
+    if (hint) *hint = H->jit_key.hint | (H->jit_key.hspace ? 2 : 0);
+    if (pred) *pred = (H->jit_key.pred ? 1 : 0) | (H->jit_key.pair ? 2 : 0) | (H->jit_key.minb > 1 ? H->jit_key.minb << 2 : 0);
     return LBM_OK;
 }
 
 int lbm_kernel_config(lbm_handle H, int *block, int *hint, int *pred) {
     if (!H) return fail(LBM_ERR_INVALID, "null handle");
     if (block) *block = H->jit_kernel ? H->jit_key.block : STEP_BLOCK;
-    if (hint) *hint = H->jit_kernel ? H->jit_key.hint : 0;
-    if (pred) *pred = H->jit_kernel && H->jit_key.pred ? 1 : 0;
+    if (hint) *hint = H->jit_kernel ? H->jit_key.hint | (H->jit_key.hspace ? 2 : 0) : 0;
+    if (pred)
+        *pred = H->jit_kernel ? (H->jit_key.pred ? 1 : 0) | (H->jit_key.pair ? 2 : 0) |
+                                    (H->jit_key.minb > 1 ? H->jit_key.minb << 2 : 0)
+                              : 0;
     return LBM_OK;
 }
 
 int lbm_jit_check(int q, int coll, int storage, int phys, int wrap, int nx, int ny, int nz, int block, int hint,
                   int pred) {
-    JitStepKey k{q, coll, storage, phys != 0, wrap != 0, nx, ny, nz, block, hint, pred != 0, true};
+    JitStepKey k{q, coll, storage, phys != 0, wrap != 0, nx, ny, nz, block, hint & 1, (pred & 1) != 0, true,
+                 (pred & 2) != 0, (pred >> 2) > 1 ? (pred >> 2) : 1};
+    k.hspace = (hint & 2) != 0;
     std::string err;
     if (jit_step_kernel(k, nullptr, err)) return fail(LBM_ERR_CUDA, err);
     return LBM_OK;

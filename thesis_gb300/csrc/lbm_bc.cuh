@@ -214,6 +214,22 @@ __device__ __forceinline__ void zou_he_face(R (&f)[Q], bool pressure, R rho_set,
     }
 }
 
+// Moving wall (Ladd): after half-way bounce-back, each incoming population d
+// of a wall link gains 6 w_d rho_0 (c_d . u_w), rho_0 the reference density.
+// For a wall velocity tangential to the face the gains cancel pairwise, so the
+// node's mass is unchanged.  (The node's own density in place of rho_0 feeds
+// back on itself and slowly destabilises a cavity lid.)
+template <int Q, class R>
+__device__ __forceinline__ void bc_moving_wall(R (&f)[Q], unsigned long long links, R rho, R uwx, R uwy, R uwz) {
+    using L = Lat<Q>;
+#pragma unroll
+    for (int d = 1; d < Q; ++d)
+        if ((links >> d) & 1ull) {
+            const R cu = (R)L::cx(d) * uwx + (R)L::cy(d) * uwy + (R)L::cz(d) * uwz;
+            f[d] += (R)(6.0 * L::w(d)) * rho * cu;
+        }
+}
+
 template <int Q, class R>
 __device__ __forceinline__ void bc_phys(R (&f)[Q], int face, bool pressure, R rho_set, R ux, R uy, R uz) {
     switch (face) {

@@ -231,6 +231,7 @@ struct lbm_cg_handle_s {
     double *partial = nullptr, *sums = nullptr;
     int cur = 0;
     cudaStream_t stream = nullptr;
+    cudaEvent_t stepped = nullptr;  // after the last lbm_cg_step, on its stream
 };
 
 static CgArgs cg_args(const lbm_cg_handle_s *H, int from, int write_macro) {
@@ -296,6 +297,7 @@ int lbm_cg_create(int n, int m, const lbm_cg_params *P, lbm_cg_handle *out) {
     if (e == cudaSuccess) e = cudaMalloc((void **)&H->R, sizeof(float) * 5 * N);
     if (e == cudaSuccess) e = cudaMalloc((void **)&H->partial, sizeof(double) * (LAP_BLOCKS * 5 + 5));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&H->stepped, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         lbm_cg_destroy(H);
         return cg_fail(LBM_ERR_NOMEM, std::string("allocation: ") + cudaGetErrorString(e));
@@ -335,6 +337,7 @@ int lbm_cg_step(lbm_cg_handle H, int nsteps, int write_macro_last, void *stream)
         H->cur ^= 1;
     }
     cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventRecord(H->stepped, s);
     if (e != cudaSuccess) return cg_fail(LBM_ERR_CUDA, std::string("step: ") + cudaGetErrorString(e));
     return LBM_OK;
 }
@@ -364,6 +367,7 @@ int lbm_cg_get_populations(lbm_cg_handle H, float *r, float *b) {
 
 int lbm_cg_laplace(lbm_cg_handle H, double *out) {
     if (!H || !out) return cg_fail(LBM_ERR_INVALID, "null argument");
+    if (H->stepped) cudaStreamWaitEvent(H->stream, H->stepped, 0);
     cg_laplace_partial<<<LAP_BLOCKS, LAP_THREADS, 0, H->stream>>>(H->R, H->B, H->ux, H->uy, H->N,
                                                                    (float)H->P.control_param, H->partial);
     cg_laplace_final<<<1, 32, 0, H->stream>>>(H->partial, H->sums);
@@ -384,6 +388,7 @@ void lbm_cg_destroy(lbm_cg_handle H) {
     if (H->buf) cudaFree(H->buf);
     if (H->R) cudaFree(H->R);
     if (H->partial) cudaFree(H->partial);
+    if (H->stepped) cudaEventDestroy(H->stepped);
     if (H->stream) cudaStreamDestroy(H->stream);
     delete H;
 }

@@ -154,13 +154,15 @@ __device__ __forceinline__ double ld_pop(const double *p) {
 }
 
 template <int ST> struct Store;
+// F32 holds f - shift: the deviation from the collision model's rest state in
+// physics mode (shift 0 in reference mode, which keeps the reference's f).
 template <> struct Store<LBM_STORE_F32> {
     using T = float;   // element type in HBM
     using R = float;   // arithmetic type
-    __device__ static __forceinline__ R load(const T *p, float, float) { return __ldg(p); }
-    __device__ static __forceinline__ R decode(T v, float, float) { return v; }
-    __device__ static __forceinline__ void store(T *p, R v, float, float) { *p = v; }
-    __device__ static __forceinline__ T encode(R v, float, float) { return v; }
+    __device__ static __forceinline__ R load(const T *p, float w, float) { return __ldg(p) + w; }
+    __device__ static __forceinline__ R decode(T v, float w, float) { return v + w; }
+    __device__ static __forceinline__ void store(T *p, R v, float w, float) { *p = v - w; }
+    __device__ static __forceinline__ T encode(R v, float w, float) { return v - w; }
 };
 template <> struct Store<LBM_STORE_F16S> {
     using T = __half;

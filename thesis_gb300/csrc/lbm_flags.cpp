@@ -251,6 +251,25 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
                 if (((r.linked[(size_t)ind] >> d) & 1u) && ref_type(r, node, d) == mt)
                     face = face_of_link(q, d);
             if (face < 0) continue;
+            // a velocity inlet whose velocity has no component along the
+            // face normal is a moving wall (a cavity lid): bounce-back plus
+            // the wall's momentum on every inlet link conserves mass exactly,
+            // where the Zou-He closure lets the mean density drift
+            if (mt == LBM_BC_INLET && P.inlet_profile != LBM_INLET_PRESSURE) {
+                const double nrm = face < 2 ? P.u : (face < 4 ? P.v : (q == 19 ? P.w : 0.0));
+                if (nrm == 0.0) {
+                    uint64_t moving = 0;
+                    for (int d = 1; d < q; ++d)
+                        if (((r.linked[(size_t)ind] >> d) & 1u) && ref_type(r, node, d) == LBM_BC_INLET)
+                            moving |= 1ull << lattice_opp(q, d);
+                    out.slot[(size_t)ind] = (int32_t)out.slot_node.size();
+                    out.slot_node.push_back(ind);
+                    out.mask.push_back(moving);
+                    out.kind.push_back(face | BCK_ACTIVE | BCK_MOVING);
+                    out.word[(size_t)ind] |= W_SPECIAL;
+                    continue;
+                }
+            }
             kind = face | BCK_ACTIVE;
             if (mt == LBM_BC_INLET) {
                 if (P.inlet_profile == LBM_INLET_PRESSURE) kind |= BCK_PRESSURE;

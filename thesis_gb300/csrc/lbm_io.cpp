@@ -336,6 +336,66 @@ int lbm_read_initial_conditions(const char *path, long long nodes, int n, int m,
     return LBM_OK;
 }
 
+int lbm_write_midlines(const char *path, int dims, int n, int m, int h, const float *x, const float *y,
+                       const float *z, const float *u, const float *v, const float *w, double ulid) {
+    if (!path || !x || !y || !u || !v || (dims == 3 && (!z || !w)) || !(ulid != 0))
+        return io_fail(LBM_ERR_INVALID, "invalid argument");
+    FILE *f = fopen(path, "w");
+    if (!f) return io_fail(LBM_ERR_FILE, std::string("cannot write ") + path);
+    fprintf(f, "CASE: Ulid = %f Nx = %d\n", ulid, n);
+    const float U = (float)ulid;
+    if (dims == 3) {
+        // the reference pairs the k-th node of one line with the k-th of the other
+        fprintf(f, "U/Ulid\tZ\tX\tW/Ulid\n");
+        std::vector<float> uz, zz, xx, wx;
+        const int yc = m / 2, xc = n / 2, zc = h / 2;
+        for (int k = 0; k < h; ++k)
+            for (int i = 0; i < n; ++i) {
+                const size_t id = (size_t)i + (size_t)n * (yc + (size_t)m * k);
+                if (i == xc) {
+                    uz.push_back(u[id] / U);
+                    zz.push_back(z[id]);
+                }
+                if (k == zc) {
+                    xx.push_back(x[id]);
+                    wx.push_back(w[id] / U);
+                }
+            }
+        for (size_t r = 0; r < uz.size(); ++r)
+            fprintf(f, "%.8f\t%.8f\t%.8f\t%.8f\n", uz[r], zz[r], r < xx.size() ? xx[r] : 0.f,
+                    r < wx.size() ? wx[r] : 0.f);
+    } else {
+        fprintf(f, "U/Ulid\tY\tX\tV/Ulid\n");
+        const int xc = n / 2, yc = m / 2;
+        const int rows = m > n ? m : n;
+        for (int r = 0; r < rows; ++r) {
+            const size_t a = (size_t)xc + (size_t)n * (r < m ? r : m - 1);  // along x = n/2
+            const size_t b = (size_t)(r < n ? r : n - 1) + (size_t)n * yc;  // along y = m/2
+            fprintf(f, "%.8f\t%.8f\t%.8f\t%.8f\n", r < m ? u[a] / U : 0.f, r < m ? y[a] : 0.f,
+                    r < n ? x[b] : 0.f, r < n ? v[b] / U : 0.f);
+        }
+    }
+    fclose(f);
+    return LBM_OK;
+}
+
+int lbm_write_cross_section(const char *path, int n, int m, int h, const float *x, const float *y,
+                            const float *z, const float *u, const float *v, const float *w, double uin) {
+    if (!path || !x || !y || !z || !u || !v || !w) return io_fail(LBM_ERR_INVALID, "null argument");
+    FILE *f = fopen(path, "w");
+    if (!f) return io_fail(LBM_ERR_FILE, std::string("cannot write ") + path);
+    fprintf(f, "CASE: Uin = %f Ny = %d\n", uin, m);
+    fprintf(f, "X\tY\tZ\tU\tV\tW\n");
+    const int xc = (int)((3. / 4.) * n);
+    for (int k = 0; k < h; ++k)
+        for (int j = 0; j < m; ++j) {
+            const size_t id = (size_t)xc + (size_t)n * (j + (size_t)m * k);
+            fprintf(f, "%.10f %.10f %.10f %.10f %.10f %.10f\n", x[id], y[id], z[id], u[id], v[id], w[id]);
+        }
+    fclose(f);
+    return LBM_OK;
+}
+
 int lbm_compare_results(const char *f1, const char *f2, double *diff_sum, double *diff_max) {
     const long long l1 = lbm_count_lines(f1), l2 = lbm_count_lines(f2);
     if (l1 < 0 || l2 < 0) return io_fail(LBM_ERR_FILE, "cannot read a result file");

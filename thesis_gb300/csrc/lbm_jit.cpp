@@ -33,11 +33,16 @@ const char *kStddef = "#pragma once\ntypedef unsigned long size_t;\n";
 }  // namespace
 
 int jit_step_kernel(const JitStepKey &k, cudaKernel_t *out, std::string &err) {
-    const std::string expr = "lbm::step_kernel_fixed<" + std::to_string(k.q) + ", " + std::to_string(k.coll) +
-                             ", " + std::to_string(k.storage) + ", " + (k.phys ? "true" : "false") + ", " +
-                             (k.wrap ? "true" : "false") + ", " + std::to_string(k.nx) + ", " +
-                             std::to_string(k.ny) + ", " + std::to_string(k.nz) + ", " + std::to_string(k.block) +
-                             ", " + std::to_string(k.hint) + ", " + (k.pred ? "true" : "false") + ">";
+    const std::string common = std::to_string(k.q) + ", " + std::to_string(k.coll) + ", " +
+                               std::to_string(k.storage) + ", " + (k.phys ? "true" : "false") + ", " +
+                               (k.wrap ? "true" : "false") + ", " + std::to_string(k.nx) + ", " +
+                               std::to_string(k.ny) + ", " + std::to_string(k.nz) + ", " + std::to_string(k.block);
+    const std::string minb = std::to_string(k.minb > 0 ? k.minb : 1);
+    const std::string expr =
+        k.pair     ? "lbm::step_kernel_x2_fixed<" + common + ", " + minb + ">"
+        : k.hspace ? "lbm::step_kernel_h_fixed<" + common + ", " + minb + ">"
+                   : "lbm::step_kernel_fixed<" + common + ", " + std::to_string(k.hint) + ", " +
+                         (k.pred ? "true" : "false") + ", " + minb + ">";
     {
         std::lock_guard<std::mutex> lock(g_jit_mutex);
         auto it = g_jit_cache.find(expr);
@@ -56,7 +61,7 @@ int jit_step_kernel(const JitStepKey &k, cudaKernel_t *out, std::string &err) {
     names.push_back("stdint.h");
     hdr.push_back(kStddef);
     names.push_back("stddef.h");
-    const char *src = "#include \"lbm_step.cuh\"\n";
+    const char *src = "#include \"lbm_step_x2.cuh\"\n";
     nvrtcProgram prog;
     nvrtcResult r = nvrtcCreateProgram(&prog, src, "lbm_step_fixed.cu", (int)hdr.size(), hdr.data(), names.data());
     if (r != NVRTC_SUCCESS) {

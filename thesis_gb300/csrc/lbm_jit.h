@@ -14,6 +14,9 @@ struct JitStepKey {
     int hint;           // population load form (ld_pop)
     bool pred;          // blocked links by predicated loads
     bool compile_only;  // compile to a cubin and stop (no GPU needed)
+    bool pair;          // two nodes per thread (step_kernel_x2_fixed; hint, pred unused)
+    int minb = 1;       // __launch_bounds__ minimum blocks per SM (1: no constraint)
+    bool hspace = false;  // one node per thread in storage units (step_kernel_h_fixed)
 };
 
 // Compile (or fetch from the process cache) step_kernel_fixed for `k` and

@@ -54,6 +54,35 @@ int launch_init_q19(const StepParams &p, const StepParams &o, int coll, int st, 
     return -1;
 }
 
+// The reference's L2 residual: per-block partials, then their fixed-order sum.
+int launch_resid_l2_q19(const StepParams &p, int st, int phys, double *partial, double *out, cudaStream_t s) {
+    const dim3 grid = node_grid(p);
+    const long long nb = (long long)grid.x * grid.y * grid.z;
+#define R_CASE(S, P)                                                               \
+    if (st == S && (phys != 0) == P) resid_l2_kernel<19, S, P><<<grid, STEP_BLOCK, 0, s>>>(p, partial);
+    R_CASE(0, false) R_CASE(1, false) R_CASE(2, false) R_CASE(0, true) R_CASE(1, true) R_CASE(2, true)
+#undef R_CASE
+    sum_partials_kernel<<<1, 1024, 0, s>>>(partial, nb, out);
+    return 0;
+}
+
+int launch_momentum_exchange_q19(const StepParams &p, int st, const int *box, double *partial, double *out,
+                                 cudaStream_t s) {
+    const dim3 grid = node_grid(p);
+    const long long nb = (long long)grid.x * grid.y * grid.z;
+    const int4 lo = make_int4(box[0], box[2], box[4], 0), hi = make_int4(box[1], box[3], box[5], 0);
+    if (st == LBM_STORE_F32) momentum_exchange_kernel<19, LBM_STORE_F32><<<grid, STEP_BLOCK, 0, s>>>(p, lo, hi, partial, nb);
+    else if (st == LBM_STORE_F16S) momentum_exchange_kernel<19, LBM_STORE_F16S><<<grid, STEP_BLOCK, 0, s>>>(p, lo, hi, partial, nb);
+    else momentum_exchange_kernel<19, LBM_STORE_F64><<<grid, STEP_BLOCK, 0, s>>>(p, lo, hi, partial, nb);
+    for (int k = 0; k < 3; ++k) sum_partials_kernel<<<1, 1024, 0, s>>>(partial + k * nb, nb, out + k);
+    return 0;
+}
+
+long long resid_l2_partials_q19(const StepParams &p) {
+    const dim3 g = node_grid(p);
+    return (long long)g.x * g.y * g.z;
+}
+
 int launch_decode_q19(const StepParams &p, int st, double *out, long long n, cudaStream_t s) {
     const unsigned blocks = (unsigned)((n + 255) / 256);
     if (st == LBM_STORE_F32) decode_kernel<19, LBM_STORE_F32><<<blocks, 256, 0, s>>>(p, out, n);

@@ -38,10 +38,13 @@ struct StepParams {
     int write_macro;
     double omega, omega_m, gshift;
     double rho_in, rho_out;
+    double rho0;  // reference density (moving walls)
     float scale, inv_scale;
-    // F16S storage holds (f_d - shift_d) * scale: shift is the collision
-    // model's rest-state equilibrium (0 for F32/F64 storage)
+    // F16S storage holds (f_d - shift_d) * scale and physics-mode F32 storage
+    // f_d - shift_d: shift is the collision model's rest-state equilibrium
+    // (0 for F64 and reference-mode F32); sigma is 1 when shift is applied
     float shift[19];
+    float sigma;
     int outlet_profile;
     int update_inlet_outlet;
     // initial state (init kernel only): constants for the fields not given as
@@ -71,12 +74,17 @@ __device__ __forceinline__ void collide(typename Store<ST>::R (&f)[Q], typename 
 
 // Everything a fluid node does after its populations are gathered: boundary
 // conditions, macroscopic moments (stored when p.write_macro), collision.
-template <int Q, int COLL, int ST, bool PHYS>
-__device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], uint32_t w, int node,
-                                            const StepParams &p) {
+// Boundary conditions of a fluid node whose populations are gathered
+// (pulled, bounced back): Zou-He faces, moving walls, the reference's wall
+// copies.  keep_macro / zero_v report the reference's 3D inlet and 2D outlet
+// special cases.
+template <int Q, int ST, bool PHYS>
+__device__ __forceinline__ void apply_bc(typename Store<ST>::R (&f)[Q], uint32_t w, int node, const StepParams &p,
+                                         bool &keep_macro, bool &zero_v) {
     using R = typename Store<ST>::R;
     using L = Lat<Q>;
-    bool keep_macro = false, zero_v = false;
+    keep_macro = false;
+    zero_v = false;
     if (w & W_SPECIAL) {
         const int sl = __ldg(p.slot + node);
         const R u0 = (R)__ldg(p.bc_uvw + 3 * sl), v0 = (R)__ldg(p.bc_uvw + 3 * sl + 1),
@@ -89,7 +97,9 @@ __device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], uint3
                 bc_ref_d3q19<R>(f, mk, u0, v0, w0, p.update_inlet_outlet, keep_macro);
         } else {
             const int kind = __ldg(p.bc_kind + sl);
-            if (kind & BCK_ACTIVE) {
+            if (kind & BCK_MOVING) {
+                bc_moving_wall<Q, R>(f, __ldg(p.bc_mask + sl), (R)p.rho0, u0, v0, w0);
+            } else if (kind & BCK_ACTIVE) {
                 const bool pressure = (kind & BCK_PRESSURE) != 0;
                 const R rset = (kind & BCK_OUTLET) ? (R)p.rho_out : (R)p.rho_in;
                 bc_phys<Q, R>(f, kind & BCK_FACE_MASK, pressure, rset, u0, v0, w0);
@@ -103,6 +113,15 @@ __device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], uint3
         for (int dir = 1; dir < Q; ++dir)
             if ((w >> L::opp(dir)) & 1u) f[L::opp(dir)] = f[dir];
     }
+}
+
+template <int Q, int COLL, int ST, bool PHYS>
+__device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], uint32_t w, int node,
+                                            const StepParams &p) {
+    using R = typename Store<ST>::R;
+    using L = Lat<Q>;
+    bool keep_macro, zero_v;
+    apply_bc<Q, ST, PHYS>(f, w, node, p, keep_macro, zero_v);
 
     R rho = 0, jx = 0, jy = 0, jz = 0;
 #pragma unroll
@@ -145,6 +164,51 @@ struct FixedGeom {
     static constexpr int nx = NX, ny = NY, nz = NZ, pitch = PITCH;
 };
 
+// Populations of a fluid node after streaming: pulled from x - c_d, or
+// across a blocked link the node's own population (opp(d) for half-way
+// bounce-back, d itself in the reference's wall model).  `in` points at the
+// node's own element of direction 0.
+template <int Q, int ST, bool PHYS, bool WRAP, class G, int HINT, bool PRED>
+__device__ __forceinline__ void gather_node(const StepParams &p, const G &g, int x, int y, int z, uint32_t w,
+                                            const typename Store<ST>::T *in, typename Store<ST>::R (&f)[Q]) {
+    using S = Store<ST>;
+    using T = typename S::T;
+    using L = Lat<Q>;
+    // Pull offsets to the six face neighbours.  With WRAP, coordinates wrap
+    // and links that must not wrap are blocked in the flag word, so a wrapped
+    // address is only read where the lattice is periodic.
+    const int plane = g.pitch * g.ny;
+    int oxm = -1, oxp = 1, oym = -g.pitch, oyp = g.pitch, ozm = -plane, ozp = plane;
+    if (WRAP) {
+        oxm = x == 0 ? g.nx - 1 : -1;
+        oxp = x == g.nx - 1 ? 1 - g.nx : 1;
+        oym = y == 0 ? (g.ny - 1) * g.pitch : -g.pitch;
+        oyp = y == g.ny - 1 ? (1 - g.ny) * g.pitch : g.pitch;
+        ozm = z == 0 ? (g.nz - 1) * plane : -plane;
+        ozp = z == g.nz - 1 ? (1 - g.nz) * plane : plane;
+    }
+
+    f[0] = S::decode(ld_pop<HINT>(in), p.shift[0], p.inv_scale);
+#pragma unroll
+    for (int d = 1; d < Q; ++d) {
+        const int pull = d * g.nx + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
+                         (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
+                         (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
+        // across a blocked link: the node's own population, opp(d) for
+        // half-way bounce-back, d itself in the reference's wall model
+        const int own = (PHYS ? L::opp(d) : d) * g.nx;
+        const bool blocked = (w >> d) & 1u;
+        T v;
+        if (PRED) {
+            if (blocked) v = ld_pop<HINT>(in + own);
+            else v = ld_pop<HINT>(in + pull);
+        } else {
+            v = ld_pop<HINT>(in + (blocked ? own : pull));
+        }
+        f[d] = S::decode(v, p.shift[d], p.inv_scale);
+    }
+}
+
 // One node of the fused step.  WRAP: coordinates wrap at the lattice faces
 // (periodic lattices, or any out-of-domain link left open); without it the
 // pull offsets are constants and every out-of-domain link must be blocked.
@@ -177,40 +241,8 @@ __device__ __forceinline__ void step_node(const StepParams &p, const G &g, int x
         return;
     }
 
-    // Pull offsets to the six face neighbours.  With WRAP, coordinates wrap
-    // and links that must not wrap are blocked in the flag word, so a wrapped
-    // address is only read where the lattice is periodic.
-    const int plane = g.pitch * g.ny;
-    int oxm = -1, oxp = 1, oym = -g.pitch, oyp = g.pitch, ozm = -plane, ozp = plane;
-    if (WRAP) {
-        oxm = x == 0 ? g.nx - 1 : -1;
-        oxp = x == g.nx - 1 ? 1 - g.nx : 1;
-        oym = y == 0 ? (g.ny - 1) * g.pitch : -g.pitch;
-        oyp = y == g.ny - 1 ? (1 - g.ny) * g.pitch : g.pitch;
-        ozm = z == 0 ? (g.nz - 1) * plane : -plane;
-        ozp = z == g.nz - 1 ? (1 - g.nz) * plane : plane;
-    }
-
-    R f[Q];
-    f[0] = S::decode(ld_pop<HINT>(in), p.shift[0], p.inv_scale);
-#pragma unroll
-    for (int d = 1; d < Q; ++d) {
-        const int pull = d * g.nx + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
-                         (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
-                         (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
-        // across a blocked link: the node's own population, opp(d) for
-        // half-way bounce-back, d itself in the reference's wall model
-        const int own = (PHYS ? L::opp(d) : d) * g.nx;
-        const bool blocked = (w >> d) & 1u;
-        T v;
-        if (PRED) {
-            if (blocked) v = ld_pop<HINT>(in + own);
-            else v = ld_pop<HINT>(in + pull);
-        } else {
-            v = ld_pop<HINT>(in + (blocked ? own : pull));
-        }
-        f[d] = S::decode(v, p.shift[d], p.inv_scale);
-    }
+    typename Store<ST>::R f[Q];
+    gather_node<Q, ST, PHYS, WRAP, G, HINT, PRED>(p, g, x, y, z, w, in, f);
 
     update_node<Q, COLL, ST, PHYS>(f, w, node, p);
 
@@ -229,11 +261,120 @@ __global__ void __launch_bounds__(STEP_BLOCK) step_kernel(const StepParams p) {
 // are immediates of the loads and stores.
 // BLOCK threads along x, HINT and PRED as in step_node: the knobs the
 // autotuner (lbm_autotune) chooses among.
-template <int Q, int COLL, int ST, bool PHYS, bool WRAP, int NX, int NY, int NZ, int BLOCK, int HINT, bool PRED>
-__global__ void __launch_bounds__(BLOCK) step_kernel_fixed(const StepParams p) {
+// MINB: minimum resident blocks per SM asked of the register allocator (1 =
+// no constraint).
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, int NX, int NY, int NZ, int BLOCK, int HINT, bool PRED,
+          int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) step_kernel_fixed(const StepParams p) {
     const FixedGeom<NX, NY, NZ, Q * NX> g;
     step_node<Q, COLL, ST, PHYS, WRAP, FixedGeom<NX, NY, NZ, Q * NX>, HINT, PRED>(
         p, g, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// The reference's L2 residual (computeResidual2D/3D, ComputeResiduals.cu:13-26):
+// sqrt of the sum over all populations of (f - fColl)^2, f the post-stream,
+// post-boundary field and fColl the post-collision field it streams from.
+// The state between steps is fColl, so this recomputes f (the next step's
+// gather and boundary conditions, no collision) and sums per block in FP64;
+// solid nodes contribute 0 as in the reference, which writes neither array
+// there.
+template <int Q, int ST, bool PHYS>
+__global__ void __launch_bounds__(STEP_BLOCK) resid_l2_kernel(const StepParams p, double *partial) {
+    using S = Store<ST>;
+    using T = typename S::T;
+    using R = typename S::R;
+    const DynGeom g{p.nx, p.ny, p.nz, p.pitch};
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    double acc = 0.0;
+    if (x < g.nx) {
+        const int row = y + g.ny * z;
+        const int node = x + g.nx * row;
+        const uint32_t w = __ldg(p.word + node);
+        if (w & W_FLUID) {
+            const T *in = (const T *)p.fin[0] + (x + (long long)g.pitch * row);
+            R f[Q];
+            gather_node<Q, ST, PHYS, true, DynGeom, 0, false>(p, g, x, y, z, w, in, f);
+            bool keep, zv;
+            apply_bc<Q, ST, PHYS>(f, w, node, p, keep, zv);
+#pragma unroll
+            for (int d = 0; d < Q; ++d) {
+                const double df = (double)f[d] - (double)S::decode(in[d * g.nx], p.shift[d], p.inv_scale);
+                acc += df * df;
+            }
+        }
+    }
+    __shared__ double sm[STEP_BLOCK / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < STEP_BLOCK / 32; ++k) t += sm[k];
+        partial[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * (size_t)blockIdx.z)] = t;
+    }
+}
+
+// Force on the solid nodes inside a box by momentum exchange (physics mode,
+// half-way bounce-back): every blocked link of a fluid node x whose solid
+// neighbour x - c_d lies in the box carries 2 c_opp(d) f*_opp(d)(x) to the
+// wall per step, f* the post-collision state.  Per-block FP64 partials of the
+// three components, stored component-major.
+template <int Q, int ST>
+__global__ void __launch_bounds__(STEP_BLOCK) momentum_exchange_kernel(const StepParams p, int4 lo, int4 hi,
+                                                                        double *partial, long long nb) {
+    using S = Store<ST>;
+    using T = typename S::T;
+    using L = Lat<Q>;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    double F[3] = {0, 0, 0};
+    if (x < p.nx) {
+        const int row = y + p.ny * z;
+        const uint32_t w = __ldg(p.word + x + p.nx * row);
+        if ((w & W_FLUID) && (w & 0x7FFFEu)) {
+            const T *in = (const T *)p.fin[0] + (x + (long long)p.pitch * row);
+#pragma unroll
+            for (int d = 1; d < Q; ++d) {
+                if (!((w >> d) & 1u)) continue;
+                const int sx = x - L::cx(d), sy = y - L::cy(d), sz = z - L::cz(d);
+                if (sx < lo.x || sx > hi.x || sy < lo.y || sy > hi.y || sz < lo.z || sz > hi.z) continue;
+                if (sx < 0 || sx >= p.nx || sy < 0 || sy >= p.ny || sz < 0 || sz >= p.nz) continue;
+                const int o = L::opp(d);
+                const double fo = (double)S::decode(in[o * p.nx], p.shift[o], p.inv_scale);
+                F[0] += 2.0 * L::cx(o) * fo;
+                F[1] += 2.0 * L::cy(o) * fo;
+                F[2] += 2.0 * L::cz(o) * fo;
+            }
+        }
+    }
+    __shared__ double sm[3][STEP_BLOCK / 32];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double v = F[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) sm[k][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int k = 0; k < STEP_BLOCK / 32; ++k) t += sm[threadIdx.x][k];
+        partial[threadIdx.x * nb + blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * (size_t)blockIdx.z)] = t;
+    }
+}
+
+// Deterministic sum of n partials (one block of 1024 threads, fixed order).
+static __global__ void __launch_bounds__(1024) sum_partials_kernel(const double *partial, long long n, double *out) {
+    __shared__ double sm[1024];
+    double t = 0.0;
+    for (long long i = threadIdx.x; i < n; i += 1024) t += partial[i];
+    sm[threadIdx.x] = t;
+    __syncthreads();
+    for (int s = 512; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sm[0];
 }
 
 // First post-collision field: f0 = 0 (the reference's start, Iterate.cu:244)

@@ -7,13 +7,15 @@
 // aligned pair load; pulls with cx = +/-1 take the source row's aligned pair
 // and its left or right neighbour pair and pick the shifted elements.
 //
-// Arithmetic runs in storage space: h = (f - sigma w) * S, with sigma = 1 and
-// S = scale for F16S (FP16 deviation from the rest weights) and sigma = 0,
-// S = 1 for F32.  Every collision operator is linear in f except through the
-// equilibria, so it is applied to h directly with equilibria expressed in the
-// same units; a load is one half2->float2 convert and a store one float2->half2
-// convert, with no per-population shift and scale.  Boundary nodes convert to f
-// and reuse the scalar boundary code.
+// Arithmetic runs in storage space: h = (f - sigma w) * S, w the collision
+// model's rest state, with S = scale for F16S and 1 for F32, sigma = 1 when
+// the storage holds deviations (F16S, physics-mode F32) and 0 otherwise.
+// Every collision operator is linear in f except through the equilibria, so
+// it is applied to h directly with equilibria expressed in the same units; a
+// load is one half2->float2 convert and a store one float2->half2 convert,
+// with no per-population shift and scale, and the moments come from the small
+// deviations instead of cancelling sums of O(w) values.  Boundary nodes
+// convert to f and reuse the scalar boundary code.
 #pragma once
 #include "lbm_step.cuh"
 
@@ -33,6 +35,20 @@ __device__ __forceinline__ f2 operator-(f2 a, f2 b) { return f2(__ffma2_rn(b.v, 
 __device__ __forceinline__ f2 operator-(f2 a) { return f2(__fmul2_rn(a.v, make_float2(-1.f, -1.f))); }
 __device__ __forceinline__ f2 &operator+=(f2 &a, f2 b) { return a = a + b; }
 __device__ __forceinline__ f2 &operator-=(f2 &a, f2 b) { return a = a - b; }
+
+// One lane: the same collision code on one node per thread (h_node).
+struct f1 {
+    float v;
+    __device__ __forceinline__ f1() {}
+    __device__ __forceinline__ f1(float s) : v(s) {}
+};
+__device__ __forceinline__ f1 operator+(f1 a, f1 b) { return f1(a.v + b.v); }
+__device__ __forceinline__ f1 operator*(f1 a, f1 b) { return f1(a.v * b.v); }
+__device__ __forceinline__ f1 fma2(f1 a, f1 b, f1 c) { return f1(fmaf(a.v, b.v, c.v)); }
+__device__ __forceinline__ f1 operator-(f1 a, f1 b) { return f1(a.v - b.v); }
+__device__ __forceinline__ f1 operator-(f1 a) { return f1(-a.v); }
+__device__ __forceinline__ f1 &operator+=(f1 &a, f1 b) { return a = a + b; }
+__device__ __forceinline__ f1 &operator-=(f1 &a, f1 b) { return a = a - b; }
 
 // Pair storage: element type of a pair in HBM and its conversion to h.
 template <int ST> struct Pair;
@@ -55,43 +71,43 @@ template <> struct Pair<LBM_STORE_F16S> {
 // vanish by isotropy.
 
 // BGK / TRT in h units: h_eq,d = S w_d [(rho - sigma) + rho (3 cu + 4.5 cu^2 - 1.5 u^2)].
-template <int Q>
-__device__ __forceinline__ f2 heq(int d, f2 rho_m_sigma, f2 rho, f2 ux, f2 uy, f2 uz, f2 usq15, float S) {
+template <int Q, class V>
+__device__ __forceinline__ V heq(int d, V rho_m_sigma, V rho, V ux, V uy, V uz, V usq15, float S) {
     using L = Lat<Q>;
-    f2 cu = 0.f;
+    V cu = 0.f;
     if (L::cx(d)) cu = L::cx(d) > 0 ? ux : -ux;
     if (L::cy(d)) cu = L::cy(d) > 0 ? cu + uy : cu - uy;
     if (L::cz(d)) cu = L::cz(d) > 0 ? cu + uz : cu - uz;
     // rho (3 cu + 4.5 cu^2 - 1.5 u^2) = rho (cu (3 + 4.5 cu) - usq15)
-    const f2 poly = fma2(cu, fma2(cu, f2(4.5f), f2(3.f)), -usq15);
-    return f2((float)(L::w(d)) * S) * fma2(rho, poly, rho_m_sigma);
+    const V poly = fma2(cu, fma2(cu, V(4.5f), V(3.f)), -usq15);
+    return V((float)(L::w(d)) * S) * fma2(rho, poly, rho_m_sigma);
 }
 
-template <int Q>
-__device__ __forceinline__ void collide_bgk_x2(f2 (&h)[Q], f2 rho, f2 ux, f2 uy, f2 uz, float omega, float sigma,
+template <int Q, class V>
+__device__ __forceinline__ void collide_bgk_x2(V (&h)[Q], V rho, V ux, V uy, V uz, float omega, float sigma,
                                                float S) {
-    const f2 usq15 = f2(1.5f) * fma2(ux, ux, fma2(uy, uy, uz * uz));
-    const f2 rms = rho - f2(sigma);
-    const f2 om(omega);
+    const V usq15 = V(1.5f) * fma2(ux, ux, fma2(uy, uy, uz * uz));
+    const V rms = rho - V(sigma);
+    const V om(omega);
 #pragma unroll
     for (int d = 0; d < Q; ++d) h[d] = fma2(-om, h[d] - heq<Q>(d, rms, rho, ux, uy, uz, usq15, S), h[d]);
 }
 
-template <int Q>
-__device__ __forceinline__ void collide_trt_x2(f2 (&h)[Q], f2 rho, f2 ux, f2 uy, f2 uz, float omega,
+template <int Q, class V>
+__device__ __forceinline__ void collide_trt_x2(V (&h)[Q], V rho, V ux, V uy, V uz, float omega,
                                                float omega_m, float sigma, float S) {
     using L = Lat<Q>;
-    const f2 usq15 = f2(1.5f) * fma2(ux, ux, fma2(uy, uy, uz * uz));
-    const f2 rms = rho - f2(sigma);
-    f2 e[Q];
+    const V usq15 = V(1.5f) * fma2(ux, ux, fma2(uy, uy, uz * uz));
+    const V rms = rho - V(sigma);
+    V e[Q];
 #pragma unroll
     for (int d = 0; d < Q; ++d) e[d] = heq<Q>(d, rms, rho, ux, uy, uz, usq15, S);
-    f2 out[Q];
-    const f2 hp(0.5f * omega), hm(0.5f * omega_m);
+    V out[Q];
+    const V hp(0.5f * omega), hm(0.5f * omega_m);
 #pragma unroll
     for (int d = 0; d < Q; ++d) {
         const int o = L::opp(d);
-        const f2 nd = h[d] - e[d], no = h[o] - e[o];
+        const V nd = h[d] - e[d], no = h[o] - e[o];
         out[d] = h[d] - fma2(hp, nd + no, hm * (nd - no));
     }
 #pragma unroll
@@ -101,81 +117,81 @@ __device__ __forceinline__ void collide_trt_x2(f2 (&h)[Q], f2 rho, f2 ux, f2 uy,
 // D3Q19 MRT in h units, in the pair-sum form of collide_mrt19 (lbm_device.cuh):
 // d_k = s_k/|m_k|^2 (m_k(h) - S (m_eq,k - sigma m_k(w~))), with w~ the
 // model's rest state (rest_shift): m(w~) = (1, -11, 0, 0, ...).
-template <bool REF>
-__device__ __forceinline__ void collide_mrt19_x2(f2 (&h)[19], f2 rho, f2 ux, f2 uy, f2 uz, float omega,
+template <bool REF, class V>
+__device__ __forceinline__ void collide_mrt19_x2(V (&h)[19], V rho, V ux, V uy, V uz, float omega,
                                                  float sigma, float S) {
-    const f2 sX = h[1] + h[2], aX = h[1] - h[2];
-    const f2 sY = h[3] + h[4], aY = h[3] - h[4];
-    const f2 sZ = h[5] + h[6], aZ = h[5] - h[6];
-    const f2 sA = h[7] + h[10], aA = h[7] - h[10];
-    const f2 sB = h[8] + h[9], aB = h[8] - h[9];
-    const f2 sC = h[11] + h[14], aC = h[11] - h[14];
-    const f2 sD = h[12] + h[13], aD = h[12] - h[13];
-    const f2 sE = h[15] + h[18], aE = h[15] - h[18];
-    const f2 sF = h[16] + h[17], aF = h[16] - h[17];
-    const f2 sAxis = sX + sY + sZ;
-    const f2 sAB = sA + sB, sCD = sC + sD, sEF = sE + sF;
-    const f2 sABCD = sAB + sCD, sDiag = sABCD + sEF;
-    const f2 h0 = h[0];
-    const f2 tx = (aA - aB) + (aC - aD), ty = (aA + aB) + (aE - aF), tz = (aC + aD) + (aE + aF);
-    const f2 m1 = fma2(f2(-30.f), h0, fma2(f2(-11.f), sAxis, f2(8.f) * sDiag));
-    const f2 m2 = fma2(f2(12.f), h0, fma2(f2(-4.f), sAxis, sDiag));
-    const f2 m4 = fma2(f2(-4.f), aX, tx);
-    const f2 m6 = fma2(f2(-4.f), aY, ty);
-    const f2 m8 = fma2(f2(-4.f), aZ, tz);
-    const f2 sYZ = sY + sZ;
-    const f2 m9 = fma2(f2(2.f), sX - sEF, sABCD - sYZ);
-    const f2 m10 = fma2(f2(2.f), sYZ - sEF, fma2(f2(-4.f), sX, sABCD));
-    const f2 m11 = (sY - sZ) + (sAB - sCD);
-    const f2 m12 = fma2(f2(2.f), sZ - sY, sAB - sCD);
-    const f2 m13 = sA - sB, m14 = sE - sF, m15 = sC - sD;
-    const f2 m16 = (aA - aB) - (aC - aD);
-    const f2 m17 = (aE - aF) - (aA + aB);
-    const f2 m18 = (aC + aD) - (aE + aF);
-    const f2 jx = rho * ux, jy = rho * uy, jz = rho * uz;
-    const f2 jx2 = jx * jx, jy2 = jy * jy, jz2 = jz * jz;
-    const f2 jsq = jx2 + jy2 + jz2;
-    const f2 Sv(S);
+    const V sX = h[1] + h[2], aX = h[1] - h[2];
+    const V sY = h[3] + h[4], aY = h[3] - h[4];
+    const V sZ = h[5] + h[6], aZ = h[5] - h[6];
+    const V sA = h[7] + h[10], aA = h[7] - h[10];
+    const V sB = h[8] + h[9], aB = h[8] - h[9];
+    const V sC = h[11] + h[14], aC = h[11] - h[14];
+    const V sD = h[12] + h[13], aD = h[12] - h[13];
+    const V sE = h[15] + h[18], aE = h[15] - h[18];
+    const V sF = h[16] + h[17], aF = h[16] - h[17];
+    const V sAxis = sX + sY + sZ;
+    const V sAB = sA + sB, sCD = sC + sD, sEF = sE + sF;
+    const V sABCD = sAB + sCD, sDiag = sABCD + sEF;
+    const V h0 = h[0];
+    const V tx = (aA - aB) + (aC - aD), ty = (aA + aB) + (aE - aF), tz = (aC + aD) + (aE + aF);
+    const V m1 = fma2(V(-30.f), h0, fma2(V(-11.f), sAxis, V(8.f) * sDiag));
+    const V m2 = fma2(V(12.f), h0, fma2(V(-4.f), sAxis, sDiag));
+    const V m4 = fma2(V(-4.f), aX, tx);
+    const V m6 = fma2(V(-4.f), aY, ty);
+    const V m8 = fma2(V(-4.f), aZ, tz);
+    const V sYZ = sY + sZ;
+    const V m9 = fma2(V(2.f), sX - sEF, sABCD - sYZ);
+    const V m10 = fma2(V(2.f), sYZ - sEF, fma2(V(-4.f), sX, sABCD));
+    const V m11 = (sY - sZ) + (sAB - sCD);
+    const V m12 = fma2(V(2.f), sZ - sY, sAB - sCD);
+    const V m13 = sA - sB, m14 = sE - sF, m15 = sC - sD;
+    const V m16 = (aA - aB) - (aC - aD);
+    const V m17 = (aE - aF) - (aA + aB);
+    const V m18 = (aC + aD) - (aE + aF);
+    const V jx = rho * ux, jy = rho * uy, jz = rho * uz;
+    const V jx2 = jx * jx, jy2 = jy * jy, jz2 = jz * jz;
+    const V jsq = jx2 + jy2 + jz2;
+    const V Sv(S);
     // S (m_eq,k - sigma m_k(w)) for the non-conserved moments
-    const f2 E1 = Sv * fma2(f2(-11.f), rho - f2(sigma), f2(19.f) * jsq);
+    const V E1 = Sv * fma2(V(-11.f), rho - V(sigma), V(19.f) * jsq);
     // the storage shift is this model's rest state, whose eps moment is 0
-    const f2 E2 = Sv * (f2((float)(-475.0 / 63.0)) * jsq);
-    const f2 c23 = f2((float)(-2.0 / 3.0) * S);
-    const f2 d1 = f2((float)(1.19 / 2394.0)) * (m1 - E1);
-    const f2 d2 = f2((float)(1.4 / 252.0)) * (m2 - E2);
-    const f2 d4 = f2((float)(1.2 / 40.0)) * (m4 - c23 * jx);
-    const f2 d6 = f2((float)(1.2 / 40.0)) * (m6 - c23 * jy);
-    const f2 d8 = f2((float)(1.2 / 40.0)) * (m8 - c23 * jz);
-    const f2 d9 = f2(omega / 36.f) * (m9 - Sv * (fma2(f2(2.f), jx2, -jy2) - jz2));
-    const f2 d10 = f2((float)(1.4 / 72.0)) * m10;
-    const f2 d11 = f2(omega / 12.f) * (m11 - Sv * (jy2 - jz2));
-    const f2 d12 = f2((float)(1.4 / 24.0)) * m12;
-    const f2 w4(0.25f * omega);
-    const f2 d13 = w4 * (m13 - Sv * (jx * jy));
-    const f2 d14 = w4 * (m14 - Sv * (jy * jz));
-    const f2 d15 = w4 * (m15 - Sv * (jx * jz));
-    const f2 g16(1.98f / 8.f);
-    const f2 d16 = g16 * m16, d17 = g16 * m17, d18 = g16 * m18;
-    const f2 P = fma2(f2(-11.f), d1, f2(-4.f) * d2);
-    const f2 EX = fma2(f2(2.f), d9, fma2(f2(-4.f), d10, P));
-    const f2 EYZb = fma2(f2(2.f), d10, P - d9);
-    const f2 K2 = fma2(f2(-2.f), d12, d11);
-    const f2 EY = EYZb + K2, EZ = EYZb - K2;
-    const f2 G = fma2(f2(8.f), d1, d2), H = d9 + d10, K = d11 + d12;
-    const f2 GH = G + H;
-    const f2 GHp = GH + K, GHm = GH - K, G2H = fma2(f2(-2.f), H, G);
-    const f2 OA = (d4 + d6) + (d16 - d17), OB = (d6 - d4) - (d16 + d17);
-    const f2 OC = (d4 + d8) + (d18 - d16), OD = (d8 - d4) + (d16 + d18);
-    const f2 OE = (d6 + d8) + (d17 - d18), OF = (d8 - d6) - (d17 + d18);
-    const f2 m4d4 = f2(-4.f) * d4, m4d6 = f2(-4.f) * d6, m4d8 = f2(-4.f) * d8;
-    h[0] = h0 - fma2(f2(-30.f), d1, f2(12.f) * d2);
+    const V E2 = Sv * (V((float)(-475.0 / 63.0)) * jsq);
+    const V c23 = V((float)(-2.0 / 3.0) * S);
+    const V d1 = V((float)(1.19 / 2394.0)) * (m1 - E1);
+    const V d2 = V((float)(1.4 / 252.0)) * (m2 - E2);
+    const V d4 = V((float)(1.2 / 40.0)) * (m4 - c23 * jx);
+    const V d6 = V((float)(1.2 / 40.0)) * (m6 - c23 * jy);
+    const V d8 = V((float)(1.2 / 40.0)) * (m8 - c23 * jz);
+    const V d9 = V(omega / 36.f) * (m9 - Sv * (fma2(V(2.f), jx2, -jy2) - jz2));
+    const V d10 = V((float)(1.4 / 72.0)) * m10;
+    const V d11 = V(omega / 12.f) * (m11 - Sv * (jy2 - jz2));
+    const V d12 = V((float)(1.4 / 24.0)) * m12;
+    const V w4(0.25f * omega);
+    const V d13 = w4 * (m13 - Sv * (jx * jy));
+    const V d14 = w4 * (m14 - Sv * (jy * jz));
+    const V d15 = w4 * (m15 - Sv * (jx * jz));
+    const V g16(1.98f / 8.f);
+    const V d16 = g16 * m16, d17 = g16 * m17, d18 = g16 * m18;
+    const V P = fma2(V(-11.f), d1, V(-4.f) * d2);
+    const V EX = fma2(V(2.f), d9, fma2(V(-4.f), d10, P));
+    const V EYZb = fma2(V(2.f), d10, P - d9);
+    const V K2 = fma2(V(-2.f), d12, d11);
+    const V EY = EYZb + K2, EZ = EYZb - K2;
+    const V G = fma2(V(8.f), d1, d2), H = d9 + d10, K = d11 + d12;
+    const V GH = G + H;
+    const V GHp = GH + K, GHm = GH - K, G2H = fma2(V(-2.f), H, G);
+    const V OA = (d4 + d6) + (d16 - d17), OB = (d6 - d4) - (d16 + d17);
+    const V OC = (d4 + d8) + (d18 - d16), OD = (d8 - d4) + (d16 + d18);
+    const V OE = (d6 + d8) + (d17 - d18), OF = (d8 - d6) - (d17 + d18);
+    const V m4d4 = V(-4.f) * d4, m4d6 = V(-4.f) * d6, m4d8 = V(-4.f) * d8;
+    h[0] = h0 - fma2(V(-30.f), d1, V(12.f) * d2);
     h[1] -= EX + m4d4;
     h[2] -= EX - m4d4;
     h[3] -= EY + m4d6;
     h[4] -= EY - m4d6;
     h[5] -= EZ + m4d8;
     h[6] -= EZ - m4d8;
-    const f2 eA = GHp + d13, eB = GHp - d13, eC = GHm + d15, eD = GHm - d15, eE = G2H + d14, eF = G2H - d14;
+    const V eA = GHp + d13, eB = GHp - d13, eC = GHm + d15, eD = GHm - d15, eE = G2H + d14, eF = G2H - d14;
     h[7] -= eA + OA;
     h[10] -= eA - OA;
     h[8] -= eB + OB;
@@ -188,22 +204,22 @@ __device__ __forceinline__ void collide_mrt19_x2(f2 (&h)[19], f2 rho, f2 ux, f2 
     h[18] -= eE - OE;
     h[16] -= eF + OF;
     h[17] -= eF - OF;
-    if (REF) h[18] = f2((float)(-sigma * rest_shift(19, LBM_MRT, 18)) * S);  // f18 = 0
+    if (REF) h[18] = V((float)(-sigma * rest_shift(19, LBM_MRT, 18)) * S);  // f18 = 0
 }
 
 // D2Q9 MRT in h units (CellFunctions.cu:7-63 basis and rates); REF keeps the
 // reference's energy equilibria with the extra density factor.
-template <bool REF>
-__device__ __forceinline__ void collide_mrt9_x2(f2 (&h)[9], f2 rho, f2 ux, f2 uy, float omega, float sigma,
+template <bool REF, class V>
+__device__ __forceinline__ void collide_mrt9_x2(V (&h)[9], V rho, V ux, V uy, float omega, float sigma,
                                                 float S) {
-    const f2 usq = fma2(ux, ux, uy * uy);
-    const f2 ef = REF ? rho : f2(1.f);
-    const f2 Sv(S);
-    const f2 rs = rho * usq * ef;
-    f2 E[9];
+    const V usq = fma2(ux, ux, uy * uy);
+    const V ef = REF ? rho : V(1.f);
+    const V Sv(S);
+    const V rs = rho * usq * ef;
+    V E[9];
     E[0] = 0.f;
-    E[1] = Sv * fma2(f2(3.f), rs, f2(-2.f) * (rho - f2(sigma)));
-    E[2] = Sv * fma2(f2(-3.f), rs, rho - f2(sigma));
+    E[1] = Sv * fma2(V(3.f), rs, V(-2.f) * (rho - V(sigma)));
+    E[2] = Sv * fma2(V(-3.f), rs, rho - V(sigma));
     E[3] = Sv * (rho * ux);
     E[4] = -E[3];
     E[5] = Sv * (rho * uy);
@@ -211,40 +227,40 @@ __device__ __forceinline__ void collide_mrt9_x2(f2 (&h)[9], f2 rho, f2 ux, f2 uy
     E[7] = Sv * (rho * (ux * ux - uy * uy));
     E[8] = Sv * (rho * (ux * uy));
     const float s[9] = {0.f, 1.4f, 1.4f, 0.f, 1.2f, 0.f, 1.2f, omega, omega};
-    f2 dm[9];
+    V dm[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
         if (s[k] == 0.f) {
             dm[k] = 0.f;
             continue;
         }
-        f2 m = 0.f;
+        V m = 0.f;
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
             const int c = mrt2(k, i);
             if (c == 1) m += h[i];
             else if (c == -1) m -= h[i];
-            else if (c != 0) m = fma2(f2((float)c), h[i], m);
+            else if (c != 0) m = fma2(V((float)c), h[i], m);
         }
-        dm[k] = f2(s[k] / (float)mrt2_norm(k)) * (m - E[k]);
+        dm[k] = V(s[k] / (float)mrt2_norm(k)) * (m - E[k]);
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
-        f2 c = 0.f;
+        V c = 0.f;
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
             const int mk = mrt2(k, i);
             if (s[k] == 0.f || mk == 0) continue;
             if (mk == 1) c += dm[k];
             else if (mk == -1) c -= dm[k];
-            else c = fma2(f2((float)mk), dm[k], c);
+            else c = fma2(V((float)mk), dm[k], c);
         }
         h[i] -= c;
     }
 }
 
-template <int Q, int COLL, bool PHYS>
-__device__ __forceinline__ void collide_x2(f2 (&h)[Q], f2 rho, f2 ux, f2 uy, f2 uz, const StepParams &p,
+template <int Q, int COLL, bool PHYS, class V>
+__device__ __forceinline__ void collide_x2(V (&h)[Q], V rho, V ux, V uy, V uz, const StepParams &p,
                                            float sigma, float S) {
     if (COLL == LBM_BGKW) {
         collide_bgk_x2<Q>(h, rho, ux, uy, uz, (float)p.omega, sigma, S);
@@ -260,22 +276,23 @@ __device__ __forceinline__ void collide_x2(f2 (&h)[Q], f2 rho, f2 ux, f2 uy, f2 
 
 constexpr int X2_BLOCK = 128;
 
-template <int Q, int COLL, int ST, bool PHYS>
-__global__ void __launch_bounds__(X2_BLOCK) step_kernel_x2(const StepParams p) {
+// One node pair (x0, x0 + 1) of the fused step; G and WRAP as in step_node.
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G>
+__device__ __forceinline__ void pair_node(const StepParams &p, const G &g, int x0, int y, int z) {
     using L = Lat<Q>;
     using T = typename Store<ST>::T;
     using PS = Pair<ST>;
     constexpr bool F16 = ST == LBM_STORE_F16S;
-    const float sigma = F16 ? 1.f : 0.f;
+    const float sigma = p.sigma;
     const float S = F16 ? p.scale : 1.f;
     const float invS = F16 ? p.inv_scale : 1.f;
 
-    const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-    const int y = blockIdx.y, z = blockIdx.z;
-    const bool in_row = x0 < p.nx;
-    const int row = y + p.ny * z;
-    const int node = x0 + p.nx * row;   // flag words and macroscopic fields
-    const long long idx = x0 + (long long)p.pitch * row;  // populations
+    const bool in_row = x0 < g.nx;
+    const int row = y + g.ny * z;
+    const int node = x0 + g.nx * row;   // flag words and macroscopic fields
+    const long long idx = x0 + (long long)g.pitch * row;  // populations
+    const T *in = (const T *)p.fin[0] + idx;
+    T *out = (T *)p.fout[0] + idx;
     uint2 wp = make_uint2(0u, 0u);
     if (in_row) wp = __ldg((const uint2 *)(p.word + node));
     const bool fl0 = (wp.x & W_FLUID) != 0, fl1 = (wp.y & W_FLUID) != 0;
@@ -284,17 +301,23 @@ __global__ void __launch_bounds__(X2_BLOCK) step_kernel_x2(const StepParams p) {
         if (in_row && warp_fluid) {
 #pragma unroll
             for (int d = 0; d < Q; ++d)
-                PS::store((T *)p.fout[d] + idx, f2(-p.shift[d] * S));
+                PS::store(out + d * g.nx, f2(-p.shift[d] * S));
         }
         return;
     }
 
-    const int plane = p.pitch * p.ny;
-    const int oym = y == 0 ? (p.ny - 1) * p.pitch : -p.pitch, oyp = y == p.ny - 1 ? (1 - p.ny) * p.pitch : p.pitch;
-    const int ozm = z == 0 ? (p.nz - 1) * plane : -plane, ozp = z == p.nz - 1 ? (1 - p.nz) * plane : plane;
-    // x offsets of the pair's pulls: from x - 1 and from x + 1 (wrapped)
-    const int oxm0 = x0 == 0 ? p.nx - 1 : -1;              // node x0 pulling from x0 - 1
-    const int oxp1 = x0 + 2 >= p.nx ? 1 - p.nx + 0 : 1;     // node x0 + 1 pulling from x0 + 2
+    const int plane = g.pitch * g.ny;
+    int oym = -g.pitch, oyp = g.pitch, ozm = -plane, ozp = plane;
+    // x offsets of the pair's pulls: node x0 from x0 - 1, node x0 + 1 from x0 + 2
+    int oxm0 = -1, oxp1 = 1;
+    if (WRAP) {
+        oym = y == 0 ? (g.ny - 1) * g.pitch : -g.pitch;
+        oyp = y == g.ny - 1 ? (1 - g.ny) * g.pitch : g.pitch;
+        ozm = z == 0 ? (g.nz - 1) * plane : -plane;
+        ozp = z == g.nz - 1 ? (1 - g.nz) * plane : plane;
+        oxm0 = x0 == 0 ? g.nx - 1 : -1;
+        oxp1 = x0 + 2 >= g.nx ? 1 - g.nx : 1;
+    }
 
     // All loads first, none of their values used before the last is issued:
     // each element's address already selects the pull source or, across a
@@ -306,18 +329,17 @@ __global__ void __launch_bounds__(X2_BLOCK) step_kernel_x2(const StepParams p) {
     for (int d = 0; d < Q; ++d) {
         const int oyz = (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
                         (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
-        const long long s0 = idx + oyz + (L::cx(d) == 1 ? oxm0 : (L::cx(d) == -1 ? 1 : 0));
-        const long long s1 = idx + 1 + oyz + (L::cx(d) == 1 ? -1 : (L::cx(d) == -1 ? oxp1 : 0));
-        const T *pull = (const T *)p.fin[d];
+        const int s0 = d * g.nx + oyz + (L::cx(d) == 1 ? oxm0 : (L::cx(d) == -1 ? 1 : 0));
+        const int s1 = d * g.nx + 1 + oyz + (L::cx(d) == 1 ? -1 : (L::cx(d) == -1 ? oxp1 : 0));
         if (d == 0) {
-            hx[0] = PS::load1(pull + idx);
-            hy[0] = PS::load1(pull + idx + 1);
+            hx[0] = PS::load1(in);
+            hy[0] = PS::load1(in + 1);
             continue;
         }
-        const T *own = (const T *)p.fin[PHYS ? L::opp(d) : d];
+        const int own = (PHYS ? L::opp(d) : d) * g.nx;
         const bool b0 = (wp.x >> d) & 1u, b1 = (wp.y >> d) & 1u;
-        hx[d] = PS::load1(b0 ? own + idx : pull + s0);
-        hy[d] = PS::load1(b1 ? own + idx + 1 : pull + s1);
+        hx[d] = PS::load1(in + (b0 ? own : s0));
+        hy[d] = PS::load1(in + (b1 ? own + 1 : s1));
     }
     const unsigned warp_blocked = __reduce_or_sync(0xffffffffu, (wp.x | wp.y) & 0x7FFFEu);
     f2 h[Q];
@@ -348,7 +370,9 @@ __global__ void __launch_bounds__(X2_BLOCK) step_kernel_x2(const StepParams p) {
                     bc_ref_d3q19<float>(f, mk, u0, v0, w0, p.update_inlet_outlet, keep);
             } else {
                 const int kind = __ldg(p.bc_kind + sl);
-                if (kind & BCK_ACTIVE) {
+                if (kind & BCK_MOVING) {
+                    bc_moving_wall<Q, float>(f, __ldg(p.bc_mask + sl), (float)p.rho0, u0, v0, w0);
+                } else if (kind & BCK_ACTIVE) {
                     const float rset = (kind & BCK_OUTLET) ? (float)p.rho_out : (float)p.rho_in;
                     bc_phys<Q, float>(f, kind & BCK_FACE_MASK, (kind & BCK_PRESSURE) != 0, rset, u0, v0, w0);
                 }
@@ -426,7 +450,129 @@ __global__ void __launch_bounds__(X2_BLOCK) step_kernel_x2(const StepParams p) {
         }
     }
 #pragma unroll
-    for (int d = 0; d < Q; ++d) PS::store((T *)p.fout[d] + idx, h[d]);
+    for (int d = 0; d < Q; ++d) PS::store(out + d * g.nx, h[d]);
+}
+
+// One node per thread with pair_node's arithmetic (storage units h, lanes of
+// type f1): no decode or encode per population and moments from deviations.
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G>
+__device__ __forceinline__ void h_node(const StepParams &p, const G &g, int x, int y, int z) {
+    using L = Lat<Q>;
+    using T = typename Store<ST>::T;
+    constexpr bool F16 = ST == LBM_STORE_F16S;
+    const float sigma = p.sigma;
+    const float S = F16 ? p.scale : 1.f;
+    const float invS = F16 ? p.inv_scale : 1.f;
+    const bool in_row = x < g.nx;
+    const int row = y + g.ny * z;
+    const int node = x + g.nx * row;
+    const long long idx = x + (long long)g.pitch * row;
+    const uint32_t w = in_row ? __ldg(p.word + node) : 0u;
+    const bool fluid = (w & W_FLUID) != 0;
+    const T *in = (const T *)p.fin[0] + idx;
+    T *out = (T *)p.fout[0] + idx;
+    auto raw = [](const T *q) -> float {
+        if constexpr (F16) return __half2float(__ldg(q));
+        else return __ldg(q);
+    };
+    auto put = [](T *q, float v) {
+        if constexpr (F16) *q = __float2half_rn(v);
+        else *q = v;
+    };
+    const unsigned warp_fluid = __ballot_sync(0xffffffffu, fluid);
+    if (!fluid) {
+        // solid nodes keep the zero encoding (sector-complete stores)
+        if (in_row && warp_fluid) {
+#pragma unroll
+            for (int d = 0; d < Q; ++d) put(out + d * g.nx, -sigma * p.shift[d] * S);
+        }
+        return;
+    }
+    const int plane = g.pitch * g.ny;
+    int oxm = -1, oxp = 1, oym = -g.pitch, oyp = g.pitch, ozm = -plane, ozp = plane;
+    if (WRAP) {
+        oxm = x == 0 ? g.nx - 1 : -1;
+        oxp = x == g.nx - 1 ? 1 - g.nx : 1;
+        oym = y == 0 ? (g.ny - 1) * g.pitch : -g.pitch;
+        oyp = y == g.ny - 1 ? (1 - g.ny) * g.pitch : g.pitch;
+        ozm = z == 0 ? (g.nz - 1) * plane : -plane;
+        ozp = z == g.nz - 1 ? (1 - g.nz) * plane : plane;
+    }
+    f1 h[Q];
+    h[0] = raw(in);
+#pragma unroll
+    for (int d = 1; d < Q; ++d) {
+        const int pull = d * g.nx + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
+                         (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
+                         (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
+        const int own = (PHYS ? L::opp(d) : d) * g.nx;
+        h[d] = raw(in + (((w >> d) & 1u) ? own : pull));
+    }
+    bool keep = false, zv = false;
+    if ((w & W_SPECIAL) || !PHYS) {
+        if ((w & W_SPECIAL) || (w & 0x7FFFEu)) {
+            // boundary nodes and reference wall copies: to f, scalar code, back
+            float f[Q];
+#pragma unroll
+            for (int d = 0; d < Q; ++d) f[d] = fmaf(h[d].v, invS, sigma * p.shift[d]);
+            apply_bc<Q, F16 ? LBM_STORE_F16S : LBM_STORE_F32, PHYS>(f, w, node, p, keep, zv);
+#pragma unroll
+            for (int d = 0; d < Q; ++d) h[d] = f1((f[d] - sigma * p.shift[d]) * S);
+        }
+    }
+    f1 sum = h[0], jx = 0.f, jy = 0.f, jz = 0.f;
+#pragma unroll
+    for (int d = 1; d < Q; ++d) {
+        sum += h[d];
+        if (L::cx(d) == 1) jx += h[d]; else if (L::cx(d) == -1) jx -= h[d];
+        if (L::cy(d) == 1) jy += h[d]; else if (L::cy(d) == -1) jy -= h[d];
+        if (L::cz(d) == 1) jz += h[d]; else if (L::cz(d) == -1) jz -= h[d];
+    }
+    f1 rho = fma2(sum, f1(invS), f1(sigma));
+    const f1 sc = f1(invS / rho.v);
+    f1 ux = fma2(jx, sc, f1((float)p.gshift)), uy = jy * sc, uz = jz * sc;
+    if (zv) uy = 0.f;
+    if (keep) {
+        rho = p.rho[node];
+        ux = p.ux[node];
+        uy = p.uy[node];
+        uz = p.uz[node];
+    } else if (p.write_macro) {
+        p.rho[node] = rho.v;
+        p.ux[node] = ux.v;
+        p.uy[node] = uy.v;
+        p.uz[node] = uz.v;
+    }
+    collide_x2<Q, COLL, PHYS>(h, rho, ux, uy, uz, p, sigma, S);
+#pragma unroll
+    for (int d = 0; d < Q; ++d) put(out + d * g.nx, h[d].v);
+}
+
+template <int Q, int COLL, int ST, bool PHYS>
+__global__ void __launch_bounds__(STEP_BLOCK) step_kernel_h(const StepParams p) {
+    const DynGeom g{p.nx, p.ny, p.nz, p.pitch};
+    h_node<Q, COLL, ST, PHYS, true>(p, g, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// h_node with the lattice extents fixed at compile time (built at run time).
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, int NX, int NY, int NZ, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) step_kernel_h_fixed(const StepParams p) {
+    const FixedGeom<NX, NY, NZ, Q * NX> g;
+    h_node<Q, COLL, ST, PHYS, WRAP>(p, g, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <int Q, int COLL, int ST, bool PHYS>
+__global__ void __launch_bounds__(X2_BLOCK) step_kernel_x2(const StepParams p) {
+    const DynGeom g{p.nx, p.ny, p.nz, p.pitch};
+    pair_node<Q, COLL, ST, PHYS, true>(p, g, 2 * (blockIdx.x * blockDim.x + threadIdx.x), blockIdx.y, blockIdx.z);
+}
+
+// The pair step with the lattice extents fixed at compile time (built at run
+// time, lbm_jit.cpp); BLOCK threads (pairs) along x.
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, int NX, int NY, int NZ, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) step_kernel_x2_fixed(const StepParams p) {
+    const FixedGeom<NX, NY, NZ, Q * NX> g;
+    pair_node<Q, COLL, ST, PHYS, WRAP>(p, g, 2 * (blockIdx.x * blockDim.x + threadIdx.x), blockIdx.y, blockIdx.z);
 }
 
 }  // namespace lbm

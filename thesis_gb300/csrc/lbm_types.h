@@ -21,5 +21,9 @@ constexpr int BCK_FACE_MASK = 7;
 constexpr int BCK_PRESSURE = 8;
 constexpr int BCK_OUTLET = 16;
 constexpr int BCK_ACTIVE = 32;
+// A velocity face whose prescribed velocity is tangential to it is a moving
+// wall: half-way bounce-back with the momentum of the wall added on the
+// links listed (bit d: incoming direction d) in the slot's mask.
+constexpr int BCK_MOVING = 64;
 
 }  // namespace lbm

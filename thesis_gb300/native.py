@@ -104,6 +104,8 @@ def lib():
                                       C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
                                       C.POINTER(C.c_int32), C.POINTER(C.c_int)]),
         "lbm_macro_diff": (C.c_int, [vp, dp]),
+        "lbm_residual_l2": (C.c_int, [vp, dp]),
+        "lbm_momentum_exchange": (C.c_int, [vp, _IP, dp]),
         "lbm_read_init_file": (C.c_int, [C.c_char_p, C.POINTER(RunConfig)]),
         "lbm_count_lines": (C.c_longlong, [C.c_char_p]),
         "lbm_node_file_dims": (C.c_int, [C.c_char_p]),
@@ -116,6 +118,10 @@ def lib():
         "lbm_read_initial_conditions": (C.c_int, [C.c_char_p, C.c_longlong, C.c_int, C.c_int, C.c_int, fp, fp, fp,
                                                   fp]),
         "lbm_compare_results": (C.c_int, [C.c_char_p, C.c_char_p, dp, dp]),
+        "lbm_write_midlines": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, fp, fp, fp, fp, fp, fp,
+                                         C.c_double]),
+        "lbm_write_cross_section": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, fp, fp, fp, fp, fp, fp,
+                                              C.c_double]),
         "lbm_io_last_error": (C.c_char_p, []),
         "lbm_cg_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(CgParams), C.POINTER(vp)]),
         "lbm_cg_init": (C.c_int, [vp, fp, fp]),

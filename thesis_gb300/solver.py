@@ -179,6 +179,24 @@ class Solver:
             N.check(rc)
         return out, rc
 
+    def momentum_exchange(self, box):
+        """Force (fx, fy, fz) on the solid nodes inside box = (x0, x1, y0, y1,
+        z0, z1) by momentum exchange."""
+        b = np.ascontiguousarray(box, np.int32)
+        out = np.zeros(3)
+        N.check(self._lib.lbm_momentum_exchange(self._h, b.ctypes.data_as(C.POINTER(C.c_int)),
+                                                out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def residual_l2(self):
+        """The reference's L2 residual sqrt(sum (f - fColl)^2) of the current
+        state, and the status code."""
+        out = C.c_double()
+        rc = self._lib.lbm_residual_l2(self._h, C.byref(out))
+        if rc not in (N.LBM_OK, N.LBM_DIVERGED):
+            N.check(rc)
+        return out.value, rc
+
     def residual(self):
         """Velocity residual sqrt(sum|u - u_prev|^2) / sqrt(sum|u|^2) over
         fluid nodes (FP64), relative to the field at the previous call."""
