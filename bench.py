@@ -166,6 +166,19 @@ def measured_peak():
 KERNEL_NAMES = {1: "step_kernel", 2: "step_kernel_x2", 3: "step_kernel_tma", 4: "step_kernel_fixed"}
 
 
+def kernel_name(variant, knobs):
+    """Name of the step kernel a handle runs: the variant number, refined by
+    the run-time specialised kernel's knobs (storage-unit or two-node form)."""
+    name = KERNEL_NAMES.get(variant, "?")
+    if variant == 4 and knobs:
+        _, hint, pred = knobs
+        if (pred >> 1) & 1:
+            name = "step_kernel_x2_fixed"
+        elif (hint >> 1) & 1:
+            name = "step_kernel_h_fixed"
+    return name
+
+
 def profiled_traffic(kernel, storage, n, m, h):
     """DRAM bytes per launch from the committed ncu summary of this kernel and
     storage, scaled to this lattice by node count (None when no summary
@@ -351,10 +364,22 @@ def run_cg(args):
                 ms = e0.elapsed_time(e1) / args.cg_steps
                 value = n * n / (ms / 1e3) / 1e9
             lap, rc = s.laplace()
+            rr, br, _, _ = s.macro()
+        # the reference's Laplace check: colour densities averaged where
+        # |chi| >= control_param (Multiphase.cu:1054-1080); interface nodes
+        # above the threshold pull the inside average down by O(1/R)
         p_in = 3 / 5 * (1 - a.r_alpha) * lap[0] / max(lap[1], 1)
         p_out = 3 / 5 * (1 - a.b_alpha) * lap[2] / max(lap[3], 1)
-        results.append({"R": float(R), "dp": p_in - p_out, "sigma_measured": float(R * (p_in - p_out)),
-                        "max_u": float(lap[4]), "status": "ok" if rc == 0 else "diverged"})
+        # Laplace's law proper: total pressure c_s^2 (r + b) in the droplet's
+        # core (r < R/2) against the far field (r > R + 16)
+        rho = (rr.astype(np.float64) + br).reshape(n, n)
+        jj, ii = np.mgrid[0:n, 0:n]
+        dist = np.hypot(ii - (n - 1) / 2, jj - (n - 1) / 2)
+        cs2 = 3 / 5 * (1 - a.r_alpha)
+        dp = cs2 * (rho[dist < R / 2].mean() - rho[dist > R + 16].mean())
+        results.append({"R": float(R), "dp": float(dp), "sigma_measured": float(R * dp),
+                        "dp_reference_threshold": p_in - p_out, "max_u": float(lap[4]),
+                        "status": "ok" if rc == 0 else "diverged"})
     sigma_pred = mp.predicted_surface_tension(mp.CgArguments(A=0.005, r_viscosity=1 / 6, b_viscosity=1 / 6))
     inv_r = np.array([1 / r["R"] for r in results])
     dp = np.array([r["dp"] for r in results])
@@ -432,7 +457,7 @@ def main():
     knobs = s.autotune(20) if variant == 4 and args.kernel == "auto" else s.kernel_config()
     s.init(rho0, zero, zero, zero)
     fluid = s.fluid_nodes
-    kernel = KERNEL_NAMES.get(variant, "?")
+    kernel = kernel_name(variant, knobs)
     stream = torch.cuda.Stream(device=dev)
     with torch.cuda.stream(stream):
         s.step(args.warmup, write_macro=False, stream=stream.cuda_stream)

@@ -63,6 +63,29 @@ def test_cg_oracle_conserves_colour_mass():
     assert np.all(r.rr + r.br > 0)
 
 
+def _core_far_jump(rho, n, R, cs2):
+    jj, ii = np.mgrid[0:n, 0:n]
+    dist = np.hypot(ii - (n - 1) / 2, jj - (n - 1) / 2)
+    return cs2 * (rho[dist < R / 2].mean() - rho[dist > R + 16].mean())
+
+
+def test_cg_oracle_laplace_law():
+    """A static droplet's total-pressure jump follows Laplace's law with the
+    predicted surface tension 4A/(9 omega) (within 10 %), and vanishes
+    without the perturbation (A = 0)."""
+    n, R = 96, 20
+    for A in (0.005, 0.0):
+        p = po.cg_params(A=A, beta=0.7)
+        r0, b0 = po.droplet(n, n, R, p)
+        r = po.run_oracle_cg(n, n, p, r0, b0, 3000, fp64=True)
+        dp = _core_far_jump((r.rr + r.br).reshape(n, n), n, R, 3 / 5 * (1 - p.r_alpha))
+        pred = 4 * A / 9 / R
+        if A:
+            assert abs(dp - pred) < 0.1 * pred
+        else:
+            assert abs(dp) < 1e-12
+
+
 def test_create_bubble_and_prediction():
     a = mp.CgArguments(bubble_radius=0.25, r_density=1.0, b_density=0.5, r_alpha=0.6, b_alpha=0.2)
     r, b = mp.create_bubble(17, 17, a)
@@ -169,3 +192,24 @@ def test_cg_gpu_refusals():
         mp.CgSolver(4, 16, mp.CgArguments())
     with pytest.raises(N.LbmError):
         mp.CgSolver(16, 16, mp.CgArguments(r_viscosity=0.0))
+
+
+@pytest.mark.gpu
+def test_cg_gpu_laplace_law():
+    """The GPU droplet obeys Laplace's law as the oracle does: the total
+    pressure jump over two radii scales as 1/R with the predicted tension."""
+    n = 160
+    dps = []
+    for R in (24, 40):
+        a = mp.CgArguments(bubble_radius=R / (n - 1), A=0.005, beta=0.7, r_viscosity=1 / 6, b_viscosity=1 / 6,
+                           control_param=0.9)
+        r0, b0 = mp.create_bubble(n, n, a)
+        with mp.CgSolver(n, n, a) as s:
+            s.init(r0, b0)
+            s.step(6000, write_macro=True)
+            rr, br, _, _ = s.macro()
+        dp = _core_far_jump((rr.astype(np.float64) + br).reshape(n, n), n, R, 3 / 5 * (1 - a.r_alpha))
+        pred = mp.predicted_surface_tension(a) / R
+        assert abs(dp - pred) < 0.15 * pred
+        dps.append(dp)
+    assert dps[0] > dps[1] > 0

@@ -752,8 +752,6 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
     if (!H) return fail(LBM_ERR_INVALID, "null handle");
     if (!H->jit_kernel) return fail(LBM_ERR_UNSUPPORTED, "autotuning needs the run-time specialised kernel");
     if (trial_steps < 2) trial_steps = 2;
-    // one node per thread: block, load form, bounce-back form, and a register
-    // cap that buys occupancy; two nodes per thread: block and register cap
     // one node per thread in f space: block, load form, bounce-back form and a
     // register cap that buys occupancy; in storage units (h): block and
     // register cap; two nodes per thread (storage units): block and cap.
