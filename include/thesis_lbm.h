@@ -106,13 +106,17 @@ typedef struct lbm_params {
     int outlet_profile;       /* LBM_OUTLET_* */
     int collision_model;      /* LBM_BGKW, LBM_TRT, LBM_MRT */
     int boundary_type;        /* LBM_STRAIGHT (LBM_CURVED unsupported) */
-    int bc_wall_model;        /* LBM_WALL_SIMPLE (COMPLEX unsupported) */
+    int bc_wall_model;        /* LBM_WALL_SIMPLE, or LBM_WALL_COMPLEX: the reference's HH wall
+                                 (gpuBcComplexWall3D, GpuBoundaries.cu:492-1560), reference
+                                 mode only; the reference's 2D loop has straight walls only */
     int update_inlet_outlet;  /* UpdateInltOutl */
     int mode;                 /* LBM_MODE_REFERENCE or LBM_MODE_PHYSICS */
     int storage;              /* LBM_STORE_* */
     double rho_in, rho_out;   /* pressure faces */
     double f16_scale;         /* F16S scale; 0 selects 1024 */
-    int periodic[3];          /* physics mode: periodic x, y, z */
+    int periodic[3];          /* physics mode: periodic x, y, z (reference mode follows the BC
+                                 file's periodic links with the reference's copies from the
+                                 opposite face, gpuBcPeriodic3D, GpuBoundaries.cu:2025-2084) */
     int init_equilibrium;     /* 0: f starts at 0 (reference); 1: f_eq(rho, u) */
 } lbm_params;
 

@@ -34,10 +34,11 @@
  *   macroscopic update      GpuUpdateMacro.cu:6-41 (2D), :137-213 (3D)
  *   L2 residual             ComputeResiduals.cu:13-26
  *   loop order              Iterate.cu:385-518, Iterate3D.cu:493-653
+ *   HH ("complex") 3D wall  GpuBoundaries.cu:492-1560
  *
  * Not restated (the entry points return ORC_UNSUPPORTED): curved walls, the
- * HH "complex" 3D wall, the 3D outlet kernel (it addresses directions with the
- * 2D plane size, GpuBoundaries.cu:1662, so it rewrites other nodes) and the
+ * 3D outlet kernel (it addresses directions with the 2D plane size,
+ * GpuBoundaries.cu:1662, so it rewrites other nodes) and the
  * INLET_PROF 3D profile the reference itself refuses (Iterate3D.cu:200-206).
  */
 #include <math.h>
@@ -608,6 +609,7 @@ void bc_node_3d(Lattice<T> &L, int i, uint64_t mk) {
             if (hit) zou_he_3d(f, N, i, face, uu, vv, ww);
         }
     }
+    if (L.p.bc_wall_model == 2) return; /* HH wall: complex_wall_node_3d */
     /* straight simple wall (GpuBoundaries.cu:445-490) */
     for (int dir = 1; dir < 19; ++dir) {
         uint64_t all = mk & bc3_mask(7, dir), wall = mk & bc3_mask(1, dir);
@@ -615,16 +617,144 @@ void bc_node_3d(Lattice<T> &L, int i, uint64_t mk) {
     }
 }
 
-/* 3D periodic copy from the opposite face (GpuBoundaries.cu:2025-2084) and
- * mirror symmetry (:2086-2168), reference mode. */
+/* D3Q19 direction of s1 unit(a1) + s2 unit(a2) in the reference ordering. */
+int dir3_of(int a1, int s1, int a2 = 0, int s2 = 0) {
+    const int v[3] = {(a1 == 0 ? s1 : 0) + (a2 == 0 ? s2 : 0), (a1 == 1 ? s1 : 0) + (a2 == 1 ? s2 : 0),
+                      (a1 == 2 ? s1 : 0) + (a2 == 2 ? s2 : 0)};
+    for (int d = 0; d < 19; ++d)
+        if (cx3[d] == v[0] && cy3[d] == v[1] && cz3[d] == v[2]) return d;
+    return -1;
+}
+int comp3(int a, int d) { return a == 0 ? cx3[d] : (a == 1 ? cy3[d] : cz3[d]); }
+
+/* HH ("complex") wall, gpuBcComplexWall3D (GpuBoundaries.cu:492-1560), wall
+ * at rest.  FP32 evaluation follows the reference's: sums in FLOAT_TYPE,
+ * products with double constants in double and rounded on assignment; the
+ * zero wall-velocity terms of the face formulas add exact zeros and are left
+ * out.  Runs for every node of the boundary list, as the kernel does (its edge
+ * and corner branches do not test the fluid bit). */
 template <class T>
-void periodic_node_3d(Lattice<T> &L, int i, uint64_t mk) {
+void complex_wall_node_3d(Lattice<T> &L, int i, uint64_t mk) {
+    const size_t N = (size_t)L.N;
+    T *f = L.f.data();
+    auto F = [&](int d) -> T & { return f[i + (size_t)d * N]; };
+    int walls = 0;
+    for (int d = 1; d < 19; ++d)
+        if ((mk & bc3_mask(7, d)) == (mk & bc3_mask(1, d)) && (mk & bc3_mask(1, d))) ++walls;
+    /* normal search (:513-556): slot j takes the first direction 1..6 with a
+     * wall bit whose axis is still free; direction c gives normal -c */
+    int slot[3] = {-1, -1, -1}, sgn[3] = {0, 0, 0};
+    for (int j = 0; j < 3; ++j)
+        for (int d = 1; d <= 6; ++d) {
+            const int a = (d - 1) / 2;
+            if ((mk & bc3_mask(1, d)) && slot[a] < 0) {
+                slot[a] = j;
+                sgn[a] = (d % 2) ? -1 : 1;
+                break;
+            }
+        }
+    if (walls == 5 && (mk & BC3_FLUID) && (mk & BC3_WALL_B)) {
+        const int order[6] = {2, 1, 4, 3, 6, 5};
+        for (int k = 0; k < 6; ++k) {
+            const int dw = order[k];
+            const uint64_t wb = mk & bc3_mask(1, dw);
+            if (!(wb && (mk & bc3_mask(7, dw)) == wb)) continue;
+            const int A = (dw - 1) / 2, S = (dw % 2) ? -1 : 1;  /* inward normal */
+            int tang[2], nt = 0;
+            for (int a = 0; a < 3; ++a)
+                if (a != A) tang[nt++] = a;
+            T N2[2];
+            for (int t = 0; t < 2; ++t) {
+                T ps = 0, ms = 0;
+                bool pf = true, mf = true;
+                for (int d = 1; d < 19; ++d) {
+                    if (comp3(A, d) != 0) continue;
+                    if (comp3(tang[t], d) == 1) { ps = pf ? F(d) : (T)(ps + F(d)); pf = false; }
+                    if (comp3(tang[t], d) == -1) { ms = mf ? F(d) : (T)(ms + F(d)); mf = false; }
+                }
+                N2[t] = (T)(0.5 * (double)(T)(ps - ms));
+            }
+            F(dir3_of(A, S)) = F(dir3_of(A, -S));
+            for (int t = 0; t < 2; ++t) {
+                F(dir3_of(A, S, tang[t], 1)) = (T)((double)F(dir3_of(A, -S, tang[t], -1)) - (double)N2[t]);
+                F(dir3_of(A, S, tang[t], -1)) = (T)((double)F(dir3_of(A, -S, tang[t], 1)) + (double)N2[t]);
+            }
+        }
+    }
+    if (walls == 9) {
+        int a1 = -1, a2 = -1;
+        if (slot[0] == 0 && slot[2] == 1) { a1 = 0; a2 = 2; }
+        if (slot[1] == 0 && slot[2] == 1) { a1 = 1; a2 = 2; }
+        if (slot[0] == 0 && slot[1] == 1) { a1 = 0; a2 = 1; }
+        if (a1 >= 0) {
+            const int s1 = sgn[a1], s2 = sgn[a2], t = 3 - a1 - a2;
+            const T ntv = (T)(-0.25 * (double)(T)(F(dir3_of(t, 1)) - F(dir3_of(t, -1))));
+            F(dir3_of(a1, s1)) = F(dir3_of(a1, -s1));
+            F(dir3_of(a2, s2)) = F(dir3_of(a2, -s2));
+            F(dir3_of(a1, s1, a2, s2)) = F(dir3_of(a1, -s1, a2, -s2));
+            F(dir3_of(a1, s1, t, 1)) = (T)(F(dir3_of(a1, -s1, t, -1)) + ntv);
+            F(dir3_of(a1, s1, t, -1)) = (T)(F(dir3_of(a1, -s1, t, 1)) - ntv);
+            F(dir3_of(a2, s2, t, 1)) = (T)(F(dir3_of(a2, -s2, t, -1)) + ntv);
+            F(dir3_of(a2, s2, t, -1)) = (T)(F(dir3_of(a2, -s2, t, 1)) - ntv);
+            const int b1 = dir3_of(a1, s1, a2, -s2), b2 = dir3_of(a1, -s1, a2, s2);
+            T sum = 0;
+            bool first = true;
+            for (int d = 1; d < 19; ++d) {
+                if (d == b1 || d == b2) continue;
+                sum = first ? F(d) : (T)(sum + F(d));
+                first = false;
+            }
+            const int lo = b1 < b2 ? b1 : b2, hi = b1 < b2 ? b2 : b1;
+            F(lo) = (T)((1. / 22.) * (double)sum);
+            F(hi) = (T)((1. / 22.) * (double)sum);
+            F(0) = (T)((12. / 22.) * (double)sum);
+        }
+    }
+    if (walls == 12 && slot[0] == 0 && slot[1] == 1 && slot[2] == 2) {
+        const int sx = sgn[0], sy = sgn[1], sz = sgn[2];
+        F(dir3_of(0, sx)) = F(dir3_of(0, -sx));
+        F(dir3_of(1, sy)) = F(dir3_of(1, -sy));
+        F(dir3_of(2, sz)) = F(dir3_of(2, -sz));
+        F(dir3_of(0, sx, 1, sy)) = F(dir3_of(0, -sx, 1, -sy));
+        F(dir3_of(0, sx, 2, sz)) = F(dir3_of(0, -sx, 2, -sz));
+        F(dir3_of(1, sy, 2, sz)) = F(dir3_of(1, -sy, 2, -sz));
+        const int b[6] = {dir3_of(0, sx, 1, -sy), dir3_of(0, -sx, 1, sy), dir3_of(0, sx, 2, -sz),
+                          dir3_of(0, -sx, 2, sz), dir3_of(1, sy, 2, -sz), dir3_of(1, -sy, 2, sz)};
+        auto buried = [&](int d) {
+            for (int k = 0; k < 6; ++k)
+                if (b[k] == d) return true;
+            return false;
+        };
+        T sum = 0;
+        bool first = true;
+        for (int d = 1; d < 19; ++d) {
+            if (buried(d)) continue;
+            sum = first ? F(d) : (T)(sum + F(d));
+            first = false;
+        }
+        const T c = (T)((1. / 18.) * (double)sum);
+        for (int d = 1; d < 19; ++d)
+            if (buried(d)) F(d) = c;
+        F(0) = (T)(12. * (double)c);
+    }
+}
+
+/* 3D periodic copy from the opposite face (GpuBoundaries.cu:2025-2084) and
+ * mirror symmetry (:2086-2168), reference mode.  The copies read every
+ * partner's populations as they were before any periodic copy (`snap`): the
+ * reference runs them as concurrent GPU threads, which agree with this where
+ * a partner does not copy the same directions itself (one periodic axis) and
+ * race where two periodic faces meet. */
+template <class T>
+void periodic_node_3d(Lattice<T> &L, const std::vector<T> &snap, int i, uint64_t mk) {
     const size_t N = (size_t)L.N;
     T *f = L.f.data();
     if (!(mk & BC3_FLUID) || !(mk & BC3_CYCL_B)) return;
     const int ox = L.n - 1, oy = L.n * (L.m - 1), oz = L.n * L.m * (L.h - 1);
     auto cp = [&](const int *ds, int off) {
-        for (int k = 0; k < 5; ++k) f[i + (size_t)ds[k] * N] = f[i + (size_t)ds[k] * N + off];
+        const long long pn = (long long)i + off;
+        if (pn < 0 || pn >= (long long)N) return;
+        for (int k = 0; k < 5; ++k) f[i + (size_t)ds[k] * N] = snap[(size_t)pn + (size_t)ds[k] * N];
     };
     const int dW[5] = {1, 7, 9, 11, 13}, dE[5] = {2, 8, 10, 12, 14}, dS[5] = {3, 7, 8, 15, 17},
               dN[5] = {4, 9, 10, 16, 18}, dB[5] = {5, 11, 12, 15, 16}, dT[5] = {6, 13, 14, 17, 18};
@@ -824,7 +954,8 @@ int run(int dims, int n, int m, int h, const int *node_type, int nconn, const in
         uint8_t *out_stream, int *out_count, double *out_resid) {
     if (n < 1 || m < 1 || h < 1 || (dims != 2 && dims != 3)) return ORC_BAD_INPUT;
     if (p->collision_model < 1 || p->collision_model > 3) return ORC_BAD_INPUT;
-    if (p->boundary_type == 1 || p->bc_wall_model == 2) return ORC_UNSUPPORTED;
+    if (p->boundary_type == 1) return ORC_UNSUPPORTED;
+    if (p->bc_wall_model == 2 && p->mode == 1) return ORC_UNSUPPORTED;
     if (dims == 3 && p->mode == 0 && p->collision_model == 2) return ORC_UNSUPPORTED;
     if (dims == 3 && p->inlet_profile == 1) return ORC_UNSUPPORTED;
     if (dims == 2 && p->inlet_profile == 1) return ORC_UNSUPPORTED;
@@ -898,8 +1029,11 @@ int run(int dims, int n, int m, int h, const int *node_type, int nconn, const in
             for (int i : L.bcnodes) bc_node_2d(L, i, L.mask[i]);
         } else {
             for (int i : L.bcnodes) bc_node_3d(L, i, L.mask[i]);
+            if (p->bc_wall_model == 2)
+                for (int i : L.bcnodes) complex_wall_node_3d(L, i, L.mask[i]);
             if (p->mode == 0) {
-                for (int i : L.bcnodes) periodic_node_3d(L, i, L.mask[i]);
+                const std::vector<T> snap = L.f;
+                for (int i : L.bcnodes) periodic_node_3d(L, snap, i, L.mask[i]);
                 for (int i : L.bcnodes) symm_node_3d(L, i, L.mask[i]);
             }
         }

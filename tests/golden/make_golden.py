@@ -30,6 +30,14 @@ def cases():
                     dict(u=0.05, viscosity=0.1, collision_model=coll), 12))
     out.append(("cav2d_40x24_bgk_long", ("cavity2d", (40, 24)),
                 dict(u=0.1, viscosity=0.05, collision_model=1, outlet_profile=1), 200))
+    # HH walls (gpuBcComplexWall3D) and periodic copies (gpuBcPeriodic3D)
+    for coll, tag in ((1, "bgk"), (3, "mrt")):
+        out.append(("hh_cav3d_10x9x8_" + tag, ("cavity3d", (10, 9, 8)),
+                    dict(u=0.05, viscosity=0.1, collision_model=coll, bc_wall_model=2), 12))
+    out.append(("per_x_chan3d_10x9x8_bgk", ("periodic_channel3d", (10, 9, 8)),
+                dict(u=0.05, viscosity=0.1, collision_model=1), 12))
+    out.append(("per_x_chan3d_10x9x8_hh_mrt", ("periodic_channel3d", (10, 9, 8)),
+                dict(u=0.05, viscosity=0.1, collision_model=3, bc_wall_model=2), 12))
     return out
 
 

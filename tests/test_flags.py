@@ -77,6 +77,29 @@ def test_unsupported_reference_features_are_refused(native_lib):
     assert e.value.code == N.LBM_ERR_UNSUPPORTED
 
 
+def test_hh_walls_and_periodic_links_reference_mode(native_lib):
+    """Reference mode takes the HH wall model (every boundary node gets a
+    slot, so the wall kernel's face/edge/corner cases can run) and periodic
+    links; physics mode refuses the HH model; 2D ignores it, as the
+    reference's 2D loop does."""
+    lat = lattice.cavity3d(7, 6, 5)
+    mask, word, slot, nbc = build_flags(lat, Arguments(bc_wall_model=N.WALL_COMPLEX))
+    special = ((word >> 19) & 1) == 1
+    assert special.sum() == np.count_nonzero(mask) == nbc
+    _, word_s, _, _ = build_flags(lat, Arguments())
+    assert (((word_s >> 19) & 1) == 1).sum() < special.sum()
+    with pytest.raises(N.LbmError) as e:
+        build_flags(lat, Arguments(bc_wall_model=N.WALL_COMPLEX, mode=N.MODE_PHYSICS))
+    assert e.value.code == N.LBM_ERR_UNSUPPORTED
+    lat2 = lattice.cavity2d(8)
+    w_hh = build_flags(lat2, Arguments(bc_wall_model=N.WALL_COMPLEX))[1]
+    np.testing.assert_array_equal(w_hh, build_flags(lat2, Arguments())[1])
+    per = lattice.periodic_channel3d(8, 7, 6)
+    mask_p, word_p, _, _ = build_flags(per, Arguments())
+    cycl = (mask_p >> np.uint64(54)) & np.uint64(4)
+    assert np.all(((word_p >> 19) & 1)[cycl != 0] == 1)
+
+
 def test_invalid_links_are_rejected(native_lib):
     lat = lattice.cavity2d(6)
     bc = lat.bc.copy()

@@ -40,7 +40,8 @@ def run_pair(oracle, lat, args, steps, init=None):
         f = s.populations()
     okw = dict(u=args.u, v=args.v, w=args.w, rho=args.rho, viscosity=args.viscosity, g=args.g,
                inlet_profile=args.inlet_profile, outlet_profile=args.outlet_profile,
-               collision_model=args.collision_model, update_inlet_outlet=args.update_inlet_outlet)
+               collision_model=args.collision_model, update_inlet_outlet=args.update_inlet_outlet,
+               bc_wall_model=args.bc_wall_model)
     r = oracle.run_oracle(lat, steps, fp64=args.storage == N.STORE_F64, mode=args.mode,
                           init_kind=args.init_equilibrium, rho_in=args.rho_in, rho_out=args.rho_out,
                           extra_collide=True, init=init, periodic=args.periodic, **okw)
@@ -97,6 +98,42 @@ def test_reference_cavity3d(oracle, coll):
     lat = lattice.cavity3d(12, 10, 9)
     args = Arguments(u=0.05, viscosity=0.1, collision_model=coll)
     g, r, fl = run_pair(oracle, lat, args, 25)
+    compare(g, r, fl, N.STORE_F32, 3)
+
+
+REF3_CASES = {
+    "hh_cavity": (lambda: lattice.cavity3d(14, 12, 10), N.WALL_COMPLEX),
+    "periodic_x": (lambda: lattice.periodic_channel3d(14, 12, 10), N.WALL_SIMPLE),
+    "periodic_x_hh": (lambda: lattice.periodic_channel3d(14, 12, 10), N.WALL_COMPLEX),
+    "periodic_xy_hh": (lambda: lattice.periodic_channel3d(14, 12, 10, periodic_axes=(0, 1)), N.WALL_COMPLEX),
+}
+
+
+@pytest.mark.parametrize("case", sorted(REF3_CASES))
+@pytest.mark.parametrize("coll", [N.BGKW, N.MRT])
+@pytest.mark.parametrize("storage", [N.STORE_F32, N.STORE_F64])
+def test_reference_hh_walls_and_periodic_copies(oracle, case, coll, storage):
+    """The reference's HH wall (faces, edges, corners) and its 3D periodic
+    copies from the opposite face, against the oracle (which matches the
+    reference's kernels bit for bit on these lattices, one periodic axis)."""
+    make, wm = REF3_CASES[case]
+    # equilibrium start: from the reference's zero populations the density
+    # passes near 0 at some nodes and u = j / rho magnifies FP32 rounding
+    args = Arguments(u=0.05, viscosity=0.1, collision_model=coll, bc_wall_model=wm, storage=storage,
+                     init_equilibrium=1)
+    g, r, fl = run_pair(oracle, make(), args, 20)
+    compare(g, r, fl, storage, 3)
+
+
+@pytest.mark.parametrize("variant", ["pair", "jith", "scalar", "jit2"])
+def test_reference_periodic_hh_every_kernel_form(oracle, monkeypatch, variant):
+    """Partner pulls and HH walls are shared by the one-node, storage-unit and
+    two-node kernels."""
+    monkeypatch.setenv("THESIS_LBM_KERNEL", variant)
+    args = Arguments(u=0.05, viscosity=0.1, collision_model=N.MRT, bc_wall_model=N.WALL_COMPLEX,
+                     init_equilibrium=1)
+    g, r, fl = run_pair(oracle, lattice.periodic_channel3d(14, 12, 10), args, 20)
+    monkeypatch.delenv("THESIS_LBM_KERNEL", raising=False)
     compare(g, r, fl, N.STORE_F32, 3)
 
 

@@ -21,6 +21,10 @@ from thesis_gb300.solver import Arguments, Solver
     (19, N.MRT, N.STORE_F16S, 1, 0, (256, 256, 512), (128, 2, 0)),
     (9, N.TRT, N.STORE_F32, 0, 1, (160, 48, 1), (256, 2, 5 << 2)),
     (9, N.TRT, N.STORE_F32, 0, 1, (160, 48, 1), (128, 0, 2)),
+    # reference-mode D3Q19 (HH walls, periodic copies) in every kernel form
+    (19, N.MRT, N.STORE_F32, 0, 0, (64, 48, 40), (128, 0, 0)),
+    (19, N.BGKW, N.STORE_F32, 0, 1, (64, 48, 40), (128, 2, 0)),
+    (19, N.MRT, N.STORE_F32, 0, 0, (64, 48, 40), (64, 0, 2)),
 ])
 def test_jit_sources_compile(native_lib, q, coll, storage, phys, wrap, dims, knobs):
     rc = native_lib.lbm_jit_check(q, coll, storage, phys, wrap, *dims, *knobs)

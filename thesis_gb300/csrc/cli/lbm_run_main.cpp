@@ -152,6 +152,11 @@ int main(int argc, char **argv) {
     p.collision_model = cfg.collision_model;
     p.boundary_type = cfg.boundary_type;
     p.bc_wall_model = cfg.bc_wall_model;
+    if (mode == LBM_MODE_PHYSICS && p.bc_wall_model == LBM_WALL_COMPLEX) {
+        // physics-mode walls are half-way bounce-back whatever the init file names
+        fprintf(stderr, "physics mode: walls are half-way bounce-back (BCwallModel HHmodel ignored)\n");
+        p.bc_wall_model = LBM_WALL_SIMPLE;
+    }
     p.update_inlet_outlet = cfg.update_inlet_outlet;
     p.mode = mode;
     p.storage = storage;

@@ -130,6 +130,7 @@ static StepParams make_params(const lbm_handle_s *H, int from, int write_macro) 
     p.rho_in = H->P.rho_in;
     p.rho_out = H->P.rho_out;
     p.rho0 = H->P.rho;
+    p.ref_hh = H->P.mode != LBM_MODE_PHYSICS && H->q == 19 && H->P.bc_wall_model == LBM_WALL_COMPLEX;
     p.scale = H->scale;
     p.inv_scale = 1.0f / H->scale;
     // populations stored as deviations from the rest state: F16S always, F32

@@ -13,8 +13,8 @@ __device__ __forceinline__ uint32_t m2(uint32_t type, int dir) { return type << 
 constexpr uint32_t R2_INLT_B = 0x20000u, R2_CORNER = 0x40000u, R2_FLUID = 0x80000u;
 // Reference 3D BC mask bits (include/BcMacros3D.h:16-170), 64-bit.
 __device__ __forceinline__ uint64_t m3(uint64_t type, int dir) { return type << ((dir - 1) * 3); }
-constexpr uint64_t R3_INLT_B = 2ull << 54, R3_OUTL_B = 3ull << 54, R3_SYMP_B = 5ull << 54,
-                   R3_CORNER = 1ull << 57, R3_FLUID = 1ull << 58;
+constexpr uint64_t R3_WALL_B = 1ull << 54, R3_INLT_B = 2ull << 54, R3_OUTL_B = 3ull << 54,
+                   R3_CYCL_B = 4ull << 54, R3_SYMP_B = 5ull << 54, R3_CORNER = 1ull << 57, R3_FLUID = 1ull << 58;
 
 // ---------------------------------------------------------------------------
 // Reference semantics, D2Q9: gpuBcInlet2D, gpuBcWall2D (straight), and the
@@ -125,9 +125,166 @@ __device__ __forceinline__ void ref_face3(R (&f)[19], int face, R uu, R vv, R ww
     }
 }
 
+// ---------------------------------------------------------------------------
+// The reference's HH ("complex") wall, gpuBcComplexWall3D
+// (GpuBoundaries.cu:492-1560), for walls at rest.  The kernel counts the
+// node's wall-typed links and finds up to three inward wall normals from the
+// wall bits of directions 1-6; then
+//   5 wall links (face, normal e):  f_e = f_-e and, for each tangential axis
+//     t, N_t = (1/2)(sum_{c.e=0, c_t=+1} f_c - sum_{c.e=0, c_t=-1} f_c),
+//     f_(e+t) = f_(-e-t) - N_t, f_(e-t) = f_(-e+t) + N_t            (:558-861)
+//   9 wall links (edge, normals a, b, third axis t):
+//     N_t = -(f_(+t) - f_(-t))/4; f_a = f_-a, f_b = f_-b, f_(a+b) = f_(-a-b),
+//     f_(n+t) = f_(-n-t) + N_t, f_(n-t) = f_(-n+t) - N_t for n = a, b; the
+//     two buried links a-b and b-a get S/22 and the rest population 12 S/22,
+//     S the sum of the other populations                             (:863-1364)
+//   12 wall links (corner, normals a, b, c): f_n = f_-n for the three axes
+//     and the three inward diagonals; the six buried diagonals get S/18 and
+//     the rest population 12 S/18, S the sum over the twelve others  (:1366-1559)
+// The wall velocity terms of the face formulas are zero and left out.
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int dir19(int cx, int cy, int cz) {
+    int r = -1;
+    for (int d = 0; d < 19; ++d)
+        if (Lat<19>::cx(d) == cx && Lat<19>::cy(d) == cy && Lat<19>::cz(d) == cz) r = d;
+    return r;
+}
+// direction of s1 * unit(a1) + s2 * unit(a2) (s2 = 0: the axis direction)
+__host__ __device__ constexpr int dir_of(int a1, int s1, int a2 = 0, int s2 = 0) {
+    return dir19((a1 == 0 ? s1 : 0) + (a2 == 0 ? s2 : 0), (a1 == 1 ? s1 : 0) + (a2 == 1 ? s2 : 0),
+                 (a1 == 2 ? s1 : 0) + (a2 == 2 ? s2 : 0));
+}
+template <int A>
+__host__ __device__ constexpr int comp19(int d) {
+    return A == 0 ? Lat<19>::cx(d) : (A == 1 ? Lat<19>::cy(d) : Lat<19>::cz(d));
+}
+
+template <int A, int S, class R>
+__device__ __forceinline__ void hh_face(R (&f)[19]) {
+    constexpr int T1 = A == 0 ? 1 : 0, T2 = A == 2 ? 1 : 2;
+    R p1 = 0, m1 = 0, p2 = 0, m2 = 0;
+#pragma unroll
+    for (int d = 1; d < 19; ++d) {
+        if (comp19<A>(d) != 0) continue;
+        if (comp19<T1>(d) == 1) p1 += f[d];
+        if (comp19<T1>(d) == -1) m1 += f[d];
+        if (comp19<T2>(d) == 1) p2 += f[d];
+        if (comp19<T2>(d) == -1) m2 += f[d];
+    }
+    const R n1 = (R)0.5 * (p1 - m1), n2 = (R)0.5 * (p2 - m2);
+    f[dir_of(A, S)] = f[dir_of(A, -S)];
+    f[dir_of(A, S, T1, 1)] = f[dir_of(A, -S, T1, -1)] - n1;
+    f[dir_of(A, S, T1, -1)] = f[dir_of(A, -S, T1, 1)] + n1;
+    f[dir_of(A, S, T2, 1)] = f[dir_of(A, -S, T2, -1)] - n2;
+    f[dir_of(A, S, T2, -1)] = f[dir_of(A, -S, T2, 1)] + n2;
+}
+
+template <int A1, int S1, int A2, int S2, class R>
+__device__ __forceinline__ void hh_edge(R (&f)[19]) {
+    constexpr int T = 3 - A1 - A2;
+    constexpr int b1 = dir_of(A1, S1, A2, -S2), b2 = dir_of(A1, -S1, A2, S2);
+    const R nt = (R)-0.25 * (f[dir_of(T, 1)] - f[dir_of(T, -1)]);
+    f[dir_of(A1, S1)] = f[dir_of(A1, -S1)];
+    f[dir_of(A2, S2)] = f[dir_of(A2, -S2)];
+    f[dir_of(A1, S1, A2, S2)] = f[dir_of(A1, -S1, A2, -S2)];
+    f[dir_of(A1, S1, T, 1)] = f[dir_of(A1, -S1, T, -1)] + nt;
+    f[dir_of(A1, S1, T, -1)] = f[dir_of(A1, -S1, T, 1)] - nt;
+    f[dir_of(A2, S2, T, 1)] = f[dir_of(A2, -S2, T, -1)] + nt;
+    f[dir_of(A2, S2, T, -1)] = f[dir_of(A2, -S2, T, 1)] - nt;
+    R s = 0;
+#pragma unroll
+    for (int d = 1; d < 19; ++d)
+        if (d != b1 && d != b2) s += f[d];
+    f[b1] = s * (R)(1.0 / 22.0);
+    f[b2] = s * (R)(1.0 / 22.0);
+    f[0] = s * (R)(12.0 / 22.0);
+}
+
+template <int SX, int SY, int SZ, class R>
+__device__ __forceinline__ void hh_corner(R (&f)[19]) {
+    f[dir_of(0, SX)] = f[dir_of(0, -SX)];
+    f[dir_of(1, SY)] = f[dir_of(1, -SY)];
+    f[dir_of(2, SZ)] = f[dir_of(2, -SZ)];
+    f[dir_of(0, SX, 1, SY)] = f[dir_of(0, -SX, 1, -SY)];
+    f[dir_of(0, SX, 2, SZ)] = f[dir_of(0, -SX, 2, -SZ)];
+    f[dir_of(1, SY, 2, SZ)] = f[dir_of(1, -SY, 2, -SZ)];
+    // buried: diagonals whose two components have the opposite sign pattern
+    // of the normal
+    constexpr int b0 = dir_of(0, SX, 1, -SY), b1 = dir_of(0, -SX, 1, SY), b2 = dir_of(0, SX, 2, -SZ),
+                  b3 = dir_of(0, -SX, 2, SZ), b4 = dir_of(1, SY, 2, -SZ), b5 = dir_of(1, -SY, 2, SZ);
+    R s = 0;
+#pragma unroll
+    for (int d = 1; d < 19; ++d)
+        if (d != b0 && d != b1 && d != b2 && d != b3 && d != b4 && d != b5) s += f[d];
+    const R c = s * (R)(1.0 / 18.0);
+    f[b0] = c; f[b1] = c; f[b2] = c; f[b3] = c; f[b4] = c; f[b5] = c;
+    f[0] = (R)12 * c;
+}
+
+template <int A1, int A2, class R>
+__device__ __forceinline__ void hh_edge_signed(R (&f)[19], int s1, int s2) {
+    if (s1 > 0) {
+        if (s2 > 0) hh_edge<A1, 1, A2, 1>(f); else hh_edge<A1, 1, A2, -1>(f);
+    } else {
+        if (s2 > 0) hh_edge<A1, -1, A2, 1>(f); else hh_edge<A1, -1, A2, -1>(f);
+    }
+}
+
 template <class R>
-__device__ __forceinline__ void bc_ref_d3q19(R (&f)[19], uint64_t mk, R uu, R vv, R ww,
-                                             int update_inlet_outlet, bool &keep_macro) {
+__device__ __forceinline__ void hh_wall3(R (&f)[19], uint64_t mk) {
+    int walls = 0;
+#pragma unroll
+    for (int d = 1; d < 19; ++d) walls += (mk & m3(7, d)) == m3(1, d);
+    // inward normals: slot j = 0, 1, 2 takes the first of directions 1..6
+    // whose wall bit is set and whose axis has no normal yet; a wall bit in
+    // direction c gives the normal -c on its axis
+    int sgn[3] = {0, 0, 0}, slot[3] = {-1, -1, -1};
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        bool done = false;
+#pragma unroll
+        for (int d = 1; d <= 6; ++d) {
+            const int a = (d - 1) >> 1;
+            if (!done && (mk & m3(1, d)) && slot[a] < 0) {
+                slot[a] = j;
+                sgn[a] = (d & 1) ? -1 : 1;
+                done = true;
+            }
+        }
+    }
+    if (walls == 5 && (mk & R3_FLUID) && (mk & R3_WALL_B)) {
+        auto is = [&](int d) { return (mk & m3(1, d)) && (mk & m3(7, d)) == (mk & m3(1, d)); };
+        if (is(2)) hh_face<0, 1>(f);
+        if (is(1)) hh_face<0, -1>(f);
+        if (is(4)) hh_face<1, 1>(f);
+        if (is(3)) hh_face<1, -1>(f);
+        if (is(6)) hh_face<2, 1>(f);
+        if (is(5)) hh_face<2, -1>(f);
+    }
+    if (walls == 9) {
+        if (slot[0] == 0 && slot[2] == 1) hh_edge_signed<0, 2>(f, sgn[0], sgn[2]);
+        if (slot[1] == 0 && slot[2] == 1) hh_edge_signed<1, 2>(f, sgn[1], sgn[2]);
+        if (slot[0] == 0 && slot[1] == 1) hh_edge_signed<0, 1>(f, sgn[0], sgn[1]);
+    }
+    if (walls == 12 && slot[0] == 0 && slot[1] == 1 && slot[2] == 2) {
+        const int k = (sgn[0] > 0) | ((sgn[1] > 0) << 1) | ((sgn[2] > 0) << 2);
+        switch (k) {
+        case 0: hh_corner<-1, -1, -1>(f); break;
+        case 1: hh_corner<1, -1, -1>(f); break;
+        case 2: hh_corner<-1, 1, -1>(f); break;
+        case 3: hh_corner<1, 1, -1>(f); break;
+        case 4: hh_corner<-1, -1, 1>(f); break;
+        case 5: hh_corner<1, -1, 1>(f); break;
+        case 6: hh_corner<-1, 1, 1>(f); break;
+        default: hh_corner<1, 1, 1>(f); break;
+        }
+    }
+}
+
+// gpuBcInlet3D faces W, E, S, N, B, T (GpuBoundaries.cu:92-394) and the
+// straight walls of gpuBcSimpleWall3D (:445-490) or the HH wall.
+template <class R>
+__device__ __forceinline__ void bc_ref3_inlet_wall(R (&f)[19], uint64_t mk, R uu, R vv, R ww, bool hh) {
     if (!(mk & R3_FLUID)) return;
     if (mk & R3_INLT_B) {
         const int faces[6] = {2, 1, 4, 3, 6, 5};
@@ -139,21 +296,32 @@ __device__ __forceinline__ void bc_ref_d3q19(R (&f)[19], uint64_t mk, R uu, R vv
             if (hit) ref_face3(f, face, uu, vv, ww);
         }
     }
+    if (hh) {
+        hh_wall3(f, mk);
+    } else {
 #pragma unroll
-    for (int dir = 1; dir < 19; ++dir)
-        if ((mk & m3(7, dir)) == m3(1, dir)) f[Lat<19>::opp(dir)] = f[dir];
-    if (mk & R3_SYMP_B) {
-        auto is = [&](int dir) { return (mk & m3(7, dir)) == m3(5, dir); };
-        if (is(2)) { f[1] = f[2]; f[7] = f[8]; f[9] = f[10]; f[11] = f[12]; f[13] = f[14]; }
-        if (is(1)) { f[2] = f[1]; f[8] = f[7]; f[10] = f[9]; f[12] = f[11]; f[14] = f[13]; }
-        if (is(4)) { f[3] = f[4]; f[7] = f[9]; f[8] = f[10]; f[15] = f[16]; f[17] = f[18]; }
-        if (is(3)) { f[4] = f[3]; f[9] = f[7]; f[10] = f[8]; f[16] = f[15]; f[18] = f[17]; }
-        if (is(6)) { f[5] = f[6]; f[11] = f[13]; f[12] = f[14]; f[15] = f[17]; f[16] = f[18]; }
-        if (is(5)) { f[6] = f[5]; f[13] = f[11]; f[14] = f[12]; f[17] = f[15]; f[18] = f[16]; }
+        for (int dir = 1; dir < 19; ++dir)
+            if ((mk & m3(7, dir)) == m3(1, dir)) f[Lat<19>::opp(dir)] = f[dir];
     }
-    // gpuUpdateMacro3D leaves inlet nodes untouched unless UpdateInltOutl
-    // (GpuUpdateMacro.cu:150-151).
-    if ((mk & R3_OUTL_B) == R3_INLT_B && !update_inlet_outlet) keep_macro = true;
+}
+
+// gpuBcSymm3D (GpuBoundaries.cu:2086-2168).
+template <class R>
+__device__ __forceinline__ void bc_ref3_symm(R (&f)[19], uint64_t mk) {
+    if (!(mk & R3_FLUID) || !(mk & R3_SYMP_B)) return;
+    auto is = [&](int dir) { return (mk & m3(7, dir)) == m3(5, dir); };
+    if (is(2)) { f[1] = f[2]; f[7] = f[8]; f[9] = f[10]; f[11] = f[12]; f[13] = f[14]; }
+    if (is(1)) { f[2] = f[1]; f[8] = f[7]; f[10] = f[9]; f[12] = f[11]; f[14] = f[13]; }
+    if (is(4)) { f[3] = f[4]; f[7] = f[9]; f[8] = f[10]; f[15] = f[16]; f[17] = f[18]; }
+    if (is(3)) { f[4] = f[3]; f[9] = f[7]; f[10] = f[8]; f[16] = f[15]; f[18] = f[17]; }
+    if (is(6)) { f[5] = f[6]; f[11] = f[13]; f[12] = f[14]; f[15] = f[17]; f[16] = f[18]; }
+    if (is(5)) { f[6] = f[5]; f[13] = f[11]; f[14] = f[12]; f[17] = f[15]; f[18] = f[16]; }
+}
+
+// gpuUpdateMacro3D leaves inlet nodes untouched unless UpdateInltOutl
+// (GpuUpdateMacro.cu:150-151).
+__device__ __forceinline__ bool ref3_keep_macro(uint64_t mk, int update_inlet_outlet) {
+    return (mk & R3_FLUID) && (mk & R3_OUTL_B) == R3_INLT_B && !update_inlet_outlet;
 }
 
 // ---------------------------------------------------------------------------

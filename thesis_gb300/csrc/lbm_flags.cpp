@@ -153,10 +153,16 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
         err = "curved (q-interpolated) walls are not supported";
         return LBM_ERR_UNSUPPORTED;
     }
-    if (P.bc_wall_model == LBM_WALL_COMPLEX) {
-        err = "the HH complex wall model is not supported";
+    if (P.bc_wall_model == LBM_WALL_COMPLEX && phys) {
+        err = "the HH wall model is a reference-mode boundary; physics-mode walls are half-way bounce-back "
+              "(use LBM_WALL_SIMPLE)";
         return LBM_ERR_UNSUPPORTED;
     }
+    // reference 3D HH walls: every boundary node takes the wall kernel's
+    // path (a node whose wall links match none of its face, edge and corner
+    // cases keeps its streamed populations); the reference's 2D loop has
+    // straight walls only (Iterate.cu), so there the model changes nothing
+    const bool hh = !phys && q == 19 && P.bc_wall_model == LBM_WALL_COMPLEX;
 
     // fluid bit and blocked pulls, in parallel over node ranges
     auto word_range = [&](long long lo, long long hi) {
@@ -209,7 +215,7 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
         bool special = false;
         int kind = 0;
         if (!phys) {
-            bool simple = ref_main_type(r, node) == LBM_BC_WALL;
+            bool simple = !hh && ref_main_type(r, node) == LBM_BC_WALL;
             for (int d = 1; d < q && simple; ++d) {
                 const uint64_t t = ref_type(r, node, d);
                 const bool wall = t == LBM_BC_WALL;
@@ -218,13 +224,6 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
             }
             special = !simple;
             if (special) {
-                for (int d = 1; d < q; ++d) {
-                    const uint64_t t = ref_type(r, node, d);
-                    if (t == LBM_BC_PERIODIC && q == 19 && !ref_corner(r, node)) {
-                        err = "reference-mode 3D periodic copies are not supported (use physics mode)";
-                        return LBM_ERR_UNSUPPORTED;
-                    }
-                }
                 const uint64_t mt = ref_main_type(r, node);
                 if (q == 19 && mt == LBM_BC_OUTLET) {
                     err = "the reference's 3D outlet kernel addresses populations with the 2D plane "

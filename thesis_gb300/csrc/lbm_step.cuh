@@ -39,6 +39,7 @@ struct StepParams {
     double omega, omega_m, gshift;
     double rho_in, rho_out;
     double rho0;  // reference density (moving walls)
+    int ref_hh;   // reference mode: the HH wall model instead of straight walls
     float scale, inv_scale;
     // F16S storage holds (f_d - shift_d) * scale and physics-mode F32 storage
     // f_d - shift_d: shift is the collision model's rest-state equilibrium
@@ -72,15 +73,88 @@ __device__ __forceinline__ void collide(typename Store<ST>::R (&f)[Q], typename 
     }
 }
 
-// Everything a fluid node does after its populations are gathered: boundary
-// conditions, macroscopic moments (stored when p.write_macro), collision.
+// Lattice extents seen by the step: read from the parameters (DynGeom) or
+// fixed at compile time (FixedGeom, the build specialised for one lattice,
+// where every population offset becomes an immediate).
+struct DynGeom {
+    int nx, ny, nz, pitch;
+};
+template <int NX, int NY, int NZ, int PITCH>
+struct FixedGeom {
+    static constexpr int nx = NX, ny = NY, nz = NZ, pitch = PITCH;
+};
+
+template <int Q, int ST, bool PHYS, bool WRAP, class G, int HINT, bool PRED>
+__device__ __forceinline__ void gather_node(const StepParams &p, const G &g, int x, int y, int z, uint32_t w,
+                                            const typename Store<ST>::T *in, typename Store<ST>::R (&f)[Q]);
+
+// The reference's 3D periodic copy (gpuBcPeriodic3D, GpuBoundaries.cu:
+// 2025-2084): a node with a periodic link on a face takes the five
+// populations entering through that face from the node one lattice length
+// away (linear offsets n-1, n(m-1), nm(h-1)), as that node holds them after
+// streaming, inlet and wall conditions.  The partner's populations are
+// recomputed here from the read buffer (pull + its own boundary conditions),
+// so every periodic node sees its partners' values from before any periodic
+// copy; the reference runs the copies as concurrent threads, which agree with
+// this wherever a partner does not itself copy the same directions (one
+// periodic axis) and race where two periodic faces meet.
+template <int ST, bool WRAP, class G>
+__device__ __forceinline__ void ref3_periodic(typename Store<ST>::R (&f)[19], uint64_t mk, int node,
+                                              const StepParams &p, const G &g) {
+    using S = Store<ST>;
+    using T = typename S::T;
+    using R = typename S::R;
+    using L = Lat<19>;
+    if (!(mk & R3_FLUID) || !(mk & R3_CYCL_B)) return;
+    const int n = g.nx, nm = g.nx * g.ny;
+    const long long total = (long long)nm * g.nz;
+#pragma unroll 1
+    for (int k = 0; k < 6; ++k) {
+        // faces in the reference's order W, E, S, N, B, T: periodic bit of
+        // direction 2, 1, 4, 3, 6, 5; partner offset +-(n-1), +-n(m-1), +-nm(h-1)
+        const int dir = (k & 1) ? k : k + 2;
+        if (!(mk & m3(4, dir))) continue;
+        const int axis_off = k < 2 ? n - 1 : (k < 4 ? n * (g.ny - 1) : nm * (g.nz - 1));
+        const long long pn = (long long)node + ((k & 1) ? -axis_off : axis_off);
+        if (pn < 0 || pn >= total) continue;
+        const int px = (int)(pn % n), py = (int)((pn / n) % g.ny), pz = (int)(pn / nm);
+        const uint32_t pw = __ldg(p.word + pn);
+        R fb[19];
+        if (pw & W_FLUID) {
+            const T *in = (const T *)p.fin[0] + (px + (long long)g.pitch * (py + g.ny * pz));
+            gather_node<19, ST, false, WRAP, G, 0, false>(p, g, px, py, pz, pw, in, fb);
+            if (pw & W_SPECIAL) {
+                const int sl = __ldg(p.slot + pn);
+                bc_ref3_inlet_wall<R>(fb, __ldg(p.bc_mask + sl), (R)__ldg(p.bc_uvw + 3 * sl),
+                                      (R)__ldg(p.bc_uvw + 3 * sl + 1), (R)__ldg(p.bc_uvw + 3 * sl + 2),
+                                      p.ref_hh != 0);
+            } else {
+#pragma unroll
+                for (int d = 1; d < 19; ++d)
+                    if ((pw >> L::opp(d)) & 1u) fb[L::opp(d)] = fb[d];
+            }
+        } else {
+#pragma unroll
+            for (int d = 0; d < 19; ++d) fb[d] = (R)0;
+        }
+        switch (k) {
+        case 0: f[1] = fb[1]; f[7] = fb[7]; f[9] = fb[9]; f[11] = fb[11]; f[13] = fb[13]; break;
+        case 1: f[2] = fb[2]; f[8] = fb[8]; f[10] = fb[10]; f[12] = fb[12]; f[14] = fb[14]; break;
+        case 2: f[3] = fb[3]; f[7] = fb[7]; f[8] = fb[8]; f[15] = fb[15]; f[17] = fb[17]; break;
+        case 3: f[4] = fb[4]; f[9] = fb[9]; f[10] = fb[10]; f[16] = fb[16]; f[18] = fb[18]; break;
+        case 4: f[5] = fb[5]; f[11] = fb[11]; f[12] = fb[12]; f[15] = fb[15]; f[16] = fb[16]; break;
+        default: f[6] = fb[6]; f[13] = fb[13]; f[14] = fb[14]; f[17] = fb[17]; f[18] = fb[18]; break;
+        }
+    }
+}
+
 // Boundary conditions of a fluid node whose populations are gathered
-// (pulled, bounced back): Zou-He faces, moving walls, the reference's wall
-// copies.  keep_macro / zero_v report the reference's 3D inlet and 2D outlet
-// special cases.
-template <int Q, int ST, bool PHYS>
+// (pulled, bounced back): Zou-He faces, moving walls, the reference's wall,
+// periodic and symmetry copies.  keep_macro / zero_v report the reference's
+// 3D inlet and 2D outlet special cases.
+template <int Q, int ST, bool PHYS, bool WRAP, class G>
 __device__ __forceinline__ void apply_bc(typename Store<ST>::R (&f)[Q], uint32_t w, int node, const StepParams &p,
-                                         bool &keep_macro, bool &zero_v) {
+                                         const G &g, bool &keep_macro, bool &zero_v) {
     using R = typename Store<ST>::R;
     using L = Lat<Q>;
     keep_macro = false;
@@ -91,10 +165,15 @@ __device__ __forceinline__ void apply_bc(typename Store<ST>::R (&f)[Q], uint32_t
                 w0 = (R)__ldg(p.bc_uvw + 3 * sl + 2);
         if constexpr (!PHYS) {
             const unsigned long long mk = __ldg(p.bc_mask + sl);
-            if constexpr (Q == 9)
+            if constexpr (Q == 9) {
                 bc_ref_d2q9<R>(f, (uint32_t)mk, u0, p.outlet_profile, zero_v);
-            else
-                bc_ref_d3q19<R>(f, mk, u0, v0, w0, p.update_inlet_outlet, keep_macro);
+            } else {
+                // the reference's kernel order: inlet, wall, (outlet), periodic, symmetry
+                bc_ref3_inlet_wall<R>(f, mk, u0, v0, w0, p.ref_hh != 0);
+                ref3_periodic<ST, WRAP, G>(f, mk, node, p, g);
+                bc_ref3_symm<R>(f, mk);
+                keep_macro = ref3_keep_macro(mk, p.update_inlet_outlet);
+            }
         } else {
             const int kind = __ldg(p.bc_kind + sl);
             if (kind & BCK_MOVING) {
@@ -115,13 +194,13 @@ __device__ __forceinline__ void apply_bc(typename Store<ST>::R (&f)[Q], uint32_t
     }
 }
 
-template <int Q, int COLL, int ST, bool PHYS>
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G>
 __device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], uint32_t w, int node,
-                                            const StepParams &p) {
+                                            const StepParams &p, const G &g) {
     using R = typename Store<ST>::R;
     using L = Lat<Q>;
     bool keep_macro, zero_v;
-    apply_bc<Q, ST, PHYS>(f, w, node, p, keep_macro, zero_v);
+    apply_bc<Q, ST, PHYS, WRAP, G>(f, w, node, p, g, keep_macro, zero_v);
 
     R rho = 0, jx = 0, jy = 0, jz = 0;
 #pragma unroll
@@ -152,17 +231,6 @@ __device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], uint3
 
     collide<Q, COLL, ST, PHYS>(f, rho, ux, uy, uz, p);
 }
-
-// Lattice extents seen by the step: read from the parameters (DynGeom) or
-// fixed at compile time (FixedGeom, the build specialised for one lattice,
-// where every population offset becomes an immediate).
-struct DynGeom {
-    int nx, ny, nz, pitch;
-};
-template <int NX, int NY, int NZ, int PITCH>
-struct FixedGeom {
-    static constexpr int nx = NX, ny = NY, nz = NZ, pitch = PITCH;
-};
 
 // Populations of a fluid node after streaming: pulled from x - c_d, or
 // across a blocked link the node's own population (opp(d) for half-way
@@ -244,7 +312,7 @@ __device__ __forceinline__ void step_node(const StepParams &p, const G &g, int x
     typename Store<ST>::R f[Q];
     gather_node<Q, ST, PHYS, WRAP, G, HINT, PRED>(p, g, x, y, z, w, in, f);
 
-    update_node<Q, COLL, ST, PHYS>(f, w, node, p);
+    update_node<Q, COLL, ST, PHYS, WRAP, G>(f, w, node, p, g);
 
 #pragma unroll
     for (int d = 0; d < Q; ++d) S::store(out + d * g.nx, f[d], p.shift[d], p.scale);
@@ -295,7 +363,7 @@ __global__ void __launch_bounds__(STEP_BLOCK) resid_l2_kernel(const StepParams p
             R f[Q];
             gather_node<Q, ST, PHYS, true, DynGeom, 0, false>(p, g, x, y, z, w, in, f);
             bool keep, zv;
-            apply_bc<Q, ST, PHYS>(f, w, node, p, keep, zv);
+            apply_bc<Q, ST, PHYS, true, DynGeom>(f, w, node, p, g, keep, zv);
 #pragma unroll
             for (int d = 0; d < Q; ++d) {
                 const double df = (double)f[d] - (double)S::decode(in[d * g.nx], p.shift[d], p.inv_scale);

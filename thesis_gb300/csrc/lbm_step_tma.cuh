@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(TMA_THREADS) step_kernel_tma(const StepParams 
                 if (d != 0 && ((w >> d) & 1u)) v = own[L::opp(d) * nx + x];
                 f[d] = S::decode(v, p.shift[d], p.inv_scale);
             }
-            update_node<Q, COLL, ST, true>(f, w, node, p);
+            update_node<Q, COLL, ST, true, true, DynGeom>(f, w, node, p, DynGeom{p.nx, p.ny, p.nz, p.pitch});
 #pragma unroll
             for (int d = 0; d < Q; ++d) S::store((T *)p.fout[d] + idx, f[d], p.shift[d], p.scale);
         }

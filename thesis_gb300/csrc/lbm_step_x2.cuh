@@ -364,10 +364,14 @@ __device__ __forceinline__ void pair_node(const StepParams &p, const G &g, int x
             bool keep = false, zv = false;
             if constexpr (!PHYS) {
                 const unsigned long long mk = __ldg(p.bc_mask + sl);
-                if constexpr (Q == 9)
+                if constexpr (Q == 9) {
                     bc_ref_d2q9<float>(f, (uint32_t)mk, u0, p.outlet_profile, zv);
-                else
-                    bc_ref_d3q19<float>(f, mk, u0, v0, w0, p.update_inlet_outlet, keep);
+                } else {
+                    bc_ref3_inlet_wall<float>(f, mk, u0, v0, w0, p.ref_hh != 0);
+                    ref3_periodic<ST, WRAP, G>(f, mk, nd, p, g);
+                    bc_ref3_symm<float>(f, mk);
+                    keep = ref3_keep_macro(mk, p.update_inlet_outlet);
+                }
             } else {
                 const int kind = __ldg(p.bc_kind + sl);
                 if (kind & BCK_MOVING) {
@@ -515,7 +519,7 @@ __device__ __forceinline__ void h_node(const StepParams &p, const G &g, int x, i
             float f[Q];
 #pragma unroll
             for (int d = 0; d < Q; ++d) f[d] = fmaf(h[d].v, invS, sigma * p.shift[d]);
-            apply_bc<Q, F16 ? LBM_STORE_F16S : LBM_STORE_F32, PHYS>(f, w, node, p, keep, zv);
+            apply_bc<Q, ST, PHYS, WRAP, G>(f, w, node, p, g, keep, zv);
 #pragma unroll
             for (int d = 0; d < Q; ++d) h[d] = f1((f[d] - sigma * p.shift[d]) * S);
         }

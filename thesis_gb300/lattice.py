@@ -129,6 +129,21 @@ def cavity3d(n, m=None, h=None):
     return Lattice(3, n, m, h, fluid, _boundary_links(3, n, m, h, fluid, ft))
 
 
+def periodic_channel3d(n, m=None, h=None, periodic_axes=(0,)):
+    """Lid-driven channel in the reference's BC types: links leaving through
+    the faces of `periodic_axes` are periodic (type 4), the lid z = h-1 an
+    inlet, every other face a wall."""
+    m = n if m is None else m
+    h = n if h is None else h
+    fluid = np.ones(n * m * h, np.int32)
+
+    def ft(axis, side):
+        if axis in periodic_axes:
+            return 4
+        return 2 if (axis == 2 and side == 1) else 1
+    return Lattice(3, n, m, h, fluid, _boundary_links(3, n, m, h, fluid, ft))
+
+
 def pack_spheres(shape, porosity=0.70, rmin=6.0, rmax=14.0, seed=0, margin_axis=2, margin=2,
                  max_attempts=2_000_000):
     """Random sequential insertion of non-overlapping spheres.
