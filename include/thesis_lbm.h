@@ -283,6 +283,15 @@ int lbm_batch_create(const lbm_lattice_desc *const *lattices, const lbm_params *
                      lbm_batch *out);
 /* Equilibrium start of every domain from its params' rho, u, v, w. */
 int lbm_batch_init(lbm_batch b);
+/* Per-node inlet/outlet velocity of one domain (host arrays of its n*m*h
+ * nodes; a NULL component keeps the params' constant), as
+ * lbm_set_inlet_velocity does for one lattice. */
+int lbm_batch_set_inlet_velocity(lbm_batch b, int domain, const float *u, const float *v, const float *w);
+/* Equilibrium start of one domain from macroscopic fields (host arrays of
+ * n*m*h; NULL = the params' constant), e.g. a predicted steady state.  Call
+ * after lbm_batch_init and before the first step. */
+int lbm_batch_init_fields(lbm_batch b, int domain, const float *rho, const float *u, const float *v,
+                          const float *w);
 /* nsteps steps of every active domain (stream NULL = the batch's own). */
 int lbm_batch_step(lbm_batch b, int nsteps, int write_macro_last, void *stream);
 /* res[d]: sqrt(sum |u - u_prev|^2) / sqrt(sum |u|^2) over fluid nodes of the

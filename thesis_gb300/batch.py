@@ -16,6 +16,8 @@ def _sig(L):
         "lbm_batch_create": (C.c_int, [C.POINTER(C.POINTER(N.LatticeDesc)), C.POINTER(N.Params), C.c_int,
                                        C.POINTER(vp)]),
         "lbm_batch_init": (C.c_int, [vp]),
+        "lbm_batch_set_inlet_velocity": (C.c_int, [vp, C.c_int, fp, fp, fp]),
+        "lbm_batch_init_fields": (C.c_int, [vp, C.c_int, fp, fp, fp, fp]),
         "lbm_batch_step": (C.c_int, [vp, C.c_int, C.c_int, vp]),
         "lbm_batch_residuals": (C.c_int, [vp, dp]),
         "lbm_batch_set_active": (C.c_int, [vp, C.POINTER(C.c_int)]),
@@ -38,6 +40,10 @@ def check(lib, rc):
     if rc != N.LBM_OK:
         raise N.LbmError(rc, lib.lbm_batch_last_error().decode(errors="replace"))
     return rc
+
+
+def _fptr(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
 
 
 class Batch:
@@ -79,6 +85,15 @@ class Batch:
 
     def init(self):
         check(self._lib, self._lib.lbm_batch_init(self._h))
+
+    def set_inlet_velocity(self, d, u=None, v=None, w=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float32).reshape(-1) for a in (u, v, w)]
+        check(self._lib, self._lib.lbm_batch_set_inlet_velocity(self._h, int(d), *[_fptr(a) for a in arrs]))
+
+    def init_fields(self, d, rho=None, u=None, v=None, w=None):
+        """Equilibrium start of domain d from fields (after init, before any step)."""
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float32).reshape(-1) for a in (rho, u, v, w)]
+        check(self._lib, self._lib.lbm_batch_init_fields(self._h, int(d), *[_fptr(a) for a in arrs]))
 
     def step(self, nsteps, write_macro=True, stream=None):
         check(self._lib, self._lib.lbm_batch_step(self._h, int(nsteps), int(bool(write_macro)),

@@ -160,6 +160,7 @@ struct lbm_batch_s {
     long long steps_done = 0;
     std::vector<long long> dom_steps;
     std::vector<int> dom_buf;          // buffer holding each domain's state
+    std::vector<std::vector<long long>> slot_node;  // per domain: node of each boundary slot
     std::vector<double> residual;
     int grid = 0;
     BatchKernel kern = nullptr;
@@ -365,8 +366,10 @@ int lbm_batch_create(const lbm_lattice_desc *const *lattices, const lbm_params *
     std::vector<unsigned long long> mask(nslots);
     std::vector<int32_t> kind(nslots);
     std::vector<double> uvw(3 * nslots);
+    B->slot_node.resize(count);
     for (int d = 0; d < count; ++d) {
         const DeviceFlags &F = flags[d];
+        B->slot_node[d] = F.slot_node;
         std::copy(F.word.begin(), F.word.end(), word.begin() + B->node_off[d]);
         std::copy(F.slot.begin(), F.slot.end(), slot.begin() + B->node_off[d]);  // slots stay domain-local
         for (size_t s = 0; s < F.slot_node.size(); ++s) {
@@ -545,6 +548,51 @@ int lbm_batch_run_to_tolerance(lbm_batch B, double tol, int check_every, long lo
     if (steps) memcpy(steps, B->dom_steps.data(), sizeof(long long) * B->ndom);
     if (res) memcpy(res, B->residual.data(), sizeof(double) * B->ndom);
     return rc;
+}
+
+int lbm_batch_set_inlet_velocity(lbm_batch B, int d, const float *u, const float *v, const float *w) {
+    if (!B || d < 0 || d >= B->ndom) return bfail(LBM_ERR_INVALID, "invalid domain");
+    const std::vector<long long> &sn = B->slot_node[d];
+    if (sn.empty()) return LBM_OK;
+    std::vector<double> uvw(3 * sn.size());
+    const lbm_params &P = B->P[d];
+    for (size_t k = 0; k < sn.size(); ++k) {
+        uvw[3 * k] = u ? u[sn[k]] : P.u;
+        uvw[3 * k + 1] = v ? v[sn[k]] : P.v;
+        uvw[3 * k + 2] = w ? w[sn[k]] : P.w;
+    }
+    cudaError_t e = cudaStreamSynchronize(B->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(B->uvw + 3 * B->slot_off[d], uvw.data(), sizeof(double) * uvw.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return bfail(LBM_ERR_CUDA, std::string("set_inlet_velocity: ") + cudaGetErrorString(e));
+    return LBM_OK;
+}
+
+int lbm_batch_init_fields(lbm_batch B, int d, const float *rho, const float *u, const float *v, const float *w) {
+    if (!B || d < 0 || d >= B->ndom) return bfail(LBM_ERR_INVALID, "invalid domain");
+    if (B->steps_done != 0 || B->cur != 0)
+        return bfail(LBM_ERR_INVALID, "lbm_batch_init_fields must follow lbm_batch_init, before any step");
+    const long long T = B->total_nodes, no = B->node_off[d];
+    const size_t nn = (size_t)B->n[d] * B->m[d] * B->h[d];
+    const float *src[4] = {rho, u, v, w};
+    int mask = 0;
+    cudaError_t e = cudaStreamSynchronize(B->stream);
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k)
+        if (src[k]) {
+            e = cudaMemcpy(B->macro + k * T + no, src[k], sizeof(float) * nn, cudaMemcpyHostToDevice);
+            mask |= 1 << k;
+        }
+    if (e != cudaSuccess) return bfail(LBM_ERR_CUDA, std::string("init_fields: ") + cudaGetErrorString(e));
+    StepParams p = batch_params(B, d, 1, 0);        // writes buffer 0
+    const StepParams o = batch_params(B, d, 0, 0);  // writes buffer 1
+    p.init_from_arrays = mask;
+    const int rc = B->q == 9 ? launch_init_q9(p, o, B->coll, B->storage, 1, 1, B->stream)
+                             : launch_init_q19(p, o, B->coll, B->storage, 1, 1, B->stream);
+    if (rc) return bfail(LBM_ERR_UNSUPPORTED, "no init kernel for this configuration");
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
+    if (e != cudaSuccess) return bfail(LBM_ERR_CUDA, std::string("init_fields: ") + cudaGetErrorString(e));
+    return LBM_OK;
 }
 
 int lbm_batch_get_macro(lbm_batch B, int d, float *rho, float *u, float *v, float *w) {

@@ -1,0 +1,883 @@
+// U-Net warm start: BF16 tensor-core convolution kernels (forward, data
+// gradient, weight gradient), the small kernels around them (pooling,
+// upsampling, ReLU masks, loss, Adam) and the host side of the C ABI in
+// include/thesis_unet.h.
+//
+// Tensors are NHWC BF16 with channel counts that are multiples of 16.  A 3x3
+// convolution is an implicit GEMM: M = pixels, N = output channels, K = 9 taps
+// x input channels, computed with mma.sync.m16n8k16 (BF16 in, FP32
+// accumulate).  One block of 4 warps owns 64 consecutive pixels of one image
+// row; the three input rows it needs (with a one-pixel halo) are staged in
+// shared memory in chunks of 32 channels, the weights come through L1.  The
+// data gradient is the same kernel run on the output gradient with the
+// weights transposed (cin <-> cout) and flipped (tap -> 8 - tap).  The weight
+// gradient is a GEMM over pixels (M = cout, N = cin, K = pixels): each block
+// owns one tap, stages pixel-major tiles of the output gradient and of the
+// shifted input row, and adds its FP32 partial sums atomically.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "thesis_lbm.h"
+#include "thesis_unet.h"
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+thread_local std::string g_unet_error;
+int ufail(int code, const std::string &m) {
+    g_unet_error = m;
+    return code;
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core primitive.  Fragment layout of m16n8k16 (g = lane / 4,
+// t = lane % 4): A (16x16, row-major) registers hold (g, 2t..2t+1),
+// (g+8, 2t..), (g, 2t+8..), (g+8, 2t+8..); B (16x8, K-major) holds
+// (k = 2t..2t+1, n = g), (k = 2t+8.., n = g); C holds (g, 2t..2t+1),
+// (g+8, 2t..2t+1).  The lower 16 bits of a register hold the lower index.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack2(const bf16 *lo, const bf16 *hi) {
+    return (uint32_t)*(const uint16_t *)lo | ((uint32_t)*(const uint16_t *)hi << 16);
+}
+
+constexpr int TILE_X = 64;     // pixels per block (4 warps x 16)
+constexpr int CHUNK = 32;      // input channels staged per pass
+constexpr int SROW = 40;       // staged pixel pitch in bf16 (80 B: conflict-free fragment loads)
+
+// out[n, y, x0+p, co] = act(bias[co] + sum_{tap, ci} w[tap][co][ci] in[n, y+ky-1, x0+p+kx-1, ci])
+template <int COUT>
+__global__ void __launch_bounds__(128) conv3x3_kernel(const bf16 *__restrict__ in, int in_cs, int in_co, int cin,
+                                                      const bf16 *__restrict__ w, const float *__restrict__ bias,
+                                                      bf16 *__restrict__ out, int out_cs, int out_co,
+                                                      float *__restrict__ out32, int H, int W, int relu) {
+    __shared__ __align__(16) bf16 s_in[3][TILE_X + 2][SROW];
+    const int x0 = blockIdx.x * TILE_X, y = blockIdx.y, n = blockIdx.z;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    constexpr int NT = COUT / 8;
+    float acc[NT][4];
+#pragma unroll
+    for (int j = 0; j < NT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    const int p0 = warp * 16 + g;  // this thread's A rows: pixels p0 and p0 + 8
+
+    for (int c0 = 0; c0 < cin; c0 += CHUNK) {
+        const int nvec = (cin - c0 >= CHUNK ? CHUNK : cin - c0) / 8;  // 16-byte vectors per pixel
+        __syncthreads();
+        for (int i = tid; i < 3 * (TILE_X + 2) * 4; i += 128) {
+            const int r = i / ((TILE_X + 2) * 4), rem = i % ((TILE_X + 2) * 4), px = rem >> 2, v = rem & 3;
+            const int gy = y + r - 1, gx = x0 + px - 1;
+            uint4 val = make_uint4(0u, 0u, 0u, 0u);
+            if (v < nvec && gy >= 0 && gy < H && gx >= 0 && gx < W)
+                val = *(const uint4 *)(in + (((size_t)n * H + gy) * W + gx) * in_cs + in_co + c0 + v * 8);
+            *(uint4 *)&s_in[r][px][v * 8] = val;
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int tap = 0; tap < 9; ++tap) {
+            const int ky = tap / 3, kx = tap % 3;
+#pragma unroll
+            for (int kk = 0; kk < 2; ++kk) {
+                if (kk * 2 >= nvec) break;
+                const int kc = kk * 16 + 2 * t;
+                uint32_t a[4];
+                a[0] = *(const uint32_t *)&s_in[ky][p0 + kx][kc];
+                a[1] = *(const uint32_t *)&s_in[ky][p0 + 8 + kx][kc];
+                a[2] = *(const uint32_t *)&s_in[ky][p0 + kx][kc + 8];
+                a[3] = *(const uint32_t *)&s_in[ky][p0 + 8 + kx][kc + 8];
+                const bf16 *wt = w + (size_t)tap * COUT * cin + c0 + kc;
+#pragma unroll
+                for (int j = 0; j < NT; ++j) {
+                    const bf16 *wr = wt + (size_t)(j * 8 + g) * cin;
+                    const uint32_t b0 = __ldg((const unsigned int *)wr);
+                    const uint32_t b1 = __ldg((const unsigned int *)(wr + 8));
+                    mma16816(acc[j], a, b0, b1);
+                }
+            }
+        }
+    }
+    // epilogue: bias, ReLU, BF16 (and optionally FP32) store
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int x = x0 + p0 + 8 * h;
+        if (x >= W) continue;
+        const size_t pix = ((size_t)n * H + y) * W + x;
+#pragma unroll
+        for (int j = 0; j < NT; ++j) {
+            const int co = j * 8 + 2 * t;
+            float v0 = acc[j][2 * h], v1 = acc[j][2 * h + 1];
+            if (bias) {
+                v0 += bias[co];
+                v1 += bias[co + 1];
+            }
+            if (relu) {
+                v0 = fmaxf(v0, 0.f);
+                v1 = fmaxf(v1, 0.f);
+            }
+            if (out) *(__nv_bfloat162 *)(out + pix * out_cs + out_co + co) = __floats2bfloat162_rn(v0, v1);
+            if (out32) {
+                out32[pix * COUT + co] = v0;
+                out32[pix * COUT + co + 1] = v1;
+            }
+        }
+    }
+}
+
+// dw[tap][co][ci] += sum_p dpre[p][co] in[p shifted by tap][ci]  (one tap per blockIdx.y)
+template <int COUT, int CIN>
+__global__ void __launch_bounds__(128) wgrad_kernel(const bf16 *__restrict__ dpre, const bf16 *__restrict__ in,
+                                                    int in_cs, int in_co, float *__restrict__ dw, int B, int H,
+                                                    int W) {
+    constexpr int DP = TILE_X + 8;        // pixel pitch of the staged output gradient
+    constexpr int IP = TILE_X + 2 + 8;    // pixel pitch of the staged input row
+    __shared__ __align__(16) bf16 sD[COUT][DP];
+    __shared__ __align__(16) bf16 sI[CIN][IP];
+    constexpr int MT = COUT / 16, NTL = CIN / 8, TILES = MT * NTL;
+    constexpr int PER = (TILES + 3) / 4;  // tiles per warp
+    const int tap = blockIdx.y, ky = tap / 3, kx = tap % 3;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    float acc[PER][4];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.f;
+    const int xt = (W + TILE_X - 1) / TILE_X;
+    const long long rows = (long long)B * H * xt;
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int xi = (int)(r % xt);
+        const long long ny = r / xt;
+        const int y = (int)(ny % H), n = (int)(ny / H);
+        const int x0 = xi * TILE_X;
+        __syncthreads();
+        // output gradient tile, transposed to [co][pixel]
+        for (int i = tid; i < TILE_X * (COUT / 8); i += 128) {
+            const int px = i / (COUT / 8), cv = i % (COUT / 8);
+            uint4 val = make_uint4(0u, 0u, 0u, 0u);
+            if (x0 + px < W) val = *(const uint4 *)(dpre + (((size_t)n * H + y) * W + x0 + px) * COUT + cv * 8);
+            const bf16 *e = (const bf16 *)&val;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) sD[cv * 8 + k][px] = e[k];
+        }
+        // input row y + ky - 1, pixels x0 - 1 .. x0 + 64, transposed to [ci][pixel]
+        const int gy = y + ky - 1;
+        for (int i = tid; i < (TILE_X + 2) * (CIN / 8); i += 128) {
+            const int px = i / (CIN / 8), cv = i % (CIN / 8);
+            const int gx = x0 + px - 1;
+            uint4 val = make_uint4(0u, 0u, 0u, 0u);
+            if (gy >= 0 && gy < H && gx >= 0 && gx < W)
+                val = *(const uint4 *)(in + (((size_t)n * H + gy) * W + gx) * in_cs + in_co + cv * 8);
+            const bf16 *e = (const bf16 *)&val;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) sI[cv * 8 + k][px] = e[k];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k0 = 0; k0 < TILE_X; k0 += 16) {
+#pragma unroll
+            for (int i = 0; i < PER; ++i) {
+                const int tile = warp + 4 * i;
+                if (tile >= TILES) break;
+                const int co0 = (tile / NTL) * 16, ci0 = (tile % NTL) * 8;
+                uint32_t a[4];
+                const int kc = k0 + 2 * t;
+                a[0] = *(const uint32_t *)&sD[co0 + g][kc];
+                a[1] = *(const uint32_t *)&sD[co0 + g + 8][kc];
+                a[2] = *(const uint32_t *)&sD[co0 + g][kc + 8];
+                a[3] = *(const uint32_t *)&sD[co0 + g + 8][kc + 8];
+                // output pixel p reads staged input pixel p + kx
+                const bf16 *ir = &sI[ci0 + g][kc + kx];
+                const uint32_t b0 = pack2(ir, ir + 1), b1 = pack2(ir + 8, ir + 9);
+                mma16816(acc[i], a, b0, b1);
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int tile = warp + 4 * i;
+        if (tile >= TILES) break;
+        const int co0 = (tile / NTL) * 16, ci0 = (tile % NTL) * 8;
+        float *d = dw + ((size_t)tap * COUT + co0 + g) * CIN + ci0 + 2 * t;
+        atomicAdd(d, acc[i][0]);
+        atomicAdd(d + 1, acc[i][1]);
+        atomicAdd(d + (size_t)8 * CIN, acc[i][2]);
+        atomicAdd(d + (size_t)8 * CIN + 1, acc[i][3]);
+    }
+}
+
+// db[co] += sum_p dpre[p][co]
+__global__ void bias_grad_kernel(const bf16 *__restrict__ dpre, int cout, long long npix, float *__restrict__ db) {
+    const int co = threadIdx.x % cout, lane_set = threadIdx.x / cout, sets = blockDim.x / cout;
+    float s = 0.f;
+    for (long long p = (long long)blockIdx.x * sets + lane_set; p < npix; p += (long long)gridDim.x * sets)
+        s += __bfloat162float(dpre[p * cout + co]);
+    if (lane_set < sets) atomicAdd(db + co, s);
+}
+
+// 2x2 average pooling: out[n, y, x, c] = mean of in[n, 2y+i, 2x+j, c]
+__global__ void pool_kernel(const bf16 *in, int in_cs, int in_co, bf16 *out, int C, int B, int Ho, int Wo) {
+    const long long total = (long long)B * Ho * Wo * C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho), n = (int)(p / ((long long)Wo * Ho));
+        const int Wi = 2 * Wo;
+        const size_t b = (((size_t)n * 2 * Ho + 2 * y) * Wi + 2 * x) * in_cs + in_co + c;
+        const float s = __bfloat162float(in[b]) + __bfloat162float(in[b + in_cs]) +
+                        __bfloat162float(in[b + (size_t)Wi * in_cs]) + __bfloat162float(in[b + (size_t)Wi * in_cs + in_cs]);
+        out[i] = __float2bfloat16(0.25f * s);
+    }
+}
+
+// nearest x2 upsampling into channels [out_co, out_co + C) of out
+__global__ void up_kernel(const bf16 *in, int C, bf16 *out, int out_cs, int out_co, int B, int Ho, int Wo) {
+    const long long total = (long long)B * Ho * Wo * C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho), n = (int)(p / ((long long)Wo * Ho));
+        const int Hi = Ho / 2, Wi = Wo / 2;
+        out[p * out_cs + out_co + c] = in[(((size_t)n * Hi + y / 2) * Wi + x / 2) * C + c];
+    }
+}
+
+// dpre[p][c] = g[p][c] * (act[p][c] > 0)
+__global__ void relu_bwd_kernel(const bf16 *g, int g_cs, int g_co, const bf16 *act, int a_cs, int a_co, bf16 *dpre,
+                                int C, long long npix) {
+    const long long total = npix * C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const float a = __bfloat162float(act[p * a_cs + a_co + c]);
+        dpre[i] = a > 0.f ? g[p * g_cs + g_co + c] : __float2bfloat16(0.f);
+    }
+}
+
+// dpre = (pool gradient + skip gradient) masked by ReLU, at full resolution
+__global__ void pool_skip_bwd_kernel(const bf16 *gpool, const bf16 *gskip, int s_cs, int s_co, const bf16 *act,
+                                     int a_cs, int a_co, bf16 *dpre, int C, int B, int H, int W) {
+    const long long total = (long long)B * H * W * C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const int x = (int)(p % W), y = (int)((p / W) % H), n = (int)(p / ((long long)W * H));
+        const float gp = __bfloat162float(gpool[(((size_t)n * (H / 2) + y / 2) * (W / 2) + x / 2) * C + c]);
+        const float gs = __bfloat162float(gskip[p * s_cs + s_co + c]);
+        const float a = __bfloat162float(act[p * a_cs + a_co + c]);
+        dpre[i] = __float2bfloat16(a > 0.f ? 0.25f * gp + gs : 0.f);
+    }
+}
+
+// dpre at low resolution = sum of the 2x2 upsampled gradient, masked by ReLU
+__global__ void up_bwd_kernel(const bf16 *gup, int g_cs, int g_co, const bf16 *act, bf16 *dpre, int C, int B, int H,
+                              int W) {
+    const long long total = (long long)B * H * W * C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const int x = (int)(p % W), y = (int)((p / W) % H), n = (int)(p / ((long long)W * H));
+        const int W2 = 2 * W;
+        const size_t b = (((size_t)n * 2 * H + 2 * y) * W2 + 2 * x) * g_cs + g_co + c;
+        const float s = __bfloat162float(gup[b]) + __bfloat162float(gup[b + g_cs]) +
+                        __bfloat162float(gup[b + (size_t)W2 * g_cs]) +
+                        __bfloat162float(gup[b + (size_t)W2 * g_cs + g_cs]);
+        dpre[i] = __float2bfloat16(__bfloat162float(act[i]) > 0.f ? s : 0.f);
+    }
+}
+
+// loss sums: sums[0] += sum_p w_p sum_{c<oc} (y - t)^2, sums[1] += sum_p w_p
+__global__ void loss_kernel(const float *pred, int pc, const float *tgt, int oc, const float *wt, long long npix,
+                            double *sums) {
+    double a = 0, b = 0;
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x) {
+        const float wp = wt[p];
+        float e = 0.f;
+        for (int c = 0; c < oc; ++c) {
+            const float d = pred[p * pc + c] - tgt[p * oc + c];
+            e += d * d;
+        }
+        a += (double)wp * e;
+        b += wp;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(sums, a);
+        atomicAdd(sums + 1, b);
+    }
+}
+
+// output gradient of the weighted MSE, BF16, pc channels (the unused ones 0)
+__global__ void loss_grad_kernel(const float *pred, int pc, const float *tgt, int oc, const float *wt,
+                                 long long npix, const double *sums, bf16 *dout) {
+    const double norm = sums[1] > 0 ? 2.0 / (oc * sums[1]) : 0.0;
+    const long long total = npix * pc;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % pc);
+        const long long p = i / pc;
+        float v = 0.f;
+        if (c < oc) v = (float)(norm * wt[p] * (pred[i] - tgt[p * oc + c]));
+        dout[i] = __float2bfloat16(v);
+    }
+}
+
+__global__ void adam_kernel(float *p, const float *g, float *m, float *v, long long n, float lr, float c1, float c2) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = 0.9f * m[i] + 0.1f * gi;
+        const float vi = 0.999f * v[i] + 0.001f * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + 1e-8f);
+    }
+}
+
+// BF16 copies of one layer's FP32 weights [9][cout][cin]: w and the data-
+// gradient form wt[tap'][ci][co] = w[8 - tap'][co][ci]
+__global__ void weights_kernel(const float *p, bf16 *w, bf16 *wt, int cout, int cin) {
+    const int total = 9 * cout * cin;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int ci = i % cin, co = (i / cin) % cout, tap = i / (cin * cout);
+        const bf16 b = __float2bfloat16(p[i]);
+        w[i] = b;
+        wt[((size_t)(8 - tap) * cin + ci) * cout + co] = b;
+    }
+}
+
+// float inputs [n][H][W][ic] -> BF16 [n][H][W][16], zero padded
+__global__ void pack_input_kernel(const float *in, int ic, bf16 *out, long long npix) {
+    const long long total = npix * 16;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % 16);
+        const long long p = i / 16;
+        out[i] = __float2bfloat16(c < ic ? in[p * ic + c] : 0.f);
+    }
+}
+
+__global__ void unpack_output_kernel(const float *in, int pc, float *out, int oc, long long npix) {
+    const long long total = npix * oc;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x)
+        out[i] = in[(i / oc) * pc + i % oc];
+}
+
+int grid_for(long long n, int block = 256) {
+    long long b = (n + block - 1) / block;
+    return (int)(b < 4096 ? (b > 0 ? b : 1) : 4096);
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct Act {  // a tensor of the network: NHWC, channel stride cs, first channel co
+    bf16 *p = nullptr;
+    int cs = 0, co = 0, C = 0, level = 0;
+};
+
+struct Layer {
+    int cin, cout, relu;
+    size_t w_off, b_off;  // into the FP32 parameter vector
+    bf16 *w = nullptr, *wt = nullptr;
+};
+
+}  // namespace
+
+struct lbm_unet_s {
+    lbm_unet_config cfg;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    double last_ms = 0;
+    std::vector<Layer> L;
+    long long nparams = 0;
+    float *params = nullptr, *grad = nullptr, *adam_m = nullptr, *adam_v = nullptr;
+    long long adam_t = 0;
+    std::vector<void *> allocs;
+    // activations and their gradients
+    Act x0, e0a, cat0, p0, e1a, cat1, p1, e2a, cat2, p2, ba, bb, d2a, d2b, d1a, d1b, d0a, d0b;
+    Act g_e0a, g_cat0, g_p0, g_e1a, g_cat1, g_p1, g_e2a, g_cat2, g_p2, g_ba, g_bb, g_d2a, g_d2b, g_d1a, g_d1b,
+        g_d0a, g_d0b;
+    float *out32 = nullptr;     // [B][H][W][16] FP32 output
+    bf16 *dout = nullptr;       // its gradient
+    bf16 *dpre = nullptr;       // scratch: a layer's pre-activation gradient
+    float *fin = nullptr, *fout = nullptr;  // host-format staging
+    float *tgt = nullptr, *wt = nullptr;    // batch targets and weights
+    double *sums = nullptr;
+    // dataset
+    int ds_count = 0;
+    bf16 *ds_in = nullptr;
+    float *ds_tgt = nullptr, *ds_wt = nullptr;
+};
+
+namespace {
+
+int H_of(const lbm_unet_s *u, int level) { return u->cfg.height >> level; }
+int W_of(const lbm_unet_s *u, int level) { return u->cfg.width >> level; }
+
+int alloc(lbm_unet_s *u, void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes > 0 ? bytes : 16);
+    if (e != cudaSuccess) return ufail(LBM_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    u->allocs.push_back(*p);
+    cudaMemsetAsync(*p, 0, bytes > 0 ? bytes : 16, u->stream);
+    return LBM_OK;
+}
+
+int make_act(lbm_unet_s *u, Act &a, int C, int level) {
+    a.C = C;
+    a.cs = C;
+    a.co = 0;
+    a.level = level;
+    const size_t n = (size_t)u->cfg.max_batch * H_of(u, level) * W_of(u, level) * C;
+    return alloc(u, (void **)&a.p, n * sizeof(bf16));
+}
+
+Act view(const Act &a, int co, int C) {
+    Act v = a;
+    v.co = co;
+    v.C = C;
+    return v;
+}
+
+void conv(lbm_unet_s *u, const Layer &l, const Act &in, const Act &out, const float *bias, float *out32, int B,
+          int level, bool transposed) {
+    const int H = H_of(u, level), W = W_of(u, level);
+    dim3 grid((W + TILE_X - 1) / TILE_X, H, B);
+    const bf16 *w = transposed ? l.wt : l.w;
+    const int cin = transposed ? l.cout : l.cin, cout = transposed ? l.cin : l.cout;
+    const int relu = transposed ? 0 : l.relu;
+    bf16 *op = out.p;
+    switch (cout) {
+    case 16: conv3x3_kernel<16><<<grid, 128, 0, u->stream>>>(in.p, in.cs, in.co, cin, w, bias, op, out.cs, out.co, out32, H, W, relu); break;
+    case 32: conv3x3_kernel<32><<<grid, 128, 0, u->stream>>>(in.p, in.cs, in.co, cin, w, bias, op, out.cs, out.co, out32, H, W, relu); break;
+    case 64: conv3x3_kernel<64><<<grid, 128, 0, u->stream>>>(in.p, in.cs, in.co, cin, w, bias, op, out.cs, out.co, out32, H, W, relu); break;
+    default: conv3x3_kernel<128><<<grid, 128, 0, u->stream>>>(in.p, in.cs, in.co, cin, w, bias, op, out.cs, out.co, out32, H, W, relu); break;
+    }
+}
+
+void wgrad(lbm_unet_s *u, const Layer &l, const Act &in, int B, int level) {
+    const int H = H_of(u, level), W = W_of(u, level);
+    const long long rows = (long long)B * H * ((W + TILE_X - 1) / TILE_X);
+    dim3 grid((unsigned)(rows < 64 ? rows : 64), 9);
+    float *dw = u->grad + l.w_off;
+#define WG(CO, CI)                                                                                            \
+    if (l.cout == CO && l.cin == CI) {                                                                        \
+        wgrad_kernel<CO, CI><<<grid, 128, 0, u->stream>>>(u->dpre, in.p, in.cs, in.co, dw, B, H, W);         \
+    } else
+    WG(16, 16) WG(32, 16) WG(32, 32) WG(64, 32) WG(64, 64) WG(64, 128) WG(32, 64) WG(16, 32) {}
+#undef WG
+    const long long npix = (long long)B * H * W;
+    bias_grad_kernel<<<grid_for(npix, 256), 256, 0, u->stream>>>(u->dpre, l.cout, npix, u->grad + l.b_off);
+}
+
+void refresh_weights(lbm_unet_s *u) {
+    for (const Layer &l : u->L)
+        weights_kernel<<<grid_for(9LL * l.cout * l.cin), 256, 0, u->stream>>>(u->params + l.w_off, l.w, l.wt, l.cout,
+                                                                               l.cin);
+}
+
+// forward pass on the batch in x0; FP32 output in out32
+void forward(lbm_unet_s *u, int B) {
+    auto &L = u->L;
+    const float *P = u->params;
+    auto cv = [&](int k, const Act &in, const Act &out, int lev, float *o32 = nullptr) {
+        conv(u, L[k], in, out, P + L[k].b_off, o32, B, lev, false);
+    };
+    auto pool = [&](const Act &in, const Act &out, int lev_out) {
+        const long long n = (long long)B * H_of(u, lev_out) * W_of(u, lev_out) * out.C;
+        pool_kernel<<<grid_for(n), 256, 0, u->stream>>>(in.p, in.cs, in.co, out.p, out.C, B, H_of(u, lev_out),
+                                                          W_of(u, lev_out));
+    };
+    auto up = [&](const Act &in, const Act &out, int lev_out) {
+        const long long n = (long long)B * H_of(u, lev_out) * W_of(u, lev_out) * in.C;
+        up_kernel<<<grid_for(n), 256, 0, u->stream>>>(in.p, in.C, out.p, out.cs, out.co, B, H_of(u, lev_out),
+                                                        W_of(u, lev_out));
+    };
+    cv(0, u->x0, u->e0a, 0);
+    cv(1, u->e0a, view(u->cat0, 16, 16), 0);
+    pool(view(u->cat0, 16, 16), u->p0, 1);
+    cv(2, u->p0, u->e1a, 1);
+    cv(3, u->e1a, view(u->cat1, 32, 32), 1);
+    pool(view(u->cat1, 32, 32), u->p1, 2);
+    cv(4, u->p1, u->e2a, 2);
+    cv(5, u->e2a, view(u->cat2, 64, 64), 2);
+    pool(view(u->cat2, 64, 64), u->p2, 3);
+    cv(6, u->p2, u->ba, 3);
+    cv(7, u->ba, u->bb, 3);
+    up(u->bb, view(u->cat2, 0, 64), 2);
+    cv(8, u->cat2, u->d2a, 2);
+    cv(9, u->d2a, u->d2b, 2);
+    up(u->d2b, view(u->cat1, 0, 32), 1);
+    cv(10, u->cat1, u->d1a, 1);
+    cv(11, u->d1a, u->d1b, 1);
+    up(u->d1b, view(u->cat0, 0, 16), 0);
+    cv(12, u->cat0, u->d0a, 0);
+    cv(13, u->d0a, u->d0b, 0);
+    Act none;
+    cv(14, u->d0b, none, 0, u->out32);
+}
+
+// backward pass from dout; parameter gradients accumulate into grad
+void backward(lbm_unet_s *u, int B) {
+    auto &L = u->L;
+    auto npix = [&](int lev) { return (long long)B * H_of(u, lev) * W_of(u, lev); };
+    auto dgrad = [&](int k, const Act &gin, int lev) {
+        Act d;
+        d.p = u->dpre;
+        d.cs = L[k].cout;
+        d.co = 0;
+        d.C = L[k].cout;
+        conv(u, L[k], d, gin, nullptr, nullptr, B, lev, true);
+    };
+    auto relu_bwd = [&](const Act &g, const Act &act, int C, int lev) {
+        const long long n = npix(lev) * C;
+        relu_bwd_kernel<<<grid_for(n), 256, 0, u->stream>>>(g.p, g.cs, g.co, act.p, act.cs, act.co, u->dpre, C,
+                                                              npix(lev));
+    };
+    auto pool_skip = [&](const Act &gpool, const Act &gskip, const Act &act, int C, int lev) {
+        const long long n = npix(lev) * C;
+        pool_skip_bwd_kernel<<<grid_for(n), 256, 0, u->stream>>>(gpool.p, gskip.p, gskip.cs, gskip.co, act.p,
+                                                                   act.cs, act.co, u->dpre, C, B, H_of(u, lev),
+                                                                   W_of(u, lev));
+    };
+    auto up_bwd = [&](const Act &gup, const Act &act, int C, int lev) {
+        const long long n = npix(lev) * C;
+        up_bwd_kernel<<<grid_for(n), 256, 0, u->stream>>>(gup.p, gup.cs, gup.co, act.p, u->dpre, C, B, H_of(u, lev),
+                                                            W_of(u, lev));
+    };
+    // output layer: dpre = dout
+    cudaMemcpyAsync(u->dpre, u->dout, sizeof(bf16) * npix(0) * 16, cudaMemcpyDeviceToDevice, u->stream);
+    wgrad(u, L[14], u->d0b, B, 0);
+    dgrad(14, u->g_d0b, 0);
+    relu_bwd(u->g_d0b, u->d0b, 16, 0);
+    wgrad(u, L[13], u->d0a, B, 0);
+    dgrad(13, u->g_d0a, 0);
+    relu_bwd(u->g_d0a, u->d0a, 16, 0);
+    wgrad(u, L[12], u->cat0, B, 0);
+    dgrad(12, u->g_cat0, 0);
+    up_bwd(view(u->g_cat0, 0, 16), u->d1b, 16, 1);
+    wgrad(u, L[11], u->d1a, B, 1);
+    dgrad(11, u->g_d1a, 1);
+    relu_bwd(u->g_d1a, u->d1a, 32, 1);
+    wgrad(u, L[10], u->cat1, B, 1);
+    dgrad(10, u->g_cat1, 1);
+    up_bwd(view(u->g_cat1, 0, 32), u->d2b, 32, 2);
+    wgrad(u, L[9], u->d2a, B, 2);
+    dgrad(9, u->g_d2a, 2);
+    relu_bwd(u->g_d2a, u->d2a, 64, 2);
+    wgrad(u, L[8], u->cat2, B, 2);
+    dgrad(8, u->g_cat2, 2);
+    up_bwd(view(u->g_cat2, 0, 64), u->bb, 64, 3);
+    wgrad(u, L[7], u->ba, B, 3);
+    dgrad(7, u->g_ba, 3);
+    relu_bwd(u->g_ba, u->ba, 64, 3);
+    wgrad(u, L[6], u->p2, B, 3);
+    dgrad(6, u->g_p2, 3);
+    pool_skip(u->g_p2, view(u->g_cat2, 64, 64), view(u->cat2, 64, 64), 64, 2);
+    wgrad(u, L[5], u->e2a, B, 2);
+    dgrad(5, u->g_e2a, 2);
+    relu_bwd(u->g_e2a, u->e2a, 64, 2);
+    wgrad(u, L[4], u->p1, B, 2);
+    dgrad(4, u->g_p1, 2);
+    pool_skip(u->g_p1, view(u->g_cat1, 32, 32), view(u->cat1, 32, 32), 32, 1);
+    wgrad(u, L[3], u->e1a, B, 1);
+    dgrad(3, u->g_e1a, 1);
+    relu_bwd(u->g_e1a, u->e1a, 32, 1);
+    wgrad(u, L[2], u->p0, B, 1);
+    dgrad(2, u->g_p0, 1);
+    pool_skip(u->g_p0, view(u->g_cat0, 16, 16), view(u->cat0, 16, 16), 16, 0);
+    wgrad(u, L[1], u->e0a, B, 0);
+    dgrad(1, u->g_e0a, 0);
+    relu_bwd(u->g_e0a, u->e0a, 16, 0);
+    wgrad(u, L[0], u->x0, B, 0);
+}
+
+// loss and output gradient of the batch whose targets and weights are in tgt, wt
+void loss(lbm_unet_s *u, int B) {
+    const long long np = (long long)B * u->cfg.height * u->cfg.width;
+    cudaMemsetAsync(u->sums, 0, 2 * sizeof(double), u->stream);
+    loss_kernel<<<grid_for(np), 256, 0, u->stream>>>(u->out32, 16, u->tgt, u->cfg.out_channels, u->wt, np, u->sums);
+    loss_grad_kernel<<<grid_for(np * 16), 256, 0, u->stream>>>(u->out32, 16, u->tgt, u->cfg.out_channels, u->wt, np,
+                                                                u->sums, u->dout);
+}
+
+int gather_batch(lbm_unet_s *u, int batch, const int *idx) {
+    if (batch < 1 || batch > u->cfg.max_batch) return ufail(LBM_ERR_INVALID, "batch outside 1..max_batch");
+    if (!u->ds_count) return ufail(LBM_ERR_INVALID, "no dataset");
+    const size_t hw = (size_t)u->cfg.height * u->cfg.width;
+    const int oc = u->cfg.out_channels;
+    for (int i = 0; i < batch; ++i) {
+        if (idx[i] < 0 || idx[i] >= u->ds_count) return ufail(LBM_ERR_INVALID, "sample index out of range");
+        cudaMemcpyAsync(u->x0.p + i * hw * 16, u->ds_in + (size_t)idx[i] * hw * 16, hw * 16 * sizeof(bf16),
+                        cudaMemcpyDeviceToDevice, u->stream);
+        cudaMemcpyAsync(u->tgt + i * hw * oc, u->ds_tgt + (size_t)idx[i] * hw * oc, hw * oc * sizeof(float),
+                        cudaMemcpyDeviceToDevice, u->stream);
+        cudaMemcpyAsync(u->wt + i * hw, u->ds_wt + (size_t)idx[i] * hw, hw * sizeof(float), cudaMemcpyDeviceToDevice,
+                        u->stream);
+    }
+    return LBM_OK;
+}
+
+int finish(lbm_unet_s *u, const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(u->stream);
+    if (e != cudaSuccess) return ufail(LBM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return LBM_OK;
+}
+
+uint64_t splitmix(uint64_t &s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_unet_create(const lbm_unet_config *cfg, lbm_unet *out) {
+    if (!cfg || !out) return ufail(LBM_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (cfg->height < 8 || cfg->width < 8 || cfg->height % 8 || cfg->width % 8)
+        return ufail(LBM_ERR_INVALID, "height and width must be positive multiples of 8");
+    if (cfg->in_channels < 1 || cfg->in_channels > 16 || cfg->out_channels < 1 || cfg->out_channels > 16)
+        return ufail(LBM_ERR_INVALID, "in_channels and out_channels must be 1..16");
+    if (cfg->max_batch < 1) return ufail(LBM_ERR_INVALID, "max_batch must be positive");
+    lbm_unet_s *u = new lbm_unet_s();
+    u->cfg = *cfg;
+    if (cudaStreamCreateWithFlags(&u->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&u->e0) != cudaSuccess || cudaEventCreate(&u->e1) != cudaSuccess) {
+        lbm_unet_destroy(u);
+        return ufail(LBM_ERR_CUDA, "stream or event creation failed");
+    }
+    // layers: (cin, cout, relu)
+    const int spec[15][3] = {{16, 16, 1}, {16, 16, 1}, {16, 32, 1}, {32, 32, 1}, {32, 64, 1},
+                             {64, 64, 1}, {64, 64, 1}, {64, 64, 1}, {128, 64, 1}, {64, 32, 1},
+                             {64, 32, 1}, {32, 16, 1}, {32, 16, 1}, {16, 16, 1}, {16, 16, 0}};
+    size_t off = 0;
+    for (int k = 0; k < 15; ++k) {
+        Layer l;
+        l.cin = spec[k][0];
+        l.cout = spec[k][1];
+        l.relu = spec[k][2];
+        l.w_off = off;
+        off += (size_t)9 * l.cin * l.cout;
+        l.b_off = off;
+        off += l.cout;
+        u->L.push_back(l);
+    }
+    u->nparams = (long long)off;
+    int rc = LBM_OK;
+    const size_t pb = sizeof(float) * off;
+    rc = rc ? rc : alloc(u, (void **)&u->params, pb);
+    rc = rc ? rc : alloc(u, (void **)&u->grad, pb);
+    rc = rc ? rc : alloc(u, (void **)&u->adam_m, pb);
+    rc = rc ? rc : alloc(u, (void **)&u->adam_v, pb);
+    for (Layer &l : u->L) {
+        rc = rc ? rc : alloc(u, (void **)&l.w, sizeof(bf16) * 9 * l.cin * l.cout);
+        rc = rc ? rc : alloc(u, (void **)&l.wt, sizeof(bf16) * 9 * l.cin * l.cout);
+    }
+    struct {
+        Act *a;
+        int C, level;
+    } acts[] = {{&u->x0, 16, 0},   {&u->e0a, 16, 0}, {&u->cat0, 32, 0}, {&u->p0, 16, 1},  {&u->e1a, 32, 1},
+                {&u->cat1, 64, 1}, {&u->p1, 32, 2},  {&u->e2a, 64, 2},  {&u->cat2, 128, 2}, {&u->p2, 64, 3},
+                {&u->ba, 64, 3},   {&u->bb, 64, 3},  {&u->d2a, 64, 2},  {&u->d2b, 32, 2}, {&u->d1a, 32, 1},
+                {&u->d1b, 16, 1},  {&u->d0a, 16, 0}, {&u->d0b, 16, 0},
+                {&u->g_e0a, 16, 0}, {&u->g_cat0, 32, 0}, {&u->g_p0, 16, 1}, {&u->g_e1a, 32, 1},
+                {&u->g_cat1, 64, 1}, {&u->g_p1, 32, 2}, {&u->g_e2a, 64, 2}, {&u->g_cat2, 128, 2},
+                {&u->g_p2, 64, 3}, {&u->g_ba, 64, 3}, {&u->g_bb, 64, 3}, {&u->g_d2a, 64, 2}, {&u->g_d2b, 32, 2},
+                {&u->g_d1a, 32, 1}, {&u->g_d1b, 16, 1}, {&u->g_d0a, 16, 0}, {&u->g_d0b, 16, 0}};
+    for (auto &a : acts) rc = rc ? rc : make_act(u, *a.a, a.C, a.level);
+    const size_t np = (size_t)cfg->max_batch * cfg->height * cfg->width;
+    rc = rc ? rc : alloc(u, (void **)&u->out32, np * 16 * sizeof(float));
+    rc = rc ? rc : alloc(u, (void **)&u->dout, np * 16 * sizeof(bf16));
+    // largest pre-activation gradient: level 0 x 16 channels (level l holds 16 * 2^l channels on 4^-l pixels)
+    rc = rc ? rc : alloc(u, (void **)&u->dpre, np * 16 * sizeof(bf16));
+    rc = rc ? rc : alloc(u, (void **)&u->fin, np * 16 * sizeof(float));
+    rc = rc ? rc : alloc(u, (void **)&u->fout, np * 16 * sizeof(float));
+    rc = rc ? rc : alloc(u, (void **)&u->tgt, np * 16 * sizeof(float));
+    rc = rc ? rc : alloc(u, (void **)&u->wt, np * sizeof(float));
+    rc = rc ? rc : alloc(u, (void **)&u->sums, 4 * sizeof(double));
+    if (rc) {
+        lbm_unet_destroy(u);
+        return rc;
+    }
+    // He-normal initialisation over the real fan-in; padded input channels
+    // and unused outputs start (and, without gradient, stay) at zero
+    std::vector<float> p((size_t)off, 0.f);
+    uint64_t s = cfg->seed * 0x2545F4914F6CDD1Dull + 1;
+    for (int k = 0; k < 15; ++k) {
+        const Layer &l = u->L[k];
+        const int cin_real = k == 0 ? cfg->in_channels : l.cin;
+        const int cout_real = k == 14 ? cfg->out_channels : l.cout;
+        const double sd = sqrt(2.0 / (9.0 * cin_real));
+        for (int tap = 0; tap < 9; ++tap)
+            for (int co = 0; co < l.cout; ++co)
+                for (int ci = 0; ci < l.cin; ++ci) {
+                    const double u1 = ((splitmix(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+                    const double u2 = ((splitmix(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+                    const double z = sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+                    if (ci < cin_real && co < cout_real)
+                        p[l.w_off + ((size_t)tap * l.cout + co) * l.cin + ci] = (float)(sd * z);
+                }
+    }
+    cudaMemcpyAsync(u->params, p.data(), pb, cudaMemcpyHostToDevice, u->stream);
+    refresh_weights(u);
+    rc = finish(u, "create");
+    if (rc) {
+        lbm_unet_destroy(u);
+        return rc;
+    }
+    *out = u;
+    return LBM_OK;
+}
+
+long long lbm_unet_param_count(lbm_unet u) { return u ? u->nparams : -1; }
+
+int lbm_unet_get_params(lbm_unet u, float *params) {
+    if (!u || !params) return ufail(LBM_ERR_INVALID, "null argument");
+    cudaMemcpyAsync(params, u->params, sizeof(float) * u->nparams, cudaMemcpyDeviceToHost, u->stream);
+    return finish(u, "get_params");
+}
+
+int lbm_unet_set_params(lbm_unet u, const float *params) {
+    if (!u || !params) return ufail(LBM_ERR_INVALID, "null argument");
+    cudaMemcpyAsync(u->params, params, sizeof(float) * u->nparams, cudaMemcpyHostToDevice, u->stream);
+    cudaMemsetAsync(u->adam_m, 0, sizeof(float) * u->nparams, u->stream);
+    cudaMemsetAsync(u->adam_v, 0, sizeof(float) * u->nparams, u->stream);
+    u->adam_t = 0;
+    refresh_weights(u);
+    return finish(u, "set_params");
+}
+
+int lbm_unet_set_dataset(lbm_unet u, int count, const float *inputs, const float *targets, const float *weights) {
+    if (!u || count < 1 || !inputs || !targets || !weights) return ufail(LBM_ERR_INVALID, "bad dataset arguments");
+    const size_t hw = (size_t)u->cfg.height * u->cfg.width;
+    const int ic = u->cfg.in_channels, oc = u->cfg.out_channels;
+    cudaStreamSynchronize(u->stream);
+    if (u->ds_in) cudaFree(u->ds_in);
+    if (u->ds_tgt) cudaFree(u->ds_tgt);
+    if (u->ds_wt) cudaFree(u->ds_wt);
+    u->ds_in = nullptr;
+    u->ds_tgt = u->ds_wt = nullptr;
+    u->ds_count = 0;
+    if (cudaMalloc((void **)&u->ds_in, (size_t)count * hw * 16 * sizeof(bf16)) != cudaSuccess ||
+        cudaMalloc((void **)&u->ds_tgt, (size_t)count * hw * oc * sizeof(float)) != cudaSuccess ||
+        cudaMalloc((void **)&u->ds_wt, (size_t)count * hw * sizeof(float)) != cudaSuccess)
+        return ufail(LBM_ERR_NOMEM, "dataset does not fit on the device");
+    // inputs go through the float staging buffer, max_batch samples at a time
+    for (int s0 = 0; s0 < count; s0 += u->cfg.max_batch) {
+        const int k = count - s0 < u->cfg.max_batch ? count - s0 : u->cfg.max_batch;
+        cudaMemcpyAsync(u->fin, inputs + (size_t)s0 * hw * ic, (size_t)k * hw * ic * sizeof(float),
+                        cudaMemcpyHostToDevice, u->stream);
+        pack_input_kernel<<<grid_for((long long)k * hw * 16), 256, 0, u->stream>>>(u->fin, ic, u->ds_in + (size_t)s0 * hw * 16,
+                                                                                  (long long)k * hw);
+        const int rc = finish(u, "set_dataset");
+        if (rc) return rc;
+    }
+    cudaMemcpyAsync(u->ds_tgt, targets, (size_t)count * hw * oc * sizeof(float), cudaMemcpyHostToDevice, u->stream);
+    cudaMemcpyAsync(u->ds_wt, weights, (size_t)count * hw * sizeof(float), cudaMemcpyHostToDevice, u->stream);
+    const int rc = finish(u, "set_dataset");
+    if (rc == LBM_OK) u->ds_count = count;
+    return rc;
+}
+
+static int grad_pass(lbm_unet u, int batch, const int *idx, double *loss_out) {
+    int rc = gather_batch(u, batch, idx);
+    if (rc) return rc;
+    cudaMemsetAsync(u->grad, 0, sizeof(float) * u->nparams, u->stream);
+    forward(u, batch);
+    loss(u, batch);
+    backward(u, batch);
+    if (loss_out) {
+        double s[2];
+        cudaMemcpyAsync(s, u->sums, sizeof(s), cudaMemcpyDeviceToHost, u->stream);
+        rc = finish(u, "gradients");
+        if (rc) return rc;
+        *loss_out = s[1] > 0 ? s[0] / (u->cfg.out_channels * s[1]) : 0.0;
+    }
+    return LBM_OK;
+}
+
+int lbm_unet_train_step(lbm_unet u, int batch, const int *idx, float lr, double *loss_out) {
+    if (!u || !idx) return ufail(LBM_ERR_INVALID, "null argument");
+    cudaEventRecord(u->e0, u->stream);
+    int rc = grad_pass(u, batch, idx, nullptr);
+    if (rc) return rc;
+    ++u->adam_t;
+    const float c1 = (float)(1.0 / (1.0 - pow(0.9, (double)u->adam_t)));
+    const float c2 = (float)(1.0 / (1.0 - pow(0.999, (double)u->adam_t)));
+    adam_kernel<<<grid_for(u->nparams), 256, 0, u->stream>>>(u->params, u->grad, u->adam_m, u->adam_v, u->nparams, lr,
+                                                              c1, c2);
+    refresh_weights(u);
+    cudaEventRecord(u->e1, u->stream);
+    double s[2] = {0, 0};
+    cudaMemcpyAsync(s, u->sums, sizeof(s), cudaMemcpyDeviceToHost, u->stream);
+    rc = finish(u, "train_step");
+    if (rc) return rc;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, u->e0, u->e1);
+    u->last_ms = ms;
+    const double l = s[1] > 0 ? s[0] / (u->cfg.out_channels * s[1]) : 0.0;
+    if (loss_out) *loss_out = l;
+    if (!isfinite(l)) return ufail(LBM_DIVERGED, "non-finite loss");
+    return LBM_OK;
+}
+
+int lbm_unet_gradients(lbm_unet u, int batch, const int *idx, float *grad, double *loss_out) {
+    if (!u || !idx || !grad) return ufail(LBM_ERR_INVALID, "null argument");
+    int rc = grad_pass(u, batch, idx, loss_out);
+    if (rc) return rc;
+    cudaMemcpyAsync(grad, u->grad, sizeof(float) * u->nparams, cudaMemcpyDeviceToHost, u->stream);
+    return finish(u, "gradients");
+}
+
+int lbm_unet_predict(lbm_unet u, int count, const float *inputs, float *outputs) {
+    if (!u || !inputs || !outputs) return ufail(LBM_ERR_INVALID, "null argument");
+    if (count < 1 || count > u->cfg.max_batch) return ufail(LBM_ERR_INVALID, "count outside 1..max_batch");
+    const long long np = (long long)count * u->cfg.height * u->cfg.width;
+    const int ic = u->cfg.in_channels, oc = u->cfg.out_channels;
+    cudaMemcpyAsync(u->fin, inputs, sizeof(float) * np * ic, cudaMemcpyHostToDevice, u->stream);
+    cudaEventRecord(u->e0, u->stream);
+    pack_input_kernel<<<grid_for(np * 16), 256, 0, u->stream>>>(u->fin, ic, u->x0.p, np);
+    forward(u, count);
+    unpack_output_kernel<<<grid_for(np * oc), 256, 0, u->stream>>>(u->out32, 16, u->fout, oc, np);
+    cudaEventRecord(u->e1, u->stream);
+    cudaMemcpyAsync(outputs, u->fout, sizeof(float) * np * oc, cudaMemcpyDeviceToHost, u->stream);
+    const int rc = finish(u, "predict");
+    if (rc) return rc;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, u->e0, u->e1);
+    u->last_ms = ms;
+    return LBM_OK;
+}
+
+double lbm_unet_last_ms(lbm_unet u) { return u ? u->last_ms : -1.0; }
+
+const char *lbm_unet_last_error(void) { return g_unet_error.c_str(); }
+
+void lbm_unet_destroy(lbm_unet u) {
+    if (!u) return;
+    if (u->stream) cudaStreamSynchronize(u->stream);
+    for (void *p : u->allocs) cudaFree(p);
+    if (u->ds_in) cudaFree(u->ds_in);
+    if (u->ds_tgt) cudaFree(u->ds_tgt);
+    if (u->ds_wt) cudaFree(u->ds_wt);
+    if (u->e0) cudaEventDestroy(u->e0);
+    if (u->e1) cudaEventDestroy(u->e1);
+    if (u->stream) cudaStreamDestroy(u->stream);
+    delete u;
+}
+
+}  // extern "C"

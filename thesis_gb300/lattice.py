@@ -210,10 +210,12 @@ def sphere_duct(n=256, m=256, h=512, porosity=0.70, rmin=6.0, rmax=14.0, seed=0)
     return lat
 
 
-def channel2d(n=1024, m=256, seed=0, n_obstacles=None):
+def channel2d(n=1024, m=256, seed=0, n_obstacles=None, size_scale=1.0):
     """2D channel along x with 1-6 circles (radius 8-32) and rectangles
     (sides 10-60), non-overlapping and clear of the inlet and outlet; walls at
-    y = 0 and y = m-1, inlet x = 0, outlet x = n-1."""
+    y = 0 and y = m-1, inlet x = 0, outlet x = n-1.  size_scale multiplies the
+    obstacle sizes (0.25 for a 256 x 64 channel with the proportions of the
+    1024 x 256 one)."""
     rng = np.random.default_rng(seed)
     k = n_obstacles if n_obstacles is not None else int(rng.integers(1, 7))
     solid = np.zeros((m, n), bool)
@@ -221,18 +223,19 @@ def channel2d(n=1024, m=256, seed=0, n_obstacles=None):
     yy, xx = np.mgrid[0:m, 0:n]
     placed = 0
     tries = 0
+    s = float(size_scale)
     while placed < k and tries < 10_000:
         tries += 1
-        rmax = min(32.0, (m - 8) / 2.0, n * 0.3)
-        smax = min(60.0, m - 8.0, n * 0.5)
+        rmax = min(32.0 * s, (m - 8) / 2.0, n * 0.3)
+        smax = min(60.0 * s, m - 8.0, n * 0.5)
         if rng.uniform() < 0.5:
-            r = rng.uniform(min(8.0, rmax), rmax)
+            r = rng.uniform(min(8.0 * s, rmax), rmax)
             cx = rng.uniform(n * 0.1 + r, n * 0.85 - r)
             cy = rng.uniform(r + 3, m - 4 - r)
             bb = (cx - r, cy - r, cx + r, cy + r)
             shape = ("circle", cx, cy, r)
         else:
-            w, hh = rng.uniform(min(10.0, smax), smax, 2)
+            w, hh = rng.uniform(min(10.0 * s, smax), smax, 2)
             x0 = rng.uniform(n * 0.1, n * 0.85 - w)
             y0 = rng.uniform(3, m - 4 - hh)
             bb = (x0, y0, x0 + w, y0 + hh)

@@ -62,6 +62,12 @@ class RunConfig(C.Structure):
                 ("boundary_id", C.c_int), ("update_inlet_outlet", C.c_int), ("unparsed_lines", C.c_int)]
 
 
+class UnetConfig(C.Structure):
+    """lbm_unet_config (include/thesis_unet.h)."""
+    _fields_ = [("height", C.c_int), ("width", C.c_int), ("in_channels", C.c_int), ("out_channels", C.c_int),
+                ("max_batch", C.c_int), ("seed", C.c_ulonglong)]
+
+
 _lib = None
 
 
@@ -132,6 +138,17 @@ def lib():
         "lbm_cg_nodes": (C.c_longlong, [vp]),
         "lbm_cg_last_error": (C.c_char_p, []),
         "lbm_cg_destroy": (None, [vp]),
+        "lbm_unet_create": (C.c_int, [C.POINTER(UnetConfig), C.POINTER(vp)]),
+        "lbm_unet_param_count": (C.c_longlong, [vp]),
+        "lbm_unet_get_params": (C.c_int, [vp, fp]),
+        "lbm_unet_set_params": (C.c_int, [vp, fp]),
+        "lbm_unet_set_dataset": (C.c_int, [vp, C.c_int, fp, fp, fp]),
+        "lbm_unet_train_step": (C.c_int, [vp, C.c_int, _IP, C.c_float, dp]),
+        "lbm_unet_gradients": (C.c_int, [vp, C.c_int, _IP, fp, dp]),
+        "lbm_unet_predict": (C.c_int, [vp, C.c_int, fp, fp]),
+        "lbm_unet_last_ms": (C.c_double, [vp]),
+        "lbm_unet_last_error": (C.c_char_p, []),
+        "lbm_unet_destroy": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -156,4 +173,10 @@ def check(rc):
 def check_cg(rc):
     if rc != LBM_OK:
         raise LbmError(rc, lib().lbm_cg_last_error().decode(errors="replace"))
+    return rc
+
+
+def check_unet(rc):
+    if rc != LBM_OK:
+        raise LbmError(rc, lib().lbm_unet_last_error().decode(errors="replace"))
     return rc
