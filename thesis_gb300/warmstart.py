@@ -11,8 +11,14 @@ Workload (a 256 x 64 version of the 1024 x 256 channel with the same
 proportions): D2Q9 TRT, walls at y = 0 and y = m-1 (half-way bounce-back),
 1-6 circles and rectangles, parabolic velocity inlet at x = 0 with centre-line
 velocity 0.05, pressure outlet rho = 1 at x = n-1, Re = 0.05 m / nu uniform
-in [20, 200], FP32 storage.  Residual: sqrt(sum |u - u_prev|^2) /
-sqrt(sum |u|^2) over fluid nodes every 100 steps (lbm_batch_residuals).
+in [20, 100], FP32 storage.  Residual: sqrt(sum |u - u_prev|^2) /
+sqrt(sum |u|^2) over fluid nodes every 100 steps (lbm_batch_residuals),
+tolerance 1e-5.  Measured on this family: above Re ~ 110 the flows develop
+growing unsteady modes (the residual rises again after 100k steps), and with
+FP32 storage the steady flows settle at a residual of 1.5-3.5e-6 (rounding
+keeps the weakly damped acoustic modes between the velocity inlet and the
+pressure outlet excited; FP64 storage settles near 2e-7), so 1e-6 is out of
+reach in FP32 and 1e-5 is the tolerance every steady FP32 run meets.
 """
 import ctypes as C
 import time
@@ -29,7 +35,8 @@ SCALE_U = 0.05        # u, v targets in units of the inlet centre-line velocity
 SCALE_RHO = 0.01      # rho - 1 target scale
 IN_CHANNELS = 4       # fluid mask, Re / 200, inlet profile, x / n
 OUT_CHANNELS = 3      # u, v, rho - 1 (scaled)
-RE_RANGE = (20.0, 200.0)
+RE_RANGE = (20.0, 100.0)
+TOL = 1e-5
 
 
 def geometry(seed, n=256, m=64):
@@ -192,7 +199,7 @@ class UNet:
         return np.array(hist)
 
 
-def solve_batch(lats, res, init=None, tol=1e-6, check_every=100, max_steps=2_000_000, storage=N.STORE_F32):
+def solve_batch(lats, res, init=None, tol=TOL, check_every=100, max_steps=400_000, storage=N.STORE_F32):
     """Run every channel to the residual tolerance in one batch.  init: None
     (fluid at rest, rho = 1) or a list of (rho, u, v) per domain.  Returns
     (steps, residuals, status, seconds, fields) with fields[d] = (rho, u, v)."""
@@ -225,7 +232,7 @@ def dataset(seeds, n=256, m=64, **kw):
     lats = [geometry(s, n, m) for s in seeds]
     res = [reynolds(s) for s in seeds]
     steps, resid, rc, secs, out = solve_batch(lats, res, **kw)
-    tol = kw.get("tol", 1e-6)
+    tol = kw.get("tol", TOL)
     X = np.stack([features(l, r) for l, r in zip(lats, res)])
     Y = np.zeros((len(seeds), m, n, OUT_CHANNELS), np.float32)
     Wt = np.zeros((len(seeds), m, n), np.float32)
@@ -235,7 +242,7 @@ def dataset(seeds, n=256, m=64, **kw):
     return X, Y, Wt, steps, resid, secs
 
 
-def compare(unet, seeds, n=256, m=64, tol=1e-6, check_every=100, max_steps=2_000_000):
+def compare(unet, seeds, n=256, m=64, tol=TOL, check_every=100, max_steps=400_000):
     """Cold start (fluid at rest) against the U-Net warm start on the same
     channels, each batch run to the tolerance.  Returns a dict with per-domain
     steps, wall times, the prediction time and the converged fields'
