@@ -9,14 +9,15 @@
  * has no learned part; this is the project's extension of its steady-state
  * loop (Iterate.cu:385-625: residual-driven iteration to a stop condition).
  *
- * Network (3 pooling levels, base width 16): two 3x3 convolutions + ReLU per
- * level (16, 32, 64 channels), 2x2 average pooling, a 64-channel bottleneck,
- * nearest upsampling with skip concatenation, and a 3x3 output convolution
- * with 16 channels of which the first out_channels are used.  Activations are
- * NHWC BF16 with channels padded to multiples of 16, weights BF16 copies of
- * FP32 master weights, accumulation FP32 on the tensor cores (hand-written
- * mma.sync.m16n8k16 BF16 kernels: forward, data gradient, weight gradient),
- * Adam in FP32.
+ * Network (L pooling levels, widths c_l = min(16 * 2^l, 64)): two 3x3
+ * convolutions + ReLU per encoder level, 2x2 average pooling, a bottleneck of
+ * two convolutions at level L, nearest upsampling with skip concatenation and
+ * two convolutions per decoder level, and a 3x3 output convolution with 16
+ * channels of which the first out_channels are used (4L + 3 convolutions).
+ * Activations are NHWC BF16 with channels padded to multiples of 16, weights
+ * BF16 copies of FP32 master weights, accumulation FP32 on the tensor cores
+ * (hand-written mma.sync.m16n8k16 BF16 kernels: forward, data gradient,
+ * weight gradient), Adam in FP32.
  *
  * Conventions as in thesis_lbm.h: status codes (LBM_OK ...), caller-owned
  * host buffers, device buffers owned by the handle, one handle per thread.
@@ -31,11 +32,13 @@ extern "C" {
 typedef struct lbm_unet_s *lbm_unet;
 
 typedef struct lbm_unet_config {
-    int height, width;        /* image = lattice m x n; multiples of 8 */
+    int height, width;        /* image = lattice m x n */
     int in_channels;          /* input features per pixel, 1..16 */
     int out_channels;         /* predicted fields per pixel, 1..16 */
     int max_batch;            /* largest training / prediction batch */
     unsigned long long seed;  /* weight initialisation (He normal) */
+    int levels;               /* pooling levels L, 3..5 (0 selects 3); height and
+                                 width must be multiples of 2^L */
 } lbm_unet_config;
 
 int lbm_unet_create(const lbm_unet_config *cfg, lbm_unet *out);

@@ -10,14 +10,31 @@ TEST INFRASTRUCTURE ONLY: imported by tests/ and never by the product.
 """
 import numpy as np
 
-# (cin, cout, relu) of the 15 convolutions, in parameter order
-SPEC = [(16, 16, 1), (16, 16, 1), (16, 32, 1), (32, 32, 1), (32, 64, 1), (64, 64, 1), (64, 64, 1),
-        (64, 64, 1), (128, 64, 1), (64, 32, 1), (64, 32, 1), (32, 16, 1), (32, 16, 1), (16, 16, 1),
-        (16, 16, 0)]
+def ch(l):
+    """Width of level l: min(16 * 2^l, 64)."""
+    return min(16 << l, 64)
 
 
-def param_count():
-    return sum(9 * ci * co + co for ci, co, _ in SPEC)
+def spec(levels=3):
+    """(cin, cout, relu) of the 4L + 3 convolutions, in parameter order:
+    two per encoder level, two at the bottleneck, two per decoder level from
+    the deepest up, and the output convolution."""
+    out = []
+    for l in range(levels):
+        out += [(16 if l == 0 else ch(l - 1), ch(l), 1), (ch(l), ch(l), 1)]
+    out += [(ch(levels - 1), ch(levels), 1), (ch(levels), ch(levels), 1)]
+    for l in range(levels - 1, -1, -1):
+        up = ch(levels) if l == levels - 1 else ch(l)
+        out += [(up + ch(l), ch(l), 1), (ch(l), ch(l - 1) if l > 0 else ch(0), 1)]
+    out.append((ch(0), 16, 0))
+    return out
+
+
+SPEC = spec(3)
+
+
+def param_count(levels=3):
+    return sum(9 * ci * co + co for ci, co, _ in spec(levels))
 
 
 def bf16(x, on=True):
@@ -30,9 +47,9 @@ def bf16(x, on=True):
     return r.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-def unpack(params):
+def unpack(params, levels=3):
     out, off = [], 0
-    for ci, co, _ in SPEC:
+    for ci, co, _ in spec(levels):
         w = np.asarray(params[off:off + 9 * ci * co], np.float64).reshape(9, co, ci)
         off += 9 * ci * co
         b = np.asarray(params[off:off + co], np.float64)
@@ -85,43 +102,35 @@ def up_grad(g):
     return g.reshape(B, H // 2, 2, W // 2, 2, C).sum(axis=(2, 4))
 
 
-def forward(params, x_in, rnd=True):
+def forward(params, x_in, rnd=True, levels=3):
     """x_in [B,H,W,in_ch] -> (output [B,H,W,16], cache)."""
-    P = unpack(params)
+    S = spec(levels)
+    P = unpack(params, levels)
     Wr = [bf16(w, rnd) for w, _ in P]
     R = lambda a: bf16(a, rnd)
     B, H, W, ic = x_in.shape
     x0 = np.zeros((B, H, W, 16))
     x0[..., :ic] = x_in
     x0 = R(x0)
-    c = {"x0": x0}
+    c = {"x0": x0, "Wr": Wr, "levels": levels}
 
     def cv(k, x):
         y = conv(x, Wr[k], P[k][1])
-        return R(np.maximum(y, 0.0)) if SPEC[k][2] else y
+        return R(np.maximum(y, 0.0)) if S[k][2] else y
 
-    c["e0a"] = cv(0, x0)
-    c["e0b"] = cv(1, c["e0a"])
-    c["p0"] = R(pool(c["e0b"]))
-    c["e1a"] = cv(2, c["p0"])
-    c["e1b"] = cv(3, c["e1a"])
-    c["p1"] = R(pool(c["e1b"]))
-    c["e2a"] = cv(4, c["p1"])
-    c["e2b"] = cv(5, c["e2a"])
-    c["p2"] = R(pool(c["e2b"]))
-    c["ba"] = cv(6, c["p2"])
-    c["bb"] = cv(7, c["ba"])
-    c["cat2"] = np.concatenate([up(c["bb"]), c["e2b"]], -1)
-    c["d2a"] = cv(8, c["cat2"])
-    c["d2b"] = cv(9, c["d2a"])
-    c["cat1"] = np.concatenate([up(c["d2b"]), c["e1b"]], -1)
-    c["d1a"] = cv(10, c["cat1"])
-    c["d1b"] = cv(11, c["d1a"])
-    c["cat0"] = np.concatenate([up(c["d1b"]), c["e0b"]], -1)
-    c["d0a"] = cv(12, c["cat0"])
-    c["d0b"] = cv(13, c["d0a"])
-    c["out"] = cv(14, c["d0b"])
-    c["Wr"] = Wr
+    x = x0
+    for l in range(levels):
+        c["ea%d" % l] = cv(2 * l, x)
+        c["eb%d" % l] = cv(2 * l + 1, c["ea%d" % l])
+        x = c["p%d" % l] = R(pool(c["eb%d" % l]))
+    c["ba"] = cv(2 * levels, x)
+    prev = c["bb"] = cv(2 * levels + 1, c["ba"])
+    for l in range(levels - 1, -1, -1):
+        k = 2 * levels + 2 + 2 * (levels - 1 - l)
+        c["cat%d" % l] = np.concatenate([up(prev), c["eb%d" % l]], -1)
+        c["da%d" % l] = cv(k, c["cat%d" % l])
+        prev = c["db%d" % l] = cv(k + 1, c["da%d" % l])
+    c["out"] = cv(4 * levels + 2, prev)
     return c["out"], c
 
 
@@ -138,48 +147,53 @@ def loss_and_grad(out, target, weight, oc, rnd=True):
 def backward(params, cache, dout, rnd=True):
     """Parameter gradients in parameter order (FP64)."""
     c = cache
-    Wr = c["Wr"]
+    Wr, levels = c["Wr"], c["levels"]
     R = lambda a: bf16(a, rnd)
-    grads = [None] * 15
+    grads = [None] * (4 * levels + 3)
 
-    def layer(k, dpre, x):
+    def layer(k, dpre, x, data_grad=True):
         grads[k] = (conv_weight_grad(dpre, x), dpre.sum(axis=(0, 1, 2)))
-        return R(conv_data_grad(dpre, Wr[k]))
+        return R(conv_data_grad(dpre, Wr[k])) if data_grad else None
 
     relu = lambda g, a: g * (a > 0)
-    g = layer(14, dout, c["d0b"])
-    g = layer(13, relu(g, c["d0b"]), c["d0a"])
-    g_cat0 = layer(12, relu(g, c["d0a"]), c["cat0"])
-    g = layer(11, R(up_grad(g_cat0[..., :16])) * (c["d1b"] > 0), c["d1a"])
-    g_cat1 = layer(10, relu(g, c["d1a"]), c["cat1"])
-    g = layer(9, R(up_grad(g_cat1[..., :32])) * (c["d2b"] > 0), c["d2a"])
-    g_cat2 = layer(8, relu(g, c["d2a"]), c["cat2"])
-    g = layer(7, R(up_grad(g_cat2[..., :64])) * (c["bb"] > 0), c["ba"])
-    g_p2 = layer(6, relu(g, c["ba"]), c["p2"])
-    g = layer(5, R(0.25 * up(g_p2) + g_cat2[..., 64:]) * (c["e2b"] > 0), c["e2a"])
-    g_p1 = layer(4, relu(g, c["e2a"]), c["p1"])
-    g = layer(3, R(0.25 * up(g_p1) + g_cat1[..., 32:]) * (c["e1b"] > 0), c["e1a"])
-    g_p0 = layer(2, relu(g, c["e1a"]), c["p0"])
-    g = layer(1, R(0.25 * up(g_p0) + g_cat0[..., 16:]) * (c["e0b"] > 0), c["e0a"])
-    d0 = relu(g, c["e0a"])
-    grads[0] = (conv_weight_grad(d0, c["x0"]), d0.sum(axis=(0, 1, 2)))
+    g = layer(4 * levels + 2, dout, c["db0"])
+    g_cat = {}
+    for l in range(levels):
+        k = 2 * levels + 2 + 2 * (levels - 1 - l)
+        if l == 0:
+            dpre = relu(g, c["db0"])
+        else:
+            cu = c["db%d" % l].shape[-1]
+            dpre = R(up_grad(g_cat[l - 1][..., :cu])) * (c["db%d" % l] > 0)
+        g = layer(k + 1, dpre, c["da%d" % l])
+        g_cat[l] = layer(k, relu(g, c["da%d" % l]), c["cat%d" % l])
+    cb = c["bb"].shape[-1]
+    g = layer(2 * levels + 1, R(up_grad(g_cat[levels - 1][..., :cb])) * (c["bb"] > 0), c["ba"])
+    g_p = layer(2 * levels, relu(g, c["ba"]), c["p%d" % (levels - 1)])
+    for l in range(levels - 1, -1, -1):
+        cu = g_cat[l].shape[-1] - c["eb%d" % l].shape[-1]
+        dpre = R(0.25 * up(g_p) + g_cat[l][..., cu:]) * (c["eb%d" % l] > 0)
+        g = layer(2 * l + 1, dpre, c["ea%d" % l])
+        x = c["x0"] if l == 0 else c["p%d" % (l - 1)]
+        g_p = layer(2 * l, relu(g, c["ea%d" % l]), x, data_grad=l > 0)
     return np.concatenate([np.concatenate([w.reshape(-1), b]) for w, b in grads])
 
 
-def loss_and_gradients(params, x_in, target, weight, oc, rnd=True):
-    out, cache = forward(params, x_in, rnd)
+def loss_and_gradients(params, x_in, target, weight, oc, rnd=True, levels=3):
+    out, cache = forward(params, x_in, rnd, levels)
     loss, dout = loss_and_grad(out, target, weight, oc, rnd)
     return loss, backward(params, cache, dout, rnd)
 
 
-def init_params(in_channels, out_channels, seed):
+def init_params(in_channels, out_channels, seed, levels=3):
     """He-normal weights over the real fan-in (any generator: the tests set
     the GPU's parameters from this)."""
     rng = np.random.default_rng(seed)
     out = []
-    for k, (ci, co, _) in enumerate(SPEC):
+    S = spec(levels)
+    for k, (ci, co, _) in enumerate(S):
         cin_real = in_channels if k == 0 else ci
-        cout_real = out_channels if k == 14 else co
+        cout_real = out_channels if k == len(S) - 1 else co
         w = rng.standard_normal((9, co, ci)) * np.sqrt(2.0 / (9 * cin_real))
         w[:, cout_real:, :] = 0.0
         w[:, :, cin_real:] = 0.0

@@ -23,11 +23,12 @@ def _problem(B, H, W, ic, oc, seed):
     return x, t, w
 
 
-def test_oracle_matches_finite_differences():
-    x, t, w = _problem(1, 8, 16, 4, 3, 0)
-    p = uo.init_params(4, 3, 1).astype(np.float64)
-    loss, g = uo.loss_and_gradients(p, x, t, w, 3, rnd=False)
-    assert p.size == uo.param_count() == g.size
+@pytest.mark.parametrize("levels", [3, 4])
+def test_oracle_matches_finite_differences(levels):
+    x, t, w = _problem(1, 16, 32, 4, 3, 0)
+    p = uo.init_params(4, 3, 1, levels).astype(np.float64)
+    loss, g = uo.loss_and_gradients(p, x, t, w, 3, rnd=False, levels=levels)
+    assert p.size == uo.param_count(levels) == g.size
     rng = np.random.default_rng(2)
     live = np.nonzero(np.abs(g) > 1e-6 * np.abs(g).max())[0]
     for i in rng.choice(live, 24, replace=False):
@@ -35,42 +36,43 @@ def test_oracle_matches_finite_differences():
         pp, pm = p.copy(), p.copy()
         pp[i] += e
         pm[i] -= e
-        fd = (uo.loss_and_gradients(pp, x, t, w, 3, rnd=False)[0] -
-              uo.loss_and_gradients(pm, x, t, w, 3, rnd=False)[0]) / (2 * e)
+        fd = (uo.loss_and_gradients(pp, x, t, w, 3, rnd=False, levels=levels)[0] -
+              uo.loss_and_gradients(pm, x, t, w, 3, rnd=False, levels=levels)[0]) / (2 * e)
         assert abs(fd - g[i]) <= 1e-6 * max(abs(g[i]), 1e-3 * np.abs(g).max()), (i, fd, g[i])
 
 
-def _layer_slices():
+def _layer_slices(levels):
     off = 0
-    for ci, co, _ in uo.SPEC:
+    for ci, co, _ in uo.spec(levels):
         n = 9 * ci * co + co
         yield slice(off, off + n)
         off += n
 
 
 @pytest.mark.gpu
-def test_gpu_gradients_match_oracle():
+@pytest.mark.parametrize("levels", [3, 4])
+def test_gpu_gradients_match_oracle(levels):
     from thesis_gb300.warmstart import UNet
     B, H, W, ic, oc = 2, 16, 32, 4, 3
     x, t, w = _problem(B, H, W, ic, oc, 5)
-    p = uo.init_params(ic, oc, 7)
-    with UNet(H, W, max_batch=B, in_channels=ic, out_channels=oc) as net:
+    p = uo.init_params(ic, oc, 7, levels)
+    with UNet(H, W, max_batch=B, in_channels=ic, out_channels=oc, levels=levels) as net:
         assert net.num_params == p.size
         net.set_params(p)
         np.testing.assert_array_equal(net.params(), p)
         net.set_dataset(x, t, w)
         g, loss = net.gradients([0, 1])
         pred = net.predict(x)
-    ref_loss, ref_g = uo.loss_and_gradients(p, x, t, w, oc, rnd=True)
+    ref_loss, ref_g = uo.loss_and_gradients(p, x, t, w, oc, rnd=True, levels=levels)
     assert abs(loss - ref_loss) <= 1e-3 * ref_loss
-    for k, s in enumerate(_layer_slices()):
+    for k, s in enumerate(_layer_slices(levels)):
         a, b = g[s].astype(np.float64), ref_g[s]
         nb = np.linalg.norm(b)
         if nb == 0:
             assert np.linalg.norm(a) == 0
             continue
         assert np.linalg.norm(a - b) <= 3e-2 * nb, (k, np.linalg.norm(a - b) / nb)
-    out, _ = uo.forward(p, x, rnd=True)
+    out, _ = uo.forward(p, x, rnd=True, levels=levels)
     err = np.abs(pred - out[..., :oc]).max() / np.abs(out[..., :oc]).max()
     assert err < 2e-2, err
 

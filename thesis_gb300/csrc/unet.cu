@@ -20,6 +20,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <array>
 #include <string>
 #include <vector>
 
@@ -395,18 +396,21 @@ struct Layer {
 
 struct lbm_unet_s {
     lbm_unet_config cfg;
+    int levels = 3;
     cudaStream_t stream = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     double last_ms = 0;
-    std::vector<Layer> L;
+    std::vector<Layer> L;  // enc_a(l), enc_b(l) for l < levels; bottleneck a, b; dec_a(l), dec_b(l) for
+                           // l = levels-1 .. 0; output
     long long nparams = 0;
     float *params = nullptr, *grad = nullptr, *adam_m = nullptr, *adam_v = nullptr;
     long long adam_t = 0;
     std::vector<void *> allocs;
-    // activations and their gradients
-    Act x0, e0a, cat0, p0, e1a, cat1, p1, e2a, cat2, p2, ba, bb, d2a, d2b, d1a, d1b, d0a, d0b;
-    Act g_e0a, g_cat0, g_p0, g_e1a, g_cat1, g_p1, g_e2a, g_cat2, g_p2, g_ba, g_bb, g_d2a, g_d2b, g_d1a, g_d1b,
-        g_d0a, g_d0b;
+    // activations per level and their gradients: e_a[l] first encoder conv,
+    // cat[l] = [upsampled decoder input | second encoder conv (the skip)],
+    // p[l] pooled (level l + 1), d_a[l] / d_b[l] decoder convs, ba / bb bottleneck
+    Act x0, ba, bb, g_ba, g_bb;
+    std::vector<Act> e_a, cat, p, d_a, d_b, g_e_a, g_cat, g_p, g_d_a, g_d_b;
     float *out32 = nullptr;     // [B][H][W][16] FP32 output
     bf16 *dout = nullptr;       // its gradient
     bf16 *dpre = nullptr;       // scratch: a layer's pre-activation gradient
@@ -423,6 +427,20 @@ namespace {
 
 int H_of(const lbm_unet_s *u, int level) { return u->cfg.height >> level; }
 int W_of(const lbm_unet_s *u, int level) { return u->cfg.width >> level; }
+
+// widths: c_l = min(16 * 2^l, 64); the second decoder conv of level l
+// outputs c_(l-1) (c_0 at level 0), which level l-1 upsamples into its
+// concatenation; level levels-1 upsamples the bottleneck (c_levels)
+int ch(int l) { return (16 << l) < 64 ? (16 << l) : 64; }
+int ch_dec_b(int l) { return l > 0 ? ch(l - 1) : ch(0); }
+int ch_up(const lbm_unet_s *u, int l) { return l == u->levels - 1 ? ch(u->levels) : ch(l); }
+int enc_a(int l) { return 2 * l; }
+int enc_b(int l) { return 2 * l + 1; }
+int bott_a(const lbm_unet_s *u) { return 2 * u->levels; }
+int bott_b(const lbm_unet_s *u) { return 2 * u->levels + 1; }
+int dec_a(const lbm_unet_s *u, int l) { return 2 * u->levels + 2 + 2 * (u->levels - 1 - l); }
+int dec_b(const lbm_unet_s *u, int l) { return dec_a(u, l) + 1; }
+int out_layer(const lbm_unet_s *u) { return 4 * u->levels + 2; }
 
 int alloc(lbm_unet_s *u, void **p, size_t bytes) {
     cudaError_t e = cudaMalloc(p, bytes > 0 ? bytes : 16);
@@ -473,7 +491,9 @@ void wgrad(lbm_unet_s *u, const Layer &l, const Act &in, int B, int level) {
     if (l.cout == CO && l.cin == CI) {                                                                        \
         wgrad_kernel<CO, CI><<<grid, 128, 0, u->stream>>>(u->dpre, in.p, in.cs, in.co, dw, B, H, W);         \
     } else
-    WG(16, 16) WG(32, 16) WG(32, 32) WG(64, 32) WG(64, 64) WG(64, 128) WG(32, 64) WG(16, 32) {}
+    WG(16, 16) WG(32, 16) WG(32, 32) WG(64, 32) WG(64, 64) WG(64, 128) WG(32, 64) WG(16, 32) {
+        ufail(LBM_ERR_INVALID, "no weight-gradient kernel for this layer shape");
+    }
 #undef WG
     const long long npix = (long long)B * H * W;
     bias_grad_kernel<<<grid_for(npix, 256), 256, 0, u->stream>>>(u->dpre, l.cout, npix, u->grad + l.b_off);
@@ -489,46 +509,39 @@ void refresh_weights(lbm_unet_s *u) {
 void forward(lbm_unet_s *u, int B) {
     auto &L = u->L;
     const float *P = u->params;
+    const int NL = u->levels;
     auto cv = [&](int k, const Act &in, const Act &out, int lev, float *o32 = nullptr) {
         conv(u, L[k], in, out, P + L[k].b_off, o32, B, lev, false);
     };
-    auto pool = [&](const Act &in, const Act &out, int lev_out) {
-        const long long n = (long long)B * H_of(u, lev_out) * W_of(u, lev_out) * out.C;
-        pool_kernel<<<grid_for(n), 256, 0, u->stream>>>(in.p, in.cs, in.co, out.p, out.C, B, H_of(u, lev_out),
-                                                          W_of(u, lev_out));
-    };
-    auto up = [&](const Act &in, const Act &out, int lev_out) {
-        const long long n = (long long)B * H_of(u, lev_out) * W_of(u, lev_out) * in.C;
-        up_kernel<<<grid_for(n), 256, 0, u->stream>>>(in.p, in.C, out.p, out.cs, out.co, B, H_of(u, lev_out),
-                                                        W_of(u, lev_out));
-    };
-    cv(0, u->x0, u->e0a, 0);
-    cv(1, u->e0a, view(u->cat0, 16, 16), 0);
-    pool(view(u->cat0, 16, 16), u->p0, 1);
-    cv(2, u->p0, u->e1a, 1);
-    cv(3, u->e1a, view(u->cat1, 32, 32), 1);
-    pool(view(u->cat1, 32, 32), u->p1, 2);
-    cv(4, u->p1, u->e2a, 2);
-    cv(5, u->e2a, view(u->cat2, 64, 64), 2);
-    pool(view(u->cat2, 64, 64), u->p2, 3);
-    cv(6, u->p2, u->ba, 3);
-    cv(7, u->ba, u->bb, 3);
-    up(u->bb, view(u->cat2, 0, 64), 2);
-    cv(8, u->cat2, u->d2a, 2);
-    cv(9, u->d2a, u->d2b, 2);
-    up(u->d2b, view(u->cat1, 0, 32), 1);
-    cv(10, u->cat1, u->d1a, 1);
-    cv(11, u->d1a, u->d1b, 1);
-    up(u->d1b, view(u->cat0, 0, 16), 0);
-    cv(12, u->cat0, u->d0a, 0);
-    cv(13, u->d0a, u->d0b, 0);
+    Act x = u->x0;
+    for (int l = 0; l < NL; ++l) {
+        cv(enc_a(l), x, u->e_a[l], l);
+        const Act skip = view(u->cat[l], ch_up(u, l), ch(l));
+        cv(enc_b(l), u->e_a[l], skip, l);
+        const long long n = (long long)B * H_of(u, l + 1) * W_of(u, l + 1) * ch(l);
+        pool_kernel<<<grid_for(n), 256, 0, u->stream>>>(skip.p, skip.cs, skip.co, u->p[l].p, ch(l), B,
+                                                          H_of(u, l + 1), W_of(u, l + 1));
+        x = u->p[l];
+    }
+    cv(bott_a(u), x, u->ba, NL);
+    cv(bott_b(u), u->ba, u->bb, NL);
+    Act prev = u->bb;
+    for (int l = NL - 1; l >= 0; --l) {
+        const long long n = (long long)B * H_of(u, l) * W_of(u, l) * prev.C;
+        up_kernel<<<grid_for(n), 256, 0, u->stream>>>(prev.p, prev.C, u->cat[l].p, u->cat[l].cs, 0, B, H_of(u, l),
+                                                        W_of(u, l));
+        cv(dec_a(u, l), u->cat[l], u->d_a[l], l);
+        cv(dec_b(u, l), u->d_a[l], u->d_b[l], l);
+        prev = u->d_b[l];
+    }
     Act none;
-    cv(14, u->d0b, none, 0, u->out32);
+    cv(out_layer(u), u->d_b[0], none, 0, u->out32);
 }
 
 // backward pass from dout; parameter gradients accumulate into grad
 void backward(lbm_unet_s *u, int B) {
     auto &L = u->L;
+    const int NL = u->levels;
     auto npix = [&](int lev) { return (long long)B * H_of(u, lev) * W_of(u, lev); };
     auto dgrad = [&](int k, const Act &gin, int lev) {
         Act d;
@@ -556,49 +569,36 @@ void backward(lbm_unet_s *u, int B) {
     };
     // output layer: dpre = dout
     cudaMemcpyAsync(u->dpre, u->dout, sizeof(bf16) * npix(0) * 16, cudaMemcpyDeviceToDevice, u->stream);
-    wgrad(u, L[14], u->d0b, B, 0);
-    dgrad(14, u->g_d0b, 0);
-    relu_bwd(u->g_d0b, u->d0b, 16, 0);
-    wgrad(u, L[13], u->d0a, B, 0);
-    dgrad(13, u->g_d0a, 0);
-    relu_bwd(u->g_d0a, u->d0a, 16, 0);
-    wgrad(u, L[12], u->cat0, B, 0);
-    dgrad(12, u->g_cat0, 0);
-    up_bwd(view(u->g_cat0, 0, 16), u->d1b, 16, 1);
-    wgrad(u, L[11], u->d1a, B, 1);
-    dgrad(11, u->g_d1a, 1);
-    relu_bwd(u->g_d1a, u->d1a, 32, 1);
-    wgrad(u, L[10], u->cat1, B, 1);
-    dgrad(10, u->g_cat1, 1);
-    up_bwd(view(u->g_cat1, 0, 32), u->d2b, 32, 2);
-    wgrad(u, L[9], u->d2a, B, 2);
-    dgrad(9, u->g_d2a, 2);
-    relu_bwd(u->g_d2a, u->d2a, 64, 2);
-    wgrad(u, L[8], u->cat2, B, 2);
-    dgrad(8, u->g_cat2, 2);
-    up_bwd(view(u->g_cat2, 0, 64), u->bb, 64, 3);
-    wgrad(u, L[7], u->ba, B, 3);
-    dgrad(7, u->g_ba, 3);
-    relu_bwd(u->g_ba, u->ba, 64, 3);
-    wgrad(u, L[6], u->p2, B, 3);
-    dgrad(6, u->g_p2, 3);
-    pool_skip(u->g_p2, view(u->g_cat2, 64, 64), view(u->cat2, 64, 64), 64, 2);
-    wgrad(u, L[5], u->e2a, B, 2);
-    dgrad(5, u->g_e2a, 2);
-    relu_bwd(u->g_e2a, u->e2a, 64, 2);
-    wgrad(u, L[4], u->p1, B, 2);
-    dgrad(4, u->g_p1, 2);
-    pool_skip(u->g_p1, view(u->g_cat1, 32, 32), view(u->cat1, 32, 32), 32, 1);
-    wgrad(u, L[3], u->e1a, B, 1);
-    dgrad(3, u->g_e1a, 1);
-    relu_bwd(u->g_e1a, u->e1a, 32, 1);
-    wgrad(u, L[2], u->p0, B, 1);
-    dgrad(2, u->g_p0, 1);
-    pool_skip(u->g_p0, view(u->g_cat0, 16, 16), view(u->cat0, 16, 16), 16, 0);
-    wgrad(u, L[1], u->e0a, B, 0);
-    dgrad(1, u->g_e0a, 0);
-    relu_bwd(u->g_e0a, u->e0a, 16, 0);
-    wgrad(u, L[0], u->x0, B, 0);
+    wgrad(u, L[out_layer(u)], u->d_b[0], B, 0);
+    dgrad(out_layer(u), u->g_d_b[0], 0);
+    // decoder, from level 0 up
+    for (int l = 0; l < NL; ++l) {
+        if (l == 0)
+            relu_bwd(u->g_d_b[0], u->d_b[0], ch_dec_b(0), 0);
+        else  // d_b[l] was upsampled into the first channels of cat[l-1]
+            up_bwd(view(u->g_cat[l - 1], 0, ch_dec_b(l)), u->d_b[l], ch_dec_b(l), l);
+        wgrad(u, L[dec_b(u, l)], u->d_a[l], B, l);
+        dgrad(dec_b(u, l), u->g_d_a[l], l);
+        relu_bwd(u->g_d_a[l], u->d_a[l], ch(l), l);
+        wgrad(u, L[dec_a(u, l)], u->cat[l], B, l);
+        dgrad(dec_a(u, l), u->g_cat[l], l);
+    }
+    // bottleneck
+    up_bwd(view(u->g_cat[NL - 1], 0, ch(NL)), u->bb, ch(NL), NL);
+    wgrad(u, L[bott_b(u)], u->ba, B, NL);
+    dgrad(bott_b(u), u->g_ba, NL);
+    relu_bwd(u->g_ba, u->ba, ch(NL), NL);
+    wgrad(u, L[bott_a(u)], u->p[NL - 1], B, NL);
+    dgrad(bott_a(u), u->g_p[NL - 1], NL);
+    // encoder, from the deepest level down
+    for (int l = NL - 1; l >= 0; --l) {
+        pool_skip(u->g_p[l], view(u->g_cat[l], ch_up(u, l), ch(l)), view(u->cat[l], ch_up(u, l), ch(l)), ch(l), l);
+        wgrad(u, L[enc_b(l)], u->e_a[l], B, l);
+        dgrad(enc_b(l), u->g_e_a[l], l);
+        relu_bwd(u->g_e_a[l], u->e_a[l], ch(l), l);
+        wgrad(u, L[enc_a(l)], l == 0 ? u->x0 : u->p[l - 1], B, l);
+        if (l > 0) dgrad(enc_a(l), u->g_p[l - 1], l);
+    }
 }
 
 // loss and output gradient of the batch whose targets and weights are in tgt, wt
@@ -648,28 +648,41 @@ extern "C" {
 int lbm_unet_create(const lbm_unet_config *cfg, lbm_unet *out) {
     if (!cfg || !out) return ufail(LBM_ERR_INVALID, "null argument");
     *out = nullptr;
-    if (cfg->height < 8 || cfg->width < 8 || cfg->height % 8 || cfg->width % 8)
-        return ufail(LBM_ERR_INVALID, "height and width must be positive multiples of 8");
+    const int NL = cfg->levels ? cfg->levels : 3;
+    if (NL < 3 || NL > 5) return ufail(LBM_ERR_INVALID, "levels must be 3..5");
+    const int mult = 1 << NL;
+    if (cfg->height < mult || cfg->width < mult || cfg->height % mult || cfg->width % mult)
+        return ufail(LBM_ERR_INVALID, "height and width must be positive multiples of 2^levels");
     if (cfg->in_channels < 1 || cfg->in_channels > 16 || cfg->out_channels < 1 || cfg->out_channels > 16)
         return ufail(LBM_ERR_INVALID, "in_channels and out_channels must be 1..16");
     if (cfg->max_batch < 1) return ufail(LBM_ERR_INVALID, "max_batch must be positive");
     lbm_unet_s *u = new lbm_unet_s();
     u->cfg = *cfg;
+    u->levels = NL;
     if (cudaStreamCreateWithFlags(&u->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&u->e0) != cudaSuccess || cudaEventCreate(&u->e1) != cudaSuccess) {
         lbm_unet_destroy(u);
         return ufail(LBM_ERR_CUDA, "stream or event creation failed");
     }
-    // layers: (cin, cout, relu)
-    const int spec[15][3] = {{16, 16, 1}, {16, 16, 1}, {16, 32, 1}, {32, 32, 1}, {32, 64, 1},
-                             {64, 64, 1}, {64, 64, 1}, {64, 64, 1}, {128, 64, 1}, {64, 32, 1},
-                             {64, 32, 1}, {32, 16, 1}, {32, 16, 1}, {16, 16, 1}, {16, 16, 0}};
+    // layers (cin, cout, relu) in parameter order
+    std::vector<std::array<int, 3>> spec;
+    for (int l = 0; l < NL; ++l) {
+        spec.push_back({l == 0 ? 16 : ch(l - 1), ch(l), 1});
+        spec.push_back({ch(l), ch(l), 1});
+    }
+    spec.push_back({ch(NL - 1), ch(NL), 1});
+    spec.push_back({ch(NL), ch(NL), 1});
+    for (int l = NL - 1; l >= 0; --l) {
+        spec.push_back({ch_up(u, l) + ch(l), ch(l), 1});
+        spec.push_back({ch(l), ch_dec_b(l), 1});
+    }
+    spec.push_back({ch(0), 16, 0});
     size_t off = 0;
-    for (int k = 0; k < 15; ++k) {
+    for (const auto &sp : spec) {
         Layer l;
-        l.cin = spec[k][0];
-        l.cout = spec[k][1];
-        l.relu = spec[k][2];
+        l.cin = sp[0];
+        l.cout = sp[1];
+        l.relu = sp[2];
         l.w_off = off;
         off += (size_t)9 * l.cin * l.cout;
         l.b_off = off;
@@ -687,18 +700,25 @@ int lbm_unet_create(const lbm_unet_config *cfg, lbm_unet *out) {
         rc = rc ? rc : alloc(u, (void **)&l.w, sizeof(bf16) * 9 * l.cin * l.cout);
         rc = rc ? rc : alloc(u, (void **)&l.wt, sizeof(bf16) * 9 * l.cin * l.cout);
     }
-    struct {
-        Act *a;
-        int C, level;
-    } acts[] = {{&u->x0, 16, 0},   {&u->e0a, 16, 0}, {&u->cat0, 32, 0}, {&u->p0, 16, 1},  {&u->e1a, 32, 1},
-                {&u->cat1, 64, 1}, {&u->p1, 32, 2},  {&u->e2a, 64, 2},  {&u->cat2, 128, 2}, {&u->p2, 64, 3},
-                {&u->ba, 64, 3},   {&u->bb, 64, 3},  {&u->d2a, 64, 2},  {&u->d2b, 32, 2}, {&u->d1a, 32, 1},
-                {&u->d1b, 16, 1},  {&u->d0a, 16, 0}, {&u->d0b, 16, 0},
-                {&u->g_e0a, 16, 0}, {&u->g_cat0, 32, 0}, {&u->g_p0, 16, 1}, {&u->g_e1a, 32, 1},
-                {&u->g_cat1, 64, 1}, {&u->g_p1, 32, 2}, {&u->g_e2a, 64, 2}, {&u->g_cat2, 128, 2},
-                {&u->g_p2, 64, 3}, {&u->g_ba, 64, 3}, {&u->g_bb, 64, 3}, {&u->g_d2a, 64, 2}, {&u->g_d2b, 32, 2},
-                {&u->g_d1a, 32, 1}, {&u->g_d1b, 16, 1}, {&u->g_d0a, 16, 0}, {&u->g_d0b, 16, 0}};
-    for (auto &a : acts) rc = rc ? rc : make_act(u, *a.a, a.C, a.level);
+    for (auto *v : {&u->e_a, &u->cat, &u->p, &u->d_a, &u->d_b, &u->g_e_a, &u->g_cat, &u->g_p, &u->g_d_a, &u->g_d_b})
+        v->resize(NL);
+    rc = rc ? rc : make_act(u, u->x0, 16, 0);
+    for (int l = 0; l < NL; ++l) {
+        rc = rc ? rc : make_act(u, u->e_a[l], ch(l), l);
+        rc = rc ? rc : make_act(u, u->cat[l], ch_up(u, l) + ch(l), l);
+        rc = rc ? rc : make_act(u, u->p[l], ch(l), l + 1);
+        rc = rc ? rc : make_act(u, u->d_a[l], ch(l), l);
+        rc = rc ? rc : make_act(u, u->d_b[l], ch_dec_b(l), l);
+        rc = rc ? rc : make_act(u, u->g_e_a[l], ch(l), l);
+        rc = rc ? rc : make_act(u, u->g_cat[l], ch_up(u, l) + ch(l), l);
+        rc = rc ? rc : make_act(u, u->g_p[l], ch(l), l + 1);
+        rc = rc ? rc : make_act(u, u->g_d_a[l], ch(l), l);
+        rc = rc ? rc : make_act(u, u->g_d_b[l], ch_dec_b(l), l);
+    }
+    rc = rc ? rc : make_act(u, u->ba, ch(NL), NL);
+    rc = rc ? rc : make_act(u, u->bb, ch(NL), NL);
+    rc = rc ? rc : make_act(u, u->g_ba, ch(NL), NL);
+    rc = rc ? rc : make_act(u, u->g_bb, ch(NL), NL);
     const size_t np = (size_t)cfg->max_batch * cfg->height * cfg->width;
     rc = rc ? rc : alloc(u, (void **)&u->out32, np * 16 * sizeof(float));
     rc = rc ? rc : alloc(u, (void **)&u->dout, np * 16 * sizeof(bf16));
@@ -717,10 +737,10 @@ int lbm_unet_create(const lbm_unet_config *cfg, lbm_unet *out) {
     // and unused outputs start (and, without gradient, stay) at zero
     std::vector<float> p((size_t)off, 0.f);
     uint64_t s = cfg->seed * 0x2545F4914F6CDD1Dull + 1;
-    for (int k = 0; k < 15; ++k) {
+    for (int k = 0; k < (int)u->L.size(); ++k) {
         const Layer &l = u->L[k];
         const int cin_real = k == 0 ? cfg->in_channels : l.cin;
-        const int cout_real = k == 14 ? cfg->out_channels : l.cout;
+        const int cout_real = k == out_layer(u) ? cfg->out_channels : l.cout;
         const double sd = sqrt(2.0 / (9.0 * cin_real));
         for (int tap = 0; tap < 9; ++tap)
             for (int co = 0; co < l.cout; ++co)

@@ -100,14 +100,15 @@ def fields(lat, pred):
 class UNet:
     """Handle of the BF16 tensor-core U-Net (lbm_unet_*)."""
 
-    def __init__(self, height, width, max_batch=32, seed=0, in_channels=IN_CHANNELS, out_channels=OUT_CHANNELS):
+    def __init__(self, height, width, max_batch=32, seed=0, in_channels=IN_CHANNELS, out_channels=OUT_CHANNELS,
+                 levels=3):
         self._lib = N.lib()
-        cfg = N.UnetConfig(height, width, in_channels, out_channels, max_batch, seed)
+        cfg = N.UnetConfig(height, width, in_channels, out_channels, max_batch, seed, levels)
         h = C.c_void_p()
         N.check_unet(self._lib.lbm_unet_create(C.byref(cfg), C.byref(h)))
         self._h = h
         self.height, self.width, self.max_batch = height, width, max_batch
-        self.in_channels, self.out_channels = in_channels, out_channels
+        self.in_channels, self.out_channels, self.levels = in_channels, out_channels, levels
         self.dataset_size = 0
 
     def close(self):
