@@ -55,10 +55,15 @@ def parse():
     ap.add_argument("--cpu-sample", default="64,64,128", help="n,m,h of the CPU-baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="target CPU time of one CPU-baseline sample (steps are chosen to fill it)")
-    ap.add_argument("--workload", default="duct", choices=["duct", "cavities", "cg"],
+    ap.add_argument("--workload", default="duct", choices=["duct", "cavities", "cg", "warmstart"],
                     help="duct: the D3Q19 MRT sphere-packed duct (default); cavities: a batch of D2Q9 MRT "
                          "lid-driven cavities of uneven sizes, batched vs one by one; cg: colour-gradient "
-                         "static droplets on a periodic 1024^2 lattice (Laplace law)")
+                         "static droplets on a periodic 1024^2 lattice (Laplace law); warmstart: time to the "
+                         "steady-state tolerance of D2Q9 TRT channels from a U-Net prediction vs from rest")
+    ap.add_argument("--ws-train", type=int, default=2048, help="training channels (steady fields from the solver)")
+    ap.add_argument("--ws-epochs", type=int, default=150)
+    ap.add_argument("--ws-eval", type=int, default=128, help="held-out channels timed cold and warm")
+    ap.add_argument("--ws-levels", type=int, default=5, help="U-Net pooling levels")
     ap.add_argument("--cg-size", type=int, default=1024)
     ap.add_argument("--cg-seeds", type=int, default=3, help="droplets (radius uniform in [64, 256] nodes)")
     ap.add_argument("--cg-steps", type=int, default=40000, help="steps per droplet before the Laplace-law check")
@@ -418,8 +423,119 @@ def run_cg(args):
     return 0
 
 
+def run_warmstart(args):
+    """Learned warm start: steady fields of seeded 256x64 channels from the
+    batched solver train the U-Net on the GPU; held-out channels are then
+    solved to the residual tolerance from rest and from the prediction."""
+    from thesis_gb300 import build as native_build
+    from thesis_gb300 import warmstart as ws
+    native_build.build()
+    n, m = 256, 64
+    t0 = time.perf_counter()
+    X, Y, Wt, dsteps, dres, dsecs = ws.dataset(range(args.ws_train), n, m)
+    conv = dres <= ws.TOL
+    t_data = time.perf_counter() - t0
+    net = ws.UNet(m, n, max_batch=32, seed=1, levels=args.ws_levels)
+    net.set_dataset(X[conv], Y[conv], Wt[conv])
+    batch = 16
+    t0 = time.perf_counter()
+    hist = net.train(epochs=args.ws_epochs, batch=batch, lr=2e-3, lr_final=5e-5)
+    t_train = time.perf_counter() - t0
+    step_ms = float(np.median(net.step_ms[len(net.step_ms) // 2:]))
+    train_flops = 3.0 * ws.forward_flops(m, n, args.ws_levels) * batch  # forward + data and weight gradients
+    achieved = train_flops / (step_ms / 1e3) / 1e12
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak_tf, peak_kind = float(json.load(f)["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        peak_tf, peak_kind = 1900.0, "fallback"
+
+    seeds = range(100000, 100000 + args.ws_eval)
+    clocks = ClockSampler(0)
+    clocks.start()
+    r = ws.compare(net, seeds, n, m)
+    clk = clocks.stop()
+    ok = (r["cold_res"] <= ws.TOL) & (r["warm_res"] <= ws.TOL)
+    perr = []
+    for d, lat in enumerate(r["lats"]):
+        fl = lat.node_type == 1
+        ur = r["cold_fields"][d][1][fl]
+        perr.append(float(np.linalg.norm(r["init"][d][1][fl] - ur) / np.linalg.norm(ur)))
+    # converged-field error of both starts against 300k-step runs of 16 channels
+    k = min(16, len(r["lats"]))
+    ref = ws.solve_batch(r["lats"][:k], r["re"][:k], None, tol=1e-12, max_steps=300_000)[4]
+    ec, ew = [], []
+    for d in range(k):
+        fl = r["lats"][d].node_type == 1
+        ur = ref[d][1][fl]
+        ec.append(float(np.linalg.norm(r["cold_fields"][d][1][fl] - ur) / np.linalg.norm(ur)))
+        ew.append(float(np.linalg.norm(r["warm_fields"][d][1][fl] - ur) / np.linalg.norm(ur)))
+    fluid = np.array([int((lat.node_type == 1).sum()) for lat in r["lats"]])
+    cold_updates = float((r["cold_steps"] * fluid).sum())
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import pyoracle
+        L = pyoracle.oracle_lib()
+        lat = r["lats"][0]
+        kw = dict(u=ws.UMAX, viscosity=ws.UMAX * m / r["re"][0], collision_model=2, outlet_profile=5)
+        nn = lat.num_nodes
+        init = (np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
+        t0 = time.perf_counter()
+        pyoracle.run_oracle(lat, 20, mode=1, init_kind=1, init=init, **kw)
+        est = (time.perf_counter() - t0) / 20
+        steps = int(min(max(args.cpu_seconds / max(est, 1e-6), 20), 200000))
+        t0 = time.perf_counter()
+        res_c = pyoracle.run_oracle(lat, steps, mode=1, init_kind=1, init=init, **kw)
+        dt = time.perf_counter() - t0
+        assert res_c.rc == 0
+        glups = int((lat.node_type == 1).sum()) * steps / dt / 1e9
+        cpu = {"value": cold_updates / (glups * 1e9), "unit": "s", "cores": L.orc_threads(), "kind": "port",
+               "sample": "oracle restatement (FP32, OpenMP) of one 256x64 TRT channel from rest, %d steps in "
+                         "%.1f s = %.4f GLUPS; value = the cold solves' %d fluid-node updates at that rate"
+                         % (steps, dt, glups, int(cold_updates))}
+    line = {"metric": "wall time to a 1e-5 steady-state residual, %d held-out 256x64 D2Q9 TRT channels "
+                      "(Re 20-100), U-Net warm start including its prediction" % len(r["lats"]),
+            "value": r["warm_total_seconds"], "unit": "s", "n_gpus": 1, "steps": int(r["warm_steps"].sum()),
+            "warmup": 0, "ms_per_step": None, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 solver, bf16 network",
+            "data": "synthetic (seeded channel geometries and Reynolds numbers)",
+            "config": {"workload": "256x64 D2Q9 TRT channels, 1-6 obstacles, parabolic inlet u_max 0.05, "
+                                   "pressure outlet, Re uniform in [20, 100], residual every 100 steps, "
+                                   "tolerance 1e-5, one batch of all channels per start",
+                       "unet": {"levels": args.ws_levels, "params": net.num_params, "train_channels": int(conv.sum()),
+                                "epochs": args.ws_epochs, "batch": batch},
+                       "l2_policy": "batch working set (%d x 16k nodes) below L2; timing is wall time "
+                                    "of whole solves" % len(r["lats"])},
+            "cold_seconds": r["cold_total_seconds"], "warm_seconds": r["warm_total_seconds"],
+            "speedup": r["cold_total_seconds"] / r["warm_total_seconds"],
+            "iteration_seconds": {"cold": r["cold_seconds"], "warm": r["warm_seconds"],
+                                  "prediction": r["predict_seconds"]},
+            "steps_to_tolerance": {"converged_both": int(ok.sum()), "cold_median": float(np.median(r["cold_steps"])),
+                                   "warm_median": float(np.median(r["warm_steps"])),
+                                   "warm_over_cold_sum": float(r["warm_steps"][ok].sum() / r["cold_steps"][ok].sum())},
+            "prediction_error_u": {"median": float(np.median(perr)), "p90": float(np.percentile(perr, 90))},
+            "converged_field_error_vs_300k_step_runs": {"channels": k, "cold_median": float(np.median(ec)),
+                                                        "warm_median": float(np.median(ew)),
+                                                        "cold_max": float(max(ec)), "warm_max": float(max(ew))},
+            "training": {"data_seconds": t_data, "data_solve_seconds": dsecs, "train_seconds": t_train,
+                         "step_ms": step_ms, "loss_first": float(hist[0]), "loss_last": float(hist[-1]),
+                         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
+                                      "frac": achieved / peak_tf, "peak_kind": peak_kind,
+                                      "flops_per_step": train_flops}},
+            "e2e": {"value": r["warm_total_seconds"], "unit": "s",
+                    "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                    "includes": "prediction from host features, batch creation, upload of the initial fields, "
+                                "iteration to the tolerance, read-back of the converged fields"},
+            "clocks": clk, "gpu_launches": None, "cpu_baseline": cpu}
+    print(json.dumps(line))
+    net.close()
+
+
 def main():
     args = parse()
+    if args.workload == "warmstart" and args.impl != "reference":
+        return run_warmstart(args)
     if args.workload == "cg" and args.impl != "reference":
         return run_cg(args)
     if args.workload == "cavities" and args.impl != "reference":

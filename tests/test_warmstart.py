@@ -1,0 +1,56 @@
+"""Learned warm start (thesis_gb300/warmstart.py): feature and target
+encoding on the CPU; on the GPU, a network trained on solver-generated
+steady channels must start held-out channels closer to their steady state
+than a start from rest, so they reach the residual tolerance in fewer steps,
+to the same converged field."""
+import numpy as np
+import pytest
+
+from oracle import unet_oracle as uo
+from thesis_gb300 import warmstart as ws
+
+
+def test_encoding_round_trip_and_flop_count():
+    lat = ws.geometry(3)
+    fl = lat.node_type == 1
+    rng = np.random.default_rng(0)
+    rho = (1 + 0.01 * rng.standard_normal(lat.num_nodes)).astype(np.float32)
+    u = (0.05 * rng.standard_normal(lat.num_nodes)).astype(np.float32)
+    v = (0.01 * rng.standard_normal(lat.num_nodes)).astype(np.float32)
+    t, w = ws.targets(lat, rho, u, v)
+    r2, u2, v2 = ws.fields(lat, t)
+    np.testing.assert_allclose(u2[fl], u[fl], rtol=1e-6, atol=1e-9)
+    np.testing.assert_allclose(v2[fl], v[fl], rtol=1e-6, atol=1e-9)
+    np.testing.assert_allclose(r2[fl], rho[fl], rtol=1e-6)
+    assert np.all(u2[~fl] == 0) and np.all(w.reshape(-1)[~fl] == 0)
+    f = ws.features(lat, 50.0)
+    assert f.shape == (lat.m, lat.n, ws.IN_CHANNELS)
+    assert np.all(f[..., 1] == np.float32(0.25))
+    np.testing.assert_allclose(f[:, 0, 2] * ws.UMAX, ws.inlet_profile(lat.m), rtol=1e-6)
+    # FLOPs follow the oracle's layer list
+    for levels in (3, 5):
+        spec = uo.spec(levels)
+        assert len(spec) == 4 * levels + 3
+        assert ws.forward_flops(64, 256, levels) > 2 * 9 * 16 * 16 * 64 * 256
+    assert ws.RE_RANGE[0] <= ws.reynolds(7) <= ws.RE_RANGE[1]
+
+
+@pytest.mark.gpu
+def test_warm_start_reaches_tolerance_in_fewer_steps():
+    X, Y, Wt, steps, resid, _ = ws.dataset(range(256))
+    assert np.all(resid <= ws.TOL)
+    with ws.UNet(64, 256, max_batch=32, seed=2, levels=5) as net:
+        net.set_dataset(X, Y, Wt)
+        hist = net.train(epochs=60, batch=16, lr=2e-3, lr_final=1e-4)
+        assert hist[-1] < 0.05 * hist[0]
+        r = ws.compare(net, range(200000, 200016))
+        lats, res = r["lats"][:4], r["re"][:4]
+        fb_steps, fb_res, fb_out, fb_cold = ws.solve_with_warm_start(net, lats, res)
+    assert np.all(r["cold_res"] <= ws.TOL) and np.all(r["warm_res"] <= ws.TOL)
+    # measured 0.61 with this training; a start from rest is 1.0
+    assert r["warm_steps"].sum() < 0.85 * r["cold_steps"].sum(), (r["warm_steps"], r["cold_steps"])
+    for d, lat in enumerate(r["lats"]):
+        fl = lat.node_type == 1
+        uc, uw = r["cold_fields"][d][1][fl], r["warm_fields"][d][1][fl]
+        assert np.linalg.norm(uw - uc) < 1e-2 * np.linalg.norm(uc)
+    assert np.all(fb_res <= ws.TOL) and not fb_cold.any()

@@ -188,12 +188,14 @@ class UNet:
         steps_per_epoch = max(1, n // batch)
         total = epochs * steps_per_epoch
         hist = []
+        self.step_ms = []
         k = 0
         for ep in range(epochs):
             perm = rng.permutation(n)
             for s in range(steps_per_epoch):
                 rate = lr * (lr_final / lr) ** (k / max(total - 1, 1))
                 hist.append(self.train_step(perm[s * batch:(s + 1) * batch], rate))
+                self.step_ms.append(self.last_ms)
                 k += 1
             if log_every and (ep + 1) % log_every == 0:
                 print("epoch %d loss %.4e" % (ep + 1, float(np.mean(hist[-steps_per_epoch:]))), flush=True)
@@ -203,7 +205,10 @@ class UNet:
 def solve_batch(lats, res, init=None, tol=TOL, check_every=100, max_steps=400_000, storage=N.STORE_F32):
     """Run every channel to the residual tolerance in one batch.  init: None
     (fluid at rest, rho = 1) or a list of (rho, u, v) per domain.  Returns
-    (steps, residuals, status, seconds, fields) with fields[d] = (rho, u, v)."""
+    (steps, residuals, status, seconds, fields, total seconds): seconds of the
+    iteration, fields[d] = (rho, u, v), and the time from batch creation to
+    the fields' read-back."""
+    t_all = time.perf_counter()
     args = [channel_args(r, lat.m, storage) for lat, r in zip(lats, res)]
     with Batch(lats, args) as b:
         b.init()
@@ -222,7 +227,7 @@ def solve_batch(lats, res, init=None, tol=TOL, check_every=100, max_steps=400_00
         for d in range(len(lats)):
             rho, u, v, _ = b.macro(d)
             out.append((rho, u, v))
-    return steps, resid, rc, secs, out
+    return steps, resid, rc, secs, out, time.perf_counter() - t_all
 
 
 def dataset(seeds, n=256, m=64, **kw):
@@ -232,7 +237,7 @@ def dataset(seeds, n=256, m=64, **kw):
     seeds = list(seeds)
     lats = [geometry(s, n, m) for s in seeds]
     res = [reynolds(s) for s in seeds]
-    steps, resid, rc, secs, out = solve_batch(lats, res, **kw)
+    steps, resid, rc, secs, out, _ = solve_batch(lats, res, **kw)
     tol = kw.get("tol", TOL)
     X = np.stack([features(l, r) for l, r in zip(lats, res)])
     Y = np.zeros((len(seeds), m, n, OUT_CHANNELS), np.float32)
@@ -264,4 +269,40 @@ def compare(unet, seeds, n=256, m=64, tol=TOL, check_every=100, max_steps=400_00
         du.append(float(np.abs(warm[4][d][1] - cold[4][d][1])[fl].max() / UMAX))
     return dict(seeds=seeds, re=res, lats=lats, cold_steps=cold[0], warm_steps=warm[0], cold_res=cold[1],
                 warm_res=warm[1], cold_seconds=cold[3], warm_seconds=warm[3], predict_seconds=t_pred,
+                cold_total_seconds=cold[5], warm_total_seconds=warm[5] + t_pred,
                 converged_du=np.array(du), pred=pred, init=init, cold_fields=cold[4], warm_fields=warm[4])
+
+
+def solve_with_warm_start(unet, lats, res, tol=TOL, check_every=100, max_steps=400_000):
+    """Steady solve of every channel from the network's prediction; a domain
+    whose warm run diverges or misses the tolerance is solved again from rest,
+    so the plain cold start is the fallback and the converged LBM field, not
+    the prediction, is the result.  Returns (steps, residuals, fields, cold)
+    with cold[d] True where the fallback ran."""
+    X = np.stack([features(l, r) for l, r in zip(lats, res)])
+    pred = unet.predict(X)
+    init = [fields(l, p) for l, p in zip(lats, pred)]
+    steps, resid, rc, _, out, _ = solve_batch(lats, res, init, tol, check_every, max_steps)
+    redo = [d for d in range(len(lats))
+            if not (resid[d] <= tol and np.all(np.isfinite(out[d][1])))]
+    cold = np.zeros(len(lats), bool)
+    if redo:
+        s2, r2, _, _, o2, _ = solve_batch([lats[d] for d in redo], [res[d] for d in redo], None, tol, check_every,
+                                          max_steps)
+        for k, d in enumerate(redo):
+            steps[d], resid[d], out[d], cold[d] = s2[k], r2[k], o2[k], True
+    return steps, resid, out, cold
+
+
+def forward_flops(height, width, levels=3):
+    """Multiply-add FLOPs (2 per MAC) of one forward pass of the network."""
+    ch = lambda l: min(16 << l, 64)
+    layers = []
+    for l in range(levels):
+        layers += [(16 if l == 0 else ch(l - 1), ch(l), l), (ch(l), ch(l), l)]
+    layers += [(ch(levels - 1), ch(levels), levels), (ch(levels), ch(levels), levels)]
+    for l in range(levels - 1, -1, -1):
+        up = ch(levels) if l == levels - 1 else ch(l)
+        layers += [(up + ch(l), ch(l), l), (ch(l), ch(l - 1) if l > 0 else ch(0), l)]
+    layers.append((ch(0), 16, 0))
+    return sum(2 * 9 * ci * co * (height >> l) * (width >> l) for ci, co, l in layers)
