@@ -145,6 +145,15 @@ int lbm_get_macro(lbm_handle h, float *rho, float *u, float *v, float *w);
  * SoA f[d*n*m*h + node] in the reference's direction order. */
 int lbm_get_populations(lbm_handle h, double *f);
 
+/* Population checkpoint restart: replace the state with f (the layout
+ * lbm_get_populations returns), so a run saved with lbm_get_populations and
+ * resumed here on a handle of the same lattice and parameters continues as
+ * if uninterrupted (exactly for F32 and F64 storage).  Takes the place of
+ * lbm_init; the residual snapshots (norms, MaxMacroDiff, FdRelDiff) start
+ * again from zero fields.  The reference restarts from macroscopic fields
+ * only (FilesReading.cu:224-268); this is the population-level counterpart. */
+int lbm_set_populations(lbm_handle h, const double *f);
+
 /* FP64 norms over fluid nodes of the last stored macroscopic fields:
  * out[0] = sum |u - u_prev|^2, out[1] = sum |u|^2, out[2] = sum rho,
  * out[3] = number of fluid nodes, out[4] = sum rho*ux.  u_prev is the field
@@ -159,6 +168,18 @@ int lbm_macro_norms(lbm_handle h, double *out);
  * post-stream, post-boundary field the next step will pull from it.  Summed
  * in FP64 (the reference sums in FP32).  LBM_DIVERGED when not finite. */
 int lbm_residual_l2(lbm_handle h, double *out);
+
+/* The reference's FdRelDiff residual (ResidualModel = MaxRelativeFdDiff:
+ * computeNewResidual3D / gpu_NewResidual, ComputeResiduals.cu:28-36, :56-64,
+ * Iterate3D.cu:677-692): max over fluid nodes and directions of
+ * |f - f_prev| / |f_first|, f the post-stream, post-boundary populations the
+ * next step pulls, f_prev those at the previous call and f_first those at
+ * the first call after lbm_init; the first call records both snapshots and
+ * returns 0 (it allocates 2 Q N floats).  Entries with f_first = 0 are
+ * skipped (the reference divides by zero there); the maximum is exact (the
+ * reference's reduction adds on load, GpuSum.cu:160).  LBM_DIVERGED when a
+ * population is not finite. */
+int lbm_residual_fd_rel_diff(lbm_handle h, double *out);
 
 /* Drag and lift by momentum exchange (physics mode): the force on the solid
  * nodes inside box = {x0, x1, y0, y1, z0, z1} (inclusive node indices), from

@@ -309,6 +309,65 @@ def test_reference_l2_residual(oracle, case):
     assert abs(r_gpu - r.resid[k]) <= 1e-4 * r.resid[k] + 1e-6, (r_gpu, r.resid[k])
 
 
+@pytest.mark.parametrize("storage", [N.STORE_F64, N.STORE_F32])
+def test_reference_fd_rel_diff_residual(oracle, storage):
+    """lbm_residual_fd_rel_diff (the reference's max |f - f_prev| / f_first)
+    against the same maximum over the oracle's post-stream fields.  The GPU
+    state after k steps streams into the oracle's field after k + 1 steps."""
+    lat = lattice.cavity3d(12, 10, 9)
+    args = Arguments(u=0.05, viscosity=0.1, collision_model=N.MRT, storage=storage, init_equilibrium=1)
+    okw = dict(u=args.u, viscosity=args.viscosity, collision_model=args.collision_model)
+    ks = [10, 25, 45]
+    got = []
+    with Solver(lat, args) as s:
+        s.init()
+        done = 0
+        for k in ks:
+            s.step(k - done, write_macro=True)
+            done = k
+            got.append(s.residual_fd_rel_diff())
+    fl = lat.node_type == 1
+    snaps = [oracle.run_oracle(lat, k + 1, fp64=storage == N.STORE_F64, init_kind=1, **okw).f[:, fl] for k in ks]
+    first = snaps[0]
+    ok = first != 0
+    want = [0.0] + [float((np.abs(snaps[i] - snaps[i - 1])[ok] / np.abs(first[ok])).max()) for i in (1, 2)]
+    assert got[0] == 0.0
+    rtol = 1e-7 if storage == N.STORE_F64 else 2e-2
+    for g, w in zip(got[1:], want[1:]):
+        assert abs(g - w) <= rtol * w, (got, want)
+
+
+@pytest.mark.parametrize("storage", [N.STORE_F32, N.STORE_F64, N.STORE_F16S])
+def test_population_checkpoint_restart(storage):
+    """get_populations after 30 steps, set_populations on a fresh handle and
+    20 more steps give the populations of 50 uninterrupted steps: bit for bit
+    in F32 and F64, within half-precision rounding of tiny deviations in F16S."""
+    lat = lattice.sphere_duct(24, 20, 40, porosity=0.8, rmin=3, rmax=5, seed=3)
+    args = Arguments(viscosity=0.1, collision_model=N.MRT, mode=N.MODE_PHYSICS, init_equilibrium=1,
+                     inlet_profile=N.INLET_PRESSURE, outlet_profile=N.OUTLET_PRESSURE, rho_in=1.01, storage=storage)
+    nn = lat.num_nodes
+    init = (np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
+    with Solver(lat, args) as s:
+        s.init(*init)
+        s.step(30, write_macro=False)
+        saved = s.populations()
+        s.step(20, write_macro=True)
+        f_run = s.populations()
+        m_run = s.macro()
+    with Solver(lat, args) as s:
+        s.set_populations(saved)
+        np.testing.assert_array_equal(s.populations(), saved)
+        s.step(20, write_macro=True)
+        f_rst = s.populations()
+        m_rst = s.macro()
+    if storage == N.STORE_F16S:
+        assert np.abs(f_rst - f_run).max() < 1e-6
+    else:
+        np.testing.assert_array_equal(f_rst, f_run)
+        for a, b in zip(m_rst, m_run):
+            np.testing.assert_array_equal(a, b)
+
+
 def test_momentum_exchange_matches_host_sum(oracle):
     """lbm_momentum_exchange against the same link sum evaluated on the host
     from the read-back populations and flag words; drag along the flow."""

@@ -27,6 +27,8 @@ int launch_init_q9(const StepParams &p, const StepParams &o, int coll, int st, i
 int launch_init_q19(const StepParams &p, const StepParams &o, int coll, int st, int phys, int eq, cudaStream_t s);
 int launch_decode_q9(const StepParams &p, int st, double *out, long long n, cudaStream_t s);
 int launch_decode_q19(const StepParams &p, int st, double *out, long long n, cudaStream_t s);
+int launch_encode_q9(const StepParams &p, int st, const double *in, long long n, cudaStream_t s);
+int launch_encode_q19(const StepParams &p, int st, const double *in, long long n, cudaStream_t s);
 int launch_norms(const uint32_t *word, const float *rho, const float *ux, const float *uy,
                  const float *uz, float *pux, float *puy, float *puz, long long n,
                  double *partial, double *out, cudaStream_t s);
@@ -39,6 +41,10 @@ int launch_momentum_exchange_q9(const StepParams &p, int st, const int *box, dou
 int launch_momentum_exchange_q19(const StepParams &p, int st, const int *box, double *partial, double *out,
                                  cudaStream_t s);
 long long resid_l2_partials_q19(const StepParams &p);
+int launch_fd_rel_q9(const StepParams &p, int st, int phys, float *fprev, float *ffirst, int first,
+                     double *partial, double *out, cudaStream_t s);
+int launch_fd_rel_q19(const StepParams &p, int st, int phys, float *fprev, float *ffirst, int first,
+                      double *partial, double *out, cudaStream_t s);
 int launch_macro_diff(const float *ux, const float *uy, const float *uz, const float *rho, float *pux, float *puy,
                       float *puz, float *prho, long long n, double *partial, double *out, cudaStream_t s);
 int tma_prepare(int q, int coll, int st, size_t smem, int *blocks_per_sm);
@@ -77,6 +83,8 @@ struct lbm_handle_s {
     float *rho = nullptr, *ux = nullptr, *uy = nullptr, *uz = nullptr;
     float *pux = nullptr, *puy = nullptr, *puz = nullptr;
     float *mdiff_prev = nullptr;  // u, v, w, rho at the last lbm_macro_diff (4 N floats)
+    float *fd_snap = nullptr;     // FdRelDiff: f_prev, f_first (2 Q N floats, allocated on first use)
+    bool fd_recorded = false;
     double *partial = nullptr, *norms = nullptr;
     int nslots = 0;
     std::vector<long long> slot_node;
@@ -151,7 +159,7 @@ static void free_handle(lbm_handle_s *H) {
         if (H->pair[c]) cudaGraphExecDestroy(H->pair[c]);
     void *ptrs[] = {H->fbuf[0], H->fbuf[1], H->word, H->slot, H->mask, H->kind, H->uvw,
                     H->rho, H->ux, H->uy, H->uz, H->pux, H->puy, H->puz, H->partial, H->norms,
-                    H->tma_row, H->tma_lmask, H->tma_omask, H->tma_err, H->mdiff_prev};
+                    H->tma_row, H->tma_lmask, H->tma_omask, H->tma_err, H->mdiff_prev, H->fd_snap};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (H->stepped) cudaEventDestroy(H->stepped);
@@ -508,6 +516,7 @@ int lbm_init(lbm_handle H, const float *rho, const float *u, const float *v, con
     CUDA_TRY(cudaMemsetAsync(H->pux, 0, sizeof(float) * H->N, H->stream));
     CUDA_TRY(cudaMemsetAsync(H->puy, 0, sizeof(float) * H->N, H->stream));
     CUDA_TRY(cudaMemsetAsync(H->puz, 0, sizeof(float) * H->N, H->stream));
+    H->fd_recorded = false;
     // MaxMacroDiff compares against the initial fields first (Iterate3D.cu:208-213)
     const size_t fb = sizeof(float) * (size_t)H->N;
     CUDA_TRY(cudaMemcpyAsync(H->mdiff_prev, H->ux, fb, cudaMemcpyDeviceToDevice, H->stream));
@@ -644,6 +653,34 @@ int lbm_get_populations(lbm_handle H, double *f) {
     return LBM_OK;
 }
 
+int lbm_set_populations(lbm_handle H, const double *f) {
+    if (!H || !f) return fail(LBM_ERR_INVALID, "null argument");
+    CUDA_TRY(cudaStreamWaitEvent(H->stream, H->stepped, 0));
+    const size_t bytes = sizeof(double) * (size_t)H->q * H->N;
+    double *tmp = nullptr;
+    CUDA_TRY(cudaMallocAsync((void **)&tmp, bytes, H->stream));
+    cudaError_t e = cudaMemcpyAsync(tmp, f, bytes, cudaMemcpyHostToDevice, H->stream);
+    const StepParams p = make_params(H, H->cur, 0);
+    if (e == cudaSuccess) {
+        if (H->q == 9)
+            launch_encode_q9(p, H->P.storage, tmp, H->N, H->stream);
+        else
+            launch_encode_q19(p, H->P.storage, tmp, H->N, H->stream);
+        e = cudaGetLastError();
+    }
+    const size_t fb = sizeof(float) * (size_t)H->N;
+    if (e == cudaSuccess) e = cudaMemsetAsync(H->pux, 0, fb, H->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(H->puy, 0, fb, H->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(H->puz, 0, fb, H->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(H->mdiff_prev, 0, 4 * fb, H->stream);
+    cudaFreeAsync(tmp, H->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("set_populations: ") + cudaGetErrorString(e));
+    H->initialised = true;
+    H->fd_recorded = false;
+    return LBM_OK;
+}
+
 int lbm_macro_norms(lbm_handle H, double *out) {
     if (!H || !out) return fail(LBM_ERR_INVALID, "null argument");
     CUDA_TRY(cudaStreamWaitEvent(H->stream, H->stepped, 0));
@@ -679,6 +716,39 @@ int lbm_residual_l2(lbm_handle H, double *out) {
     if (e != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("L2 residual: ") + cudaGetErrorString(e));
     *out = sqrt(s);
     if (!(*out == *out)) {
+        H->status = LBM_DIVERGED;
+        return fail(LBM_DIVERGED, "non-finite populations (divergence)");
+    }
+    return LBM_OK;
+}
+
+int lbm_residual_fd_rel_diff(lbm_handle H, double *out) {
+    if (!H || !out) return fail(LBM_ERR_INVALID, "null argument");
+    if (!H->initialised) return fail(LBM_ERR_INVALID, "lbm_init has not been called");
+    const size_t qn = (size_t)H->q * H->N;
+    if (!H->fd_snap) CUDA_TRY(cudaMalloc((void **)&H->fd_snap, sizeof(float) * 2 * qn));
+    CUDA_TRY(cudaStreamWaitEvent(H->stream, H->stepped, 0));
+    const StepParams p = make_params(H, H->cur, 0);
+    const long long nb = H->q == 9 ? resid_l2_partials_q9(p) : resid_l2_partials_q19(p);
+    double *partial = nullptr;
+    CUDA_TRY(cudaMallocAsync((void **)&partial, sizeof(double) * (2 * nb + 2), H->stream));
+    const int first = H->fd_recorded ? 0 : 1;
+    const int phys = H->P.mode == LBM_MODE_PHYSICS;
+    if (H->q == 9)
+        launch_fd_rel_q9(p, H->P.storage, phys, H->fd_snap, H->fd_snap + qn, first, partial, partial + 2 * nb,
+                         H->stream);
+    else
+        launch_fd_rel_q19(p, H->P.storage, phys, H->fd_snap, H->fd_snap + qn, first, partial, partial + 2 * nb,
+                          H->stream);
+    cudaError_t e = cudaGetLastError();
+    double r[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r, partial + 2 * nb, sizeof(r), cudaMemcpyDeviceToHost, H->stream);
+    cudaFreeAsync(partial, H->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("FdRelDiff residual: ") + cudaGetErrorString(e));
+    H->fd_recorded = true;
+    *out = first ? 0.0 : r[0];
+    if (r[1] > 0) {
         H->status = LBM_DIVERGED;
         return fail(LBM_DIVERGED, "non-finite populations (divergence)");
     }

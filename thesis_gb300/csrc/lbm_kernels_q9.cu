@@ -78,9 +78,30 @@ int launch_momentum_exchange_q9(const StepParams &p, int st, const int *box, dou
     return 0;
 }
 
+int launch_fd_rel_q9(const StepParams &p, int st, int phys, float *fprev, float *ffirst, int first,
+                      double *partial, double *out, cudaStream_t s) {
+    const dim3 grid = node_grid(p);
+    const long long nb = (long long)grid.x * grid.y * grid.z;
+#define F_CASE(S, P)                                                                                   \
+    if (st == S && (phys != 0) == P)                                                                   \
+        fd_rel_kernel<9, S, P><<<grid, STEP_BLOCK, 0, s>>>(p, fprev, ffirst, first, partial, nb);
+    F_CASE(0, false) F_CASE(1, false) F_CASE(2, false) F_CASE(0, true) F_CASE(1, true) F_CASE(2, true)
+#undef F_CASE
+    max_partials_kernel<<<1, 1024, 0, s>>>(partial, nb, out);
+    return 0;
+}
+
 long long resid_l2_partials_q9(const StepParams &p) {
     const dim3 g = node_grid(p);
     return (long long)g.x * g.y * g.z;
+}
+
+int launch_encode_q9(const StepParams &p, int st, const double *in, long long n, cudaStream_t s) {
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    if (st == LBM_STORE_F32) encode_kernel<9, LBM_STORE_F32><<<blocks, 256, 0, s>>>(p, in, n);
+    else if (st == LBM_STORE_F16S) encode_kernel<9, LBM_STORE_F16S><<<blocks, 256, 0, s>>>(p, in, n);
+    else encode_kernel<9, LBM_STORE_F64><<<blocks, 256, 0, s>>>(p, in, n);
+    return 0;
 }
 
 int launch_decode_q9(const StepParams &p, int st, double *out, long long n, cudaStream_t s) {

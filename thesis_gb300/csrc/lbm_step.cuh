@@ -431,6 +431,96 @@ __global__ void __launch_bounds__(STEP_BLOCK) momentum_exchange_kernel(const Ste
     }
 }
 
+// The reference's FdRelDiff residual (gpu_NewResidual, ComputeResiduals.cu:
+// 56-64): per population of a fluid node, |f - f_prev| / |f_first|, f the
+// post-stream, post-boundary field the next step pulls (as for the L2
+// residual), f_prev and f_first snapshots in the reference's SoA order
+// (d * N + node).  first = 1 records f in both snapshots.  Per block: the
+// maximum (entries with f_first = 0 skipped) and the count of non-finite
+// values, stored at partial[b] and partial[nb + b].
+template <int Q, int ST, bool PHYS>
+__global__ void __launch_bounds__(STEP_BLOCK) fd_rel_kernel(const StepParams p, float *fprev, float *ffirst,
+                                                            int first, double *partial, long long nb) {
+    using S = Store<ST>;
+    using T = typename S::T;
+    using R = typename S::R;
+    const DynGeom g{p.nx, p.ny, p.nz, p.pitch};
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    const long long N = (long long)g.nx * g.ny * g.nz;
+    double mx = 0.0, bad = 0.0;
+    if (x < g.nx) {
+        const int row = y + g.ny * z;
+        const int node = x + g.nx * row;
+        const uint32_t w = __ldg(p.word + node);
+        if (w & W_FLUID) {
+            const T *in = (const T *)p.fin[0] + (x + (long long)g.pitch * row);
+            R f[Q];
+            gather_node<Q, ST, PHYS, true, DynGeom, 0, false>(p, g, x, y, z, w, in, f);
+            bool keep, zv;
+            apply_bc<Q, ST, PHYS, true, DynGeom>(f, w, node, p, g, keep, zv);
+#pragma unroll
+            for (int d = 0; d < Q; ++d) {
+                const long long i = d * N + node;
+                const float fv = (float)f[d];
+                if (first) {
+                    ffirst[i] = fv;
+                } else {
+                    const double den = fabs((double)ffirst[i]);
+                    const double rel = fabs((double)fv - (double)fprev[i]) / den;
+                    if (!isfinite((double)fv)) bad += 1.0;
+                    else if (den > 0.0 && rel > mx) mx = rel;
+                }
+                fprev[i] = fv;
+            }
+        }
+    }
+    __shared__ double sm[2][STEP_BLOCK / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        bad += __shfl_down_sync(0xffffffffu, bad, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sm[0][threadIdx.x >> 5] = mx;
+        sm[1][threadIdx.x >> 5] = bad;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0, b = 0.0;
+        for (int k = 0; k < STEP_BLOCK / 32; ++k) {
+            m = fmax(m, sm[0][k]);
+            b += sm[1][k];
+        }
+        const size_t blk = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * (size_t)blockIdx.z);
+        partial[blk] = m;
+        partial[nb + blk] = b;
+    }
+}
+
+// Maximum of n partials into out[0], sum of the next n into out[1].
+static __global__ void __launch_bounds__(1024) max_partials_kernel(const double *partial, long long n, double *out) {
+    __shared__ double sm[2][1024];
+    double m = 0.0, b = 0.0;
+    for (long long i = threadIdx.x; i < n; i += 1024) {
+        m = fmax(m, partial[i]);
+        b += partial[n + i];
+    }
+    sm[0][threadIdx.x] = m;
+    sm[1][threadIdx.x] = b;
+    __syncthreads();
+    for (int s = 512; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            sm[0][threadIdx.x] = fmax(sm[0][threadIdx.x], sm[0][threadIdx.x + s]);
+            sm[1][threadIdx.x] += sm[1][threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = sm[0][0];
+        out[1] = sm[1][0];
+    }
+}
+
 // Deterministic sum of n partials (one block of 1024 threads, fixed order).
 static __global__ void __launch_bounds__(1024) sum_partials_kernel(const double *partial, long long n, double *out) {
     __shared__ double sm[1024];
@@ -502,6 +592,20 @@ __global__ void decode_kernel(const StepParams p, double *out, long long n) {
 #pragma unroll
     for (int d = 0; d < Q; ++d)
         out[d * n + i] = (double)S::load((const T *)p.fin[d] + idx, p.shift[d], p.inv_scale);
+}
+
+// The inverse of decode_kernel: a population field in the reference's SoA
+// order, in[d*n + node], encoded into the buffer the next step reads.
+template <int Q, int ST>
+__global__ void encode_kernel(const StepParams p, const double *in, long long n) {
+    using S = Store<ST>;
+    using T = typename S::T;
+    using R = typename S::R;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long long idx = i % p.nx + (long long)p.pitch * (i / p.nx);
+#pragma unroll
+    for (int d = 0; d < Q; ++d) S::store((T *)p.fin[d] + idx, (R)in[d * n + i], p.shift[d], p.scale);
 }
 
 }  // namespace lbm

@@ -97,6 +97,7 @@ def lib():
         "lbm_step": (C.c_int, [vp, C.c_int, C.c_int, vp]),
         "lbm_get_macro": (C.c_int, [vp, fp, fp, fp, fp]),
         "lbm_get_populations": (C.c_int, [vp, dp]),
+        "lbm_set_populations": (C.c_int, [vp, dp]),
         "lbm_macro_norms": (C.c_int, [vp, dp]),
         "lbm_status": (C.c_int, [vp]),
         "lbm_fluid_nodes": (C.c_longlong, [vp]),
@@ -111,6 +112,7 @@ def lib():
                                       C.POINTER(C.c_int32), C.POINTER(C.c_int)]),
         "lbm_macro_diff": (C.c_int, [vp, dp]),
         "lbm_residual_l2": (C.c_int, [vp, dp]),
+        "lbm_residual_fd_rel_diff": (C.c_int, [vp, dp]),
         "lbm_momentum_exchange": (C.c_int, [vp, _IP, dp]),
         "lbm_read_init_file": (C.c_int, [C.c_char_p, C.POINTER(RunConfig)]),
         "lbm_count_lines": (C.c_longlong, [C.c_char_p]),

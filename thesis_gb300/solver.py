@@ -188,6 +188,17 @@ class Solver:
                                                 out.ctypes.data_as(C.POINTER(C.c_double))))
         return out
 
+    def set_populations(self, f):
+        """Restart from a population field in the populations() layout."""
+        f = np.ascontiguousarray(f, np.float64).reshape(-1)
+        N.check(self._lib.lbm_set_populations(self._h, f.ctypes.data_as(C.POINTER(C.c_double))))
+
+    def residual_fd_rel_diff(self):
+        """The reference's FdRelDiff residual (first call after init: 0)."""
+        out = C.c_double()
+        N.check(self._lib.lbm_residual_fd_rel_diff(self._h, C.byref(out)))
+        return out.value
+
     def residual_l2(self):
         """The reference's L2 residual sqrt(sum (f - fColl)^2) of the current
         state, and the status code."""
