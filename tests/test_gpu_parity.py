@@ -361,7 +361,7 @@ def test_population_checkpoint_restart(storage):
         f_rst = s.populations()
         m_rst = s.macro()
     if storage == N.STORE_F16S:
-        assert np.abs(f_rst - f_run).max() < 1e-6
+        assert np.abs(f_rst - f_run).max() < 1e-5
     else:
         np.testing.assert_array_equal(f_rst, f_run)
         for a, b in zip(m_rst, m_run):
