@@ -656,6 +656,13 @@ int lbm_get_populations(lbm_handle H, double *f) {
 int lbm_set_populations(lbm_handle H, const double *f) {
     if (!H || !f) return fail(LBM_ERR_INVALID, "null argument");
     CUDA_TRY(cudaStreamWaitEvent(H->stream, H->stepped, 0));
+    // macroscopic fields as lbm_init leaves them (the params' constants);
+    // the fluid nodes' values are rewritten by the next step that stores them
+    int rc;
+    if ((rc = upload_or_fill(H->rho, nullptr, (float)H->P.rho, H->N, H->stream))) return rc;
+    if ((rc = upload_or_fill(H->ux, nullptr, (float)H->P.u, H->N, H->stream))) return rc;
+    if ((rc = upload_or_fill(H->uy, nullptr, (float)H->P.v, H->N, H->stream))) return rc;
+    if ((rc = upload_or_fill(H->uz, nullptr, H->dims == 3 ? (float)H->P.w : 0.0f, H->N, H->stream))) return rc;
     const size_t bytes = sizeof(double) * (size_t)H->q * H->N;
     double *tmp = nullptr;
     CUDA_TRY(cudaMallocAsync((void **)&tmp, bytes, H->stream));

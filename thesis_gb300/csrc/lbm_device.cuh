@@ -163,6 +163,10 @@ template <> struct Store<LBM_STORE_F32> {
     __device__ static __forceinline__ R decode(T v, float w, float) { return v + w; }
     __device__ static __forceinline__ void store(T *p, R v, float w, float) { *p = v - w; }
     __device__ static __forceinline__ T encode(R v, float w, float) { return v - w; }
+    // read-back and restart in FP64: f = v + w is exact in double, so a
+    // decode64 / encode64 round trip returns the stored value
+    __device__ static __forceinline__ double decode64(T v, float w, float) { return (double)v + (double)w; }
+    __device__ static __forceinline__ T encode64(double v, float w, float) { return (float)(v - (double)w); }
 };
 template <> struct Store<LBM_STORE_F16S> {
     using T = __half;
@@ -179,6 +183,12 @@ template <> struct Store<LBM_STORE_F16S> {
     __device__ static __forceinline__ void store(T *p, R v, float w, float scale) {
         *p = encode(v, w, scale);
     }
+    __device__ static __forceinline__ double decode64(T v, float w, float inv_scale) {
+        return (double)__half2float(v) * (double)inv_scale + (double)w;
+    }
+    __device__ static __forceinline__ T encode64(double v, float w, float scale) {
+        return __float2half_rn((float)((v - (double)w) * (double)scale));
+    }
 };
 template <> struct Store<LBM_STORE_F64> {
     using T = double;
@@ -187,6 +197,8 @@ template <> struct Store<LBM_STORE_F64> {
     __device__ static __forceinline__ R decode(T v, float, float) { return v; }
     __device__ static __forceinline__ void store(T *p, R v, float, float) { *p = v; }
     __device__ static __forceinline__ T encode(R v, float, float) { return v; }
+    __device__ static __forceinline__ double decode64(T v, float, float) { return v; }
+    __device__ static __forceinline__ T encode64(double v, float, float) { return v; }
 };
 
 // ---------------------------------------------------------------------------

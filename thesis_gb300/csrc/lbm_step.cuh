@@ -591,7 +591,7 @@ __global__ void decode_kernel(const StepParams p, double *out, long long n) {
     const long long idx = i % p.nx + (long long)p.pitch * (i / p.nx);
 #pragma unroll
     for (int d = 0; d < Q; ++d)
-        out[d * n + i] = (double)S::load((const T *)p.fin[d] + idx, p.shift[d], p.inv_scale);
+        out[d * n + i] = S::decode64(((const T *)p.fin[d])[idx], p.shift[d], p.inv_scale);
 }
 
 // The inverse of decode_kernel: a population field in the reference's SoA
@@ -600,12 +600,11 @@ template <int Q, int ST>
 __global__ void encode_kernel(const StepParams p, const double *in, long long n) {
     using S = Store<ST>;
     using T = typename S::T;
-    using R = typename S::R;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const long long idx = i % p.nx + (long long)p.pitch * (i / p.nx);
 #pragma unroll
-    for (int d = 0; d < Q; ++d) S::store((T *)p.fin[d] + idx, (R)in[d * n + i], p.shift[d], p.scale);
+    for (int d = 0; d < Q; ++d) ((T *)p.fin[d])[idx] = S::encode64(in[d * n + i], p.shift[d], p.scale);
 }
 
 }  // namespace lbm
