@@ -145,14 +145,26 @@ int lbm_get_macro(lbm_handle h, float *rho, float *u, float *v, float *w);
  * SoA f[d*n*m*h + node] in the reference's direction order. */
 int lbm_get_populations(lbm_handle h, double *f);
 
-/* Population checkpoint restart: replace the state with f (the layout
- * lbm_get_populations returns), so a run saved with lbm_get_populations and
- * resumed here on a handle of the same lattice and parameters continues as
- * if uninterrupted (exactly for F32 and F64 storage).  Takes the place of
- * lbm_init; the residual snapshots (norms, MaxMacroDiff, FdRelDiff) start
- * again from zero fields.  The reference restarts from macroscopic fields
- * only (FilesReading.cu:224-268); this is the population-level counterpart. */
+/* Restart from a population field: replace the state with f (the layout
+ * lbm_get_populations returns), encoded into the handle's storage.  Takes
+ * the place of lbm_init; the residual snapshots (norms, MaxMacroDiff,
+ * FdRelDiff) start again from zero fields.  A field read back by
+ * lbm_get_populations is restored exactly except where a shifted storage's
+ * deviation f - shift is below ~1e-16 of the shift (FP64 cannot hold
+ * shift + deviation there); lbm_get_state / lbm_set_state are the exact
+ * checkpoint.  The reference restarts from macroscopic fields only
+ * (FilesReading.cu:224-268); these are the population-level counterparts. */
 int lbm_set_populations(lbm_handle h, const double *f);
+
+/* Exact checkpoint: the stored populations as they are held (F32, F64, or
+ * F16S half deviations; lbm_state_bytes(h) bytes, SoA order state[d N +
+ * node] of the storage element type).  A state saved by lbm_get_state and
+ * loaded by lbm_set_state into a handle of the same lattice and parameters
+ * continues bit for bit as the uninterrupted run; lbm_set_state takes the
+ * place of lbm_init as lbm_set_populations does. */
+long long lbm_state_bytes(lbm_handle h);
+int lbm_get_state(lbm_handle h, void *state);
+int lbm_set_state(lbm_handle h, const void *state);
 
 /* FP64 norms over fluid nodes of the last stored macroscopic fields:
  * out[0] = sum |u - u_prev|^2, out[1] = sum |u|^2, out[2] = sum rho,

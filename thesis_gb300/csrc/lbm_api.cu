@@ -688,6 +688,54 @@ int lbm_set_populations(lbm_handle H, const double *f) {
     return LBM_OK;
 }
 
+// Raw storage state in the reference's SoA order: one 2D copy per direction
+// between the row layout (direction d of row r at (r Q + d) n) and
+// state[d N + node].
+long long lbm_state_bytes(lbm_handle H) { return H ? (long long)H->q * H->N * (long long)H->elem : -1; }
+
+static int state_copy(lbm_handle H, void *host, bool to_host) {
+    CUDA_TRY(cudaStreamWaitEvent(H->stream, H->stepped, 0));
+    const size_t e = H->elem, n = (size_t)H->n, rows = (size_t)H->m * H->h;
+    char *dev = (char *)H->fbuf[H->cur];
+    cudaError_t err = cudaSuccess;
+    for (int d = 0; d < H->q && err == cudaSuccess; ++d) {
+        char *h = (char *)host + (size_t)d * H->N * e;
+        char *g = dev + (size_t)d * n * e;
+        err = to_host ? cudaMemcpy2DAsync(h, n * e, g, (size_t)H->q * n * e, n * e, rows, cudaMemcpyDeviceToHost,
+                                          H->stream)
+                      : cudaMemcpy2DAsync(g, (size_t)H->q * n * e, h, n * e, n * e, rows, cudaMemcpyHostToDevice,
+                                          H->stream);
+    }
+    if (err == cudaSuccess) err = cudaStreamSynchronize(H->stream);
+    if (err != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("state copy: ") + cudaGetErrorString(err));
+    return LBM_OK;
+}
+
+int lbm_get_state(lbm_handle H, void *state) {
+    if (!H || !state) return fail(LBM_ERR_INVALID, "null argument");
+    if (!H->initialised) return fail(LBM_ERR_INVALID, "lbm_init has not been called");
+    return state_copy(H, state, true);
+}
+
+int lbm_set_state(lbm_handle H, const void *state) {
+    if (!H || !state) return fail(LBM_ERR_INVALID, "null argument");
+    int rc;
+    if ((rc = upload_or_fill(H->rho, nullptr, (float)H->P.rho, H->N, H->stream))) return rc;
+    if ((rc = upload_or_fill(H->ux, nullptr, (float)H->P.u, H->N, H->stream))) return rc;
+    if ((rc = upload_or_fill(H->uy, nullptr, (float)H->P.v, H->N, H->stream))) return rc;
+    if ((rc = upload_or_fill(H->uz, nullptr, H->dims == 3 ? (float)H->P.w : 0.0f, H->N, H->stream))) return rc;
+    if ((rc = state_copy(H, const_cast<void *>(state), false))) return rc;
+    const size_t fb = sizeof(float) * (size_t)H->N;
+    CUDA_TRY(cudaMemsetAsync(H->pux, 0, fb, H->stream));
+    CUDA_TRY(cudaMemsetAsync(H->puy, 0, fb, H->stream));
+    CUDA_TRY(cudaMemsetAsync(H->puz, 0, fb, H->stream));
+    CUDA_TRY(cudaMemsetAsync(H->mdiff_prev, 0, 4 * fb, H->stream));
+    CUDA_TRY(cudaStreamSynchronize(H->stream));
+    H->initialised = true;
+    H->fd_recorded = false;
+    return LBM_OK;
+}
+
 int lbm_macro_norms(lbm_handle H, double *out) {
     if (!H || !out) return fail(LBM_ERR_INVALID, "null argument");
     CUDA_TRY(cudaStreamWaitEvent(H->stream, H->stepped, 0));

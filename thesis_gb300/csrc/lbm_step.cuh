@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(STEP_BLOCK) momentum_exchange_kernel(const Ste
                 if (sx < lo.x || sx > hi.x || sy < lo.y || sy > hi.y || sz < lo.z || sz > hi.z) continue;
                 if (sx < 0 || sx >= p.nx || sy < 0 || sy >= p.ny || sz < 0 || sz >= p.nz) continue;
                 const int o = L::opp(d);
-                const double fo = (double)S::decode(in[o * p.nx], p.shift[o], p.inv_scale);
+                const double fo = S::decode64(in[o * p.nx], p.shift[o], p.inv_scale);
                 F[0] += 2.0 * L::cx(o) * fo;
                 F[1] += 2.0 * L::cy(o) * fo;
                 F[2] += 2.0 * L::cz(o) * fo;

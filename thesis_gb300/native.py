@@ -98,6 +98,9 @@ def lib():
         "lbm_get_macro": (C.c_int, [vp, fp, fp, fp, fp]),
         "lbm_get_populations": (C.c_int, [vp, dp]),
         "lbm_set_populations": (C.c_int, [vp, dp]),
+        "lbm_state_bytes": (C.c_longlong, [vp]),
+        "lbm_get_state": (C.c_int, [vp, vp]),
+        "lbm_set_state": (C.c_int, [vp, vp]),
         "lbm_macro_norms": (C.c_int, [vp, dp]),
         "lbm_status": (C.c_int, [vp]),
         "lbm_fluid_nodes": (C.c_longlong, [vp]),

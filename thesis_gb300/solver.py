@@ -193,6 +193,17 @@ class Solver:
         f = np.ascontiguousarray(f, np.float64).reshape(-1)
         N.check(self._lib.lbm_set_populations(self._h, f.ctypes.data_as(C.POINTER(C.c_double))))
 
+    def get_state(self):
+        """Exact checkpoint: the stored populations as raw bytes."""
+        buf = np.empty(int(self._lib.lbm_state_bytes(self._h)), np.uint8)
+        N.check(self._lib.lbm_get_state(self._h, buf.ctypes.data_as(C.c_void_p)))
+        return buf
+
+    def set_state(self, buf):
+        buf = np.ascontiguousarray(buf, np.uint8)
+        assert buf.size == int(self._lib.lbm_state_bytes(self._h))
+        N.check(self._lib.lbm_set_state(self._h, buf.ctypes.data_as(C.c_void_p)))
+
     def residual_fd_rel_diff(self):
         """The reference's FdRelDiff residual (first call after init: 0)."""
         out = C.c_double()
