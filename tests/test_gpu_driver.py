@@ -31,7 +31,7 @@ MinMacroDiffs(u_v_w_rho)(StopCond) = {stop}
 OutputFormat = {fmt}
 InitialConditionFromFile = {ic}
 InitialFile = "{icfile}"
-ResidualModel = MaxMacroDiff
+ResidualModel = {resmodel}
 ResidualsAndMacroDiffsAfter = 100
 Force = 0
 DragAndLift = 0
@@ -42,7 +42,7 @@ UpdateInltOutl = yes
 def _setup(tmp_path, lat, **kw):
     (tmp_path / "Mesh").mkdir(exist_ok=True)
     lattice.write_files(lat, str(tmp_path / "Mesh" / "cav_Node.dat"), str(tmp_path / "Mesh" / "cav_BC.dat"))
-    d = dict(coll="SRT", iters=400, stop="0 0 0 0", fmt="CSV", ic="no", icfile="none")
+    d = dict(coll="SRT", iters=400, stop="0 0 0 0", fmt="CSV", ic="no", icfile="none", resmodel="MaxMacroDiff")
     d.update(kw)
     (tmp_path / "SetUpData.ini").write_text(INIT.format(**d))
 
@@ -105,9 +105,42 @@ def test_driver_stop_condition_and_restart(tmp_path):
     assert len(md2) < len(md)
 
 
+def test_driver_fd_rel_diff_residual_model(tmp_path):
+    """ResidualModel MaxRelativeFdDiff: the residual is written every 100
+    steps to Residuals.txt, decreases as the cavity settles, and the run stops
+    once it is below StopCondition[0]."""
+    lat = lattice.cavity2d(24)
+    _setup(tmp_path, lat, iters=200000, stop="1e-5 0 0 0", coll="MRT", resmodel="MaxRelativeFdDiff")
+    r = _run(tmp_path, "--physics")
+    assert r.returncode == 0 and "converged" in r.stdout, r.stderr
+    lines = (tmp_path / "Results" / "Residuals.txt").read_text().splitlines()
+    assert lines[0] == "iteration\tMaxRelativeFdDiff"
+    res = np.array([float(x.split()[1]) for x in lines[1:]])
+    assert res[-1] < 1e-5 and res[0] > res[-1] and len(res) < 2000
+
+
+def test_driver_l2_residual_model(tmp_path):
+    """ResidualModel L2: sqrt(sum (f - fColl)^2) every 100 steps in
+    Residuals.txt, equal to the API's value at the end of the same run (it
+    settles at the size of the steady streaming step, not at zero)."""
+    lat = lattice.cavity2d(24)
+    _setup(tmp_path, lat, iters=1000, stop="0 0 0 0", coll="MRT", resmodel="L2")
+    r = _run(tmp_path, "--physics")
+    assert r.returncode == 0, r.stderr
+    lines = (tmp_path / "Results" / "Residuals.txt").read_text().splitlines()
+    assert lines[0] == "iteration\tL2" and len(lines) == 11
+    f32 = lambda v: float(np.float32(v))
+    args = Arguments(u=f32(0.1), viscosity=f32(0.128), collision_model=N.MRT, mode=N.MODE_PHYSICS, init_equilibrium=1)
+    with Solver(lat, args) as s:
+        s.init()
+        s.step(1000, write_macro=True)
+        want, rc = s.residual_l2()
+    assert abs(float(lines[-1].split()[1]) - want) <= 1e-9 * want
+
+
 def test_driver_missing_lattice(tmp_path):
     (tmp_path / "SetUpData.ini").write_text(INIT.format(coll="SRT", iters=10, stop="0 0 0 0", fmt="CSV", ic="no",
-                                                        icfile="x"))
+                                                        icfile="x", resmodel="MaxMacroDiff"))
     assert _run(tmp_path).returncode == 2
 
 

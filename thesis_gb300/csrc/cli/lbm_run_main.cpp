@@ -205,6 +205,15 @@ int main(int argc, char **argv) {
     FILE *md = fopen((out + "MacroDiffs.txt").c_str(), "w");
     if (md) fprintf(md, "iteration\tMax u diff\tMax v diff\tMax w diff\tMax rho diff\n");
 
+    FILE *resf = nullptr;
+    if (cfg.residual_model == LBM_RES_L2 || cfg.residual_model == LBM_RES_FD_REL_DIFF) {
+        resf = fopen((out + "Residuals.txt").c_str(), "w");
+        if (resf) fprintf(resf, "iteration\t%s\n", cfg.residual_model == LBM_RES_L2 ? "L2" : "MaxRelativeFdDiff");
+        // FdRelDiff measures against the populations at the start (f_prev and
+        // f_first both taken here; the reference takes f_first at its first check)
+        double r0;
+        if (cfg.residual_model == LBM_RES_FD_REL_DIFF) lbm_residual_fd_rel_diff(hd, &r0);
+    }
     const int every = cfg.show_macro_diff > 0 ? cfg.show_macro_diff : cfg.iterations;
     int status = 0, autosave_it = 1;
     for (int iter = 0; iter < cfg.iterations;) {
@@ -234,6 +243,22 @@ int main(int argc, char **argv) {
                 printf("simulation converged!\n");
                 break;
             }
+            // L2 and MaxRelativeFdDiff stop on |r| < StopCondition[0] (Iterate3D.cu:758-765)
+            if (cfg.residual_model == LBM_RES_L2 || cfg.residual_model == LBM_RES_FD_REL_DIFF) {
+                double res = 0.0;
+                const int rr = cfg.residual_model == LBM_RES_L2 ? lbm_residual_l2(hd, &res)
+                                                                : lbm_residual_fd_rel_diff(hd, &res);
+                if (rr == LBM_DIVERGED) {
+                    fprintf(stderr, "\nDIVERGENCE!\n");
+                    status = 1;
+                    break;
+                }
+                if (resf) fprintf(resf, "%d\t%.10e\n", iter, res);
+                if (fabs(res) < cfg.stop_condition[0]) {
+                    printf("simulation converged!\n");
+                    break;
+                }
+            }
         }
         if (cfg.autosave_every > 0 && iter == cfg.autosave_every * autosave_it) {
             ++autosave_it;
@@ -241,6 +266,7 @@ int main(int argc, char **argv) {
         }
     }
     if (md) fclose(md);
+    if (resf) fclose(resf);
     if (status != 3) write(out + "FinalData." + ext);
     lbm_destroy(hd);
     return status;
