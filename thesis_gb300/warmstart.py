@@ -263,13 +263,20 @@ def compare(unet, seeds, n=256, m=64, tol=TOL, check_every=100, max_steps=400_00
     init = [fields(l, p) for l, p in zip(lats, pred)]
     cold = solve_batch(lats, res, None, tol, check_every, max_steps)
     warm = solve_batch(lats, res, init, tol, check_every, max_steps)
+    # channels whose warm run missed the tolerance fall back to the cold start
+    miss = [d for d in range(len(lats)) if not warm[1][d] <= tol]
+    t_fallback = 0.0
+    if miss:
+        fb = solve_batch([lats[d] for d in miss], [res[d] for d in miss], None, tol, check_every, max_steps)
+        t_fallback = fb[5]
     du = []
     for d, lat in enumerate(lats):
         fl = lat.node_type == 1
         du.append(float(np.abs(warm[4][d][1] - cold[4][d][1])[fl].max() / UMAX))
     return dict(seeds=seeds, re=res, lats=lats, cold_steps=cold[0], warm_steps=warm[0], cold_res=cold[1],
                 warm_res=warm[1], cold_seconds=cold[3], warm_seconds=warm[3], predict_seconds=t_pred,
-                cold_total_seconds=cold[5], warm_total_seconds=warm[5] + t_pred,
+                cold_total_seconds=cold[5], warm_total_seconds=warm[5] + t_pred + t_fallback,
+                fallbacks=len(miss),
                 converged_du=np.array(du), pred=pred, init=init, cold_fields=cold[4], warm_fields=warm[4])
 
 
