@@ -896,8 +896,10 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
         vs.insert(vs.end(), fv, fv + 7);
     }
     if (hs_ok) {
-        const V hv[] = {{128, 0, 0, 0, 1, 1}, {128, 0, 0, 0, 10, 1}, {256, 0, 0, 0, 1, 1}, {256, 0, 0, 0, 5, 1}};
-        vs.insert(vs.end(), hv, hv + 4);
+        // register caps of about 64, 48, 40 and 32 per thread
+        const V hv[] = {{128, 0, 0, 0, 1, 1}, {128, 0, 0, 0, 10, 1}, {128, 0, 0, 0, 12, 1}, {128, 0, 0, 0, 14, 1},
+                        {256, 0, 0, 0, 1, 1}, {256, 0, 0, 0, 5, 1}, {256, 0, 0, 0, 6, 1}, {256, 0, 0, 0, 7, 1}};
+        vs.insert(vs.end(), hv, hv + 8);
     }
     if (H->n % 2 == 0 && hs_ok) {
         const V pv[] = {{64, 0, 0, 1, 1, 0}, {128, 0, 0, 1, 1, 0}, {64, 0, 0, 1, 12, 0}, {128, 0, 0, 1, 6, 0}};
