@@ -70,7 +70,8 @@ def parse():
     ap.add_argument("--domains", type=int, default=512, help="cavities in the batch")
     ap.add_argument("--one-by-one-steps", type=int, default=20,
                     help="steps per cavity when the cavities run one launch per step each")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "jit", "jit2", "jith", "jitf", "tma", "pair", "scalar"],
+    ap.add_argument("--kernel", default="auto", choices=["auto", "jit", "jit2", "jith", "jiths", "jitf", "tma", "pair",
+                                                         "scalar"],
                     help="step kernel (auto: the library's default for the storage)")
     return ap.parse_args()
 
@@ -653,7 +654,8 @@ def main():
                 "config": dict(workload_config(args, n, m, h), kernel=kernel,
                                kernel_knobs={"block": knobs[0], "l2_256B_loads": knobs[1] & 1,
                                              "storage_unit_arithmetic": (knobs[1] >> 1) & 1,
-                                             "predicated_bounce_back": knobs[2] & 1,
+                                             "predicated_bounce_back": knobs[2] & 1 & ~(knobs[1] >> 1),
+                                             "speculative_loads": knobs[2] & 1 & (knobs[1] >> 1),
                                              "two_nodes_per_thread": (knobs[2] >> 1) & 1,
                                              "min_blocks_per_sm": knobs[2] >> 2}),
                 "fluid_nodes_per_gpu": fluid, "status": status,

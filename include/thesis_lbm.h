@@ -238,7 +238,9 @@ long long lbm_fluid_nodes(lbm_handle h);
 /* Step kernel of the handle, chosen at lbm_create: 4 (the default) the
  * one-node kernel specialised for this lattice's extents at run time (in
  * physics mode computing in storage units, deviations from the rest state;
- * THESIS_LBM_KERNEL=jith|jitf forces storage-unit or f-space), 1 the
+ * THESIS_LBM_KERNEL=jith|jitf forces storage-unit or f-space, jiths the
+ * storage-unit kernel that loads pull and bounce-back values before the flag
+ * word arrives), 1 the
  * compiled-in one-node kernel (used when the run-time build is unavailable),
  * 2 two nodes per thread (even n, F32/F16S), 3 the row-staged bulk-copy
  * kernel.  THESIS_LBM_KERNEL=scalar|pair|tma|jit|jit2 in the environment at

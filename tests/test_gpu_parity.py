@@ -125,7 +125,7 @@ def test_reference_hh_walls_and_periodic_copies(oracle, case, coll, storage):
     compare(g, r, fl, storage, 3)
 
 
-@pytest.mark.parametrize("variant", ["pair", "jith", "scalar", "jit2"])
+@pytest.mark.parametrize("variant", ["pair", "jith", "jiths", "scalar", "jit2"])
 def test_reference_periodic_hh_every_kernel_form(oracle, monkeypatch, variant):
     """Partner pulls and HH walls are shared by the one-node, storage-unit and
     two-node kernels."""

@@ -25,6 +25,9 @@ from thesis_gb300.solver import Arguments, Solver
     (19, N.MRT, N.STORE_F32, 0, 0, (64, 48, 40), (128, 0, 0)),
     (19, N.BGKW, N.STORE_F32, 0, 1, (64, 48, 40), (128, 2, 0)),
     (19, N.MRT, N.STORE_F32, 0, 0, (64, 48, 40), (64, 0, 2)),
+    # storage-unit kernel with speculative loads
+    (19, N.MRT, N.STORE_F16S, 1, 0, (256, 256, 512), (128, 2, 1 | (10 << 2))),
+    (9, N.TRT, N.STORE_F32, 1, 1, (160, 48, 1), (128, 2, 1)),
 ])
 def test_jit_sources_compile(native_lib, q, coll, storage, phys, wrap, dims, knobs):
     rc = native_lib.lbm_jit_check(q, coll, storage, phys, wrap, *dims, *knobs)
@@ -163,10 +166,11 @@ def test_jit_pair_reference_cavity(oracle, monkeypatch):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kernel", ["jith", "jitf"])
+@pytest.mark.parametrize("kernel", ["jith", "jiths", "jitf"])
 @pytest.mark.parametrize("storage", [N.STORE_F32, N.STORE_F16S])
 def test_storage_unit_and_f_space_kernels(oracle, monkeypatch, kernel, storage):
-    """Both one-node arithmetic forms against the oracle (physics mode)."""
+    """Both one-node arithmetic forms (and the storage-unit kernel with
+    speculative loads) against the oracle (physics mode)."""
     monkeypatch.setenv("THESIS_LBM_KERNEL", kernel)
     from test_gpu_parity import compare, run_pair
     lat = lattice.sphere_duct(24, 20, 48, porosity=0.75, rmin=3, rmax=5, seed=7)
@@ -174,7 +178,8 @@ def test_storage_unit_and_f_space_kernels(oracle, monkeypatch, kernel, storage):
                      init_equilibrium=1, inlet_profile=N.INLET_PRESSURE, outlet_profile=N.OUTLET_PRESSURE,
                      rho_in=1.005, rho_out=1.0)
     with Solver(lat, args) as s:
-        assert s.kernel_config()[1] >> 1 == (kernel == "jith")
+        assert s.kernel_config()[1] >> 1 == (kernel != "jitf")
+        assert s.kernel_config()[2] & 1 == (kernel == "jiths")
     g, r, fl = run_pair(oracle, lat, args, 40, init=_rest(lat.num_nodes))
     compare(g, r, fl, storage, 3)
 

@@ -297,6 +297,7 @@ static int setup_jit(lbm_handle_s *H, const std::vector<uint32_t> &word, bool pa
     // moments); reference mode keeps the f-space form of the reference
     k.hspace = !pair && (hspace > 0 || (hspace < 0 && H->P.mode == LBM_MODE_PHYSICS &&
                                         H->P.storage != LBM_STORE_F64));
+    k.pred = k.hspace && hspace == 2;
     {
         std::lock_guard<std::mutex> lock(g_tuned_mutex);
         auto it = g_tuned.find(tune_key(k));
@@ -402,10 +403,13 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
         H->pair_kernel = kv && strcmp(kv, "pair") == 0 && can_pair;
         want_tma = kv && strcmp(kv, "tma") == 0;
         want_jit = !kv || !*kv || strcmp(kv, "jit") == 0 || strcmp(kv, "jit2") == 0 || strcmp(kv, "jith") == 0 ||
-                   strcmp(kv, "jitf") == 0;
+                   strcmp(kv, "jiths") == 0 || strcmp(kv, "jitf") == 0;
         jit_required = kv && *kv && want_jit;
         jit_pair = kv && strcmp(kv, "jit2") == 0 && can_pair;
-        jit_hspace = kv && strcmp(kv, "jith") == 0 ? 1 : (kv && strcmp(kv, "jitf") == 0 ? 0 : -1);
+        jit_hspace = kv && strcmp(kv, "jith") == 0    ? 1
+                     : kv && strcmp(kv, "jiths") == 0 ? 2  // storage units, speculative loads
+                     : kv && strcmp(kv, "jitf") == 0  ? 0
+                                                      : -1;
     }
     H->nslots = (int)flags.slot_node.size();
     H->slot_node = flags.slot_node;
@@ -897,9 +901,12 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
     }
     if (hs_ok) {
         // register caps of about 64, 48, 40 and 32 per thread
-        const V hv[] = {{128, 0, 0, 0, 1, 1}, {128, 0, 0, 0, 10, 1}, {128, 0, 0, 0, 12, 1}, {128, 0, 0, 0, 14, 1},
-                        {256, 0, 0, 0, 1, 1}, {256, 0, 0, 0, 5, 1}, {256, 0, 0, 0, 6, 1}, {256, 0, 0, 0, 7, 1}};
-        vs.insert(vs.end(), hv, hv + 8);
+        // register caps of about 64, 48 and 40 per thread; pred = 1 loads the
+        // pull and own values before the flag word arrives
+        const V hv[] = {{128, 0, 0, 0, 1, 1},  {128, 0, 0, 0, 10, 1}, {128, 0, 0, 0, 12, 1}, {256, 0, 0, 0, 1, 1},
+                        {256, 0, 0, 0, 5, 1},  {128, 0, 1, 0, 1, 1},  {128, 0, 1, 0, 10, 1}, {128, 0, 1, 0, 12, 1},
+                        {256, 0, 1, 0, 5, 1},  {256, 0, 1, 0, 6, 1}};
+        vs.insert(vs.end(), hv, hv + 10);
     }
     if (H->n % 2 == 0 && hs_ok) {
         const V pv[] = {{64, 0, 0, 1, 1, 0}, {128, 0, 0, 1, 1, 0}, {64, 0, 0, 1, 12, 0}, {128, 0, 0, 1, 6, 0}};

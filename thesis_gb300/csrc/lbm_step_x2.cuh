@@ -459,7 +459,11 @@ __device__ __forceinline__ void pair_node(const StepParams &p, const G &g, int x
 
 // One node per thread with pair_node's arithmetic (storage units h, lanes of
 // type f1): no decode or encode per population and moments from deviations.
-template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G>
+// SPEC: the pull values (guarded by the node's coordinates, not its flag
+// word) and the node's own bounce-back values are loaded together with the
+// flag word and selected once it arrives: one memory round trip per node
+// instead of two (flag word, then the addresses it selects).
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC = false>
 __device__ __forceinline__ void h_node(const StepParams &p, const G &g, int x, int y, int z) {
     using L = Lat<Q>;
     using T = typename Store<ST>::T;
@@ -472,13 +476,42 @@ __device__ __forceinline__ void h_node(const StepParams &p, const G &g, int x, i
     const int node = x + g.nx * row;
     const long long idx = x + (long long)g.pitch * row;
     const uint32_t w = in_row ? __ldg(p.word + node) : 0u;
-    const bool fluid = (w & W_FLUID) != 0;
     const T *in = (const T *)p.fin[0] + idx;
     T *out = (T *)p.fout[0] + idx;
     auto raw = [](const T *q) -> float {
         if constexpr (F16) return __half2float(__ldg(q));
         else return __ldg(q);
     };
+    const int plane = g.pitch * g.ny;
+    int oxm = -1, oxp = 1, oym = -g.pitch, oyp = g.pitch, ozm = -plane, ozp = plane;
+    if (WRAP) {
+        oxm = x == 0 ? g.nx - 1 : -1;
+        oxp = x == g.nx - 1 ? 1 - g.nx : 1;
+        oym = y == 0 ? (g.ny - 1) * g.pitch : -g.pitch;
+        oyp = y == g.ny - 1 ? (1 - g.ny) * g.pitch : g.pitch;
+        ozm = z == 0 ? (g.nz - 1) * plane : -plane;
+        ozp = z == g.nz - 1 ? (1 - g.nz) * plane : plane;
+    }
+    float spec_pull[SPEC ? Q : 1], spec_own[SPEC ? Q : 1];
+    if constexpr (SPEC) {
+        // every address below lies inside the lattice: pulls only where the
+        // source coordinate does (with WRAP every offset wraps into it)
+        const bool xl = WRAP || x > 0, xh = WRAP || x < g.nx - 1, yl = WRAP || y > 0, yh = WRAP || y < g.ny - 1,
+                   zl = WRAP || z > 0, zh = WRAP || z < g.nz - 1;
+#pragma unroll
+        for (int d = 1; d < Q; ++d) {
+            const bool inside = in_row && (L::cx(d) == 1 ? xl : (L::cx(d) == -1 ? xh : true)) &&
+                                (L::cy(d) == 1 ? yl : (L::cy(d) == -1 ? yh : true)) &&
+                                (L::cz(d) == 1 ? zl : (L::cz(d) == -1 ? zh : true));
+            const int pull = d * g.nx + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
+                             (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
+                             (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
+            spec_pull[d] = inside ? raw(in + pull) : 0.f;
+            spec_own[d] = in_row ? raw(in + (PHYS ? L::opp(d) : d) * g.nx) : 0.f;
+        }
+        spec_pull[0] = in_row ? raw(in) : 0.f;
+    }
+    const bool fluid = (w & W_FLUID) != 0;
     auto put = [](T *q, float v) {
         if constexpr (F16) *q = __float2half_rn(v);
         else *q = v;
@@ -492,25 +525,21 @@ __device__ __forceinline__ void h_node(const StepParams &p, const G &g, int x, i
         }
         return;
     }
-    const int plane = g.pitch * g.ny;
-    int oxm = -1, oxp = 1, oym = -g.pitch, oyp = g.pitch, ozm = -plane, ozp = plane;
-    if (WRAP) {
-        oxm = x == 0 ? g.nx - 1 : -1;
-        oxp = x == g.nx - 1 ? 1 - g.nx : 1;
-        oym = y == 0 ? (g.ny - 1) * g.pitch : -g.pitch;
-        oyp = y == g.ny - 1 ? (1 - g.ny) * g.pitch : g.pitch;
-        ozm = z == 0 ? (g.nz - 1) * plane : -plane;
-        ozp = z == g.nz - 1 ? (1 - g.nz) * plane : plane;
-    }
     f1 h[Q];
-    h[0] = raw(in);
+    if constexpr (SPEC) {
+        h[0] = spec_pull[0];
 #pragma unroll
-    for (int d = 1; d < Q; ++d) {
-        const int pull = d * g.nx + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
-                         (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
-                         (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
-        const int own = (PHYS ? L::opp(d) : d) * g.nx;
-        h[d] = raw(in + (((w >> d) & 1u) ? own : pull));
+        for (int d = 1; d < Q; ++d) h[d] = ((w >> d) & 1u) ? spec_own[d] : spec_pull[d];
+    } else {
+        h[0] = raw(in);
+#pragma unroll
+        for (int d = 1; d < Q; ++d) {
+            const int pull = d * g.nx + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
+                             (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
+                             (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
+            const int own = (PHYS ? L::opp(d) : d) * g.nx;
+            h[d] = raw(in + (((w >> d) & 1u) ? own : pull));
+        }
     }
     bool keep = false, zv = false;
     if ((w & W_SPECIAL) || !PHYS) {
@@ -559,10 +588,11 @@ __global__ void __launch_bounds__(STEP_BLOCK) step_kernel_h(const StepParams p) 
 }
 
 // h_node with the lattice extents fixed at compile time (built at run time).
-template <int Q, int COLL, int ST, bool PHYS, bool WRAP, int NX, int NY, int NZ, int BLOCK, int MINB>
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, int NX, int NY, int NZ, int BLOCK, int MINB, bool SPEC = false>
 __global__ void __launch_bounds__(BLOCK, MINB) step_kernel_h_fixed(const StepParams p) {
     const FixedGeom<NX, NY, NZ, Q * NX> g;
-    h_node<Q, COLL, ST, PHYS, WRAP>(p, g, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y, blockIdx.z);
+    h_node<Q, COLL, ST, PHYS, WRAP, FixedGeom<NX, NY, NZ, Q * NX>, SPEC>(p, g, blockIdx.x * blockDim.x + threadIdx.x,
+                                                                        blockIdx.y, blockIdx.z);
 }
 
 template <int Q, int COLL, int ST, bool PHYS>
