@@ -654,8 +654,9 @@ def main():
                 "config": dict(workload_config(args, n, m, h), kernel=kernel,
                                kernel_knobs={"block": knobs[0], "l2_256B_loads": knobs[1] & 1,
                                              "storage_unit_arithmetic": (knobs[1] >> 1) & 1,
-                                             "predicated_bounce_back": knobs[2] & 1 & ~(knobs[1] >> 1),
-                                             "speculative_loads": knobs[2] & 1 & (knobs[1] >> 1),
+                                             "z_walk": max(knobs[1] >> 2, 1),
+                                             "predicated_bounce_back": knobs[2] & 1 & (1 - ((knobs[1] >> 1) & 1)),
+                                             "speculative_loads": knobs[2] & 1 & (knobs[1] >> 1) & 1,
                                              "two_nodes_per_thread": (knobs[2] >> 1) & 1,
                                              "min_blocks_per_sm": knobs[2] >> 2}),
                 "fluid_nodes_per_gpu": fluid, "status": status,

@@ -258,9 +258,12 @@ int lbm_kernel_variant(lbm_handle h);
  * the process on the same lattice and parameters.  The trial steps leave the
  * populations undefined: call lbm_init afterwards.  The chosen knobs go to
  * block, hint (bit 0 L2-256-byte loads, bit 1 arithmetic in storage units,
- * one node per thread) and pred (bit 0 predicated bounce-back, bit 1 two
- * nodes per thread, bits 2 and up the minimum resident blocks per SM asked of
- * the register allocator, 0 for none); each may be NULL.  In physics mode with
+ * one node per thread; bits 2 and up, storage units: nodes a thread updates
+ * along z with the next flag word loaded ahead, 0 for one) and pred (bit 0
+ * predicated bounce-back, or in storage units loads issued before the flag
+ * word arrives; bit 1 two nodes per thread; bits 2 and up the minimum
+ * resident blocks per SM asked of the register allocator, 0 for none); each
+ * may be NULL.  In physics mode with
  * F32 storage only storage-unit variants are candidates (their moments come
  * from deviations from the rest state).  This function has no
  * counterpart in the reference. */

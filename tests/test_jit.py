@@ -25,8 +25,10 @@ from thesis_gb300.solver import Arguments, Solver
     (19, N.MRT, N.STORE_F32, 0, 0, (64, 48, 40), (128, 0, 0)),
     (19, N.BGKW, N.STORE_F32, 0, 1, (64, 48, 40), (128, 2, 0)),
     (19, N.MRT, N.STORE_F32, 0, 0, (64, 48, 40), (64, 0, 2)),
-    # storage-unit kernel with speculative loads
+    # storage-unit kernel with speculative loads, and walking 4 nodes along z
     (19, N.MRT, N.STORE_F16S, 1, 0, (256, 256, 512), (128, 2, 1 | (10 << 2))),
+    (19, N.MRT, N.STORE_F16S, 1, 0, (256, 256, 512), (128, 2 | (4 << 2), 10 << 2)),
+    (19, N.BGKW, N.STORE_F32, 0, 1, (20, 16, 21), (128, 2 | (8 << 2), 0)),
     (9, N.TRT, N.STORE_F32, 1, 1, (160, 48, 1), (128, 2, 1)),
 ])
 def test_jit_sources_compile(native_lib, q, coll, storage, phys, wrap, dims, knobs):
@@ -166,7 +168,7 @@ def test_jit_pair_reference_cavity(oracle, monkeypatch):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kernel", ["jith", "jiths", "jitf"])
+@pytest.mark.parametrize("kernel", ["jith", "jiths", "jithz4", "jithz5", "jitf"])
 @pytest.mark.parametrize("storage", [N.STORE_F32, N.STORE_F16S])
 def test_storage_unit_and_f_space_kernels(oracle, monkeypatch, kernel, storage):
     """Both one-node arithmetic forms (and the storage-unit kernel with
@@ -178,8 +180,9 @@ def test_storage_unit_and_f_space_kernels(oracle, monkeypatch, kernel, storage):
                      init_equilibrium=1, inlet_profile=N.INLET_PRESSURE, outlet_profile=N.OUTLET_PRESSURE,
                      rho_in=1.005, rho_out=1.0)
     with Solver(lat, args) as s:
-        assert s.kernel_config()[1] >> 1 == (kernel != "jitf")
+        assert (s.kernel_config()[1] >> 1) & 1 == (kernel != "jitf")
         assert s.kernel_config()[2] & 1 == (kernel == "jiths")
+        assert s.kernel_config()[1] >> 2 == (int(kernel[5:]) if kernel.startswith("jithz") else 0)
     g, r, fl = run_pair(oracle, lat, args, 40, init=_rest(lat.num_nodes))
     compare(g, r, fl, storage, 3)
 

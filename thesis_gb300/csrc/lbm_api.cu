@@ -85,6 +85,7 @@ struct lbm_handle_s {
     float *mdiff_prev = nullptr;  // u, v, w, rho at the last lbm_macro_diff (4 N floats)
     float *fd_snap = nullptr;     // FdRelDiff: f_prev, f_first (2 Q N floats, allocated on first use)
     bool fd_recorded = false;
+    int zwalk_request = 0;        // THESIS_LBM_KERNEL=jithz<k>
     double *partial = nullptr, *norms = nullptr;
     int nslots = 0;
     std::vector<long long> slot_node;
@@ -274,6 +275,7 @@ struct TunedKnobs {
     bool pred, pair;
     int minb;
     bool hspace;
+    int zwalk;
 };
 static std::mutex g_tuned_mutex;
 static std::map<std::string, TunedKnobs> g_tuned;
@@ -298,6 +300,7 @@ static int setup_jit(lbm_handle_s *H, const std::vector<uint32_t> &word, bool pa
     k.hspace = !pair && (hspace > 0 || (hspace < 0 && H->P.mode == LBM_MODE_PHYSICS &&
                                         H->P.storage != LBM_STORE_F64));
     k.pred = k.hspace && hspace == 2;
+    k.zwalk = k.hspace && H->zwalk_request > 1 ? H->zwalk_request : 1;
     {
         std::lock_guard<std::mutex> lock(g_tuned_mutex);
         auto it = g_tuned.find(tune_key(k));
@@ -308,6 +311,7 @@ static int setup_jit(lbm_handle_s *H, const std::vector<uint32_t> &word, bool pa
             k.pair = it->second.pair;
             k.minb = it->second.minb;
             k.hspace = it->second.hspace;
+            k.zwalk = it->second.zwalk;
         }
     }
     std::string err;
@@ -402,11 +406,14 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
         const bool can_pair = (L->n % 2 == 0) && P->storage != LBM_STORE_F64;
         H->pair_kernel = kv && strcmp(kv, "pair") == 0 && can_pair;
         want_tma = kv && strcmp(kv, "tma") == 0;
+        // jithz<k>: storage units walking k nodes along z
+        const int zw_env = kv && strncmp(kv, "jithz", 5) == 0 ? atoi(kv + 5) : 0;
         want_jit = !kv || !*kv || strcmp(kv, "jit") == 0 || strcmp(kv, "jit2") == 0 || strcmp(kv, "jith") == 0 ||
-                   strcmp(kv, "jiths") == 0 || strcmp(kv, "jitf") == 0;
+                   strcmp(kv, "jiths") == 0 || strcmp(kv, "jitf") == 0 || zw_env > 0;
+        H->zwalk_request = zw_env;
         jit_required = kv && *kv && want_jit;
         jit_pair = kv && strcmp(kv, "jit2") == 0 && can_pair;
-        jit_hspace = kv && strcmp(kv, "jith") == 0    ? 1
+        jit_hspace = kv && (strcmp(kv, "jith") == 0 || zw_env > 0) ? 1
                      : kv && strcmp(kv, "jiths") == 0 ? 2  // storage units, speculative loads
                      : kv && strcmp(kv, "jitf") == 0  ? 0
                                                       : -1;
@@ -553,7 +560,8 @@ static int launch(lbm_handle_s *H, int from, int write_macro, cudaStream_t s) {
     if (H->jit_kernel) {
         const int bx = H->jit_key.block;
         const int units = H->jit_key.pair ? H->n / 2 : H->n;  // threads along x (h-space: one node each)
-        const dim3 grid((unsigned)((units + bx - 1) / bx), (unsigned)H->m, (unsigned)H->h);
+        const int zw = H->jit_key.hspace && H->jit_key.zwalk > 1 ? H->jit_key.zwalk : 1;
+        const dim3 grid((unsigned)((units + bx - 1) / bx), (unsigned)H->m, (unsigned)((H->h + zw - 1) / zw));
         void *args[] = {(void *)&p};
         cudaError_t e = cudaLaunchKernel((const void *)H->jit_fn, grid, dim3((unsigned)bx), args, 0, s);
         return e == cudaSuccess ? LBM_OK : fail(LBM_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
@@ -889,27 +897,34 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
     // from deviations: an f-space kernel would bring back the ~1e-6 residual
     // floor of cancelling FP32 sums.
     struct V {
-        int block, hint, pred, pair, minb, hs;
+        int block, hint, pred, pair, minb, hs, zw;
     };
     const bool fspace_ok = !(H->P.mode == LBM_MODE_PHYSICS && H->P.storage == LBM_STORE_F32);
     const bool hs_ok = H->P.storage != LBM_STORE_F64;
     std::vector<V> vs;
     if (fspace_ok) {
-        const V fv[] = {{128, 0, 0, 0, 1, 0}, {128, 1, 0, 0, 1, 0}, {128, 0, 1, 0, 1, 0}, {128, 1, 1, 0, 1, 0},
-                        {256, 0, 0, 0, 1, 0}, {256, 1, 1, 0, 1, 0}, {128, 1, 1, 0, 12, 0}};
+        const V fv[] = {{128, 0, 0, 0, 1, 0, 1}, {128, 1, 0, 0, 1, 0, 1}, {128, 0, 1, 0, 1, 0, 1},
+                        {128, 1, 1, 0, 1, 0, 1}, {256, 0, 0, 0, 1, 0, 1}, {256, 1, 1, 0, 1, 0, 1},
+                        {128, 1, 1, 0, 12, 0, 1}};
         vs.insert(vs.end(), fv, fv + 7);
     }
     if (hs_ok) {
-        // register caps of about 64, 48, 40 and 32 per thread
         // register caps of about 64, 48 and 40 per thread; pred = 1 loads the
-        // pull and own values before the flag word arrives
-        const V hv[] = {{128, 0, 0, 0, 1, 1},  {128, 0, 0, 0, 10, 1}, {128, 0, 0, 0, 12, 1}, {256, 0, 0, 0, 1, 1},
-                        {256, 0, 0, 0, 5, 1},  {128, 0, 1, 0, 1, 1},  {128, 0, 1, 0, 10, 1}, {128, 0, 1, 0, 12, 1},
-                        {256, 0, 1, 0, 5, 1},  {256, 0, 1, 0, 6, 1}};
-        vs.insert(vs.end(), hv, hv + 10);
+        // pull and own values before the flag word arrives; zw > 1 walks zw
+        // nodes along z per thread with the next flag word loaded ahead
+        const V hv[] = {{128, 0, 0, 0, 1, 1, 1}, {128, 0, 0, 0, 10, 1, 1}, {128, 0, 0, 0, 12, 1, 1},
+                        {256, 0, 0, 0, 1, 1, 1}, {256, 0, 0, 0, 5, 1, 1},  {128, 0, 1, 0, 1, 1, 1},
+                        {128, 0, 1, 0, 10, 1, 1}};
+        vs.insert(vs.end(), hv, hv + 7);
+        if (H->h >= 16) {
+            const V hz[] = {{128, 0, 0, 0, 1, 1, 4}, {128, 0, 0, 0, 10, 1, 2}, {128, 0, 0, 0, 10, 1, 4},
+                            {128, 0, 0, 0, 10, 1, 8}, {256, 0, 0, 0, 5, 1, 4}, {128, 0, 0, 0, 12, 1, 4}};
+            vs.insert(vs.end(), hz, hz + 6);
+        }
     }
     if (H->n % 2 == 0 && hs_ok) {
-        const V pv[] = {{64, 0, 0, 1, 1, 0}, {128, 0, 0, 1, 1, 0}, {64, 0, 0, 1, 12, 0}, {128, 0, 0, 1, 6, 0}};
+        const V pv[] = {{64, 0, 0, 1, 1, 0, 1}, {128, 0, 0, 1, 1, 0, 1}, {64, 0, 0, 1, 12, 0, 1},
+                        {128, 0, 0, 1, 6, 0, 1}};
         vs.insert(vs.end(), pv, pv + 4);
     }
     std::vector<JitStepKey> cand;
@@ -921,6 +936,7 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
         k.pair = v.pair != 0;
         k.minb = v.minb;
         k.hspace = v.hs != 0;
+        k.zwalk = v.zw;
         cand.push_back(k);
     }
     std::vector<cudaKernel_t> fn(cand.size(), nullptr);
@@ -972,11 +988,12 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
     {
         std::lock_guard<std::mutex> lock(g_tuned_mutex);
         g_tuned[tune_key(H->jit_key)] = TunedKnobs{H->jit_key.block, H->jit_key.hint, H->jit_key.pred,
-                                                   H->jit_key.pair, H->jit_key.minb, H->jit_key.hspace};
+                                                   H->jit_key.pair, H->jit_key.minb, H->jit_key.hspace,
+                                                   H->jit_key.zwalk};
     }
     H->initialised = false;  // the trial steps leave the populations undefined
     if (block) *block = H->jit_key.block;
-    if (hint) *hint = H->jit_key.hint | (H->jit_key.hspace ? 2 : 0);
+    if (hint) *hint = H->jit_key.hint | (H->jit_key.hspace ? 2 : 0) | (H->jit_key.zwalk > 1 ? H->jit_key.zwalk << 2 : 0);
     if (pred) *pred = (H->jit_key.pred ? 1 : 0) | (H->jit_key.pair ? 2 : 0) | (H->jit_key.minb > 1 ? H->jit_key.minb << 2 : 0);
     return LBM_OK;
 }
@@ -984,7 +1001,10 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
 int lbm_kernel_config(lbm_handle H, int *block, int *hint, int *pred) {
     if (!H) return fail(LBM_ERR_INVALID, "null handle");
     if (block) *block = H->jit_kernel ? H->jit_key.block : STEP_BLOCK;
-    if (hint) *hint = H->jit_kernel ? H->jit_key.hint | (H->jit_key.hspace ? 2 : 0) : 0;
+    if (hint)
+        *hint = H->jit_kernel ? H->jit_key.hint | (H->jit_key.hspace ? 2 : 0) |
+                                    (H->jit_key.zwalk > 1 ? H->jit_key.zwalk << 2 : 0)
+                              : 0;
     if (pred)
         *pred = H->jit_kernel ? (H->jit_key.pred ? 1 : 0) | (H->jit_key.pair ? 2 : 0) |
                                     (H->jit_key.minb > 1 ? H->jit_key.minb << 2 : 0)
@@ -997,6 +1017,7 @@ int lbm_jit_check(int q, int coll, int storage, int phys, int wrap, int nx, int 
     JitStepKey k{q, coll, storage, phys != 0, wrap != 0, nx, ny, nz, block, hint & 1, (pred & 1) != 0, true,
                  (pred & 2) != 0, (pred >> 2) > 1 ? (pred >> 2) : 1};
     k.hspace = (hint & 2) != 0;
+    k.zwalk = k.hspace && (hint >> 2) > 1 ? hint >> 2 : 1;
     std::string err;
     if (jit_step_kernel(k, nullptr, err)) return fail(LBM_ERR_CUDA, err);
     return LBM_OK;

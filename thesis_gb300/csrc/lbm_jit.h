@@ -17,6 +17,7 @@ struct JitStepKey {
     bool pair;          // two nodes per thread (step_kernel_x2_fixed; hint, pred unused)
     int minb = 1;       // __launch_bounds__ minimum blocks per SM (1: no constraint)
     bool hspace = false;  // one node per thread in storage units (step_kernel_h_fixed)
+    int zwalk = 1;        // storage units: nodes a thread updates along z (flag word loaded ahead)
 };
 
 // Compile (or fetch from the process cache) step_kernel_fixed for `k` and

@@ -464,7 +464,7 @@ __device__ __forceinline__ void pair_node(const StepParams &p, const G &g, int x
 // flag word and selected once it arrives: one memory round trip per node
 // instead of two (flag word, then the addresses it selects).
 template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC = false>
-__device__ __forceinline__ void h_node(const StepParams &p, const G &g, int x, int y, int z) {
+__device__ __forceinline__ void h_node_w(const StepParams &p, const G &g, int x, int y, int z, uint32_t w) {
     using L = Lat<Q>;
     using T = typename Store<ST>::T;
     constexpr bool F16 = ST == LBM_STORE_F16S;
@@ -475,7 +475,6 @@ __device__ __forceinline__ void h_node(const StepParams &p, const G &g, int x, i
     const int row = y + g.ny * z;
     const int node = x + g.nx * row;
     const long long idx = x + (long long)g.pitch * row;
-    const uint32_t w = in_row ? __ldg(p.word + node) : 0u;
     const T *in = (const T *)p.fin[0] + idx;
     T *out = (T *)p.fout[0] + idx;
     auto raw = [](const T *q) -> float {
@@ -581,6 +580,13 @@ __device__ __forceinline__ void h_node(const StepParams &p, const G &g, int x, i
     for (int d = 0; d < Q; ++d) put(out + d * g.nx, h[d].v);
 }
 
+// One node: its flag word, then the update.
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC = false>
+__device__ __forceinline__ void h_node(const StepParams &p, const G &g, int x, int y, int z) {
+    const uint32_t w = x < g.nx ? __ldg(p.word + x + g.nx * (y + g.ny * z)) : 0u;
+    h_node_w<Q, COLL, ST, PHYS, WRAP, G, SPEC>(p, g, x, y, z, w);
+}
+
 template <int Q, int COLL, int ST, bool PHYS>
 __global__ void __launch_bounds__(STEP_BLOCK) step_kernel_h(const StepParams p) {
     const DynGeom g{p.nx, p.ny, p.nz, p.pitch};
@@ -588,11 +594,31 @@ __global__ void __launch_bounds__(STEP_BLOCK) step_kernel_h(const StepParams p) 
 }
 
 // h_node with the lattice extents fixed at compile time (built at run time).
-template <int Q, int COLL, int ST, bool PHYS, bool WRAP, int NX, int NY, int NZ, int BLOCK, int MINB, bool SPEC = false>
+// ZW > 1: a thread updates ZW nodes in a column along z, loading the next
+// node's flag word before it works on the current one, so the populations'
+// addresses do not wait a memory round trip for it (blockIdx.z = z / ZW).
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, int NX, int NY, int NZ, int BLOCK, int MINB, bool SPEC = false,
+          int ZW = 1>
 __global__ void __launch_bounds__(BLOCK, MINB) step_kernel_h_fixed(const StepParams p) {
-    const FixedGeom<NX, NY, NZ, Q * NX> g;
-    h_node<Q, COLL, ST, PHYS, WRAP, FixedGeom<NX, NY, NZ, Q * NX>, SPEC>(p, g, blockIdx.x * blockDim.x + threadIdx.x,
-                                                                        blockIdx.y, blockIdx.z);
+    using G = FixedGeom<NX, NY, NZ, Q * NX>;
+    const G g;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if constexpr (ZW == 1) {
+        h_node<Q, COLL, ST, PHYS, WRAP, G, SPEC>(p, g, x, blockIdx.y, blockIdx.z);
+    } else {
+        const int y = blockIdx.y, z0 = blockIdx.z * ZW;
+        const bool in_row = x < NX;
+        uint32_t w = in_row ? __ldg(p.word + x + NX * (y + NY * z0)) : 0u;
+#pragma unroll 1
+        for (int k = 0; k < ZW; ++k) {
+            const int z = z0 + k;
+            if (z >= NZ) break;  // the same z for every thread of the block
+            const uint32_t wn =
+                in_row && k + 1 < ZW && z + 1 < NZ ? __ldg(p.word + x + NX * (y + NY * (z + 1))) : 0u;
+            h_node_w<Q, COLL, ST, PHYS, WRAP, G, SPEC>(p, g, x, y, z, w);
+            w = wn;
+        }
+    }
 }
 
 template <int Q, int COLL, int ST, bool PHYS>
