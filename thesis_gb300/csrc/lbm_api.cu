@@ -917,9 +917,10 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
                         {128, 0, 1, 0, 10, 1, 1}};
         vs.insert(vs.end(), hv, hv + 7);
         if (H->h >= 16) {
-            const V hz[] = {{128, 0, 0, 0, 1, 1, 4}, {128, 0, 0, 0, 10, 1, 2}, {128, 0, 0, 0, 10, 1, 4},
-                            {128, 0, 0, 0, 10, 1, 8}, {256, 0, 0, 0, 5, 1, 4}, {128, 0, 0, 0, 12, 1, 4}};
-            vs.insert(vs.end(), hz, hz + 6);
+            const V hz[] = {{128, 0, 0, 0, 10, 1, 2}, {128, 0, 0, 0, 10, 1, 4}, {128, 0, 0, 0, 10, 1, 8},
+                            {128, 0, 0, 0, 10, 1, 16}, {128, 0, 0, 0, 11, 1, 4}, {256, 0, 0, 0, 5, 1, 4},
+                            {64, 0, 0, 0, 20, 1, 4}};
+            vs.insert(vs.end(), hz, hz + 7);
         }
     }
     if (H->n % 2 == 0 && hs_ok) {
