@@ -70,9 +70,9 @@ def parse():
     ap.add_argument("--domains", type=int, default=512, help="cavities in the batch")
     ap.add_argument("--one-by-one-steps", type=int, default=20,
                     help="steps per cavity when the cavities run one launch per step each")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "jit", "jit2", "jith", "jiths", "jitf", "tma", "pair",
-                                                         "scalar"],
-                    help="step kernel (auto: the library's default for the storage)")
+    ap.add_argument("--kernel", default="auto",
+                    help="step kernel: auto (the library's default, autotuned) or a THESIS_LBM_KERNEL value: jit, "
+                         "jit2, jith, jiths, jithz<k>[b<block>][m<min blocks>], jitf, tma, pair, scalar")
     return ap.parse_args()
 
 

@@ -85,7 +85,8 @@ struct lbm_handle_s {
     float *mdiff_prev = nullptr;  // u, v, w, rho at the last lbm_macro_diff (4 N floats)
     float *fd_snap = nullptr;     // FdRelDiff: f_prev, f_first (2 Q N floats, allocated on first use)
     bool fd_recorded = false;
-    int zwalk_request = 0;        // THESIS_LBM_KERNEL=jithz<k>
+    int zwalk_request = 0;        // THESIS_LBM_KERNEL=jithz<k>[b<block>][m<min blocks>]
+    int block_request = 0, minb_request = 0;
     double *partial = nullptr, *norms = nullptr;
     int nslots = 0;
     std::vector<long long> slot_node;
@@ -301,6 +302,9 @@ static int setup_jit(lbm_handle_s *H, const std::vector<uint32_t> &word, bool pa
                                         H->P.storage != LBM_STORE_F64));
     k.pred = k.hspace && hspace == 2;
     k.zwalk = k.hspace && H->zwalk_request > 1 ? H->zwalk_request : 1;
+    if (k.hspace && H->block_request >= 32 && H->block_request <= 1024 && H->block_request % 32 == 0)
+        k.block = H->block_request;
+    if (k.hspace && H->minb_request > 1) k.minb = H->minb_request;
     {
         std::lock_guard<std::mutex> lock(g_tuned_mutex);
         auto it = g_tuned.find(tune_key(k));
@@ -406,8 +410,15 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
         const bool can_pair = (L->n % 2 == 0) && P->storage != LBM_STORE_F64;
         H->pair_kernel = kv && strcmp(kv, "pair") == 0 && can_pair;
         want_tma = kv && strcmp(kv, "tma") == 0;
-        // jithz<k>: storage units walking k nodes along z
-        const int zw_env = kv && strncmp(kv, "jithz", 5) == 0 ? atoi(kv + 5) : 0;
+        // jithz<k>[b<block>][m<min blocks>]: storage units walking k nodes along z
+        int zw_env = 0, b_env = 0, m_env = 0;
+        if (kv && strncmp(kv, "jithz", 5) == 0) {
+            zw_env = atoi(kv + 5);
+            if (const char *bp = strchr(kv, 'b')) b_env = atoi(bp + 1);
+            if (const char *mp = strchr(kv + 5, 'm')) m_env = atoi(mp + 1);
+        }
+        H->block_request = b_env;
+        H->minb_request = m_env;
         want_jit = !kv || !*kv || strcmp(kv, "jit") == 0 || strcmp(kv, "jit2") == 0 || strcmp(kv, "jith") == 0 ||
                    strcmp(kv, "jiths") == 0 || strcmp(kv, "jitf") == 0 || zw_env > 0;
         H->zwalk_request = zw_env;
