@@ -459,6 +459,77 @@ __device__ __forceinline__ void pair_node(const StepParams &p, const G &g, int x
 
 // One node per thread with pair_node's arithmetic (storage units h, lanes of
 // type f1): no decode or encode per population and moments from deviations.
+// The update of one fluid node in storage units: gather (pull or bounce
+// back), boundary conditions, moments, collision; h receives the new state.
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC>
+__device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x, int node, uint32_t w,
+                                         const typename Store<ST>::T *in, f1 (&h)[Q],
+                                         const float (&spec_pull)[SPEC ? Q : 1], const float (&spec_own)[SPEC ? Q : 1],
+                                         int oxm, int oxp, int oym, int oyp, int ozm,
+                                         int ozp) {
+    using L = Lat<Q>;
+    using T = typename Store<ST>::T;
+    constexpr bool F16 = ST == LBM_STORE_F16S;
+    const float sigma = p.sigma;
+    const float S = F16 ? p.scale : 1.f;
+    const float invS = F16 ? p.inv_scale : 1.f;
+    auto raw = [](const T *q) -> float {
+        if constexpr (F16) return __half2float(__ldg(q));
+        else return __ldg(q);
+    };
+    if constexpr (SPEC) {
+        h[0] = spec_pull[0];
+#pragma unroll
+        for (int d = 1; d < Q; ++d) h[d] = ((w >> d) & 1u) ? spec_own[d] : spec_pull[d];
+    } else {
+        h[0] = raw(in);
+#pragma unroll
+        for (int d = 1; d < Q; ++d) {
+            const int pull = d * g.nx + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
+                             (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
+                             (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
+            const int own = (PHYS ? L::opp(d) : d) * g.nx;
+            h[d] = raw(in + (((w >> d) & 1u) ? own : pull));
+        }
+    }
+    bool keep = false, zv = false;
+    if ((w & W_SPECIAL) || !PHYS) {
+        if ((w & W_SPECIAL) || (w & 0x7FFFEu)) {
+            // boundary nodes and reference wall copies: to f, scalar code, back
+            float f[Q];
+#pragma unroll
+            for (int d = 0; d < Q; ++d) f[d] = fmaf(h[d].v, invS, sigma * p.shift[d]);
+            apply_bc<Q, ST, PHYS, WRAP, G>(f, w, node, p, g, keep, zv);
+#pragma unroll
+            for (int d = 0; d < Q; ++d) h[d] = f1((f[d] - sigma * p.shift[d]) * S);
+        }
+    }
+    f1 sum = h[0], jx = 0.f, jy = 0.f, jz = 0.f;
+#pragma unroll
+    for (int d = 1; d < Q; ++d) {
+        sum += h[d];
+        if (L::cx(d) == 1) jx += h[d]; else if (L::cx(d) == -1) jx -= h[d];
+        if (L::cy(d) == 1) jy += h[d]; else if (L::cy(d) == -1) jy -= h[d];
+        if (L::cz(d) == 1) jz += h[d]; else if (L::cz(d) == -1) jz -= h[d];
+    }
+    f1 rho = fma2(sum, f1(invS), f1(sigma));
+    const f1 sc = f1(invS / rho.v);
+    f1 ux = fma2(jx, sc, f1((float)p.gshift)), uy = jy * sc, uz = jz * sc;
+    if (zv) uy = 0.f;
+    if (keep) {
+        rho = p.rho[node];
+        ux = p.ux[node];
+        uy = p.uy[node];
+        uz = p.uz[node];
+    } else if (p.write_macro) {
+        p.rho[node] = rho.v;
+        p.ux[node] = ux.v;
+        p.uy[node] = uy.v;
+        p.uz[node] = uz.v;
+    }
+    collide_x2<Q, COLL, PHYS>(h, rho, ux, uy, uz, p, sigma, S);
+}
+
 // SPEC: the pull values (guarded by the node's coordinates, not its flag
 // word) and the node's own bounce-back values are loaded together with the
 // flag word and selected once it arrives: one memory round trip per node
@@ -516,69 +587,24 @@ __device__ __forceinline__ void h_node_w(const StepParams &p, const G &g, int x,
         else *q = v;
     };
     const unsigned warp_fluid = __ballot_sync(0xffffffffu, fluid);
-    if (!fluid) {
-        // solid nodes keep the zero encoding (sector-complete stores)
-        if (in_row && warp_fluid) {
-#pragma unroll
-            for (int d = 0; d < Q; ++d) put(out + d * g.nx, -sigma * p.shift[d] * S);
-        }
-        return;
-    }
+    if (!warp_fluid) return;  // a warp of solid nodes writes nothing
     f1 h[Q];
-    if constexpr (SPEC) {
-        h[0] = spec_pull[0];
-#pragma unroll
-        for (int d = 1; d < Q; ++d) h[d] = ((w >> d) & 1u) ? spec_own[d] : spec_pull[d];
+    if (fluid) {
+        h_update<Q, COLL, ST, PHYS, WRAP, G, SPEC>(p, g, x, node, w, in, h, spec_pull, spec_own, oxm, oxp, oym, oyp,
+                                                   ozm, ozp);
     } else {
-        h[0] = raw(in);
+        // solid lanes of a warp with fluid nodes store the zero encoding in
+        // the same store instructions, so every store covers whole sectors
 #pragma unroll
-        for (int d = 1; d < Q; ++d) {
-            const int pull = d * g.nx + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
-                             (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
-                             (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
-            const int own = (PHYS ? L::opp(d) : d) * g.nx;
-            h[d] = raw(in + (((w >> d) & 1u) ? own : pull));
-        }
+        for (int d = 0; d < Q; ++d) h[d] = f1(-sigma * p.shift[d] * S);
     }
-    bool keep = false, zv = false;
-    if ((w & W_SPECIAL) || !PHYS) {
-        if ((w & W_SPECIAL) || (w & 0x7FFFEu)) {
-            // boundary nodes and reference wall copies: to f, scalar code, back
-            float f[Q];
+    if (in_row) {
 #pragma unroll
-            for (int d = 0; d < Q; ++d) f[d] = fmaf(h[d].v, invS, sigma * p.shift[d]);
-            apply_bc<Q, ST, PHYS, WRAP, G>(f, w, node, p, g, keep, zv);
-#pragma unroll
-            for (int d = 0; d < Q; ++d) h[d] = f1((f[d] - sigma * p.shift[d]) * S);
-        }
+        for (int d = 0; d < Q; ++d) put(out + d * g.nx, h[d].v);
     }
-    f1 sum = h[0], jx = 0.f, jy = 0.f, jz = 0.f;
-#pragma unroll
-    for (int d = 1; d < Q; ++d) {
-        sum += h[d];
-        if (L::cx(d) == 1) jx += h[d]; else if (L::cx(d) == -1) jx -= h[d];
-        if (L::cy(d) == 1) jy += h[d]; else if (L::cy(d) == -1) jy -= h[d];
-        if (L::cz(d) == 1) jz += h[d]; else if (L::cz(d) == -1) jz -= h[d];
-    }
-    f1 rho = fma2(sum, f1(invS), f1(sigma));
-    const f1 sc = f1(invS / rho.v);
-    f1 ux = fma2(jx, sc, f1((float)p.gshift)), uy = jy * sc, uz = jz * sc;
-    if (zv) uy = 0.f;
-    if (keep) {
-        rho = p.rho[node];
-        ux = p.ux[node];
-        uy = p.uy[node];
-        uz = p.uz[node];
-    } else if (p.write_macro) {
-        p.rho[node] = rho.v;
-        p.ux[node] = ux.v;
-        p.uy[node] = uy.v;
-        p.uz[node] = uz.v;
-    }
-    collide_x2<Q, COLL, PHYS>(h, rho, ux, uy, uz, p, sigma, S);
-#pragma unroll
-    for (int d = 0; d < Q; ++d) put(out + d * g.nx, h[d].v);
 }
+
+
 
 // One node: its flag word, then the update.
 template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC = false>
