@@ -44,7 +44,8 @@ batch_step_kernel(const StepParams *__restrict__ tab, const int4 *__restrict__ t
         const int4 tl = tiles[t];
         const StepParams &p = tab[tl.x];
         const DynGeom g{p.nx, p.ny, p.nz, p.pitch};
-        h_node<Q, COLL, ST, PHYS, true>(p, g, tl.z + (int)threadIdx.x, tl.y % p.ny, tl.y / p.ny);
+        h_node<Q, COLL, ST, PHYS, true, DynGeom, false, false>(p, g, tl.z + (int)threadIdx.x, tl.y % p.ny,
+                                                               tl.y / p.ny);
     }
 }
 

@@ -534,7 +534,11 @@ __device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x,
 // word) and the node's own bounce-back values are loaded together with the
 // flag word and selected once it arrives: one memory round trip per node
 // instead of two (flag word, then the addresses it selects).
-template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC = false>
+// MERGE: solid lanes of a warp with fluid nodes store their zero encoding in
+// the fluid lanes' store instructions (one store per direction and warp);
+// without it they store in a branch of their own, which keeps fewer
+// registers live (the batch kernel, whose domains are mostly all fluid).
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC = false, bool MERGE = true>
 __device__ __forceinline__ void h_node_w(const StepParams &p, const G &g, int x, int y, int z, uint32_t w) {
     using L = Lat<Q>;
     using T = typename Store<ST>::T;
@@ -589,6 +593,20 @@ __device__ __forceinline__ void h_node_w(const StepParams &p, const G &g, int x,
     const unsigned warp_fluid = __ballot_sync(0xffffffffu, fluid);
     if (!warp_fluid) return;  // a warp of solid nodes writes nothing
     f1 h[Q];
+    if constexpr (!MERGE) {
+        if (!fluid) {
+            if (in_row) {
+#pragma unroll
+                for (int d = 0; d < Q; ++d) put(out + d * g.nx, -sigma * p.shift[d] * S);
+            }
+            return;
+        }
+        h_update<Q, COLL, ST, PHYS, WRAP, G, SPEC>(p, g, x, node, w, in, h, spec_pull, spec_own, oxm, oxp, oym, oyp,
+                                                   ozm, ozp);
+#pragma unroll
+        for (int d = 0; d < Q; ++d) put(out + d * g.nx, h[d].v);
+        return;
+    }
     if (fluid) {
         h_update<Q, COLL, ST, PHYS, WRAP, G, SPEC>(p, g, x, node, w, in, h, spec_pull, spec_own, oxm, oxp, oym, oyp,
                                                    ozm, ozp);
@@ -607,10 +625,10 @@ __device__ __forceinline__ void h_node_w(const StepParams &p, const G &g, int x,
 
 
 // One node: its flag word, then the update.
-template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC = false>
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC = false, bool MERGE = true>
 __device__ __forceinline__ void h_node(const StepParams &p, const G &g, int x, int y, int z) {
     const uint32_t w = x < g.nx ? __ldg(p.word + x + g.nx * (y + g.ny * z)) : 0u;
-    h_node_w<Q, COLL, ST, PHYS, WRAP, G, SPEC>(p, g, x, y, z, w);
+    h_node_w<Q, COLL, ST, PHYS, WRAP, G, SPEC, MERGE>(p, g, x, y, z, w);
 }
 
 template <int Q, int COLL, int ST, bool PHYS>
