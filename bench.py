@@ -454,7 +454,8 @@ def run_warmstart(args):
     seeds = range(100000, 100000 + args.ws_eval)
     clocks = ClockSampler(0)
     clocks.start()
-    r = ws.compare(net, seeds, n, m)
+    warm_cap = int(2 * dsteps[conv].max())  # warm runs beyond it fall back to the cold start
+    r = ws.compare(net, seeds, n, m, warm_max_steps=warm_cap)
     clk = clocks.stop()
     ok = (r["cold_res"] <= ws.TOL) & (r["warm_res"] <= ws.TOL)
     perr = []
@@ -513,6 +514,7 @@ def run_warmstart(args):
             "iteration_seconds": {"cold": r["cold_seconds"], "warm": r["warm_seconds"],
                                   "prediction": r["predict_seconds"]},
             "steps_to_tolerance": {"converged_both": int(ok.sum()), "warm_fallbacks_to_cold": r["fallbacks"],
+                                   "warm_step_cap": warm_cap,
                                    "cold_median": float(np.median(r["cold_steps"])),
                                    "warm_median": float(np.median(r["warm_steps"])),
                                    "warm_over_cold_sum": float(r["warm_steps"][ok].sum() / r["cold_steps"][ok].sum())},

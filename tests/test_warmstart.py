@@ -37,21 +37,24 @@ def test_encoding_round_trip_and_flop_count():
 
 @pytest.mark.gpu
 def test_warm_start_reaches_tolerance_in_fewer_steps():
-    X, Y, Wt, steps, resid, _ = ws.dataset(range(256))
+    X, Y, Wt, steps, resid, _ = ws.dataset(range(512))
     assert np.all(resid <= ws.TOL)
+    # a warm run gets twice the longest cold solve of the training set before
+    # its channel falls back to the cold start
+    cap = int(2 * steps.max())
     with ws.UNet(64, 256, max_batch=32, seed=2, levels=5) as net:
         net.set_dataset(X, Y, Wt)
-        hist = net.train(epochs=60, batch=16, lr=2e-3, lr_final=1e-4)
+        hist = net.train(epochs=80, batch=16, lr=2e-3, lr_final=1e-4)
         assert hist[-1] < 0.05 * hist[0]
-        r = ws.compare(net, range(200000, 200016))
+        r = ws.compare(net, range(200000, 200016), warm_max_steps=cap)
         lats, res = r["lats"][:4], r["re"][:4]
-        fb_steps, fb_res, fb_out, fb_cold = ws.solve_with_warm_start(net, lats, res)
+        fb_steps, fb_res, fb_out, fb_cold = ws.solve_with_warm_start(net, lats, res, warm_max_steps=cap)
     assert np.all(r["cold_res"] <= ws.TOL)
     # a warm run that misses the tolerance (a prediction can excite a slowly
-    # growing mode; 0 or 1 of 16 seen) is charged its steps plus the cold
-    # fallback's; measured 0.61 of the cold steps with this training
+    # growing mode; 0-2 of 16 seen with a smaller network) is charged its
+    # capped steps plus the cold fallback's
     ok = r["warm_res"] <= ws.TOL
-    assert (~ok).sum() <= 2
+    assert (~ok).sum() <= 3
     effective = r["warm_steps"] + np.where(ok, 0, r["cold_steps"])
     assert effective.sum() < 0.85 * r["cold_steps"].sum(), (r["warm_steps"], r["cold_steps"])
     # at a 1e-5 residual the two converged fields still carry slowly decaying

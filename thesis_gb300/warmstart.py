@@ -248,11 +248,13 @@ def dataset(seeds, n=256, m=64, **kw):
     return X, Y, Wt, steps, resid, secs
 
 
-def compare(unet, seeds, n=256, m=64, tol=TOL, check_every=100, max_steps=400_000):
+def compare(unet, seeds, n=256, m=64, tol=TOL, check_every=100, max_steps=400_000, warm_max_steps=None):
     """Cold start (fluid at rest) against the U-Net warm start on the same
-    channels, each batch run to the tolerance.  Returns a dict with per-domain
-    steps, wall times, the prediction time and the converged fields'
-    difference (max |u_warm - u_cold| / u_max)."""
+    channels, each batch run to the tolerance.  A warm run gets at most
+    warm_max_steps (default max_steps) before its channel falls back to the
+    cold start.  Returns a dict with per-domain steps, wall times, the
+    prediction time and the converged fields' difference
+    (max |u_warm - u_cold| / u_max)."""
     seeds = list(seeds)
     lats = [geometry(s, n, m) for s in seeds]
     res = [reynolds(s) for s in seeds]
@@ -262,7 +264,7 @@ def compare(unet, seeds, n=256, m=64, tol=TOL, check_every=100, max_steps=400_00
     t_pred = time.perf_counter() - t0
     init = [fields(l, p) for l, p in zip(lats, pred)]
     cold = solve_batch(lats, res, None, tol, check_every, max_steps)
-    warm = solve_batch(lats, res, init, tol, check_every, max_steps)
+    warm = solve_batch(lats, res, init, tol, check_every, warm_max_steps or max_steps)
     # channels whose warm run missed the tolerance fall back to the cold start
     miss = [d for d in range(len(lats)) if not warm[1][d] <= tol]
     t_fallback = 0.0
@@ -280,16 +282,17 @@ def compare(unet, seeds, n=256, m=64, tol=TOL, check_every=100, max_steps=400_00
                 converged_du=np.array(du), pred=pred, init=init, cold_fields=cold[4], warm_fields=warm[4])
 
 
-def solve_with_warm_start(unet, lats, res, tol=TOL, check_every=100, max_steps=400_000):
+def solve_with_warm_start(unet, lats, res, tol=TOL, check_every=100, max_steps=400_000, warm_max_steps=None):
     """Steady solve of every channel from the network's prediction; a domain
-    whose warm run diverges or misses the tolerance is solved again from rest,
-    so the plain cold start is the fallback and the converged LBM field, not
-    the prediction, is the result.  Returns (steps, residuals, fields, cold)
-    with cold[d] True where the fallback ran."""
+    whose warm run diverges or misses the tolerance within warm_max_steps
+    (default max_steps) is solved again from rest, so the plain cold start is
+    the fallback and the converged LBM field, not the prediction, is the
+    result.  Returns (steps, residuals, fields, cold) with cold[d] True where
+    the fallback ran (steps then count both runs)."""
     X = np.stack([features(l, r) for l, r in zip(lats, res)])
     pred = unet.predict(X)
     init = [fields(l, p) for l, p in zip(lats, pred)]
-    steps, resid, rc, _, out, _ = solve_batch(lats, res, init, tol, check_every, max_steps)
+    steps, resid, rc, _, out, _ = solve_batch(lats, res, init, tol, check_every, warm_max_steps or max_steps)
     redo = [d for d in range(len(lats))
             if not (resid[d] <= tol and np.all(np.isfinite(out[d][1])))]
     cold = np.zeros(len(lats), bool)
@@ -297,7 +300,7 @@ def solve_with_warm_start(unet, lats, res, tol=TOL, check_every=100, max_steps=4
         s2, r2, _, _, o2, _ = solve_batch([lats[d] for d in redo], [res[d] for d in redo], None, tol, check_every,
                                           max_steps)
         for k, d in enumerate(redo):
-            steps[d], resid[d], out[d], cold[d] = s2[k], r2[k], o2[k], True
+            steps[d], resid[d], out[d], cold[d] = steps[d] + s2[k], r2[k], o2[k], True
     return steps, resid, out, cold
 
 
