@@ -517,7 +517,10 @@ def run_warmstart(args):
                                    "warm_step_cap": warm_cap,
                                    "cold_median": float(np.median(r["cold_steps"])),
                                    "warm_median": float(np.median(r["warm_steps"])),
-                                   "warm_over_cold_sum": float(r["warm_steps"][ok].sum() / r["cold_steps"][ok].sum())},
+                                   "warm_over_cold_sum": float(r["warm_steps"][ok].sum() / r["cold_steps"][ok].sum()),
+                                   "warm_with_fallbacks_over_cold_sum": float(
+                                       (r["warm_steps"] + np.where(r["warm_res"] <= ws.TOL, 0, r["cold_steps"])).sum()
+                                       / r["cold_steps"].sum())},
             "prediction_error_u": {"median": float(np.median(perr)), "p90": float(np.percentile(perr, 90))},
             "converged_field_error_vs_300k_step_runs": {"channels": k, "cold_median": float(np.median(ec)),
                                                         "warm_median": float(np.median(ew)),
