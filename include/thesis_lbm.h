@@ -105,7 +105,9 @@ typedef struct lbm_params {
     int inlet_profile;        /* LBM_NO_INLET, LBM_INLET_PRESSURE */
     int outlet_profile;       /* LBM_OUTLET_* */
     int collision_model;      /* LBM_BGKW, LBM_TRT, LBM_MRT */
-    int boundary_type;        /* LBM_STRAIGHT (LBM_CURVED unsupported) */
+    int boundary_type;        /* LBM_STRAIGHT, or LBM_CURVED: the reference's q-interpolated
+                                 walls (reference mode, simple wall model; link fractions
+                                 from lbm_set_link_q, 1/2 until then) */
     int bc_wall_model;        /* LBM_WALL_SIMPLE, or LBM_WALL_COMPLEX: the reference's HH wall
                                  (gpuBcComplexWall3D, GpuBoundaries.cu:492-1560), reference
                                  mode only; the reference's 2D loop has straight walls only */
@@ -128,6 +130,36 @@ int lbm_create(const lbm_lattice_desc *lattice, const lbm_params *params, lbm_ha
 /* Per-node inlet/outlet velocity field (the reference's u0/u1 arrays); any
  * NULL component keeps the constant from params.  Host arrays of n*m*h. */
 int lbm_set_inlet_velocity(lbm_handle h, const float *u, const float *v, const float *w);
+
+/* Curved walls (boundary_type LBM_CURVED): the fraction q of each BC link
+ * (num_conns values in the lattice's link order) at which the wall cuts the
+ * link from the node, |node -> wall| / |c_dir| in lattice spacings.  The
+ * reference computes q in initBoundaryConditions2D/3D (GpuInit.cu:1086-1088,
+ * :1203-1207; links without an entry keep 1/2) and applies the CURVED
+ * branch of gpuBcWall2D / gpuBcSimpleWall3D (GpuBoundaries.cu:414-432,
+ * :461-479) on every wall link of a fluid node, interpolating between the
+ * last step's post-collision populations (f* at the node and at its
+ * upstream neighbour, or f* at the node and its opposite, for q < 1/2 and
+ * q >= 1/2).  The reference's first coefficient of the q < 1/2 branch reads
+ * the next entry of its per-node table (link dir+1; for the last direction
+ * the next boundary node's first link, 1/2 past the last node), and it
+ * reads the upstream value at the flat index node + dir N + c(dir) of its
+ * direction-major array, which for a node whose upstream neighbour lies
+ * outside the lattice is a neighbouring row's or another direction's value;
+ * this engine does the same (0 past either end of the array, where the
+ * reference's read is undefined).  Takes effect from the next step.  LBM_ERR_UNSUPPORTED
+ * when the handle has no curved walls (straight walls, physics mode, or the
+ * HH wall model, whose reference kernel has no curved branch). */
+int lbm_set_link_q(lbm_handle h, const double *q);
+
+/* The reference's link fractions from coordinates: q[c] = |B_c - X_c| /
+ * (delta |c_dir|), B_c the BC file's boundary point of link c and X_c the
+ * Node file's coordinates of its node (node_x/y/z hold n*m*h values indexed
+ * by node, x fastest; bc_k, bc_z, node_z NULL in 2D), delta the grid spacing
+ * (getGridSpacing, FilesReading.cu:473-489).  FP64 arithmetic.  Host only. */
+int lbm_link_q(int dims, int n, int m, int h, int num_conns, const int *bc_i, const int *bc_j, const int *bc_k,
+               const int *bc_dir, const float *bc_x, const float *bc_y, const float *bc_z, const float *node_x,
+               const float *node_y, const float *node_z, double delta, double *q);
 
 /* Initial macroscopic state (NULL = constant from params) and the first
  * collision, which produces the state lbm_step advances. */

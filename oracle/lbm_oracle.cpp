@@ -36,7 +36,10 @@
  *   loop order              Iterate.cu:385-518, Iterate3D.cu:493-653
  *   HH ("complex") 3D wall  GpuBoundaries.cu:492-1560
  *
- * Not restated (the entry points return ORC_UNSUPPORTED): curved walls, the
+ *   curved walls            GpuBoundaries.cu:414-432 (2D), :461-479 (3D);
+ *                           link fractions GpuInit.cu:1086-1088, :1203-1207
+ *
+ * Not restated (the entry points return ORC_UNSUPPORTED): the
  * 3D outlet kernel (it addresses directions with the 2D plane size,
  * GpuBoundaries.cu:1662, so it rewrites other nodes) and the
  * INLET_PROF 3D profile the reference itself refuses (Iterate3D.cu:200-206).
@@ -126,6 +129,7 @@ typedef struct {
     int init_kind;       /* 0 f=0 (reference), 1 f=feq(rho,u) */
     double rho_in, rho_out;
     int periodic[3];     /* physics mode: axes whose out-of-domain pulls wrap */
+    const double *link_q; /* CURVED: wall fraction of every BC link (NULL: all 1/2) */
 } orc_params;
 
 }  // extern "C"
@@ -155,6 +159,7 @@ struct Lattice {
     std::vector<uint64_t> mask;    /* reference BC mask per node */
     std::vector<uint8_t> stream;   /* (q-1)*N, 1 = streamed */
     std::vector<int> bcnodes;      /* collapsed BC node list, ascending */
+    std::vector<T> qc;             /* CURVED: collapsed link fractions, (q-1) per BC node */
     T msc[361];                    /* reference M^-1 S, row-major */
     T mm[361];                     /* reference M */
 
@@ -467,8 +472,30 @@ void stream_all(Lattice<T> &L) {
 
 /* --------------------------- 2D boundaries ------------------------------- */
 
+/* Curved wall (CURVED branch of gpuBcWall2D / gpuBcSimpleWall3D,
+ * GpuBoundaries.cu:414-432, :461-479): the population entering against wall
+ * link dir of BC node number b, from this step's post-collision values.  The
+ * first coefficient of the q < 1/2 branch reads entry b*(q-1)+dir of the
+ * collapsed table, one past the link's own, and the upstream value sits at
+ * the flat index i + dir*N + c(dir) of the SoA array (a neighbouring row, or
+ * another direction's array, where the neighbour is outside the lattice);
+ * past either end of the array the reference's read is undefined, 0 here. */
 template <class T>
-void bc_node_2d(Lattice<T> &L, int i, uint64_t mk) {
+T curved_value(const Lattice<T> &L, int b, int i, int dir) {
+    const size_t N = (size_t)L.N;
+    const int D = L.q - 1;
+    const T *fc = L.fc.data();
+    const T q0 = L.qc[(size_t)b * D + dir - 1];
+    if (q0 < 0.5) {
+        const long long up = (long long)i + (long long)dir * (long long)N + L.off[dir];
+        const T fu = up >= 0 && up < (long long)L.fc.size() ? fc[up] : (T)0;
+        return 2 * L.qc[(size_t)b * D + dir] * fc[i + dir * N] + (1 - 2 * q0) * fu;
+    }
+    return fc[i + dir * N] / 2 / q0 + (2 * q0 - 1) / (2 * q0) * fc[i + (size_t)L.opp(dir) * N];
+}
+
+template <class T>
+void bc_node_2d(Lattice<T> &L, int b, int i, uint64_t mk) {
     const int N = L.N;
     T *f = L.f.data();
     auto F = [&](int d) -> T & { return f[i + (size_t)d * N]; };
@@ -493,7 +520,7 @@ void bc_node_2d(Lattice<T> &L, int i, uint64_t mk) {
      * streaming, in direction order */
     for (int dir = 1; dir < 9; ++dir) {
         uint64_t all = mk & bc2_mask(3, dir), wall = mk & bc2_mask(1, dir);
-        if (all == wall && wall) F(opp2[dir]) = F(dir);
+        if (all == wall && wall) F(opp2[dir]) = L.p.boundary_type == 1 ? curved_value(L, b, i, dir) : F(dir);
     }
     /* east outlet (GpuBoundaries.cu:1562-1653) */
     if ((mk & bc2_mask(3, 1)) == bc2_mask(3, 1)) {
@@ -593,7 +620,7 @@ void zou_he_3d(T *f, size_t N, int i, int face, T uu, T vv, T ww) {
 }
 
 template <class T>
-void bc_node_3d(Lattice<T> &L, int i, uint64_t mk) {
+void bc_node_3d(Lattice<T> &L, int b, int i, uint64_t mk) {
     const size_t N = (size_t)L.N;
     T *f = L.f.data();
     if (!(mk & BC3_FLUID)) return;
@@ -613,7 +640,8 @@ void bc_node_3d(Lattice<T> &L, int i, uint64_t mk) {
     /* straight simple wall (GpuBoundaries.cu:445-490) */
     for (int dir = 1; dir < 19; ++dir) {
         uint64_t all = mk & bc3_mask(7, dir), wall = mk & bc3_mask(1, dir);
-        if (all == wall && wall) f[i + (size_t)opp3[dir] * N] = f[i + (size_t)dir * N];
+        if (all == wall && wall)
+            f[i + (size_t)opp3[dir] * N] = L.p.boundary_type == 1 ? curved_value(L, b, i, dir) : f[i + (size_t)dir * N];
     }
 }
 
@@ -954,7 +982,7 @@ int run(int dims, int n, int m, int h, const int *node_type, int nconn, const in
         uint8_t *out_stream, int *out_count, double *out_resid) {
     if (n < 1 || m < 1 || h < 1 || (dims != 2 && dims != 3)) return ORC_BAD_INPUT;
     if (p->collision_model < 1 || p->collision_model > 3) return ORC_BAD_INPUT;
-    if (p->boundary_type == 1) return ORC_UNSUPPORTED;
+    if (p->boundary_type == 1 && p->mode == 1) return ORC_UNSUPPORTED;
     if (p->bc_wall_model == 2 && p->mode == 1) return ORC_UNSUPPORTED;
     if (dims == 3 && p->mode == 0 && p->collision_model == 2) return ORC_UNSUPPORTED;
     if (dims == 3 && p->inlet_profile == 1) return ORC_UNSUPPORTED;
@@ -975,6 +1003,26 @@ int run(int dims, int n, int m, int h, const int *node_type, int nconn, const in
     L.fluid.assign(node_type, node_type + N);
     int rc = build_masks(L, nconn, bi, bj, bk, bdir, btype, bid);
     if (rc) return rc;
+    if (p->boundary_type == 1 && p->mode == 0) {
+        if (dims == 3 && p->bc_wall_model == 2) {
+            L.p.boundary_type = 2; /* the HH wall kernel has no curved branch */
+        } else {
+            /* per-node table filled with 1/2 (Iterate.cu:277, Iterate3D.cu:364),
+             * link entries q[ind*(q-1)+dir-1] (GpuInit.cu:1088, :1203-1207),
+             * collapsed in BC node order (GpuInit.cu:1125-1155, :1239-1277);
+             * one more node's worth of 1/2 stands for what the reference reads
+             * past the end of its device array */
+            const int D = L.q - 1;
+            std::vector<T> qn((size_t)D * N, (T)0.5);
+            for (int c = 0; c < nconn; ++c) {
+                const int ind = bi[c] + bj[c] * n + (dims == 3 ? bk[c] * n * m : 0);
+                qn[(size_t)ind * D + bdir[c] - 1] = p->link_q ? (T)p->link_q[c] : (T)0.5;
+            }
+            L.qc.assign((L.bcnodes.size() + 1) * (size_t)D, (T)0.5);
+            for (size_t b = 0; b < L.bcnodes.size(); ++b)
+                for (int j = 0; j < D; ++j) L.qc[b * D + j] = qn[(size_t)L.bcnodes[b] * D + j];
+        }
+    }
     if (dims == 3 && p->mode == 0) {
         for (int i : L.bcnodes)
             if ((L.mask[i] & BC3_B_ALL) == BC3_OUTL_B) return ORC_UNSUPPORTED;
@@ -1026,9 +1074,9 @@ int run(int dims, int n, int m, int h, const int *node_type, int nconn, const in
                 zou_he_face(L, i, face, pressure, rset, L.u0[i], L.v0[i], dims == 3 ? L.w0[i] : (T)0);
             }
         } else if (dims == 2) {
-            for (int i : L.bcnodes) bc_node_2d(L, i, L.mask[i]);
+            for (size_t b = 0; b < L.bcnodes.size(); ++b) bc_node_2d(L, (int)b, L.bcnodes[b], L.mask[L.bcnodes[b]]);
         } else {
-            for (int i : L.bcnodes) bc_node_3d(L, i, L.mask[i]);
+            for (size_t b = 0; b < L.bcnodes.size(); ++b) bc_node_3d(L, (int)b, L.bcnodes[b], L.mask[L.bcnodes[b]]);
             if (p->bc_wall_model == 2)
                 for (int i : L.bcnodes) complex_wall_node_3d(L, i, L.mask[i]);
             if (p->mode == 0) {

@@ -30,7 +30,7 @@ class RefParams(C.Structure):
 class OrcParams(C.Structure):
     _fields_ = RefParams._fields_ + [("mode", C.c_int), ("init_kind", C.c_int),
                                      ("rho_in", C.c_double), ("rho_out", C.c_double),
-                                     ("periodic", C.c_int * 3)]
+                                     ("periodic", C.c_int * 3), ("link_q", C.POINTER(C.c_double))]
 
 
 def build_oracle(force=False):
@@ -92,9 +92,10 @@ class Result:
 
 
 def run_oracle(lat, steps, fp64=False, mode=0, init_kind=0, rho_in=1.0, rho_out=1.0,
-               extra_collide=False, init=None, periodic=(0, 0, 0), **kw):
+               extra_collide=False, init=None, periodic=(0, 0, 0), link_q=None, **kw):
     """Run the oracle restatement; returns a Result with f, fc (q, N), rho,
-    u, v, w (N), mask, stream, count, resid, rc."""
+    u, v, w (N), mask, stream, count, resid, rc.  link_q: curved walls' link
+    fractions, one per BC link (boundary_type=1)."""
     L = oracle_lib()
     q = lat.q
     nn = lat.num_nodes
@@ -102,6 +103,10 @@ def run_oracle(lat, steps, fp64=False, mode=0, init_kind=0, rho_in=1.0, rho_out=
                                 rho_in=rho_in, rho_out=rho_out))
     for a in range(3):
         p.periodic[a] = int(periodic[a])
+    lq = None
+    if link_q is not None:
+        lq = np.ascontiguousarray(link_q, np.float64)
+        p.link_q = lq.ctypes.data_as(C.POINTER(C.c_double))
     cols = _cols(lat)
     r = Result()
     r.f, r.fc = np.zeros(q * nn), np.zeros(q * nn)
@@ -124,9 +129,50 @@ def run_oracle(lat, steps, fp64=False, mode=0, init_kind=0, rho_in=1.0, rho_out=
     return r
 
 
-def run_reference(lat, steps, fp64=False, **kw):
+def curved_bc_points(lat, link_q, delta=1.0):
+    """BC-file boundary points that give the links the fractions link_q:
+    node + q delta c_dir (the reference's q = |B - X| / (delta |c_dir|))."""
+    from thesis_gb300.lattice import CX2, CX3, CY2, CY3, CZ3
+    cols = _cols(lat)
+    x, y, z = lat.coords(delta)
+    ind = cols[0] + lat.n * (cols[1] + lat.m * cols[2])
+    d = cols[3]
+    if lat.q == 9:
+        cx, cy, cz = CX2[d], CY2[d], np.zeros(d.size)
+    else:
+        cx, cy, cz = CX3[d], CY3[d], CZ3[d]
+    qv = np.asarray(link_q, np.float64) * delta
+    return x[ind] + qv * cx, y[ind] + qv * cy, z[ind] + qv * cz
+
+
+def reference_q(lat, link_q, delta=1.0, fp64=False):
+    """The link fractions the reference derives from the BC points that
+    curved_bc_points writes: sqrt(dx^2 + dy^2 [+ dz^2]) / (delta qLat) in its
+    FLOAT_TYPE (GpuInit.cu:1084-1088, :1199-1207), qLat = sqrt(2) rounded
+    to FLOAT_TYPE on the diagonals."""
+    from thesis_gb300.lattice import CX2, CX3, CY2, CY3, CZ3
+    t = np.float64 if fp64 else np.float32
+    cols = _cols(lat)
+    x, y, z = lat.coords(delta)
+    ind = cols[0] + lat.n * (cols[1] + lat.m * cols[2])
+    bx, by, bz = curved_bc_points(lat, link_q, delta)
+    dx = t(bx) - t(x[ind])
+    dy = t(by) - t(y[ind])
+    s2 = dx * dx + dy * dy
+    if lat.dims == 3:
+        dz = t(bz) - t(z[ind])
+        s2 = s2 + dz * dz
+        diag = (np.abs(CX3) + np.abs(CY3) + np.abs(CZ3))[cols[3]] == 2
+    else:
+        diag = (np.abs(CX2) + np.abs(CY2))[cols[3]] == 2
+    qlat = np.where(diag, t(np.sqrt(2.0)), t(1.0)).astype(t)
+    return (np.sqrt(s2).astype(t) / (t(delta) * qlat)).astype(np.float64)
+
+
+def run_reference(lat, steps, fp64=False, link_q=None, **kw):
     """Run the reference's own kernels on the host (oracle/_ref).  Returns
-    None when oracle/_ref has not been built on this machine."""
+    None when oracle/_ref has not been built on this machine.  link_q: curved
+    walls' link fractions, passed as BC-file boundary points."""
     L = ref_lib(fp64)
     if L is None:
         return None
@@ -139,6 +185,8 @@ def run_reference(lat, steps, fp64=False, **kw):
     bx = np.ascontiguousarray(x[cols[0] + lat.n * (cols[1] + lat.m * cols[2])] if len(cols[0]) else np.zeros(0))
     by = np.ascontiguousarray(y[cols[0] + lat.n * (cols[1] + lat.m * cols[2])] if len(cols[0]) else np.zeros(0))
     bz = np.ascontiguousarray(z[cols[0] + lat.n * (cols[1] + lat.m * cols[2])] if len(cols[0]) else np.zeros(0))
+    if link_q is not None:
+        bx, by, bz = (np.ascontiguousarray(a, np.float64) for a in curved_bc_points(lat, link_q, kw.get("delta", 1.0)))
     r = Result()
     r.f, r.fc = np.zeros(q * nn), np.zeros(q * nn)
     r.rho, r.u, r.v, r.w = (np.zeros(nn) for _ in range(4))

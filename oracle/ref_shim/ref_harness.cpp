@@ -179,7 +179,9 @@ int ref_run2d(int n, int m, const int *node_type, const double *node_x, const do
                                            stream.data(), btype.data(), bcMask.data(), bcIdx.data(),
                                            mask.data(), (FLOAT_TYPE)p->delta, m, n, num_conns);
     std::vector<int> bcIdxC(bcCount > 0 ? bcCount : 1), bcMaskC(bcCount > 0 ? bcCount : 1);
-    std::vector<FLOAT_TYPE> qC(8 * (size_t)(bcCount > 0 ? bcCount : 1));
+    /* one node's worth of 1/2 past the collapsed table: the curved wall's
+     * first coefficient reads one entry ahead, past the end for the last node */
+    std::vector<FLOAT_TYPE> qC(8 * (size_t)((bcCount > 0 ? bcCount : 1) + 1), (FLOAT_TYPE)0.5);
     collapseBc2D(bcIdx.data(), bcIdxC.data(), bcMask.data(), bcMaskC.data(), q.data(), qC.data(),
                  mask.data(), m, n, bcCount);
     shim_dim3 bpgB{(unsigned)(bcCount / THREADS) + 1, 1, 1};
@@ -285,7 +287,7 @@ int ref_run3d(int n, int m, int h, const int *node_type, const double *node_x,
     int cap = bcCount > 0 ? bcCount : 1;
     std::vector<int> bcIdxC(cap);
     std::vector<unsigned long long> bcMaskC(cap);
-    std::vector<FLOAT_TYPE> qC(18 * (size_t)cap);
+    std::vector<FLOAT_TYPE> qC(18 * (size_t)(cap + 1), (FLOAT_TYPE)0.5); /* as in 2D: one node past the end */
     collapseBc3D(bcIdx.data(), bcIdxC.data(), bcMask.data(), bcMaskC.data(), q.data(), qC.data(),
                  mask.data(), m, n, h, bcCount, args.boundaryType);
     unsigned sideB = (unsigned)(sqrt((double)bcCount) / THREADS) + 1;

@@ -38,7 +38,25 @@ def cases():
                 dict(u=0.05, viscosity=0.1, collision_model=1), 12))
     out.append(("per_x_chan3d_10x9x8_hh_mrt", ("periodic_channel3d", (10, 9, 8)),
                 dict(u=0.05, viscosity=0.1, collision_model=3, bc_wall_model=2), 12))
+    # curved (q-interpolated) walls: BC points at the exact cylinder / sphere
+    # intersections, q = 0.3 on the outer walls
+    for coll, tag in ((1, "bgk"), (2, "trt"), (3, "mrt")):
+        out.append(("curved_cyl2d_48x24_" + tag, ("cylinder_channel2d", (48, 24, None, None, 0.3)),
+                    dict(u=0.05, viscosity=0.05, collision_model=coll, outlet_profile=1, boundary_type=1), 30))
+    for coll, tag in ((1, "bgk"), (3, "mrt")):
+        out.append(("curved_sph3d_14x12x12_" + tag, ("sphere_cavity3d", (14, 12, 12, None, None, 0.3)),
+                    dict(u=0.05, viscosity=0.1, collision_model=coll, boundary_type=1), 12))
     return out
+
+
+def link_q_kwargs(lat, kw, oracle_side, fp64=False):
+    """Curved cases: the reference gets the BC points of lat.link_q, the
+    oracle the fractions the reference computes from them."""
+    if kw.get("boundary_type") != 1:
+        return {}
+    if oracle_side:
+        return dict(link_q=pyoracle.reference_q(lat, lat.link_q, fp64=fp64))
+    return dict(link_q=lat.link_q)
 
 
 def make_lattice(spec):
@@ -47,7 +65,8 @@ def make_lattice(spec):
 
 
 def bc_hash(lat):
-    return hashlib.sha256(np.ascontiguousarray(lat.bc).tobytes() + lat.node_type.tobytes()).hexdigest()
+    extra = np.ascontiguousarray(lat.link_q).tobytes() if hasattr(lat, "link_q") else b""
+    return hashlib.sha256(np.ascontiguousarray(lat.bc).tobytes() + lat.node_type.tobytes() + extra).hexdigest()
 
 
 def main():
@@ -56,7 +75,7 @@ def main():
     store = {}
     for name, spec, kw, steps in cases():
         lat = make_lattice(spec)
-        r = pyoracle.run_reference(lat, steps, fp64=False, **kw)
+        r = pyoracle.run_reference(lat, steps, fp64=False, **kw, **link_q_kwargs(lat, kw, False))
         assert r.rc == 0, name
         store[name + "/f"] = r.f.astype(np.float32)
         store[name + "/fc"] = r.fc.astype(np.float32)

@@ -67,8 +67,11 @@ def test_physics_words_block_solid_and_outside(native_lib):
 def test_unsupported_reference_features_are_refused(native_lib):
     lat = lattice.cavity3d(6)
     with pytest.raises(N.LbmError) as e:
-        build_flags(lat, Arguments(boundary_type=N.CURVED))
+        build_flags(lat, Arguments(boundary_type=N.CURVED, mode=N.MODE_PHYSICS))
     assert e.value.code == N.LBM_ERR_UNSUPPORTED
+    with pytest.raises(N.LbmError) as e:
+        build_flags(lat, Arguments(boundary_type=7))
+    assert e.value.code == N.LBM_ERR_INVALID
     bc = lat.bc.copy()
     bc[bc[:, 4] == 2, 4] = 3  # lid links become outlet links
     lat2 = lattice.Lattice(3, 6, 6, 6, lat.node_type, bc)
@@ -98,6 +101,49 @@ def test_hh_walls_and_periodic_links_reference_mode(native_lib):
     mask_p, word_p, _, _ = build_flags(per, Arguments())
     cycl = (mask_p >> np.uint64(54)) & np.uint64(4)
     assert np.all(((word_p >> 19) & 1)[cycl != 0] == 1)
+
+
+def test_curved_walls_give_every_wall_node_a_slot(native_lib):
+    """Reference curved walls: every fluid node with a wall link takes the
+    boundary path (a slot), the masks stay the reference's; with the HH wall
+    model the reference has no curved branch and the words equal the HH
+    build's."""
+    for lat in (lattice.cylinder_channel2d(32, 16), lattice.sphere_cavity3d(10, 9, 9)):
+        mask, word, slot, nbc = build_flags(lat, Arguments(boundary_type=N.CURVED, outlet_profile=N.OUTLET_ZOUHE))
+        mask_s, word_s, _, _ = build_flags(lat, Arguments(outlet_profile=N.OUTLET_ZOUHE))
+        np.testing.assert_array_equal(mask, mask_s)
+        special = ((word >> 19) & 1) == 1
+        bits, wall = (2, 1) if lat.dims == 2 else (3, 1)
+        has_wall = np.zeros(lat.num_nodes, bool)
+        for d in range(1, lat.q):
+            t = (mask >> np.uint64((d - 1) * bits)) & np.uint64((1 << bits) - 1)
+            has_wall |= t == wall
+        fluid = lat.node_type == 1
+        assert np.all(special[has_wall & fluid])
+        assert special.sum() > (((word_s >> 19) & 1) == 1).sum()
+        assert np.all(slot[special] >= 0)
+    lat = lattice.sphere_cavity3d(10, 9, 9)
+    w_hh = build_flags(lat, Arguments(boundary_type=N.CURVED, bc_wall_model=N.WALL_COMPLEX))[1]
+    np.testing.assert_array_equal(w_hh, build_flags(lat, Arguments(bc_wall_model=N.WALL_COMPLEX))[1])
+
+
+def test_link_q_from_coordinates(native_lib, oracle):
+    """lbm_link_q restates the reference's q = |B - X| / (delta |c_dir|)
+    (GpuInit.cu:1086-1088, :1203-1207) in FP64: the fractions of BC points
+    placed at q along each link come back to FP32 coordinate rounding."""
+    from thesis_gb300.solver import link_q
+    for lat, delta in ((lattice.cylinder_channel2d(32, 16), 0.01), (lattice.sphere_cavity3d(10, 9, 9), 1 / 9)):
+        bx, by, bz = oracle.curved_bc_points(lat, lat.link_q, delta)
+        x, y, z = lat.coords(delta)
+        cols = (np.stack([bx, by], 1), np.stack([x, y], 1)) if lat.dims == 2 else \
+            (np.stack([bx, by, bz], 1), np.stack([x, y, z], 1))
+        q = link_q(lat, cols[0], cols[1], delta)
+        np.testing.assert_allclose(q, lat.link_q, atol=2e-5)
+        np.testing.assert_allclose(q, oracle.reference_q(lat, lat.link_q, delta, fp64=False), rtol=1e-5, atol=1e-6)
+    lat = lattice.cylinder_channel2d(32, 16)
+    with pytest.raises(N.LbmError) as e:
+        link_q(lat, np.zeros((lat.bc.shape[0], 2)), np.zeros((lat.num_nodes, 2)), 0.0)
+    assert e.value.code == N.LBM_ERR_INVALID
 
 
 def test_invalid_links_are_rejected(native_lib):

@@ -15,6 +15,8 @@ Tolerances (stated per storage type):
 The GPU state after k steps is the post-collision field the next step
 streams, i.e. the oracle's state after k steps followed by one collision.
 """
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -27,10 +29,13 @@ pytestmark = pytest.mark.gpu
 TOL = {N.STORE_F64: 1e-10, N.STORE_F32: 2e-5}
 
 
-def run_pair(oracle, lat, args, steps, init=None):
-    """Run GPU and oracle; return (gpu dict, oracle Result)."""
+def run_pair(oracle, lat, args, steps, init=None, link_q=None):
+    """Run GPU and oracle; return (gpu dict, oracle Result).  link_q: the
+    curved walls' link fractions (boundary_type CURVED)."""
     fluid = lat.node_type == 1
     with Solver(lat, args) as s:
+        if link_q is not None:
+            s.set_link_q(link_q)
         if init is not None:
             s.init(*init)
         else:
@@ -41,10 +46,10 @@ def run_pair(oracle, lat, args, steps, init=None):
     okw = dict(u=args.u, v=args.v, w=args.w, rho=args.rho, viscosity=args.viscosity, g=args.g,
                inlet_profile=args.inlet_profile, outlet_profile=args.outlet_profile,
                collision_model=args.collision_model, update_inlet_outlet=args.update_inlet_outlet,
-               bc_wall_model=args.bc_wall_model)
+               bc_wall_model=args.bc_wall_model, boundary_type=args.boundary_type)
     r = oracle.run_oracle(lat, steps, fp64=args.storage == N.STORE_F64, mode=args.mode,
                           init_kind=args.init_equilibrium, rho_in=args.rho_in, rho_out=args.rho_out,
-                          extra_collide=True, init=init, periodic=args.periodic, **okw)
+                          extra_collide=True, init=init, periodic=args.periodic, link_q=link_q, **okw)
     assert r.rc == 0
     g = dict(rho=rho.astype(np.float64), u=u.astype(np.float64), v=v.astype(np.float64),
              w=w.astype(np.float64), f=f)
@@ -135,6 +140,87 @@ def test_reference_periodic_hh_every_kernel_form(oracle, monkeypatch, variant):
     g, r, fl = run_pair(oracle, lattice.periodic_channel3d(14, 12, 10), args, 20)
     monkeypatch.delenv("THESIS_LBM_KERNEL", raising=False)
     compare(g, r, fl, N.STORE_F32, 3)
+
+
+CURVED_CASES = {
+    "cylinder2d": lambda: lattice.cylinder_channel2d(48, 24, outer_q=0.3),
+    "sphere3d": lambda: lattice.sphere_cavity3d(14, 12, 12, outer_q=0.3),
+}
+
+
+@pytest.mark.parametrize("case", sorted(CURVED_CASES))
+@pytest.mark.parametrize("coll", [N.BGKW, N.TRT, N.MRT])
+@pytest.mark.parametrize("storage", [N.STORE_F32, N.STORE_F64, N.STORE_F16S])
+def test_reference_curved_walls(oracle, case, coll, storage):
+    """The reference's q-interpolated walls (both branches, q from the exact
+    cylinder / sphere intersections, q = 0.3 on the outer walls) against the
+    oracle, which matches the reference's kernels bit for bit on these
+    lattices."""
+    lat = CURVED_CASES[case]()
+    if lat.dims == 3 and coll == N.TRT:
+        pytest.skip("the reference has no 3D TRT")
+    args = Arguments(u=0.05, viscosity=0.05 if lat.dims == 2 else 0.1, collision_model=coll,
+                     outlet_profile=N.OUTLET_ZOUHE, boundary_type=N.CURVED, storage=storage,
+                     init_equilibrium=1)
+    g, r, fl = run_pair(oracle, lat, args, 30, link_q=lat.link_q)
+    compare(g, r, fl, storage, lat.dims)
+
+
+@pytest.mark.parametrize("variant", ["jith", "jiths", "jitf", "scalar", "jithz4", "pair"])
+def test_reference_curved_walls_every_kernel_form(oracle, monkeypatch, variant):
+    """The interpolation runs in the shared boundary code of the one-node
+    f-space, storage-unit and z-walk kernels; the two-node kernels have no
+    curved path, so a request for them falls back to a one-node kernel."""
+    monkeypatch.setenv("THESIS_LBM_KERNEL", variant)
+    lat = CURVED_CASES["sphere3d"]()
+    args = Arguments(u=0.05, viscosity=0.1, collision_model=N.MRT, boundary_type=N.CURVED, init_equilibrium=1)
+    g, r, fl = run_pair(oracle, lat, args, 20, link_q=lat.link_q)
+    monkeypatch.delenv("THESIS_LBM_KERNEL", raising=False)
+    compare(g, r, fl, N.STORE_F32, 3)
+
+
+def test_reference_curved_walls_default_q_and_update(oracle):
+    """Before lbm_set_link_q every fraction is 1/2 (the reference's fill
+    value); new fractions take effect from the next step."""
+    lat = CURVED_CASES["cylinder2d"]()
+    args = Arguments(u=0.05, viscosity=0.05, collision_model=N.BGKW, outlet_profile=N.OUTLET_ZOUHE,
+                     boundary_type=N.CURVED, init_equilibrium=1)
+    g, r, fl = run_pair(oracle, lat, args, 20)
+    compare(g, r, fl, N.STORE_F32, 2)
+    half = np.full(lat.bc.shape[0], 0.5)
+    with Solver(lat, args) as s:
+        s.set_link_q(half)
+        s.init()
+        s.step(20, write_macro=True)
+        fa = s.populations()
+    assert np.array_equal(fa, g["f"])
+    with Solver(lat, dataclasses.replace(args, boundary_type=N.STRAIGHT)) as s:
+        s.init()
+        s.step(20, write_macro=True)
+        fs = s.populations()
+    # q = 1/2 returns the node's own post-collision population, the straight
+    # wall the streamed one
+    assert np.abs(fs - fa).max() > 1e-4
+
+
+def test_reference_curved_walls_l2_residual(oracle):
+    """The L2 residual recomputes the boundary conditions, curved walls
+    included."""
+    lat = CURVED_CASES["cylinder2d"]()
+    args = Arguments(u=0.05, viscosity=0.05, collision_model=N.MRT, outlet_profile=N.OUTLET_ZOUHE,
+                     boundary_type=N.CURVED, init_equilibrium=1)
+    k = 30
+    with Solver(lat, args) as s:
+        s.set_link_q(lat.link_q)
+        s.init()
+        s.step(k, write_macro=True)
+        r_gpu, rc = s.residual_l2()
+        assert rc == N.LBM_OK
+    r = oracle.run_oracle(lat, k + 1, init_kind=1, link_q=lat.link_q, u=args.u, viscosity=args.viscosity,
+                          outlet_profile=args.outlet_profile, collision_model=args.collision_model,
+                          boundary_type=N.CURVED)
+    assert r.rc == 0
+    assert abs(r_gpu - r.resid[k]) <= 1e-4 * r.resid[k] + 1e-6, (r_gpu, r.resid[k])
 
 
 def test_reference_cavity3d_gravity_no_inlet_update(oracle):

@@ -24,7 +24,7 @@ def test_oracle_matches_reference_golden(oracle, golden, case):
     lat = make_golden.make_lattice(spec)
     assert bytes(golden[name + "/lattice_sha256"]).decode() == make_golden.bc_hash(lat), \
         "lattice builder changed since the fixture was made"
-    r = oracle.run_oracle(lat, steps, fp64=False, **kw)
+    r = oracle.run_oracle(lat, steps, fp64=False, **kw, **make_golden.link_q_kwargs(lat, kw, True))
     assert r.rc == 0
     np.testing.assert_array_equal(r.mask, golden[name + "/mask"])
     np.testing.assert_array_equal(r.stream, golden[name + "/stream"])

@@ -54,9 +54,7 @@ int compare(const char *a, const char *b) {
 // Inlet extent for the 2D parabolic profile, as the reference finds it
 // (FilesReading.cu:473-606): grid spacing from nodes (0,0) and (1,0), inlet
 // links of directions 1-4, extended by half a spacing.
-void inlet_extent(const std::vector<int> &ni, const std::vector<int> &nj, const std::vector<float> &nx,
-                  const std::vector<int> &type, const std::vector<int> &dir, const std::vector<float> &by,
-                  float &ymin, float &ymax) {
+float grid_spacing(const std::vector<int> &ni, const std::vector<int> &nj, const std::vector<float> &nx) {
     float d1 = 0, d2 = 0;
     for (size_t i = 0; i < ni.size(); ++i)
         if (ni[i] == 0 && nj[i] == 0) {
@@ -68,7 +66,13 @@ void inlet_extent(const std::vector<int> &ni, const std::vector<int> &nj, const 
             d2 = nx[i];
             break;
         }
-    const float delta = fabsf(d2 - d1);
+    return fabsf(d2 - d1);
+}
+
+void inlet_extent(const std::vector<int> &ni, const std::vector<int> &nj, const std::vector<float> &nx,
+                  const std::vector<int> &type, const std::vector<int> &dir, const std::vector<float> &by,
+                  float &ymin, float &ymax) {
+    const float delta = grid_spacing(ni, nj, nx);
     bool any = false;
     for (size_t i = 0; i < type.size(); ++i)
         if (type[i] == LBM_BC_INLET && dir[i] >= 1 && dir[i] <= 4) {
@@ -157,6 +161,10 @@ int main(int argc, char **argv) {
         fprintf(stderr, "physics mode: walls are half-way bounce-back (BCwallModel HHmodel ignored)\n");
         p.bc_wall_model = LBM_WALL_SIMPLE;
     }
+    if (mode == LBM_MODE_PHYSICS && p.boundary_type == LBM_CURVED) {
+        fprintf(stderr, "physics mode: walls are half-way bounce-back (BoundaryType CURVED ignored)\n");
+        p.boundary_type = LBM_STRAIGHT;
+    }
     p.update_inlet_outlet = cfg.update_inlet_outlet;
     p.mode = mode;
     p.storage = storage;
@@ -166,6 +174,20 @@ int main(int argc, char **argv) {
     if (lbm_create(&lat, &p, &hd) != LBM_OK) {
         fprintf(stderr, "%s\n", lbm_last_error());
         return 3;
+    }
+    if (p.boundary_type == LBM_CURVED && !(dims == 3 && p.bc_wall_model == LBM_WALL_COMPLEX)) {
+        // link fractions from the BC file's boundary points and the node
+        // coordinates (initBoundaryConditions2D/3D; the reference's HH wall
+        // kernel has no curved branch)
+        std::vector<double> q((size_t)nc);
+        if (lbm_link_q(dims, n, m, h, (int)nc, bi.data(), bj.data(), dims == 3 ? bk.data() : nullptr, bd.data(),
+                       bx.data(), by.data(), dims == 3 ? bz.data() : nullptr, x.data(), y.data(),
+                       dims == 3 ? z.data() : nullptr, grid_spacing(ni, nj, x), q.data()) != LBM_OK ||
+            lbm_set_link_q(hd, q.data()) != LBM_OK) {
+            fprintf(stderr, "%s\n", lbm_last_error());
+            lbm_destroy(hd);
+            return 3;
+        }
     }
     const long long N = nn;
     std::vector<float> rho(N), u(N), v(N), w(N);

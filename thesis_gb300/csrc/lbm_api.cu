@@ -7,6 +7,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <map>
 #include <mutex>
 #include <new>
@@ -90,6 +91,13 @@ struct lbm_handle_s {
     double *partial = nullptr, *norms = nullptr;
     int nslots = 0;
     std::vector<long long> slot_node;
+    // reference curved walls: per slot Q link fractions on the device (null
+    // for straight walls), the boundary nodes in ascending order (the
+    // reference's collapsed order) and, per BC link, its node's place there
+    double *bcq = nullptr;
+    std::vector<long long> bc_nodes;
+    std::vector<int> link_b;
+    std::vector<unsigned char> link_dir;
     int cur = 0;
     cudaStream_t stream = nullptr;
     // recorded after the steps of every lbm_step, on the stream they ran on;
@@ -125,6 +133,7 @@ static StepParams make_params(const lbm_handle_s *H, int from, int write_macro) 
     p.bc_mask = H->mask;
     p.bc_kind = H->kind;
     p.bc_uvw = H->uvw;
+    p.bc_q = H->bcq;
     p.rho = H->rho;
     p.ux = H->ux;
     p.uy = H->uy;
@@ -161,7 +170,8 @@ static void free_handle(lbm_handle_s *H) {
         if (H->pair[c]) cudaGraphExecDestroy(H->pair[c]);
     void *ptrs[] = {H->fbuf[0], H->fbuf[1], H->word, H->slot, H->mask, H->kind, H->uvw,
                     H->rho, H->ux, H->uy, H->uz, H->pux, H->puy, H->puz, H->partial, H->norms,
-                    H->tma_row, H->tma_lmask, H->tma_omask, H->tma_err, H->mdiff_prev, H->fd_snap};
+                    H->tma_row, H->tma_lmask, H->tma_omask, H->tma_err, H->mdiff_prev, H->fd_snap,
+                    H->bcq};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (H->stepped) cudaEventDestroy(H->stepped);
@@ -407,7 +417,8 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
         // the run-time build is unavailable.  THESIS_LBM_KERNEL=scalar|pair|
         // tma|jit selects a variant explicitly (jit then fails loudly).
         const char *kv = getenv("THESIS_LBM_KERNEL");
-        const bool can_pair = (L->n % 2 == 0) && P->storage != LBM_STORE_F64;
+        // the two-node kernels have no curved-wall path
+        const bool can_pair = (L->n % 2 == 0) && P->storage != LBM_STORE_F64 && !curved_walls(*P, q);
         H->pair_kernel = kv && strcmp(kv, "pair") == 0 && can_pair;
         want_tma = kv && strcmp(kv, "tma") == 0;
         // jithz<k>[b<block>][m<min blocks>]: storage units walking k nodes along z
@@ -462,6 +473,7 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     ALLOC(H->mask, sizeof(unsigned long long) * H->nslots);
     ALLOC(H->kind, sizeof(int32_t) * H->nslots);
     ALLOC(H->uvw, sizeof(double) * 3 * H->nslots);
+    if (curved_walls(*P, q)) ALLOC(H->bcq, sizeof(double) * q * H->nslots);
     ALLOC(H->rho, sizeof(float) * N);
     ALLOC(H->ux, sizeof(float) * N);
     ALLOC(H->uy, sizeof(float) * N);
@@ -491,6 +503,20 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
         if (e == cudaSuccess)
             e = cudaMemcpy(H->uvw, uvw.data(), sizeof(double) * 3 * H->nslots, cudaMemcpyHostToDevice);
     }
+    if (e == cudaSuccess && H->bcq) {
+        // every link fraction starts at the reference's fill value 1/2
+        // (Iterate.cu:277, Iterate3D.cu:364) until lbm_set_link_q
+        H->bc_nodes = refm.bc_nodes;
+        H->link_b.resize((size_t)L->num_conns);
+        H->link_dir.resize((size_t)L->num_conns);
+        for (int c = 0; c < L->num_conns; ++c) {
+            const long long ind = L->bc_i[c] + (long long)L->n * (L->bc_j[c] + (long long)L->m * (L->dims == 3 ? L->bc_k[c] : 0));
+            H->link_b[c] = (int)(std::lower_bound(H->bc_nodes.begin(), H->bc_nodes.end(), ind) - H->bc_nodes.begin());
+            H->link_dir[c] = (unsigned char)L->bc_dir[c];
+        }
+        std::vector<double> qt((size_t)q * H->nslots, 0.5);
+        if (H->nslots) e = cudaMemcpy(H->bcq, qt.data(), sizeof(double) * qt.size(), cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaMemset(H->pux, 0, sizeof(float) * N);
     if (e == cudaSuccess) e = cudaMemset(H->puy, 0, sizeof(float) * N);
     if (e == cudaSuccess) e = cudaMemset(H->puz, 0, sizeof(float) * N);
@@ -514,6 +540,62 @@ int lbm_set_inlet_velocity(lbm_handle H, const float *u, const float *v, const f
     }
     CUDA_TRY(cudaMemcpyAsync(H->uvw, uvw.data(), sizeof(double) * 3 * H->nslots, cudaMemcpyHostToDevice, H->stream));
     CUDA_TRY(cudaStreamSynchronize(H->stream));
+    return LBM_OK;
+}
+
+int lbm_set_link_q(lbm_handle H, const double *q) {
+    if (!H || !q) return fail(LBM_ERR_INVALID, "null argument");
+    if (!H->bcq)
+        return fail(LBM_ERR_UNSUPPORTED, "link fractions need reference-mode curved walls (LBM_CURVED with the "
+                                         "simple wall model)");
+    const int Q = H->q, D = Q - 1;
+    const size_t nb = H->bc_nodes.size();
+    // the reference's per-node table q[node * D + dir - 1], unset links 1/2
+    // (initBoundaryConditions2D/3D, GpuInit.cu:1086-1088, :1203-1207)
+    std::vector<double> tab(nb * D, 0.5);
+    for (size_t c = 0; c < H->link_b.size(); ++c) {
+        if (!std::isfinite(q[c])) return fail(LBM_ERR_INVALID, "link fraction " + std::to_string(c) + " is not finite");
+        tab[(size_t)H->link_b[c] * D + H->link_dir[c] - 1] = q[c];
+    }
+    // per slot: the node's D entries, then the entry that follows them in the
+    // collapsed table (collapseBc2D/3D): the next boundary node's first, and
+    // past the last node (where the reference reads beyond its array) 1/2
+    std::vector<double> qt((size_t)Q * H->nslots);
+    for (int s = 0; s < H->nslots; ++s) {
+        const size_t b = (size_t)(std::lower_bound(H->bc_nodes.begin(), H->bc_nodes.end(), H->slot_node[s]) -
+                                  H->bc_nodes.begin());
+        for (int j = 0; j < D; ++j) qt[(size_t)s * Q + j] = tab[b * D + j];
+        qt[(size_t)s * Q + D] = b + 1 < nb ? tab[(b + 1) * D] : 0.5;
+    }
+    if (!H->nslots) return LBM_OK;
+    CUDA_TRY(cudaStreamWaitEvent(H->stream, H->stepped, 0));
+    CUDA_TRY(cudaMemcpyAsync(H->bcq, qt.data(), sizeof(double) * qt.size(), cudaMemcpyHostToDevice, H->stream));
+    CUDA_TRY(cudaStreamSynchronize(H->stream));
+    return LBM_OK;
+}
+
+int lbm_link_q(int dims, int n, int m, int h, int num_conns, const int *bc_i, const int *bc_j, const int *bc_k,
+               const int *bc_dir, const float *bc_x, const float *bc_y, const float *bc_z, const float *node_x,
+               const float *node_y, const float *node_z, double delta, double *q) {
+    if (dims != 2 && dims != 3) return fail(LBM_ERR_INVALID, "dims must be 2 or 3");
+    if (num_conns < 0 || (num_conns > 0 && (!bc_i || !bc_j || !bc_dir || !bc_x || !bc_y || !node_x || !node_y || !q)))
+        return fail(LBM_ERR_INVALID, "null argument");
+    if (dims == 3 && num_conns > 0 && (!bc_k || !bc_z || !node_z)) return fail(LBM_ERR_INVALID, "null argument");
+    if (!(delta > 0)) return fail(LBM_ERR_INVALID, "grid spacing must be positive");
+    const int Q = dims == 2 ? 9 : 19;
+    const int hh = dims == 2 ? 1 : h;
+    for (int c = 0; c < num_conns; ++c) {
+        const int i = bc_i[c], j = bc_j[c], k = dims == 3 ? bc_k[c] : 0, d = bc_dir[c];
+        if (i < 0 || i >= n || j < 0 || j >= m || k < 0 || k >= hh || d < 1 || d >= Q)
+            return fail(LBM_ERR_INVALID, "BC link " + std::to_string(c) + " out of range");
+        const long long ind = i + (long long)n * (j + (long long)m * k);
+        const double dx = (double)bc_x[c] - node_x[ind], dy = (double)bc_y[c] - node_y[ind];
+        const double dz = dims == 3 ? (double)bc_z[c] - node_z[ind] : 0.0;
+        // |c_d|: 1 on the axes, sqrt(2) on the diagonals (qLat, GpuInit.cu:1063-1064, :1173-1176)
+        const int cc = lattice_cx(Q, d) * lattice_cx(Q, d) + lattice_cy(Q, d) * lattice_cy(Q, d) +
+                       lattice_cz(Q, d) * lattice_cz(Q, d);
+        q[c] = std::sqrt(dx * dx + dy * dy + dz * dz) / (delta * std::sqrt((double)cc));
+    }
     return LBM_OK;
 }
 

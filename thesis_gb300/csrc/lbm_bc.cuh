@@ -19,11 +19,12 @@ constexpr uint64_t R3_WALL_B = 1ull << 54, R3_INLT_B = 2ull << 54, R3_OUTL_B = 3
 // ---------------------------------------------------------------------------
 // Reference semantics, D2Q9: gpuBcInlet2D, gpuBcWall2D (straight), and the
 // Zou-He branch of gpuBcOutlet2D (GpuBoundaries.cu:12-71, :400-443,
-// :1562-1602), in that order, on the node's streamed populations.
+// :1562-1602), in that order, on the node's streamed populations.  CURVED:
+// a wall link dir sets f_opp(dir) to cv[dir] (ref_curved) instead of f[dir].
 // ---------------------------------------------------------------------------
-template <class R>
+template <class R, bool CURVED = false>
 __device__ __forceinline__ void bc_ref_d2q9(R (&f)[9], uint32_t mk, R u0, int outlet_profile,
-                                            bool &zero_v) {
+                                            bool &zero_v, const R *cv = nullptr) {
     if (!(mk & R2_FLUID)) return;
     if (mk & R2_INLT_B) {
         if ((mk & m2(2, 2)) && !(mk & R2_CORNER)) {  // north (lid)
@@ -41,7 +42,7 @@ __device__ __forceinline__ void bc_ref_d2q9(R (&f)[9], uint32_t mk, R u0, int ou
     }
 #pragma unroll
     for (int dir = 1; dir < 9; ++dir)
-        if ((mk & m2(3, dir)) == m2(1, dir)) f[Lat<9>::opp(dir)] = f[dir];
+        if ((mk & m2(3, dir)) == m2(1, dir)) f[Lat<9>::opp(dir)] = CURVED ? cv[dir] : f[dir];
     if ((mk & m2(3, 1)) == m2(3, 1)) {  // east outlet
         if (outlet_profile == LBM_OUTLET_ZOUHE) {
             const R r = (f[0] + f[2] + f[4] + (R)2 * (f[1] + f[5] + f[8])) / ((R)1 - u0);
@@ -282,9 +283,11 @@ __device__ __forceinline__ void hh_wall3(R (&f)[19], uint64_t mk) {
 }
 
 // gpuBcInlet3D faces W, E, S, N, B, T (GpuBoundaries.cu:92-394) and the
-// straight walls of gpuBcSimpleWall3D (:445-490) or the HH wall.
-template <class R>
-__device__ __forceinline__ void bc_ref3_inlet_wall(R (&f)[19], uint64_t mk, R uu, R vv, R ww, bool hh) {
+// straight walls of gpuBcSimpleWall3D (:445-490) or the HH wall.  CURVED:
+// the simple wall's curved branch, f_opp(dir) = cv[dir] (ref_curved).
+template <class R, bool CURVED = false>
+__device__ __forceinline__ void bc_ref3_inlet_wall(R (&f)[19], uint64_t mk, R uu, R vv, R ww, bool hh,
+                                                   const R *cv = nullptr) {
     if (!(mk & R3_FLUID)) return;
     if (mk & R3_INLT_B) {
         const int faces[6] = {2, 1, 4, 3, 6, 5};
@@ -301,7 +304,7 @@ __device__ __forceinline__ void bc_ref3_inlet_wall(R (&f)[19], uint64_t mk, R uu
     } else {
 #pragma unroll
         for (int dir = 1; dir < 19; ++dir)
-            if ((mk & m3(7, dir)) == m3(1, dir)) f[Lat<19>::opp(dir)] = f[dir];
+            if ((mk & m3(7, dir)) == m3(1, dir)) f[Lat<19>::opp(dir)] = CURVED ? cv[dir] : f[dir];
     }
 }
 

@@ -137,6 +137,11 @@ static int face_of_link(int q, int dir) {
     return -1;
 }
 
+bool curved_walls(const lbm_params &P, int q) {
+    return P.mode != LBM_MODE_PHYSICS && P.boundary_type == LBM_CURVED &&
+           !(q == 19 && P.bc_wall_model == LBM_WALL_COMPLEX);
+}
+
 int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const RefMasks &r,
                        DeviceFlags &out, std::string &err) {
     const int q = r.q;
@@ -149,8 +154,13 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
     out.kind.clear();
     out.slot_node.clear();
 
-    if (P.boundary_type == LBM_CURVED) {
-        err = "curved (q-interpolated) walls are not supported";
+    if (P.boundary_type != LBM_CURVED && P.boundary_type != LBM_STRAIGHT) {
+        err = "unknown boundary type";
+        return LBM_ERR_INVALID;
+    }
+    if (P.boundary_type == LBM_CURVED && phys) {
+        err = "curved (q-interpolated) walls are the reference's wall kernels; physics-mode walls are "
+              "half-way bounce-back (use LBM_STRAIGHT)";
         return LBM_ERR_UNSUPPORTED;
     }
     if (P.bc_wall_model == LBM_WALL_COMPLEX && phys) {
@@ -163,6 +173,10 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
     // cases keeps its streamed populations); the reference's 2D loop has
     // straight walls only (Iterate.cu), so there the model changes nothing
     const bool hh = !phys && q == 19 && P.bc_wall_model == LBM_WALL_COMPLEX;
+    // reference curved walls (the simple wall kernels' CURVED branch; the HH
+    // kernel has none): every node with a wall link takes the boundary path,
+    // which interpolates between the node's own and upstream populations
+    const bool curved = curved_walls(P, q);
 
     // fluid bit and blocked pulls, in parallel over node ranges
     auto word_range = [&](long long lo, long long hi) {
@@ -215,7 +229,7 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
         bool special = false;
         int kind = 0;
         if (!phys) {
-            bool simple = !hh && ref_main_type(r, node) == LBM_BC_WALL;
+            bool simple = !hh && !curved && ref_main_type(r, node) == LBM_BC_WALL;
             for (int d = 1; d < q && simple; ++d) {
                 const uint64_t t = ref_type(r, node, d);
                 const bool wall = t == LBM_BC_WALL;

@@ -39,6 +39,9 @@ uint64_t ref_main_type(const RefMasks &r, int node);
 bool ref_corner(const RefMasks &r, int node);
 
 int build_ref_masks(const lbm_lattice_desc &L, RefMasks &r, std::string &err);
+// Reference curved walls in effect: reference mode, CURVED boundary type and
+// the simple wall model (the reference's HH wall kernel has no curved branch).
+bool curved_walls(const lbm_params &P, int q);
 int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const RefMasks &r,
                        DeviceFlags &out, std::string &err);
 

@@ -32,6 +32,10 @@ struct StepParams {
     const unsigned long long *bc_mask;
     const int32_t *bc_kind;
     const double *bc_uvw;
+    // reference curved walls: per boundary slot Q link fractions q (entry
+    // dir-1 for link dir, entry Q-1 the next boundary node's direction-1
+    // entry); null for straight walls
+    const double *bc_q;
     float *rho, *ux, *uy, *uz;
     int nx, ny, nz;
     int pitch;  // elements from one row of a direction to the next (Q * nx)
@@ -88,6 +92,64 @@ template <int Q, int ST, bool PHYS, bool WRAP, class G, int HINT, bool PRED>
 __device__ __forceinline__ void gather_node(const StepParams &p, const G &g, int x, int y, int z, uint32_t w,
                                             const typename Store<ST>::T *in, typename Store<ST>::R (&f)[Q]);
 
+// The reference's curved (q-interpolated) wall: the CURVED branch of
+// gpuBcWall2D / gpuBcSimpleWall3D (GpuBoundaries.cu:414-432, :461-479),
+// linear interpolation (Bouzidi) between post-collision populations f* of the
+// last step, i.e. the read buffer.  For every wall link dir of node x, with
+// q0 the link's fraction and q1 the entry after it in the reference's
+// per-node table (the link dir+1, and for the last direction the first link
+// of the next boundary node: the reference reads its first coefficient one
+// entry ahead, p.bc_q keeps that entry as the slot's last),
+//   q0 < 1/2:  f_opp(dir) = 2 q1 f*_dir(x) + (1 - 2 q0) f*_dir(x - c_dir)
+//   else:      f_opp(dir) = f*_dir(x) / 2 / q0 + (2 q0 - 1) / (2 q0) f*_opp(dir)(x)
+// cv[dir] receives the value for each wall link.  The reference reads
+// f*_dir(x - c_dir) at the flat index node + dir N + c(dir) of its SoA array
+// (N nodes per direction, c(dir) the linear pull offset): the upstream node
+// inside the lattice, a neighbouring row's or another direction's value
+// where x - c_dir lies outside it; the same element is read here from the
+// row layout, and 0 past either end of the array (undefined there in the
+// reference).
+template <int Q, int ST, class G>
+__device__ __forceinline__ void ref_curved(typename Store<ST>::R (&cv)[Q], uint64_t mk, int sl, int node,
+                                           const StepParams &p, const G &g) {
+    using S = Store<ST>;
+    using T = typename S::T;
+    using R = typename S::R;
+    using L = Lat<Q>;
+    const int x = node % g.nx, row = node / g.nx;
+    const T *base = (const T *)p.fin[0];
+    const T *in = base + (x + (long long)g.pitch * row);
+    const long long total = (long long)g.nx * g.ny * g.nz;
+    const double *qs = p.bc_q + (long long)sl * Q;
+#pragma unroll
+    for (int dir = 1; dir < Q; ++dir) {
+        bool wall;
+        if constexpr (Q == 9)
+            wall = ((uint32_t)mk & m2(3, dir)) == m2(1, dir);
+        else
+            wall = (mk & m3(7, dir)) == m3(1, dir);
+        if (!wall) continue;
+        const R own = S::decode(in[dir * g.nx], p.shift[dir], p.inv_scale);
+        const R q0 = (R)qs[dir - 1];
+        if (q0 < (R)0.5) {
+            const long long flat = (long long)node + dir * total -
+                                   (L::cx(dir) + (long long)L::cy(dir) * g.nx + (long long)L::cz(dir) * g.nx * g.ny);
+            R up = (R)0;
+            if (flat >= 0 && flat < Q * total) {
+                const int du = (int)(flat / total);
+                const long long nu = flat - du * total;
+                const long long xu = nu % g.nx, ru = nu / g.nx;
+                up = S::decode(base[du * g.nx + xu + (long long)g.pitch * ru], p.shift[du], p.inv_scale);
+            }
+            cv[dir] = (R)2 * (R)qs[dir] * own + ((R)1 - (R)2 * q0) * up;
+        } else {
+            const int o = L::opp(dir);
+            const R own_o = S::decode(in[o * g.nx], p.shift[o], p.inv_scale);
+            cv[dir] = own / (R)2 / q0 + ((R)2 * q0 - (R)1) / ((R)2 * q0) * own_o;
+        }
+    }
+}
+
 // The reference's 3D periodic copy (gpuBcPeriodic3D, GpuBoundaries.cu:
 // 2025-2084): a node with a periodic link on a face takes the five
 // populations entering through that face from the node one lattice length
@@ -125,9 +187,16 @@ __device__ __forceinline__ void ref3_periodic(typename Store<ST>::R (&f)[19], ui
             gather_node<19, ST, false, WRAP, G, 0, false>(p, g, px, py, pz, pw, in, fb);
             if (pw & W_SPECIAL) {
                 const int sl = __ldg(p.slot + pn);
-                bc_ref3_inlet_wall<R>(fb, __ldg(p.bc_mask + sl), (R)__ldg(p.bc_uvw + 3 * sl),
-                                      (R)__ldg(p.bc_uvw + 3 * sl + 1), (R)__ldg(p.bc_uvw + 3 * sl + 2),
-                                      p.ref_hh != 0);
+                const uint64_t pmk = __ldg(p.bc_mask + sl);
+                const R pu = (R)__ldg(p.bc_uvw + 3 * sl), pv = (R)__ldg(p.bc_uvw + 3 * sl + 1),
+                        pw0 = (R)__ldg(p.bc_uvw + 3 * sl + 2);
+                if (p.bc_q) {
+                    R cv[19];
+                    ref_curved<19, ST, G>(cv, pmk, sl, (int)pn, p, g);
+                    bc_ref3_inlet_wall<R, true>(fb, pmk, pu, pv, pw0, false, cv);
+                } else {
+                    bc_ref3_inlet_wall<R>(fb, pmk, pu, pv, pw0, p.ref_hh != 0);
+                }
             } else {
 #pragma unroll
                 for (int d = 1; d < 19; ++d)
@@ -165,11 +234,21 @@ __device__ __forceinline__ void apply_bc(typename Store<ST>::R (&f)[Q], uint32_t
                 w0 = (R)__ldg(p.bc_uvw + 3 * sl + 2);
         if constexpr (!PHYS) {
             const unsigned long long mk = __ldg(p.bc_mask + sl);
+            // curved walls: the interpolated values come from the read buffer
+            // only, so they are formed before any condition changes f
+            R cv[Q];
+            if (p.bc_q) ref_curved<Q, ST, G>(cv, mk, sl, node, p, g);
             if constexpr (Q == 9) {
-                bc_ref_d2q9<R>(f, (uint32_t)mk, u0, p.outlet_profile, zero_v);
+                if (p.bc_q)
+                    bc_ref_d2q9<R, true>(f, (uint32_t)mk, u0, p.outlet_profile, zero_v, cv);
+                else
+                    bc_ref_d2q9<R>(f, (uint32_t)mk, u0, p.outlet_profile, zero_v);
             } else {
                 // the reference's kernel order: inlet, wall, (outlet), periodic, symmetry
-                bc_ref3_inlet_wall<R>(f, mk, u0, v0, w0, p.ref_hh != 0);
+                if (p.bc_q)
+                    bc_ref3_inlet_wall<R, true>(f, mk, u0, v0, w0, false, cv);
+                else
+                    bc_ref3_inlet_wall<R>(f, mk, u0, v0, w0, p.ref_hh != 0);
                 ref3_periodic<ST, WRAP, G>(f, mk, node, p, g);
                 bc_ref3_symm<R>(f, mk);
                 keep_macro = ref3_keep_macro(mk, p.update_inlet_outlet);

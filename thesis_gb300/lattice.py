@@ -13,6 +13,8 @@ Builders here emit the workloads this engine is measured on:
 * sphere_duct -- a duct packed with non-overlapping spheres of random radii
   until a target porosity, pressure faces at both ends of the long axis.
 * channel2d -- a 2D channel with circular and rectangular obstacles.
+* cylinder_channel2d / sphere_cavity3d -- curved-wall cases: every link into
+  the cylinder or sphere is a wall link with its exact fraction q (link_q).
 """
 from dataclasses import dataclass, field
 
@@ -255,6 +257,95 @@ def channel2d(n=1024, m=256, seed=0, n_obstacles=None, size_scale=1.0):
             return 2 if side == 0 else 3
         return 1
     return Lattice(2, n, m, 1, fluid, _boundary_links(2, n, m, 1, fluid, ft))
+
+
+def _curved_links(dims, n, m, h, fluid, solid_of, centre, radius, outer, outer_q):
+    """Wall links of fluid nodes into a ball (disk in 2D) with their exact
+    fractions q along the link (the smaller root of |x + t c - centre| = r),
+    merged with the domain-leaving links `outer` (fraction outer_q), in
+    node-major, direction order.  Returns (bc, link_q).
+
+    A q < 1/2 link reads the upstream population at the flat index
+    node + dir N + c(dir) of the direction-major array (the reference's
+    addressing); an outer wall link for which that index falls past either
+    end of the array, where the reference's read is undefined, takes 1/2."""
+    if dims == 2:
+        cxs, cys, czs = CX2, CY2, np.zeros(9, int)
+    else:
+        cxs, cys, czs = CX3, CY3, CZ3
+    idx = np.nonzero(fluid)[0]
+    x, y, z = idx % n, (idx // n) % m, idx // (n * m)
+    rows, qs = [], []
+    cen = np.asarray(centre, float)
+    for d in range(1, len(cxs)):
+        tx, ty, tz = x + cxs[d], y + cys[d], z + czs[d]
+        inside = (tx >= 0) & (tx < n) & (ty >= 0) & (ty < m) & (tz >= 0) & (tz < h)
+        sel = np.zeros(idx.shape, bool)
+        sel[inside] = solid_of(tx[inside], ty[inside], tz[inside])
+        if not sel.any():
+            continue
+        p = np.stack([x[sel], y[sel], z[sel]], 1).astype(float) - cen[: 3]
+        c = np.array([cxs[d], cys[d], czs[d]], float)
+        a = c @ c
+        b = 2 * (p @ c)
+        cc = (p * p).sum(1) - radius * radius
+        t = (-b - np.sqrt(np.maximum(b * b - 4 * a * cc, 0))) / (2 * a)
+        k = int(sel.sum())
+        rows.append(np.stack([x[sel], y[sel], z[sel], np.full(k, d), np.ones(k, int), np.zeros(k, int)], 1))
+        qs.append(np.clip(t, 0.0, 1.0))
+    rows.append(outer)
+    if outer.size:
+        d = outer[:, 3]
+        flat = (outer[:, 0] + n * (outer[:, 1] + m * outer[:, 2]) + d * (n * m * h)
+                - (cxs[d] + n * cys[d] + n * m * czs[d]))
+        inside = (flat >= 0) & (flat < len(cxs) * n * m * h)
+        qs.append(np.where((outer[:, 4] == 1) & inside, outer_q, 0.5))
+    else:
+        qs.append(np.zeros(0))
+    bc = np.concatenate(rows).astype(np.int32)
+    q = np.concatenate(qs)
+    order = np.lexsort((bc[:, 3], bc[:, 0] + n * (bc[:, 1] + m * bc[:, 2])))
+    return bc[order], q[order]
+
+
+def cylinder_channel2d(n=48, m=24, centre=None, radius=None, outer_q=0.5):
+    """2D channel along x (inlet x = 0, outlet x = n-1, walls y = 0 and m-1)
+    around a cylinder, with curved walls: every link of a fluid node into the
+    cylinder is a wall link carrying its exact fraction q (lat.link_q, one
+    per BC row), the outer walls' links carry outer_q."""
+    cx, cy = centre if centre is not None else (0.35 * n, 0.5 * m - 0.37)
+    r = radius if radius is not None else 0.21 * m
+    yy, xx = np.mgrid[0:m, 0:n]
+    solid = (xx - cx) ** 2 + (yy - cy) ** 2 <= r * r
+    fluid = (~solid).astype(np.int32).reshape(-1)
+
+    def ft(axis, side):
+        if axis == 0:
+            return 2 if side == 0 else 3
+        return 1
+    outer = _boundary_links(2, n, m, 1, fluid, ft)
+    bc, q = _curved_links(2, n, m, 1, fluid, lambda tx, ty, tz: solid[ty, tx], (cx, cy, 0.0), r, outer, outer_q)
+    lat = Lattice(2, n, m, 1, fluid, bc)
+    lat.link_q = q
+    return lat
+
+
+def sphere_cavity3d(n=14, m=12, h=12, centre=None, radius=None, outer_q=0.5):
+    """3D lid-driven cavity (lid z = h-1) around a sphere, with curved walls
+    as in cylinder_channel2d (lat.link_q)."""
+    c = centre if centre is not None else (0.45 * n + 0.13, 0.5 * m - 0.29, 0.45 * h + 0.21)
+    r = radius if radius is not None else 0.24 * min(n, m, h)
+    zz, yy, xx = np.mgrid[0:h, 0:m, 0:n]
+    solid = (xx - c[0]) ** 2 + (yy - c[1]) ** 2 + (zz - c[2]) ** 2 <= r * r
+    fluid = (~solid).astype(np.int32).reshape(-1)
+
+    def ft(axis, side):
+        return 2 if (axis == 2 and side == 1) else 1
+    outer = _boundary_links(3, n, m, h, fluid, ft)
+    bc, q = _curved_links(3, n, m, h, fluid, lambda tx, ty, tz: solid[tz, ty, tx], c, r, outer, outer_q)
+    lat = Lattice(3, n, m, h, fluid, bc)
+    lat.link_q = q
+    return lat
 
 
 def read_node_file(path, dims):

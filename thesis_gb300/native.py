@@ -93,6 +93,8 @@ def lib():
         "lbm_last_error": (C.c_char_p, []),
         "lbm_create": (C.c_int, [C.POINTER(LatticeDesc), C.POINTER(Params), C.POINTER(vp)]),
         "lbm_set_inlet_velocity": (C.c_int, [vp, fp, fp, fp]),
+        "lbm_set_link_q": (C.c_int, [vp, dp]),
+        "lbm_link_q": (C.c_int, [C.c_int] * 5 + [_IP] * 4 + [fp] * 6 + [C.c_double, dp]),
         "lbm_init": (C.c_int, [vp, fp, fp, fp, fp]),
         "lbm_step": (C.c_int, [vp, C.c_int, C.c_int, vp]),
         "lbm_get_macro": (C.c_int, [vp, fp, fp, fp, fp]),

@@ -93,6 +93,25 @@ def build_flags(lat: Lattice, args: Arguments):
     return mask, word, slot, nbc.value
 
 
+def link_q(lat: Lattice, bc_xyz, node_xyz, delta):
+    """The reference's link fractions |B - X| / (delta |c_dir|) (lbm_link_q):
+    bc_xyz the BC file's boundary points (num_conns x 2 or 3), node_xyz the
+    Node file's coordinates by node index (num_nodes x 2 or 3)."""
+    L = N.lib()
+    bc = lat.bc
+    cols = [np.ascontiguousarray(bc[:, k], dtype=np.int32) for k in range(4)]
+    b = [np.ascontiguousarray(np.asarray(bc_xyz, np.float32)[:, k]) for k in range(lat.dims)]
+    x = [np.ascontiguousarray(np.asarray(node_xyz, np.float32)[:, k]) for k in range(lat.dims)]
+    if lat.dims == 2:
+        b.append(None)
+        x.append(None)
+    q = np.zeros(bc.shape[0], np.float64)
+    N.check(L.lbm_link_q(lat.dims, lat.n, lat.m, lat.h, int(bc.shape[0]), _iptr(cols[0]), _iptr(cols[1]),
+                         _iptr(cols[2]) if lat.dims == 3 else None, _iptr(cols[3]), *[_fptr(a) for a in b],
+                         *[_fptr(a) for a in x], float(delta), q.ctypes.data_as(C.POINTER(C.c_double))))
+    return q
+
+
 class Solver:
     """One lattice on the GPU.  Usage: s = Solver(lat, args); s.init();
     s.step(100, write_macro=True); rho, u, v, w = s.macro()."""
@@ -128,6 +147,14 @@ class Solver:
     def set_inlet_velocity(self, u=None, v=None, w=None):
         arrs = [None if a is None else np.ascontiguousarray(a, np.float32).reshape(-1) for a in (u, v, w)]
         N.check(self._lib.lbm_set_inlet_velocity(self._h, *[_fptr(a) for a in arrs]))
+
+    def set_link_q(self, q):
+        """Curved walls: the wall's fraction along each BC link, in the
+        lattice's link order (lbm_set_link_q)."""
+        a = np.ascontiguousarray(q, np.float64).reshape(-1)
+        if a.size != self.lat.bc.shape[0]:
+            raise ValueError("expected %d link fractions, got %d" % (self.lat.bc.shape[0], a.size))
+        N.check(self._lib.lbm_set_link_q(self._h, a.ctypes.data_as(C.POINTER(C.c_double))))
 
     def autotune(self, trial_steps=20):
         """Pick the fastest variant of the specialised step kernel (block size,
