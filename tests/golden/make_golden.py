@@ -46,6 +46,12 @@ def cases():
     for coll, tag in ((1, "bgk"), (3, "mrt")):
         out.append(("curved_sph3d_14x12x12_" + tag, ("sphere_cavity3d", (14, 12, 12, None, None, 0.3)),
                     dict(u=0.05, viscosity=0.1, collision_model=coll, boundary_type=1), 12))
+    # 2D extrapolation outlets (second and first order) and HEmodel, which the
+    # 2D outlet kernel has no case for
+    for prof, ptag, coll, tag, bt in ((2, "2nd", 1, "bgk", 2), (3, "1st", 3, "mrt", 2), (4, "he", 2, "trt", 2),
+                                      (2, "2nd_curved", 3, "mrt", 1)):
+        out.append(("outlet%s_cyl2d_48x24_%s" % (ptag, tag), ("cylinder_channel2d", (48, 24, None, None, 0.3)),
+                    dict(u=0.05, viscosity=0.05, collision_model=coll, outlet_profile=prof, boundary_type=bt), 40))
     return out
 
 

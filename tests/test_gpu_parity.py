@@ -223,6 +223,32 @@ def test_reference_curved_walls_l2_residual(oracle):
     assert abs(r_gpu - r.resid[k]) <= 1e-4 * r.resid[k] + 1e-6, (r_gpu, r.resid[k])
 
 
+@pytest.mark.parametrize("profile", [N.OUTLET_SECOND, N.OUTLET_FIRST, N.OUTLET_HEMODEL])
+@pytest.mark.parametrize("boundary", [N.STRAIGHT, N.CURVED])
+@pytest.mark.parametrize("storage", [N.STORE_F32, N.STORE_F64])
+def test_reference_extrapolation_outlets_2d(oracle, profile, boundary, storage):
+    """The reference's 2D east outlets: second- and first-order
+    extrapolation of f1, f5, f8 from the post-stream, post-wall values of the
+    two western neighbours (recomputed by the outlet node's thread), and
+    HEmodel, which the 2D outlet kernel leaves without a case."""
+    lat = CURVED_CASES["cylinder2d"]()
+    args = Arguments(u=0.05, viscosity=0.05, collision_model=N.MRT, outlet_profile=profile,
+                     boundary_type=boundary, storage=storage, init_equilibrium=1)
+    g, r, fl = run_pair(oracle, lat, args, 40, link_q=lat.link_q if boundary == N.CURVED else None)
+    compare(g, r, fl, storage, 2)
+
+
+@pytest.mark.parametrize("variant", ["jith", "scalar", "pair", "jit2"])
+def test_reference_extrapolation_outlet_kernel_forms(oracle, monkeypatch, variant):
+    monkeypatch.setenv("THESIS_LBM_KERNEL", variant)
+    lat = CURVED_CASES["cylinder2d"]()
+    args = Arguments(u=0.05, viscosity=0.05, collision_model=N.BGKW, outlet_profile=N.OUTLET_SECOND,
+                     init_equilibrium=1)
+    g, r, fl = run_pair(oracle, lat, args, 30)
+    monkeypatch.delenv("THESIS_LBM_KERNEL", raising=False)
+    compare(g, r, fl, N.STORE_F32, 2)
+
+
 def test_reference_cavity3d_gravity_no_inlet_update(oracle):
     lat = lattice.cavity3d(9, 8, 7)
     args = Arguments(u=0.05, viscosity=0.1, collision_model=N.BGKW, g=1e-5, update_inlet_outlet=0)

@@ -318,7 +318,9 @@ static int setup_jit(lbm_handle_s *H, const std::vector<uint32_t> &word, bool pa
     {
         std::lock_guard<std::mutex> lock(g_tuned_mutex);
         auto it = g_tuned.find(tune_key(k));
-        if (it != g_tuned.end() && !pair) {
+        // a two-node choice tuned on another lattice of this shape does not
+        // carry over to boundaries only the one-node kernels apply
+        if (it != g_tuned.end() && !pair && !(it->second.pair && one_node_boundaries(H->P, H->q))) {
             k.block = it->second.block;
             k.hint = it->second.hint;
             k.pred = it->second.pred;
@@ -417,8 +419,8 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
         // the run-time build is unavailable.  THESIS_LBM_KERNEL=scalar|pair|
         // tma|jit selects a variant explicitly (jit then fails loudly).
         const char *kv = getenv("THESIS_LBM_KERNEL");
-        // the two-node kernels have no curved-wall path
-        const bool can_pair = (L->n % 2 == 0) && P->storage != LBM_STORE_F64 && !curved_walls(*P, q);
+        // the two-node kernels have no curved-wall or extrapolation-outlet path
+        const bool can_pair = (L->n % 2 == 0) && P->storage != LBM_STORE_F64 && !one_node_boundaries(*P, q);
         H->pair_kernel = kv && strcmp(kv, "pair") == 0 && can_pair;
         want_tma = kv && strcmp(kv, "tma") == 0;
         // jithz<k>[b<block>][m<min blocks>]: storage units walking k nodes along z
@@ -1016,7 +1018,7 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
             vs.insert(vs.end(), hz, hz + 7);
         }
     }
-    if (H->n % 2 == 0 && hs_ok) {
+    if (H->n % 2 == 0 && hs_ok && !one_node_boundaries(H->P, H->q)) {
         const V pv[] = {{64, 0, 0, 1, 1, 0, 1}, {128, 0, 0, 1, 1, 0, 1}, {64, 0, 0, 1, 12, 0, 1},
                         {128, 0, 0, 1, 6, 0, 1}};
         vs.insert(vs.end(), pv, pv + 4);

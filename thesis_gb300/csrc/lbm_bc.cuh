@@ -18,13 +18,17 @@ constexpr uint64_t R3_WALL_B = 1ull << 54, R3_INLT_B = 2ull << 54, R3_OUTL_B = 3
 
 // ---------------------------------------------------------------------------
 // Reference semantics, D2Q9: gpuBcInlet2D, gpuBcWall2D (straight), and the
-// Zou-He branch of gpuBcOutlet2D (GpuBoundaries.cu:12-71, :400-443,
-// :1562-1602), in that order, on the node's streamed populations.  CURVED:
+// east outlet of gpuBcOutlet2D (GpuBoundaries.cu:12-71, :400-443,
+// :1562-1653), in that order, on the node's streamed populations.  CURVED:
 // a wall link dir sets f_opp(dir) to cv[dir] (ref_curved) instead of f[dir].
+// The extrapolation outlets rewrite f1, f5, f8 from the post-stream,
+// post-wall values of the nodes one and two to the west, ext[0..2] and
+// ext[3..5] (ref2_outlet_neighbours); with ext null, or HEmodel, which the
+// 2D kernel has no case for, they leave the node as it is.
 // ---------------------------------------------------------------------------
 template <class R, bool CURVED = false>
 __device__ __forceinline__ void bc_ref_d2q9(R (&f)[9], uint32_t mk, R u0, int outlet_profile,
-                                            bool &zero_v, const R *cv = nullptr) {
+                                            bool &zero_v, const R *cv = nullptr, const R *ext = nullptr) {
     if (!(mk & R2_FLUID)) return;
     if (mk & R2_INLT_B) {
         if ((mk & m2(2, 2)) && !(mk & R2_CORNER)) {  // north (lid)
@@ -49,6 +53,14 @@ __device__ __forceinline__ void bc_ref_d2q9(R (&f)[9], uint32_t mk, R u0, int ou
             f[3] = f[1] - (R)2 * r * u0 / (R)3;
             f[7] = f[5] - r * u0 / (R)6;
             f[6] = f[8] - r * u0 / (R)6;
+        } else if (ext && outlet_profile == LBM_OUTLET_SECOND) {
+            f[1] = (R)2 * ext[0] - ext[3];
+            f[5] = (R)2 * ext[1] - ext[4];
+            f[8] = (R)2 * ext[2] - ext[5];
+        } else if (ext && outlet_profile == LBM_OUTLET_FIRST) {
+            f[1] = ext[0];
+            f[5] = ext[1];
+            f[8] = ext[2];
         }
         zero_v = true;  // gpuUpdateMacro2D forces v = 0 on east outlets (GpuUpdateMacro.cu:30)
     }

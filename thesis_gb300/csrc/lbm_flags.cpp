@@ -142,6 +142,11 @@ bool curved_walls(const lbm_params &P, int q) {
            !(q == 19 && P.bc_wall_model == LBM_WALL_COMPLEX);
 }
 
+bool one_node_boundaries(const lbm_params &P, int q) {
+    return curved_walls(P, q) || (q == 9 && P.mode != LBM_MODE_PHYSICS &&
+                                  (P.outlet_profile == LBM_OUTLET_SECOND || P.outlet_profile == LBM_OUTLET_FIRST));
+}
+
 int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const RefMasks &r,
                        DeviceFlags &out, std::string &err) {
     const int q = r.q;
@@ -245,10 +250,9 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
                     return LBM_ERR_UNSUPPORTED;
                 }
                 if (q == 9 && ref_type(r, node, 1) == LBM_BC_OUTLET &&
-                    P.outlet_profile != LBM_OUTLET_ZOUHE) {
-                    err = "extrapolation outlets read neighbouring boundary nodes; only the Zou-He "
-                          "outlet is supported";
-                    return LBM_ERR_UNSUPPORTED;
+                    (P.outlet_profile < LBM_OUTLET_ZOUHE || P.outlet_profile > LBM_OUTLET_HEMODEL)) {
+                    err = "unknown 2D outlet profile";
+                    return LBM_ERR_INVALID;
                 }
             }
         } else {

@@ -42,6 +42,9 @@ int build_ref_masks(const lbm_lattice_desc &L, RefMasks &r, std::string &err);
 // Reference curved walls in effect: reference mode, CURVED boundary type and
 // the simple wall model (the reference's HH wall kernel has no curved branch).
 bool curved_walls(const lbm_params &P, int q);
+// Boundary conditions only the one-node kernels apply (the shared boundary
+// code): curved walls and the reference's 2D extrapolation outlets.
+bool one_node_boundaries(const lbm_params &P, int q);
 int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const RefMasks &r,
                        DeviceFlags &out, std::string &err);
 

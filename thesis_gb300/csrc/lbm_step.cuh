@@ -217,6 +217,54 @@ __device__ __forceinline__ void ref3_periodic(typename Store<ST>::R (&f)[19], ui
     }
 }
 
+// The 2D extrapolation outlets (OUTLET_SECOND / OUTLET_FIRST of
+// gpuBcOutlet2D, GpuBoundaries.cu:1608-1638) read f1, f5 and f8 of the nodes
+// one and two to the west (flat indices node - 1, node - 2) as they stand
+// after streaming, inlet and wall conditions.  Those values are recomputed
+// here from the read buffer: the neighbour's pull and its own inlet and wall
+// conditions (curved walls included); a solid neighbour holds 0, as the
+// reference's never-streamed solid nodes do.
+template <int ST, bool WRAP, class G>
+__device__ __forceinline__ void ref2_outlet_neighbours(typename Store<ST>::R (&ext)[6], int node, const StepParams &p,
+                                                       const G &g) {
+    using R = typename Store<ST>::R;
+    using T = typename Store<ST>::T;
+    using L = Lat<9>;
+#pragma unroll 1
+    for (int k = 0; k < 2; ++k) {
+        const int nb = node - 1 - k;
+        R fb[9];
+#pragma unroll
+        for (int d = 0; d < 9; ++d) fb[d] = (R)0;
+        const uint32_t w = nb >= 0 ? __ldg(p.word + nb) : 0u;
+        if (w & W_FLUID) {
+            const int x = nb % g.nx, y = nb / g.nx;
+            const T *in = (const T *)p.fin[0] + (x + (long long)g.pitch * y);
+            gather_node<9, ST, false, WRAP, G, 0, false>(p, g, x, y, 0, w, in, fb);
+            if (w & W_SPECIAL) {
+                const int sl = __ldg(p.slot + nb);
+                const uint64_t mk = __ldg(p.bc_mask + sl);
+                const R u0 = (R)__ldg(p.bc_uvw + 3 * sl);
+                bool zv;
+                if (p.bc_q) {
+                    R cv[9];
+                    ref_curved<9, ST, G>(cv, mk, sl, nb, p, g);
+                    bc_ref_d2q9<R, true>(fb, (uint32_t)mk, u0, LBM_OUTLET_HEMODEL, zv, cv);
+                } else {
+                    bc_ref_d2q9<R>(fb, (uint32_t)mk, u0, LBM_OUTLET_HEMODEL, zv);
+                }
+            } else {
+#pragma unroll
+                for (int dir = 1; dir < 9; ++dir)
+                    if ((w >> L::opp(dir)) & 1u) fb[L::opp(dir)] = fb[dir];
+            }
+        }
+        ext[3 * k] = fb[1];
+        ext[3 * k + 1] = fb[5];
+        ext[3 * k + 2] = fb[8];
+    }
+}
+
 // Boundary conditions of a fluid node whose populations are gathered
 // (pulled, bounced back): Zou-He faces, moving walls, the reference's wall,
 // periodic and symmetry copies.  keep_macro / zero_v report the reference's
@@ -239,10 +287,14 @@ __device__ __forceinline__ void apply_bc(typename Store<ST>::R (&f)[Q], uint32_t
             R cv[Q];
             if (p.bc_q) ref_curved<Q, ST, G>(cv, mk, sl, node, p, g);
             if constexpr (Q == 9) {
+                R ext[6];
+                const bool extrap = (mk & R2_FLUID) && ((uint32_t)mk & m2(3, 1)) == m2(3, 1) &&
+                                    (p.outlet_profile == LBM_OUTLET_SECOND || p.outlet_profile == LBM_OUTLET_FIRST);
+                if (extrap) ref2_outlet_neighbours<ST, WRAP, G>(ext, node, p, g);
                 if (p.bc_q)
-                    bc_ref_d2q9<R, true>(f, (uint32_t)mk, u0, p.outlet_profile, zero_v, cv);
+                    bc_ref_d2q9<R, true>(f, (uint32_t)mk, u0, p.outlet_profile, zero_v, cv, extrap ? ext : nullptr);
                 else
-                    bc_ref_d2q9<R>(f, (uint32_t)mk, u0, p.outlet_profile, zero_v);
+                    bc_ref_d2q9<R>(f, (uint32_t)mk, u0, p.outlet_profile, zero_v, nullptr, extrap ? ext : nullptr);
             } else {
                 // the reference's kernel order: inlet, wall, (outlet), periodic, symmetry
                 if (p.bc_q)
