@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--cpu-sample", default="64,64,128", help="n,m,h of the CPU-baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="target CPU time of one CPU-baseline sample (steps are chosen to fill it)")
-    ap.add_argument("--workload", default="duct", choices=["duct", "cavities", "cg", "warmstart"],
+    ap.add_argument("--workload", default="duct", choices=["duct", "cavities", "cg", "cg3d", "warmstart"],
                     help="duct: the D3Q19 MRT sphere-packed duct (default); cavities: a batch of D2Q9 MRT "
                          "lid-driven cavities of uneven sizes, batched vs one by one; cg: colour-gradient "
                          "static droplets on a periodic 1024^2 lattice (Laplace law); warmstart: time to the "
@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--cg-size", type=int, default=1024)
     ap.add_argument("--cg-seeds", type=int, default=3, help="droplets (radius uniform in [64, 256] nodes)")
     ap.add_argument("--cg-steps", type=int, default=40000, help="steps per droplet before the Laplace-law check")
+    ap.add_argument("--cg3-size", type=int, default=256, help="D3Q19 colour-gradient box side")
+    ap.add_argument("--cg3-steps", type=int, default=200)
     ap.add_argument("--domains", type=int, default=512, help="cavities in the batch")
     ap.add_argument("--one-by-one-steps", type=int, default=20,
                     help="steps per cavity when the cavities run one launch per step each")
@@ -424,6 +426,72 @@ def run_cg(args):
     return 0
 
 
+def run_cg3d(args):
+    """D3Q19 colour-gradient throughput: a static drop (R = n/4) in a
+    periodic n^3 box, FP32, 18-neighbour gradient; two launches per step."""
+    import torch
+    from thesis_gb300 import build as native_build
+    from thesis_gb300 import multiphase as mp
+    native_build.build()
+    n = args.cg3_size
+    a = mp.CgArguments(A=0.005, beta=0.7, r_viscosity=1 / 6, b_viscosity=1 / 6, r_alpha=4 / 9, b_alpha=4 / 9,
+                       control_param=0.9)
+    r0, b0 = mp.create_bubble3d(n, n, n, a, radius_nodes=n / 4)
+    nodes = n ** 3
+    with mp.CgSolver(n, n, a, h=n) as s:
+        s.init(r0, b0)
+        del r0, b0
+        stream = torch.cuda.Stream()
+        s.step(max(args.warmup, 3), write_macro=False, stream=stream.cuda_stream)
+        stream.synchronize()
+        clocks = ClockSampler(0)
+        clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.step(args.cg3_steps - 1, write_macro=False, stream=stream.cuda_stream)
+        s.step(1, write_macro=True, stream=stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        clk = clocks.stop()
+        ms = e0.elapsed_time(e1) / args.cg3_steps
+        lap, rc = s.laplace()
+    value = nodes / (ms / 1e3) / 1e9
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import pyoracle
+        L = pyoracle.oracle_lib()
+        nc = 48
+        rc0, bc0 = mp.create_bubble3d(nc, nc, nc, a, radius_nodes=nc / 4)
+        p = pyoracle.cg_params(A=0.005, beta=0.7)
+        t0 = time.perf_counter()
+        pyoracle.run_oracle_cg3(nc, nc, nc, p, rc0, bc0, 3)
+        est = (time.perf_counter() - t0) / 3
+        steps = int(min(max(args.cpu_seconds / max(est, 1e-6), 3), 100000))
+        t0 = time.perf_counter()
+        pyoracle.run_oracle_cg3(nc, nc, nc, p, rc0, bc0, steps)
+        dt = time.perf_counter() - t0
+        cpu = {"value": nc ** 3 * steps / dt / 1e9, "unit": "GLUPS", "cores": L.orc_threads(), "kind": "port",
+               "sample": "oracle restatement of the reference's 3D colour-gradient kernels (FP32, OpenMP) on a "
+                         "%d^3 drop, %d steps, %.1f s" % (nc, steps, dt)}
+    # algorithmic bytes per update: both colours' 19 populations read once
+    # and written once (304 B) plus the two colour densities (8 B)
+    algo = 312
+    achieved = algo * nodes / (ms / 1e3) / 1e9
+    line = {"metric": "GLUPS (node updates/s / 1e9), D3Q19 colour-gradient static drop %d^3 periodic" % n,
+            "value": value, "unit": "GLUPS", "n_gpus": 1, "steps": args.cg3_steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (drop of radius n/4)",
+            "config": {"workload": "D3Q19 colour-gradient drop, %d^3 periodic, R = n/4, A 0.005, beta 0.7, tau 1, "
+                                   "alpha 4/9, 18-neighbour gradient, FP32 storage" % n,
+                       "l2_policy": "inputs larger than L2 (%.1f GB of populations)" % (2 * 152 * nodes / 1e9)},
+            "status": "ok" if rc == 0 else "diverged", "max_u": float(lap[4]),
+            "roofline": {"bound": "hbm", "algorithmic_bytes_per_update": algo, "achieved": achieved, "unit": "GB/s",
+                         "peak": measured_peak()[0], "frac": achieved / measured_peak()[0]},
+            "clocks": clk, "gpu_launches": 2 * args.cg3_steps, "cpu_baseline": cpu}
+    print(json.dumps(line))
+    return 0
+
+
 def run_warmstart(args):
     """Learned warm start: steady fields of seeded 256x64 channels from the
     batched solver train the U-Net on the GPU; held-out channels are then
@@ -546,6 +614,8 @@ def main():
         return run_warmstart(args)
     if args.workload == "cg" and args.impl != "reference":
         return run_cg(args)
+    if args.workload == "cg3d" and args.impl != "reference":
+        return run_cg3d(args)
     if args.workload == "cavities" and args.impl != "reference":
         return run_cavities(args)
     rank, world, local = dist_info()

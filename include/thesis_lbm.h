@@ -408,8 +408,14 @@ typedef struct lbm_cg_params {
 
 /* n x m periodic lattice, n, m >= 5. */
 int lbm_cg_create(int n, int m, const lbm_cg_params *params, lbm_cg_handle *out);
-/* Post-streaming red and blue populations, host arrays of 9*n*m floats in
- * SoA order f[d*n*m + x + n*y]; performs the first collision. */
+/* D3Q19: n x m x h lattice periodic in all three axes, n, m, h >= 5 (the
+ * reference's 3D path, gpuCollBgkwGC3D / gpuCollEnhancedBgkwGC3D,
+ * GpuCollision.cu:283-526, :709-880, with the 18-neighbour gradient or, when
+ * high_order, the 104-point isotropic set).  The calls below take Q = 19
+ * populations per node and SoA index d*N + x + n*(y + m*z). */
+int lbm_cg_create3d(int n, int m, int h, const lbm_cg_params *params, lbm_cg_handle *out);
+/* Post-streaming red and blue populations, host arrays of Q*N floats (Q = 9
+ * in 2D) in SoA order f[d*N + x + n*y]; performs the first collision. */
 int lbm_cg_init(lbm_cg_handle h, const float *r_f, const float *b_f);
 /* nsteps of stream + densities + collide on `stream` (NULL = own stream);
  * write_macro_last stores rho, u, v on the last step. */
@@ -417,14 +423,19 @@ int lbm_cg_step(lbm_cg_handle h, int nsteps, int write_macro_last, void *stream)
 /* Colour densities of the last step and the velocity of the last step that
  * stored it, host arrays of n*m (any may be NULL). */
 int lbm_cg_get_macro(lbm_cg_handle h, float *r_rho, float *b_rho, float *u, float *v);
-/* Post-collision red and blue populations, 9*n*m floats each. */
+/* As lbm_cg_get_macro, with the z velocity (0 in 2D). */
+int lbm_cg_get_macro3d(lbm_cg_handle h, float *r_rho, float *b_rho, float *u, float *v, float *w);
+/* Post-collision red and blue populations, Q*N floats each. */
 int lbm_cg_get_populations(lbm_cg_handle h, float *r_f, float *b_f);
 /* FP64 Laplace-law sums (Iterate.cu:496-499): out[0] = sum rho_r where
  * phi >= control_param, out[1] = their count, out[2] = sum rho_b where
- * phi <= -control_param, out[3] = their count, out[4] = max |u|.
+ * phi <= -control_param, out[3] = their count, out[4] = max |u| (3D:
+ * gpuUpdateMacro3DCG's p_in / p_out sums, GpuUpdateMacro.cu:345-356).
  * Returns LBM_DIVERGED when a sum is not finite. */
 int lbm_cg_laplace(lbm_cg_handle h, double *out);
 long long lbm_cg_nodes(lbm_cg_handle h);
+/* Populations per node: 9 or 19. */
+int lbm_cg_q(lbm_cg_handle h);
 const char *lbm_cg_last_error(void);
 void lbm_cg_destroy(lbm_cg_handle h);
 

@@ -1396,3 +1396,275 @@ extern "C" int orc_cg2d_collide(int fp64, int n, int m, const orc_cg_params *p, 
     };
     return fp64 ? go(0.0) : go(0.0f);
 }
+
+/* =====================================================================
+ * Colour-gradient two-phase D3Q19 (restated from gpuCollBgkwGC3D and
+ * gpuCollEnhancedBgkwGC3D, GpuCollision.cu:283-526, :709-880; streaming
+ * GpuStream.cu:196-250; macroscopic update gpuUpdateMacro3DCG,
+ * GpuUpdateMacro.cu:215-360; constants GpuInit.cu:896-990).
+ *
+ * Same step as the D2Q9 path above, on a lattice periodic by index wrap in
+ * all three axes.  The gradient stencils: the 18 lattice neighbours with
+ * weights 1/6 (axes) and 1/12 (diagonals), or the 104-point isotropic set
+ * of shells |c|^2 = 1, 2, 3, 4, 5, 6, 9 with weights 4/45, 1/21, 2/105,
+ * 5/504, 1/315, 1/630, 1/5040 (Shan's eighth-order 3D set), summed here shell
+ * by shell in lexicographic order (the reference sums its own table order).
+ * Below the gradient limit the recolouring cosine is 0 (the reference's
+ * non-enhanced kernel leaves it unset there).  No body force.
+ * Test infrastructure only.
+ * ===================================================================== */
+namespace {
+
+const double CG3_W[19] = {1. / 3., 1. / 18., 1. / 18., 1. / 18., 1. / 18., 1. / 18., 1. / 18., 1. / 36., 1. / 36.,
+                          1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36.};
+
+inline double cg3_phi(int d) { return d == 0 ? 0.0 : (d <= 6 ? 1. / 12. : 1. / 24.); }
+inline double cg3_teta(int d) { return d == 0 ? 1.0 : (d <= 6 ? -1. / 12. : -1. / 24.); }
+inline double cg3_chi(int d) { return d == 0 ? -5.0 / 2.0 : (d <= 6 ? -1. / 6. : 1. / 24.); }
+inline double cg3_psi(int d) { return d == 0 ? 0.0 : (d <= 6 ? 1. / 4. : 1. / 8.); }
+inline double cg3_wpert(int d) { return d == 0 ? -2.0 / 9.0 : (d <= 6 ? 1.0 / 54.0 : 1.0 / 27.0); }
+inline double cg3_gw(int d) { return d == 0 ? 0.0 : (d <= 6 ? 1. / 6. : 1. / 12.); }
+
+struct Ho3 {
+    int n = 0;
+    int c[104][3];
+    double w[104];
+    Ho3() {
+        const int shells[7] = {1, 2, 3, 4, 5, 6, 9};
+        const double ws[7] = {4. / 45., 1. / 21., 2. / 105., 5. / 504., 1. / 315., 1. / 630., 1. / 5040.};
+        for (int s = 0; s < 7; ++s)
+            for (int x = -2; x <= 2; ++x)
+                for (int y = -2; y <= 2; ++y)
+                    for (int z = -2; z <= 2; ++z)
+                        if (x * x + y * y + z * z == shells[s]) {
+                            c[n][0] = x;
+                            c[n][1] = y;
+                            c[n][2] = z;
+                            w[n] = ws[s];
+                            ++n;
+                        }
+    }
+};
+const Ho3 HO3;
+
+template <class T>
+struct CgState3 {
+    int n, m, h, N;
+    orc_cg_params p;
+    std::vector<T> rf, bf, rfc, bfc, rr, br, rho, u, v, w;
+    int wrap(int x, int y, int z) const {
+        return ((x % n + n) % n) + n * (((y % m + m) % m) + m * ((z % h + h) % h));
+    }
+};
+
+template <class T>
+void cg3_macro(CgState3<T> &S) {
+    const size_t N = (size_t)S.N;
+    for (int i = 0; i < S.N; ++i) {
+        T r = 0, b = 0, ju = 0, jv = 0, jw = 0;
+        for (int d = 0; d < 19; ++d) {
+            const T fd = S.rf[i + d * N] + S.bf[i + d * N];
+            r += S.rf[i + d * N];
+            b += S.bf[i + d * N];
+            ju += (T)cx3[d] * fd;
+            jv += (T)cy3[d] * fd;
+            jw += (T)cz3[d] * fd;
+        }
+        const T rho = r + b;
+        S.rr[i] = r;
+        S.br[i] = b;
+        S.rho[i] = rho;
+        S.u[i] = ju / rho;
+        S.v[i] = jv / rho;
+        S.w[i] = jw / rho;
+    }
+}
+
+template <class T>
+void cg3_collide(CgState3<T> &S) {
+    const size_t N = (size_t)S.N;
+    const orc_cg_params &p = S.p;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < S.N; ++i) {
+        const int x = i % S.n, y = (i / S.n) % S.m, z = i / (S.n * S.m);
+        T cgx = 0, cgy = 0, cgz = 0, grx = 0, gry = 0, grz = 0;
+        auto add = [&](int ox, int oy, int oz, T wgt) {
+            const int j = S.wrap(x + ox, y + oy, z + oz);
+            const T a1 = wgt * (S.rr[j] - S.br[j]) / S.rho[j], a2 = wgt * S.rho[j];
+            grx += a2 * (T)ox;
+            gry += a2 * (T)oy;
+            grz += a2 * (T)oz;
+            cgx += a1 * (T)ox;
+            cgy += a1 * (T)oy;
+            cgz += a1 * (T)oz;
+        };
+        if (p.high_order) {
+            for (int k = 0; k < HO3.n; ++k) add(HO3.c[k][0], HO3.c[k][1], HO3.c[k][2], (T)HO3.w[k]);
+        } else {
+            for (int k = 1; k < 19; ++k) add(cx3[k], cy3[k], cz3[k], (T)cg3_gw(k));
+        }
+        const T r_r = S.rr[i], b_r = S.br[i], r = S.rho[i], u = S.u[i], v = S.v[i], w = S.w[i];
+        const T G1 = (T)2.0 * u * grx, G2 = u * gry + v * grx, G3 = u * grz + w * grx;
+        const T G4 = G2, G5 = (T)2.0 * v * gry, G6 = v * grz + w * gry;
+        const T G7 = G3, G8 = G6, G9 = (T)2.0 * w * grz;
+        const T ugr = u * grx + v * gry + w * grz;
+        const T cu1 = u * u + v * v + w * w;
+        const T gnorm = std::sqrt(cgx * cgx + cgy * cgy + cgz * cgz);
+        const T k_r = r_r / r, k_b = b_r / r, k_k = (T)p.beta * r_r * b_r / r;
+        const T mean_nu = (T)1.0 / (r_r / (r * (T)p.r_viscosity) + b_r / (r * (T)p.b_viscosity));
+        const T omega_eff = (T)1.0 / ((T)3.0 * mean_nu + (T)0.5);
+        const T mean_alpha = (T)p.r_alpha * r_r / r + (T)p.b_alpha * b_r / r;
+        for (int k = 0; k < 19; ++k) {
+            const T cx = (T)cx3[k], cy = (T)cy3[k], cz = (T)cz3[k];
+            const T wk = (T)CG3_W[k];
+            T pert = 0, cosin = 0;
+            if (gnorm > (T)p.g_limit) {
+                const T pcg = cx * cgx + cy * cgy + cz * cgz;
+                const T cn = (T)std::sqrt((double)(cx3[k] * cx3[k] + cy3[k] * cy3[k] + cz3[k] * cz3[k]));
+                cosin = k != 0 ? pcg / (gnorm * cn) : (T)0;
+                pert = (T)p.A * gnorm * (wk * (pcg * pcg) / (gnorm * gnorm) - (T)cg3_wpert(k));
+            }
+            const T cu2 = u * cx + v * cy + w * cz;
+            const T rest = (T)cg3_phi(k) + (T)cg3_teta(k) * mean_alpha;
+            T feq = r * (rest + wk * ((T)3. * cu2 + (T)4.5 * cu2 * cu2 - (T)1.5 * cu1));
+            if (p.enhanced) {
+                T TC = 0;
+                TC += G1 * cx * cx;
+                TC += G2 * cx * cy;
+                TC += G3 * cx * cz;
+                TC += G4 * cx * cy;
+                TC += G5 * cy * cy;
+                TC += G6 * cy * cz;
+                TC += G7 * cx * cz;
+                TC += G8 * cy * cz;
+                TC += G9 * cz * cz;
+                feq = mean_nu * ((T)cg3_chi(k) * ugr + (T)cg3_psi(k) * TC) + feq;
+            }
+            const T fk = S.rf[i + k * N] + S.bf[i + k * N];
+            const T fp = omega_eff * feq + ((T)1 - omega_eff) * fk + pert;
+            S.rfc[i + k * N] = k_r * fp + k_k * cosin * rest;
+            S.bfc[i + k * N] = k_b * fp - k_k * cosin * rest;
+        }
+    }
+}
+
+template <class T>
+void cg3_stream(CgState3<T> &S) {
+    const size_t N = (size_t)S.N;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < S.N; ++i) {
+        const int x = i % S.n, y = (i / S.n) % S.m, z = i / (S.n * S.m);
+        for (int d = 0; d < 19; ++d) {
+            const int j = S.wrap(x - cx3[d], y - cy3[d], z - cz3[d]);
+            S.rf[i + d * N] = S.rfc[j + d * N];
+            S.bf[i + d * N] = S.bfc[j + d * N];
+        }
+    }
+}
+
+template <class T>
+void cg3_alloc(CgState3<T> &S, int n, int m, int h, const orc_cg_params *p) {
+    S.n = n;
+    S.m = m;
+    S.h = h;
+    S.N = n * m * h;
+    S.p = *p;
+    const size_t Q = 19 * (size_t)S.N;
+    S.rf.assign(Q, (T)0);
+    S.bf.assign(Q, (T)0);
+    S.rfc.assign(Q, (T)0);
+    S.bfc.assign(Q, (T)0);
+    for (auto *a : {&S.rr, &S.br, &S.rho, &S.u, &S.v, &S.w}) a->assign(S.N, (T)0);
+}
+
+template <class T>
+int run_cg3(int n, int m, int h, const orc_cg_params *p, const double *r0, const double *b0, int steps,
+            int extra_collide, double *out_rfc, double *out_bfc, double *out_rr, double *out_br, double *out_u,
+            double *out_v, double *out_w, double *out_laplace) {
+    CgState3<T> S;
+    cg3_alloc(S, n, m, h, p);
+    const size_t Q = 19 * (size_t)S.N;
+    for (size_t k = 0; k < Q; ++k) {
+        S.rf[k] = (T)r0[k];
+        S.bf[k] = (T)b0[k];
+    }
+    cg3_macro(S);
+    for (int it = 0; it < steps; ++it) {
+        cg3_collide(S);
+        cg3_stream(S);
+        cg3_macro(S);
+    }
+    if (extra_collide) cg3_collide(S);
+    for (size_t k = 0; k < Q; ++k) {
+        if (out_rfc) out_rfc[k] = S.rfc[k];
+        if (out_bfc) out_bfc[k] = S.bfc[k];
+    }
+    double pin = 0, pout = 0, nin = 0, nout = 0, umax = 0;
+    for (int i = 0; i < S.N; ++i) {
+        if (out_rr) out_rr[i] = S.rr[i];
+        if (out_br) out_br[i] = S.br[i];
+        if (out_u) out_u[i] = S.u[i];
+        if (out_v) out_v[i] = S.v[i];
+        if (out_w) out_w[i] = S.w[i];
+        const double chi = ((double)S.rr[i] - (double)S.br[i]) / (double)S.rho[i];
+        if (chi >= p->control_param) { pin += S.rr[i]; nin += 1; }
+        else if (chi <= -p->control_param) { pout += S.br[i]; nout += 1; }
+        const double um = sqrt((double)S.u[i] * S.u[i] + (double)S.v[i] * S.v[i] + (double)S.w[i] * S.w[i]);
+        if (um > umax) umax = um;
+    }
+    if (out_laplace) {
+        out_laplace[0] = pin;
+        out_laplace[1] = nin;
+        out_laplace[2] = pout;
+        out_laplace[3] = nout;
+        out_laplace[4] = umax;
+    }
+    return ORC_OK;
+}
+
+}  // namespace
+
+/* steps of the D3Q19 colour-gradient loop from post-streaming populations
+ * r0, b0 (19*n*m*h each); extra_collide as in orc_run. */
+extern "C" int orc_run_cg3d(int fp64, int n, int m, int h, const orc_cg_params *p, const double *r0,
+                            const double *b0, int steps, int extra_collide, double *out_rfc, double *out_bfc,
+                            double *out_rr, double *out_br, double *out_u, double *out_v, double *out_w,
+                            double *out_laplace) {
+    if (n < 5 || m < 5 || h < 5 || !p || !r0 || !b0) return ORC_BAD_INPUT;
+    if (p->g != 0.0) return ORC_UNSUPPORTED;
+    if (fp64)
+        return run_cg3<double>(n, m, h, p, r0, b0, steps, extra_collide, out_rfc, out_bfc, out_rr, out_br, out_u,
+                               out_v, out_w, out_laplace);
+    return run_cg3<float>(n, m, h, p, r0, b0, steps, extra_collide, out_rfc, out_bfc, out_rr, out_br, out_u, out_v,
+                          out_w, out_laplace);
+}
+
+/* One D3Q19 colour-gradient collision from given macroscopic fields and
+ * summed populations f (the inputs of gpuCollBgkwGC3D), for pinning against
+ * the reference kernel. */
+extern "C" int orc_cg3d_collide(int fp64, int n, int m, int h, const orc_cg_params *p, const double *rho,
+                                const double *r_rho, const double *b_rho, const double *u, const double *v,
+                                const double *w, const double *f, double *out_rfc, double *out_bfc) {
+    auto go = [&](auto tag) {
+        using T = decltype(tag);
+        CgState3<T> S;
+        cg3_alloc(S, n, m, h, p);
+        const size_t Q = 19 * (size_t)S.N;
+        for (size_t k = 0; k < Q; ++k) S.rf[k] = (T)f[k];
+        for (int i = 0; i < S.N; ++i) {
+            S.rr[i] = (T)r_rho[i];
+            S.br[i] = (T)b_rho[i];
+            S.rho[i] = (T)rho[i];
+            S.u[i] = (T)u[i];
+            S.v[i] = (T)v[i];
+            S.w[i] = (T)w[i];
+        }
+        cg3_collide(S);
+        for (size_t k = 0; k < Q; ++k) {
+            out_rfc[k] = S.rfc[k];
+            out_bfc[k] = S.bfc[k];
+        }
+        return ORC_OK;
+    };
+    return fp64 ? go(0.0) : go(0.0f);
+}

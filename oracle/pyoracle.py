@@ -279,3 +279,57 @@ def cg_collide_pair(n, m, p, rho, r_rho, b_rho, u, v, f, fp64=False):
         L.ref_cg2d_collide(n, m, C.byref(p), *[_vp(a) for a in arrs], _vp(rr), _vp(bb), _vp(cd))
         ref = (rr.reshape(9, nn), bb.reshape(9, nn), cd)
     return (orc[0].reshape(9, nn), orc[1].reshape(9, nn)), ref
+
+
+def cg3_rest_populations(alpha, density):
+    """D3Q19 colour populations at rest (initCGBubble3D, GpuInit.cu:536-600,
+    with phi3D + theta3D alpha): density * (alpha, (1-alpha)/12 x6,
+    (1-alpha)/24 x12)."""
+    return density * np.array([alpha] + [(1 - alpha) / 12] * 6 + [(1 - alpha) / 24] * 12)
+
+
+def droplet3d(n, m, h, radius, p, centre=None):
+    """Red droplet in blue at rest on an n x m x h lattice: (19, N) each."""
+    c = centre if centre is not None else ((n - 1) / 2, (m - 1) / 2, (h - 1) / 2)
+    idx = np.arange(n * m * h)
+    x, y, z = idx % n, (idx // n) % m, idx // (n * m)
+    inside = (x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2 <= radius ** 2
+    r = np.where(inside[None, :], cg3_rest_populations(p.r_alpha, p.r_density)[:, None], 0.0)
+    b = np.where(~inside[None, :], cg3_rest_populations(p.b_alpha, p.b_density)[:, None], 0.0)
+    return np.ascontiguousarray(r), np.ascontiguousarray(b)
+
+
+def run_oracle_cg3(n, m, h, p, r0, b0, steps, fp64=False, extra_collide=False):
+    """The D3Q19 colour-gradient loop in the oracle: Result with rfc, bfc
+    (19, N), rr, br, u, v, w (N), laplace (5), rc."""
+    L = oracle_lib()
+    nn = n * m * h
+    r = Result()
+    r.rfc, r.bfc = np.zeros(19 * nn), np.zeros(19 * nn)
+    r.rr, r.br, r.u, r.v, r.w = (np.zeros(nn) for _ in range(5))
+    r.laplace = np.zeros(5)
+    r0 = np.ascontiguousarray(r0, np.float64).reshape(-1)
+    b0 = np.ascontiguousarray(b0, np.float64).reshape(-1)
+    r.rc = L.orc_run_cg3d(int(fp64), n, m, h, C.byref(p), _vp(r0), _vp(b0), int(steps), int(extra_collide),
+                          _vp(r.rfc), _vp(r.bfc), _vp(r.rr), _vp(r.br), _vp(r.u), _vp(r.v), _vp(r.w),
+                          _vp(r.laplace))
+    r.rfc, r.bfc = r.rfc.reshape(19, nn), r.bfc.reshape(19, nn)
+    return r
+
+
+def cg3_collide_pair(n, m, h, p, rho, r_rho, b_rho, u, v, w, f, fp64=False):
+    """One D3Q19 colour-gradient collision by the oracle and, where
+    oracle/_ref exists, by the reference kernel; as cg_collide_pair."""
+    arrs = [np.ascontiguousarray(a, np.float64).reshape(-1) for a in (rho, r_rho, b_rho, u, v, w, f)]
+    nn = n * m * h
+    orc = (np.zeros(19 * nn), np.zeros(19 * nn))
+    rc = oracle_lib().orc_cg3d_collide(int(fp64), n, m, h, C.byref(p), *[_vp(a) for a in arrs],
+                                       _vp(orc[0]), _vp(orc[1]))
+    assert rc == 0
+    ref = None
+    L = ref_lib(fp64)
+    if L is not None:
+        rr, bb, cd = np.zeros(19 * nn), np.zeros(19 * nn), np.zeros(nn, np.int32)
+        L.ref_cg3d_collide(n, m, h, C.byref(p), *[_vp(a) for a in arrs], _vp(rr), _vp(bb), _vp(cd))
+        ref = (rr.reshape(19, nn), bb.reshape(19, nn), cd)
+    return (orc[0].reshape(19, nn), orc[1].reshape(19, nn)), ref

@@ -404,6 +404,67 @@ int ref_cg2d_collide(int n, int m, const ref_cg_params *cp, const double *rho, c
     return 0;
 }
 
+/* One D3Q19 colour-gradient collision by gpuCollBgkwGC3D /
+ * gpuCollEnhancedBgkwGC3D (GpuCollision.cu:709-880) on given fields, with
+ * the reference's gradient-direction map (GpuInit.cu:262-321) in
+ * out_cgdir. */
+int ref_cg3d_collide(int n, int m, int h, const ref_cg_params *cp, const double *rho, const double *r_rho,
+                     const double *b_rho, const double *u, const double *v, const double *w, const double *f,
+                     double *out_rfc, double *out_bfc, int *out_cgdir) {
+    const int ms = n * m * h;
+    Arguments args;
+    memset(&args, 0, sizeof(args));
+    args.viscosity = (FLOAT_TYPE)0.1;
+    args.multiPhase = 1;
+    args.r_density = (FLOAT_TYPE)cp->r_density;
+    args.b_density = (FLOAT_TYPE)cp->b_density;
+    args.r_alpha = (FLOAT_TYPE)cp->r_alpha;
+    args.b_alpha = (FLOAT_TYPE)cp->b_alpha;
+    args.r_viscosity = (FLOAT_TYPE)cp->r_viscosity;
+    args.b_viscosity = (FLOAT_TYPE)cp->b_viscosity;
+    args.beta = (FLOAT_TYPE)cp->beta;
+    args.A = (FLOAT_TYPE)cp->A;
+    args.g_limit = (FLOAT_TYPE)cp->g_limit;
+    args.control_param = (FLOAT_TYPE)cp->control_param;
+    args.g = (FLOAT_TYPE)cp->g;
+    args.external_force = cp->external_force != 0;
+    args.bubble_radius = (FLOAT_TYPE)1.0;
+    initConstants3D(&args, 0, 0, 0, 0, 1, m, n, h);
+    std::vector<int> cgdir(ms, 0), fluid(ms, 1);
+    if (cp->high_order)
+        initHOColorGradient3D(cgdir.data(), n, m, h);
+    else
+        initColorGradient3D(cgdir.data(), n, m, h);
+    std::vector<FLOAT_TYPE> R(ms), RR(ms), BR(ms), U(ms), V(ms), W(ms), F(19 * (size_t)ms),
+        RC(19 * (size_t)ms, 0), BC(19 * (size_t)ms, 0);
+    for (int i = 0; i < ms; ++i) {
+        R[i] = (FLOAT_TYPE)rho[i];
+        RR[i] = (FLOAT_TYPE)r_rho[i];
+        BR[i] = (FLOAT_TYPE)b_rho[i];
+        U[i] = (FLOAT_TYPE)u[i];
+        V[i] = (FLOAT_TYPE)v[i];
+        W[i] = (FLOAT_TYPE)w[i];
+    }
+    for (size_t k = 0; k < 19 * (size_t)ms; ++k) F[k] = (FLOAT_TYPE)f[k];
+    shim_dim3 tpb{THREADS, THREADS, 1};
+    unsigned side = (unsigned)(sqrt((double)ms) / THREADS) + 1;
+    shim_dim3 bpg1{side, side, 1};
+    launch(bpg1, tpb, [&] {
+        if (cp->enhanced)
+            gpuCollEnhancedBgkwGC3D(fluid.data(), R.data(), RR.data(), BR.data(), U.data(), V.data(), W.data(),
+                                    F.data(), RC.data(), BC.data(), cgdir.data(), cp->high_order != 0);
+        else
+            gpuCollBgkwGC3D(fluid.data(), R.data(), RR.data(), BR.data(), U.data(), V.data(), W.data(), F.data(),
+                            RC.data(), BC.data(), cgdir.data(), cp->high_order != 0);
+    });
+    for (size_t k = 0; k < 19 * (size_t)ms; ++k) {
+        out_rfc[k] = RC[k];
+        out_bfc[k] = BC[k];
+    }
+    if (out_cgdir) memcpy(out_cgdir, cgdir.data(), sizeof(int) * (size_t)ms);
+    return 0;
+}
+
 /* The reference's MRT matrices (CellFunctions.cu:7-153) for a given omega. */
 void ref_mrt_matrices(int q, double omega, double *vel_mom_map, double *mom_coll_mtx) {
     int n = q * q;

@@ -22,6 +22,7 @@
 #include <string>
 #include <vector>
 
+#include "lbm_cg3.cuh"
 #include "lbm_device.cuh"
 #include "thesis_lbm.h"
 
@@ -174,8 +175,8 @@ __global__ void __launch_bounds__(CG_BLOCK) cg_collide_kernel(const CgArgs a) {
 // count where chi <= -c, max |u| (Iterate.cu:496-499, GpuUpdateMacro.cu:122-133).
 constexpr int LAP_BLOCKS = 304, LAP_THREADS = 256;
 __global__ void __launch_bounds__(LAP_THREADS)
-cg_laplace_partial(const float *R, const float *B, const float *ux, const float *uy, long long n, float c,
-                   double *partial) {
+cg_laplace_partial(const float *R, const float *B, const float *ux, const float *uy, const float *uz, long long n,
+                   float c, double *partial) {
     double acc[5] = {0, 0, 0, 0, 0};
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const double r = R[i], b = B[i], chi = (r - b) / (r + b);
@@ -186,7 +187,8 @@ cg_laplace_partial(const float *R, const float *B, const float *ux, const float 
             acc[2] += b;
             acc[3] += 1;
         }
-        const double um = sqrt((double)ux[i] * ux[i] + (double)uy[i] * uy[i]);
+        const double wz = uz ? (double)uz[i] : 0.0;
+        const double um = sqrt((double)ux[i] * ux[i] + (double)uy[i] * uy[i] + wz * wz);
         acc[4] = um > acc[4] ? um : acc[4];
     }
     __shared__ double sm[LAP_THREADS][5];
@@ -223,11 +225,11 @@ int cg_fail(int code, const std::string &m) {
 using namespace lbm;
 
 struct lbm_cg_handle_s {
-    int n = 0, m = 0;
+    int n = 0, m = 0, h = 1, q = 9;  // D2Q9 (h = 1) or D3Q19
     long long N = 0;
     lbm_cg_params P{};
-    float *buf = nullptr;  // 2 buffers x 2 colours x 9 directions x N
-    float *R = nullptr, *B = nullptr, *rho = nullptr, *ux = nullptr, *uy = nullptr;
+    float *buf = nullptr;  // 2 buffers x 2 colours x q directions x N
+    float *R = nullptr, *B = nullptr, *rho = nullptr, *ux = nullptr, *uy = nullptr, *uz = nullptr;
     double *partial = nullptr, *sums = nullptr;
     int cur = 0;
     cudaStream_t stream = nullptr;
@@ -263,6 +265,47 @@ static CgArgs cg_args(const lbm_cg_handle_s *H, int from, int write_macro) {
     return a;
 }
 
+static Cg3Args cg3_args(const lbm_cg_handle_s *H, int from, int write_macro) {
+    Cg3Args a;
+    memset(&a, 0, sizeof(a));
+    const size_t N = (size_t)H->N;
+    a.in = H->buf + (size_t)from * 38 * N;
+    a.out = H->buf + (size_t)(1 - from) * 38 * N;
+    a.R = H->R;
+    a.B = H->B;
+    a.rho = H->rho;
+    a.ux = H->ux;
+    a.uy = H->uy;
+    a.uz = H->uz;
+    a.nx = H->n;
+    a.ny = H->m;
+    a.nz = H->h;
+    a.N = H->N;
+    a.write_macro = write_macro;
+    a.r_alpha = (float)H->P.r_alpha;
+    a.b_alpha = (float)H->P.b_alpha;
+    a.r_visc = (float)H->P.r_viscosity;
+    a.b_visc = (float)H->P.b_viscosity;
+    a.beta = (float)H->P.beta;
+    a.A = (float)H->P.A;
+    a.g_limit = (float)H->P.g_limit;
+    return a;
+}
+
+template <bool PULL>
+static void cg3_launch(const lbm_cg_handle_s *H, int from, int write_macro, cudaStream_t s) {
+    const Cg3Args a = cg3_args(H, from, write_macro);
+    const dim3 grid((unsigned)((H->n + CG3_BLOCK - 1) / CG3_BLOCK), (unsigned)H->m, (unsigned)H->h);
+    cg3_density_kernel<PULL><<<grid, CG3_BLOCK, 0, s>>>(a);
+    if (H->P.high_order) {
+        if (H->P.enhanced) cg3_collide_kernel<PULL, true, true><<<grid, CG3_BLOCK, 0, s>>>(a);
+        else cg3_collide_kernel<PULL, true, false><<<grid, CG3_BLOCK, 0, s>>>(a);
+    } else {
+        if (H->P.enhanced) cg3_collide_kernel<PULL, false, true><<<grid, CG3_BLOCK, 0, s>>>(a);
+        else cg3_collide_kernel<PULL, false, false><<<grid, CG3_BLOCK, 0, s>>>(a);
+    }
+}
+
 template <bool PULL>
 static void cg_launch(const lbm_cg_handle_s *H, const CgArgs &a, cudaStream_t s) {
     const dim3 grid((unsigned)((H->n + CG_BLOCK - 1) / CG_BLOCK), (unsigned)H->m);
@@ -280,21 +323,25 @@ extern "C" {
 
 const char *lbm_cg_last_error(void) { return g_cg_error.c_str(); }
 
-int lbm_cg_create(int n, int m, const lbm_cg_params *P, lbm_cg_handle *out) {
+static int cg_create(int n, int m, int h, const lbm_cg_params *P, lbm_cg_handle *out) {
     if (!P || !out) return cg_fail(LBM_ERR_INVALID, "null argument");
     *out = nullptr;
-    if (n < 5 || m < 5 || m > 65535) return cg_fail(LBM_ERR_INVALID, "lattice must be at least 5x5 (m <= 65535)");
+    if (n < 5 || m < 5 || h < 1 || m > 65535 || h > 65535 || (h > 1 && h < 5))
+        return cg_fail(LBM_ERR_INVALID, "lattice must be at least 5 nodes along each axis (m, h <= 65535)");
+    if ((long long)n * m * h >= (1ll << 31)) return cg_fail(LBM_ERR_INVALID, "more than 2^31 nodes");
     if (P->storage != LBM_STORE_F32) return cg_fail(LBM_ERR_UNSUPPORTED, "colour-gradient storage is F32");
     if (!(P->r_viscosity > 0) || !(P->b_viscosity > 0)) return cg_fail(LBM_ERR_INVALID, "viscosities must be positive");
     lbm_cg_handle_s *H = new (std::nothrow) lbm_cg_handle_s();
     if (!H) return cg_fail(LBM_ERR_NOMEM, "out of host memory");
     H->n = n;
     H->m = m;
-    H->N = (long long)n * m;
+    H->h = h;
+    H->q = h > 1 ? 19 : 9;
+    H->N = (long long)n * m * h;
     H->P = *P;
     const size_t N = (size_t)H->N;
-    cudaError_t e = cudaMalloc((void **)&H->buf, sizeof(float) * 36 * N);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&H->R, sizeof(float) * 5 * N);
+    cudaError_t e = cudaMalloc((void **)&H->buf, sizeof(float) * 4 * H->q * N);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&H->R, sizeof(float) * 6 * N);
     if (e == cudaSuccess) e = cudaMalloc((void **)&H->partial, sizeof(double) * (LAP_BLOCKS * 5 + 5));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&H->stepped, cudaEventDisableTiming);
@@ -306,22 +353,33 @@ int lbm_cg_create(int n, int m, const lbm_cg_params *P, lbm_cg_handle *out) {
     H->rho = H->R + 2 * N;
     H->ux = H->R + 3 * N;
     H->uy = H->R + 4 * N;
+    H->uz = H->R + 5 * N;
     H->sums = H->partial + LAP_BLOCKS * 5;
-    cudaMemset(H->R, 0, sizeof(float) * 5 * N);
+    cudaMemset(H->R, 0, sizeof(float) * 6 * N);
     *out = H;
     return LBM_OK;
 }
 
+int lbm_cg_create(int n, int m, const lbm_cg_params *P, lbm_cg_handle *out) { return cg_create(n, m, 1, P, out); }
+
+int lbm_cg_create3d(int n, int m, int h, const lbm_cg_params *P, lbm_cg_handle *out) {
+    if (h < 5) return cg_fail(LBM_ERR_INVALID, "lattice must be at least 5 nodes along each axis");
+    return cg_create(n, m, h, P, out);
+}
+
 int lbm_cg_init(lbm_cg_handle H, const float *r_f, const float *b_f) {
     if (!H || !r_f || !b_f) return cg_fail(LBM_ERR_INVALID, "null argument");
-    const size_t N = (size_t)H->N;
+    const size_t N = (size_t)H->N, Q = (size_t)H->q;
     // the given post-stream state goes to buffer 1; one collision without
     // streaming turns it into the post-collision state in buffer 0
-    float *b1 = H->buf + 18 * N;
-    cudaError_t e = cudaMemcpyAsync(b1, r_f, sizeof(float) * 9 * N, cudaMemcpyHostToDevice, H->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(b1 + 9 * N, b_f, sizeof(float) * 9 * N, cudaMemcpyHostToDevice, H->stream);
+    float *b1 = H->buf + 2 * Q * N;
+    cudaError_t e = cudaMemcpyAsync(b1, r_f, sizeof(float) * Q * N, cudaMemcpyHostToDevice, H->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b1 + Q * N, b_f, sizeof(float) * Q * N, cudaMemcpyHostToDevice, H->stream);
     if (e != cudaSuccess) return cg_fail(LBM_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(e));
-    cg_launch<false>(H, cg_args(H, 1, 1), H->stream);
+    if (H->q == 19)
+        cg3_launch<false>(H, 1, 1, H->stream);
+    else
+        cg_launch<false>(H, cg_args(H, 1, 1), H->stream);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
     if (e != cudaSuccess) return cg_fail(LBM_ERR_CUDA, std::string("init: ") + cudaGetErrorString(e));
@@ -333,7 +391,11 @@ int lbm_cg_step(lbm_cg_handle H, int nsteps, int write_macro_last, void *stream)
     if (!H || nsteps < 0) return cg_fail(LBM_ERR_INVALID, "invalid argument");
     cudaStream_t s = stream ? (cudaStream_t)stream : H->stream;
     for (int i = 0; i < nsteps; ++i) {
-        cg_launch<true>(H, cg_args(H, H->cur, write_macro_last && i == nsteps - 1), s);
+        const int wm = write_macro_last && i == nsteps - 1;
+        if (H->q == 19)
+            cg3_launch<true>(H, H->cur, wm, s);
+        else
+            cg_launch<true>(H, cg_args(H, H->cur, wm), s);
         H->cur ^= 1;
     }
     cudaError_t e = cudaGetLastError();
@@ -354,13 +416,21 @@ int lbm_cg_get_macro(lbm_cg_handle H, float *r_rho, float *b_rho, float *u, floa
     return LBM_OK;
 }
 
+int lbm_cg_get_macro3d(lbm_cg_handle H, float *r_rho, float *b_rho, float *u, float *v, float *w) {
+    int rc = lbm_cg_get_macro(H, r_rho, b_rho, u, v);
+    if (rc || !w) return rc;
+    cudaError_t e = cudaMemcpy(w, H->uz, sizeof(float) * (size_t)H->N, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cg_fail(LBM_ERR_CUDA, std::string("read-back: ") + cudaGetErrorString(e));
+    return LBM_OK;
+}
+
 int lbm_cg_get_populations(lbm_cg_handle H, float *r, float *b) {
     if (!H || !r || !b) return cg_fail(LBM_ERR_INVALID, "null argument");
-    const size_t N = (size_t)H->N;
+    const size_t N = (size_t)H->N, Q = (size_t)H->q;
     cudaError_t e = cudaDeviceSynchronize();
-    const float *src = H->buf + (size_t)H->cur * 18 * N;
-    if (e == cudaSuccess) e = cudaMemcpy(r, src, sizeof(float) * 9 * N, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(b, src + 9 * N, sizeof(float) * 9 * N, cudaMemcpyDeviceToHost);
+    const float *src = H->buf + (size_t)H->cur * 2 * Q * N;
+    if (e == cudaSuccess) e = cudaMemcpy(r, src, sizeof(float) * Q * N, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(b, src + Q * N, sizeof(float) * Q * N, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cg_fail(LBM_ERR_CUDA, std::string("read-back: ") + cudaGetErrorString(e));
     return LBM_OK;
 }
@@ -368,8 +438,8 @@ int lbm_cg_get_populations(lbm_cg_handle H, float *r, float *b) {
 int lbm_cg_laplace(lbm_cg_handle H, double *out) {
     if (!H || !out) return cg_fail(LBM_ERR_INVALID, "null argument");
     if (H->stepped) cudaStreamWaitEvent(H->stream, H->stepped, 0);
-    cg_laplace_partial<<<LAP_BLOCKS, LAP_THREADS, 0, H->stream>>>(H->R, H->B, H->ux, H->uy, H->N,
-                                                                   (float)H->P.control_param, H->partial);
+    cg_laplace_partial<<<LAP_BLOCKS, LAP_THREADS, 0, H->stream>>>(H->R, H->B, H->ux, H->uy, H->q == 19 ? H->uz : nullptr,
+                                                                   H->N, (float)H->P.control_param, H->partial);
     cg_laplace_final<<<1, 32, 0, H->stream>>>(H->partial, H->sums);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, H->sums, sizeof(double) * 5, cudaMemcpyDeviceToHost, H->stream);
@@ -381,6 +451,8 @@ int lbm_cg_laplace(lbm_cg_handle H, double *out) {
 }
 
 long long lbm_cg_nodes(lbm_cg_handle H) { return H ? H->N : -1; }
+
+int lbm_cg_q(lbm_cg_handle H) { return H ? H->q : -1; }
 
 void lbm_cg_destroy(lbm_cg_handle H) {
     if (!H) return;

@@ -60,6 +60,29 @@ def create_bubble(n, m, args: CgArguments, x=None, y=None):
     return np.ascontiguousarray(r), np.ascontiguousarray(b)
 
 
+def rest_weights3d(alpha):
+    """D3Q19 phi_k + theta_k alpha of a colour at rest (GpuInit.cu:905-913):
+    alpha, (1-alpha)/12 on the axes, (1-alpha)/24 on the diagonals."""
+    return np.array([alpha] + [(1 - alpha) / 12] * 6 + [(1 - alpha) / 24] * 12)
+
+
+def create_bubble3d(n, m, h, args: CgArguments, radius_nodes=None):
+    """Red sphere of radius `args.bubble_radius` * n nodes (or radius_nodes)
+    centred in the box, blue around it (initCGBubble3D test case 1,
+    GpuInit.cu:536-600): each colour's populations are its density times
+    phi_k (1/12 on the axes, 1/24 on the diagonals, 0 at rest), as the
+    reference starts them whatever alpha.  Returns (19, n*m*h) float64
+    each."""
+    R = args.bubble_radius * n if radius_nodes is None else radius_nodes
+    idx = np.arange(n * m * h)
+    x, y, z = idx % n, (idx // n) % m, idx // (n * m)
+    inside = (x - (n - 1) / 2) ** 2 + (y - (m - 1) / 2) ** 2 + (z - (h - 1) / 2) ** 2 <= R * R
+    phi = rest_weights3d(0.0)
+    r = np.where(inside[None, :], (args.r_density * phi)[:, None], 0.0)
+    b = np.where(~inside[None, :], (args.b_density * phi)[:, None], 0.0)
+    return np.ascontiguousarray(r), np.ascontiguousarray(b)
+
+
 def predicted_surface_tension(args: CgArguments):
     """sigma = 4 A / (9 omega_eff) with omega_eff from the density-weighted
     harmonic mean viscosity (Iterate.cu:163-168)."""
@@ -67,6 +90,15 @@ def predicted_surface_tension(args: CgArguments):
     mean_nu = 1.0 / (rd / ((rd + bd) * args.r_viscosity) + bd / ((rd + bd) * args.b_viscosity))
     omega_eff = 1.0 / (3.0 * mean_nu + 0.5)
     return 4.0 * args.A / 9.0 / omega_eff
+
+
+def laplace_pressure_jump3d(laplace, args: CgArguments):
+    """Mean pressures inside and outside a 3D drop from the Laplace sums,
+    p = (1/2)(1 - alpha) rho_colour (calculateSurfaceTension3D,
+    Multiphase.cu:1093-1102); returns p_in - p_out."""
+    p_in = laplace[0] / laplace[1] if laplace[1] > 0 else 0.0
+    p_out = laplace[2] / laplace[3] if laplace[3] > 0 else 0.0
+    return 0.5 * (1.0 - args.r_alpha) * p_in - 0.5 * (1.0 - args.b_alpha) * p_out
 
 
 def surface_tension_error(laplace, args: CgArguments, radius_nodes):
@@ -87,15 +119,25 @@ def _fp(a):
 
 
 class CgSolver:
-    """One periodic n x m colour-gradient lattice on the GPU."""
+    """One periodic n x m (D2Q9) or n x m x h (D3Q19, h given)
+    colour-gradient lattice on the GPU."""
 
-    def __init__(self, n, m, args: CgArguments):
+    def __init__(self, n, m, args: CgArguments, h=None):
         self.n, self.m, self.args = n, m, args
+        self.h = 1 if h is None else int(h)
+        self.q = 9 if h is None else 19
         self._lib = N.lib()
-        h = C.c_void_p()
+        hd = C.c_void_p()
         p = args.to_c()
-        N.check_cg(self._lib.lbm_cg_create(n, m, C.byref(p), C.byref(h)))
-        self._h = h
+        if h is None:
+            N.check_cg(self._lib.lbm_cg_create(n, m, C.byref(p), C.byref(hd)))
+        else:
+            N.check_cg(self._lib.lbm_cg_create3d(n, m, self.h, C.byref(p), C.byref(hd)))
+        self._h = hd
+
+    @property
+    def num_nodes(self):
+        return self.n * self.m * self.h
 
     def close(self):
         if getattr(self, "_h", None):
@@ -117,8 +159,8 @@ class CgSolver:
     def init(self, r_f, b_f):
         r = np.ascontiguousarray(r_f, np.float32).reshape(-1)
         b = np.ascontiguousarray(b_f, np.float32).reshape(-1)
-        if r.size != 9 * self.n * self.m or b.size != r.size:
-            raise ValueError("populations must hold 9*n*m values per colour")
+        if r.size != self.q * self.num_nodes or b.size != r.size:
+            raise ValueError("populations must hold %d values per node and colour" % self.q)
         N.check_cg(self._lib.lbm_cg_init(self._h, _fp(r), _fp(b)))
 
     def step(self, nsteps, write_macro=True, stream=None):
@@ -126,15 +168,19 @@ class CgSolver:
                                          None if stream is None else C.c_void_p(stream)))
 
     def macro(self):
-        out = [np.empty(self.n * self.m, np.float32) for _ in range(4)]
-        N.check_cg(self._lib.lbm_cg_get_macro(self._h, *[_fp(a) for a in out]))
+        """rho_r, rho_b, u, v (and w in 3D)."""
+        out = [np.empty(self.num_nodes, np.float32) for _ in range(4 if self.q == 9 else 5)]
+        if self.q == 9:
+            N.check_cg(self._lib.lbm_cg_get_macro(self._h, *[_fp(a) for a in out]))
+        else:
+            N.check_cg(self._lib.lbm_cg_get_macro3d(self._h, *[_fp(a) for a in out]))
         return out
 
     def populations(self):
-        r = np.empty(9 * self.n * self.m, np.float32)
+        r = np.empty(self.q * self.num_nodes, np.float32)
         b = np.empty_like(r)
         N.check_cg(self._lib.lbm_cg_get_populations(self._h, _fp(r), _fp(b)))
-        return r.reshape(9, -1), b.reshape(9, -1)
+        return r.reshape(self.q, -1), b.reshape(self.q, -1)
 
     def laplace(self):
         out = np.zeros(5, np.float64)

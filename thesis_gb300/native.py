@@ -137,6 +137,9 @@ def lib():
                                               C.c_double]),
         "lbm_io_last_error": (C.c_char_p, []),
         "lbm_cg_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(CgParams), C.POINTER(vp)]),
+        "lbm_cg_create3d": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(CgParams), C.POINTER(vp)]),
+        "lbm_cg_get_macro3d": (C.c_int, [vp, fp, fp, fp, fp, fp]),
+        "lbm_cg_q": (C.c_int, [vp]),
         "lbm_cg_init": (C.c_int, [vp, fp, fp]),
         "lbm_cg_step": (C.c_int, [vp, C.c_int, C.c_int, vp]),
         "lbm_cg_get_macro": (C.c_int, [vp, fp, fp, fp, fp]),
