@@ -230,6 +230,7 @@ struct lbm_cg_handle_s {
     lbm_cg_params P{};
     float *buf = nullptr;  // 2 buffers x 2 colours x q directions x N
     float *R = nullptr, *B = nullptr, *rho = nullptr, *ux = nullptr, *uy = nullptr, *uz = nullptr;
+    float *phi = nullptr, *dn = nullptr;  // D3Q19: colour field and density for the gradients
     double *partial = nullptr, *sums = nullptr;
     int cur = 0;
     cudaStream_t stream = nullptr;
@@ -273,6 +274,8 @@ static Cg3Args cg3_args(const lbm_cg_handle_s *H, int from, int write_macro) {
     a.out = H->buf + (size_t)(1 - from) * 38 * N;
     a.R = H->R;
     a.B = H->B;
+    a.phi = H->phi;
+    a.dn = H->dn;
     a.rho = H->rho;
     a.ux = H->ux;
     a.uy = H->uy;
@@ -341,7 +344,7 @@ static int cg_create(int n, int m, int h, const lbm_cg_params *P, lbm_cg_handle 
     H->P = *P;
     const size_t N = (size_t)H->N;
     cudaError_t e = cudaMalloc((void **)&H->buf, sizeof(float) * 4 * H->q * N);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&H->R, sizeof(float) * 6 * N);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&H->R, sizeof(float) * 8 * N);
     if (e == cudaSuccess) e = cudaMalloc((void **)&H->partial, sizeof(double) * (LAP_BLOCKS * 5 + 5));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&H->stepped, cudaEventDisableTiming);
@@ -354,8 +357,10 @@ static int cg_create(int n, int m, int h, const lbm_cg_params *P, lbm_cg_handle 
     H->ux = H->R + 3 * N;
     H->uy = H->R + 4 * N;
     H->uz = H->R + 5 * N;
+    H->phi = H->R + 6 * N;
+    H->dn = H->R + 7 * N;
     H->sums = H->partial + LAP_BLOCKS * 5;
-    cudaMemset(H->R, 0, sizeof(float) * 6 * N);
+    cudaMemset(H->R, 0, sizeof(float) * 8 * N);
     *out = H;
     return LBM_OK;
 }

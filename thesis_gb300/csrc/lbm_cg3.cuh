@@ -5,15 +5,16 @@
 // of gpuUpdateMacro3DCG, GpuUpdateMacro.cu:215-360).
 //
 // The same two launches per step as the D2Q9 path (lbm_cg.cu):
-//   cg3_density_kernel  pull both colours, write rho_r and rho_b per node;
-//   cg3_collide_kernel  pull both colours again, take the neighbours' colour
-//                       field (rho_r - rho_b)/rho from the density arrays,
-//                       collide, perturb, recolour, write both colours.
+//   cg3_density_kernel  pull both colours, write the colour field
+//                       phi = (rho_r - rho_b)/rho and rho per node;
+//   cg3_collide_kernel  pull both colours again, take the neighbours' phi and
+//                       rho for the gradients, collide, perturb, recolour,
+//                       write both colours and the node's rho_r, rho_b.
 // State between steps: post-collision red and blue populations, SoA by
 // direction (direction d of colour c at base + (c*19 + d) N), pull double
 // buffer.  Per update the two kernels read 2 x 152 B of populations and
-// write 152 B, plus 8 B of densities written and the neighbours' densities
-// read through L1/L2.
+// write 152 B, plus 16 B of per-node fields written and the neighbours'
+// phi and rho read through L1/L2.
 #pragma once
 #include "lbm_device.cuh"
 
@@ -22,7 +23,8 @@ namespace lbm {
 struct Cg3Args {
     const float *in;   // red directions 0..18, then blue, N floats each
     float *out;
-    float *R, *B;      // colour densities
+    float *R, *B;      // colour densities (output)
+    float *phi, *dn;   // colour field and density of the streamed state (gradients)
     float *rho, *ux, *uy, *uz;
     int nx, ny, nz;
     long long N;
@@ -31,23 +33,42 @@ struct Cg3Args {
 };
 
 constexpr int CG3_BLOCK = 128;
+// minimum resident blocks per SM the collide kernel is compiled for (a
+// register cap of 65536 / (128 * CG3_MINB) per thread)
+#ifndef CG3_MINB
+#define CG3_MINB 5
+#endif
 
 __device__ __forceinline__ int cg3_wrap(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
-// Both colours of node (x, y, z) after streaming (PULL) or as stored.
+// Wrapped neighbour coordinates of node (x, y, z) as node-index parts:
+// X[1 + t] + Y[1 + t'] + Z[1 + t''] is the node at offset (t, t', t''),
+// t in {-1, 0, 1}.  Node indices fit in 32 bits (fewer than 2^31 nodes).
+struct Cg3Nb {
+    int X[3], Y[3], Z[3];
+    __device__ __forceinline__ Cg3Nb(const Cg3Args &a, int x, int y, int z) {
+        const int plane = a.nx * a.ny;
+        X[0] = x == 0 ? a.nx - 1 : x - 1;
+        X[1] = x;
+        X[2] = x == a.nx - 1 ? 0 : x + 1;
+        Y[0] = (y == 0 ? a.ny - 1 : y - 1) * a.nx;
+        Y[1] = y * a.nx;
+        Y[2] = (y == a.ny - 1 ? 0 : y + 1) * a.nx;
+        Z[0] = (z == 0 ? a.nz - 1 : z - 1) * plane;
+        Z[1] = z * plane;
+        Z[2] = (z == a.nz - 1 ? 0 : z + 1) * plane;
+    }
+    __device__ __forceinline__ int at(int cx, int cy, int cz) const { return X[1 + cx] + Y[1 + cy] + Z[1 + cz]; }
+};
+
+// Both colours of the node after streaming (PULL: population d from the
+// node at -c_d) or as stored.
 template <bool PULL>
-__device__ __forceinline__ void cg3_gather(const Cg3Args &a, int x, int y, int z, float (&r)[19], float (&b)[19]) {
+__device__ __forceinline__ void cg3_gather(const Cg3Args &a, const Cg3Nb &nb, float (&r)[19], float (&b)[19]) {
     using L = Lat<19>;
 #pragma unroll
     for (int d = 0; d < 19; ++d) {
-        long long s;
-        if (PULL) {
-            const int sx = cg3_wrap(x - L::cx(d), a.nx), sy = cg3_wrap(y - L::cy(d), a.ny),
-                      sz = cg3_wrap(z - L::cz(d), a.nz);
-            s = sx + (long long)a.nx * (sy + (long long)a.ny * sz);
-        } else {
-            s = x + (long long)a.nx * (y + (long long)a.ny * z);
-        }
+        const int s = PULL ? nb.at(-L::cx(d), -L::cy(d), -L::cz(d)) : nb.at(0, 0, 0);
         r[d] = __ldg(a.in + d * a.N + s);
         b[d] = __ldg(a.in + (19 + d) * a.N + s);
     }
@@ -58,16 +79,17 @@ __global__ void __launch_bounds__(CG3_BLOCK) cg3_density_kernel(const Cg3Args a)
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
     if (x >= a.nx) return;
     float r[19], b[19];
-    cg3_gather<PULL>(a, x, y, z, r, b);
+    cg3_gather<PULL>(a, Cg3Nb(a, x, y, z), r, b);
     float rr = 0.f, bb = 0.f;
 #pragma unroll
     for (int d = 0; d < 19; ++d) {
         rr += r[d];
         bb += b[d];
     }
-    const long long node = x + (long long)a.nx * (y + (long long)a.ny * z);
-    a.R[node] = rr;
-    a.B[node] = bb;
+    const int node = x + a.nx * (y + a.ny * z);
+    const float rho = rr + bb;
+    a.phi[node] = (rr - bb) / rho;
+    a.dn[node] = rho;
 }
 
 // Per-direction constants of the 3D colour-gradient model (GpuInit.cu:
@@ -105,16 +127,17 @@ __device__ __forceinline__ float cg3_ho_weight(int s2) {
 // enhanced equilibrium's nu (chi_k u.grad rho + psi_k G:c_k c_k).  Below the
 // gradient limit the perturbation and the recolouring vanish.
 template <bool PULL, bool HO, bool ENH>
-__global__ void __launch_bounds__(CG3_BLOCK) cg3_collide_kernel(const Cg3Args a) {
+__global__ void __launch_bounds__(CG3_BLOCK, CG3_MINB) cg3_collide_kernel(const Cg3Args a) {
     using L = Lat<19>;
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
     if (x >= a.nx) return;
-    const long long plane = (long long)a.nx * a.ny;
-    const long long node = x + a.nx * (long long)y + plane * z;
+    const int plane = a.nx * a.ny;
+    const int node = x + a.nx * y + plane * z;
+    const Cg3Nb nb(a, x, y, z);
     float f[19], r_r = 0.f, b_r = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
     {
         float r[19], b[19];
-        cg3_gather<PULL>(a, x, y, z, r, b);
+        cg3_gather<PULL>(a, nb, r, b);
 #pragma unroll
         for (int d = 0; d < 19; ++d) {
             f[d] = r[d] + b[d];
@@ -127,6 +150,8 @@ __global__ void __launch_bounds__(CG3_BLOCK) cg3_collide_kernel(const Cg3Args a)
     }
     const float rho = r_r + b_r;
     const float u = jx / rho, v = jy / rho, w = jz / rho;
+    a.R[node] = r_r;
+    a.B[node] = b_r;
     if (a.write_macro) {
         a.rho[node] = rho;
         a.ux[node] = u;
@@ -134,11 +159,10 @@ __global__ void __launch_bounds__(CG3_BLOCK) cg3_collide_kernel(const Cg3Args a)
         a.uz[node] = w;
     }
     float cgx = 0.f, cgy = 0.f, cgz = 0.f, grx = 0.f, gry = 0.f, grz = 0.f;
-    auto add = [&](long long j, float wt, int ox, int oy, int oz) {
-        const float Rj = __ldg(a.R + j), Bj = __ldg(a.B + j), rj = Rj + Bj;
-        const float a1 = wt * (Rj - Bj) / rj;
+    auto add = [&](int j, float wt, int ox, int oy, int oz) {
+        const float a1 = wt * __ldg(a.phi + j);
         if (ENH) {
-            const float a2 = wt * rj;
+            const float a2 = wt * __ldg(a.dn + j);
             grx += a2 * (float)ox;
             gry += a2 * (float)oy;
             grz += a2 * (float)oz;
@@ -148,11 +172,11 @@ __global__ void __launch_bounds__(CG3_BLOCK) cg3_collide_kernel(const Cg3Args a)
         cgz += a1 * (float)oz;
     };
     if (HO) {
-        long long xo[5], yo[5], zo[5];
+        int xo[5], yo[5], zo[5];
 #pragma unroll
         for (int t = 0; t < 5; ++t) {
             xo[t] = cg3_wrap(x + t - 2, a.nx);
-            yo[t] = (long long)a.nx * cg3_wrap(y + t - 2, a.ny);
+            yo[t] = a.nx * cg3_wrap(y + t - 2, a.ny);
             zo[t] = plane * cg3_wrap(z + t - 2, a.nz);
         }
 #pragma unroll
@@ -167,11 +191,8 @@ __global__ void __launch_bounds__(CG3_BLOCK) cg3_collide_kernel(const Cg3Args a)
                 }
     } else {
 #pragma unroll
-        for (int k = 1; k < 19; ++k) {
-            const long long j = cg3_wrap(x + L::cx(k), a.nx) + (long long)a.nx * cg3_wrap(y + L::cy(k), a.ny) +
-                                plane * cg3_wrap(z + L::cz(k), a.nz);
-            add(j, k <= 6 ? 1.f / 6.f : 1.f / 12.f, L::cx(k), L::cy(k), L::cz(k));
-        }
+        for (int k = 1; k < 19; ++k)
+            add(nb.at(L::cx(k), L::cy(k), L::cz(k)), k <= 6 ? 1.f / 6.f : 1.f / 12.f, L::cx(k), L::cy(k), L::cz(k));
     }
     const float mean_nu = 1.f / (r_r / (rho * a.r_visc) + b_r / (rho * a.b_visc));
     const float omega_eff = 1.f / (3.f * mean_nu + 0.5f);
@@ -183,6 +204,8 @@ __global__ void __launch_bounds__(CG3_BLOCK) cg3_collide_kernel(const Cg3Args a)
     const float G5 = 2.f * v * gry, G6 = v * grz + w * gry, G9 = 2.f * w * grz;
     const float ugr = u * grx + v * gry + w * grz;
     const bool interface = gnorm > a.g_limit;
+    // one reciprocal per node instead of two divisions per direction
+    const float inv_g = interface ? 1.f / gnorm : 0.f, inv_g2 = inv_g * inv_g;
     float *rout = a.out + node, *bout = a.out + 19 * a.N + node;
 #pragma unroll
     for (int k = 0; k < 19; ++k) {
@@ -191,8 +214,8 @@ __global__ void __launch_bounds__(CG3_BLOCK) cg3_collide_kernel(const Cg3Args a)
         float pert = 0.f, cosin = 0.f;
         if (interface) {
             const float pcg = cx * cgx + cy * cgy + cz * cgz;
-            if (k != 0) cosin = pcg / (gnorm * (k <= 6 ? 1.f : 1.41421356f));
-            pert = a.A * gnorm * (wk * (pcg * pcg) / (gnorm * gnorm) - cg3_bpert(k));
+            if (k != 0) cosin = pcg * inv_g * (k <= 6 ? 1.f : 0.70710678f);
+            pert = a.A * gnorm * (wk * (pcg * pcg) * inv_g2 - cg3_bpert(k));
         }
         const float cu2 = u * cx + v * cy + w * cz;
         const float rest = cg3_phi(k) + cg3_teta(k) * mean_alpha;
