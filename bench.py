@@ -700,9 +700,7 @@ def main():
         s2 = Solver(lat, sargs)
         s2.init(*host)
         s2.step(args.e2e_steps, write_macro=True)
-        rho, u, v, w = s2.macro()
-        for dst, src in zip(outs, (rho, u, v, w)):
-            dst[:] = src
+        s2.macro(out=outs)
         t1 = time.perf_counter()
         s2.close()
         tt = torch.tensor([t1 - t0], dtype=torch.float64, device=dev)

@@ -184,7 +184,7 @@ static void free_handle(lbm_handle_s *H) {
 // an open link) and the arrays whose own row it must copy (opp(d) for every
 // d that some fluid node of the row cannot pull).
 template <int Q>
-static void tma_row_tables(const std::vector<uint32_t> &word, int nx, long long nrows_all,
+static void tma_row_tables(const HostArray<uint32_t> &word, int nx, long long nrows_all,
                            std::vector<int32_t> &rows, std::vector<uint32_t> &lm, std::vector<uint32_t> &om) {
     using L = Lat<Q>;
     const uint32_t dirs = (1u << Q) - 1u;
@@ -213,7 +213,7 @@ static void tma_row_tables(const std::vector<uint32_t> &word, int nx, long long 
 // physics mode, F32/F16S storage, rows a multiple of 16 bytes and at least
 // two stages in shared memory.  Returns LBM_OK with H->tma_kernel false when
 // it cannot.
-static int setup_tma(lbm_handle_s *H, const std::vector<uint32_t> &word) {
+static int setup_tma(lbm_handle_s *H, const HostArray<uint32_t> &word) {
     H->tma_kernel = false;
     if (H->P.mode != LBM_MODE_PHYSICS) return LBM_OK;
     if (H->P.storage != LBM_STORE_F32 && H->P.storage != LBM_STORE_F16S) return LBM_OK;
@@ -261,7 +261,7 @@ static int setup_tma(lbm_handle_s *H, const std::vector<uint32_t> &word) {
 // True when some fluid node pulls across an out-of-domain link that is not
 // blocked: the step must then wrap coordinates at the faces.
 template <int Q>
-static bool open_outside_links(const std::vector<uint32_t> &word, int n, int m, int h) {
+static bool open_outside_links(const HostArray<uint32_t> &word, int n, int m, int h) {
     using L = Lat<Q>;
     for (int z = 0; z < h; ++z)
         for (int y = 0; y < m; ++y) {
@@ -299,7 +299,7 @@ static std::string tune_key(const JitStepKey &k) {
 }
 
 // Build the run-time specialised step kernel for this lattice.
-static int setup_jit(lbm_handle_s *H, const std::vector<uint32_t> &word, bool pair, int hspace) {
+static int setup_jit(lbm_handle_s *H, const HostArray<uint32_t> &word, bool pair, int hspace) {
     const bool periodic = H->P.mode == LBM_MODE_PHYSICS &&
                           (H->P.periodic[0] || H->P.periodic[1] || (H->dims == 3 && H->P.periodic[2]));
     const bool wrap = periodic || (H->q == 9 ? open_outside_links<9>(word, H->n, H->m, H->h)
@@ -965,8 +965,11 @@ int lbm_build_flags(const lbm_lattice_desc *L, const lbm_params *P, uint64_t *ma
     if (rc) return fail(rc, err);
     rc = build_device_flags(*L, *P, refm, flags, err);
     if (rc) return fail(rc, err);
-    const size_t N = refm.mask.size();
-    if (mask) memcpy(mask, refm.mask.data(), sizeof(uint64_t) * N);
+    const size_t N = (size_t)L->n * L->m * (L->dims == 2 ? 1 : L->h);
+    if (mask) {
+        memset(mask, 0, sizeof(uint64_t) * N);
+        for (size_t b = 0; b < refm.bc_nodes.size(); ++b) mask[refm.bc_nodes[b]] = refm.mask[b];
+    }
     if (word) memcpy(word, flags.word.data(), sizeof(uint32_t) * N);
     if (slot) memcpy(slot, flags.slot.data(), sizeof(int32_t) * N);
     if (num_bc_nodes) *num_bc_nodes = (int)refm.bc_nodes.size();

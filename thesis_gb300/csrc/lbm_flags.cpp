@@ -15,6 +15,8 @@
 
 #include <string.h>
 
+#include <algorithm>
+
 #include <thread>
 
 namespace lbm {
@@ -34,94 +36,113 @@ int lattice_cy(int q, int d) { return q == 9 ? CY2[d] : CY3[d]; }
 int lattice_cz(int q, int d) { return q == 9 ? 0 : CZ3[d]; }
 int lattice_opp(int q, int d) { return q == 9 ? OPP2[d] : OPP3[d]; }
 
-uint64_t ref_type(const RefMasks &r, int node, int dir) {
-    const int b = r.q == 9 ? 2 : 3;
-    return (r.mask[node] >> ((dir - 1) * b)) & (r.q == 9 ? 3ull : 7ull);
+uint64_t ref_type(const RefMasks &r, size_t b, int dir) {
+    const int bits = r.q == 9 ? 2 : 3;
+    return (r.mask[b] >> ((dir - 1) * bits)) & (r.q == 9 ? 3ull : 7ull);
 }
 
-uint64_t ref_main_type(const RefMasks &r, int node) {
-    return r.q == 9 ? (r.mask[node] >> 16) & 3ull : (r.mask[node] >> 54) & 7ull;
+uint64_t ref_main_type(const RefMasks &r, size_t b) {
+    return r.q == 9 ? (r.mask[b] >> 16) & 3ull : (r.mask[b] >> 54) & 7ull;
 }
 
-bool ref_corner(const RefMasks &r, int node) {
-    return r.q == 9 ? (r.mask[node] >> 18) & 1ull : (r.mask[node] >> 57) & 1ull;
+bool ref_corner(const RefMasks &r, size_t b) {
+    return r.q == 9 ? (r.mask[b] >> 18) & 1ull : (r.mask[b] >> 57) & 1ull;
+}
+
+long long find_bc(const RefMasks &r, long long node) {
+    auto it = std::lower_bound(r.bc_nodes.begin(), r.bc_nodes.end(), node);
+    return it != r.bc_nodes.end() && *it == node ? (long long)(it - r.bc_nodes.begin()) : -1;
 }
 
 int build_ref_masks(const lbm_lattice_desc &L, RefMasks &r, std::string &err) {
     const int q = L.dims == 2 ? 9 : 19;
-    const long long N = (long long)L.n * L.m * (L.dims == 2 ? 1 : L.h);
-    r.q = q;
-    r.mask.assign((size_t)N, 0ull);
-    r.blocked.assign((size_t)N, 0u);
-    r.linked.assign((size_t)N, 0u);
-    std::vector<uint8_t> seen((size_t)N, 0);
     const int h = L.dims == 2 ? 1 : L.h;
-    for (int c = 0; c < L.num_conns; ++c) {
+    const int nc = L.num_conns > 0 ? L.num_conns : 0;
+    r.q = q;
+    r.bc_nodes.clear();
+    r.mask.clear();
+    r.blocked.clear();
+    r.linked.clear();
+    // node of every link; the links of one node are combined below, so they
+    // are visited node by node (BC files list them node-major already)
+    std::vector<long long> li((size_t)nc);
+    bool sorted = true;
+    for (int c = 0; c < nc; ++c) {
         const int i = L.bc_i[c], j = L.bc_j[c], k = L.bc_k ? L.bc_k[c] : 0;
         const int dir = L.bc_dir[c];
         if (i < 0 || i >= L.n || j < 0 || j >= L.m || k < 0 || k >= h || dir < 1 || dir >= q) {
             err = "BC link " + std::to_string(c) + " out of range";
             return LBM_ERR_INVALID;
         }
-        const long long ind = i + (long long)L.n * (j + (long long)L.m * k);
-        const uint64_t type = (uint64_t)L.bc_type[c];
-        uint64_t &mk = r.mask[(size_t)ind];
-        const uint64_t fluid = (uint64_t)(L.node_type[ind] & 1);
-        if (q == 9) {
-            mk |= type << ((dir - 1) * 2);
-            mk |= fluid << 19;
-            const uint64_t all = 3ull << 16;
-            if (!(mk & all)) {
-                mk |= type << 16;
-            } else if ((mk & all) != (type << 16)) {
-                mk &= ~all;
-                mk |= 1ull << 16;
-                mk |= 1ull << 18;
-            }
-            const uint32_t id = L.bc_id ? (uint32_t)L.bc_id[c] : 0u;
-            mk = (uint64_t)((uint32_t)mk | (id << 24));
-        } else {
-            mk |= type << ((dir - 1) * 3);
-            mk |= fluid << 58;
-            const uint64_t all = 7ull << 54;
-            if (!(mk & all)) {
-                mk |= type << 54;
-            } else if ((mk & all) != (type << 54)) {
-                mk &= ~all;
-                mk |= 1ull << 54;
-                mk |= 1ull << 57;
-            }
-        }
-        r.blocked[(size_t)ind] |= 1u << lattice_opp(q, dir);
-        r.linked[(size_t)ind] |= 1u << dir;
-        seen[(size_t)ind] = 1;
+        li[(size_t)c] = i + (long long)L.n * (j + (long long)L.m * k);
+        if (c && li[(size_t)c] < li[(size_t)c - 1]) sorted = false;
     }
-    for (long long ind = 0; ind < N; ++ind) {
-        if (!seen[(size_t)ind]) continue;
-        uint64_t &mk = r.mask[(size_t)ind];
+    std::vector<int> order((size_t)nc);
+    for (int c = 0; c < nc; ++c) order[(size_t)c] = c;
+    if (!sorted)
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return li[(size_t)a] < li[(size_t)b]; });
+    for (size_t t = 0; t < (size_t)nc;) {
+        const long long ind = li[(size_t)order[t]];
+        const uint64_t fluid = (uint64_t)(L.node_type[ind] & 1);
+        uint64_t mk = 0;
+        uint32_t blocked = 0, linked = 0;
+        for (; t < (size_t)nc && li[(size_t)order[t]] == ind; ++t) {
+            const int c = order[t];
+            const int dir = L.bc_dir[c];
+            const uint64_t type = (uint64_t)L.bc_type[c];
+            if (q == 9) {
+                mk |= type << ((dir - 1) * 2);
+                mk |= fluid << 19;
+                const uint64_t all = 3ull << 16;
+                if (!(mk & all)) {
+                    mk |= type << 16;
+                } else if ((mk & all) != (type << 16)) {
+                    mk &= ~all;
+                    mk |= 1ull << 16;
+                    mk |= 1ull << 18;
+                }
+                const uint32_t id = L.bc_id ? (uint32_t)L.bc_id[c] : 0u;
+                mk = (uint64_t)((uint32_t)mk | (id << 24));
+            } else {
+                mk |= type << ((dir - 1) * 3);
+                mk |= fluid << 58;
+                const uint64_t all = 7ull << 54;
+                if (!(mk & all)) {
+                    mk |= type << 54;
+                } else if ((mk & all) != (type << 54)) {
+                    mk &= ~all;
+                    mk |= 1ull << 54;
+                    mk |= 1ull << 57;
+                }
+            }
+            blocked |= 1u << lattice_opp(q, dir);
+            linked |= 1u << dir;
+        }
+        // corner pass
         if (q == 9) {
-            if (!((mk >> 18) & 1ull)) continue;
-            auto any = [&](int d) { return ((mk >> ((d - 1) * 2)) & 3ull) != 0; };
-            auto wall = [&](int d) {
-                mk &= ~(3ull << ((d - 1) * 2));
-                mk |= 1ull << ((d - 1) * 2);
-            };
-            if (any(1) && any(2)) wall(5);
-            if (any(3) && any(2)) wall(6);
-            if (any(3) && any(4)) wall(7);
-            if (any(1) && any(4)) wall(8);
-        } else {
-            if (!((mk >> 57) & 1ull)) continue;
+            if ((mk >> 18) & 1ull) {
+                auto any = [&](int d) { return ((mk >> ((d - 1) * 2)) & 3ull) != 0; };
+                auto wall = [&](int d) {
+                    mk &= ~(3ull << ((d - 1) * 2));
+                    mk |= 1ull << ((d - 1) * 2);
+                };
+                if (any(1) && any(2)) wall(5);
+                if (any(3) && any(2)) wall(6);
+                if (any(3) && any(4)) wall(7);
+                if (any(1) && any(4)) wall(8);
+            }
+        } else if ((mk >> 57) & 1ull) {
             for (int d = 1; d < 19; ++d)
                 if ((mk >> ((d - 1) * 3)) & 7ull) {
                     mk &= ~(7ull << ((d - 1) * 3));
                     mk |= 1ull << ((d - 1) * 3);
                 }
         }
+        r.bc_nodes.push_back(ind);
+        r.mask.push_back(mk);
+        r.blocked.push_back(blocked);
+        r.linked.push_back(linked);
     }
-    r.bc_nodes.clear();
-    for (long long ind = 0; ind < N; ++ind)
-        if (seen[(size_t)ind]) r.bc_nodes.push_back(ind);
     return LBM_OK;
 }
 
@@ -153,8 +174,8 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
     const int n = L.n, m = L.m, h = L.dims == 2 ? 1 : L.h;
     const long long N = (long long)n * m * h;
     const bool phys = P.mode == LBM_MODE_PHYSICS;
-    out.word.assign((size_t)N, 0u);
-    out.slot.assign((size_t)N, -1);
+    out.word.resize((size_t)N);  // every entry written below
+    out.slot.resize((size_t)N);
     out.mask.clear();
     out.kind.clear();
     out.slot_node.clear();
@@ -183,33 +204,62 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
     // which interpolates between the node's own and upstream populations
     const bool curved = curved_walls(P, q);
 
-    // fluid bit and blocked pulls, in parallel over node ranges
+    // fluid bit and blocked pulls, in parallel over node ranges; a range
+    // walks the boundary-node list alongside
+    const size_t nb = r.bc_nodes.size();
+    int off[19];
+    for (int d = 0; d < q; ++d)
+        off[d] = lattice_cx(q, d) + n * lattice_cy(q, d) + n * m * lattice_cz(q, d);
     auto word_range = [&](long long lo, long long hi) {
+        size_t b = (size_t)(std::lower_bound(r.bc_nodes.begin(), r.bc_nodes.end(), lo) - r.bc_nodes.begin());
+        int x = (int)(lo % n), y = (int)((lo / n) % m), z = (int)(lo / ((long long)n * m));
         for (long long ind = lo; ind < hi; ++ind) {
-            if (!(L.node_type[ind] & 1)) continue;
-            uint32_t w = W_FLUID | r.blocked[(size_t)ind];
+            const bool isbc = b < nb && r.bc_nodes[b] == ind;
+            const size_t bi = b;
+            if (isbc) ++b;
+            const int cx = x, cy = y, cz = z;
+            if (++x == n) {
+                x = 0;
+                if (++y == m) {
+                    y = 0;
+                    ++z;
+                }
+            }
+            out.slot[(size_t)ind] = -1;
+            if (!(L.node_type[ind] & 1)) {
+                out.word[(size_t)ind] = 0u;
+                continue;
+            }
+            uint32_t w = W_FLUID | (isbc ? r.blocked[bi] : 0u);
             if (phys) {
-                const int x = (int)(ind % n), y = (int)((ind / n) % m), z = (int)(ind / ((long long)n * m));
-                uint32_t b = 0;
+                uint32_t bl = 0;
+                const bool interior = cx > 0 && cx < n - 1 && cy > 0 && cy < m - 1 && (h == 1 || (cz > 0 && cz < h - 1));
+                if (interior && !isbc) {
+                    // no link leaves the lattice: only solid neighbours block
+                    for (int d = 1; d < q; ++d)
+                        if (!(L.node_type[ind - off[d]] & 1)) bl |= 1u << d;
+                    out.word[(size_t)ind] = W_FLUID | bl;
+                    continue;
+                }
                 for (int d = 1; d < q; ++d) {
                     const int opp = lattice_opp(q, d);
                     // a periodic-type link on the opposite direction streams by wrapping
-                    const bool periodic_link = ((r.linked[(size_t)ind] >> opp) & 1u) &&
-                                               ref_type(r, (int)ind, opp) == LBM_BC_PERIODIC;
-                    if (((w >> d) & 1u) && !periodic_link) b |= 1u << d;
-                    int sx = x - lattice_cx(q, d), sy = y - lattice_cy(q, d), sz = z - lattice_cz(q, d);
+                    const bool periodic_link =
+                        isbc && ((r.linked[bi] >> opp) & 1u) && ref_type(r, bi, opp) == LBM_BC_PERIODIC;
+                    if (((w >> d) & 1u) && !periodic_link) bl |= 1u << d;
+                    int sx = cx - lattice_cx(q, d), sy = cy - lattice_cy(q, d), sz = cz - lattice_cz(q, d);
                     bool outside = false;
                     if (sx < 0 || sx >= n) { if (P.periodic[0] || periodic_link) sx = (sx + n) % n; else outside = true; }
                     if (sy < 0 || sy >= m) { if (P.periodic[1] || periodic_link) sy = (sy + m) % m; else outside = true; }
                     if (sz < 0 || sz >= h) { if (P.periodic[2] || periodic_link) sz = (sz + h) % h; else outside = true; }
                     if (outside) {
-                        b |= 1u << d;
+                        bl |= 1u << d;
                         continue;
                     }
-                    const long long s = sx + (long long)n * (sy + (long long)m * sz);
-                    if (!(L.node_type[s] & 1)) b |= 1u << d;
+                    const long long src = sx + (long long)n * (sy + (long long)m * sz);
+                    if (!(L.node_type[src] & 1)) bl |= 1u << d;
                 }
-                w = W_FLUID | b;
+                w = W_FLUID | bl;
             }
             out.word[(size_t)ind] = w;
         }
@@ -228,9 +278,9 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
     }
 
     // special nodes
-    for (long long ind : r.bc_nodes) {
+    for (size_t node = 0; node < nb; ++node) {
+        const long long ind = r.bc_nodes[node];
         if (!(L.node_type[ind] & 1)) continue;
-        const int node = (int)ind;
         bool special = false;
         int kind = 0;
         if (!phys) {
@@ -238,7 +288,7 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
             for (int d = 1; d < q && simple; ++d) {
                 const uint64_t t = ref_type(r, node, d);
                 const bool wall = t == LBM_BC_WALL;
-                const bool blocked_opp = (r.blocked[(size_t)ind] >> lattice_opp(q, d)) & 1u;
+                const bool blocked_opp = (r.blocked[node] >> lattice_opp(q, d)) & 1u;
                 if (t > LBM_BC_WALL || wall != blocked_opp) simple = false;
             }
             special = !simple;
@@ -265,7 +315,7 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
             if (mt != LBM_BC_INLET && mt != LBM_BC_OUTLET) continue;
             int face = -1;
             for (int d = 1; d < q && face < 0; ++d)
-                if (((r.linked[(size_t)ind] >> d) & 1u) && ref_type(r, node, d) == mt)
+                if (((r.linked[node] >> d) & 1u) && ref_type(r, node, d) == mt)
                     face = face_of_link(q, d);
             if (face < 0) continue;
             // a velocity inlet whose velocity has no component along the
@@ -277,7 +327,7 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
                 if (nrm == 0.0) {
                     uint64_t moving = 0;
                     for (int d = 1; d < q; ++d)
-                        if (((r.linked[(size_t)ind] >> d) & 1u) && ref_type(r, node, d) == LBM_BC_INLET)
+                        if (((r.linked[node] >> d) & 1u) && ref_type(r, node, d) == LBM_BC_INLET)
                             moving |= 1ull << lattice_opp(q, d);
                     out.slot[(size_t)ind] = (int32_t)out.slot_node.size();
                     out.slot_node.push_back(ind);
@@ -304,7 +354,7 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
         if (!special) continue;
         out.slot[(size_t)ind] = (int32_t)out.slot_node.size();
         out.slot_node.push_back(ind);
-        out.mask.push_back(r.mask[(size_t)ind]);
+        out.mask.push_back(r.mask[node]);
         out.kind.push_back(kind);
         out.word[(size_t)ind] |= W_SPECIAL;
     }

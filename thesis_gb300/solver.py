@@ -177,9 +177,15 @@ class Solver:
         N.check(self._lib.lbm_step(self._h, int(nsteps), int(bool(write_macro)),
                                    None if stream is None else C.c_void_p(stream)))
 
-    def macro(self):
+    def macro(self, out=None):
+        """rho, u, v, w of the last step that stored them; `out` may hold four
+        contiguous float32 arrays of num_nodes (pinned ones are filled by
+        direct copies) that receive them."""
         nn = self.lat.num_nodes
-        out = [np.empty(nn, np.float32) for _ in range(4)]
+        if out is None:
+            out = [np.empty(nn, np.float32) for _ in range(4)]
+        elif len(out) != 4 or any(a.dtype != np.float32 or a.size != nn or not a.flags.c_contiguous for a in out):
+            raise ValueError("out must be four contiguous float32 arrays of %d values" % nn)
         N.check(self._lib.lbm_get_macro(self._h, *[_fptr(a) for a in out]))
         return out
 
