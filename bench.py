@@ -395,6 +395,18 @@ def run_cg(args):
     cpu = None
     if not args.no_cpu_baseline:
         from oracle import pyoracle
+        # the reference's own serial CPU loop where its sources were built
+        # (oracle/_ref), else the oracle port below
+        probe = pyoracle.run_reference_cpu_cg(128, 128, 5)
+        if probe is not None:
+            steps = int(min(max(args.cpu_seconds / max(probe[2] / 5, 1e-6), 5), 100000))
+            _, _, dt = pyoracle.run_reference_cpu_cg(128, 128, steps)
+            cpu = {"value": 128 * 128 * steps / dt / 1e9, "unit": "GLUPS", "cores": 1, "kind": "reference",
+                   "sample": "the reference's serial CPU colour-gradient loop (Multiphase.cu mp2DColl, streamMP, "
+                             "peridicBoundaries, updateMacroMP) on its 128x128 test-case-1 bubble, %d steps, "
+                             "%.1f s" % (steps, dt)}
+    if not args.no_cpu_baseline and cpu is None:
+        from oracle import pyoracle
         L = pyoracle.oracle_lib()
         nc = 192
         ac = mp.CgArguments(bubble_radius=0.25, A=0.005, beta=0.7)

@@ -43,6 +43,7 @@ tmp="$(mktemp -d)"
     Vector2D.cpp Vector3D.cpp -o "$OUT/latticegen" -lm )
 # reference serial colour-gradient CPU functions (Multiphase.cu), host-only
 "$CXX" -x c++ -std=c++17 -O2 -fPIC -shared -w -D__global__= -D__device__= -D__host__= \
-  -I"$S/include" -I"$CUDA_INC" "$S/Multiphase.cu" "$S/CellFunctions.cu" -o "$OUT/libref_multiphase.so" -lm 2>"$tmp/mp.log" \
+  -I"$S/include" -I"$CUDA_INC" "$S/Multiphase.cu" "$S/CellFunctions.cu" -x none "$HERE/ref_shim/ref_cpu_cg.cpp" \
+  -o "$OUT/libref_multiphase.so" -lm 2>"$tmp/mp.log" \
   || echo "build_ref: Multiphase.cu host build failed (see $tmp/mp.log)" >&2
 echo "build_ref: built $(ls "$OUT" | tr '\n' ' ')"

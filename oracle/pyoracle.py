@@ -333,3 +333,29 @@ def cg3_collide_pair(n, m, h, p, rho, r_rho, b_rho, u, v, w, f, fp64=False):
         L.ref_cg3d_collide(n, m, h, C.byref(p), *[_vp(a) for a in arrs], _vp(rr), _vp(bb), _vp(cd))
         ref = (rr.reshape(19, nn), bb.reshape(19, nn), cd)
     return (orc[0].reshape(19, nn), orc[1].reshape(19, nn)), ref
+
+
+class RefCpuCgParams(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("r_density", "b_density", "r_alpha", "b_alpha", "r_viscosity",
+                                          "b_viscosity", "beta", "A", "g_limit", "control_param", "bubble_radius")]
+
+
+def run_reference_cpu_cg(n, m, steps, **kw):
+    """The reference's serial CPU colour-gradient loop (Multiphase.cu through
+    oracle/ref_shim/ref_cpu_cg.cpp) from its test-case-1 bubble; returns
+    (r_rho, b_rho, seconds), or None where oracle/_ref is absent."""
+    import time
+    path = os.path.join(REF_DIR, "libref_multiphase.so")
+    if not os.path.exists(path):
+        return None
+    L = C.CDLL(path)
+    base = dict(r_density=1.0, b_density=1.0, r_alpha=4 / 9, b_alpha=4 / 9, r_viscosity=1 / 6, b_viscosity=1 / 6,
+                beta=0.7, A=0.005, g_limit=0.0, control_param=0.9, bubble_radius=0.25)
+    base.update(kw)
+    p = _params(RefCpuCgParams, base)
+    rr, bb = np.zeros(n * m), np.zeros(n * m)
+    t0 = time.perf_counter()
+    rc = L.ref_cpu_cg2d(n, m, C.byref(p), int(steps), _vp(rr), _vp(bb))
+    dt = time.perf_counter() - t0
+    assert rc == 0
+    return rr, bb, dt

@@ -213,3 +213,19 @@ def test_cg_gpu_laplace_law():
         assert abs(dp - pred) < 0.15 * pred
         dps.append(dp)
     assert dps[0] > dps[1] > 0
+
+
+def test_reference_cpu_colour_gradient_loop():
+    """The reference's serial CPU colour-gradient loop (Multiphase.cu, built
+    from its sources into oracle/_ref where the reference tree is present)
+    runs from its test-case-1 bubble and keeps each colour's mass to FP32
+    accumulation rounding; it is the colour-gradient workload's CPU
+    baseline there (its arithmetic differs from the GPU kernels, so it is not
+    a parity target)."""
+    r0 = po.run_reference_cpu_cg(64, 64, 0)
+    if r0 is None:
+        pytest.skip("oracle/_ref not built")
+    r = po.run_reference_cpu_cg(64, 64, 200)
+    assert abs(r[0].sum() - r0[0].sum()) < 1e-5 * r0[0].sum()
+    assert abs(r[1].sum() - r0[1].sum()) < 1e-5 * r0[1].sum()
+    assert r0[0].sum() > 0 and r0[1].sum() > 0
