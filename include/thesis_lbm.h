@@ -234,6 +234,19 @@ int lbm_residual_fd_rel_diff(lbm_handle h, double *out);
  * boundary id instead; this is the standard link-based force. */
 int lbm_momentum_exchange(lbm_handle h, const int *box, double *force);
 
+/* The reference's 2D drag and lift sums (gpuUpdateMacro2D,
+ * GpuUpdateMacro.cu:33-38, summed by computeDragLift2D, ComputeResiduals.cu:
+ * 39-45, into the Drag and Lift columns of its residual file): over the fluid
+ * nodes whose BC mask carries boundary id boundary_id, out[0] =
+ * sum 0.33333333 rho (20 - x) 0.2 and out[1] = sum 0.33333333 rho (20 - y) 0.2,
+ * rho the last stored density and x, y the Node file's coordinates
+ * (node_x/y hold n*m values by node).  A hard-wired expression of the
+ * reference, not a force; lbm_momentum_exchange is the physical one.  Zero
+ * for boundary_id <= 0 and in 3D, where the reference's loop has no such
+ * term.  Per-node terms rounded to FP32 as the reference stores them, FP64
+ * sum. */
+int lbm_reference_drag_lift(lbm_handle h, int boundary_id, const float *node_x, const float *node_y, double *out);
+
 /* The reference's MaxMacroDiff residual (Iterate3D.cu:696-735): out[0..3] =
  * max over all nodes of |u - u_prev|, |v - v_prev|, |w - w_prev|,
  * |rho - rho_prev| for the last stored macroscopic fields, where _prev is the

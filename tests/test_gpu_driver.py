@@ -34,7 +34,7 @@ InitialFile = "{icfile}"
 ResidualModel = {resmodel}
 ResidualsAndMacroDiffsAfter = 100
 Force = 0
-DragAndLift = 0
+DragAndLift = {dl}
 UpdateInltOutl = yes
 """
 
@@ -42,7 +42,8 @@ UpdateInltOutl = yes
 def _setup(tmp_path, lat, **kw):
     (tmp_path / "Mesh").mkdir(exist_ok=True)
     lattice.write_files(lat, str(tmp_path / "Mesh" / "cav_Node.dat"), str(tmp_path / "Mesh" / "cav_BC.dat"))
-    d = dict(coll="SRT", iters=400, stop="0 0 0 0", fmt="CSV", ic="no", icfile="none", resmodel="MaxMacroDiff")
+    d = dict(coll="SRT", iters=400, stop="0 0 0 0", fmt="CSV", ic="no", icfile="none", resmodel="MaxMacroDiff",
+             dl=0)
     d.update(kw)
     (tmp_path / "SetUpData.ini").write_text(INIT.format(**d))
 
@@ -113,10 +114,12 @@ def test_driver_fd_rel_diff_residual_model(tmp_path):
     _setup(tmp_path, lat, iters=200000, stop="1e-5 0 0 0", coll="MRT", resmodel="MaxRelativeFdDiff")
     r = _run(tmp_path, "--physics")
     assert r.returncode == 0 and "converged" in r.stdout, r.stderr
-    lines = (tmp_path / "Results" / "Residuals.txt").read_text().splitlines()
-    assert lines[0] == "iteration\tMaxRelativeFdDiff"
-    res = np.array([float(x.split()[1]) for x in lines[1:]])
-    assert res[-1] < 1e-5 and res[0] > res[-1] and len(res) < 2000
+    rows = _residual_rows(tmp_path, 200000)
+    # the file is the reference's: one row per iteration, in 2D the L2 norm
+    # at the checks (every 100 steps until the FdRelDiff stop test held)
+    chk = rows[rows[:, 1] != 0]
+    assert 2 <= len(chk) < 2000 and chk[-1, 1] < chk[0, 1]
+    assert np.all(chk[:, 0] % 100 == 99)
 
 
 def test_driver_l2_residual_model(tmp_path):
@@ -127,20 +130,59 @@ def test_driver_l2_residual_model(tmp_path):
     _setup(tmp_path, lat, iters=1000, stop="0 0 0 0", coll="MRT", resmodel="L2")
     r = _run(tmp_path, "--physics")
     assert r.returncode == 0, r.stderr
-    lines = (tmp_path / "Results" / "Residuals.txt").read_text().splitlines()
-    assert lines[0] == "iteration\tL2" and len(lines) == 11
+    rows = _residual_rows(tmp_path, 1000)
+    chk = rows[rows[:, 1] != 0]
+    assert len(chk) == 10 and np.array_equal(chk[:, 0], np.arange(99, 1000, 100))
+    np.testing.assert_allclose(chk[:, 2], chk[:, 1] / lat.num_nodes, rtol=2e-4)
     f32 = lambda v: float(np.float32(v))
     args = Arguments(u=f32(0.1), viscosity=f32(0.128), collision_model=N.MRT, mode=N.MODE_PHYSICS, init_equilibrium=1)
     with Solver(lat, args) as s:
         s.init()
         s.step(1000, write_macro=True)
         want, rc = s.residual_l2()
-    assert abs(float(lines[-1].split()[1]) - want) <= 1e-9 * want
+    assert abs(rows[999, 1] - want) <= 1e-4 * want  # %5.4e in the file
+
+
+def _residual_rows(tmp_path, iterations):
+    lines = (tmp_path / "Results" / "Residuals.txt").read_text().splitlines()
+    assert lines[0] == "Iter L2_norm L2_norm_weighted Drag Lift"
+    rows = np.array([[float(v) for v in ln.split()] for ln in lines[1:]])
+    assert rows.shape == (iterations, 5) and np.array_equal(rows[:, 0], np.arange(iterations))
+    return rows
+
+
+def test_driver_reference_drag_lift_columns(tmp_path):
+    """BoundaryId (init file line 22): the Drag and Lift columns hold the
+    reference's sums 0.33333333 rho (20 - x) 0.2 and (20 - y) over the fluid
+    nodes of that boundary id at every check (gpuUpdateMacro2D, computeDragLift2D),
+    equal at the last check to the sums over the final density."""
+    lat = lattice.cylinder_channel2d(48, 24)
+    bc = lat.bc.copy()
+    # the cylinder's links (their target node lies inside the lattice) get id 1
+    tx = bc[:, 0] + lattice.CX2[bc[:, 3]]
+    ty = bc[:, 1] + lattice.CY2[bc[:, 3]]
+    obstacle = (tx >= 0) & (tx < lat.n) & (ty >= 0) & (ty < lat.m)
+    bc[obstacle, 5] = 1
+    lat = lattice.Lattice(2, lat.n, lat.m, 1, lat.node_type, bc)
+    _setup(tmp_path, lat, iters=300, dl=1)
+    r = _run(tmp_path)
+    assert r.returncode == 0, r.stderr
+    rows = _residual_rows(tmp_path, 300)
+    chk = rows[rows[:, 1] != 0]
+    assert len(chk) == 3 and np.all(chk[:, 3] > 0) and np.all(chk[:, 4] > 0)
+    data = np.loadtxt(tmp_path / "Results" / "FinalData.csv", delimiter=",", skiprows=1)
+    x, y, rho = data[:, 0].astype(np.float32), data[:, 1].astype(np.float32), data[:, 7]
+    nodes = np.unique(bc[obstacle, 0] + lat.n * bc[obstacle, 1])
+    nodes = nodes[lat.node_type[nodes] == 1]
+    drag = np.float32(0.33333333 * rho[nodes] * (np.float32(20) - x[nodes]).astype(np.float64) * 0.2).sum()
+    lift = np.float32(0.33333333 * rho[nodes] * (np.float32(20) - y[nodes]).astype(np.float64) * 0.2).sum()
+    np.testing.assert_allclose(rows[299, 3], drag, rtol=1e-6)
+    np.testing.assert_allclose(rows[299, 4], lift, rtol=1e-6)
 
 
 def test_driver_missing_lattice(tmp_path):
     (tmp_path / "SetUpData.ini").write_text(INIT.format(coll="SRT", iters=10, stop="0 0 0 0", fmt="CSV", ic="no",
-                                                        icfile="x", resmodel="MaxMacroDiff"))
+                                                        icfile="x", resmodel="MaxMacroDiff", dl=0))
     assert _run(tmp_path).returncode == 2
 
 

@@ -227,14 +227,19 @@ int main(int argc, char **argv) {
     FILE *md = fopen((out + "MacroDiffs.txt").c_str(), "w");
     if (md) fprintf(md, "iteration\tMax u diff\tMax v diff\tMax w diff\tMax rho diff\n");
 
-    FILE *resf = nullptr;
-    if (cfg.residual_model == LBM_RES_L2 || cfg.residual_model == LBM_RES_FD_REL_DIFF) {
-        resf = fopen((out + "Residuals.txt").c_str(), "w");
-        if (resf) fprintf(resf, "iteration\t%s\n", cfg.residual_model == LBM_RES_L2 ? "L2" : "MaxRelativeFdDiff");
+    // the reference's residual file (writeResiduals, LogWriter.cu:190-205):
+    // one row per iteration, filled at the checks; in 2D the norm column is
+    // the L2 residual with the drag/lift sums of BoundaryId beside it
+    // (Iterate.cu:548-571), in 3D the residual model's value (Iterate3D.cu:
+    // 737-780) and no drag/lift.  The stop test uses the residual model in
+    // both (the reference's 2D single-phase loop has none).
+    const bool res_file = dims == 2 || cfg.residual_model != LBM_RES_MACRO_DIFF;
+    std::vector<double> norm((size_t)(cfg.iterations > 0 ? cfg.iterations : 1), 0.0), drag(norm), lift(norm);
+    if (cfg.residual_model == LBM_RES_FD_REL_DIFF) {
         // FdRelDiff measures against the populations at the start (f_prev and
         // f_first both taken here; the reference takes f_first at its first check)
         double r0;
-        if (cfg.residual_model == LBM_RES_FD_REL_DIFF) lbm_residual_fd_rel_diff(hd, &r0);
+        lbm_residual_fd_rel_diff(hd, &r0);
     }
     const int every = cfg.show_macro_diff > 0 ? cfg.show_macro_diff : cfg.iterations;
     int status = 0, autosave_it = 1;
@@ -266,17 +271,26 @@ int main(int argc, char **argv) {
                 break;
             }
             // L2 and MaxRelativeFdDiff stop on |r| < StopCondition[0] (Iterate3D.cu:758-765)
-            if (cfg.residual_model == LBM_RES_L2 || cfg.residual_model == LBM_RES_FD_REL_DIFF) {
-                double res = 0.0;
-                const int rr = cfg.residual_model == LBM_RES_L2 ? lbm_residual_l2(hd, &res)
-                                                                : lbm_residual_fd_rel_diff(hd, &res);
+            if (res_file) {
+                double res = 0.0, l2 = 0.0;
+                int rr = LBM_OK;
+                if (cfg.residual_model == LBM_RES_FD_REL_DIFF) rr = lbm_residual_fd_rel_diff(hd, &res);
+                if (rr == LBM_OK && (dims == 2 || cfg.residual_model == LBM_RES_L2)) rr = lbm_residual_l2(hd, &l2);
+                if (cfg.residual_model == LBM_RES_L2) res = l2;
                 if (rr == LBM_DIVERGED) {
                     fprintf(stderr, "\nDIVERGENCE!\n");
                     status = 1;
                     break;
                 }
-                if (resf) fprintf(resf, "%d\t%.10e\n", iter, res);
-                if (fabs(res) < cfg.stop_condition[0]) {
+                norm[(size_t)iter - 1] = dims == 2 ? l2 : res;
+                if (dims == 2 && cfg.boundary_id > 0) {
+                    double dl[2];
+                    if (lbm_reference_drag_lift(hd, cfg.boundary_id, x.data(), y.data(), dl) == LBM_OK) {
+                        drag[(size_t)iter - 1] = dl[0];
+                        lift[(size_t)iter - 1] = dl[1];
+                    }
+                }
+                if (cfg.residual_model != LBM_RES_MACRO_DIFF && fabs(res) < cfg.stop_condition[0]) {
                     printf("simulation converged!\n");
                     break;
                 }
@@ -288,7 +302,15 @@ int main(int argc, char **argv) {
         }
     }
     if (md) fclose(md);
-    if (resf) fclose(resf);
+    if (res_file) {
+        if (FILE *resf = fopen((out + "Residuals.txt").c_str(), "w")) {
+            fprintf(resf, "Iter L2_norm L2_norm_weighted Drag Lift\n");
+            for (int i = 0; i < cfg.iterations; ++i)
+                fprintf(resf, "%d %5.4e %5.4e %f %f\n", i, norm[(size_t)i], norm[(size_t)i] / (double)N, drag[(size_t)i],
+                        lift[(size_t)i]);
+            fclose(resf);
+        }
+    }
     if (status != 3) write(out + "FinalData." + ext);
     lbm_destroy(hd);
     return status;

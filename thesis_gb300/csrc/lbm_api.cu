@@ -95,6 +95,10 @@ struct lbm_handle_s {
     // for straight walls), the boundary nodes in ascending order (the
     // reference's collapsed order) and, per BC link, its node's place there
     double *bcq = nullptr;
+    // reference-mode 2D: boundary nodes whose mask carries a boundary id
+    // (bits 24-31), for the reference's drag/lift sums
+    std::vector<long long> id_nodes;
+    std::vector<unsigned char> id_bits;
     std::vector<long long> bc_nodes;
     std::vector<int> link_b;
     std::vector<unsigned char> link_dir;
@@ -444,6 +448,12 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     }
     H->nslots = (int)flags.slot_node.size();
     H->slot_node = flags.slot_node;
+    if (L->dims == 2)
+        for (size_t b = 0; b < refm.bc_nodes.size(); ++b)
+            if (((refm.mask[b] >> 24) & 0xFFull) && (L->node_type[refm.bc_nodes[b]] & 1)) {
+                H->id_nodes.push_back(refm.bc_nodes[b]);
+                H->id_bits.push_back((unsigned char)((refm.mask[b] >> 24) & 0xFFull));
+            }
     if (want_tma) {
         rc = setup_tma(H, flags.word);
         if (rc) {
@@ -573,6 +583,27 @@ int lbm_set_link_q(lbm_handle H, const double *q) {
     CUDA_TRY(cudaStreamWaitEvent(H->stream, H->stepped, 0));
     CUDA_TRY(cudaMemcpyAsync(H->bcq, qt.data(), sizeof(double) * qt.size(), cudaMemcpyHostToDevice, H->stream));
     CUDA_TRY(cudaStreamSynchronize(H->stream));
+    return LBM_OK;
+}
+
+int lbm_reference_drag_lift(lbm_handle H, int boundary_id, const float *node_x, const float *node_y, double *out) {
+    if (!H || !out) return fail(LBM_ERR_INVALID, "null argument");
+    out[0] = out[1] = 0.0;
+    if (H->dims != 2 || boundary_id <= 0 || H->id_nodes.empty()) return LBM_OK;
+    if (!node_x || !node_y) return fail(LBM_ERR_INVALID, "null coordinates");
+    CUDA_TRY(cudaStreamWaitEvent(H->stream, H->stepped, 0));
+    std::vector<float> rho((size_t)H->N);
+    CUDA_TRY(cudaMemcpyAsync(rho.data(), H->rho, sizeof(float) * H->N, cudaMemcpyDeviceToHost, H->stream));
+    CUDA_TRY(cudaStreamSynchronize(H->stream));
+    // per node as gpuUpdateMacro2D stores it (FLOAT_TYPE of a double
+    // product), summed in FP64
+    for (size_t k = 0; k < H->id_nodes.size(); ++k) {
+        if (H->id_bits[k] != (unsigned)boundary_id) continue;
+        const long long i = H->id_nodes[k];
+        const float r = rho[(size_t)i];
+        out[0] += (double)(float)(0.33333333 * (double)r * (double)(20.0f - node_x[i]) * 0.2);
+        out[1] += (double)(float)(0.33333333 * (double)r * (double)(20.0f - node_y[i]) * 0.2);
+    }
     return LBM_OK;
 }
 

@@ -94,6 +94,7 @@ def lib():
         "lbm_create": (C.c_int, [C.POINTER(LatticeDesc), C.POINTER(Params), C.POINTER(vp)]),
         "lbm_set_inlet_velocity": (C.c_int, [vp, fp, fp, fp]),
         "lbm_set_link_q": (C.c_int, [vp, dp]),
+        "lbm_reference_drag_lift": (C.c_int, [vp, C.c_int, fp, fp, dp]),
         "lbm_link_q": (C.c_int, [C.c_int] * 5 + [_IP] * 4 + [fp] * 6 + [C.c_double, dp]),
         "lbm_init": (C.c_int, [vp, fp, fp, fp, fp]),
         "lbm_step": (C.c_int, [vp, C.c_int, C.c_int, vp]),

@@ -212,6 +212,16 @@ class Solver:
             N.check(rc)
         return out, rc
 
+    def reference_drag_lift(self, boundary_id, x, y):
+        """The reference's 2D drag and lift sums over the fluid nodes of a
+        boundary id (lbm_reference_drag_lift); x, y: node coordinates."""
+        xs = np.ascontiguousarray(x, np.float32).reshape(-1)
+        ys = np.ascontiguousarray(y, np.float32).reshape(-1)
+        out = np.zeros(2, np.float64)
+        N.check(self._lib.lbm_reference_drag_lift(self._h, int(boundary_id), _fptr(xs), _fptr(ys),
+                                                  out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
     def momentum_exchange(self, box):
         """Force (fx, fy, fz) on the solid nodes inside box = (x0, x1, y0, y1,
         z0, z1) by momentum exchange."""
