@@ -5,7 +5,7 @@
  * Reynolds number, inlet profile) to its steady velocity and density; the
  * prediction seeds equilibrium populations (lbm_init) that the plain solver
  * then iterates to the residual tolerance, and the plain cold start stays
- * the fallback and the judge of the converged field.  The reference solver
+ * the fallback and the yardstick of the converged field.  The reference solver
  * has no learned part; this is the project's extension of its steady-state
  * loop (Iterate.cu:385-625: residual-driven iteration to a stop condition).
  *

@@ -97,7 +97,7 @@ def main():
 
 
 def main_cavity128():
-    """configs[0]: D2Q9 BGK lid-driven cavity 128x128, u_lid 0.1, Re 100
+    """The D2Q9 BGK lid-driven cavity 128x128, u_lid 0.1, Re 100
     (nu = 0.128), 20,000 steps, FP32, by the reference's kernels; the final
     rho, u, v and the centre lines go to cavity128_bgk_20000.npz."""
     if pyoracle.ref_lib() is None:
