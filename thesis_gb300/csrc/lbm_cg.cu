@@ -7,10 +7,11 @@
 // The collision of a node needs the colour field (rho_r - rho_b)/rho of its
 // 8 (3x3 stencil) or 24 (5x5 stencil) neighbours after streaming, so a step is
 // two launches over the lattice:
-//   cg_density_kernel  pull both colours, write rho_r and rho_b per node;
-//   cg_collide_kernel  pull both colours again, take the neighbours' colour
-//                      field from the density arrays, collide, perturb,
-//                      recolour, write both post-collision colours.
+//   cg_density_kernel  pull both colours, write the colour field
+//                      phi = (rho_r - rho_b)/rho and rho per node;
+//   cg_collide_kernel  pull both colours again, take the neighbours' phi and
+//                      rho for the gradients, collide, perturb, recolour,
+//                      write both post-collision colours and rho_r, rho_b.
 // State between steps: post-collision red and blue populations, SoA by
 // direction, pull double buffer.  Both kernels are HBM-bound: 72 B of
 // populations read by each, 72 B written by the second, 8 B of densities.
@@ -32,7 +33,8 @@ namespace {
 struct CgArgs {
     const float *rin[9], *bin[9];
     float *rout[9], *bout[9];
-    float *R, *B;            // colour densities
+    float *R, *B;            // colour densities (output)
+    float *phi, *dn;         // colour field and density of the streamed state (gradients)
     float *rho, *ux, *uy;    // macroscopic output (when write_macro)
     int nx, ny;
     int write_macro;
@@ -73,8 +75,9 @@ __global__ void __launch_bounds__(CG_BLOCK) cg_density_kernel(const CgArgs a) {
         bb += b[d];
     }
     const int node = x + a.nx * y;
-    a.R[node] = rr;
-    a.B[node] = bb;
+    const float rho = rr + bb;
+    a.phi[node] = (rr - bb) / rho;
+    a.dn[node] = rho;
 }
 
 template <bool PULL, bool HO, bool ENH>
@@ -96,6 +99,8 @@ __global__ void __launch_bounds__(CG_BLOCK) cg_collide_kernel(const CgArgs a) {
     }
     const float rho = r_r + b_r;
     const float u = jx / rho, v = jy / rho;
+    a.R[node] = r_r;
+    a.B[node] = b_r;
     if (a.write_macro) {
         a.rho[node] = rho;
         a.ux[node] = u;
@@ -111,9 +116,8 @@ __global__ void __launch_bounds__(CG_BLOCK) cg_collide_kernel(const CgArgs a) {
 #pragma unroll
         for (int k = 0; k < 24; ++k) {
             const int j = wrapi(x + hx[k], a.nx) + a.nx * wrapi(y + hy[k], a.ny);
-            const float Rj = __ldg(a.R + j), Bj = __ldg(a.B + j), rj = Rj + Bj;
             const float w = (float)(hw[k] / 5040.0);
-            const float a1 = w * (Rj - Bj) / rj, a2 = w * rj;
+            const float a1 = w * __ldg(a.phi + j), a2 = ENH ? w * __ldg(a.dn + j) : 0.f;
             if (ENH) {
                 grx += a2 * (float)hx[k];
                 gry += a2 * (float)hy[k];
@@ -125,9 +129,8 @@ __global__ void __launch_bounds__(CG_BLOCK) cg_collide_kernel(const CgArgs a) {
 #pragma unroll
         for (int k = 1; k < 9; ++k) {
             const int j = wrapi(x + L::cx(k), a.nx) + a.nx * wrapi(y + L::cy(k), a.ny);
-            const float Rj = __ldg(a.R + j), Bj = __ldg(a.B + j), rj = Rj + Bj;
             const float w = k <= 4 ? (float)(4.0 / 12.0) : (float)(1.0 / 12.0);
-            const float a1 = w * (Rj - Bj) / rj, a2 = w * rj;
+            const float a1 = w * __ldg(a.phi + j), a2 = ENH ? w * __ldg(a.dn + j) : 0.f;
             if (ENH) {
                 grx += a2 * (float)L::cx(k);
                 gry += a2 * (float)L::cy(k);
@@ -145,6 +148,8 @@ __global__ void __launch_bounds__(CG_BLOCK) cg_collide_kernel(const CgArgs a) {
     const float G1 = 2.f * u * grx, G2 = u * gry + v * grx, G4 = 2.f * v * gry;
     const float ugr = u * grx + v * gry;
     const bool interface = gnorm > a.g_limit;
+    // one reciprocal per node instead of two divisions per direction
+    const float inv_g = interface ? 1.f / gnorm : 0.f, inv_g2 = inv_g * inv_g;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
         const float cxk = (float)L::cx(k), cyk = (float)L::cy(k);
@@ -152,9 +157,9 @@ __global__ void __launch_bounds__(CG_BLOCK) cg_collide_kernel(const CgArgs a) {
         float pert = 0.f, cosin = 0.f;
         if (interface) {
             const float pcg = cxk * cgx + cyk * cgy;
-            if (k != 0) cosin = pcg / (gnorm * (k <= 4 ? 1.f : (float)1.4142135623730951));
+            if (k != 0) cosin = pcg * inv_g * (k <= 4 ? 1.f : 0.70710678f);
             const float bk = k == 0 ? (float)(-4. / 27.) : (k <= 4 ? (float)(2. / 27.) : (float)(5. / 108.));
-            pert = a.A * gnorm * (wk * (pcg * pcg) / (gnorm * gnorm) - bk);
+            pert = a.A * gnorm * (wk * (pcg * pcg) * inv_g2 - bk);
         }
         const float cu2 = u * cxk + v * cyk;
         const float rest = c_phi[k] + c_teta[k] * mean_alpha;
@@ -250,6 +255,8 @@ static CgArgs cg_args(const lbm_cg_handle_s *H, int from, int write_macro) {
     }
     a.R = H->R;
     a.B = H->B;
+    a.phi = H->phi;
+    a.dn = H->dn;
     a.rho = H->rho;
     a.ux = H->ux;
     a.uy = H->uy;
