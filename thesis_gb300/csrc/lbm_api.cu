@@ -1048,8 +1048,9 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
         if (H->h >= 16) {
             const V hz[] = {{128, 0, 0, 0, 10, 1, 2}, {128, 0, 0, 0, 10, 1, 4}, {128, 0, 0, 0, 10, 1, 8},
                             {128, 0, 0, 0, 10, 1, 16}, {128, 0, 0, 0, 11, 1, 4}, {256, 0, 0, 0, 5, 1, 4},
-                            {64, 0, 0, 0, 20, 1, 4}};
-            vs.insert(vs.end(), hz, hz + 7);
+                            {64, 0, 0, 0, 20, 1, 4},   {64, 0, 0, 0, 20, 1, 8}, {128, 0, 0, 0, 12, 1, 8},
+                            {256, 0, 0, 0, 5, 1, 8}};
+            vs.insert(vs.end(), hz, hz + 10);
         }
     }
     if (H->n % 2 == 0 && hs_ok && !one_node_boundaries(H->P, H->q)) {
