@@ -46,6 +46,10 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--windows", type=int, default=5,
+                    help="timed windows of --steps steps each (at least this many; the value is their median)")
+    ap.add_argument("--window-seconds", type=float, default=2.0,
+                    help="repeat windows until they fill about this much time (clock sampling)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f16s", choices=list(STORAGE_NAMES))
     ap.add_argument("--size", default=None, help="n,m,h (default 256,256,512)")
@@ -55,7 +59,7 @@ def parse():
     ap.add_argument("--cpu-sample", default="64,64,128", help="n,m,h of the CPU-baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="target CPU time of one CPU-baseline sample (steps are chosen to fill it)")
-    ap.add_argument("--workload", default="duct", choices=["duct", "cavities", "cg", "cg3d", "warmstart"],
+    ap.add_argument("--workload", default="duct", choices=["duct", "cavities", "cg", "cg3d", "warmstart", "precision"],
                     help="duct: the D3Q19 MRT sphere-packed duct (default); cavities: a batch of D2Q9 MRT "
                          "lid-driven cavities of uneven sizes, batched vs one by one; cg: colour-gradient "
                          "static droplets on a periodic 1024^2 lattice (Laplace law); warmstart: time to the "
@@ -64,6 +68,10 @@ def parse():
     ap.add_argument("--ws-epochs", type=int, default=150)
     ap.add_argument("--ws-eval", type=int, default=128, help="held-out channels timed cold and warm")
     ap.add_argument("--ws-levels", type=int, default=5, help="U-Net pooling levels")
+    ap.add_argument("--prec-steps", default="5000,50000", help="precision: checkpoints (steps) of the duct runs")
+    ap.add_argument("--prec-storages", default="f32,f16s", help="precision: storages compared with f64")
+    ap.add_argument("--prec-cavity-steps", type=int, default=20000)
+    ap.add_argument("--prec-cylinder-steps", type=int, default=40000)
     ap.add_argument("--cg-size", type=int, default=1024)
     ap.add_argument("--cg-seeds", type=int, default=3, help="droplets (radius uniform in [64, 256] nodes)")
     ap.add_argument("--cg-steps", type=int, default=40000, help="steps per droplet before the Laplace-law check")
@@ -268,6 +276,126 @@ def cavity_sweep(count, seed=0):
     sides = rng.choice(np.arange(64, 769, 32), size=count)
     re = rng.uniform(100.0, 3200.0, size=count)
     return [int(x) for x in sides], [float(r) for r in re]
+
+
+def _rel_l2(a, b, fl):
+    """Relative L2 difference of a list of fields over the fluid nodes."""
+    num = sum(float((((x.astype(np.float64) - y.astype(np.float64))[fl]) ** 2).sum()) for x, y in zip(a, b))
+    den = sum(float(((y.astype(np.float64)[fl]) ** 2).sum()) for y in b)
+    return float(np.sqrt(num / max(den, 1e-300)))
+
+
+def run_precision(args):
+    """Storage precision against F64 storage of the same solver on the
+    duct workload (full size by default) and on the cavity centrelines and
+    cylinder drag of smaller 2D cases: relative L2 of u and of rho - 1 over
+    fluid nodes at each checkpoint, plus the velocity residual of the F64 run
+    there (how close to steady it is)."""
+    import torch
+    from thesis_gb300 import build as native_build
+    from thesis_gb300 import lattice
+    from thesis_gb300 import native as N
+    from thesis_gb300.solver import Arguments, Solver
+
+    native_build.build()
+    torch.cuda.set_device(0)
+    n, m, h = (int(x) for x in args.size.split(",")) if args.size else (WORKLOAD["n"], WORKLOAD["m"], WORKLOAD["h"])
+    checkpoints = sorted(int(x) for x in args.prec_steps.split(","))
+    stores = ["f64"] + [x for x in args.prec_storages.split(",") if x and x != "f64"]
+    lat = make_lattice(n, m, h, 0)
+    fl = lat.node_type == 1
+    nn = lat.num_nodes
+    fields = {}
+    resid = {}
+    seconds = {}
+    for st in stores:
+        t0 = time.perf_counter()
+        with Solver(lat, solver_args(STORAGE_NAMES[st])) as s:
+            s.init(np.ones(nn, np.float32), np.zeros(nn, np.float32), np.zeros(nn, np.float32),
+                   np.zeros(nn, np.float32))
+            done = 0
+            for c in checkpoints:
+                s.step(c - 100 - done, write_macro=True)
+                s.norms()
+                s.step(100, write_macro=True)
+                nr, rc = s.norms()
+                done = c
+                fields[(st, c)] = [a.copy() for a in s.macro()]
+                resid[(st, c)] = float(np.sqrt(nr[0] / max(nr[1], 1e-300)))
+        seconds[st] = time.perf_counter() - t0
+    duct = []
+    for c in checkpoints:
+        ref = fields[("f64", c)]
+        row = {"steps": c, "f64_velocity_residual_100_steps": resid[("f64", c)],
+               "u_max_f64": float(np.sqrt(ref[1] ** 2 + ref[2] ** 2 + ref[3] ** 2)[fl].max())}
+        for st in stores[1:]:
+            g = fields[(st, c)]
+            row[st] = {"velocity_rel_l2": _rel_l2(g[1:], ref[1:], fl),
+                       "rho_minus_1_rel_l2": _rel_l2([g[0] - 1.0], [ref[0] - 1.0], fl)}
+        duct.append(row)
+
+    # lid-driven cavity 128^2 (D2Q9 MRT, u_lid 0.1, Re 100): centreline profiles
+    cav = lattice.cavity2d(128)
+    cavfl = cav.node_type == 1
+    prof = {}
+    for st in stores:
+        a = Arguments(u=0.1, viscosity=0.128, collision_model=N.MRT, mode=N.MODE_PHYSICS, init_equilibrium=1,
+                      outlet_profile=N.OUTLET_ZOUHE, storage=STORAGE_NAMES[st])
+        with Solver(cav, a) as s:
+            s.init(np.ones(cav.num_nodes), np.zeros(cav.num_nodes), np.zeros(cav.num_nodes),
+                   np.zeros(cav.num_nodes))
+            s.step(args.prec_cavity_steps, write_macro=True)
+            rho, u, v, _ = s.macro()
+        U = u.reshape(128, 128).astype(np.float64)
+        V = v.reshape(128, 128).astype(np.float64)
+        prof[st] = (U[:, 64], V[64, :], [rho, u, v])
+    cavity = {"lattice": [128, 128], "steps": args.prec_cavity_steps}
+    for st in stores[1:]:
+        du = np.abs(prof[st][0] - prof["f64"][0]).max() / np.abs(prof["f64"][0]).max()
+        dv = np.abs(prof[st][1] - prof["f64"][1]).max() / np.abs(prof["f64"][1]).max()
+        cavity[st] = {"centreline_u_max_rel": float(du), "centreline_v_max_rel": float(dv),
+                      "velocity_rel_l2": _rel_l2(prof[st][2][1:], prof["f64"][2][1:], cavfl)}
+
+    # cylinder in a channel (D2Q9 MRT, parabolic inlet u_max 0.05, pressure
+    # outlet, straight walls): drag and lift by momentum exchange
+    cn, cm = 440, 82
+    cyl = lattice.cylinder_channel2d(cn, cm, centre=(0.2 / 0.41 * cm, 0.2 / 0.41 * cm), radius=0.05 / 0.41 * cm)
+    y = np.arange(cm, dtype=np.float64)
+    prof_in = 4 * 0.05 * y * (cm - 1 - y) / (cm - 1) ** 2
+    umean = 2.0 / 3.0 * 0.05
+    dia = 2 * 0.05 / 0.41 * cm
+    nu = umean * dia / 20.0
+    r = 0.05 / 0.41 * cm
+    cx0 = 0.2 / 0.41 * cm
+    box = (int(cx0 - r) - 1, int(cx0 + r) + 2, int(cx0 - r) - 1, int(cx0 + r) + 2, 0, 0)
+    forces = {}
+    for st in stores:
+        a = Arguments(u=0.05, viscosity=nu, collision_model=N.MRT, mode=N.MODE_PHYSICS, init_equilibrium=1,
+                      inlet_profile=N.INLET, outlet_profile=N.OUTLET_PRESSURE, rho_out=1.0, storage=STORAGE_NAMES[st])
+        with Solver(cyl, a) as s:
+            uin = np.zeros(cyl.num_nodes, np.float32)
+            uin.reshape(cm, cn)[:, 0] = prof_in
+            s.set_inlet_velocity(uin, np.zeros(cyl.num_nodes, np.float32), np.zeros(cyl.num_nodes, np.float32))
+            s.init(np.ones(cyl.num_nodes), uin, np.zeros(cyl.num_nodes), np.zeros(cyl.num_nodes))
+            s.step(args.prec_cylinder_steps, write_macro=True)
+            forces[st] = s.momentum_exchange(box)
+    cylinder = {"lattice": [cn, cm], "steps": args.prec_cylinder_steps, "re": 20, "diameter_nodes": dia,
+                "drag_f64": float(forces["f64"][0]), "lift_f64": float(forces["f64"][1]),
+                "drag_coefficient_f64": float(2 * forces["f64"][0] / (umean ** 2 * dia))}
+    for st in stores[1:]:
+        cylinder[st] = {"drag_rel": float(abs(forces[st][0] - forces["f64"][0]) / abs(forces["f64"][0])),
+                        "lift_abs_over_drag": float(abs(forces[st][1] - forces["f64"][1]) / abs(forces["f64"][0]))}
+    line = {"metric": "storage precision against F64 storage (relative L2 over fluid nodes)",
+            "value": duct[0][stores[1]]["velocity_rel_l2"] if len(stores) > 1 else None,
+            "unit": "relative L2 of u, %s storage at %d steps" % (stores[1] if len(stores) > 1 else "-", checkpoints[0]),
+            "n_gpus": 1, "steps": checkpoints[-1], "warmup": 0, "ms_per_step": None, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 arithmetic, storage per entry",
+            "data": "synthetic (seeded sphere packing)",
+            "config": dict(workload_config(args, n, m, h), storage="f64 reference vs " + ",".join(stores[1:])),
+            "duct": duct, "cavity_centrelines": cavity, "cylinder_drag": cylinder,
+            "run_seconds": seconds, "gpu_launches": None}
+    print(json.dumps(line))
+    return 0
 
 
 def run_cavities(args):
@@ -630,6 +758,8 @@ def main():
         return run_cg3d(args)
     if args.workload == "cavities" and args.impl != "reference":
         return run_cavities(args)
+    if args.workload == "precision" and args.impl != "reference":
+        return run_precision(args)
     rank, world, local = dist_info()
     if args.impl == "reference":
         return run_reference_arm(args, rank, world)
@@ -670,17 +800,32 @@ def main():
     stream.synchronize()
     if world > 1:
         dist.barrier()
+    # the timed region is repeated as windows of exactly --steps steps each,
+    # at least --windows of them and enough to fill --window-seconds, so the
+    # clock sampler sees the load; the value comes from the median window
     clocks = ClockSampler(local)
     clocks.start()
+    time.sleep(0.2)
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
+    ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev[0].record(stream)
     s.step(args.steps, write_macro=False, stream=stream.cuda_stream)
-    e1.record(stream)
-    e1.synchronize()
+    ev[1].record(stream)
+    ev[1].synchronize()
+    first_ms = ev[0].elapsed_time(ev[1])
+    nwin = max(args.windows, int(args.window_seconds * 1e3 / max(first_ms, 1e-3)))
+    nwin = min(nwin, 2000)
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nwin)]
+    torch.cuda.synchronize()
+    for a, b in events:
+        a.record(stream)
+        s.step(args.steps, write_macro=False, stream=stream.cuda_stream)
+        b.record(stream)
+    events[-1][1].synchronize()
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
+    win_ms = [a.elapsed_time(b) for a, b in events]
+    ms = statistics.median(win_ms)
     t = torch.tensor([ms], dtype=torch.float64, device=dev)
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -750,7 +895,13 @@ def main():
                              "traffic": traffic,
                              "algorithmic_bytes_per_launch": alg_bytes,
                              "bytes_per_fluid_update": B_LU[storage]},
-                "clocks": clk, "gpu_launches": args.steps,
+                "clocks": clk, "gpu_launches": (nwin + 1) * args.steps,
+                "windows": {"count": nwin, "steps_each": args.steps, "median_ms": ms,
+                            "min_ms": min(win_ms), "max_ms": max(win_ms),
+                            "p10_ms": float(np.percentile(win_ms, 10)), "p90_ms": float(np.percentile(win_ms, 90)),
+                            "value_at_min_ms": total_updates / (min(win_ms) / 1e3) / 1e9,
+                            "value_at_max_ms": total_updates / (max(win_ms) / 1e3) / 1e9,
+                            "ms_per_step_x_sm_mhz": (ms / args.steps * clk["sm_mhz"]) if clk.get("sm_mhz") else None},
                 "e2e": e2e, "cpu_baseline": cpu}
         print(json.dumps(line))
     if world > 1:

@@ -266,7 +266,12 @@ int lbm_macro_diff(lbm_handle h, double *out);
  * the process exits), so n is limited to lbm_noalloc_max_nodes() (67,108,864)
  * and larger calls return LBM_ERR_INVALID.  Calls share that array, so calls
  * that overlap on the GPU race and must be serialised.  The first call on a
- * device looks up the array's address; make it before any stream capture.
+ * device looks up the array's address and keeps it; make it before any
+ * stream capture.  That address lives as long as the device's context: after
+ * cudaDeviceReset on a device, do not call this function on it again in the
+ * same process.  A CUDA error pending at entry or raised by the launches
+ * returns LBM_ERR_CUDA (message in lbm_noalloc_last_error()); pending errors
+ * are left for the caller's own checks, not cleared.
  * Work is queued on `stream` (a cudaStream_t, NULL = legacy default). */
 int lbm_fluid_norms_noalloc(const uint32_t *word, const float *rho, const float *u, const float *v,
                             const float *w, float *u_prev, float *v_prev, float *w_prev, long long n,
@@ -293,6 +298,15 @@ long long lbm_fluid_nodes(lbm_handle h);
  * variant the lattice does not admit falls back to 1, except jit and jit2,
  * whose build failure lbm_create reports. */
 int lbm_kernel_variant(lbm_handle h);
+
+/* Empty when the handle runs the kernel lbm_create meant to use; otherwise
+ * why it fell back (the run-time specialised kernel could not be built, for
+ * example without NVRTC or the toolkit headers it compiles against), in
+ * which case the handle runs the compiled-in one-node kernel, about 1.4x
+ * slower.  The first fallback in a process is also printed on stderr; with
+ * the environment variable THESIS_LBM_REQUIRE_JIT=1, lbm_create fails
+ * instead (LBM_ERR_CUDA).  No counterpart in the reference. */
+const char *lbm_kernel_warning(lbm_handle h);
 
 /* Autotuner of the run-time specialised kernel: builds its variants (one
  * node per thread with blocks of 128 or 256 threads along x, plain or

@@ -17,6 +17,22 @@ REF_DIR = os.path.join(HERE, "_ref")
 
 ORC_OK, ORC_UNSUPPORTED, ORC_BAD_INPUT = 0, 3, 4
 
+
+def reference_root():
+    """Root of the reference project's tree when it is mounted (environment
+    variable THESIS_REFERENCE_ROOT, else its usual mount point), or None."""
+    root = os.environ.get("THESIS_REFERENCE_ROOT", "/root/reference")
+    return root if os.path.isdir(root) else None
+
+
+def reference_file(*parts):
+    """Path of a file inside the reference tree, or None when it is absent."""
+    root = reference_root()
+    if root is None:
+        return None
+    path = os.path.join(root, *parts)
+    return path if os.path.exists(path) else None
+
 _RP = ["u", "v", "w", "rho", "viscosity", "g"]
 _RI = ["inlet_profile", "outlet_profile", "collision_model", "boundary_type", "bc_wall_model",
        "update_inlet_outlet", "boundary_id"]

@@ -157,9 +157,11 @@ def test_invalid_links_are_rejected(native_lib):
 
 def test_reference_generator_mesh_masks(native_lib, oracle):
     import os
-    g = "/root/reference/Source code/latticegen2_W8/"
-    if not os.path.exists(g + "lidvalidation_Node.dat"):
+    from oracle.pyoracle import reference_file
+    g = reference_file("Source code", "latticegen2_W8")
+    if g is None or not os.path.exists(os.path.join(g, "lidvalidation_Node.dat")):
         pytest.skip("reference tree not mounted")
+    g += os.sep
     lat = lattice.from_files(g + "lidvalidation_Node.dat", g + "lidvalidation_BC.dat")
     mask, _, _, _ = build_flags(lat, Arguments())
     ref = oracle.run_reference(lat, 0)

@@ -17,7 +17,9 @@ import latticegen_cases as LC  # noqa: E402
 
 from thesis_gb300 import lattice  # noqa: E402
 
-REF_TREE = "/root/reference/Source code/latticegen2_W8"
+from oracle.pyoracle import reference_file  # noqa: E402
+
+REF_TREE = reference_file("Source code", "latticegen2_W8") or "reference tree not mounted"
 
 
 @pytest.mark.parametrize("case", LC.CASES, ids=lambda c: "%s_%d_%d" % c)

@@ -68,9 +68,11 @@ def test_reference_lid_cavity_golden_mesh(oracle):
     """The 30^3 lid cavity the reference generator ships (latticegen2_W8/
     lidvalidation_{Node,BC}.dat): masks, stream flags and 5 MRT steps."""
     import os
-    g = "/root/reference/Source code/latticegen2_W8/"
-    if not os.path.exists(g + "lidvalidation_Node.dat"):
+    from oracle.pyoracle import reference_file
+    g = reference_file("Source code", "latticegen2_W8")
+    if g is None or not os.path.exists(os.path.join(g, "lidvalidation_Node.dat")):
         pytest.skip("reference tree not mounted")
+    g += os.sep
     lat = lattice.from_files(g + "lidvalidation_Node.dat", g + "lidvalidation_BC.dat")
     kw = dict(u=0.05, viscosity=0.1, collision_model=3, delta=1 / 29)
     ref = oracle.run_reference(lat, 5, **kw)

@@ -28,12 +28,15 @@ def _noalloc_fn(lib):
     return fn
 
 
-def test_noalloc_norms_match_allocating_norms(native_lib):
+# one block of partial sums covers 16,384 nodes: 20x16x32 fits one block;
+# 40x32x70 (89,600 nodes) needs six, the last one partly filled
+@pytest.mark.parametrize("dims", [(20, 16, 32), (40, 32, 70)])
+def test_noalloc_norms_match_allocating_norms(native_lib, dims):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     fn = _noalloc_fn(native_lib)
-    lat = lattice.sphere_duct(20, 16, 32, porosity=0.8, rmin=3, rmax=4, seed=3)
+    lat = lattice.sphere_duct(*dims, porosity=0.8, rmin=3, rmax=4, seed=3)
     args = Arguments(viscosity=0.1, collision_model=N.MRT, mode=N.MODE_PHYSICS, init_equilibrium=1,
                      inlet_profile=N.INLET_PRESSURE, outlet_profile=N.OUTLET_PRESSURE,
                      rho_in=1.01, rho_out=1.0)
@@ -58,8 +61,10 @@ def test_noalloc_norms_match_allocating_norms(native_lib):
             torch.cuda.synchronize(dev)
             got = out.cpu().numpy()
             np.testing.assert_allclose(got, expect, rtol=RTOL, atol=0.0)
-            # the previous-velocity arrays now hold this call's velocity
-            np.testing.assert_array_equal(prev[0].cpu().numpy(), fields[1].cpu().numpy())
+            # at fluid nodes the previous-velocity arrays now hold this call's velocity
+            fl = lat.node_type == 1
+            for k in range(3):
+                np.testing.assert_array_equal(prev[k].cpu().numpy()[fl], fields[1 + k].cpu().numpy()[fl])
 
 
 def test_noalloc_rejects_oversized_calls(native_lib):

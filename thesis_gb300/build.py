@@ -49,7 +49,8 @@ def tool_path(name):
 def _newest_input():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if os.path.isfile(os.path.join(CSRC, f))]
     files += [os.path.join(CLI_DIR, f) for f in os.listdir(CLI_DIR)]
-    files.append(os.path.join(ROOT, "include", "thesis_lbm.h"))
+    inc = os.path.join(ROOT, "include")
+    files += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith(".h")]
     files.append(os.path.abspath(__file__))
     return max(os.path.getmtime(f) for f in files)
 

@@ -113,6 +113,7 @@ struct lbm_handle_s {
     bool pair_kernel = false;  // two nodes per thread (even nx, F32/F16S)
     bool tma_kernel = false;   // row-staged bulk-copy kernel
     bool jit_kernel = false;   // step kernel specialised for this lattice at run time
+    std::string kernel_warning; // why the run-time build fell back to the compiled-in kernel
     cudaKernel_t jit_fn = nullptr;
     JitStepKey jit_key{};
     int32_t *tma_row = nullptr;
@@ -463,9 +464,21 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     }
     if (want_jit) {
         rc = setup_jit(H, flags.word, jit_pair, jit_hspace);
-        if (rc && jit_required) {
+        const char *req = getenv("THESIS_LBM_REQUIRE_JIT");
+        if (rc && (jit_required || (req && *req && strcmp(req, "0") != 0))) {
             free_handle(H);
             return rc;
+        }
+        if (rc) {
+            // the default kernel could not be built (no NVRTC, or the toolkit
+            // headers it compiles against are missing): keep the compiled-in
+            // kernel, which is slower, and say so once per process on stderr
+            // and per handle through lbm_kernel_warning
+            H->kernel_warning = "run-time specialised step kernel unavailable, using the compiled-in kernel: " +
+                                std::string(lbm_last_error());
+            static std::once_flag warned;
+            std::call_once(warned, [&] { fprintf(stderr, "thesis_lbm: %s\n", H->kernel_warning.c_str()); });
+            rc = LBM_OK;
         }
     }
 
@@ -1014,6 +1027,8 @@ long long lbm_fluid_nodes(lbm_handle H) { return H ? H->fluid : -1; }
 int lbm_kernel_variant(lbm_handle H) {
     return H ? (H->jit_kernel ? 4 : (H->tma_kernel ? 3 : (H->pair_kernel ? 2 : 1))) : -1;
 }
+
+const char *lbm_kernel_warning(lbm_handle H) { return H ? H->kernel_warning.c_str() : ""; }
 
 int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred) {
     if (!H) return fail(LBM_ERR_INVALID, "null handle");

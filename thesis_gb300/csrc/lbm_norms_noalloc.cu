@@ -21,7 +21,15 @@
 //     race on the partials and give wrong sums: serialise them;
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (with that device current) and caches it; make that
-//     first call before any stream capture on the device.
+//     first call before any stream capture on the device.  The cached address
+//     belongs to the device's context: cudaDeviceReset destroys that context
+//     and the library's module with it, so a process that resets a device must
+//     not call this entry point on that device afterwards (the cached address
+//     would point at memory that no longer holds the array);
+//   * errors: a CUDA error already pending when the call starts, or raised by
+//     its launches, is returned as LBM_ERR_CUDA with a message in
+//     lbm_noalloc_last_error().  The pending error is only peeked at, never
+//     cleared, so the caller's own error checks still see it.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -120,8 +128,12 @@ int lbm_fluid_norms_noalloc(const uint32_t *word, const float *rho, const float 
         return noalloc_fail(LBM_ERR_INVALID,
                             "lbm_fluid_norms_noalloc: " + std::to_string(n) + " nodes exceed the maximum of " +
                                 std::to_string(lbm_noalloc_max_nodes()) + " (static partials array)");
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess)
+        return noalloc_fail(LBM_ERR_CUDA, std::string("lbm_fluid_norms_noalloc: an earlier CUDA error is pending: ") +
+                                              cudaGetErrorString(e));
     int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return noalloc_fail(LBM_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
         return noalloc_fail(LBM_ERR_INVALID, "lbm_fluid_norms_noalloc: device ordinal out of range");
@@ -141,7 +153,7 @@ int lbm_fluid_norms_noalloc(const uint32_t *word, const float *rho, const float 
     cudaStream_t s = (cudaStream_t)stream;
     noalloc_partial<<<nblocks, NOALLOC_THREADS, 0, s>>>(word, rho, u, v, w, u_prev, v_prev, w_prev, n, partials);
     noalloc_final<<<1, 32, 0, s>>>(partials, nblocks, out);
-    e = cudaGetLastError();
+    e = cudaPeekAtLastError();
     if (e != cudaSuccess) return noalloc_fail(LBM_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
     return LBM_OK;
 }

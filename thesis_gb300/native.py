@@ -109,6 +109,7 @@ def lib():
         "lbm_fluid_nodes": (C.c_longlong, [vp]),
         "lbm_bytes_per_update": (C.c_int, [vp]),
         "lbm_kernel_variant": (C.c_int, [vp]),
+        "lbm_kernel_warning": (C.c_char_p, [vp]),
         "lbm_jit_check": (C.c_int, [C.c_int] * 11),
         "lbm_autotune": (C.c_int, [vp, C.c_int, _IP, _IP, _IP]),
         "lbm_kernel_config": (C.c_int, [vp, _IP, _IP, _IP]),

@@ -6,6 +6,7 @@ loop reads; `Solver` wraps one libthesis_lbm handle.  All compute runs in the
 CUDA library; this module only marshals arrays.
 """
 import ctypes as C
+import warnings
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -126,6 +127,9 @@ class Solver:
         N.check(self._lib.lbm_create(C.byref(d), C.byref(p), C.byref(h)))
         del keep
         self._h = h
+        warn = self._lib.lbm_kernel_warning(h)
+        if warn:
+            warnings.warn(warn.decode(), RuntimeWarning, stacklevel=2)
 
     def close(self):
         if getattr(self, "_h", None):
