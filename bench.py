@@ -37,8 +37,8 @@ sys.path.insert(0, ROOT)
 WORKLOAD = dict(n=256, m=256, h=512, porosity=0.70, rmin=6.0, rmax=14.0, tau=0.8,
                 rho_in=1.005, rho_out=1.0)
 METRIC = "GLUPS (fluid-node updates/s / 1e9), D3Q19 MRT sphere-packed duct"
-STORAGE_NAMES = {"f16s": 1, "f32": 0, "f64": 2}
-B_LU = {0: 152, 1: 76, 2: 304}   # algorithmic population bytes per fluid-node update
+STORAGE_NAMES = {"f16s": 1, "f32": 0, "f64": 2, "f16c": 3}
+B_LU = {0: 152, 1: 76, 2: 304, 3: 76}   # algorithmic population bytes per fluid-node update
 
 
 def parse():
@@ -69,15 +69,21 @@ def parse():
     ap.add_argument("--ws-eval", type=int, default=128, help="held-out channels timed cold and warm")
     ap.add_argument("--ws-levels", type=int, default=5, help="U-Net pooling levels")
     ap.add_argument("--prec-steps", default="5000,50000", help="precision: checkpoints (steps) of the duct runs")
-    ap.add_argument("--prec-storages", default="f32,f16s", help="precision: storages compared with f64")
+    ap.add_argument("--prec-storages", default="f32,f16s,f16c", help="precision: storages compared with f64")
     ap.add_argument("--prec-cavity-steps", type=int, default=20000)
     ap.add_argument("--prec-cylinder-steps", type=int, default=40000)
     ap.add_argument("--cg-size", type=int, default=1024)
+    ap.add_argument("--cg-storages", default="f16s,f32,f64",
+                    help="cg: storages run (the first gives the value; f64 is the precision reference)")
     ap.add_argument("--cg-seeds", type=int, default=3, help="droplets (radius uniform in [64, 256] nodes)")
     ap.add_argument("--cg-steps", type=int, default=40000, help="steps per droplet before the Laplace-law check")
     ap.add_argument("--cg3-size", type=int, default=256, help="D3Q19 colour-gradient box side")
     ap.add_argument("--cg3-steps", type=int, default=200)
     ap.add_argument("--domains", type=int, default=512, help="cavities in the batch")
+    ap.add_argument("--cav-tol-side", type=int, default=0,
+                    help="cavities: also run the cavities with sides up to this to --cav-tol (0: skip)")
+    ap.add_argument("--cav-tol", type=float, default=1e-6)
+    ap.add_argument("--cav-tol-max-steps", type=int, default=1000000)
     ap.add_argument("--one-by-one-steps", type=int, default=20,
                     help="steps per cavity when the cavities run one launch per step each")
     ap.add_argument("--kernel", default="auto",
@@ -101,7 +107,7 @@ def workload_config(args, n, m, h):
             "lattice": [n, m, h], "collision": "MRT", "storage": args.storage,
             "boundaries": "Zou-He pressure z faces, half-way bounce-back",
             "l2_policy": "inputs larger than L2 (population buffers 2 x %.2f GB vs 129 MB L2)"
-                         % (19 * n * m * h * (2 if args.storage == "f16s" else 4) / 1e9)}
+                         % (19 * n * m * h * B_LU[STORAGE_NAMES[args.storage]] / 76 * 2 / 2 / 1e9)}
 
 
 def make_lattice(n, m, h, seed):
@@ -449,6 +455,28 @@ def run_cavities(args):
             upd_one += s.fluid_nodes * k1
     del os.environ["THESIS_LBM_KERNEL"]
     one = upd_one / t_one / 1e9
+    blu = B_LU.get(storage, 0) * 9 // 19  # D2Q9: 9 populations read and written
+    peak, peak_kind = measured_peak()
+    achieved = blu * fluid / (ms / args.steps / 1e3) / 1e9
+    tol_run = run_cavities_to_tolerance(args, sides, res, storage) if args.cav_tol_side > 0 else None
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import pyoracle
+        L = pyoracle.oracle_lib()
+        nc = 192
+        lat = lattice.cavity2d(nc)
+        kw = dict(u=0.1, viscosity=0.1 * nc / 1000.0, collision_model=3, outlet_profile=1)
+        t0 = time.perf_counter()
+        pyoracle.run_oracle(lat, 20, mode=1, init_kind=1, **kw)
+        est = (time.perf_counter() - t0) / 20
+        steps = int(min(max(args.cpu_seconds / max(est, 1e-6), 20), 200000))
+        t0 = time.perf_counter()
+        pyoracle.run_oracle(lat, steps, mode=1, init_kind=1, **kw)
+        dt = time.perf_counter() - t0
+        cpu = {"value": int((lat.node_type == 1).sum()) * steps / dt / 1e9, "unit": "GLUPS",
+               "cores": L.orc_threads(), "kind": "port",
+               "sample": "oracle restatement of the reference kernels (physics mode, FP32, OpenMP) on one "
+                         "%dx%d MRT cavity at Re 1000, %d steps, %.1f s" % (nc, nc, steps, dt)}
     line = {"metric": "GLUPS (fluid-node updates/s / 1e9), batch of %d D2Q9 MRT lid-driven cavities" % args.domains,
             "value": value, "unit": "GLUPS", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -459,67 +487,151 @@ def run_cavities(args):
                        "l2_policy": "inputs larger than L2"},
             "one_by_one": {"value": one, "unit": "GLUPS", "steps_per_cavity": k1,
                            "kernel": "step_kernel_h_fixed (same code as the batch), one launch per cavity step"},
-            "batched_over_one_by_one": value / one, "clocks": clk, "gpu_launches": args.steps}
+            "batched_over_one_by_one": value / one, "clocks": clk, "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "bytes_per_fluid_update": blu},
+            "to_tolerance": tol_run, "cpu_baseline": cpu}
     print(json.dumps(line))
     return 0
 
 
+def run_cavities_to_tolerance(args, sides, res, storage):
+    """The cavities of the sweep with sides up to --cav-tol-side, each run
+    to a 1e-6 velocity residual (checked every 100 steps, FP64 sums): all in
+    one batch (lbm_batch_run_to_tolerance, converged domains retire from the
+    tile table) against one handle per cavity stepped and checked in turn."""
+    import torch
+    from thesis_gb300 import lattice
+    from thesis_gb300 import native as N
+    from thesis_gb300.batch import Batch, cavity_args
+    from thesis_gb300.solver import Solver
+    pick = [i for i, n in enumerate(sides) if n <= args.cav_tol_side]
+    ss = [sides[i] for i in pick]
+    rr = [res[i] for i in pick]
+    lats = [lattice.cavity2d(n) for n in ss]
+    cargs = [cavity_args(n, r, storage=storage) for n, r in zip(ss, rr)]
+    tol, every, cap = args.cav_tol, 100, args.cav_tol_max_steps
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b = Batch(lats, cargs)
+    b.init()
+    steps, last, rc = b.run_to_tolerance(tol, every, cap)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    b.close()
+    fl = np.array([int((l.node_type == 1).sum()) for l in lats])
+    conv = last <= tol
+    upd = int((fl * steps).sum())
+    # one by one: the same cavities, one handle each, stepped and checked in
+    # turn; a cavity stops at the batch's step count for it (the same check
+    # cadence gives the same count) or at the cap
+    os.environ["THESIS_LBM_KERNEL"] = "jith"
+    t_one = 0.0
+    one_steps = []
+    for lat, a, k in zip(lats, cargs, steps):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        with Solver(lat, a) as s:
+            s.init()
+            done = 0
+            s.residual()
+            while done < cap:
+                s.step(every, write_macro=True)
+                done += every
+                r, rcs = s.residual()
+                if not (r > tol) or rcs != N.LBM_OK:
+                    break
+        torch.cuda.synchronize()
+        t_one += time.perf_counter() - t1
+        one_steps.append(done)
+    del os.environ["THESIS_LBM_KERNEL"]
+    return {"cavities": len(ss), "max_side": args.cav_tol_side, "tolerance": tol, "check_every": every,
+            "step_cap": cap, "converged": int(conv.sum()),
+            "not_converged": [{"side": int(n), "re": float(r), "steps": int(k), "residual": float(x)}
+                              for n, r, k, x, c in zip(ss, rr, steps, last, conv) if not c],
+            "steps_median": float(np.median(steps)), "steps_max": int(steps.max()),
+            "batch_seconds": t_batch, "one_by_one_seconds": t_one, "batched_speedup": t_one / t_batch,
+            "fluid_node_updates": upd, "batch_glups": upd / t_batch / 1e9,
+            "one_by_one_steps_match": int(sum(int(a) == int(b) for a, b in zip(one_steps, steps))),
+            "includes": "handle creation (host flags, upload), initial state, steps, residual checks"}
+
+
 def run_cg(args):
-    """Colour-gradient static droplets: GPU step throughput, Laplace-law
-    pressure jump against 1/R, peak spurious current."""
+    """Colour-gradient static droplets: GPU step throughput per storage,
+    Laplace-law pressure jump against 1/R, peak spurious current, and each
+    storage's error in those against F64 storage of the same solver."""
     import torch
     from thesis_gb300 import build as native_build
     from thesis_gb300 import multiphase as mp
+    from thesis_gb300 import native as N
     native_build.build()
     n = args.cg_size
     rng = np.random.default_rng(0)
     radii = rng.uniform(64.0, 256.0, size=args.cg_seeds)
-    results = []
-    value = ms = None
+    stores = [x for x in args.cg_storages.split(",") if x]
+    results = {st: [] for st in stores}
+    speed = {}
     clk = None
-    for k, R in enumerate(radii):
-        a = mp.CgArguments(bubble_radius=R / (n - 1), A=0.005, beta=0.7, r_viscosity=1 / 6, b_viscosity=1 / 6,
-                           r_alpha=4 / 9, b_alpha=4 / 9, control_param=0.9)
-        r0, b0 = mp.create_bubble(n, n, a)
-        with mp.CgSolver(n, n, a) as s:
-            s.init(r0, b0)
-            stream = torch.cuda.Stream()
-            s.step(max(args.warmup, 3), write_macro=False, stream=stream.cuda_stream)
-            stream.synchronize()
-            if k == 0:
-                clocks = ClockSampler(0)
-                clocks.start()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            s.step(args.cg_steps - 1, write_macro=False, stream=stream.cuda_stream)
-            s.step(1, write_macro=True, stream=stream.cuda_stream)
-            e1.record(stream)
-            e1.synchronize()
-            if k == 0:
-                clk = clocks.stop()
-                ms = e0.elapsed_time(e1) / args.cg_steps
-                value = n * n / (ms / 1e3) / 1e9
-            lap, rc = s.laplace()
-            rr, br, _, _ = s.macro()
-        # the reference's Laplace check: colour densities averaged where
-        # |chi| >= control_param (Multiphase.cu:1054-1080); interface nodes
-        # above the threshold pull the inside average down by O(1/R)
-        p_in = 3 / 5 * (1 - a.r_alpha) * lap[0] / max(lap[1], 1)
-        p_out = 3 / 5 * (1 - a.b_alpha) * lap[2] / max(lap[3], 1)
-        # Laplace's law proper: total pressure c_s^2 (r + b) in the droplet's
-        # core (r < R/2) against the far field (r > R + 16)
-        rho = (rr.astype(np.float64) + br).reshape(n, n)
-        jj, ii = np.mgrid[0:n, 0:n]
-        dist = np.hypot(ii - (n - 1) / 2, jj - (n - 1) / 2)
-        cs2 = 3 / 5 * (1 - a.r_alpha)
-        dp = cs2 * (rho[dist < R / 2].mean() - rho[dist > R + 16].mean())
-        results.append({"R": float(R), "dp": float(dp), "sigma_measured": float(R * dp),
-                        "dp_reference_threshold": p_in - p_out, "max_u": float(lap[4]),
-                        "status": "ok" if rc == 0 else "diverged"})
+    for st in stores:
+        for k, R in enumerate(radii):
+            a = mp.CgArguments(bubble_radius=R / (n - 1), A=0.005, beta=0.7, r_viscosity=1 / 6, b_viscosity=1 / 6,
+                               r_alpha=4 / 9, b_alpha=4 / 9, control_param=0.9, storage=STORAGE_NAMES[st])
+            r0, b0 = mp.create_bubble(n, n, a)
+            with mp.CgSolver(n, n, a) as s:
+                s.init(r0, b0)
+                stream = torch.cuda.Stream()
+                s.step(max(args.warmup, 3), write_macro=False, stream=stream.cuda_stream)
+                stream.synchronize()
+                timed = k == 0
+                if timed and clk is None:
+                    clocks = ClockSampler(0)
+                    clocks.start()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                s.step(args.cg_steps - 1, write_macro=False, stream=stream.cuda_stream)
+                s.step(1, write_macro=True, stream=stream.cuda_stream)
+                e1.record(stream)
+                e1.synchronize()
+                if timed:
+                    if clk is None:
+                        clk = clocks.stop()
+                    ms = e0.elapsed_time(e1) / args.cg_steps
+                    speed[st] = {"ms_per_step": ms, "glups": n * n / (ms / 1e3) / 1e9}
+                lap, rc = s.laplace()
+                rr, br, _, _ = s.macro()
+            # the reference's Laplace check: colour densities averaged where
+            # |chi| >= control_param (Multiphase.cu:1054-1080); interface nodes
+            # above the threshold pull the inside average down by O(1/R)
+            p_in = 3 / 5 * (1 - a.r_alpha) * lap[0] / max(lap[1], 1)
+            p_out = 3 / 5 * (1 - a.b_alpha) * lap[2] / max(lap[3], 1)
+            # Laplace's law proper: total pressure c_s^2 (r + b) in the droplet's
+            # core (r < R/2) against the far field (r > R + 16)
+            rho = (rr.astype(np.float64) + br).reshape(n, n)
+            jj, ii = np.mgrid[0:n, 0:n]
+            dist = np.hypot(ii - (n - 1) / 2, jj - (n - 1) / 2)
+            cs2 = 3 / 5 * (1 - a.r_alpha)
+            dp = cs2 * (rho[dist < R / 2].mean() - rho[dist > R + 16].mean())
+            results[st].append({"R": float(R), "dp": float(dp), "sigma_measured": float(R * dp),
+                                "dp_reference_threshold": p_in - p_out, "max_u": float(lap[4]),
+                                "status": "ok" if rc == 0 else "diverged"})
     sigma_pred = mp.predicted_surface_tension(mp.CgArguments(A=0.005, r_viscosity=1 / 6, b_viscosity=1 / 6))
-    inv_r = np.array([1 / r["R"] for r in results])
-    dp = np.array([r["dp"] for r in results])
-    slope = float(np.polyfit(inv_r, dp, 1)[0]) if len(results) > 1 else float(dp[0] / inv_r[0])
+    laplace = {}
+    for st in stores:
+        inv_r = np.array([1 / r["R"] for r in results[st]])
+        dp = np.array([r["dp"] for r in results[st]])
+        slope = float(np.polyfit(inv_r, dp, 1)[0]) if len(dp) > 1 else float(dp[0] / inv_r[0])
+        laplace[st] = {"droplets": results[st], "sigma_from_slope": slope}
+    laplace["sigma_predicted"] = sigma_pred
+    vs_f64 = None
+    if "f64" in stores:
+        vs_f64 = {}
+        for st in stores:
+            if st == "f64":
+                continue
+            vs_f64[st] = [{"R": a["R"], "dp_rel": abs(a["dp"] - b["dp"]) / abs(b["dp"]),
+                           "max_u_rel": abs(a["max_u"] - b["max_u"]) / max(b["max_u"], 1e-300)}
+                          for a, b in zip(results[st], results["f64"])]
     cpu = None
     if not args.no_cpu_baseline:
         from oracle import pyoracle
@@ -550,17 +662,28 @@ def run_cg(args):
         cpu = {"value": nc * nc * steps / dt / 1e9, "unit": "GLUPS", "cores": L.orc_threads(), "kind": "port",
                "sample": "oracle restatement of the reference's colour-gradient kernels (FP32, OpenMP) on a "
                          "%dx%d droplet, %d steps, %.1f s" % (nc, nc, steps, dt)}
+    head = stores[0]
+    ms = speed[head]["ms_per_step"]
+    # algorithmic bytes per update: both populations per direction read once
+    # and written once, plus the per-node colour field written (FP32 arithmetic
+    # types; FP64 for F64 storage)
+    blu = {"f32": 2 * 9 * 4 * 2 + 8, "f16s": 2 * 9 * 2 * 2 + 8, "f64": 2 * 9 * 8 * 2 + 16}
+    peak = measured_peak()[0]
     line = {"metric": "GLUPS (node updates/s / 1e9), D2Q9 colour-gradient static droplet %dx%d periodic" % (n, n),
-            "value": value, "unit": "GLUPS", "n_gpus": 1, "steps": args.cg_steps, "warmup": args.warmup,
-            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "value": speed[head]["glups"], "unit": "GLUPS", "n_gpus": 1, "steps": args.cg_steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 arithmetic, %s storage" % head,
             "data": "synthetic (seeded droplet radii)",
             "config": {"workload": "colour-gradient droplets, %dx%d periodic, R uniform in [64,256], A 0.005, "
-                                   "beta 0.7, tau 1 both phases, alpha 4/9, FP32 storage" % (n, n),
-                       "l2_policy": "inputs larger than L2 (2 x 75 MB populations + densities)"},
-            "laplace": {"droplets": results, "sigma_from_slope": slope, "sigma_predicted": sigma_pred},
-            "roofline": {"bound": "hbm", "algorithmic_bytes_per_update": 152,
-                         "achieved": 152 * n * n / (ms / 1e3) / 1e9 if ms else None, "unit": "GB/s",
-                         "peak": measured_peak()[0], "frac": (152 * n * n / (ms / 1e3) / 1e9) / measured_peak()[0]},
+                                   "beta 0.7, tau 1 both phases, alpha 4/9, %s storage (value), %s compared"
+                                   % (n, n, head, ",".join(stores)),
+                       "l2_policy": "inputs larger than L2 (populations of 2 x %.0f MB)" % (n * n * blu[head] / 2e6)},
+            "per_storage": {st: dict(speed[st], roofline_frac=blu[st] * n * n / (speed[st]["ms_per_step"] / 1e3)
+                                     / 1e9 / peak, bytes_per_update=blu[st]) for st in stores},
+            "laplace": laplace, "error_vs_f64": vs_f64,
+            "roofline": {"bound": "hbm", "algorithmic_bytes_per_update": blu[head],
+                         "achieved": blu[head] * n * n / (ms / 1e3) / 1e9, "unit": "GB/s",
+                         "peak": peak, "frac": (blu[head] * n * n / (ms / 1e3) / 1e9) / peak},
             "clocks": clk, "gpu_launches": 2 * args.cg_steps, "cpu_baseline": cpu}
     print(json.dumps(line))
     return 0

@@ -36,11 +36,18 @@ extern "C" {
 #define LBM_ERR_CUDA 5
 #define LBM_ERR_NOMEM 6
 
-/* Population storage in HBM.  Arithmetic is FP32 for F32 and F16S, FP64 for
- * F64.  F16S stores (f_i - w_i) * scale as IEEE half. */
+/* Population storage in HBM.  Arithmetic is FP32 for F32, F16S and F16C,
+ * FP64 for F64.  F16S stores (f_i - w_i) * scale as IEEE half.  F16C stores
+ * the same scaled deviation in a 16-bit float with 4 exponent and 11
+ * mantissa bits (one significand bit more than IEEE half; the "FP16C" format
+ * of Lehmann et al., Phys. Rev. E 106, 015308 (2022)): normal range
+ * [2^-14, 2), subnormal step 2^-25, so |f_i - w_i| * scale must stay below 2
+ * (scale defaults to 512 for F16C; values beyond saturate); physics mode and
+ * the run-time specialised storage-unit kernels only. */
 #define LBM_STORE_F32 0
 #define LBM_STORE_F16S 1
 #define LBM_STORE_F64 2
+#define LBM_STORE_F16C 3
 
 /* Semantics.  REFERENCE reproduces the reference loop including its quirks
  * (zero initial populations, post-stream wall copies, the lid Zou-He with
@@ -430,7 +437,13 @@ typedef struct lbm_cg_params {
     double control_param;            /* |phi| threshold of the Laplace-law sums */
     int high_order;                  /* 1: 24-point gradient stencil */
     int enhanced;                    /* 1: enhanced equilibrium (GpuCollision.cu:630-707) */
-    int storage;                     /* LBM_STORE_F32 */
+    int storage;                     /* LBM_STORE_F32; LBM_STORE_F16S: per direction the
+                                        summed population r+b as the FP16 of
+                                        (r + b - w_d) * 1024 and the colour
+                                        difference r - b as FP16, FP32
+                                        arithmetic; LBM_STORE_F64: FP64 storage
+                                        and arithmetic (the reference run for
+                                        storage-precision checks) */
 } lbm_cg_params;
 
 /* n x m periodic lattice, n, m >= 5. */

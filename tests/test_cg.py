@@ -229,3 +229,89 @@ def test_reference_cpu_colour_gradient_loop():
     assert abs(r[0].sum() - r0[0].sum()) < 1e-5 * r0[0].sum()
     assert abs(r[1].sum() - r0[1].sum()) < 1e-5 * r0[1].sum()
     assert r0[0].sum() > 0 and r0[1].sum() > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ho,enh", [(0, 0), (1, 1)])
+def test_cg_gpu_f64_storage_matches_fp64_oracle(ho, enh):
+    """F64 storage runs the colour-gradient step in FP64: after 40 steps it
+    matches the FP64 oracle to the FP32 rounding of the read-back (the
+    populations and fields come back as FP32), far inside what FP32
+    arithmetic reaches (the F32 test's 2e-5)."""
+    from thesis_gb300 import native as N
+    n, m, steps = 48, 40, 40
+    a, p, r0, b0 = _gpu_case(n, m, ho, enh)
+    a.storage = N.STORE_F64
+    orc = po.run_oracle_cg(n, m, p, r0, b0, steps, fp64=True, extra_collide=True)
+    assert orc.rc == 0
+    with mp.CgSolver(n, m, a) as s:
+        s.init(r0, b0)
+        s.step(steps, write_macro=True)
+        rf, bf = s.populations()
+        rr, br, u, v = s.macro()
+    tol = 1e-7
+    assert np.abs(rf - orc.rfc).max() < tol
+    assert np.abs(bf - orc.bfc).max() < tol
+    assert np.abs(rr - orc.rr).max() < 4 * tol
+    assert np.abs(u - orc.u).max() < tol
+    assert np.abs(v - orc.v).max() < tol
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ho,enh", [(0, 0), (1, 1)])
+def test_cg_gpu_f16s_storage_close_to_oracle(ho, enh):
+    """F16S storage (summed population as a shifted FP16 deviation, the
+    minority colour's fraction in FP16) against the FP64 oracle after 40
+    steps of the perturbed bubble: populations and colour densities within
+    the storage rounding, velocity within a few percent of its range."""
+    from thesis_gb300 import native as N
+    n, m, steps = 48, 40, 40
+    a, p, r0, b0 = _gpu_case(n, m, ho, enh)
+    a.storage = N.STORE_F16S
+    orc = po.run_oracle_cg(n, m, p, r0, b0, steps, fp64=True, extra_collide=True)
+    assert orc.rc == 0
+    with mp.CgSolver(n, m, a) as s:
+        s.init(r0, b0)
+        s.step(steps, write_macro=True)
+        rf, bf = s.populations()
+        rr, br, u, v = s.macro()
+        lap, rc = s.laplace()
+    assert rc == 0
+    ef = max(np.abs(rf - orc.rfc).max(), np.abs(bf - orc.bfc).max())
+    ed = max(np.abs(rr - orc.rr).max(), np.abs(br - orc.br).max())
+    vel = np.sqrt(((u - orc.u) ** 2 + (v - orc.v) ** 2).sum() / (orc.u ** 2 + orc.v ** 2).sum())
+    print("F16S colour gradient vs FP64 oracle: populations %.2e, colour densities %.2e, velocity rel L2 %.2e"
+          % (ef, ed, vel))
+    assert ef < 2e-3
+    assert ed < 5e-3
+    assert vel < 5e-2
+    # a pure phase stays pure: nodes that are all red in the oracle carry no blue
+    pure = orc.br == 0
+    assert np.abs(br[pure]).max() == 0.0
+
+
+@pytest.mark.gpu
+def test_cg_gpu_storage_laplace_against_f64():
+    """A 192^2 droplet (R = 40) relaxes for 3000 steps with F32, F16S and F64
+    storage; the core-to-far-field pressure jump and the peak spurious
+    current of F32 and F16S are stated against F64."""
+    from thesis_gb300 import native as N
+    n, R = 192, 40.0
+    out = {}
+    for st in (N.STORE_F64, N.STORE_F32, N.STORE_F16S):
+        a = mp.CgArguments(bubble_radius=R / (n - 1), A=0.005, beta=0.7, control_param=0.9, storage=st)
+        r0, b0 = mp.create_bubble(n, n, a)
+        with mp.CgSolver(n, n, a) as s:
+            s.init(r0, b0)
+            s.step(3000, write_macro=True)
+            rr, br, _, _ = s.macro()
+            lap, rc = s.laplace()
+        assert rc == 0
+        out[st] = (_core_far_jump((rr.astype(np.float64) + br).reshape(n, n), n, R, 3 / 5 * (1 - a.r_alpha)),
+                   lap[4])
+    dp64, u64 = out[N.STORE_F64]
+    errs = {k: (abs(out[k][0] - dp64) / dp64, abs(out[k][1] - u64) / u64) for k in (N.STORE_F32, N.STORE_F16S)}
+    print("droplet R=40, 3000 steps: dp F64 %.4e, max|u| F64 %.3e; F32 dp %.2e u %.2e; F16S dp %.2e u %.2e"
+          % (dp64, u64, *errs[N.STORE_F32], *errs[N.STORE_F16S]))
+    assert errs[N.STORE_F32][0] < 1e-3 and errs[N.STORE_F32][1] < 5e-2
+    assert errs[N.STORE_F16S][0] < 2e-2 and errs[N.STORE_F16S][1] < 0.5

@@ -63,7 +63,7 @@ def compare(g, r, fluid, storage, dims):
         a, b = g[k][fluid], getattr(r, k)[fluid]
         errs[k] = float(np.abs(a - b).max())
     errs["f"] = float(np.abs(g["f"][:, fluid] - r.fc[:, fluid]).max())
-    if storage == N.STORE_F16S:
+    if storage in (N.STORE_F16S, N.STORE_F16C):
         vel = ["u", "v"] + (["w"] if dims == 3 else [])
         du = np.sqrt(sum(((g[k] - getattr(r, k))[fluid] ** 2).sum() for k in vel))
         uu = np.sqrt(sum((getattr(r, k)[fluid] ** 2).sum() for k in vel))

@@ -42,19 +42,23 @@ def test_storage_velocity_error_against_fp64(case):
         base = dict(viscosity=(0.8 - 0.5) / 3, collision_model=N.MRT, mode=N.MODE_PHYSICS, init_equilibrium=1,
                     inlet_profile=N.INLET_PRESSURE, outlet_profile=N.OUTLET_PRESSURE, rho_in=1.005, rho_out=1.0)
         steps = 4000
-        bounds = (3e-3, 4e-2)
+        bounds = (3e-3, 4e-2, 4e-2)
     else:
         lat = lattice.cavity2d(128)
         base = dict(u=0.1, viscosity=0.128, collision_model=N.MRT, mode=N.MODE_PHYSICS, init_equilibrium=1,
                     outlet_profile=N.OUTLET_ZOUHE)
         steps = 20000
-        bounds = (1e-5, 5e-3)
+        bounds = (1e-5, 5e-3, 5e-3)
     fl = lat.node_type == 1
     ref = _run(lat, Arguments(storage=N.STORE_F64, **base), steps)
     errs = {}
-    for name, st in (("F32", N.STORE_F32), ("F16S", N.STORE_F16S)):
-        errs[name] = _rel(_run(lat, Arguments(storage=st, **base), steps), ref, fl)
-    print("%s: relative L2 velocity error vs F64 storage after %d steps: F32 %.2e, F16S %.2e"
-          % (case, steps, errs["F32"], errs["F16S"]))
+    # F16C holds |f - w| * scale below 2: scale 512 for the slow duct, 32 for
+    # the cavity whose lid drives |f - w| to ~0.04
+    c16 = 512.0 if case == "duct" else 32.0
+    for name, st, sc in (("F32", N.STORE_F32, 0.0), ("F16S", N.STORE_F16S, 0.0), ("F16C", N.STORE_F16C, c16)):
+        errs[name] = _rel(_run(lat, Arguments(storage=st, f16_scale=sc, **base), steps), ref, fl)
+    print("%s: relative L2 velocity error vs F64 storage after %d steps: F32 %.2e, F16S %.2e, F16C %.2e"
+          % (case, steps, errs["F32"], errs["F16S"], errs["F16C"]))
     assert errs["F32"] < bounds[0]
     assert errs["F16S"] < bounds[1]
+    assert errs["F16C"] < bounds[2]

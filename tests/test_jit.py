@@ -30,6 +30,9 @@ from thesis_gb300.solver import Arguments, Solver
     (19, N.MRT, N.STORE_F16S, 1, 0, (256, 256, 512), (128, 2 | (4 << 2), 10 << 2)),
     (19, N.BGKW, N.STORE_F32, 0, 1, (20, 16, 21), (128, 2 | (8 << 2), 0)),
     (9, N.TRT, N.STORE_F32, 1, 1, (160, 48, 1), (128, 2, 1)),
+    # F16C storage, storage-unit kernels
+    (19, N.MRT, N.STORE_F16C, 1, 0, (256, 256, 512), (64, 2 | (8 << 2), 20 << 2)),
+    (9, N.MRT, N.STORE_F16C, 1, 1, (160, 48, 1), (128, 2, 0)),
 ])
 def test_jit_sources_compile(native_lib, q, coll, storage, phys, wrap, dims, knobs):
     rc = native_lib.lbm_jit_check(q, coll, storage, phys, wrap, *dims, *knobs)
@@ -57,7 +60,7 @@ def _check(oracle, lat, args, steps, init, dims, storage):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("coll", [N.BGKW, N.TRT, N.MRT])
-@pytest.mark.parametrize("storage", [N.STORE_F32, N.STORE_F16S, N.STORE_F64])
+@pytest.mark.parametrize("storage", [N.STORE_F32, N.STORE_F16S, N.STORE_F64, N.STORE_F16C])
 def test_jit_sphere_duct(oracle, jit, coll, storage):
     lat = lattice.sphere_duct(24, 20, 48, porosity=0.75, rmin=3, rmax=5, seed=7)
     args = Arguments(viscosity=(0.8 - 0.5) / 3, collision_model=coll, mode=N.MODE_PHYSICS, storage=storage,
@@ -208,3 +211,43 @@ def test_fp32_cavity_reaches_1e6_residual(monkeypatch):
             if r < 1e-6 and len(res) > 2:
                 break
         assert res[-1] < 1e-6, res[-5:]
+
+
+def _f16c_round_trip(x):
+    """The F16C storage format restated in numpy: FP32 input rounded to 12
+    significant bits (nearest even), exponent range [2^-14, 2) with subnormal
+    steps of 2^-25 below, saturation at the largest value."""
+    x = np.asarray(x, np.float32).astype(np.float64)
+    a = np.abs(x)
+    _, e = np.frexp(a)  # a = m 2^e, 1/2 <= m < 1: leading bit 2^(e-1)
+    e = np.maximum(e.astype(np.float64) - 1.0, -14.0)
+    step = 2.0 ** (e - 11)
+    q = np.round(a / step) * step  # numpy rounds halves to even
+    q = np.minimum(q, 2.0 - 2.0 ** -11)
+    return np.sign(x) * q
+
+
+@pytest.mark.gpu
+def test_f16c_storage_round_trip(native_lib):
+    """Populations written with F16C storage (lbm_set_populations) read back
+    (lbm_get_populations) exactly as the format defines: w + q((f - w) S)/S
+    with q the 1-4-11 rounding of the FP32 value."""
+    lat = lattice.sphere_duct(16, 12, 20, porosity=0.8, rmin=3, rmax=4, seed=2)
+    args = Arguments(viscosity=0.1, collision_model=N.BGKW, mode=N.MODE_PHYSICS, storage=N.STORE_F16C,
+                     init_equilibrium=1, inlet_profile=N.INLET_PRESSURE, outlet_profile=N.OUTLET_PRESSURE,
+                     rho_in=1.005, rho_out=1.0)
+    nn = lat.num_nodes
+    w = lattice.W3[:, None]
+    rng = np.random.default_rng(4)
+    # deviations spanning the subnormal range, the normal range and saturation
+    dev = rng.choice([-1, 1], size=(19, nn)) * 10.0 ** rng.uniform(-12, -2.6, size=(19, nn))
+    dev[0, :8] = [0.0, 3e-3, -3e-3, 2.0 ** -24, 2.0 ** -23 * 1.5, 1e-9, -1e-9, 0.0039]
+    f = w + dev
+    with Solver(lat, args) as s:
+        s.set_populations(f)
+        g = s.populations()
+    S = 512.0
+    w32 = w.astype(np.float32).astype(np.float64)  # the shift as the kernels hold it
+    want = w32 + _f16c_round_trip((f - w32) * S) / S
+    fl = lat.node_type == 1
+    np.testing.assert_array_equal(g[:, fl], want[:, fl])

@@ -160,7 +160,7 @@ static StepParams make_params(const lbm_handle_s *H, int from, int write_macro) 
     // populations stored as deviations from the rest state: F16S always, F32
     // in physics mode (moments then come from small numbers, without the
     // cancellation that limits an FP32 steady state to a ~1e-6 residual)
-    const bool shifted = H->P.storage == LBM_STORE_F16S ||
+    const bool shifted = H->P.storage == LBM_STORE_F16S || H->P.storage == LBM_STORE_F16C ||
                          (H->P.storage == LBM_STORE_F32 && H->P.mode == LBM_MODE_PHYSICS);
     for (int d = 0; d < H->q; ++d) p.shift[d] = shifted ? (float)rest_shift(H->q, H->P.collision_model, d) : 0.0f;
     p.sigma = shifted ? 1.f : 0.f;
@@ -380,8 +380,10 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
         return fail(LBM_ERR_INVALID, "missing BC columns");
     if (P->collision_model < LBM_BGKW || P->collision_model > LBM_MRT)
         return fail(LBM_ERR_INVALID, "unknown collision model");
-    if (P->storage < LBM_STORE_F32 || P->storage > LBM_STORE_F64)
+    if (P->storage < LBM_STORE_F32 || P->storage > LBM_STORE_F16C)
         return fail(LBM_ERR_INVALID, "unknown storage");
+    if (P->storage == LBM_STORE_F16C && P->mode != LBM_MODE_PHYSICS)
+        return fail(LBM_ERR_UNSUPPORTED, "F16C storage runs in physics mode");
     if (P->mode != LBM_MODE_REFERENCE && P->mode != LBM_MODE_PHYSICS)
         return fail(LBM_ERR_INVALID, "unknown mode");
     if (!(P->viscosity > 0)) return fail(LBM_ERR_INVALID, "viscosity must be positive");
@@ -406,8 +408,8 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     H->N = N;
     H->stride = (N + 63) / 64 * 64;
     H->P = *P;
-    H->elem = P->storage == LBM_STORE_F32 ? 4 : (P->storage == LBM_STORE_F16S ? 2 : 8);
-    H->scale = P->f16_scale > 0 ? (float)P->f16_scale : 1024.0f;
+    H->elem = P->storage == LBM_STORE_F32 ? 4 : (P->storage == LBM_STORE_F64 ? 8 : 2);
+    H->scale = P->f16_scale > 0 ? (float)P->f16_scale : (P->storage == LBM_STORE_F16C ? 512.0f : 1024.0f);
     // omega as the reference computes it (GpuInit.cu:102-103)
     H->omega = 1.0 / (3.0 * P->viscosity + 0.5);
     H->omega_m = 8.0 * (2.0 - H->omega) / (8.0 - H->omega);
@@ -425,7 +427,8 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
         // tma|jit selects a variant explicitly (jit then fails loudly).
         const char *kv = getenv("THESIS_LBM_KERNEL");
         // the two-node kernels have no curved-wall or extrapolation-outlet path
-        const bool can_pair = (L->n % 2 == 0) && P->storage != LBM_STORE_F64 && !one_node_boundaries(*P, q);
+        const bool can_pair = (L->n % 2 == 0) && (P->storage == LBM_STORE_F32 || P->storage == LBM_STORE_F16S) &&
+                              !one_node_boundaries(*P, q);
         H->pair_kernel = kv && strcmp(kv, "pair") == 0 && can_pair;
         want_tma = kv && strcmp(kv, "tma") == 0;
         // jithz<k>[b<block>][m<min blocks>]: storage units walking k nodes along z
@@ -1043,7 +1046,8 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
     struct V {
         int block, hint, pred, pair, minb, hs, zw;
     };
-    const bool fspace_ok = !(H->P.mode == LBM_MODE_PHYSICS && H->P.storage == LBM_STORE_F32);
+    const bool fspace_ok = !(H->P.mode == LBM_MODE_PHYSICS &&
+                             (H->P.storage == LBM_STORE_F32 || H->P.storage == LBM_STORE_F16C));
     const bool hs_ok = H->P.storage != LBM_STORE_F64;
     std::vector<V> vs;
     if (fspace_ok) {

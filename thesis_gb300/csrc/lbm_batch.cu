@@ -34,18 +34,52 @@ int launch_decode_q19(const StepParams &p, int st, double *out, long long n, cud
 
 namespace {
 
-// tile: x = domain, y = row (y + ny z), z = first x, w = first node index of
-// the tile in the domain's macroscopic arrays (for the residual pass)
+// A tile is one warp's work: 32 consecutive nodes of BATCH_ROWS consecutive
+// rows of one domain.  int4: x = domain, y = first row (y + ny z), z = first
+// x, w = node index of (first x, first row) in the batch's macroscopic arrays.
+constexpr int BATCH_WARPS = STEP_BLOCK / 32;
+constexpr int BATCH_ROWS = 4;
+constexpr int PARAM_WORDS = (int)(sizeof(StepParams) / 4);
+static_assert(sizeof(StepParams) % 4 == 0, "StepParams is copied as 32-bit words");
+
+// The warp's copy of its domain's step parameters, refreshed when the warp
+// moves to a tile of another domain (tiles of a domain are contiguous).
+__device__ __forceinline__ void batch_load_params(StepParams *dst, const StepParams *src) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t *s = (const uint32_t *)src;
+    uint32_t *d = (uint32_t *)dst;
+    for (int k = lane; k < PARAM_WORDS; k += 32) d[k] = __ldg(s + k);
+    __syncwarp();
+}
+
 template <int Q, int COLL, int ST, bool PHYS>
 __global__ void __launch_bounds__(STEP_BLOCK)
 batch_step_kernel(const StepParams *__restrict__ tab, const int4 *__restrict__ tiles, const int *__restrict__ count) {
+    __shared__ StepParams sp[BATCH_WARPS];
     const int ntiles = *count;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    StepParams &p = sp[warp];
+    int cur = -1;
+    for (int t = blockIdx.x * BATCH_WARPS + warp; t < ntiles; t += gridDim.x * BATCH_WARPS) {
         const int4 tl = tiles[t];
-        const StepParams &p = tab[tl.x];
+        if (tl.x != cur) {
+            __syncwarp();
+            batch_load_params(&p, tab + tl.x);
+            cur = tl.x;
+        }
         const DynGeom g{p.nx, p.ny, p.nz, p.pitch};
-        h_node<Q, COLL, ST, PHYS, true, DynGeom, false, false>(p, g, tl.z + (int)threadIdx.x, tl.y % p.ny,
-                                                               tl.y / p.ny);
+        const int x = tl.z + lane;
+        const int rows = g.ny * g.nz;
+        const int r_end = min(tl.y + BATCH_ROWS, rows);
+        const bool in_row = x < g.nx;
+        // the next row's flag word is requested before the current row's update
+        uint32_t w = in_row ? __ldg(p.word + x + g.nx * tl.y) : 0u;
+#pragma unroll 1
+        for (int r = tl.y; r < r_end; ++r) {
+            const uint32_t wn = in_row && r + 1 < r_end ? __ldg(p.word + x + g.nx * (r + 1)) : 0u;
+            h_node_w<Q, COLL, ST, PHYS, true, DynGeom, false, false>(p, g, x, r % g.ny, r / g.ny, w);
+            w = wn;
+        }
     }
 }
 
@@ -57,23 +91,27 @@ __global__ void __launch_bounds__(STEP_BLOCK)
 batch_residual_partial(const StepParams *__restrict__ tab, const int4 *__restrict__ tiles,
                        const int *__restrict__ count, float *pu, double2 *partial) {
     const int ntiles = *count;
-    __shared__ double2 sm[STEP_BLOCK / 32];
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int t = blockIdx.x * BATCH_WARPS + warp; t < ntiles; t += gridDim.x * BATCH_WARPS) {
         const int4 tl = tiles[t];
         const StepParams &p = tab[tl.x];
-        const int x = tl.z + (int)threadIdx.x;
+        const int nx = p.nx, rows = p.ny * p.nz;
+        const int x = tl.z + lane;
+        const int r_end = min(tl.y + BATCH_ROWS, rows);
         double a = 0, b = 0;
-        if (x < p.nx) {
-            const long long i = (long long)tl.w + threadIdx.x;  // node index in the shared macro arrays
-            const int local = tl.y * p.nx + x;
-            if (p.word[local] & W_FLUID) {
-                const double u = p.ux[local], v = p.uy[local], w = p.uz[local];
-                const double du = u - pu[3 * i], dv = v - pu[3 * i + 1], dw = w - pu[3 * i + 2];
-                a = du * du + dv * dv + dw * dw;
-                b = u * u + v * v + w * w;
-                pu[3 * i] = (float)u;
-                pu[3 * i + 1] = (float)v;
-                pu[3 * i + 2] = (float)w;
+        if (x < nx) {
+            for (int r = tl.y; r < r_end; ++r) {
+                const long long i = (long long)tl.w + (long long)(r - tl.y) * nx + lane;  // batch node index
+                const int local = r * nx + x;
+                if (p.word[local] & W_FLUID) {
+                    const double u = p.ux[local], v = p.uy[local], w = p.uz[local];
+                    const double du = u - pu[3 * i], dv = v - pu[3 * i + 1], dw = w - pu[3 * i + 2];
+                    a += du * du + dv * dv + dw * dw;
+                    b += u * u + v * v + w * w;
+                    pu[3 * i] = (float)u;
+                    pu[3 * i + 1] = (float)v;
+                    pu[3 * i + 2] = (float)w;
+                }
             }
         }
 #pragma unroll
@@ -81,17 +119,7 @@ batch_residual_partial(const StepParams *__restrict__ tab, const int4 *__restric
             a += __shfl_down_sync(0xffffffffu, a, o);
             b += __shfl_down_sync(0xffffffffu, b, o);
         }
-        if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = make_double2(a, b);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double2 s = make_double2(0, 0);
-            for (int k = 0; k < STEP_BLOCK / 32; ++k) {
-                s.x += sm[k].x;
-                s.y += sm[k].y;
-            }
-            partial[t] = s;
-        }
-        __syncthreads();
+        if (lane == 0) partial[t] = make_double2(a, b);
     }
 }
 
@@ -323,8 +351,9 @@ int lbm_batch_create(const lbm_lattice_desc *const *lattices, const lbm_params *
     for (int d = 0; d < count; ++d) {
         const int rows = B->m[d] * B->h[d];
         for (int r = 0; r < rows; ++r)
-            for (int x0 = 0; x0 < B->n[d]; x0 += STEP_BLOCK)
-                B->all_tiles.push_back(make_int4(d, r, x0, (int)(B->node_off[d] + (long long)r * B->n[d] + x0)));
+            if (r % BATCH_ROWS == 0)
+                for (int x0 = 0; x0 < B->n[d]; x0 += 32)
+                    B->all_tiles.push_back(make_int4(d, r, x0, (int)(B->node_off[d] + (long long)r * B->n[d] + x0)));
         B->dom_tile_begin.push_back((int)B->all_tiles.size());
     }
     if (B->total_nodes >= (1ll << 31)) {

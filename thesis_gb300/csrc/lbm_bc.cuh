@@ -426,4 +426,93 @@ __device__ __forceinline__ void bc_phys(R (&f)[Q], int face, bool pressure, R rh
     }
 }
 
+// ---------------------------------------------------------------------------
+// The physics-mode faces and moving walls in storage units: h = (f - sigma r) S
+// with r the model's rest state (isotropic: r_d = r_opp(d), sum 1) and S the
+// storage scale.  The same closures as zou_he_face and bc_moving_wall, with
+// the O(1) sums that cancel to the normal velocity or the density replaced by
+// identities of the shift: sum_{c.e=0} r + 2 sum_{c.e=-1} r = 1, r_d = r_opp(d)
+// and sum_{c.e=0} (c.t) r_c = 0.  So with K = (sum_{c.e=0} h + 2 sum_{c.e=-1}
+// h)/S the pressure face gives u_e = ((rho - sigma) - K)/rho and the velocity
+// face rho = (sigma + K)/(1 - u_e), from deviations only: an FP32 face then
+// keeps the digits that the f-space form loses to the cancellation (relative
+// 1e-4 of a 1e-3 velocity per step).  rho_dev = rho_set - sigma, formed in FP64
+// on the host.
+// ---------------------------------------------------------------------------
+template <int Q, int FACE>
+__device__ __forceinline__ void zou_he_face_h(float (&h)[Q], bool pressure, float rho_dev, float sigma, float S,
+                                              float invS, float ux, float uy, float uz) {
+    using L = Lat<Q>;
+    constexpr int ex = FACE == 0 ? 1 : (FACE == 1 ? -1 : 0);
+    constexpr int ey = FACE == 2 ? 1 : (FACE == 3 ? -1 : 0);
+    constexpr int ez = FACE == 4 ? 1 : (FACE == 5 ? -1 : 0);
+    float h0 = 0.f, hm = 0.f;
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+        const int ce = L::cx(d) * ex + L::cy(d) * ey + L::cz(d) * ez;
+        if (ce == 0) h0 += h[d];
+        if (ce == -1) hm += h[d];
+    }
+    const float K = (h0 + 2.f * hm) * invS;
+    float rho, ue;
+    if (pressure) {
+        rho = rho_dev + sigma;
+        ue = (rho_dev - K) / rho;
+        ux = ue * (float)ex;
+        uy = ue * (float)ey;
+        uz = ue * (float)ez;
+    } else {
+        ue = ux * (float)ex + uy * (float)ey + uz * (float)ez;
+        rho = (sigma + K) / (1.f - ue);
+    }
+    const float rS = rho * S;
+#pragma unroll
+    for (int d = 1; d < Q; ++d) {
+        const int ce = L::cx(d) * ex + L::cy(d) * ey + L::cz(d) * ez;
+        if (ce != 1) continue;
+        const int tx = L::cx(d) - ex, ty = L::cy(d) - ey, tz = L::cz(d) - ez;
+        const int o = L::opp(d);
+        if (tx == 0 && ty == 0 && tz == 0) {
+            h[d] = fmaf((float)(6.0 * L::w(d)) * rS, ue, h[o]);
+        } else {
+            float st = 0.f;
+#pragma unroll
+            for (int c = 0; c < Q; ++c) {
+                const int cce = L::cx(c) * ex + L::cy(c) * ey + L::cz(c) * ez;
+                const int ct = L::cx(c) * tx + L::cy(c) * ty + L::cz(c) * tz;
+                if (cce == 0 && ct != 0) st += (float)ct * h[c];
+            }
+            const float ut = ux * (float)tx + uy * (float)ty + uz * (float)tz;
+            h[d] = h[o] + rS * (ue * (1.f / 6.f) + ut * 0.5f) - 0.5f * st;
+        }
+    }
+}
+
+template <int Q>
+__device__ __forceinline__ void bc_phys_h(float (&h)[Q], int face, bool pressure, float rho_dev, float sigma, float S,
+                                          float invS, float ux, float uy, float uz) {
+    switch (face) {
+    case 0: zou_he_face_h<Q, 0>(h, pressure, rho_dev, sigma, S, invS, ux, uy, uz); break;
+    case 1: zou_he_face_h<Q, 1>(h, pressure, rho_dev, sigma, S, invS, ux, uy, uz); break;
+    case 2: zou_he_face_h<Q, 2>(h, pressure, rho_dev, sigma, S, invS, ux, uy, uz); break;
+    case 3: zou_he_face_h<Q, 3>(h, pressure, rho_dev, sigma, S, invS, ux, uy, uz); break;
+    case 4: if (Q == 19) zou_he_face_h<Q, 4>(h, pressure, rho_dev, sigma, S, invS, ux, uy, uz); break;
+    case 5: if (Q == 19) zou_he_face_h<Q, 5>(h, pressure, rho_dev, sigma, S, invS, ux, uy, uz); break;
+    default: break;
+    }
+}
+
+// Moving wall in storage units: h_d gains S 6 w_d rho_0 (c_d . u_w).
+template <int Q>
+__device__ __forceinline__ void bc_moving_wall_h(float (&h)[Q], unsigned long long links, float rho, float S,
+                                                 float uwx, float uwy, float uwz) {
+    using L = Lat<Q>;
+#pragma unroll
+    for (int d = 1; d < Q; ++d)
+        if ((links >> d) & 1ull) {
+            const float cu = (float)L::cx(d) * uwx + (float)L::cy(d) * uwy + (float)L::cz(d) * uwz;
+            h[d] += (float)(6.0 * L::w(d)) * rho * S * cu;
+        }
+}
+
 }  // namespace lbm

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "lbm_cg3.cuh"
+#include "lbm_cg_store.cuh"
 #include "lbm_device.cuh"
 #include "thesis_lbm.h"
 
@@ -31,83 +32,105 @@ namespace lbm {
 namespace {
 
 struct CgArgs {
-    const float *rin[9], *bin[9];
-    float *rout[9], *bout[9];
+    const void *in;          // slot c of direction d at (c*9 + d)*N (lbm_cg_store.cuh)
+    void *out;
     float *R, *B;            // colour densities (output)
-    float *phi, *dn;         // colour field and density of the streamed state (gradients)
+    void *phi, *dn;          // colour field and density of the streamed state (gradients), arithmetic type
     float *rho, *ux, *uy;    // macroscopic output (when write_macro)
     int nx, ny;
+    long long N;
     int write_macro;
-    float r_alpha, b_alpha, r_visc, b_visc, beta, A, g_limit;
+    double r_alpha, b_alpha, r_visc, b_visc, beta, A, g_limit;
+    float scale, inv_scale;  // F16S: S and 1/S of the summed population
 };
 
 constexpr int CG_BLOCK = 128;
 __constant__ float c_phi[9] = {0.f, 0.2f, 0.2f, 0.2f, 0.2f, 0.05f, 0.05f, 0.05f, 0.05f};
 __constant__ float c_teta[9] = {1.f, -0.2f, -0.2f, -0.2f, -0.2f, -0.05f, -0.05f, -0.05f, -0.05f};
+__constant__ double c_phi_d[9] = {0., 0.2, 0.2, 0.2, 0.2, 0.05, 0.05, 0.05, 0.05};
+__constant__ double c_teta_d[9] = {1., -0.2, -0.2, -0.2, -0.2, -0.05, -0.05, -0.05, -0.05};
+
+template <class R> __device__ __forceinline__ R cg_rest_phi(int k) {
+    if constexpr (sizeof(R) == 8) return c_phi_d[k];
+    else return c_phi[k];
+}
+template <class R> __device__ __forceinline__ R cg_rest_teta(int k) {
+    if constexpr (sizeof(R) == 8) return c_teta_d[k];
+    else return c_teta[k];
+}
 
 __device__ __forceinline__ int wrapi(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
 // PULL: gather from the neighbours (a time step); otherwise read the node's
 // own populations (the first collision from a given post-stream state).
-template <bool PULL>
-__device__ __forceinline__ void cg_gather(const CgArgs &a, int x, int y, float (&r)[9], float (&b)[9]) {
+template <int ST, bool PULL>
+__device__ __forceinline__ void cg_gather(const CgArgs &a, int x, int y, typename CgStore<ST>::R (&r)[9],
+                                          typename CgStore<ST>::R (&b)[9]) {
     using L = Lat<9>;
+    using S = CgStore<ST>;
+    using T = typename S::T;
+    using R = typename S::R;
+    const T *in = (const T *)a.in;
 #pragma unroll
     for (int d = 0; d < 9; ++d) {
         const int sx = PULL ? wrapi(x - L::cx(d), a.nx) : x;
         const int sy = PULL ? wrapi(y - L::cy(d), a.ny) : y;
-        const int s = sx + a.nx * sy;
-        r[d] = __ldg(a.rin[d] + s);
-        b[d] = __ldg(a.bin[d] + s);
+        const long long s = sx + (long long)a.nx * sy;
+        S::load(in + d * a.N + s, in + (9 + d) * a.N + s, (R)L::w(d), (R)a.inv_scale, r[d], b[d]);
     }
 }
 
-template <bool PULL>
+template <int ST, bool PULL>
 __global__ void __launch_bounds__(CG_BLOCK) cg_density_kernel(const CgArgs a) {
+    using R = typename CgStore<ST>::R;
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
     if (x >= a.nx) return;
-    float r[9], b[9];
-    cg_gather<PULL>(a, x, y, r, b);
-    float rr = 0.f, bb = 0.f;
+    R r[9], b[9];
+    cg_gather<ST, PULL>(a, x, y, r, b);
+    R rr = 0, bb = 0;
 #pragma unroll
     for (int d = 0; d < 9; ++d) {
         rr += r[d];
         bb += b[d];
     }
     const int node = x + a.nx * y;
-    const float rho = rr + bb;
-    a.phi[node] = (rr - bb) / rho;
-    a.dn[node] = rho;
+    const R rho = rr + bb;
+    ((R *)a.phi)[node] = (rr - bb) / rho;
+    ((R *)a.dn)[node] = rho;
 }
 
-template <bool PULL, bool HO, bool ENH>
+template <int ST, bool PULL, bool HO, bool ENH>
 __global__ void __launch_bounds__(CG_BLOCK) cg_collide_kernel(const CgArgs a) {
     using L = Lat<9>;
+    using SP = CgStore<ST>;
+    using T = typename SP::T;
+    using R = typename SP::R;
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
     if (x >= a.nx) return;
     const int node = x + a.nx * y;
-    float r[9], b[9];
-    cg_gather<PULL>(a, x, y, r, b);
-    float f[9], r_r = 0.f, b_r = 0.f, jx = 0.f, jy = 0.f;
+    const R *phi = (const R *)a.phi, *dn = (const R *)a.dn;
+    R r[9], b[9];
+    cg_gather<ST, PULL>(a, x, y, r, b);
+    R f[9], r_r = 0, b_r = 0, jx = 0, jy = 0;
 #pragma unroll
     for (int d = 0; d < 9; ++d) {
         f[d] = r[d] + b[d];
         r_r += r[d];
         b_r += b[d];
-        if (L::cx(d)) jx += (float)L::cx(d) * f[d];
-        if (L::cy(d)) jy += (float)L::cy(d) * f[d];
+        if (L::cx(d)) jx += (R)L::cx(d) * f[d];
+        if (L::cy(d)) jy += (R)L::cy(d) * f[d];
     }
-    const float rho = r_r + b_r;
-    const float u = jx / rho, v = jy / rho;
-    a.R[node] = r_r;
-    a.B[node] = b_r;
+    const R rho = r_r + b_r;
+    const R u = jx / rho, v = jy / rho;
+    a.R[node] = (float)r_r;
+    a.B[node] = (float)b_r;
     if (a.write_macro) {
-        a.rho[node] = rho;
-        a.ux[node] = u;
-        a.uy[node] = v;
+        a.rho[node] = (float)rho;
+        a.ux[node] = (float)u;
+        a.uy[node] = (float)v;
     }
     // colour and density gradients from the neighbours (GpuCollision.cu:112-281)
-    float cgx = 0.f, cgy = 0.f, grx = 0.f, gry = 0.f;
+    R cgx = 0, cgy = 0, grx = 0, gry = 0;
     if (HO) {
         constexpr int hx[24] = {1, 0, -1, 0, 1, -1, -1, 1, 0, 1, 2, 2, 2, 2, 2, 1, 0, -1, -2, -2, -2, -2, -2, -1};
         constexpr int hy[24] = {0, 1, 0, -1, 1, 1, -1, -1, 2, 2, 2, 1, 0, -1, -2, -2, -2, -2, -2, -1, 0, 1, 2, 2};
@@ -116,64 +139,97 @@ __global__ void __launch_bounds__(CG_BLOCK) cg_collide_kernel(const CgArgs a) {
 #pragma unroll
         for (int k = 0; k < 24; ++k) {
             const int j = wrapi(x + hx[k], a.nx) + a.nx * wrapi(y + hy[k], a.ny);
-            const float w = (float)(hw[k] / 5040.0);
-            const float a1 = w * __ldg(a.phi + j), a2 = ENH ? w * __ldg(a.dn + j) : 0.f;
+            const R w = (R)(hw[k] / 5040.0);
+            const R a1 = w * __ldg(phi + j), a2 = ENH ? w * __ldg(dn + j) : (R)0;
             if (ENH) {
-                grx += a2 * (float)hx[k];
-                gry += a2 * (float)hy[k];
+                grx += a2 * (R)hx[k];
+                gry += a2 * (R)hy[k];
             }
-            cgx += a1 * (float)hx[k];
-            cgy += a1 * (float)hy[k];
+            cgx += a1 * (R)hx[k];
+            cgy += a1 * (R)hy[k];
         }
     } else {
 #pragma unroll
         for (int k = 1; k < 9; ++k) {
             const int j = wrapi(x + L::cx(k), a.nx) + a.nx * wrapi(y + L::cy(k), a.ny);
-            const float w = k <= 4 ? (float)(4.0 / 12.0) : (float)(1.0 / 12.0);
-            const float a1 = w * __ldg(a.phi + j), a2 = ENH ? w * __ldg(a.dn + j) : 0.f;
+            const R w = k <= 4 ? (R)(4.0 / 12.0) : (R)(1.0 / 12.0);
+            const R a1 = w * __ldg(phi + j), a2 = ENH ? w * __ldg(dn + j) : (R)0;
             if (ENH) {
-                grx += a2 * (float)L::cx(k);
-                gry += a2 * (float)L::cy(k);
+                grx += a2 * (R)L::cx(k);
+                gry += a2 * (R)L::cy(k);
             }
-            cgx += a1 * (float)L::cx(k);
-            cgy += a1 * (float)L::cy(k);
+            cgx += a1 * (R)L::cx(k);
+            cgy += a1 * (R)L::cy(k);
         }
     }
-    const float mean_nu = 1.f / (r_r / (rho * a.r_visc) + b_r / (rho * a.b_visc));
-    const float omega_eff = 1.f / (3.f * mean_nu + 0.5f);
-    const float mean_alpha = a.r_alpha * r_r / rho + a.b_alpha * b_r / rho;
-    const float gnorm = sqrtf(cgx * cgx + cgy * cgy);
-    const float k_r = r_r / rho, k_b = b_r / rho, k_k = a.beta * r_r * b_r / rho;
-    const float cu1 = u * u + v * v;
-    const float G1 = 2.f * u * grx, G2 = u * gry + v * grx, G4 = 2.f * v * gry;
-    const float ugr = u * grx + v * gry;
-    const bool interface = gnorm > a.g_limit;
+    const R r_visc = (R)a.r_visc, b_visc = (R)a.b_visc, beta = (R)a.beta, A = (R)a.A;
+    const R mean_nu = (R)1 / (r_r / (rho * r_visc) + b_r / (rho * b_visc));
+    const R omega_eff = (R)1 / ((R)3 * mean_nu + (R)0.5);
+    const R mean_alpha = (R)a.r_alpha * r_r / rho + (R)a.b_alpha * b_r / rho;
+    const R gnorm = sqrt(cgx * cgx + cgy * cgy);
+    const R k_r = r_r / rho, k_b = b_r / rho, k_k = beta * r_r * b_r / rho;
+    const R cu1 = u * u + v * v;
+    const R G1 = (R)2 * u * grx, G2 = u * gry + v * grx, G4 = (R)2 * v * gry;
+    const R ugr = u * grx + v * gry;
+    const bool interface = gnorm > (R)a.g_limit;
     // one reciprocal per node instead of two divisions per direction
-    const float inv_g = interface ? 1.f / gnorm : 0.f, inv_g2 = inv_g * inv_g;
+    const R inv_g = interface ? (R)1 / gnorm : (R)0, inv_g2 = inv_g * inv_g;
+    T *out = (T *)a.out;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-        const float cxk = (float)L::cx(k), cyk = (float)L::cy(k);
-        const float wk = k == 0 ? (float)(4. / 9.) : (k <= 4 ? (float)(1. / 9.) : (float)(1. / 36.));
-        float pert = 0.f, cosin = 0.f;
+        const R cxk = (R)L::cx(k), cyk = (R)L::cy(k);
+        const R wk = k == 0 ? (R)(4. / 9.) : (k <= 4 ? (R)(1. / 9.) : (R)(1. / 36.));
+        R pert = 0, cosin = 0;
         if (interface) {
-            const float pcg = cxk * cgx + cyk * cgy;
-            if (k != 0) cosin = pcg * inv_g * (k <= 4 ? 1.f : 0.70710678f);
-            const float bk = k == 0 ? (float)(-4. / 27.) : (k <= 4 ? (float)(2. / 27.) : (float)(5. / 108.));
-            pert = a.A * gnorm * (wk * (pcg * pcg) * inv_g2 - bk);
+            const R pcg = cxk * cgx + cyk * cgy;
+            if (k != 0) cosin = pcg * inv_g * (k <= 4 ? (R)1 : (R)0.70710678118654752);
+            const R bk = k == 0 ? (R)(-4. / 27.) : (k <= 4 ? (R)(2. / 27.) : (R)(5. / 108.));
+            pert = A * gnorm * (wk * (pcg * pcg) * inv_g2 - bk);
         }
-        const float cu2 = u * cxk + v * cyk;
-        const float rest = c_phi[k] + c_teta[k] * mean_alpha;
-        float feq = rho * (rest + wk * (3.f * cu2 + 4.5f * cu2 * cu2 - 1.5f * cu1));
+        const R cu2 = u * cxk + v * cyk;
+        const R rest = cg_rest_phi<R>(k) + cg_rest_teta<R>(k) * mean_alpha;
+        R feq = rho * (rest + wk * ((R)3 * cu2 + (R)4.5 * cu2 * cu2 - (R)1.5 * cu1));
         if (ENH) {
-            const float chi = k == 0 ? (float)(-8. / 3.) : (k <= 4 ? (float)(-1. / 6.) : (float)(1. / 12.));
-            const float psi = k == 0 ? 0.f : (k <= 4 ? 0.5f : 0.125f);
-            const float TC = G1 * (cxk * cxk) + 2.f * G2 * (cxk * cyk) + G4 * (cyk * cyk);
+            const R chi = k == 0 ? (R)(-8. / 3.) : (k <= 4 ? (R)(-1. / 6.) : (R)(1. / 12.));
+            const R psi = k == 0 ? (R)0 : (k <= 4 ? (R)0.5 : (R)0.125);
+            const R TC = G1 * (cxk * cxk) + (R)2 * G2 * (cxk * cyk) + G4 * (cyk * cyk);
             feq += mean_nu * (chi * ugr + psi * TC);
         }
-        const float fp = omega_eff * feq + (1.f - omega_eff) * f[k] + pert;
-        a.rout[k][node] = k_r * fp + k_k * cosin * rest;
-        a.bout[k][node] = k_b * fp - k_k * cosin * rest;
+        const R fp = omega_eff * feq + ((R)1 - omega_eff) * f[k] + pert;
+        SP::store(out + k * a.N + node, out + (9 + k) * a.N + node, (R)L::w(k), (R)a.scale,
+                  k_r * fp + k_k * cosin * rest, k_b * fp - k_k * cosin * rest);
     }
+}
+
+// Post-streaming red and blue populations (FP32, SoA) into storage slots.
+template <int ST>
+__global__ void cg_encode_kernel(const float *r, const float *b, void *out, int q, long long N, float scale) {
+    using SP = CgStore<ST>;
+    using T = typename SP::T;
+    using R = typename SP::R;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)q * N) return;
+    const int d = (int)(i / N);
+    const R w = q == 9 ? (R)Lat<9>::w(d) : (R)Lat<19>::w(d);
+    T *o = (T *)out;
+    SP::store(o + i, o + (long long)q * N + i, w, (R)scale, (R)r[i], (R)b[i]);
+}
+
+// Storage slots back to red and blue populations (FP32, SoA).
+template <int ST>
+__global__ void cg_decode_kernel(const void *in, float *r, float *b, int q, long long N, float inv_scale) {
+    using SP = CgStore<ST>;
+    using T = typename SP::T;
+    using R = typename SP::R;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)q * N) return;
+    const int d = (int)(i / N);
+    const R w = q == 9 ? (R)Lat<9>::w(d) : (R)Lat<19>::w(d);
+    const T *s = (const T *)in;
+    R rr, bb;
+    SP::load(s + i, s + (long long)q * N + i, w, (R)inv_scale, rr, bb);
+    r[i] = (float)rr;
+    b[i] = (float)bb;
 }
 
 // FP64 Laplace-law sums: sum rho_r and count where chi >= c, sum rho_b and
@@ -233,26 +289,23 @@ struct lbm_cg_handle_s {
     int n = 0, m = 0, h = 1, q = 9;  // D2Q9 (h = 1) or D3Q19
     long long N = 0;
     lbm_cg_params P{};
-    float *buf = nullptr;  // 2 buffers x 2 colours x q directions x N
+    int st = LBM_STORE_F32;          // population storage (lbm_cg_store.cuh)
+    void *buf = nullptr;             // 2 buffers x 2 slots x q directions x N values
     float *R = nullptr, *B = nullptr, *rho = nullptr, *ux = nullptr, *uy = nullptr, *uz = nullptr;
-    float *phi = nullptr, *dn = nullptr;  // D3Q19: colour field and density for the gradients
+    void *phi = nullptr, *dn = nullptr;  // colour field and density for the gradients (arithmetic type)
     double *partial = nullptr, *sums = nullptr;
     int cur = 0;
+    float scale = 1024.f;            // F16S: scale of the summed population's deviation
     cudaStream_t stream = nullptr;
     cudaEvent_t stepped = nullptr;  // after the last lbm_cg_step, on its stream
+    size_t slot_bytes() const { return (size_t)q * (size_t)N * cg_elem_bytes(st); }
+    void *buffer(int c) const { return (char *)buf + (size_t)c * 2 * slot_bytes(); }
 };
 
-static CgArgs cg_args(const lbm_cg_handle_s *H, int from, int write_macro) {
-    CgArgs a;
-    memset(&a, 0, sizeof(a));
-    const size_t N = (size_t)H->N;
-    float *src = H->buf + (size_t)from * 18 * N, *dst = H->buf + (size_t)(1 - from) * 18 * N;
-    for (int d = 0; d < 9; ++d) {
-        a.rin[d] = src + d * N;
-        a.bin[d] = src + (9 + d) * N;
-        a.rout[d] = dst + d * N;
-        a.bout[d] = dst + (9 + d) * N;
-    }
+template <class A>
+static void cg_fill_common(const lbm_cg_handle_s *H, int from, int write_macro, A &a) {
+    a.in = H->buffer(from);
+    a.out = H->buffer(1 - from);
     a.R = H->R;
     a.B = H->B;
     a.phi = H->phi;
@@ -262,70 +315,74 @@ static CgArgs cg_args(const lbm_cg_handle_s *H, int from, int write_macro) {
     a.uy = H->uy;
     a.nx = H->n;
     a.ny = H->m;
+    a.N = H->N;
     a.write_macro = write_macro;
-    a.r_alpha = (float)H->P.r_alpha;
-    a.b_alpha = (float)H->P.b_alpha;
-    a.r_visc = (float)H->P.r_viscosity;
-    a.b_visc = (float)H->P.b_viscosity;
-    a.beta = (float)H->P.beta;
-    a.A = (float)H->P.A;
-    a.g_limit = (float)H->P.g_limit;
+    a.r_alpha = H->P.r_alpha;
+    a.b_alpha = H->P.b_alpha;
+    a.r_visc = H->P.r_viscosity;
+    a.b_visc = H->P.b_viscosity;
+    a.beta = H->P.beta;
+    a.A = H->P.A;
+    a.g_limit = H->P.g_limit;
+    a.scale = H->scale;
+    a.inv_scale = 1.0f / H->scale;
+}
+
+static CgArgs cg_args(const lbm_cg_handle_s *H, int from, int write_macro) {
+    CgArgs a;
+    memset(&a, 0, sizeof(a));
+    cg_fill_common(H, from, write_macro, a);
     return a;
 }
 
 static Cg3Args cg3_args(const lbm_cg_handle_s *H, int from, int write_macro) {
     Cg3Args a;
     memset(&a, 0, sizeof(a));
-    const size_t N = (size_t)H->N;
-    a.in = H->buf + (size_t)from * 38 * N;
-    a.out = H->buf + (size_t)(1 - from) * 38 * N;
-    a.R = H->R;
-    a.B = H->B;
-    a.phi = H->phi;
-    a.dn = H->dn;
-    a.rho = H->rho;
-    a.ux = H->ux;
-    a.uy = H->uy;
+    cg_fill_common(H, from, write_macro, a);
     a.uz = H->uz;
-    a.nx = H->n;
-    a.ny = H->m;
     a.nz = H->h;
-    a.N = H->N;
-    a.write_macro = write_macro;
-    a.r_alpha = (float)H->P.r_alpha;
-    a.b_alpha = (float)H->P.b_alpha;
-    a.r_visc = (float)H->P.r_viscosity;
-    a.b_visc = (float)H->P.b_viscosity;
-    a.beta = (float)H->P.beta;
-    a.A = (float)H->P.A;
-    a.g_limit = (float)H->P.g_limit;
     return a;
 }
 
-template <bool PULL>
-static void cg3_launch(const lbm_cg_handle_s *H, int from, int write_macro, cudaStream_t s) {
+template <int ST, bool PULL>
+static void cg3_launch_st(const lbm_cg_handle_s *H, int from, int write_macro, cudaStream_t s) {
     const Cg3Args a = cg3_args(H, from, write_macro);
     const dim3 grid((unsigned)((H->n + CG3_BLOCK - 1) / CG3_BLOCK), (unsigned)H->m, (unsigned)H->h);
-    cg3_density_kernel<PULL><<<grid, CG3_BLOCK, 0, s>>>(a);
+    cg3_density_kernel<ST, PULL><<<grid, CG3_BLOCK, 0, s>>>(a);
     if (H->P.high_order) {
-        if (H->P.enhanced) cg3_collide_kernel<PULL, true, true><<<grid, CG3_BLOCK, 0, s>>>(a);
-        else cg3_collide_kernel<PULL, true, false><<<grid, CG3_BLOCK, 0, s>>>(a);
+        if (H->P.enhanced) cg3_collide_kernel<ST, PULL, true, true><<<grid, CG3_BLOCK, 0, s>>>(a);
+        else cg3_collide_kernel<ST, PULL, true, false><<<grid, CG3_BLOCK, 0, s>>>(a);
     } else {
-        if (H->P.enhanced) cg3_collide_kernel<PULL, false, true><<<grid, CG3_BLOCK, 0, s>>>(a);
-        else cg3_collide_kernel<PULL, false, false><<<grid, CG3_BLOCK, 0, s>>>(a);
+        if (H->P.enhanced) cg3_collide_kernel<ST, PULL, false, true><<<grid, CG3_BLOCK, 0, s>>>(a);
+        else cg3_collide_kernel<ST, PULL, false, false><<<grid, CG3_BLOCK, 0, s>>>(a);
     }
 }
 
-template <bool PULL>
-static void cg_launch(const lbm_cg_handle_s *H, const CgArgs &a, cudaStream_t s) {
+template <int ST, bool PULL>
+static void cg_launch_st(const lbm_cg_handle_s *H, int from, int write_macro, cudaStream_t s) {
+    const CgArgs a = cg_args(H, from, write_macro);
     const dim3 grid((unsigned)((H->n + CG_BLOCK - 1) / CG_BLOCK), (unsigned)H->m);
-    cg_density_kernel<PULL><<<grid, CG_BLOCK, 0, s>>>(a);
+    cg_density_kernel<ST, PULL><<<grid, CG_BLOCK, 0, s>>>(a);
     if (H->P.high_order) {
-        if (H->P.enhanced) cg_collide_kernel<PULL, true, true><<<grid, CG_BLOCK, 0, s>>>(a);
-        else cg_collide_kernel<PULL, true, false><<<grid, CG_BLOCK, 0, s>>>(a);
+        if (H->P.enhanced) cg_collide_kernel<ST, PULL, true, true><<<grid, CG_BLOCK, 0, s>>>(a);
+        else cg_collide_kernel<ST, PULL, true, false><<<grid, CG_BLOCK, 0, s>>>(a);
     } else {
-        if (H->P.enhanced) cg_collide_kernel<PULL, false, true><<<grid, CG_BLOCK, 0, s>>>(a);
-        else cg_collide_kernel<PULL, false, false><<<grid, CG_BLOCK, 0, s>>>(a);
+        if (H->P.enhanced) cg_collide_kernel<ST, PULL, false, true><<<grid, CG_BLOCK, 0, s>>>(a);
+        else cg_collide_kernel<ST, PULL, false, false><<<grid, CG_BLOCK, 0, s>>>(a);
+    }
+}
+
+// One step (PULL) or the first collision from a given post-stream state.
+template <bool PULL>
+static void cg_any_launch(const lbm_cg_handle_s *H, int from, int write_macro, cudaStream_t s) {
+    if (H->q == 19) {
+        if (H->st == LBM_STORE_F16S) cg3_launch_st<LBM_STORE_F16S, PULL>(H, from, write_macro, s);
+        else if (H->st == LBM_STORE_F64) cg3_launch_st<LBM_STORE_F64, PULL>(H, from, write_macro, s);
+        else cg3_launch_st<LBM_STORE_F32, PULL>(H, from, write_macro, s);
+    } else {
+        if (H->st == LBM_STORE_F16S) cg_launch_st<LBM_STORE_F16S, PULL>(H, from, write_macro, s);
+        else if (H->st == LBM_STORE_F64) cg_launch_st<LBM_STORE_F64, PULL>(H, from, write_macro, s);
+        else cg_launch_st<LBM_STORE_F32, PULL>(H, from, write_macro, s);
     }
 }
 
@@ -339,7 +396,8 @@ static int cg_create(int n, int m, int h, const lbm_cg_params *P, lbm_cg_handle 
     if (n < 5 || m < 5 || h < 1 || m > 65535 || h > 65535 || (h > 1 && h < 5))
         return cg_fail(LBM_ERR_INVALID, "lattice must be at least 5 nodes along each axis (m, h <= 65535)");
     if ((long long)n * m * h >= (1ll << 31)) return cg_fail(LBM_ERR_INVALID, "more than 2^31 nodes");
-    if (P->storage != LBM_STORE_F32) return cg_fail(LBM_ERR_UNSUPPORTED, "colour-gradient storage is F32");
+    if (P->storage != LBM_STORE_F32 && P->storage != LBM_STORE_F16S && P->storage != LBM_STORE_F64)
+        return cg_fail(LBM_ERR_INVALID, "colour-gradient storage must be F32, F16S or F64");
     if (!(P->r_viscosity > 0) || !(P->b_viscosity > 0)) return cg_fail(LBM_ERR_INVALID, "viscosities must be positive");
     lbm_cg_handle_s *H = new (std::nothrow) lbm_cg_handle_s();
     if (!H) return cg_fail(LBM_ERR_NOMEM, "out of host memory");
@@ -349,9 +407,12 @@ static int cg_create(int n, int m, int h, const lbm_cg_params *P, lbm_cg_handle 
     H->q = h > 1 ? 19 : 9;
     H->N = (long long)n * m * h;
     H->P = *P;
+    H->st = P->storage;
     const size_t N = (size_t)H->N;
-    cudaError_t e = cudaMalloc((void **)&H->buf, sizeof(float) * 4 * H->q * N);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&H->R, sizeof(float) * 8 * N);
+    const size_t rbytes = H->st == LBM_STORE_F64 ? sizeof(double) : sizeof(float);
+    cudaError_t e = cudaMalloc((void **)&H->buf, 4 * H->slot_bytes());
+    if (e == cudaSuccess) e = cudaMalloc((void **)&H->R, sizeof(float) * 6 * N);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&H->phi, rbytes * 2 * N);
     if (e == cudaSuccess) e = cudaMalloc((void **)&H->partial, sizeof(double) * (LAP_BLOCKS * 5 + 5));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&H->stepped, cudaEventDisableTiming);
@@ -364,10 +425,10 @@ static int cg_create(int n, int m, int h, const lbm_cg_params *P, lbm_cg_handle 
     H->ux = H->R + 3 * N;
     H->uy = H->R + 4 * N;
     H->uz = H->R + 5 * N;
-    H->phi = H->R + 6 * N;
-    H->dn = H->R + 7 * N;
+    H->dn = (char *)H->phi + rbytes * N;
     H->sums = H->partial + LAP_BLOCKS * 5;
-    cudaMemset(H->R, 0, sizeof(float) * 8 * N);
+    cudaMemset(H->R, 0, sizeof(float) * 6 * N);
+    cudaMemset(H->phi, 0, rbytes * 2 * N);
     *out = H;
     return LBM_OK;
 }
@@ -382,16 +443,40 @@ int lbm_cg_create3d(int n, int m, int h, const lbm_cg_params *P, lbm_cg_handle *
 int lbm_cg_init(lbm_cg_handle H, const float *r_f, const float *b_f) {
     if (!H || !r_f || !b_f) return cg_fail(LBM_ERR_INVALID, "null argument");
     const size_t N = (size_t)H->N, Q = (size_t)H->q;
-    // the given post-stream state goes to buffer 1; one collision without
+    // the given post-stream state goes to buffer 1 (through an FP32 staging
+    // area in buffer 0, encoded into the storage); one collision without
     // streaming turns it into the post-collision state in buffer 0
-    float *b1 = H->buf + 2 * Q * N;
-    cudaError_t e = cudaMemcpyAsync(b1, r_f, sizeof(float) * Q * N, cudaMemcpyHostToDevice, H->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(b1 + Q * N, b_f, sizeof(float) * Q * N, cudaMemcpyHostToDevice, H->stream);
+    float *stage = (float *)H->buffer(0);
+    const size_t fl = sizeof(float) * Q * N;
+    float *stage_r = nullptr, *stage_b = nullptr;
+    bool own = false;
+    if (2 * fl <= 2 * H->slot_bytes()) {
+        stage_r = stage;
+        stage_b = stage + Q * N;
+    } else {
+        // F16S: buffer 0 holds fewer bytes than two FP32 colour sets
+        cudaError_t e = cudaMalloc((void **)&stage_r, 2 * fl);
+        if (e != cudaSuccess) return cg_fail(LBM_ERR_NOMEM, std::string("staging: ") + cudaGetErrorString(e));
+        stage_b = stage_r + Q * N;
+        own = true;
+    }
+    cudaError_t e = cudaMemcpyAsync(stage_r, r_f, fl, cudaMemcpyHostToDevice, H->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(stage_b, b_f, fl, cudaMemcpyHostToDevice, H->stream);
+    if (e == cudaSuccess) {
+        const unsigned blocks = (unsigned)((Q * N + 255) / 256);
+        void *dst = H->buffer(1);
+        if (H->st == LBM_STORE_F16S)
+            cg_encode_kernel<LBM_STORE_F16S><<<blocks, 256, 0, H->stream>>>(stage_r, stage_b, dst, (int)Q, (long long)N, H->scale);
+        else if (H->st == LBM_STORE_F64)
+            cg_encode_kernel<LBM_STORE_F64><<<blocks, 256, 0, H->stream>>>(stage_r, stage_b, dst, (int)Q, (long long)N, H->scale);
+        else
+            cg_encode_kernel<LBM_STORE_F32><<<blocks, 256, 0, H->stream>>>(stage_r, stage_b, dst, (int)Q, (long long)N, H->scale);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+    if (own) cudaFree(stage_r);
     if (e != cudaSuccess) return cg_fail(LBM_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(e));
-    if (H->q == 19)
-        cg3_launch<false>(H, 1, 1, H->stream);
-    else
-        cg_launch<false>(H, cg_args(H, 1, 1), H->stream);
+    cg_any_launch<false>(H, 1, 1, H->stream);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
     if (e != cudaSuccess) return cg_fail(LBM_ERR_CUDA, std::string("init: ") + cudaGetErrorString(e));
@@ -404,10 +489,7 @@ int lbm_cg_step(lbm_cg_handle H, int nsteps, int write_macro_last, void *stream)
     cudaStream_t s = stream ? (cudaStream_t)stream : H->stream;
     for (int i = 0; i < nsteps; ++i) {
         const int wm = write_macro_last && i == nsteps - 1;
-        if (H->q == 19)
-            cg3_launch<true>(H, H->cur, wm, s);
-        else
-            cg_launch<true>(H, cg_args(H, H->cur, wm), s);
+        cg_any_launch<true>(H, H->cur, wm, s);
         H->cur ^= 1;
     }
     cudaError_t e = cudaGetLastError();
@@ -440,9 +522,32 @@ int lbm_cg_get_populations(lbm_cg_handle H, float *r, float *b) {
     if (!H || !r || !b) return cg_fail(LBM_ERR_INVALID, "null argument");
     const size_t N = (size_t)H->N, Q = (size_t)H->q;
     cudaError_t e = cudaDeviceSynchronize();
-    const float *src = H->buf + (size_t)H->cur * 2 * Q * N;
-    if (e == cudaSuccess) e = cudaMemcpy(r, src, sizeof(float) * Q * N, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(b, src + Q * N, sizeof(float) * Q * N, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cg_fail(LBM_ERR_CUDA, std::string("read-back: ") + cudaGetErrorString(e));
+    // decoded into the other buffer (free between steps) or a temporary
+    const size_t fl = sizeof(float) * Q * N;
+    float *tmp = nullptr;
+    bool own = false;
+    if (2 * fl <= 2 * H->slot_bytes()) {
+        tmp = (float *)H->buffer(1 - H->cur);
+    } else {
+        e = cudaMalloc((void **)&tmp, 2 * fl);
+        if (e != cudaSuccess) return cg_fail(LBM_ERR_NOMEM, std::string("read-back: ") + cudaGetErrorString(e));
+        own = true;
+    }
+    const unsigned blocks = (unsigned)((Q * N + 255) / 256);
+    const void *src = H->buffer(H->cur);
+    const float inv = 1.0f / H->scale;
+    if (H->st == LBM_STORE_F16S)
+        cg_decode_kernel<LBM_STORE_F16S><<<blocks, 256, 0, H->stream>>>(src, tmp, tmp + Q * N, (int)Q, (long long)N, inv);
+    else if (H->st == LBM_STORE_F64)
+        cg_decode_kernel<LBM_STORE_F64><<<blocks, 256, 0, H->stream>>>(src, tmp, tmp + Q * N, (int)Q, (long long)N, inv);
+    else
+        cg_decode_kernel<LBM_STORE_F32><<<blocks, 256, 0, H->stream>>>(src, tmp, tmp + Q * N, (int)Q, (long long)N, inv);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(r, tmp, fl, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(b, tmp + Q * N, fl, cudaMemcpyDeviceToHost);
+    if (own) cudaFree(tmp);
     if (e != cudaSuccess) return cg_fail(LBM_ERR_CUDA, std::string("read-back: ") + cudaGetErrorString(e));
     return LBM_OK;
 }
@@ -471,6 +576,7 @@ void lbm_cg_destroy(lbm_cg_handle H) {
     if (H->stream) cudaStreamSynchronize(H->stream);
     if (H->buf) cudaFree(H->buf);
     if (H->R) cudaFree(H->R);
+    if (H->phi) cudaFree(H->phi);
     if (H->partial) cudaFree(H->partial);
     if (H->stepped) cudaEventDestroy(H->stepped);
     if (H->stream) cudaStreamDestroy(H->stream);

@@ -16,20 +16,22 @@
 // write 152 B, plus 16 B of per-node fields written and the neighbours'
 // phi and rho read through L1/L2.
 #pragma once
+#include "lbm_cg_store.cuh"
 #include "lbm_device.cuh"
 
 namespace lbm {
 
 struct Cg3Args {
-    const float *in;   // red directions 0..18, then blue, N floats each
-    float *out;
+    const void *in;    // slot c of direction d at (c*19 + d)*N (lbm_cg_store.cuh)
+    void *out;
     float *R, *B;      // colour densities (output)
-    float *phi, *dn;   // colour field and density of the streamed state (gradients)
+    void *phi, *dn;    // colour field and density of the streamed state (gradients), arithmetic type
     float *rho, *ux, *uy, *uz;
     int nx, ny, nz;
     long long N;
     int write_macro;
-    float r_alpha, b_alpha, r_visc, b_visc, beta, A, g_limit;
+    double r_alpha, b_alpha, r_visc, b_visc, beta, A, g_limit;
+    float scale, inv_scale;  // F16S: S and 1/S of the summed population
 };
 
 constexpr int CG3_BLOCK = 128;
@@ -63,57 +65,74 @@ struct Cg3Nb {
 
 // Both colours of the node after streaming (PULL: population d from the
 // node at -c_d) or as stored.
-template <bool PULL>
-__device__ __forceinline__ void cg3_gather(const Cg3Args &a, const Cg3Nb &nb, float (&r)[19], float (&b)[19]) {
+template <int ST, bool PULL>
+__device__ __forceinline__ void cg3_gather(const Cg3Args &a, const Cg3Nb &nb, typename CgStore<ST>::R (&r)[19],
+                                           typename CgStore<ST>::R (&b)[19]) {
     using L = Lat<19>;
+    using SP = CgStore<ST>;
+    using T = typename SP::T;
+    using R = typename SP::R;
+    const T *in = (const T *)a.in;
 #pragma unroll
     for (int d = 0; d < 19; ++d) {
         const int s = PULL ? nb.at(-L::cx(d), -L::cy(d), -L::cz(d)) : nb.at(0, 0, 0);
-        r[d] = __ldg(a.in + d * a.N + s);
-        b[d] = __ldg(a.in + (19 + d) * a.N + s);
+        SP::load(in + d * a.N + s, in + (19 + d) * a.N + s, (R)L::w(d), (R)a.inv_scale, r[d], b[d]);
     }
 }
 
-template <bool PULL>
+template <int ST, bool PULL>
 __global__ void __launch_bounds__(CG3_BLOCK) cg3_density_kernel(const Cg3Args a) {
+    using R = typename CgStore<ST>::R;
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
     if (x >= a.nx) return;
-    float r[19], b[19];
-    cg3_gather<PULL>(a, Cg3Nb(a, x, y, z), r, b);
-    float rr = 0.f, bb = 0.f;
+    R r[19], b[19];
+    cg3_gather<ST, PULL>(a, Cg3Nb(a, x, y, z), r, b);
+    R rr = 0, bb = 0;
 #pragma unroll
     for (int d = 0; d < 19; ++d) {
         rr += r[d];
         bb += b[d];
     }
     const int node = x + a.nx * (y + a.ny * z);
-    const float rho = rr + bb;
-    a.phi[node] = (rr - bb) / rho;
-    a.dn[node] = rho;
+    const R rho = rr + bb;
+    ((R *)a.phi)[node] = (rr - bb) / rho;
+    ((R *)a.dn)[node] = rho;
 }
 
 // Per-direction constants of the 3D colour-gradient model (GpuInit.cu:
 // 896-940): lattice weight, perturbation offset B_k, rest weights phi_k and
 // theta_k, enhanced-equilibrium chi_k and psi_k, gradient weight.
-__device__ __forceinline__ float cg3_w(int k) { return k == 0 ? 1.f / 3.f : (k <= 6 ? 1.f / 18.f : 1.f / 36.f); }
-__device__ __forceinline__ float cg3_bpert(int k) { return k == 0 ? -2.f / 9.f : (k <= 6 ? 1.f / 54.f : 1.f / 27.f); }
-__device__ __forceinline__ float cg3_phi(int k) { return k == 0 ? 0.f : (k <= 6 ? 1.f / 12.f : 1.f / 24.f); }
-__device__ __forceinline__ float cg3_teta(int k) { return k == 0 ? 1.f : (k <= 6 ? -1.f / 12.f : -1.f / 24.f); }
-__device__ __forceinline__ float cg3_chi(int k) { return k == 0 ? -2.5f : (k <= 6 ? -1.f / 6.f : 1.f / 24.f); }
-__device__ __forceinline__ float cg3_psi(int k) { return k == 0 ? 0.f : (k <= 6 ? 0.25f : 0.125f); }
+template <class R = float> __device__ __forceinline__ R cg3_w(int k) {
+    return k == 0 ? (R)(1. / 3.) : (k <= 6 ? (R)(1. / 18.) : (R)(1. / 36.));
+}
+template <class R = float> __device__ __forceinline__ R cg3_bpert(int k) {
+    return k == 0 ? (R)(-2. / 9.) : (k <= 6 ? (R)(1. / 54.) : (R)(1. / 27.));
+}
+template <class R = float> __device__ __forceinline__ R cg3_phi(int k) {
+    return k == 0 ? (R)0 : (k <= 6 ? (R)(1. / 12.) : (R)(1. / 24.));
+}
+template <class R = float> __device__ __forceinline__ R cg3_teta(int k) {
+    return k == 0 ? (R)1 : (k <= 6 ? (R)(-1. / 12.) : (R)(-1. / 24.));
+}
+template <class R = float> __device__ __forceinline__ R cg3_chi(int k) {
+    return k == 0 ? (R)-2.5 : (k <= 6 ? (R)(-1. / 6.) : (R)(1. / 24.));
+}
+template <class R = float> __device__ __forceinline__ R cg3_psi(int k) {
+    return k == 0 ? (R)0 : (k <= 6 ? (R)0.25 : (R)0.125);
+}
 
 // Weight of the 104-point isotropic gradient stencil (Shan's eighth-order 3D
 // set) for an offset of squared length s2: shells 1, 2, 3, 4, 5, 6 and 9.
-__device__ __forceinline__ float cg3_ho_weight(int s2) {
+template <class R = float> __device__ __forceinline__ R cg3_ho_weight(int s2) {
     switch (s2) {
-    case 1: return 4.f / 45.f;
-    case 2: return 1.f / 21.f;
-    case 3: return 2.f / 105.f;
-    case 4: return 5.f / 504.f;
-    case 5: return 1.f / 315.f;
-    case 6: return 1.f / 630.f;
-    case 9: return 1.f / 5040.f;
-    default: return 0.f;
+    case 1: return (R)(4. / 45.);
+    case 2: return (R)(1. / 21.);
+    case 3: return (R)(2. / 105.);
+    case 4: return (R)(5. / 504.);
+    case 5: return (R)(1. / 315.);
+    case 6: return (R)(1. / 630.);
+    case 9: return (R)(1. / 5040.);
+    default: return (R)0;
     }
 }
 
@@ -126,50 +145,54 @@ __device__ __forceinline__ float cg3_ho_weight(int s2) {
 // +/- beta rho_r rho_b / rho cos(c_k, g) (phi_k + theta_k alpha); ENH adds the
 // enhanced equilibrium's nu (chi_k u.grad rho + psi_k G:c_k c_k).  Below the
 // gradient limit the perturbation and the recolouring vanish.
-template <bool PULL, bool HO, bool ENH>
+template <int ST, bool PULL, bool HO, bool ENH>
 __global__ void __launch_bounds__(CG3_BLOCK, CG3_MINB) cg3_collide_kernel(const Cg3Args a) {
     using L = Lat<19>;
+    using SP = CgStore<ST>;
+    using T = typename SP::T;
+    using R = typename SP::R;
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
     if (x >= a.nx) return;
     const int plane = a.nx * a.ny;
     const int node = x + a.nx * y + plane * z;
     const Cg3Nb nb(a, x, y, z);
-    float f[19], r_r = 0.f, b_r = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
+    const R *phi = (const R *)a.phi, *dn = (const R *)a.dn;
+    R f[19], r_r = 0, b_r = 0, jx = 0, jy = 0, jz = 0;
     {
-        float r[19], b[19];
-        cg3_gather<PULL>(a, nb, r, b);
+        R r[19], b[19];
+        cg3_gather<ST, PULL>(a, nb, r, b);
 #pragma unroll
         for (int d = 0; d < 19; ++d) {
             f[d] = r[d] + b[d];
             r_r += r[d];
             b_r += b[d];
-            if (L::cx(d)) jx += (float)L::cx(d) * f[d];
-            if (L::cy(d)) jy += (float)L::cy(d) * f[d];
-            if (L::cz(d)) jz += (float)L::cz(d) * f[d];
+            if (L::cx(d)) jx += (R)L::cx(d) * f[d];
+            if (L::cy(d)) jy += (R)L::cy(d) * f[d];
+            if (L::cz(d)) jz += (R)L::cz(d) * f[d];
         }
     }
-    const float rho = r_r + b_r;
-    const float u = jx / rho, v = jy / rho, w = jz / rho;
-    a.R[node] = r_r;
-    a.B[node] = b_r;
+    const R rho = r_r + b_r;
+    const R u = jx / rho, v = jy / rho, w = jz / rho;
+    a.R[node] = (float)r_r;
+    a.B[node] = (float)b_r;
     if (a.write_macro) {
-        a.rho[node] = rho;
-        a.ux[node] = u;
-        a.uy[node] = v;
-        a.uz[node] = w;
+        a.rho[node] = (float)rho;
+        a.ux[node] = (float)u;
+        a.uy[node] = (float)v;
+        a.uz[node] = (float)w;
     }
-    float cgx = 0.f, cgy = 0.f, cgz = 0.f, grx = 0.f, gry = 0.f, grz = 0.f;
-    auto add = [&](int j, float wt, int ox, int oy, int oz) {
-        const float a1 = wt * __ldg(a.phi + j);
+    R cgx = 0, cgy = 0, cgz = 0, grx = 0, gry = 0, grz = 0;
+    auto add = [&](int j, R wt, int ox, int oy, int oz) {
+        const R a1 = wt * __ldg(phi + j);
         if (ENH) {
-            const float a2 = wt * __ldg(a.dn + j);
-            grx += a2 * (float)ox;
-            gry += a2 * (float)oy;
-            grz += a2 * (float)oz;
+            const R a2 = wt * __ldg(dn + j);
+            grx += a2 * (R)ox;
+            gry += a2 * (R)oy;
+            grz += a2 * (R)oz;
         }
-        cgx += a1 * (float)ox;
-        cgy += a1 * (float)oy;
-        cgz += a1 * (float)oz;
+        cgx += a1 * (R)ox;
+        cgy += a1 * (R)oy;
+        cgz += a1 * (R)oz;
     };
     if (HO) {
         int xo[5], yo[5], zo[5];
@@ -185,49 +208,51 @@ __global__ void __launch_bounds__(CG3_BLOCK, CG3_MINB) cg3_collide_kernel(const 
             for (int oy = -2; oy <= 2; ++oy)
 #pragma unroll
                 for (int oz = -2; oz <= 2; ++oz) {
-                    const float wt = cg3_ho_weight(ox * ox + oy * oy + oz * oz);
-                    if (wt == 0.f) continue;
+                    const R wt = cg3_ho_weight<R>(ox * ox + oy * oy + oz * oz);
+                    if (wt == (R)0) continue;
                     add(xo[ox + 2] + yo[oy + 2] + zo[oz + 2], wt, ox, oy, oz);
                 }
     } else {
 #pragma unroll
         for (int k = 1; k < 19; ++k)
-            add(nb.at(L::cx(k), L::cy(k), L::cz(k)), k <= 6 ? 1.f / 6.f : 1.f / 12.f, L::cx(k), L::cy(k), L::cz(k));
+            add(nb.at(L::cx(k), L::cy(k), L::cz(k)), k <= 6 ? (R)(1. / 6.) : (R)(1. / 12.), L::cx(k), L::cy(k),
+                L::cz(k));
     }
-    const float mean_nu = 1.f / (r_r / (rho * a.r_visc) + b_r / (rho * a.b_visc));
-    const float omega_eff = 1.f / (3.f * mean_nu + 0.5f);
-    const float mean_alpha = a.r_alpha * r_r / rho + a.b_alpha * b_r / rho;
-    const float gnorm = sqrtf(cgx * cgx + cgy * cgy + cgz * cgz);
-    const float k_r = r_r / rho, k_b = b_r / rho, k_k = a.beta * r_r * b_r / rho;
-    const float cu1 = u * u + v * v + w * w;
-    const float G1 = 2.f * u * grx, G2 = u * gry + v * grx, G3 = u * grz + w * grx;
-    const float G5 = 2.f * v * gry, G6 = v * grz + w * gry, G9 = 2.f * w * grz;
-    const float ugr = u * grx + v * gry + w * grz;
-    const bool interface = gnorm > a.g_limit;
+    const R mean_nu = (R)1 / (r_r / (rho * (R)a.r_visc) + b_r / (rho * (R)a.b_visc));
+    const R omega_eff = (R)1 / ((R)3 * mean_nu + (R)0.5);
+    const R mean_alpha = (R)a.r_alpha * r_r / rho + (R)a.b_alpha * b_r / rho;
+    const R gnorm = sqrt(cgx * cgx + cgy * cgy + cgz * cgz);
+    const R k_r = r_r / rho, k_b = b_r / rho, k_k = (R)a.beta * r_r * b_r / rho;
+    const R cu1 = u * u + v * v + w * w;
+    const R G1 = (R)2 * u * grx, G2 = u * gry + v * grx, G3 = u * grz + w * grx;
+    const R G5 = (R)2 * v * gry, G6 = v * grz + w * gry, G9 = (R)2 * w * grz;
+    const R ugr = u * grx + v * gry + w * grz;
+    const bool interface = gnorm > (R)a.g_limit;
     // one reciprocal per node instead of two divisions per direction
-    const float inv_g = interface ? 1.f / gnorm : 0.f, inv_g2 = inv_g * inv_g;
-    float *rout = a.out + node, *bout = a.out + 19 * a.N + node;
+    const R inv_g = interface ? (R)1 / gnorm : (R)0, inv_g2 = inv_g * inv_g;
+    const R A = (R)a.A;
+    T *out = (T *)a.out;
 #pragma unroll
     for (int k = 0; k < 19; ++k) {
-        const float cx = (float)L::cx(k), cy = (float)L::cy(k), cz = (float)L::cz(k);
-        const float wk = cg3_w(k);
-        float pert = 0.f, cosin = 0.f;
+        const R cx = (R)L::cx(k), cy = (R)L::cy(k), cz = (R)L::cz(k);
+        const R wk = cg3_w<R>(k);
+        R pert = 0, cosin = 0;
         if (interface) {
-            const float pcg = cx * cgx + cy * cgy + cz * cgz;
-            if (k != 0) cosin = pcg * inv_g * (k <= 6 ? 1.f : 0.70710678f);
-            pert = a.A * gnorm * (wk * (pcg * pcg) * inv_g2 - cg3_bpert(k));
+            const R pcg = cx * cgx + cy * cgy + cz * cgz;
+            if (k != 0) cosin = pcg * inv_g * (k <= 6 ? (R)1 : (R)0.70710678118654752);
+            pert = A * gnorm * (wk * (pcg * pcg) * inv_g2 - cg3_bpert<R>(k));
         }
-        const float cu2 = u * cx + v * cy + w * cz;
-        const float rest = cg3_phi(k) + cg3_teta(k) * mean_alpha;
-        float feq = rho * (rest + wk * (3.f * cu2 + 4.5f * cu2 * cu2 - 1.5f * cu1));
+        const R cu2 = u * cx + v * cy + w * cz;
+        const R rest = cg3_phi<R>(k) + cg3_teta<R>(k) * mean_alpha;
+        R feq = rho * (rest + wk * ((R)3 * cu2 + (R)4.5 * cu2 * cu2 - (R)1.5 * cu1));
         if (ENH) {
-            const float TC = G1 * (cx * cx) + 2.f * G2 * (cx * cy) + 2.f * G3 * (cx * cz) + G5 * (cy * cy) +
-                             2.f * G6 * (cy * cz) + G9 * (cz * cz);
-            feq += mean_nu * (cg3_chi(k) * ugr + cg3_psi(k) * TC);
+            const R TC = G1 * (cx * cx) + (R)2 * G2 * (cx * cy) + (R)2 * G3 * (cx * cz) + G5 * (cy * cy) +
+                         (R)2 * G6 * (cy * cz) + G9 * (cz * cz);
+            feq += mean_nu * (cg3_chi<R>(k) * ugr + cg3_psi<R>(k) * TC);
         }
-        const float fp = omega_eff * feq + (1.f - omega_eff) * f[k] + pert;
-        rout[k * a.N] = k_r * fp + k_k * cosin * rest;
-        bout[k * a.N] = k_b * fp - k_k * cosin * rest;
+        const R fp = omega_eff * feq + ((R)1 - omega_eff) * f[k] + pert;
+        SP::store(out + k * a.N + node, out + (19 + k) * a.N + node, (R)L::w(k), (R)a.scale,
+                  k_r * fp + k_k * cosin * rest, k_b * fp - k_k * cosin * rest);
     }
 }
 

@@ -122,6 +122,39 @@ __host__ __device__ constexpr double rest_shift(int q, int coll, int d) {
 // incompressible energy-square equilibrium (eps_eq = -475/63 j^2, no density
 // term) puts its rest state at w_d - (3/252) M_eps,d (rest_shift below).
 // ---------------------------------------------------------------------------
+// F16C: a 16-bit float with 1 sign, 4 exponent and 11 mantissa bits,
+// exponent bias 15: (1 + m/2^11) 2^(E-15) for E = 1..15 ([2^-14, 2)), m 2^-25
+// for E = 0.  Rounding to nearest even from FP32; magnitudes from 2 up
+// saturate to the largest value; a non-finite input becomes 0xFFFF, which
+// decodes to NaN, so a diverging run still shows non-finite fields.
+struct f16c_t {
+    unsigned short bits;
+};
+__device__ __forceinline__ f16c_t f16c_from_float(float x) {
+    const unsigned int b = __float_as_uint(x);
+    const unsigned int sign = (b >> 16) & 0x8000u;
+    const unsigned int a = b & 0x7FFFFFFFu;
+    unsigned int out;
+    if (a >= 0x7F800000u) {
+        return f16c_t{0xFFFFu};
+    } else if (a < 0x38800000u) {  // below 2^-14: subnormal, steps of 2^-25
+        out = (unsigned int)__float2int_rn(__uint_as_float(a) * 33554432.0f);
+    } else {
+        const unsigned int r = a + 0x7FFu + ((a >> 12) & 1u);  // round the 12 dropped bits to nearest even
+        out = (r >> 12) - (112u << 11);
+        if (out > 0x7FFFu) out = 0x7FFFu;
+    }
+    if (sign && out == 0x7FFFu) out = 0x7FFEu;  // 0xFFFF is reserved for NaN
+    return f16c_t{(unsigned short)(sign | out)};
+}
+__device__ __forceinline__ float f16c_to_float(f16c_t v) {
+    const unsigned int u = v.bits;
+    if (u == 0xFFFFu) return __uint_as_float(0x7FC00000u);
+    const unsigned int a = u & 0x7FFFu;
+    const float m = a < 0x800u ? (float)a * 2.98023223876953125e-8f  // 2^-25
+                               : __uint_as_float((a << 12) + (112u << 23));
+    return (u & 0x8000u) ? -m : m;
+}
 // Read-only population load.  HINT 1 asks L2 to fetch the whole 256-byte
 // block around the address from DRAM (ld.global.nc.L2::256B), so the
 // neighbouring warps that read the rest of the block hit L2.
@@ -142,6 +175,15 @@ __device__ __forceinline__ float ld_pop(const float *p) {
         return v;
     }
     return __ldg(p);
+}
+template <int HINT>
+__device__ __forceinline__ f16c_t ld_pop(const f16c_t *p) {
+    if (HINT == 1) {
+        unsigned short v;
+        asm("ld.global.nc.L2::256B.b16 %0, [%1];" : "=h"(v) : "l"(&p->bits));
+        return f16c_t{v};
+    }
+    return f16c_t{__ldg(&p->bits)};
 }
 template <int HINT>
 __device__ __forceinline__ double ld_pop(const double *p) {
@@ -188,6 +230,24 @@ template <> struct Store<LBM_STORE_F16S> {
     }
     __device__ static __forceinline__ T encode64(double v, float w, float scale) {
         return __float2half_rn((float)((v - (double)w) * (double)scale));
+    }
+};
+template <> struct Store<LBM_STORE_F16C> {
+    using T = f16c_t;
+    using R = float;
+    __device__ static __forceinline__ R load(const T *p, float w, float inv_scale) {
+        return fmaf(f16c_to_float(T{__ldg(&p->bits)}), inv_scale, w);
+    }
+    __device__ static __forceinline__ R decode(T v, float w, float inv_scale) {
+        return fmaf(f16c_to_float(v), inv_scale, w);
+    }
+    __device__ static __forceinline__ T encode(R v, float w, float scale) { return f16c_from_float((v - w) * scale); }
+    __device__ static __forceinline__ void store(T *p, R v, float w, float scale) { *p = encode(v, w, scale); }
+    __device__ static __forceinline__ double decode64(T v, float w, float inv_scale) {
+        return (double)f16c_to_float(v) * (double)inv_scale + (double)w;
+    }
+    __device__ static __forceinline__ T encode64(double v, float w, float scale) {
+        return f16c_from_float((float)((v - (double)w) * (double)scale));
     }
 };
 template <> struct Store<LBM_STORE_F64> {

@@ -16,7 +16,8 @@ inline dim3 node_grid(const StepParams &p) {
 #define LBM_FOR_ALL(M)                                                                      \
     M(1, 0, false) M(1, 1, false) M(1, 2, false) M(2, 0, false) M(2, 1, false) M(2, 2, false) \
     M(3, 0, false) M(3, 1, false) M(3, 2, false) M(1, 0, true) M(1, 1, true) M(1, 2, true)   \
-    M(2, 0, true) M(2, 1, true) M(2, 2, true) M(3, 0, true) M(3, 1, true) M(3, 2, true)
+    M(2, 0, true) M(2, 1, true) M(2, 2, true) M(3, 0, true) M(3, 1, true) M(3, 2, true)   \
+    M(1, 3, true) M(2, 3, true) M(3, 3, true)
 
 template <int Q>
 int launch_step_t(const StepParams &p, int coll, int st, int phys, cudaStream_t s) {
@@ -71,6 +72,7 @@ int launch_resid_l2_t(const StepParams &p, int st, int phys, double *partial, do
 #define R_CASE(S, P)                                                               \
     if (st == S && (phys != 0) == P) resid_l2_kernel<Q, S, P><<<grid, STEP_BLOCK, 0, s>>>(p, partial);
     R_CASE(0, false) R_CASE(1, false) R_CASE(2, false) R_CASE(0, true) R_CASE(1, true) R_CASE(2, true)
+    R_CASE(3, true)
 #undef R_CASE
     sum_partials_kernel<<<1, 1024, 0, s>>>(partial, nb, out);
     return 0;
@@ -84,6 +86,7 @@ int launch_momentum_exchange_t(const StepParams &p, int st, const int *box, doub
     const int4 lo = make_int4(box[0], box[2], box[4], 0), hi = make_int4(box[1], box[3], box[5], 0);
     if (st == LBM_STORE_F32) momentum_exchange_kernel<Q, LBM_STORE_F32><<<grid, STEP_BLOCK, 0, s>>>(p, lo, hi, partial, nb);
     else if (st == LBM_STORE_F16S) momentum_exchange_kernel<Q, LBM_STORE_F16S><<<grid, STEP_BLOCK, 0, s>>>(p, lo, hi, partial, nb);
+    else if (st == LBM_STORE_F16C) momentum_exchange_kernel<Q, LBM_STORE_F16C><<<grid, STEP_BLOCK, 0, s>>>(p, lo, hi, partial, nb);
     else momentum_exchange_kernel<Q, LBM_STORE_F64><<<grid, STEP_BLOCK, 0, s>>>(p, lo, hi, partial, nb);
     for (int k = 0; k < 3; ++k) sum_partials_kernel<<<1, 1024, 0, s>>>(partial + k * nb, nb, out + k);
     return 0;
@@ -98,6 +101,7 @@ int launch_fd_rel_t(const StepParams &p, int st, int phys, float *fprev, float *
     if (st == S && (phys != 0) == P)                                                                   \
         fd_rel_kernel<Q, S, P><<<grid, STEP_BLOCK, 0, s>>>(p, fprev, ffirst, first, partial, nb);
     F_CASE(0, false) F_CASE(1, false) F_CASE(2, false) F_CASE(0, true) F_CASE(1, true) F_CASE(2, true)
+    F_CASE(3, true)
 #undef F_CASE
     max_partials_kernel<<<1, 1024, 0, s>>>(partial, nb, out);
     return 0;
@@ -114,6 +118,7 @@ int launch_encode_t(const StepParams &p, int st, const double *in, long long n, 
     const unsigned blocks = (unsigned)((n + 255) / 256);
     if (st == LBM_STORE_F32) encode_kernel<Q, LBM_STORE_F32><<<blocks, 256, 0, s>>>(p, in, n);
     else if (st == LBM_STORE_F16S) encode_kernel<Q, LBM_STORE_F16S><<<blocks, 256, 0, s>>>(p, in, n);
+    else if (st == LBM_STORE_F16C) encode_kernel<Q, LBM_STORE_F16C><<<blocks, 256, 0, s>>>(p, in, n);
     else encode_kernel<Q, LBM_STORE_F64><<<blocks, 256, 0, s>>>(p, in, n);
     return 0;
 }
@@ -123,6 +128,7 @@ int launch_decode_t(const StepParams &p, int st, double *out, long long n, cudaS
     const unsigned blocks = (unsigned)((n + 255) / 256);
     if (st == LBM_STORE_F32) decode_kernel<Q, LBM_STORE_F32><<<blocks, 256, 0, s>>>(p, out, n);
     else if (st == LBM_STORE_F16S) decode_kernel<Q, LBM_STORE_F16S><<<blocks, 256, 0, s>>>(p, out, n);
+    else if (st == LBM_STORE_F16C) decode_kernel<Q, LBM_STORE_F16C><<<blocks, 256, 0, s>>>(p, out, n);
     else decode_kernel<Q, LBM_STORE_F64><<<blocks, 256, 0, s>>>(p, out, n);
     return 0;
 }

@@ -50,6 +50,21 @@ __device__ __forceinline__ f1 operator-(f1 a) { return f1(-a.v); }
 __device__ __forceinline__ f1 &operator+=(f1 &a, f1 b) { return a = a + b; }
 __device__ __forceinline__ f1 &operator-=(f1 &a, f1 b) { return a = a - b; }
 
+// One stored value in storage units h and back: F32 as is, F16S as IEEE
+// half, F16C as the 1-4-11 float (lbm_device.cuh).
+template <int ST>
+__device__ __forceinline__ float h_raw(const typename Store<ST>::T *q) {
+    if constexpr (ST == LBM_STORE_F16S) return __half2float(__ldg(q));
+    else if constexpr (ST == LBM_STORE_F16C) return f16c_to_float(f16c_t{__ldg(&q->bits)});
+    else return __ldg(q);
+}
+template <int ST>
+__device__ __forceinline__ void h_put(typename Store<ST>::T *q, float v) {
+    if constexpr (ST == LBM_STORE_F16S) *q = __float2half_rn(v);
+    else if constexpr (ST == LBM_STORE_F16C) *q = f16c_from_float(v);
+    else *q = v;
+}
+
 // Pair storage: element type of a pair in HBM and its conversion to h.
 template <int ST> struct Pair;
 template <> struct Pair<LBM_STORE_F32> {
@@ -84,21 +99,19 @@ __device__ __forceinline__ V heq(int d, V rho_m_sigma, V rho, V ux, V uy, V uz, 
 }
 
 template <int Q, class V>
-__device__ __forceinline__ void collide_bgk_x2(V (&h)[Q], V rho, V ux, V uy, V uz, float omega, float sigma,
+__device__ __forceinline__ void collide_bgk_x2(V (&h)[Q], V rho, V rms, V ux, V uy, V uz, float omega,
                                                float S) {
     const V usq15 = V(1.5f) * fma2(ux, ux, fma2(uy, uy, uz * uz));
-    const V rms = rho - V(sigma);
     const V om(omega);
 #pragma unroll
     for (int d = 0; d < Q; ++d) h[d] = fma2(-om, h[d] - heq<Q>(d, rms, rho, ux, uy, uz, usq15, S), h[d]);
 }
 
 template <int Q, class V>
-__device__ __forceinline__ void collide_trt_x2(V (&h)[Q], V rho, V ux, V uy, V uz, float omega,
-                                               float omega_m, float sigma, float S) {
+__device__ __forceinline__ void collide_trt_x2(V (&h)[Q], V rho, V rms, V ux, V uy, V uz, float omega,
+                                               float omega_m, float S) {
     using L = Lat<Q>;
     const V usq15 = V(1.5f) * fma2(ux, ux, fma2(uy, uy, uz * uz));
-    const V rms = rho - V(sigma);
     V e[Q];
 #pragma unroll
     for (int d = 0; d < Q; ++d) e[d] = heq<Q>(d, rms, rho, ux, uy, uz, usq15, S);
@@ -118,7 +131,7 @@ __device__ __forceinline__ void collide_trt_x2(V (&h)[Q], V rho, V ux, V uy, V u
 // d_k = s_k/|m_k|^2 (m_k(h) - S (m_eq,k - sigma m_k(w~))), with w~ the
 // model's rest state (rest_shift): m(w~) = (1, -11, 0, 0, ...).
 template <bool REF, class V>
-__device__ __forceinline__ void collide_mrt19_x2(V (&h)[19], V rho, V ux, V uy, V uz, float omega,
+__device__ __forceinline__ void collide_mrt19_x2(V (&h)[19], V rho, V rms, V ux, V uy, V uz, float omega,
                                                  float sigma, float S) {
     const V sX = h[1] + h[2], aX = h[1] - h[2];
     const V sY = h[3] + h[4], aY = h[3] - h[4];
@@ -153,7 +166,7 @@ __device__ __forceinline__ void collide_mrt19_x2(V (&h)[19], V rho, V ux, V uy, 
     const V jsq = jx2 + jy2 + jz2;
     const V Sv(S);
     // S (m_eq,k - sigma m_k(w)) for the non-conserved moments
-    const V E1 = Sv * fma2(V(-11.f), rho - V(sigma), V(19.f) * jsq);
+    const V E1 = Sv * fma2(V(-11.f), rms, V(19.f) * jsq);
     // the storage shift is this model's rest state, whose eps moment is 0
     const V E2 = Sv * (V((float)(-475.0 / 63.0)) * jsq);
     const V c23 = V((float)(-2.0 / 3.0) * S);
@@ -210,7 +223,7 @@ __device__ __forceinline__ void collide_mrt19_x2(V (&h)[19], V rho, V ux, V uy, 
 // D2Q9 MRT in h units (CellFunctions.cu:7-63 basis and rates); REF keeps the
 // reference's energy equilibria with the extra density factor.
 template <bool REF, class V>
-__device__ __forceinline__ void collide_mrt9_x2(V (&h)[9], V rho, V ux, V uy, float omega, float sigma,
+__device__ __forceinline__ void collide_mrt9_x2(V (&h)[9], V rho, V rms, V ux, V uy, float omega, float sigma,
                                                 float S) {
     const V usq = fma2(ux, ux, uy * uy);
     const V ef = REF ? rho : V(1.f);
@@ -218,8 +231,8 @@ __device__ __forceinline__ void collide_mrt9_x2(V (&h)[9], V rho, V ux, V uy, fl
     const V rs = rho * usq * ef;
     V E[9];
     E[0] = 0.f;
-    E[1] = Sv * fma2(V(3.f), rs, V(-2.f) * (rho - V(sigma)));
-    E[2] = Sv * fma2(V(-3.f), rs, rho - V(sigma));
+    E[1] = Sv * fma2(V(3.f), rs, V(-2.f) * rms);
+    E[2] = Sv * fma2(V(-3.f), rs, rms);
     E[3] = Sv * (rho * ux);
     E[4] = -E[3];
     E[5] = Sv * (rho * uy);
@@ -259,18 +272,20 @@ __device__ __forceinline__ void collide_mrt9_x2(V (&h)[9], V rho, V ux, V uy, fl
     }
 }
 
+// rms = rho - sigma, the density's deviation from the shift's density,
+// formed as sum(h)/S by the caller: no FP32 cancellation of rho - 1.
 template <int Q, int COLL, bool PHYS, class V>
-__device__ __forceinline__ void collide_x2(V (&h)[Q], V rho, V ux, V uy, V uz, const StepParams &p,
+__device__ __forceinline__ void collide_x2(V (&h)[Q], V rho, V rms, V ux, V uy, V uz, const StepParams &p,
                                            float sigma, float S) {
     if (COLL == LBM_BGKW) {
-        collide_bgk_x2<Q>(h, rho, ux, uy, uz, (float)p.omega, sigma, S);
+        collide_bgk_x2<Q>(h, rho, rms, ux, uy, uz, (float)p.omega, S);
     } else if (COLL == LBM_TRT) {
-        collide_trt_x2<Q>(h, rho, ux, uy, uz, (float)p.omega, (float)p.omega_m, sigma, S);
+        collide_trt_x2<Q>(h, rho, rms, ux, uy, uz, (float)p.omega, (float)p.omega_m, S);
     } else {
         if constexpr (Q == 9)
-            collide_mrt9_x2<!PHYS>(h, rho, ux, uy, (float)p.omega, sigma, S);
+            collide_mrt9_x2<!PHYS>(h, rho, rms, ux, uy, (float)p.omega, sigma, S);
         else
-            collide_mrt19_x2<!PHYS>(h, rho, ux, uy, uz, (float)p.omega, sigma, S);
+            collide_mrt19_x2<!PHYS>(h, rho, rms, ux, uy, uz, (float)p.omega, sigma, S);
     }
 }
 
@@ -421,7 +436,8 @@ __device__ __forceinline__ void pair_node(const StepParams &p, const G &g, int x
         if (L::cy(d) == 1) jy += h[d]; else if (L::cy(d) == -1) jy -= h[d];
         if (L::cz(d) == 1) jz += h[d]; else if (L::cz(d) == -1) jz -= h[d];
     }
-    f2 rho = fma2(sum, f2(invS), f2(sigma));
+    f2 rms = sum * f2(invS);
+    f2 rho = rms + f2(sigma);
     const f2 irho(1.f / rho.v.x, 1.f / rho.v.y);
     const f2 sc = irho * f2(invS);
     f2 ux = fma2(jx, sc, f2((float)p.gshift)), uy = jy * sc, uz = jz * sc;
@@ -430,9 +446,11 @@ __device__ __forceinline__ void pair_node(const StepParams &p, const G &g, int x
     if (keep0 || keep1) {
         if (keep0) {
             rho.v.x = p.rho[node]; ux.v.x = p.ux[node]; uy.v.x = p.uy[node]; uz.v.x = p.uz[node];
+            rms.v.x = rho.v.x - sigma;
         }
         if (keep1) {
             rho.v.y = p.rho[node + 1]; ux.v.y = p.ux[node + 1]; uy.v.y = p.uy[node + 1]; uz.v.y = p.uz[node + 1];
+            rms.v.y = rho.v.y - sigma;
         }
     }
     if (p.write_macro) {
@@ -442,7 +460,7 @@ __device__ __forceinline__ void pair_node(const StepParams &p, const G &g, int x
         }
     }
 
-    collide_x2<Q, COLL, PHYS>(h, rho, ux, uy, uz, p, sigma, S);
+    collide_x2<Q, COLL, PHYS>(h, rho, rms, ux, uy, uz, p, sigma, S);
 
     // a solid node of a mixed pair keeps the zero encoding
     if (!fl0 || !fl1) {
@@ -469,14 +487,11 @@ __device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x,
                                          int ozp) {
     using L = Lat<Q>;
     using T = typename Store<ST>::T;
-    constexpr bool F16 = ST == LBM_STORE_F16S;
+    constexpr bool F16 = ST == LBM_STORE_F16S || ST == LBM_STORE_F16C;
     const float sigma = p.sigma;
     const float S = F16 ? p.scale : 1.f;
     const float invS = F16 ? p.inv_scale : 1.f;
-    auto raw = [](const T *q) -> float {
-        if constexpr (F16) return __half2float(__ldg(q));
-        else return __ldg(q);
-    };
+    auto raw = [](const T *q) -> float { return h_raw<ST>(q); };
     if constexpr (SPEC) {
         h[0] = spec_pull[0];
 #pragma unroll
@@ -493,7 +508,31 @@ __device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x,
         }
     }
     bool keep = false, zv = false;
-    if ((w & W_SPECIAL) || !PHYS) {
+    if constexpr (PHYS) {
+        // physics-mode faces and moving walls stay in storage units: the
+        // deviations keep their digits (an f-space detour rounds every
+        // population to FP32 near w_d, 1e-4 of a slow flow's velocity)
+        if (w & W_SPECIAL) {
+            const int sl = __ldg(p.slot + node);
+            const int kind = __ldg(p.bc_kind + sl);
+            if (kind & (BCK_MOVING | BCK_ACTIVE)) {
+                const float u0 = (float)__ldg(p.bc_uvw + 3 * sl), v0 = (float)__ldg(p.bc_uvw + 3 * sl + 1),
+                            w0 = (float)__ldg(p.bc_uvw + 3 * sl + 2);
+                float hv[Q];
+#pragma unroll
+                for (int d = 0; d < Q; ++d) hv[d] = h[d].v;
+                if (kind & BCK_MOVING) {
+                    bc_moving_wall_h<Q>(hv, __ldg(p.bc_mask + sl), (float)p.rho0, S, u0, v0, w0);
+                } else {
+                    const double rset = (kind & BCK_OUTLET) ? p.rho_out : p.rho_in;
+                    bc_phys_h<Q>(hv, kind & BCK_FACE_MASK, (kind & BCK_PRESSURE) != 0, (float)(rset - (double)sigma),
+                                 sigma, S, invS, u0, v0, w0);
+                }
+#pragma unroll
+                for (int d = 0; d < Q; ++d) h[d] = f1(hv[d]);
+            }
+        }
+    } else {
         if ((w & W_SPECIAL) || (w & 0x7FFFEu)) {
             // boundary nodes and reference wall copies: to f, scalar code, back
             float f[Q];
@@ -512,12 +551,14 @@ __device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x,
         if (L::cy(d) == 1) jy += h[d]; else if (L::cy(d) == -1) jy -= h[d];
         if (L::cz(d) == 1) jz += h[d]; else if (L::cz(d) == -1) jz -= h[d];
     }
-    f1 rho = fma2(sum, f1(invS), f1(sigma));
+    f1 rms = sum * f1(invS);
+    f1 rho = rms + f1(sigma);
     const f1 sc = f1(invS / rho.v);
     f1 ux = fma2(jx, sc, f1((float)p.gshift)), uy = jy * sc, uz = jz * sc;
     if (zv) uy = 0.f;
     if (keep) {
         rho = p.rho[node];
+        rms = rho - f1(sigma);
         ux = p.ux[node];
         uy = p.uy[node];
         uz = p.uz[node];
@@ -527,7 +568,7 @@ __device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x,
         p.uy[node] = uy.v;
         p.uz[node] = uz.v;
     }
-    collide_x2<Q, COLL, PHYS>(h, rho, ux, uy, uz, p, sigma, S);
+    collide_x2<Q, COLL, PHYS>(h, rho, rms, ux, uy, uz, p, sigma, S);
 }
 
 // SPEC: the pull values (guarded by the node's coordinates, not its flag
@@ -542,7 +583,7 @@ template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC = fa
 __device__ __forceinline__ void h_node_w(const StepParams &p, const G &g, int x, int y, int z, uint32_t w) {
     using L = Lat<Q>;
     using T = typename Store<ST>::T;
-    constexpr bool F16 = ST == LBM_STORE_F16S;
+    constexpr bool F16 = ST == LBM_STORE_F16S || ST == LBM_STORE_F16C;
     const float sigma = p.sigma;
     const float S = F16 ? p.scale : 1.f;
     const float invS = F16 ? p.inv_scale : 1.f;
@@ -552,10 +593,7 @@ __device__ __forceinline__ void h_node_w(const StepParams &p, const G &g, int x,
     const long long idx = x + (long long)g.pitch * row;
     const T *in = (const T *)p.fin[0] + idx;
     T *out = (T *)p.fout[0] + idx;
-    auto raw = [](const T *q) -> float {
-        if constexpr (F16) return __half2float(__ldg(q));
-        else return __ldg(q);
-    };
+    auto raw = [](const T *q) -> float { return h_raw<ST>(q); };
     const int plane = g.pitch * g.ny;
     int oxm = -1, oxp = 1, oym = -g.pitch, oyp = g.pitch, ozm = -plane, ozp = plane;
     if (WRAP) {
@@ -586,10 +624,7 @@ __device__ __forceinline__ void h_node_w(const StepParams &p, const G &g, int x,
         spec_pull[0] = in_row ? raw(in) : 0.f;
     }
     const bool fluid = (w & W_FLUID) != 0;
-    auto put = [](T *q, float v) {
-        if constexpr (F16) *q = __float2half_rn(v);
-        else *q = v;
-    };
+    auto put = [](T *q, float v) { h_put<ST>(q, v); };
     const unsigned warp_fluid = __ballot_sync(0xffffffffu, fluid);
     if (!warp_fluid) return;  // a warp of solid nodes writes nothing
     f1 h[Q];

@@ -33,11 +33,15 @@ class CgArguments:
     high_order: bool = False
     enhanced_distrib: bool = False
     bubble_radius: float = 0.2
+    # engine option: population storage, N.STORE_F32, N.STORE_F16S (summed
+    # population as a shifted FP16 deviation plus the colour difference in
+    # FP16, FP32 arithmetic) or N.STORE_F64 (FP64 storage and arithmetic)
+    storage: int = N.STORE_F32
 
     def to_c(self):
         return N.CgParams(self.r_alpha, self.b_alpha, self.r_viscosity, self.b_viscosity, self.beta,
                           self.A, self.g_limit, self.control_param, int(bool(self.high_order)),
-                          int(bool(self.enhanced_distrib)), N.STORE_F32)
+                          int(bool(self.enhanced_distrib)), int(self.storage))
 
 
 def rest_weights(alpha):

@@ -9,7 +9,7 @@ import os
 from . import build as _build
 
 LBM_OK, LBM_DIVERGED, LBM_ERR_FILE, LBM_ERR_UNSUPPORTED, LBM_ERR_INVALID, LBM_ERR_CUDA, LBM_ERR_NOMEM = range(7)
-STORE_F32, STORE_F16S, STORE_F64 = 0, 1, 2
+STORE_F32, STORE_F16S, STORE_F64, STORE_F16C = 0, 1, 2, 3
 MODE_REFERENCE, MODE_PHYSICS = 0, 1
 BGKW, TRT, MRT = 1, 2, 3
 INLET, NO_INLET, INLET_PRESSURE = 1, 2, 4
