@@ -110,9 +110,36 @@ def workload_config(args, n, m, h):
                          % (19 * n * m * h * B_LU[STORAGE_NAMES[args.storage]] / 76 * 2 / 2 / 1e9)}
 
 
+LATTICE_IO = {}
+
+
 def make_lattice(n, m, h, seed):
+    """The duct's lattice as a run reads it: the library's emitter writes the
+    sphere packing as reference-format Node and BC files
+    (lbm_emit_sphere_duct), the library's readers load them
+    (lbm_read_node_file, lbm_read_bc_file).  Seconds of each go to LATTICE_IO."""
+    import ctypes as C
+    import shutil
+    import tempfile
     from thesis_gb300 import lattice
-    return lattice.sphere_duct(n, m, h, WORKLOAD["porosity"], WORKLOAD["rmin"], WORKLOAD["rmax"], seed)
+    from thesis_gb300 import native as N
+    tmp = tempfile.mkdtemp(prefix="thesis_duct_")
+    node, bc = os.path.join(tmp, "duct_Node.dat"), os.path.join(tmp, "duct_BC.dat")
+    try:
+        t0 = time.perf_counter()
+        k = C.c_longlong(0)
+        rc = N.lib().lbm_emit_sphere_duct(n, m, h, WORKLOAD["porosity"], WORKLOAD["rmin"], WORKLOAD["rmax"], seed,
+                                          node.encode(), bc.encode(), C.byref(k))
+        if rc:
+            raise RuntimeError("lbm_emit_sphere_duct: " + N.lib().lbm_emit_last_error().decode())
+        t1 = time.perf_counter()
+        lat = lattice.from_files_native(node, bc)
+        t2 = time.perf_counter()
+        LATTICE_IO.update(emit_seconds=t1 - t0, read_seconds=t2 - t1, spheres=int(k.value),
+                          node_file_bytes=os.path.getsize(node), bc_file_bytes=os.path.getsize(bc))
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return lat
 
 
 def solver_args(storage):
@@ -1013,6 +1040,8 @@ def main():
                                              "two_nodes_per_thread": (knobs[2] >> 1) & 1,
                                              "min_blocks_per_sm": knobs[2] >> 2}),
                 "fluid_nodes_per_gpu": fluid, "status": status,
+                "lattice_files": dict(LATTICE_IO, source="lbm_emit_sphere_duct Node/BC files read by "
+                                      "lbm_read_node_file / lbm_read_bc_file"),
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind,
                              "traffic": traffic,

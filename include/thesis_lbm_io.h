@@ -122,6 +122,42 @@ int lbm_write_cross_section(const char *path, int n, int m, int h, const float *
 /* Message of the last failing call on this thread. */
 const char *lbm_io_last_error(void);
 
+/* ---- Lattice emitters (no counterpart in the reference) ------------------
+ * Geometries the reference generator cannot mesh (it meshes axis-aligned
+ * quadrilateral faces only, G/Intersect.cpp:98-110), written as Node and BC
+ * files in the reference's formats (3D lines as G/main.cpp:56-66 and
+ * G/FluidTracking.cpp:229-236 write them; 2D as readNodeFile/readConnFile
+ * read them, S/FilesReading.cu:270-347), coordinates index/(n-1).  Random
+ * geometry comes from SplitMix64(seed), uniform doubles from its top 53
+ * bits.  Return LBM_OK, LBM_ERR_INVALID or LBM_ERR_FILE (message in
+ * lbm_emit_last_error). */
+
+/* Random sequential packing of non-overlapping spheres in an n x m x h box:
+ * per attempt r = U(rmin, rmax), centre U(0,1) x (n-1, m-1, h-1), then the
+ * margin axis' coordinate again, U within [margin + r, ext - margin - r];
+ * a sphere that overlaps none is kept and its nodes (distance^2 <= r^2) turn
+ * solid, until the solid fraction reaches 1 - porosity or max_attempts.
+ * solid: n*m*h bytes, x fastest; spheres (may be NULL): up to max_spheres
+ * (x, y, z, r) rows; num_spheres: the count kept. */
+int lbm_pack_spheres(int n, int m, int h, double porosity, double rmin, double rmax, unsigned long long seed,
+                     int margin_axis, double margin, long long max_attempts, unsigned char *solid,
+                     double *spheres, long long max_spheres, long long *num_spheres);
+/* Duct along z packed with spheres (margin axis z, margin 2): Zou-He
+ * pressure faces z = 0 (inlet, BC type 2) and z = h-1 (outlet, type 3); the
+ * side faces and the spheres carry no BC lines (walls in physics mode). */
+int lbm_emit_sphere_duct(int n, int m, int h, double porosity, double rmin, double rmax, unsigned long long seed,
+                         const char *node_path, const char *bc_path, long long *num_spheres);
+/* 2D channel along x with n_obstacles (-1: 1 to 6 drawn) non-overlapping
+ * circles (radius 8-32) and rectangles (sides 10-60), times size_scale,
+ * clear of the inlet and outlet: inlet x = 0 (type 2), outlet x = n-1
+ * (type 3), walls y = 0 and y = m-1 (type 1). */
+int lbm_emit_channel2d(int n, int m, unsigned long long seed, int n_obstacles, double size_scale,
+                       const char *node_path, const char *bc_path);
+/* Lid-driven cavity, every node fluid: walls on all faces, the lid (y = m-1
+ * in 2D, z = h-1 in 3D) an inlet. */
+int lbm_emit_cavity(int dims, int n, int m, int h, const char *node_path, const char *bc_path);
+const char *lbm_emit_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -105,7 +105,9 @@ def build(force=False, verbose=False):
         obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
         cmd = [nvcc()] + common + ["-c", src, "-o", obj]
         if src.endswith(".cpp"):
-            cmd = [nvcc(), "-x", "c++"] + common + ["-c", src, "-o", obj]
+            # host code: no floating-point contraction, so geometric tests and
+            # the generator's comparisons give the same results on every host
+            cmd = [nvcc(), "-x", "c++"] + common + ["-Xcompiler", "-ffp-contract=off", "-c", src, "-o", obj]
         out = _run(cmd)
         if verbose and out:
             sys.stdout.write(out)

@@ -9,8 +9,11 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+#include <atomic>
 #include <fstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "thesis_lbm.h"
@@ -49,6 +52,109 @@ bool has(const std::string &s, const char *key) { return s.find(key) != std::str
 // The reference's default build parses into FP32 fields.
 double f32(double v) { return (double)(float)v; }
 
+
+// Whole file into memory; false when it cannot be read.
+bool slurp(const char *path, std::vector<char> &buf) {
+    FILE *f = path ? fopen(path, "rb") : nullptr;
+    if (!f) return false;
+    buf.clear();
+    const size_t block = 1u << 24;
+    size_t used = 0;
+    for (;;) {
+        buf.resize(used + block);
+        const size_t got = fread(buf.data() + used, 1, block, f);
+        used += got;
+        if (got < block) break;
+    }
+    const bool ok = ferror(f) == 0;
+    fclose(f);
+    buf.resize(used);
+    return ok;
+}
+
+// One whitespace-separated field of a record line, as fscanf's %d and %f
+// read it (strtol / strtof: a float field keeps strtof's rounding).
+bool next_int(const char *&p, const char *end, int &v) {
+    while (p < end && (*p == ' ' || *p == '\t' || *p == '\r')) ++p;
+    if (p >= end) return false;
+    char *q = nullptr;
+    const long x = strtol(p, &q, 10);
+    if (q == p) return false;
+    p = q;
+    v = (int)x;
+    return true;
+}
+bool next_float(const char *&p, const char *end, float &v) {
+    while (p < end && (*p == ' ' || *p == '\t' || *p == '\r')) ++p;
+    if (p >= end) return false;
+    char *q = nullptr;
+    const float x = strtof(p, &q);
+    if (q == p) return false;
+    p = q;
+    v = x;
+    return true;
+}
+
+// Records of a Node or BC file, one per non-blank line, parsed by
+// `parse(line_begin, line_end, record)` on all host threads.  Records before
+// the first malformed one are read, as the reference's fscanf loop stops
+// there (FilesReading.cu:270-347); what lies from that record on is
+// unspecified (the reference leaves it unset).
+template <class F>
+void parse_records(const std::vector<char> &buf, long long count, F parse) {
+    const char *base = buf.data();
+    const size_t size = buf.size();
+    const int T = (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 64u));
+    std::vector<size_t> cut(T + 1, size);
+    cut[0] = 0;
+    for (int t = 1; t < T; ++t) {
+        size_t c = std::max(size * t / T, cut[t - 1]);
+        while (c < size && base[c - 1] != '\n') ++c;
+        cut[t] = c;
+    }
+    auto is_blank = [](const char *a, const char *b) {
+        for (; a < b; ++a)
+            if (*a != ' ' && *a != '\t' && *a != '\r') return false;
+        return true;
+    };
+    std::vector<long long> lines(T, 0);
+    std::vector<std::thread> th;
+    for (int t = 0; t < T; ++t)
+        th.emplace_back([&, t] {
+            const char *p = base + cut[t], *e = base + cut[t + 1];
+            while (p < e) {
+                const char *nl = (const char *)memchr(p, '\n', (size_t)(e - p));
+                const char *le = nl ? nl : e;
+                if (!is_blank(p, le)) ++lines[t];
+                p = le + 1;
+            }
+        });
+    for (auto &x : th) x.join();
+    th.clear();
+    std::vector<long long> first(T + 1, 0);
+    for (int t = 0; t < T; ++t) first[t + 1] = first[t] + lines[t];
+    std::atomic<long long> bad(count);
+    for (int t = 0; t < T; ++t)
+        th.emplace_back([&, t] {
+            const char *p = base + cut[t], *e = base + cut[t + 1];
+            long long r = first[t];
+            while (p < e && r < count) {
+                const char *nl = (const char *)memchr(p, '\n', (size_t)(e - p));
+                const char *le = nl ? nl : e;
+                if (!is_blank(p, le)) {
+                    if (!parse(p, le, r)) {
+                        long long cur = bad.load();
+                        while (r < cur && !bad.compare_exchange_weak(cur, r)) {
+                        }
+                        return;
+                    }
+                    ++r;
+                }
+                p = le + 1;
+            }
+        });
+    for (auto &x : th) x.join();
+}
 }  // namespace
 
 extern "C" {
@@ -59,9 +165,10 @@ long long lbm_count_lines(const char *path) {
     FILE *f = path ? fopen(path, "rb") : nullptr;
     if (!f) return -1;
     long long lines = 0;
-    int c;
-    while ((c = fgetc(f)) != EOF)
-        if (c == '\n' || c == '\r') ++lines;
+    std::vector<char> block(1u << 22);
+    size_t got;
+    while ((got = fread(block.data(), 1, block.size(), f)) > 0)
+        for (size_t c = 0; c < got; ++c) lines += (block[c] == '\n') | (block[c] == '\r');
     fclose(f);
     return lines;
 }
@@ -150,21 +257,18 @@ int lbm_node_file_dims(const char *path) {
 int lbm_read_node_file(const char *path, int dims, long long count, int *i, int *j, int *k, float *x, float *y,
                        float *z, int *type) {
     if (!i || !j || !x || !y || !type || (dims == 3 && (!k || !z))) return io_fail(LBM_ERR_INVALID, "null array");
-    FILE *f = path ? fopen(path, "r") : nullptr;
-    if (!f) return io_fail(LBM_ERR_FILE, std::string("cannot open ") + (path ? path : "(null)"));
-    for (long long r = 0; r < count; ++r) {
-        int got;
+    std::vector<char> buf;
+    if (!slurp(path, buf)) return io_fail(LBM_ERR_FILE, std::string("cannot open ") + (path ? path : "(null)"));
+    parse_records(buf, count, [&](const char *p, const char *e, long long r) {
         if (dims == 2) {
-            got = fscanf(f, "%d %d %f %f %d", i + r, j + r, x + r, y + r, type + r);
             if (k) k[r] = 0;
             if (z) z[r] = 0.f;
-            if (got != 5) break;
-        } else {
-            got = fscanf(f, "%d\t%d\t%d\t%f\t%f\t%f\t%d", i + r, j + r, k + r, x + r, y + r, z + r, type + r);
-            if (got != 7) break;
+            return next_int(p, e, i[r]) && next_int(p, e, j[r]) && next_float(p, e, x[r]) && next_float(p, e, y[r]) &&
+                   next_int(p, e, type[r]);
         }
-    }
-    fclose(f);
+        return next_int(p, e, i[r]) && next_int(p, e, j[r]) && next_int(p, e, k[r]) && next_float(p, e, x[r]) &&
+               next_float(p, e, y[r]) && next_float(p, e, z[r]) && next_int(p, e, type[r]);
+    });
     return LBM_OK;
 }
 
@@ -172,22 +276,19 @@ int lbm_read_bc_file(const char *path, int dims, long long count, int *i, int *j
                      float *bx, float *by, float *bz, int *id) {
     if (!i || !j || !dir || !type || !bx || !by || !id || (dims == 3 && (!k || !bz)))
         return io_fail(LBM_ERR_INVALID, "null array");
-    FILE *f = path ? fopen(path, "r") : nullptr;
-    if (!f) return io_fail(LBM_ERR_FILE, std::string("cannot open ") + (path ? path : "(null)"));
-    for (long long r = 0; r < count; ++r) {
-        int got;
+    std::vector<char> buf;
+    if (!slurp(path, buf)) return io_fail(LBM_ERR_FILE, std::string("cannot open ") + (path ? path : "(null)"));
+    parse_records(buf, count, [&](const char *p, const char *e, long long r) {
         if (dims == 2) {
-            got = fscanf(f, "%d %d %d %d %f %f %d", i + r, j + r, dir + r, type + r, bx + r, by + r, id + r);
             if (k) k[r] = 0;
             if (bz) bz[r] = 0.f;
-            if (got != 7) break;
-        } else {
-            got = fscanf(f, "%d\t%d\t%d\t\t%d\t%d\t%f\t%f\t%f\t%d", i + r, j + r, k + r, dir + r, type + r, bx + r,
-                         by + r, bz + r, id + r);
-            if (got != 9) break;
+            return next_int(p, e, i[r]) && next_int(p, e, j[r]) && next_int(p, e, dir[r]) && next_int(p, e, type[r]) &&
+                   next_float(p, e, bx[r]) && next_float(p, e, by[r]) && next_int(p, e, id[r]);
         }
-    }
-    fclose(f);
+        return next_int(p, e, i[r]) && next_int(p, e, j[r]) && next_int(p, e, k[r]) && next_int(p, e, dir[r]) &&
+               next_int(p, e, type[r]) && next_float(p, e, bx[r]) && next_float(p, e, by[r]) &&
+               next_float(p, e, bz[r]) && next_int(p, e, id[r]);
+    });
     return LBM_OK;
 }
 

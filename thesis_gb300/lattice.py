@@ -146,6 +146,27 @@ def periodic_channel3d(n, m=None, h=None, periodic_axes=(0,)):
     return Lattice(3, n, m, h, fluid, _boundary_links(3, n, m, h, fluid, ft))
 
 
+class SplitMix64:
+    """SplitMix64 (Steele, Lea and Flood, OOPSLA 2014) with uniform doubles
+    from the top 53 bits.  The library's emitters (lattice_emit.cpp) draw the
+    same sequence, so a builder here and the Node/BC files emitted there give
+    the same lattice for a seed."""
+    MASK = (1 << 64) - 1
+
+    def __init__(self, seed):
+        self.s = int(seed) & self.MASK
+
+    def next(self):
+        self.s = (self.s + 0x9E3779B97F4A7C15) & self.MASK
+        z = self.s
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & self.MASK
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & self.MASK
+        return z ^ (z >> 31)
+
+    def uniform(self, lo=0.0, hi=1.0):
+        return lo + (hi - lo) * ((self.next() >> 11) * 2.0 ** -53)
+
+
 def pack_spheres(shape, porosity=0.70, rmin=6.0, rmax=14.0, seed=0, margin_axis=2, margin=2,
                  max_attempts=2_000_000):
     """Random sequential insertion of non-overlapping spheres.
@@ -153,45 +174,45 @@ def pack_spheres(shape, porosity=0.70, rmin=6.0, rmax=14.0, seed=0, margin_axis=
     Radii uniform in [rmin, rmax], centres uniform in the box (kept `margin`
     nodes plus a radius away from both ends of `margin_axis`, so the pressure
     faces stay fluid); spheres are added until the solid fraction reaches
-    1 - porosity.  Returns (solid mask (z, y, x) bool, spheres (k, 4)).
+    1 - porosity.  Per attempt the draws are r, x, y, z, then the margin
+    axis' coordinate again within its band (lbm_pack_spheres makes the same
+    draws and tests in the same order).  Returns (solid mask (z, y, x) bool,
+    spheres (k, 4)).
     """
     n, m, h = shape
-    rng = np.random.default_rng(seed)
+    rng = SplitMix64(seed)
     target = (1.0 - porosity) * n * m * h
+    ext = [float(n - 1), float(m - 1), float(h - 1)]
     solid = np.zeros((h, m, n), bool)
-    centres = np.zeros((0, 3))
-    radii = np.zeros(0)
+    cxs, cys, czs, rads = (np.zeros(0) for _ in range(4))
     solid_count = 0
     attempts = 0
-    batch = 256
     while solid_count < target and attempts < max_attempts:
-        r = rng.uniform(rmin, rmax, batch)
-        c = rng.uniform(0, 1, (batch, 3)) * np.array([n - 1, m - 1, h - 1], float)
+        attempts += 1
+        r = rng.uniform(rmin, rmax)
+        c = [rng.uniform() * ext[0], rng.uniform() * ext[1], rng.uniform() * ext[2]]
         lo = margin + r
-        hi = np.array([n - 1, m - 1, h - 1], float)[margin_axis] - margin - r
-        c[:, margin_axis] = lo + rng.uniform(0, 1, batch) * np.maximum(hi - lo, 0)
-        attempts += batch
-        for k in range(batch):
-            if centres.shape[0]:
-                d2 = ((centres - c[k]) ** 2).sum(1)
-                if np.any(d2 < (radii + r[k]) ** 2):
-                    continue
-            centres = np.vstack([centres, c[k]])
-            radii = np.append(radii, r[k])
-            x0, y0, z0 = c[k]
-            rr = r[k]
-            xs = slice(max(int(np.floor(x0 - rr)), 0), min(int(np.ceil(x0 + rr)) + 1, n))
-            ys = slice(max(int(np.floor(y0 - rr)), 0), min(int(np.ceil(y0 + rr)) + 1, m))
-            zs = slice(max(int(np.floor(z0 - rr)), 0), min(int(np.ceil(z0 + rr)) + 1, h))
-            zz, yy, xx = np.meshgrid(np.arange(zs.start, zs.stop), np.arange(ys.start, ys.stop),
-                                     np.arange(xs.start, xs.stop), indexing="ij")
-            inside = (xx - x0) ** 2 + (yy - y0) ** 2 + (zz - z0) ** 2 <= rr * rr
-            sub = solid[zs, ys, xs]
-            solid_count += int(np.count_nonzero(inside & ~sub))
-            sub |= inside
-            if solid_count >= target:
-                break
-    spheres = np.concatenate([centres, radii[:, None]], 1) if radii.size else np.zeros((0, 4))
+        hi = ext[margin_axis] - margin - r
+        c[margin_axis] = lo + rng.uniform() * max(hi - lo, 0.0)
+        if rads.size:
+            dx, dy, dz = cxs - c[0], cys - c[1], czs - c[2]
+            rr = rads + r
+            if np.any(dx * dx + dy * dy + dz * dz < rr * rr):
+                continue
+        cxs, cys, czs, rads = (np.append(a, v) for a, v in ((cxs, c[0]), (cys, c[1]), (czs, c[2]), (rads, r)))
+        x0, y0, z0 = c
+        xs = slice(max(int(np.floor(x0 - r)), 0), min(int(np.ceil(x0 + r)) + 1, n))
+        ys = slice(max(int(np.floor(y0 - r)), 0), min(int(np.ceil(y0 + r)) + 1, m))
+        zs = slice(max(int(np.floor(z0 - r)), 0), min(int(np.ceil(z0 + r)) + 1, h))
+        zz, yy, xx = np.meshgrid(np.arange(zs.start, zs.stop, dtype=np.float64),
+                                 np.arange(ys.start, ys.stop, dtype=np.float64),
+                                 np.arange(xs.start, xs.stop, dtype=np.float64), indexing="ij")
+        ddx, ddy, ddz = xx - x0, yy - y0, zz - z0
+        inside = ddx * ddx + ddy * ddy + ddz * ddz <= r * r
+        sub = solid[zs, ys, xs]
+        solid_count += int(np.count_nonzero(inside & ~sub))
+        sub |= inside
+    spheres = np.stack([cxs, cys, czs, rads], 1) if rads.size else np.zeros((0, 4))
     return solid, spheres
 
 
@@ -217,12 +238,13 @@ def channel2d(n=1024, m=256, seed=0, n_obstacles=None, size_scale=1.0):
     (sides 10-60), non-overlapping and clear of the inlet and outlet; walls at
     y = 0 and y = m-1, inlet x = 0, outlet x = n-1.  size_scale multiplies the
     obstacle sizes (0.25 for a 256 x 64 channel with the proportions of the
-    1024 x 256 one)."""
-    rng = np.random.default_rng(seed)
-    k = n_obstacles if n_obstacles is not None else int(rng.integers(1, 7))
+    1024 x 256 one).  Draws from SplitMix64(seed) in the order
+    lbm_emit_channel2d makes them."""
+    rng = SplitMix64(seed)
+    k = n_obstacles if n_obstacles is not None else 1 + min(int(rng.uniform() * 6.0), 5)
     solid = np.zeros((m, n), bool)
     boxes = []
-    yy, xx = np.mgrid[0:m, 0:n]
+    yy, xx = np.mgrid[0:m, 0:n].astype(np.float64)
     placed = 0
     tries = 0
     s = float(size_scale)
@@ -237,7 +259,8 @@ def channel2d(n=1024, m=256, seed=0, n_obstacles=None, size_scale=1.0):
             bb = (cx - r, cy - r, cx + r, cy + r)
             shape = ("circle", cx, cy, r)
         else:
-            w, hh = rng.uniform(min(10.0 * s, smax), smax, 2)
+            w = rng.uniform(min(10.0 * s, smax), smax)
+            hh = rng.uniform(min(10.0 * s, smax), smax)
             x0 = rng.uniform(n * 0.1, n * 0.85 - w)
             y0 = rng.uniform(3, m - 4 - hh)
             bb = (x0, y0, x0 + w, y0 + hh)
@@ -246,7 +269,8 @@ def channel2d(n=1024, m=256, seed=0, n_obstacles=None, size_scale=1.0):
             continue
         boxes.append(bb)
         if shape[0] == "circle":
-            solid |= (xx - shape[1]) ** 2 + (yy - shape[2]) ** 2 <= shape[3] ** 2
+            dx, dy = xx - shape[1], yy - shape[2]
+            solid |= dx * dx + dy * dy <= shape[3] * shape[3]
         else:
             solid |= (xx >= shape[1]) & (xx <= shape[1] + shape[3]) & (yy >= shape[2]) & (yy <= shape[2] + shape[4])
         placed += 1
@@ -375,6 +399,41 @@ def from_files(node_path, bc_path):
         fluid = nodes[:, 4]
         bc = np.stack([bcs[:, 0], bcs[:, 1], np.zeros(len(bcs)), bcs[:, 2], bcs[:, 3], bcs[:, 6]], 1)
     return Lattice(dims, n, m, h, fluid.astype(np.int32), bc.astype(np.int32))
+
+
+def from_files_native(node_path, bc_path):
+    """Build a Lattice from reference-format Node and BC files with the
+    library's readers (lbm_read_node_file, lbm_read_bc_file): the path a run
+    takes, and fast enough for lattices of tens of millions of nodes."""
+    import ctypes as C
+
+    from . import native as N
+    lib = N.lib()
+    np_ = node_path.encode()
+    bp = bc_path.encode()
+    dims = int(lib.lbm_node_file_dims(np_))
+    if dims not in (2, 3):
+        raise ValueError("cannot tell the dimension of %s" % node_path)
+    count = int(lib.lbm_count_lines(np_))
+    nb = int(lib.lbm_count_lines(bp))
+    ii, jj, kk, tt = (np.zeros(count, np.int32) for _ in range(4))
+    xs = [np.zeros(count, np.float32) for _ in range(3)]
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))  # noqa: E731
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+    N.check(lib.lbm_read_node_file(np_, dims, count, ip(ii), ip(jj), ip(kk), fp(xs[0]), fp(xs[1]), fp(xs[2]),
+                                   ip(tt)))
+    n, m, h = int(ii.max()) + 1, int(jj.max()) + 1, (int(kk.max()) + 1 if dims == 3 else 1)
+    node = ii.astype(np.int64) + n * (jj.astype(np.int64) + m * kk.astype(np.int64))
+    fluid = np.zeros(n * m * h, np.int32)
+    fluid[node] = tt
+    cols = [np.zeros(nb, np.int32) for _ in range(6)]
+    bx = [np.zeros(nb, np.float32) for _ in range(3)]
+    if nb:
+        N.check(lib.lbm_read_bc_file(bp, dims, nb, ip(cols[0]), ip(cols[1]), ip(cols[2]), ip(cols[3]), ip(cols[4]),
+                                     fp(bx[0]), fp(bx[1]), fp(bx[2]), ip(cols[5])))
+    if dims == 2:
+        cols[2][:] = 0
+    return Lattice(dims, n, m, h, fluid, np.stack(cols, 1))
 
 
 def write_files(lat, node_path, bc_path, delta=None):

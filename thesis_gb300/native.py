@@ -123,6 +123,15 @@ def lib():
         "lbm_momentum_exchange": (C.c_int, [vp, _IP, dp]),
         "lbm_read_init_file": (C.c_int, [C.c_char_p, C.POINTER(RunConfig)]),
         "lbm_count_lines": (C.c_longlong, [C.c_char_p]),
+        "lbm_pack_spheres": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                       C.c_ulonglong, C.c_int, C.c_double, C.c_longlong, vp, vp, C.c_longlong,
+                                       C.POINTER(C.c_longlong)]),
+        "lbm_emit_sphere_duct": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                           C.c_ulonglong, C.c_char_p, C.c_char_p, C.POINTER(C.c_longlong)]),
+        "lbm_emit_channel2d": (C.c_int, [C.c_int, C.c_int, C.c_ulonglong, C.c_int, C.c_double, C.c_char_p,
+                                         C.c_char_p]),
+        "lbm_emit_cavity": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_char_p, C.c_char_p]),
+        "lbm_emit_last_error": (C.c_char_p, []),
         "lbm_node_file_dims": (C.c_int, [C.c_char_p]),
         "lbm_read_node_file": (C.c_int, [C.c_char_p, C.c_int, C.c_longlong, _IP, _IP, _IP, fp, fp, fp, _IP]),
         "lbm_read_bc_file": (C.c_int, [C.c_char_p, C.c_int, C.c_longlong, _IP, _IP, _IP, _IP, _IP, fp, fp, fp,
