@@ -897,9 +897,53 @@ int phys_face_kind(const Lattice<T> &L, uint64_t mk, int &face, bool &pressure, 
     } else {
         if (L.p.outlet_profile == 5) pressure = true;
         else if (L.p.outlet_profile == 1) pressure = false;
+        else if (L.p.outlet_profile >= 2 && L.p.outlet_profile <= 4) return 3;
         else return -1;
     }
     return 1;
+}
+
+/* Physics-mode open outlet (the reference's OUTLET_SECOND, OUTLET_FIRST and
+ * OUTLET_HEmodel of gpuBcOutlet2D/3D, GpuBoundaries.cu:1562-1874, on any face,
+ * each population addressed at its own node): every population d entering
+ * through the face (c_d . e = 1, e the inward normal) becomes
+ *   first order   F_d(x + e),
+ *   second order  2 F_d(x + e) - F_d(x + 2e),
+ *   HEmodel       f_eq,d(rho, u) of the node's macroscopic state of the
+ *                 previous step,
+ * F the post-stream populations before any boundary condition (snap); a
+ * neighbour outside the lattice or not fluid leaves the population as
+ * streamed (second order falls back to first order without x + 2e). */
+template <class T>
+void open_outlet(Lattice<T> &L, const std::vector<T> &snap, int i, int face) {
+    const size_t N = (size_t)L.N;
+    const int q = L.q;
+    const bool d2 = q == 9;
+    int e[3] = {0, 0, 0};
+    e[face / 2] = (face % 2 == 0) ? 1 : -1;
+    const int x = L.X(i), y = L.Y(i), z = L.Z(i);
+    auto inside_fluid = [&](int k, int &j) {
+        const int yx = x + k * e[0], yy = y + k * e[1], yz = z + k * e[2];
+        if (yx < 0 || yx >= L.n || yy < 0 || yy >= L.m || yz < 0 || yz >= L.h) return false;
+        j = yx + L.n * (yy + L.m * yz);
+        return L.fluid[j] == 1;
+    };
+    int j1 = -1, j2 = -1;
+    const bool ok1 = inside_fluid(1, j1), ok2 = inside_fluid(2, j2);
+    for (int d = 1; d < q; ++d) {
+        const int cxd = d2 ? cx2[d] : cx3[d], cyd = d2 ? cy2[d] : cy3[d], czd = d2 ? 0 : cz3[d];
+        if (cxd * e[0] + cyd * e[1] + czd * e[2] != 1) continue;
+        T &fd = L.f[i + d * N];
+        if (L.p.outlet_profile == 4) {
+            fd = d2 ? feqc2<T>(L.u[i], (T)cxd, L.v[i], (T)cyd, L.rho[i], L.w[d])
+                    : feqc3<T>(L.u[i], (T)cxd, L.v[i], (T)cyd, L.w3[i], (T)czd, L.rho[i], L.w[d]);
+            continue;
+        }
+        if (!ok1) continue;
+        const T f1 = snap[j1 + d * N];
+        if (L.p.outlet_profile == 3 || !ok2) fd = f1;
+        else fd = 2 * f1 - snap[j2 + d * N];
+    }
 }
 
 /* Moving wall (Ladd): after half-way bounce-back each incoming population d of
@@ -1060,6 +1104,9 @@ int run(int dims, int n, int m, int h, const int *node_type, int nconn, const in
         collide_all(L);
         stream_all(L);
         if (p->mode == 1) {
+            const bool open = p->outlet_profile >= 2 && p->outlet_profile <= 4;
+            std::vector<T> snap;
+            if (open) snap = L.f;
             for (int i : L.bcnodes) {
                 int face;
                 bool pressure = false, outlet = false;
@@ -1067,6 +1114,10 @@ int run(int dims, int n, int m, int h, const int *node_type, int nconn, const in
                 const int kind = phys_face_kind(L, L.mask[i], face, pressure, outlet);
                 if (kind == 2) {
                     moving_wall(L, i, L.mask[i]);
+                    continue;
+                }
+                if (kind == 3) {
+                    open_outlet(L, snap, i, face);
                     continue;
                 }
                 if (kind != 1) continue;

@@ -539,3 +539,36 @@ def test_full_cavity128_against_reference_golden():
     V = v.reshape(128, 128)[64, :]  # horizontal centre line
     np.testing.assert_allclose(U, g["u"].reshape(128, 128)[:, 64], atol=5e-5)
     np.testing.assert_allclose(V, g["v"].reshape(128, 128)[64, :], atol=5e-5)
+
+
+def _rest(nn):
+    return (np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
+
+
+@pytest.mark.parametrize("outlet", [N.OUTLET_SECOND, N.OUTLET_FIRST, N.OUTLET_HEMODEL])
+@pytest.mark.parametrize("storage", [N.STORE_F32, N.STORE_F64, N.STORE_F16S])
+def test_physics_open_outlets_3d(oracle, outlet, storage):
+    """Physics-mode open outlets on a 3D face (the reference's second- and
+    first-order extrapolation and HEmodel outlets, GpuBoundaries.cu:1723-1874,
+    with every population addressed at its own node): a sphere-packed duct
+    with a pressure inlet at z = 0 and the outlet at z = h-1, MRT, against the
+    oracle."""
+    lat = lattice.sphere_duct(20, 16, 32, porosity=0.8, rmin=3, rmax=4, seed=9)
+    args = Arguments(viscosity=0.1, collision_model=N.MRT, mode=N.MODE_PHYSICS, storage=storage,
+                     init_equilibrium=1, inlet_profile=N.INLET_PRESSURE, outlet_profile=outlet,
+                     rho_in=1.01, rho_out=1.0)
+    g, r, fl = run_pair(oracle, lat, args, 60, init=_rest(lat.num_nodes))
+    compare(g, r, fl, storage, 3)
+
+
+@pytest.mark.parametrize("outlet", [N.OUTLET_SECOND, N.OUTLET_FIRST, N.OUTLET_HEMODEL])
+@pytest.mark.parametrize("coll", [N.TRT, N.MRT])
+def test_physics_open_outlets_2d(oracle, outlet, coll):
+    """The same outlets on the east face of a 2D obstacle channel with a
+    Zou-He velocity inlet (F32 and F64 storage)."""
+    lat = lattice.channel2d(96, 32, seed=5, n_obstacles=2, size_scale=0.3)
+    for storage in (N.STORE_F32, N.STORE_F64):
+        args = Arguments(u=0.04, viscosity=0.05, collision_model=coll, mode=N.MODE_PHYSICS, storage=storage,
+                         init_equilibrium=1, inlet_profile=N.INLET, outlet_profile=outlet)
+        g, r, fl = run_pair(oracle, lat, args, 80, init=_rest(lat.num_nodes))
+        compare(g, r, fl, storage, 2)

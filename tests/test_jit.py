@@ -30,6 +30,8 @@ from thesis_gb300.solver import Arguments, Solver
     (19, N.MRT, N.STORE_F16S, 1, 0, (256, 256, 512), (128, 2 | (4 << 2), 10 << 2)),
     (19, N.BGKW, N.STORE_F32, 0, 1, (20, 16, 21), (128, 2 | (8 << 2), 0)),
     (9, N.TRT, N.STORE_F32, 1, 1, (160, 48, 1), (128, 2, 1)),
+    # storage-unit z-walk kernel with predicated bounce-back loads
+    (19, N.MRT, N.STORE_F16S, 1, 0, (256, 256, 512), (64, 1 | 2 | (8 << 2), 20 << 2)),
     # F16C storage, storage-unit kernels
     (19, N.MRT, N.STORE_F16C, 1, 0, (256, 256, 512), (64, 2 | (8 << 2), 20 << 2)),
     (9, N.MRT, N.STORE_F16C, 1, 1, (160, 48, 1), (128, 2, 0)),

@@ -325,6 +325,10 @@ int lbm_batch_create(const lbm_lattice_desc *const *lattices, const lbm_params *
         std::string err;
         int rc = build_ref_masks(L, refm, err);
         if (!rc) rc = build_device_flags(L, P, refm, flags[d], err);
+        if (!rc && std::any_of(flags[d].kind.begin(), flags[d].kind.end(), [](int k) { return (k & BCK_HE) != 0; })) {
+            rc = LBM_ERR_UNSUPPORTED;
+            err = "HEmodel outlets keep per-node state that batches do not carry";
+        }
         if (rc) {
             batch_free(B);
             return bfail(rc, "domain " + std::to_string(d) + ": " + err);

@@ -164,8 +164,11 @@ bool curved_walls(const lbm_params &P, int q) {
 }
 
 bool one_node_boundaries(const lbm_params &P, int q) {
+    const bool open_outlet = P.outlet_profile == LBM_OUTLET_SECOND || P.outlet_profile == LBM_OUTLET_FIRST ||
+                             P.outlet_profile == LBM_OUTLET_HEMODEL;
     return curved_walls(P, q) || (q == 9 && P.mode != LBM_MODE_PHYSICS &&
-                                  (P.outlet_profile == LBM_OUTLET_SECOND || P.outlet_profile == LBM_OUTLET_FIRST));
+                                  (P.outlet_profile == LBM_OUTLET_SECOND || P.outlet_profile == LBM_OUTLET_FIRST)) ||
+           (P.mode == LBM_MODE_PHYSICS && open_outlet);
 }
 
 int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const RefMasks &r,
@@ -344,9 +347,15 @@ int build_device_flags(const lbm_lattice_desc &L, const lbm_params &P, const Ref
                 kind |= BCK_OUTLET;
                 if (P.outlet_profile == LBM_OUTLET_PRESSURE)
                     kind |= BCK_PRESSURE;
+                else if (P.outlet_profile == LBM_OUTLET_FIRST)
+                    kind |= BCK_EXTRAP1;
+                else if (P.outlet_profile == LBM_OUTLET_SECOND)
+                    kind |= BCK_EXTRAP2;
+                else if (P.outlet_profile == LBM_OUTLET_HEMODEL)
+                    kind |= BCK_HE;
                 else if (P.outlet_profile != LBM_OUTLET_ZOUHE) {
-                    err = "physics-mode outlets must be Zou-He velocity or pressure faces";
-                    return LBM_ERR_UNSUPPORTED;
+                    err = "unknown outlet profile";
+                    return LBM_ERR_INVALID;
                 }
             }
             special = true;

@@ -36,6 +36,9 @@ struct StepParams {
     // dir-1 for link dir, entry Q-1 the next boundary node's direction-1
     // entry); null for straight walls
     const double *bc_q;
+    // physics-mode HEmodel outlets: per boundary slot the node's rho, u, v, w
+    // of the previous step (written by the node's own thread every step)
+    float4 *bc_macro;
     float *rho, *ux, *uy, *uz;
     int nx, ny, nz;
     int pitch;  // elements from one row of a direction to the next (Q * nx)
@@ -265,6 +268,66 @@ __device__ __forceinline__ void ref2_outlet_neighbours(typename Store<ST>::R (&e
     }
 }
 
+// The physics-mode open outlet of a boundary slot (BCK_EXTRAP1, BCK_EXTRAP2,
+// BCK_HE): writes the populations that enter through the slot's face, the
+// directions d with c_d . e = 1 for the inward normal e of face
+// (kind & BCK_FACE_MASK), in storage units (ST's raw values; the caller's
+// arithmetic form): R_OUT(raw) turns a stored value into it and
+// EQ(d, rho, ux, uy, uz) gives an equilibrium in it.  The inward neighbours'
+// values are their post-stream populations as the gather forms them: pulled
+// from y - c_d, or across a blocked link y's own opp(d) (half-way
+// bounce-back); a neighbour that is not fluid leaves the population as the
+// node's own gather set it.
+template <int Q, int ST, bool WRAP, class G, class V, class RAW, class EQ>
+__device__ __forceinline__ void phys_open_outlet(V (&f)[Q], int kind, int sl, int node, const StepParams &p,
+                                                 const G &g, RAW raw_to, EQ eq) {
+    using L = Lat<Q>;
+    using T = typename Store<ST>::T;
+    const int face = kind & BCK_FACE_MASK;
+    const int ex = face == 0 ? 1 : (face == 1 ? -1 : 0), ey = face == 2 ? 1 : (face == 3 ? -1 : 0),
+              ez = face == 4 ? 1 : (face == 5 ? -1 : 0);
+    const T *base = (const T *)p.fin[0];
+    const int x = node % g.nx, y = (node / g.nx) % g.ny, z = node / (g.nx * g.ny);
+    auto wrap = [](int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); };
+    // post-stream value of direction d at the node k steps inward
+    auto value = [&](int k, int d, bool &ok) -> V {
+        const int yx = x + k * ex, yy = y + k * ey, yz = z + k * ez;
+        ok = yx >= 0 && yx < g.nx && yy >= 0 && yy < g.ny && yz >= 0 && yz < g.nz;
+        if (!ok) return V(0);
+        const uint32_t wy = __ldg(p.word + yx + g.nx * (yy + g.ny * yz));
+        ok = (wy & W_FLUID) != 0;
+        if (!ok) return V(0);
+        if ((wy >> d) & 1u) return raw_to(base + L::opp(d) * g.nx + yx + (long long)g.pitch * (yy + g.ny * yz), d);
+        int sx = yx - L::cx(d), sy = yy - L::cy(d), sz = yz - L::cz(d);
+        if (WRAP) {
+            sx = wrap(sx, g.nx);
+            sy = wrap(sy, g.ny);
+            sz = wrap(sz, g.nz);
+        }
+        return raw_to(base + d * g.nx + sx + (long long)g.pitch * (sy + g.ny * sz), d);
+    };
+    if (kind & BCK_HE) {
+        const float4 st = p.bc_macro[sl];
+#pragma unroll
+        for (int d = 1; d < Q; ++d)
+            if (L::cx(d) * ex + L::cy(d) * ey + L::cz(d) * ez == 1) f[d] = eq(d, V(st.x), V(st.y), V(st.z), V(st.w));
+        return;
+    }
+#pragma unroll
+    for (int d = 1; d < Q; ++d) {
+        if (L::cx(d) * ex + L::cy(d) * ey + L::cz(d) * ez != 1) continue;
+        bool ok1 = false, ok2 = false;
+        const V f1v = value(1, d, ok1);
+        if (!ok1) continue;
+        if (kind & BCK_EXTRAP1) {
+            f[d] = f1v;
+        } else {
+            const V f2v = value(2, d, ok2);
+            f[d] = ok2 ? V(2) * f1v - f2v : f1v;
+        }
+    }
+}
+
 // Boundary conditions of a fluid node whose populations are gathered
 // (pulled, bounced back): Zou-He faces, moving walls, the reference's wall,
 // periodic and symmetry copies.  keep_macro / zero_v report the reference's
@@ -309,6 +372,14 @@ __device__ __forceinline__ void apply_bc(typename Store<ST>::R (&f)[Q], uint32_t
             const int kind = __ldg(p.bc_kind + sl);
             if (kind & BCK_MOVING) {
                 bc_moving_wall<Q, R>(f, __ldg(p.bc_mask + sl), (R)p.rho0, u0, v0, w0);
+            } else if (kind & (BCK_EXTRAP1 | BCK_EXTRAP2 | BCK_HE)) {
+                using S = Store<ST>;
+                phys_open_outlet<Q, ST, WRAP, G, R>(
+                    f, kind, sl, node, p, g,
+                    [&](const typename S::T *q, int d) { return (R)S::decode(*q, p.shift[d], p.inv_scale); },
+                    [&](int d, R r, R ux, R uy, R uz) {
+                        return feq<Q, R>(d, r, ux, uy, uz, (R)1.5 * (ux * ux + uy * uy + uz * uz));
+                    });
             } else if (kind & BCK_ACTIVE) {
                 const bool pressure = (kind & BCK_PRESSURE) != 0;
                 const R rset = (kind & BCK_OUTLET) ? (R)p.rho_out : (R)p.rho_in;
@@ -357,6 +428,10 @@ __device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], uint3
             p.ux[node] = (float)ux;
             p.uy[node] = (float)uy;
             p.uz[node] = (float)uz;
+        }
+        if (PHYS && (w & W_SPECIAL) && p.bc_macro) {
+            const int sl = __ldg(p.slot + node);
+            if (__ldg(p.bc_kind + sl) & BCK_HE) p.bc_macro[sl] = make_float4((float)rho, (float)ux, (float)uy, (float)uz);
         }
     }
 

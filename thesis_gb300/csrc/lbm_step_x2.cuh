@@ -479,7 +479,7 @@ __device__ __forceinline__ void pair_node(const StepParams &p, const G &g, int x
 // type f1): no decode or encode per population and moments from deviations.
 // The update of one fluid node in storage units: gather (pull or bounce
 // back), boundary conditions, moments, collision; h receives the new state.
-template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC>
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC, int HB = 0>
 __device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x, int node, uint32_t w,
                                          const typename Store<ST>::T *in, f1 (&h)[Q],
                                          const float (&spec_pull)[SPEC ? Q : 1], const float (&spec_own)[SPEC ? Q : 1],
@@ -504,7 +504,16 @@ __device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x,
                              (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
                              (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
             const int own = (PHYS ? L::opp(d) : d) * g.nx;
-            h[d] = raw(in + (((w >> d) & 1u) ? own : pull));
+            if constexpr (HB == 1) {
+                // two exclusive loads at fixed offsets instead of an address
+                // selected per direction
+                float v;
+                if ((w >> d) & 1u) v = raw(in + own);
+                else v = raw(in + pull);
+                h[d] = v;
+            } else {
+                h[d] = raw(in + (((w >> d) & 1u) ? own : pull));
+            }
         }
     }
     bool keep = false, zv = false;
@@ -523,6 +532,13 @@ __device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x,
                 for (int d = 0; d < Q; ++d) hv[d] = h[d].v;
                 if (kind & BCK_MOVING) {
                     bc_moving_wall_h<Q>(hv, __ldg(p.bc_mask + sl), (float)p.rho0, S, u0, v0, w0);
+                } else if (kind & (BCK_EXTRAP1 | BCK_EXTRAP2 | BCK_HE)) {
+                    phys_open_outlet<Q, ST, WRAP, G, float>(
+                        hv, kind, sl, node, p, g, [](const T *q, int) { return h_raw<ST>(q); },
+                        [&](int d, float r, float ux, float uy, float uz) {
+                            const float usq15 = 1.5f * (ux * ux + uy * uy + uz * uz);
+                            return (feq<Q, float>(d, r, ux, uy, uz, usq15) - sigma * p.shift[d]) * S;
+                        });
                 } else {
                     const double rset = (kind & BCK_OUTLET) ? p.rho_out : p.rho_in;
                     bc_phys_h<Q>(hv, kind & BCK_FACE_MASK, (kind & BCK_PRESSURE) != 0, (float)(rset - (double)sigma),
@@ -556,6 +572,10 @@ __device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x,
     const f1 sc = f1(invS / rho.v);
     f1 ux = fma2(jx, sc, f1((float)p.gshift)), uy = jy * sc, uz = jz * sc;
     if (zv) uy = 0.f;
+    if (PHYS && (w & W_SPECIAL) && p.bc_macro) {
+        const int sl = __ldg(p.slot + node);
+        if (__ldg(p.bc_kind + sl) & BCK_HE) p.bc_macro[sl] = make_float4(rho.v, ux.v, uy.v, uz.v);
+    }
     if (keep) {
         rho = p.rho[node];
         rms = rho - f1(sigma);
@@ -579,7 +599,7 @@ __device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x,
 // the fluid lanes' store instructions (one store per direction and warp);
 // without it they store in a branch of their own, which keeps fewer
 // registers live (the batch kernel, whose domains are mostly all fluid).
-template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC = false, bool MERGE = true>
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC = false, bool MERGE = true, int HB = 0>
 __device__ __forceinline__ void h_node_w(const StepParams &p, const G &g, int x, int y, int z, uint32_t w) {
     using L = Lat<Q>;
     using T = typename Store<ST>::T;
@@ -636,14 +656,14 @@ __device__ __forceinline__ void h_node_w(const StepParams &p, const G &g, int x,
             }
             return;
         }
-        h_update<Q, COLL, ST, PHYS, WRAP, G, SPEC>(p, g, x, node, w, in, h, spec_pull, spec_own, oxm, oxp, oym, oyp,
+        h_update<Q, COLL, ST, PHYS, WRAP, G, SPEC, HB>(p, g, x, node, w, in, h, spec_pull, spec_own, oxm, oxp, oym, oyp,
                                                    ozm, ozp);
 #pragma unroll
         for (int d = 0; d < Q; ++d) put(out + d * g.nx, h[d].v);
         return;
     }
     if (fluid) {
-        h_update<Q, COLL, ST, PHYS, WRAP, G, SPEC>(p, g, x, node, w, in, h, spec_pull, spec_own, oxm, oxp, oym, oyp,
+        h_update<Q, COLL, ST, PHYS, WRAP, G, SPEC, HB>(p, g, x, node, w, in, h, spec_pull, spec_own, oxm, oxp, oym, oyp,
                                                    ozm, ozp);
     } else {
         // solid lanes of a warp with fluid nodes store the zero encoding in
@@ -660,10 +680,10 @@ __device__ __forceinline__ void h_node_w(const StepParams &p, const G &g, int x,
 
 
 // One node: its flag word, then the update.
-template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC = false, bool MERGE = true>
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC = false, bool MERGE = true, int HB = 0>
 __device__ __forceinline__ void h_node(const StepParams &p, const G &g, int x, int y, int z) {
     const uint32_t w = x < g.nx ? __ldg(p.word + x + g.nx * (y + g.ny * z)) : 0u;
-    h_node_w<Q, COLL, ST, PHYS, WRAP, G, SPEC, MERGE>(p, g, x, y, z, w);
+    h_node_w<Q, COLL, ST, PHYS, WRAP, G, SPEC, MERGE, HB>(p, g, x, y, z, w);
 }
 
 template <int Q, int COLL, int ST, bool PHYS>
@@ -676,14 +696,17 @@ __global__ void __launch_bounds__(STEP_BLOCK) step_kernel_h(const StepParams p) 
 // ZW > 1: a thread updates ZW nodes in a column along z, loading the next
 // node's flag word before it works on the current one, so the populations'
 // addresses do not wait a memory round trip for it (blockIdx.z = z / ZW).
+// HB = 1: a population across a possibly blocked link comes from one of two
+// loads at fixed offsets, predicated on the link's flag bit, instead of one
+// load from an address selected per direction.
 template <int Q, int COLL, int ST, bool PHYS, bool WRAP, int NX, int NY, int NZ, int BLOCK, int MINB, bool SPEC = false,
-          int ZW = 1>
+          int ZW = 1, int HB = 0>
 __global__ void __launch_bounds__(BLOCK, MINB) step_kernel_h_fixed(const StepParams p) {
     using G = FixedGeom<NX, NY, NZ, Q * NX>;
     const G g;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if constexpr (ZW == 1) {
-        h_node<Q, COLL, ST, PHYS, WRAP, G, SPEC>(p, g, x, blockIdx.y, blockIdx.z);
+        h_node<Q, COLL, ST, PHYS, WRAP, G, SPEC, true, HB>(p, g, x, blockIdx.y, blockIdx.z);
     } else {
         const int y = blockIdx.y, z0 = blockIdx.z * ZW;
         const bool in_row = x < NX;
@@ -694,7 +717,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) step_kernel_h_fixed(const StepPar
             if (z >= NZ) break;  // the same z for every thread of the block
             const uint32_t wn =
                 in_row && k + 1 < ZW && z + 1 < NZ ? __ldg(p.word + x + NX * (y + NY * (z + 1))) : 0u;
-            h_node_w<Q, COLL, ST, PHYS, WRAP, G, SPEC>(p, g, x, y, z, w);
+            h_node_w<Q, COLL, ST, PHYS, WRAP, G, SPEC, true, HB>(p, g, x, y, z, w);
             w = wn;
         }
     }

@@ -25,5 +25,14 @@ constexpr int BCK_ACTIVE = 32;
 // wall: half-way bounce-back with the momentum of the wall added on the
 // links listed (bit d: incoming direction d) in the slot's mask.
 constexpr int BCK_MOVING = 64;
+// Physics-mode open outlets on any face (the reference's OUTLET_FIRST,
+// OUTLET_SECOND and OUTLET_HEmodel, GpuBoundaries.cu:1562-1874, with the
+// populations addressed per node): the populations entering through the face
+// copied from the node one step inward (first order), extrapolated from the
+// nodes one and two steps inward (second order), or set to the equilibrium
+// of the node's own macroscopic state of the previous step (HEmodel).
+constexpr int BCK_EXTRAP1 = 128;
+constexpr int BCK_EXTRAP2 = 256;
+constexpr int BCK_HE = 512;
 
 }  // namespace lbm
