@@ -42,7 +42,7 @@ extern "C" {
  * mantissa bits (one significand bit more than IEEE half; the "FP16C" format
  * of Lehmann et al., Phys. Rev. E 106, 015308 (2022)): normal range
  * [2^-14, 2), subnormal step 2^-25, so |f_i - w_i| * scale must stay below 2
- * (scale defaults to 512 for F16C; values beyond saturate); physics mode and
+ * (scale defaults to 256 for F16C; values beyond saturate); physics mode and
  * the run-time specialised storage-unit kernels only. */
 #define LBM_STORE_F32 0
 #define LBM_STORE_F16S 1

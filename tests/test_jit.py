@@ -248,7 +248,7 @@ def test_f16c_storage_round_trip(native_lib):
     with Solver(lat, args) as s:
         s.set_populations(f)
         g = s.populations()
-    S = 512.0
+    S = 256.0  # the F16C default scale
     w32 = w.astype(np.float32).astype(np.float64)  # the shift as the kernels hold it
     want = w32 + _f16c_round_trip((f - w32) * S) / S
     fl = lat.node_type == 1

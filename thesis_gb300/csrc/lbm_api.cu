@@ -96,7 +96,7 @@ struct lbm_handle_s {
     // for straight walls), the boundary nodes in ascending order (the
     // reference's collapsed order) and, per BC link, its node's place there
     double *bcq = nullptr;
-    float4 *bc_macro = nullptr;  // HEmodel outlets: per slot rho, u, v, w of the previous step
+    double *bc_macro = nullptr;  // HEmodel outlets: per slot rho, u, v, w of the previous step
     // reference-mode 2D: boundary nodes whose mask carries a boundary id
     // (bits 24-31), for the reference's drag/lift sums
     std::vector<long long> id_nodes;
@@ -413,7 +413,7 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     H->stride = (N + 63) / 64 * 64;
     H->P = *P;
     H->elem = P->storage == LBM_STORE_F32 ? 4 : (P->storage == LBM_STORE_F64 ? 8 : 2);
-    H->scale = P->f16_scale > 0 ? (float)P->f16_scale : (P->storage == LBM_STORE_F16C ? 512.0f : 1024.0f);
+    H->scale = P->f16_scale > 0 ? (float)P->f16_scale : (P->storage == LBM_STORE_F16C ? 256.0f : 1024.0f);
     // omega as the reference computes it (GpuInit.cu:102-103)
     H->omega = 1.0 / (3.0 * P->viscosity + 0.5);
     H->omega_m = 8.0 * (2.0 - H->omega) / (8.0 - H->omega);
@@ -508,7 +508,7 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     ALLOC(H->uvw, sizeof(double) * 3 * H->nslots);
     if (curved_walls(*P, q)) ALLOC(H->bcq, sizeof(double) * q * H->nslots);
     if (std::any_of(flags.kind.begin(), flags.kind.end(), [](int k) { return (k & BCK_HE) != 0; }))
-        ALLOC(H->bc_macro, sizeof(float4) * H->nslots);
+        ALLOC(H->bc_macro, sizeof(double) * 4 * H->nslots);
     ALLOC(H->rho, sizeof(float) * N);
     ALLOC(H->ux, sizeof(float) * N);
     ALLOC(H->uy, sizeof(float) * N);
@@ -669,11 +669,16 @@ static int upload_or_fill(float *dst, const float *src, float value, long long N
 // HEmodel outlets start from the macroscopic fields of the initial state.
 __global__ void init_bc_macro_kernel(const uint32_t *word, const int32_t *slot, const int32_t *kind,
                                      const float *rho, const float *ux, const float *uy, const float *uz,
-                                     long long n, float4 *bc_macro) {
+                                     long long n, double *bc_macro) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !(word[i] & W_SPECIAL)) return;
     const int sl = slot[i];
-    if (kind[sl] & BCK_HE) bc_macro[sl] = make_float4(rho[i], ux[i], uy[i], uz[i]);
+    if (kind[sl] & BCK_HE) {
+        bc_macro[4 * sl] = rho[i];
+        bc_macro[4 * sl + 1] = ux[i];
+        bc_macro[4 * sl + 2] = uy[i];
+        bc_macro[4 * sl + 3] = uz[i];
+    }
 }
 
 static int init_bc_macro(lbm_handle_s *H) {

@@ -7,18 +7,21 @@
 //             same solver that the other storages are measured against);
 //   F16S      slot 0 the summed population as a shifted FP16 deviation,
 //             (r_d + b_d - w_d) * S; slot 1 the minority colour's fraction
-//             of it as FP16, its sign bit naming the majority colour: +m for
-//             b_d = m f_d (red majority), -m for r_d = m f_d (blue majority),
-//             so -0 is pure blue and +0 pure red; the arithmetic runs in FP32.
+//             mu of it, offset by 1/16 and signed by the majority colour:
+//             +(mu + 1/16) for b_d = mu f_d (red majority), -(mu + 1/16) for
+//             r_d = mu f_d (blue majority).  The offset keeps slightly
+//             negative minorities (recolouring can undershoot) down to
+//             -1/16 f_d; a pure phase (mu = 0) stores exactly 1/16.  The
+//             arithmetic runs in FP32.
 // Every colour-gradient model here relaxes the summed population as one BGK
 // fluid and only splits it by colour in the recolouring, so the summed value
 // carries the flow (mass, momentum, pressure) and is stored the way the
 // single-phase F16S storage is: as a small deviation from the rest state w_d
 // (the rest weights phi_k + theta_k alpha equal w_d for alpha = 4/9), which
 // keeps FP16's 11 significant bits on the deviation.  The colour split only
-// sets where the interface is: stored as the minority fraction, a bulk phase
-// stays exactly one colour and a small admixture keeps 11 significant bits
-// of itself, where a stored difference r_d - b_d would carry an absolute
+// sets where the interface is: stored as the minority fraction next to
+// 1/16, a bulk phase stays exactly one colour and a small admixture is kept
+// to 2^-15 f_d, where a stored difference r_d - b_d would carry an absolute
 // error of 2^-12 |f_d| into the minority colour everywhere.
 #pragma once
 #include <cuda_fp16.h>
@@ -58,11 +61,12 @@ template <> struct CgStore<LBM_STORE_F64> {
 template <> struct CgStore<LBM_STORE_F16S> {
     using T = __half;
     using R = float;
+    static constexpr float OFF = 0.0625f;  // offset of the stored minority fraction
     // inv_s = 1/S
     __device__ static __forceinline__ void load(const T *s0, const T *s1, R w, R inv_s, R &r, R &b) {
         const float f = fmaf(__half2float(__ldg(s0)), inv_s, w);
         const float m = __half2float(__ldg(s1));
-        const float minor = fabsf(m) * f;
+        const float minor = (fabsf(m) - OFF) * f;
         if (signbit(m)) {
             r = minor;
             b = f - minor;
@@ -71,13 +75,17 @@ template <> struct CgStore<LBM_STORE_F16S> {
             r = f - minor;
         }
     }
-    // s = S; a non-positive summed population (not met in a stable run)
-    // keeps no colour split: it is stored as red
+    // s = S; a minority below -1/16 of the sum is clamped there, and a
+    // non-positive sum (not met in a stable run) is stored as red
     __device__ static __forceinline__ void store(T *s0, T *s1, R w, R s, R r, R b) {
         const float f = r + b;
         *s0 = __float2half_rn((f - w) * s);
-        float m = 0.f;
-        if (f > 0.f) m = r >= b ? __fdividef(b, f) : copysignf(__fdividef(r, f), -1.f);
+        float m = OFF;
+        if (f > 0.f) {
+            const bool red = r >= b;
+            const float mu = fmaxf(__fdividef(red ? b : r, f), -OFF * 0.99f);
+            m = red ? mu + OFF : -(mu + OFF);
+        }
         *s1 = __float2half_rn(m);
     }
 };

@@ -37,8 +37,9 @@ struct StepParams {
     // entry); null for straight walls
     const double *bc_q;
     // physics-mode HEmodel outlets: per boundary slot the node's rho, u, v, w
-    // of the previous step (written by the node's own thread every step)
-    float4 *bc_macro;
+    // of the previous step (4 doubles, written by the node's own thread every
+    // step; doubles so an F64 run keeps its precision)
+    double *bc_macro;
     float *rho, *ux, *uy, *uz;
     int nx, ny, nz;
     int pitch;  // elements from one row of a direction to the next (Q * nx)
@@ -307,10 +308,11 @@ __device__ __forceinline__ void phys_open_outlet(V (&f)[Q], int kind, int sl, in
         return raw_to(base + d * g.nx + sx + (long long)g.pitch * (sy + g.ny * sz), d);
     };
     if (kind & BCK_HE) {
-        const float4 st = p.bc_macro[sl];
+        const double *st = p.bc_macro + 4 * sl;
+        const V r0 = V(st[0]), u0 = V(st[1]), v0 = V(st[2]), w0 = V(st[3]);
 #pragma unroll
         for (int d = 1; d < Q; ++d)
-            if (L::cx(d) * ex + L::cy(d) * ey + L::cz(d) * ez == 1) f[d] = eq(d, V(st.x), V(st.y), V(st.z), V(st.w));
+            if (L::cx(d) * ex + L::cy(d) * ey + L::cz(d) * ez == 1) f[d] = eq(d, r0, u0, v0, w0);
         return;
     }
 #pragma unroll
@@ -431,7 +433,13 @@ __device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], uint3
         }
         if (PHYS && (w & W_SPECIAL) && p.bc_macro) {
             const int sl = __ldg(p.slot + node);
-            if (__ldg(p.bc_kind + sl) & BCK_HE) p.bc_macro[sl] = make_float4((float)rho, (float)ux, (float)uy, (float)uz);
+            if (__ldg(p.bc_kind + sl) & BCK_HE) {
+                double *st = p.bc_macro + 4 * sl;
+                st[0] = (double)rho;
+                st[1] = (double)ux;
+                st[2] = (double)uy;
+                st[3] = (double)uz;
+            }
         }
     }
 

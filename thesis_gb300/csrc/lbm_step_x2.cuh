@@ -574,7 +574,13 @@ __device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x,
     if (zv) uy = 0.f;
     if (PHYS && (w & W_SPECIAL) && p.bc_macro) {
         const int sl = __ldg(p.slot + node);
-        if (__ldg(p.bc_kind + sl) & BCK_HE) p.bc_macro[sl] = make_float4(rho.v, ux.v, uy.v, uz.v);
+        if (__ldg(p.bc_kind + sl) & BCK_HE) {
+            double *st = p.bc_macro + 4 * sl;
+            st[0] = rho.v;
+            st[1] = ux.v;
+            st[2] = uy.v;
+            st[3] = uz.v;
+        }
     }
     if (keep) {
         rho = p.rho[node];
