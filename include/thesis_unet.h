@@ -9,15 +9,18 @@
  * has no learned part; this is the project's extension of its steady-state
  * loop (Iterate.cu:385-625: residual-driven iteration to a stop condition).
  *
- * Network (L pooling levels, widths c_l = min(16 * 2^l, 64)): two 3x3
+ * Network (L pooling levels, widths c_l = min(base * 2^l, 64), base 16 or
+ * 32): two 3x3
  * convolutions + ReLU per encoder level, 2x2 average pooling, a bottleneck of
  * two convolutions at level L, nearest upsampling with skip concatenation and
  * two convolutions per decoder level, and a 3x3 output convolution with 16
  * channels of which the first out_channels are used (4L + 3 convolutions).
  * Activations are NHWC BF16 with channels padded to multiples of 16, weights
- * BF16 copies of FP32 master weights, accumulation FP32 on the tensor cores
- * (hand-written mma.sync.m16n8k16 BF16 kernels: forward, data gradient,
- * weight gradient), Adam in FP32.
+ * BF16 copies of FP32 master weights, accumulation FP32 on the tensor cores:
+ * hand-written tcgen05.mma kernels with the accumulator in tensor memory for
+ * the forward and data-gradient convolutions with 32..256 outputs
+ * (THESIS_UNET_TC=0 selects the mma.sync form instead), mma.sync.m16n8k16
+ * for 16-output convolutions and the weight gradients; Adam in FP32.
  *
  * Conventions as in thesis_lbm.h: status codes (LBM_OK ...), caller-owned
  * host buffers, device buffers owned by the handle, one handle per thread.
@@ -39,6 +42,8 @@ typedef struct lbm_unet_config {
     unsigned long long seed;  /* weight initialisation (He normal) */
     int levels;               /* pooling levels L, 3..5 (0 selects 3); height and
                                  width must be multiples of 2^L */
+    int base_channels;        /* width of level 0: 16 or 32 (0 selects 16) */
+    int max_channels;         /* widest level: 64 (0 selects 64) */
 } lbm_unet_config;
 
 int lbm_unet_create(const lbm_unet_config *cfg, lbm_unet *out);

@@ -10,31 +10,32 @@ TEST INFRASTRUCTURE ONLY: imported by tests/ and never by the product.
 """
 import numpy as np
 
-def ch(l):
-    """Width of level l: min(16 * 2^l, 64)."""
-    return min(16 << l, 64)
+def ch(l, base=16):
+    """Width of level l: min(base * 2^l, 64)."""
+    return min(base << l, 64)
 
 
-def spec(levels=3):
+def spec(levels=3, base=16):
     """(cin, cout, relu) of the 4L + 3 convolutions, in parameter order:
     two per encoder level, two at the bottleneck, two per decoder level from
     the deepest up, and the output convolution."""
+    c = lambda l: ch(l, base)  # noqa: E731
     out = []
     for l in range(levels):
-        out += [(16 if l == 0 else ch(l - 1), ch(l), 1), (ch(l), ch(l), 1)]
-    out += [(ch(levels - 1), ch(levels), 1), (ch(levels), ch(levels), 1)]
+        out += [(16 if l == 0 else c(l - 1), c(l), 1), (c(l), c(l), 1)]
+    out += [(c(levels - 1), c(levels), 1), (c(levels), c(levels), 1)]
     for l in range(levels - 1, -1, -1):
-        up = ch(levels) if l == levels - 1 else ch(l)
-        out += [(up + ch(l), ch(l), 1), (ch(l), ch(l - 1) if l > 0 else ch(0), 1)]
-    out.append((ch(0), 16, 0))
+        up = c(levels) if l == levels - 1 else c(l)
+        out += [(up + c(l), c(l), 1), (c(l), c(l - 1) if l > 0 else c(0), 1)]
+    out.append((c(0), 16, 0))
     return out
 
 
 SPEC = spec(3)
 
 
-def param_count(levels=3):
-    return sum(9 * ci * co + co for ci, co, _ in spec(levels))
+def param_count(levels=3, base=16):
+    return sum(9 * ci * co + co for ci, co, _ in spec(levels, base))
 
 
 def bf16(x, on=True):
@@ -47,9 +48,9 @@ def bf16(x, on=True):
     return r.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-def unpack(params, levels=3):
+def unpack(params, levels=3, base=16):
     out, off = [], 0
-    for ci, co, _ in spec(levels):
+    for ci, co, _ in spec(levels, base):
         w = np.asarray(params[off:off + 9 * ci * co], np.float64).reshape(9, co, ci)
         off += 9 * ci * co
         b = np.asarray(params[off:off + co], np.float64)
@@ -102,10 +103,10 @@ def up_grad(g):
     return g.reshape(B, H // 2, 2, W // 2, 2, C).sum(axis=(2, 4))
 
 
-def forward(params, x_in, rnd=True, levels=3):
+def forward(params, x_in, rnd=True, levels=3, base=16):
     """x_in [B,H,W,in_ch] -> (output [B,H,W,16], cache)."""
-    S = spec(levels)
-    P = unpack(params, levels)
+    S = spec(levels, base)
+    P = unpack(params, levels, base)
     Wr = [bf16(w, rnd) for w, _ in P]
     R = lambda a: bf16(a, rnd)
     B, H, W, ic = x_in.shape
@@ -179,18 +180,18 @@ def backward(params, cache, dout, rnd=True):
     return np.concatenate([np.concatenate([w.reshape(-1), b]) for w, b in grads])
 
 
-def loss_and_gradients(params, x_in, target, weight, oc, rnd=True, levels=3):
-    out, cache = forward(params, x_in, rnd, levels)
+def loss_and_gradients(params, x_in, target, weight, oc, rnd=True, levels=3, base=16):
+    out, cache = forward(params, x_in, rnd, levels, base)
     loss, dout = loss_and_grad(out, target, weight, oc, rnd)
     return loss, backward(params, cache, dout, rnd)
 
 
-def init_params(in_channels, out_channels, seed, levels=3):
+def init_params(in_channels, out_channels, seed, levels=3, base=16):
     """He-normal weights over the real fan-in (any generator: the tests set
     the GPU's parameters from this)."""
     rng = np.random.default_rng(seed)
     out = []
-    S = spec(levels)
+    S = spec(levels, base)
     for k, (ci, co, _) in enumerate(S):
         cin_real = in_channels if k == 0 else ci
         cout_real = out_channels if k == len(S) - 1 else co

@@ -41,9 +41,9 @@ def test_oracle_matches_finite_differences(levels):
         assert abs(fd - g[i]) <= 1e-6 * max(abs(g[i]), 1e-3 * np.abs(g).max()), (i, fd, g[i])
 
 
-def _layer_slices(levels):
+def _layer_slices(levels, base=16):
     off = 0
-    for ci, co, _ in uo.spec(levels):
+    for ci, co, _ in uo.spec(levels, base):
         n = 9 * ci * co + co
         yield slice(off, off + n)
         off += n
@@ -99,3 +99,39 @@ def test_gpu_training_reduces_loss_and_fits_a_field():
         pred = net.predict(x)
     assert hist[-1] < 1e-2 * hist[0], (hist[0], hist[-1])
     assert np.abs(pred - t).max() < 0.15 * np.abs(t).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("levels,base", [(3, 16), (4, 32)])
+def test_gpu_tcgen05_convolutions_match_mma_sync(monkeypatch, levels, base):
+    """The tcgen05 convolutions (32 and 64 output channels: accumulator in
+    tensor memory) against the mma.sync ones (THESIS_UNET_TC=0) on the same
+    parameters and inputs: predictions and parameter gradients agree to the
+    FP32 accumulation order, far inside the oracle tolerances; and the
+    tcgen05 network's gradients match the FP64 oracle like the mma.sync
+    network's do."""
+    from thesis_gb300.warmstart import UNet
+    B, H, W, ic, oc = 2, 32, 256, 4, 3
+    x, t, w = _problem(B, H, W, ic, oc, 11)
+    p = uo.init_params(ic, oc, 13, levels, base)
+    res = {}
+    for tc in ("1", "0"):
+        monkeypatch.setenv("THESIS_UNET_TC", tc)
+        with UNet(H, W, max_batch=B, in_channels=ic, out_channels=oc, levels=levels, base_channels=base) as net:
+            assert net.num_params == p.size
+            net.set_params(p)
+            net.set_dataset(x, t, w)
+            g, loss = net.gradients([0, 1])
+            res[tc] = (net.predict(x), g, loss)
+    (p1, g1, l1), (p0, g0, l0) = res["1"], res["0"]
+    perr = np.abs(p1 - p0).max() / np.abs(p0).max()
+    gerr = np.linalg.norm(g1 - g0) / np.linalg.norm(g0)
+    print("tcgen05 vs mma.sync: prediction %.2e, gradient %.2e, loss %.3e / %.3e" % (perr, gerr, l1, l0))
+    assert perr < 2e-2 and gerr < 3e-2 and abs(l1 - l0) <= 1e-3 * l0
+    ref_loss, ref_g = uo.loss_and_gradients(p, x, t, w, oc, rnd=True, levels=levels, base=base)
+    assert abs(l1 - ref_loss) <= 1e-3 * ref_loss
+    for k, s in enumerate(_layer_slices(levels, base)):
+        a, b = g1[s].astype(np.float64), ref_g[s]
+        nb = np.linalg.norm(b)
+        if nb > 0:
+            assert np.linalg.norm(a - b) <= 3e-2 * nb, (k, np.linalg.norm(a - b) / nb)

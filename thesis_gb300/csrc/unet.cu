@@ -17,6 +17,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdlib.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -26,6 +27,7 @@
 
 #include "thesis_lbm.h"
 #include "thesis_unet.h"
+#include "unet_tc.cuh"
 
 namespace {
 
@@ -397,6 +399,9 @@ struct Layer {
 struct lbm_unet_s {
     lbm_unet_config cfg;
     int levels = 3;
+    int base = 16, cap = 64;   // channel widths c_l = min(base * 2^l, cap)
+    bool tc = true;            // 3x3 convolutions with 32..256 outputs on tcgen05 (unet_tc.cuh)
+    int *tc_err = nullptr;     // set by a tensor-core kernel whose bounded wait gave up
     cudaStream_t stream = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     double last_ms = 0;
@@ -428,12 +433,12 @@ namespace {
 int H_of(const lbm_unet_s *u, int level) { return u->cfg.height >> level; }
 int W_of(const lbm_unet_s *u, int level) { return u->cfg.width >> level; }
 
-// widths: c_l = min(16 * 2^l, 64); the second decoder conv of level l
+// widths: c_l = min(base * 2^l, cap); the second decoder conv of level l
 // outputs c_(l-1) (c_0 at level 0), which level l-1 upsamples into its
 // concatenation; level levels-1 upsamples the bottleneck (c_levels)
-int ch(int l) { return (16 << l) < 64 ? (16 << l) : 64; }
-int ch_dec_b(int l) { return l > 0 ? ch(l - 1) : ch(0); }
-int ch_up(const lbm_unet_s *u, int l) { return l == u->levels - 1 ? ch(u->levels) : ch(l); }
+int ch(const lbm_unet_s *u, int l) { return (u->base << l) < u->cap ? (u->base << l) : u->cap; }
+int ch_dec_b(const lbm_unet_s *u, int l) { return l > 0 ? ch(u, l - 1) : ch(u, 0); }
+int ch_up(const lbm_unet_s *u, int l) { return l == u->levels - 1 ? ch(u, u->levels) : ch(u, l); }
 int enc_a(int l) { return 2 * l; }
 int enc_b(int l) { return 2 * l + 1; }
 int bott_a(const lbm_unet_s *u) { return 2 * u->levels; }
@@ -474,11 +479,37 @@ void conv(lbm_unet_s *u, const Layer &l, const Act &in, const Act &out, const fl
     const int cin = transposed ? l.cout : l.cin, cout = transposed ? l.cin : l.cout;
     const int relu = transposed ? 0 : l.relu;
     bf16 *op = out.p;
+    if (u->tc && (cout == 32 || cout == 64 || cout == 128 || cout == 256)) {
+        const dim3 tg((W + unet_tc::TC_M - 1) / unet_tc::TC_M, H, B);
+#define TC_CASE(CO, CH)                                                                                       \
+    case CO: {                                                                                                \
+        constexpr int bytes = unet_tc::TcSmem<CO, CH>::BYTES;                                                 \
+        static bool attr = false;                                                                             \
+        if (!attr) {                                                                                          \
+            cudaFuncSetAttribute(unet_tc::conv3x3_tc_kernel<CO, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                 bytes);                                                                      \
+            attr = true;                                                                                      \
+        }                                                                                                     \
+        unet_tc::conv3x3_tc_kernel<CO, CH><<<tg, 128, bytes, u->stream>>>(in.p, in.cs, in.co, cin, w, bias, op,  \
+                                                                         out.cs, out.co, out32, H, W, relu,  \
+                                                                         u->tc_err);                          \
+        return;                                                                                               \
+    }
+        switch (cout) {
+            TC_CASE(32, 64)
+            TC_CASE(64, 64)
+            TC_CASE(128, 64)
+            TC_CASE(256, 32)
+        default: break;
+        }
+#undef TC_CASE
+    }
     switch (cout) {
     case 16: conv3x3_kernel<16><<<grid, 128, 0, u->stream>>>(in.p, in.cs, in.co, cin, w, bias, op, out.cs, out.co, out32, H, W, relu); break;
     case 32: conv3x3_kernel<32><<<grid, 128, 0, u->stream>>>(in.p, in.cs, in.co, cin, w, bias, op, out.cs, out.co, out32, H, W, relu); break;
     case 64: conv3x3_kernel<64><<<grid, 128, 0, u->stream>>>(in.p, in.cs, in.co, cin, w, bias, op, out.cs, out.co, out32, H, W, relu); break;
-    default: conv3x3_kernel<128><<<grid, 128, 0, u->stream>>>(in.p, in.cs, in.co, cin, w, bias, op, out.cs, out.co, out32, H, W, relu); break;
+    case 128: conv3x3_kernel<128><<<grid, 128, 0, u->stream>>>(in.p, in.cs, in.co, cin, w, bias, op, out.cs, out.co, out32, H, W, relu); break;
+    default: ufail(LBM_ERR_INVALID, "no convolution kernel for this width"); break;
     }
 }
 
@@ -516,10 +547,10 @@ void forward(lbm_unet_s *u, int B) {
     Act x = u->x0;
     for (int l = 0; l < NL; ++l) {
         cv(enc_a(l), x, u->e_a[l], l);
-        const Act skip = view(u->cat[l], ch_up(u, l), ch(l));
+        const Act skip = view(u->cat[l], ch_up(u, l), ch(u, l));
         cv(enc_b(l), u->e_a[l], skip, l);
-        const long long n = (long long)B * H_of(u, l + 1) * W_of(u, l + 1) * ch(l);
-        pool_kernel<<<grid_for(n), 256, 0, u->stream>>>(skip.p, skip.cs, skip.co, u->p[l].p, ch(l), B,
+        const long long n = (long long)B * H_of(u, l + 1) * W_of(u, l + 1) * ch(u, l);
+        pool_kernel<<<grid_for(n), 256, 0, u->stream>>>(skip.p, skip.cs, skip.co, u->p[l].p, ch(u, l), B,
                                                           H_of(u, l + 1), W_of(u, l + 1));
         x = u->p[l];
     }
@@ -574,28 +605,28 @@ void backward(lbm_unet_s *u, int B) {
     // decoder, from level 0 up
     for (int l = 0; l < NL; ++l) {
         if (l == 0)
-            relu_bwd(u->g_d_b[0], u->d_b[0], ch_dec_b(0), 0);
+            relu_bwd(u->g_d_b[0], u->d_b[0], ch_dec_b(u, 0), 0);
         else  // d_b[l] was upsampled into the first channels of cat[l-1]
-            up_bwd(view(u->g_cat[l - 1], 0, ch_dec_b(l)), u->d_b[l], ch_dec_b(l), l);
+            up_bwd(view(u->g_cat[l - 1], 0, ch_dec_b(u, l)), u->d_b[l], ch_dec_b(u, l), l);
         wgrad(u, L[dec_b(u, l)], u->d_a[l], B, l);
         dgrad(dec_b(u, l), u->g_d_a[l], l);
-        relu_bwd(u->g_d_a[l], u->d_a[l], ch(l), l);
+        relu_bwd(u->g_d_a[l], u->d_a[l], ch(u, l), l);
         wgrad(u, L[dec_a(u, l)], u->cat[l], B, l);
         dgrad(dec_a(u, l), u->g_cat[l], l);
     }
     // bottleneck
-    up_bwd(view(u->g_cat[NL - 1], 0, ch(NL)), u->bb, ch(NL), NL);
+    up_bwd(view(u->g_cat[NL - 1], 0, ch(u, NL)), u->bb, ch(u, NL), NL);
     wgrad(u, L[bott_b(u)], u->ba, B, NL);
     dgrad(bott_b(u), u->g_ba, NL);
-    relu_bwd(u->g_ba, u->ba, ch(NL), NL);
+    relu_bwd(u->g_ba, u->ba, ch(u, NL), NL);
     wgrad(u, L[bott_a(u)], u->p[NL - 1], B, NL);
     dgrad(bott_a(u), u->g_p[NL - 1], NL);
     // encoder, from the deepest level down
     for (int l = NL - 1; l >= 0; --l) {
-        pool_skip(u->g_p[l], view(u->g_cat[l], ch_up(u, l), ch(l)), view(u->cat[l], ch_up(u, l), ch(l)), ch(l), l);
+        pool_skip(u->g_p[l], view(u->g_cat[l], ch_up(u, l), ch(u, l)), view(u->cat[l], ch_up(u, l), ch(u, l)), ch(u, l), l);
         wgrad(u, L[enc_b(l)], u->e_a[l], B, l);
         dgrad(enc_b(l), u->g_e_a[l], l);
-        relu_bwd(u->g_e_a[l], u->e_a[l], ch(l), l);
+        relu_bwd(u->g_e_a[l], u->e_a[l], ch(u, l), l);
         wgrad(u, L[enc_a(l)], l == 0 ? u->x0 : u->p[l - 1], B, l);
         if (l > 0) dgrad(enc_a(l), u->g_p[l - 1], l);
     }
@@ -631,6 +662,15 @@ int finish(lbm_unet_s *u, const char *what) {
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(u->stream);
     if (e != cudaSuccess) return ufail(LBM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    if (u->tc_err) {
+        int flag = 0;
+        e = cudaMemcpy(&flag, u->tc_err, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return ufail(LBM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+        if (flag) {
+            cudaMemset(u->tc_err, 0, sizeof(int));
+            return ufail(LBM_ERR_CUDA, std::string(what) + ": a tensor-core convolution's bounded wait gave up");
+        }
+    }
     return LBM_OK;
 }
 
@@ -656,9 +696,16 @@ int lbm_unet_create(const lbm_unet_config *cfg, lbm_unet *out) {
     if (cfg->in_channels < 1 || cfg->in_channels > 16 || cfg->out_channels < 1 || cfg->out_channels > 16)
         return ufail(LBM_ERR_INVALID, "in_channels and out_channels must be 1..16");
     if (cfg->max_batch < 1) return ufail(LBM_ERR_INVALID, "max_batch must be positive");
+    const int base = cfg->base_channels ? cfg->base_channels : 16, cap = cfg->max_channels ? cfg->max_channels : 64;
+    if ((base != 16 && base != 32) || cap != 64)
+        return ufail(LBM_ERR_INVALID, "base_channels must be 16 or 32 and max_channels 64");
     lbm_unet_s *u = new lbm_unet_s();
     u->cfg = *cfg;
     u->levels = NL;
+    u->base = base;
+    u->cap = cap;
+    const char *tce = getenv("THESIS_UNET_TC");
+    u->tc = !(tce && strcmp(tce, "0") == 0);
     if (cudaStreamCreateWithFlags(&u->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&u->e0) != cudaSuccess || cudaEventCreate(&u->e1) != cudaSuccess) {
         lbm_unet_destroy(u);
@@ -667,16 +714,16 @@ int lbm_unet_create(const lbm_unet_config *cfg, lbm_unet *out) {
     // layers (cin, cout, relu) in parameter order
     std::vector<std::array<int, 3>> spec;
     for (int l = 0; l < NL; ++l) {
-        spec.push_back({l == 0 ? 16 : ch(l - 1), ch(l), 1});
-        spec.push_back({ch(l), ch(l), 1});
+        spec.push_back({l == 0 ? 16 : ch(u, l - 1), ch(u, l), 1});
+        spec.push_back({ch(u, l), ch(u, l), 1});
     }
-    spec.push_back({ch(NL - 1), ch(NL), 1});
-    spec.push_back({ch(NL), ch(NL), 1});
+    spec.push_back({ch(u, NL - 1), ch(u, NL), 1});
+    spec.push_back({ch(u, NL), ch(u, NL), 1});
     for (int l = NL - 1; l >= 0; --l) {
-        spec.push_back({ch_up(u, l) + ch(l), ch(l), 1});
-        spec.push_back({ch(l), ch_dec_b(l), 1});
+        spec.push_back({ch_up(u, l) + ch(u, l), ch(u, l), 1});
+        spec.push_back({ch(u, l), ch_dec_b(u, l), 1});
     }
-    spec.push_back({ch(0), 16, 0});
+    spec.push_back({ch(u, 0), 16, 0});
     size_t off = 0;
     for (const auto &sp : spec) {
         Layer l;
@@ -691,6 +738,7 @@ int lbm_unet_create(const lbm_unet_config *cfg, lbm_unet *out) {
     }
     u->nparams = (long long)off;
     int rc = LBM_OK;
+    rc = rc ? rc : alloc(u, (void **)&u->tc_err, sizeof(int));
     const size_t pb = sizeof(float) * off;
     rc = rc ? rc : alloc(u, (void **)&u->params, pb);
     rc = rc ? rc : alloc(u, (void **)&u->grad, pb);
@@ -704,21 +752,21 @@ int lbm_unet_create(const lbm_unet_config *cfg, lbm_unet *out) {
         v->resize(NL);
     rc = rc ? rc : make_act(u, u->x0, 16, 0);
     for (int l = 0; l < NL; ++l) {
-        rc = rc ? rc : make_act(u, u->e_a[l], ch(l), l);
-        rc = rc ? rc : make_act(u, u->cat[l], ch_up(u, l) + ch(l), l);
-        rc = rc ? rc : make_act(u, u->p[l], ch(l), l + 1);
-        rc = rc ? rc : make_act(u, u->d_a[l], ch(l), l);
-        rc = rc ? rc : make_act(u, u->d_b[l], ch_dec_b(l), l);
-        rc = rc ? rc : make_act(u, u->g_e_a[l], ch(l), l);
-        rc = rc ? rc : make_act(u, u->g_cat[l], ch_up(u, l) + ch(l), l);
-        rc = rc ? rc : make_act(u, u->g_p[l], ch(l), l + 1);
-        rc = rc ? rc : make_act(u, u->g_d_a[l], ch(l), l);
-        rc = rc ? rc : make_act(u, u->g_d_b[l], ch_dec_b(l), l);
+        rc = rc ? rc : make_act(u, u->e_a[l], ch(u, l), l);
+        rc = rc ? rc : make_act(u, u->cat[l], ch_up(u, l) + ch(u, l), l);
+        rc = rc ? rc : make_act(u, u->p[l], ch(u, l), l + 1);
+        rc = rc ? rc : make_act(u, u->d_a[l], ch(u, l), l);
+        rc = rc ? rc : make_act(u, u->d_b[l], ch_dec_b(u, l), l);
+        rc = rc ? rc : make_act(u, u->g_e_a[l], ch(u, l), l);
+        rc = rc ? rc : make_act(u, u->g_cat[l], ch_up(u, l) + ch(u, l), l);
+        rc = rc ? rc : make_act(u, u->g_p[l], ch(u, l), l + 1);
+        rc = rc ? rc : make_act(u, u->g_d_a[l], ch(u, l), l);
+        rc = rc ? rc : make_act(u, u->g_d_b[l], ch_dec_b(u, l), l);
     }
-    rc = rc ? rc : make_act(u, u->ba, ch(NL), NL);
-    rc = rc ? rc : make_act(u, u->bb, ch(NL), NL);
-    rc = rc ? rc : make_act(u, u->g_ba, ch(NL), NL);
-    rc = rc ? rc : make_act(u, u->g_bb, ch(NL), NL);
+    rc = rc ? rc : make_act(u, u->ba, ch(u, NL), NL);
+    rc = rc ? rc : make_act(u, u->bb, ch(u, NL), NL);
+    rc = rc ? rc : make_act(u, u->g_ba, ch(u, NL), NL);
+    rc = rc ? rc : make_act(u, u->g_bb, ch(u, NL), NL);
     const size_t np = (size_t)cfg->max_batch * cfg->height * cfg->width;
     rc = rc ? rc : alloc(u, (void **)&u->out32, np * 16 * sizeof(float));
     rc = rc ? rc : alloc(u, (void **)&u->dout, np * 16 * sizeof(bf16));

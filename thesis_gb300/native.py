@@ -65,7 +65,8 @@ class RunConfig(C.Structure):
 class UnetConfig(C.Structure):
     """lbm_unet_config (include/thesis_unet.h)."""
     _fields_ = [("height", C.c_int), ("width", C.c_int), ("in_channels", C.c_int), ("out_channels", C.c_int),
-                ("max_batch", C.c_int), ("seed", C.c_ulonglong), ("levels", C.c_int)]
+                ("max_batch", C.c_int), ("seed", C.c_ulonglong), ("levels", C.c_int),
+                ("base_channels", C.c_int), ("max_channels", C.c_int)]
 
 
 _lib = None

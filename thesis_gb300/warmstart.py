@@ -101,9 +101,9 @@ class UNet:
     """Handle of the BF16 tensor-core U-Net (lbm_unet_*)."""
 
     def __init__(self, height, width, max_batch=32, seed=0, in_channels=IN_CHANNELS, out_channels=OUT_CHANNELS,
-                 levels=3):
+                 levels=3, base_channels=16):
         self._lib = N.lib()
-        cfg = N.UnetConfig(height, width, in_channels, out_channels, max_batch, seed, levels)
+        cfg = N.UnetConfig(height, width, in_channels, out_channels, max_batch, seed, levels, base_channels, 64)
         h = C.c_void_p()
         N.check_unet(self._lib.lbm_unet_create(C.byref(cfg), C.byref(h)))
         self._h = h
@@ -304,9 +304,9 @@ def solve_with_warm_start(unet, lats, res, tol=TOL, check_every=100, max_steps=4
     return steps, resid, out, cold
 
 
-def forward_flops(height, width, levels=3):
+def forward_flops(height, width, levels=3, base_channels=16):
     """Multiply-add FLOPs (2 per MAC) of one forward pass of the network."""
-    ch = lambda l: min(16 << l, 64)
+    ch = lambda l: min(base_channels << l, 64)
     layers = []
     for l in range(levels):
         layers += [(16 if l == 0 else ch(l - 1), ch(l), l), (ch(l), ch(l), l)]
