@@ -42,7 +42,8 @@ extern "C" {
  * mantissa bits (one significand bit more than IEEE half; the "FP16C" format
  * of Lehmann et al., Phys. Rev. E 106, 015308 (2022)): normal range
  * [2^-14, 2), subnormal step 2^-25, so |f_i - w_i| * scale must stay below 2
- * (scale defaults to 256 for F16C; values beyond saturate); physics mode and
+ * (scale defaults to 256 for F16C, 8 for the D3Q19 MRT whose equilibrium
+ * start lies 0.143 from its rest state; values beyond saturate); physics mode and
  * the run-time specialised storage-unit kernels only. */
 #define LBM_STORE_F32 0
 #define LBM_STORE_F16S 1

@@ -287,7 +287,8 @@ def test_cg_gpu_f16s_storage_close_to_oracle(ho, enh):
     assert vel < 5e-2
     # a pure phase stays pure: nodes that are all red in the oracle carry no blue
     pure = orc.br == 0
-    assert np.abs(br[pure]).max() == 0.0
+    if pure.any():
+        assert np.abs(br[pure]).max() == 0.0
 
 
 @pytest.mark.gpu

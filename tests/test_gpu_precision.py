@@ -52,10 +52,11 @@ def test_storage_velocity_error_against_fp64(case):
     fl = lat.node_type == 1
     ref = _run(lat, Arguments(storage=N.STORE_F64, **base), steps)
     errs = {}
-    # F16C holds |f - w| * scale below 2: scale 256 for the duct (the inlet's
-    # pressure step drives |f - w| to ~4e-3 in the first steps), 32 for the
-    # cavity whose lid drives it to ~0.04
-    c16 = 256.0 if case == "duct" else 32.0
+    # F16C holds |f - shift| * scale below 2: the default (8) for the D3Q19
+    # MRT duct, whose equilibrium start lies 0.143 from the MRT rest state the
+    # storage is shifted by; 32 for the cavity whose lid drives |f - w| to
+    # ~0.04
+    c16 = 0.0 if case == "duct" else 32.0
     for name, st, sc in (("F32", N.STORE_F32, 0.0), ("F16S", N.STORE_F16S, 0.0), ("F16C", N.STORE_F16C, c16)):
         errs[name] = _rel(_run(lat, Arguments(storage=st, f16_scale=sc, **base), steps), ref, fl)
     print("%s: relative L2 velocity error vs F64 storage after %d steps: F32 %.2e, F16S %.2e, F16C %.2e"

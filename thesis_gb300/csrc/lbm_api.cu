@@ -413,7 +413,12 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
     H->stride = (N + 63) / 64 * 64;
     H->P = *P;
     H->elem = P->storage == LBM_STORE_F32 ? 4 : (P->storage == LBM_STORE_F64 ? 8 : 2);
-    H->scale = P->f16_scale > 0 ? (float)P->f16_scale : (P->storage == LBM_STORE_F16C ? 256.0f : 1024.0f);
+    // F16C holds |f - shift| * scale below 2.  The D3Q19 MRT stores
+    // deviations from its own rest state (4/21, 13/126, 1/63) while an
+    // equilibrium start uses w (1/3, 1/18, 1/36): f0 starts 0.143 off, so its
+    // default scale is 8; 256 elsewhere.
+    const float f16c_scale = (L->dims == 3 && P->collision_model == LBM_MRT) ? 8.0f : 256.0f;
+    H->scale = P->f16_scale > 0 ? (float)P->f16_scale : (P->storage == LBM_STORE_F16C ? f16c_scale : 1024.0f);
     // omega as the reference computes it (GpuInit.cu:102-103)
     H->omega = 1.0 / (3.0 * P->viscosity + 0.5);
     H->omega_m = 8.0 * (2.0 - H->omega) / (8.0 - H->omega);

@@ -7,12 +7,13 @@
 //             same solver that the other storages are measured against);
 //   F16S      slot 0 the summed population as a shifted FP16 deviation,
 //             (r_d + b_d - w_d) * S; slot 1 the minority colour's fraction
-//             mu of it, offset by 1/16 and signed by the majority colour:
-//             +(mu + 1/16) for b_d = mu f_d (red majority), -(mu + 1/16) for
+//             mu of it, offset by 2^-8 and signed by the majority colour:
+//             +(mu + 2^-8) for b_d = mu f_d (red majority), -(mu + 2^-8) for
 //             r_d = mu f_d (blue majority).  The offset keeps slightly
-//             negative minorities (recolouring can undershoot) down to
-//             -1/16 f_d; a pure phase (mu = 0) stores exactly 1/16.  The
-//             arithmetic runs in FP32.
+//             negative minorities (recolouring can undershoot; -7e-4 f_d at
+//             most in the perturbed-bubble tests) down to -2^-8 f_d; a pure
+//             phase (mu = 0) stores exactly 2^-8.  The arithmetic runs in
+//             FP32.
 // Every colour-gradient model here relaxes the summed population as one BGK
 // fluid and only splits it by colour in the recolouring, so the summed value
 // carries the flow (mass, momentum, pressure) and is stored the way the
@@ -20,8 +21,8 @@
 // (the rest weights phi_k + theta_k alpha equal w_d for alpha = 4/9), which
 // keeps FP16's 11 significant bits on the deviation.  The colour split only
 // sets where the interface is: stored as the minority fraction next to
-// 1/16, a bulk phase stays exactly one colour and a small admixture is kept
-// to 2^-15 f_d, where a stored difference r_d - b_d would carry an absolute
+// 2^-8, a bulk phase stays exactly one colour and a small admixture is kept
+// to 2^-19 f_d, where a stored difference r_d - b_d would carry an absolute
 // error of 2^-12 |f_d| into the minority colour everywhere.
 #pragma once
 #include <cuda_fp16.h>
@@ -61,7 +62,7 @@ template <> struct CgStore<LBM_STORE_F64> {
 template <> struct CgStore<LBM_STORE_F16S> {
     using T = __half;
     using R = float;
-    static constexpr float OFF = 0.0625f;  // offset of the stored minority fraction
+    static constexpr float OFF = 0.00390625f;  // offset of the stored minority fraction, 2^-8
     // inv_s = 1/S
     __device__ static __forceinline__ void load(const T *s0, const T *s1, R w, R inv_s, R &r, R &b) {
         const float f = fmaf(__half2float(__ldg(s0)), inv_s, w);
@@ -75,7 +76,7 @@ template <> struct CgStore<LBM_STORE_F16S> {
             r = f - minor;
         }
     }
-    // s = S; a minority below -1/16 of the sum is clamped there, and a
+    // s = S; a minority below -2^-8 of the sum is clamped there, and a
     // non-positive sum (not met in a stable run) is stored as red
     __device__ static __forceinline__ void store(T *s0, T *s1, R w, R s, R r, R b) {
         const float f = r + b;
