@@ -1045,7 +1045,8 @@ def main():
                                              "predicated_bounce_back": knobs[2] & 1 & (1 - ((knobs[1] >> 1) & 1)),
                                              "speculative_loads": knobs[2] & 1 & (knobs[1] >> 1) & 1,
                                              "two_nodes_per_thread": (knobs[2] >> 1) & 1,
-                                             "min_blocks_per_sm": knobs[2] >> 2}),
+                                             "min_blocks_per_sm": (knobs[2] >> 2) & 255,
+                                             "z_pairs_fp32x2": (knobs[2] >> 10) & 1}),
                 "fluid_nodes_per_gpu": fluid, "status": status,
                 "lattice_files": dict(LATTICE_IO, source="lbm_emit_sphere_duct Node/BC files read by "
                                       "lbm_read_node_file / lbm_read_bc_file"),

@@ -4,7 +4,8 @@ that its blocks cross many tiles and for hundreds of steps.
 The autotuner keeps, on the 256x256x512 sphere-packed duct (F16S), the
 storage-unit kernel walking 8 nodes along z with 64-thread blocks and a
 20-blocks-per-SM register cap (THESIS_LBM_KERNEL=jithz8b64m20).  This test
-pins that variant, and a second z-walk shape, on a 96x96x192 duct with the
+pins that variant, a second z-walk shape and the z-walk that updates two
+nodes at a time on packed FP32x2, on a 96x96x192 duct with the
 benchmark's sphere radii (6-14 nodes), porosity 0.70, pressure faces and
 tau 0.8, runs 300 steps and compares with the FP32 oracle run on the host
 cores: F32 storage within 2e-5 absolute (populations, density, velocity),
@@ -21,7 +22,7 @@ pytestmark = pytest.mark.gpu
 
 DIMS = (96, 96, 192)
 STEPS = 300
-VARIANTS = ["jithz8b64m20", "jithz4b128m10"]
+VARIANTS = ["jithz8b64m20", "jithz4b128m10", "jithz8b64m10q"]
 
 _cache = {}
 
@@ -65,6 +66,7 @@ def test_bench_kernel_matches_oracle_at_scale(oracle, monkeypatch, variant, stor
         block, hint, pred = s.kernel_config()
         zw = int(variant[5])
         assert hint >> 2 == zw and block == int(variant.split("b")[1].split("m")[0])
+        assert (pred >> 10) & 1 == ("q" in variant)
         s.init(np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
         s.step(STEPS, write_macro=True)
         rho, u, v, w = s.macro()

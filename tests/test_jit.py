@@ -30,6 +30,9 @@ from thesis_gb300.solver import Arguments, Solver
     (19, N.MRT, N.STORE_F16S, 1, 0, (256, 256, 512), (128, 2 | (4 << 2), 10 << 2)),
     (19, N.BGKW, N.STORE_F32, 0, 1, (20, 16, 21), (128, 2 | (8 << 2), 0)),
     (9, N.TRT, N.STORE_F32, 1, 1, (160, 48, 1), (128, 2, 1)),
+    # storage-unit z-walk kernel, two z nodes at a time on FP32x2
+    (19, N.MRT, N.STORE_F16S, 1, 0, (256, 256, 512), (64, 2 | (8 << 2), (10 << 2) | (1 << 10))),
+    (19, N.MRT, N.STORE_F32, 1, 1, (20, 16, 22), (64, 1 | 2 | (4 << 2), (1 << 10))),
     # storage-unit z-walk kernel with predicated bounce-back loads
     (19, N.MRT, N.STORE_F16S, 1, 0, (256, 256, 512), (64, 1 | 2 | (8 << 2), 20 << 2)),
     # F16C storage, storage-unit kernels
@@ -173,7 +176,7 @@ def test_jit_pair_reference_cavity(oracle, monkeypatch):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kernel", ["jith", "jiths", "jithz4", "jithz5", "jitf"])
+@pytest.mark.parametrize("kernel", ["jith", "jiths", "jithz4", "jithz5", "jitf", "jithz4q", "jithz6pq"])
 @pytest.mark.parametrize("storage", [N.STORE_F32, N.STORE_F16S])
 def test_storage_unit_and_f_space_kernels(oracle, monkeypatch, kernel, storage):
     """Both one-node arithmetic forms (and the storage-unit kernel with
@@ -187,7 +190,9 @@ def test_storage_unit_and_f_space_kernels(oracle, monkeypatch, kernel, storage):
     with Solver(lat, args) as s:
         assert (s.kernel_config()[1] >> 1) & 1 == (kernel != "jitf")
         assert s.kernel_config()[2] & 1 == (kernel == "jiths")
-        assert s.kernel_config()[1] >> 2 == (int(kernel[5:]) if kernel.startswith("jithz") else 0)
+        zw = int(kernel[5:].rstrip("pq")) if kernel.startswith("jithz") else 0
+        assert s.kernel_config()[1] >> 2 == zw
+        assert (s.kernel_config()[2] >> 10) & 1 == ("q" in kernel)
     g, r, fl = run_pair(oracle, lat, args, 40, init=_rest(lat.num_nodes))
     compare(g, r, fl, storage, 3)
 

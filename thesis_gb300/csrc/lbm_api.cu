@@ -88,6 +88,7 @@ struct lbm_handle_s {
     bool fd_recorded = false;
     int zwalk_request = 0;        // THESIS_LBM_KERNEL=jithz<k>[b<block>][m<min blocks>][p]
     int hb_request = 0;           // ... p: predicated bounce-back loads
+    int zp_request = 0;           // ... q: two z nodes at a time on packed FP32x2
     int block_request = 0, minb_request = 0;
     double *partial = nullptr, *norms = nullptr;
     int nslots = 0;
@@ -294,6 +295,7 @@ struct TunedKnobs {
     bool pred, pair;
     int minb;
     bool hspace;
+    bool zpair;
     int zwalk;
 };
 static std::mutex g_tuned_mutex;
@@ -324,6 +326,7 @@ static int setup_jit(lbm_handle_s *H, const HostArray<uint32_t> &word, bool pair
         k.block = H->block_request;
     if (k.hspace && H->minb_request > 1) k.minb = H->minb_request;
     if (k.hspace && H->hb_request) k.hint = 1;
+    if (k.hspace && H->zp_request && k.zwalk > 1 && k.zwalk % 2 == 0) k.zpair = true;
     {
         std::lock_guard<std::mutex> lock(g_tuned_mutex);
         auto it = g_tuned.find(tune_key(k));
@@ -337,6 +340,7 @@ static int setup_jit(lbm_handle_s *H, const HostArray<uint32_t> &word, bool pair
             k.minb = it->second.minb;
             k.hspace = it->second.hspace;
             k.zwalk = it->second.zwalk;
+            k.zpair = it->second.zpair;
         }
     }
     std::string err;
@@ -447,6 +451,7 @@ int lbm_create(const lbm_lattice_desc *L, const lbm_params *P, lbm_handle *out) 
             if (const char *bp = strchr(kv, 'b')) b_env = atoi(bp + 1);
             if (const char *mp = strchr(kv + 5, 'm')) m_env = atoi(mp + 1);
             H->hb_request = strchr(kv + 5, 'p') ? 1 : 0;
+            H->zp_request = strchr(kv + 5, 'q') ? 1 : 0;
         }
         H->block_request = b_env;
         H->minb_request = m_env;
@@ -1111,6 +1116,10 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
                             {64, 1, 0, 0, 20, 1, 8},   {64, 1, 0, 0, 20, 1, 4}, {128, 1, 0, 0, 10, 1, 8},
                             {128, 1, 0, 0, 12, 1, 8}};
             vs.insert(vs.end(), hz, hz + 14);
+            // two z nodes at a time on FP32x2 (zw + 100 marks them below)
+            const V zp[] = {{64, 0, 0, 0, 10, 1, 108}, {64, 0, 0, 0, 8, 1, 108}, {128, 0, 0, 0, 5, 1, 108},
+                            {64, 1, 0, 0, 10, 1, 108}, {64, 0, 0, 0, 10, 1, 104}, {128, 0, 0, 0, 4, 1, 108}};
+            vs.insert(vs.end(), zp, zp + 6);
         }
     }
     if (H->n % 2 == 0 && hs_ok && !one_node_boundaries(H->P, H->q)) {
@@ -1127,7 +1136,8 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
         k.pair = v.pair != 0;
         k.minb = v.minb;
         k.hspace = v.hs != 0;
-        k.zwalk = v.zw;
+        k.zwalk = v.zw > 100 ? v.zw - 100 : v.zw;
+        k.zpair = v.zw > 100;
         cand.push_back(k);
     }
     std::vector<cudaKernel_t> fn(cand.size(), nullptr);
@@ -1198,12 +1208,14 @@ int lbm_autotune(lbm_handle H, int trial_steps, int *block, int *hint, int *pred
         std::lock_guard<std::mutex> lock(g_tuned_mutex);
         g_tuned[tune_key(H->jit_key)] = TunedKnobs{H->jit_key.block, H->jit_key.hint, H->jit_key.pred,
                                                    H->jit_key.pair, H->jit_key.minb, H->jit_key.hspace,
-                                                   H->jit_key.zwalk};
+                                                   H->jit_key.zpair, H->jit_key.zwalk};
     }
     H->initialised = false;  // the trial steps leave the populations undefined
     if (block) *block = H->jit_key.block;
     if (hint) *hint = H->jit_key.hint | (H->jit_key.hspace ? 2 : 0) | (H->jit_key.zwalk > 1 ? H->jit_key.zwalk << 2 : 0);
-    if (pred) *pred = (H->jit_key.pred ? 1 : 0) | (H->jit_key.pair ? 2 : 0) | (H->jit_key.minb > 1 ? H->jit_key.minb << 2 : 0);
+    if (pred)
+        *pred = (H->jit_key.pred ? 1 : 0) | (H->jit_key.pair ? 2 : 0) | (H->jit_key.minb > 1 ? H->jit_key.minb << 2 : 0) |
+                (H->jit_key.zpair ? 1 << 10 : 0);
     return LBM_OK;
 }
 
@@ -1216,17 +1228,19 @@ int lbm_kernel_config(lbm_handle H, int *block, int *hint, int *pred) {
                               : 0;
     if (pred)
         *pred = H->jit_kernel ? (H->jit_key.pred ? 1 : 0) | (H->jit_key.pair ? 2 : 0) |
-                                    (H->jit_key.minb > 1 ? H->jit_key.minb << 2 : 0)
+                                    (H->jit_key.minb > 1 ? H->jit_key.minb << 2 : 0) | (H->jit_key.zpair ? 1 << 10 : 0)
                               : 0;
     return LBM_OK;
 }
 
 int lbm_jit_check(int q, int coll, int storage, int phys, int wrap, int nx, int ny, int nz, int block, int hint,
                   int pred) {
+    const int minb = (pred >> 2) & 255;
     JitStepKey k{q, coll, storage, phys != 0, wrap != 0, nx, ny, nz, block, hint & 1, (pred & 1) != 0, true,
-                 (pred & 2) != 0, (pred >> 2) > 1 ? (pred >> 2) : 1};
+                 (pred & 2) != 0, minb > 1 ? minb : 1};
     k.hspace = (hint & 2) != 0;
     k.zwalk = k.hspace && (hint >> 2) > 1 ? hint >> 2 : 1;
+    k.zpair = k.hspace && ((pred >> 10) & 1) && k.zwalk % 2 == 0;
     std::string err;
     if (jit_step_kernel(k, nullptr, err)) return fail(LBM_ERR_CUDA, err);
     return LBM_OK;

@@ -41,7 +41,8 @@ int jit_step_kernel(const JitStepKey &k, cudaKernel_t *out, std::string &err) {
     const std::string expr =
         k.pair     ? "lbm::step_kernel_x2_fixed<" + common + ", " + minb + ">"
         : k.hspace ? "lbm::step_kernel_h_fixed<" + common + ", " + minb + (k.pred ? ", true" : ", false") + ", " +
-                         std::to_string(k.zwalk > 1 ? k.zwalk : 1) + ", " + std::to_string(k.hint & 1) + ">"
+                         std::to_string(k.zwalk > 1 ? k.zwalk : 1) + ", " + std::to_string(k.hint & 1) +
+                         (k.zpair && k.zwalk > 1 ? ", true" : ", false") + ">"
                    : "lbm::step_kernel_fixed<" + common + ", " + std::to_string(k.hint) + ", " +
                          (k.pred ? "true" : "false") + ", " + minb + ">";
     {

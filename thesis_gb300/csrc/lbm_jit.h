@@ -18,6 +18,7 @@ struct JitStepKey {
     int minb = 1;       // __launch_bounds__ minimum blocks per SM (1: no constraint)
     bool hspace = false;  // one node per thread in storage units (step_kernel_h_fixed)
     int zwalk = 1;        // storage units: nodes a thread updates along z (flag word loaded ahead)
+    bool zpair = false;   // storage units, zwalk even: two z nodes at a time on packed FP32x2
 };
 
 // Compile (or fetch from the process cache) step_kernel_fixed for `k` and

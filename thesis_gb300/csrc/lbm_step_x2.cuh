@@ -685,6 +685,113 @@ __device__ __forceinline__ void h_node_w(const StepParams &p, const G &g, int x,
 
 
 
+// Two nodes of one column, (x, y, z) and (x, y, z + 1), updated together:
+// each gathers by its own flag word (pull, or its own opposite population
+// across a blocked link), then moments and collision run on packed FP32x2
+// lanes (collide_x2 with f2), so one FFMA2 serves both nodes.  Neither node
+// may be a boundary-slot node (the caller takes the one-node path for a warp
+// that holds one).  A solid node loads nothing and stores its zero encoding,
+// as in h_node_w.
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, int HB>
+__device__ __forceinline__ void h_zpair_w(const StepParams &p, const G &g, int x, int y, int z, uint32_t w0,
+                                          uint32_t w1) {
+    using L = Lat<Q>;
+    using T = typename Store<ST>::T;
+    constexpr bool F16 = ST == LBM_STORE_F16S || ST == LBM_STORE_F16C;
+    const float sigma = p.sigma;
+    const float S = F16 ? p.scale : 1.f;
+    const float invS = F16 ? p.inv_scale : 1.f;
+    const bool in_row = x < g.nx;
+    const int row0 = y + g.ny * z;
+    const int node0 = x + g.nx * row0, node1 = node0 + g.nx * g.ny;
+    const int plane = g.pitch * g.ny;
+    const long long idx = x + (long long)g.pitch * row0;
+    const T *in0 = (const T *)p.fin[0] + idx;
+    const T *in1 = in0 + plane;
+    T *out0 = (T *)p.fout[0] + idx;
+    T *out1 = out0 + plane;
+    const bool fl0 = (w0 & W_FLUID) != 0, fl1 = (w1 & W_FLUID) != 0;
+    if (!__ballot_sync(0xffffffffu, fl0 || fl1)) return;  // a warp of solid nodes writes nothing
+    int oxm = -1, oxp = 1, oym = -g.pitch, oyp = g.pitch;
+    int ozm0 = -plane, ozp0 = plane, ozm1 = -plane, ozp1 = plane;
+    if (WRAP) {
+        oxm = x == 0 ? g.nx - 1 : -1;
+        oxp = x == g.nx - 1 ? 1 - g.nx : 1;
+        oym = y == 0 ? (g.ny - 1) * g.pitch : -g.pitch;
+        oyp = y == g.ny - 1 ? (1 - g.ny) * g.pitch : g.pitch;
+        // node 0 (at z < nz - 1) and node 1 (at z + 1 > 0) wrap on one side only
+        ozm0 = z == 0 ? (g.nz - 1) * plane : -plane;
+        ozp1 = z + 1 == g.nz - 1 ? (1 - g.nz) * plane : plane;
+    }
+    auto raw = [](const T *q) -> float { return h_raw<ST>(q); };
+    f2 h[Q];
+    {
+        const float a0 = fl0 ? raw(in0) : 0.f, a1 = fl1 ? raw(in1) : 0.f;
+        h[0] = f2(a0, a1);
+    }
+#pragma unroll
+    for (int d = 1; d < Q; ++d) {
+        const int pxy = d * g.nx + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
+                        (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0));
+        const int pull0 = pxy + (L::cz(d) == 1 ? ozm0 : (L::cz(d) == -1 ? ozp0 : 0));
+        const int pull1 = pxy + (L::cz(d) == 1 ? ozm1 : (L::cz(d) == -1 ? ozp1 : 0));
+        const int own = (PHYS ? L::opp(d) : d) * g.nx;
+        float a0 = 0.f, a1 = 0.f;
+        if constexpr (HB == 1) {
+            if (fl0) {
+                if ((w0 >> d) & 1u) a0 = raw(in0 + own);
+                else a0 = raw(in0 + pull0);
+            }
+            if (fl1) {
+                if ((w1 >> d) & 1u) a1 = raw(in1 + own);
+                else a1 = raw(in1 + pull1);
+            }
+        } else {
+            if (fl0) a0 = raw(in0 + (((w0 >> d) & 1u) ? own : pull0));
+            if (fl1) a1 = raw(in1 + (((w1 >> d) & 1u) ? own : pull1));
+        }
+        h[d] = f2(a0, a1);
+    }
+    f2 sum = h[0], jx = 0.f, jy = 0.f, jz = 0.f;
+#pragma unroll
+    for (int d = 1; d < Q; ++d) {
+        sum += h[d];
+        if (L::cx(d) == 1) jx += h[d]; else if (L::cx(d) == -1) jx -= h[d];
+        if (L::cy(d) == 1) jy += h[d]; else if (L::cy(d) == -1) jy -= h[d];
+        if (L::cz(d) == 1) jz += h[d]; else if (L::cz(d) == -1) jz -= h[d];
+    }
+    const f2 rms = sum * f2(invS);
+    const f2 rho = rms + f2(sigma);
+    // a solid lane's rho is sigma + 0 = 1 (F16S/F32 shifted) or 0 (unshifted);
+    // guard the reciprocal, its results are discarded
+    const float r0 = fl0 ? rho.v.x : 1.f, r1 = fl1 ? rho.v.y : 1.f;
+    const f2 sc(invS / r0, invS / r1);
+    const f2 ux = fma2(jx, sc, f2((float)p.gshift)), uy = jy * sc, uz = jz * sc;
+    if (p.write_macro) {
+        if (fl0) {
+            p.rho[node0] = rho.v.x;
+            p.ux[node0] = ux.v.x;
+            p.uy[node0] = uy.v.x;
+            p.uz[node0] = uz.v.x;
+        }
+        if (fl1) {
+            p.rho[node1] = rho.v.y;
+            p.ux[node1] = ux.v.y;
+            p.uy[node1] = uy.v.y;
+            p.uz[node1] = uz.v.y;
+        }
+    }
+    collide_x2<Q, COLL, PHYS>(h, rho, rms, ux, uy, uz, p, sigma, S);
+    if (in_row) {
+#pragma unroll
+        for (int d = 0; d < Q; ++d) {
+            const float zero = -sigma * p.shift[d] * S;
+            h_put<ST>(out0 + d * g.nx, fl0 ? h[d].v.x : zero);
+            h_put<ST>(out1 + d * g.nx, fl1 ? h[d].v.y : zero);
+        }
+    }
+}
+
 // One node: its flag word, then the update.
 template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC = false, bool MERGE = true, int HB = 0>
 __device__ __forceinline__ void h_node(const StepParams &p, const G &g, int x, int y, int z) {
@@ -706,13 +813,36 @@ __global__ void __launch_bounds__(STEP_BLOCK) step_kernel_h(const StepParams p) 
 // loads at fixed offsets, predicated on the link's flag bit, instead of one
 // load from an address selected per direction.
 template <int Q, int COLL, int ST, bool PHYS, bool WRAP, int NX, int NY, int NZ, int BLOCK, int MINB, bool SPEC = false,
-          int ZW = 1, int HB = 0>
+          int ZW = 1, int HB = 0, bool ZP = false>
 __global__ void __launch_bounds__(BLOCK, MINB) step_kernel_h_fixed(const StepParams p) {
     using G = FixedGeom<NX, NY, NZ, Q * NX>;
     const G g;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if constexpr (ZW == 1) {
         h_node<Q, COLL, ST, PHYS, WRAP, G, SPEC, true, HB>(p, g, x, blockIdx.y, blockIdx.z);
+    } else if constexpr (ZP) {
+        // ZP: the column's nodes two at a time on packed FP32x2 (h_zpair_w);
+        // a warp holding a boundary-slot node takes the one-node path
+        const int y = blockIdx.y, z0 = blockIdx.z * ZW;
+        const bool in_row = x < NX;
+        auto flag = [&](int z) -> uint32_t { return in_row && z < NZ ? __ldg(p.word + x + NX * (y + NY * z)) : 0u; };
+        uint32_t wa = flag(z0), wb = flag(z0 + 1);
+#pragma unroll 1
+        for (int k = 0; k < ZW; k += 2) {
+            const int z = z0 + k;
+            if (z >= NZ) break;  // the same z for every thread of the block
+            const bool two = k + 1 < ZW && z + 1 < NZ;
+            const uint32_t wc = k + 2 < ZW ? flag(z + 2) : 0u, wd = k + 3 < ZW ? flag(z + 3) : 0u;
+            const bool special = __any_sync(0xffffffffu, ((wa | (two ? wb : 0u)) & W_SPECIAL) != 0);
+            if (two && !special) {
+                h_zpair_w<Q, COLL, ST, PHYS, WRAP, G, HB>(p, g, x, y, z, wa, wb);
+            } else {
+                h_node_w<Q, COLL, ST, PHYS, WRAP, G, SPEC, true, HB>(p, g, x, y, z, wa);
+                if (two) h_node_w<Q, COLL, ST, PHYS, WRAP, G, SPEC, true, HB>(p, g, x, y, z + 1, wb);
+            }
+            wa = wc;
+            wb = wd;
+        }
     } else {
         const int y = blockIdx.y, z0 = blockIdx.z * ZW;
         const bool in_row = x < NX;
