@@ -64,10 +64,18 @@ def parse():
                          "lid-driven cavities of uneven sizes, batched vs one by one; cg: colour-gradient "
                          "static droplets on a periodic 1024^2 lattice (Laplace law); warmstart: time to the "
                          "steady-state tolerance of D2Q9 TRT channels from a U-Net prediction vs from rest")
-    ap.add_argument("--ws-train", type=int, default=2048, help="training channels (steady fields from the solver)")
-    ap.add_argument("--ws-epochs", type=int, default=150)
-    ap.add_argument("--ws-eval", type=int, default=128, help="held-out channels timed cold and warm")
-    ap.add_argument("--ws-levels", type=int, default=5, help="U-Net pooling levels")
+    ap.add_argument("--ws-train", type=int, default=4096, help="training channels (steady fields from the solver)")
+    ap.add_argument("--ws-epochs", type=int, default=20)
+    ap.add_argument("--ws-eval", type=int, default=256, help="held-out channels timed cold and warm")
+    ap.add_argument("--ws-levels", type=int, default=4, help="U-Net pooling levels")
+    ap.add_argument("--ws-base", type=int, default=32, help="U-Net channels at level 0 (widths min(base 2^l, 64))")
+    ap.add_argument("--ws-n", type=int, default=1024)
+    ap.add_argument("--ws-m", type=int, default=256)
+    ap.add_argument("--ws-re-max", type=float, default=200.0)
+    ap.add_argument("--ws-tol", type=float, default=1e-6, help="residual tolerance of the timed solves")
+    ap.add_argument("--ws-train-tol", type=float, default=1e-4, help="residual tolerance of the training fields")
+    ap.add_argument("--ws-max-steps", type=int, default=400000)
+    ap.add_argument("--ws-ref-steps", type=int, default=600000)
     ap.add_argument("--prec-steps", default="5000,50000", help="precision: checkpoints (steps) of the duct runs")
     ap.add_argument("--prec-storages", default="f32,f16s,f16c", help="precision: storages compared with f64")
     ap.add_argument("--prec-cavity-steps", type=int, default=20000)
@@ -790,25 +798,30 @@ def run_cg3d(args):
 
 
 def run_warmstart(args):
-    """Learned warm start: steady fields of seeded 256x64 channels from the
-    batched solver train the U-Net on the GPU; held-out channels are then
-    solved to the residual tolerance from rest and from the prediction."""
+    """Learned warm start: steady fields of seeded n x m channels (default
+    1024 x 256, Re 20-200) from the batched solver train the U-Net on the GPU;
+    held-out channels are then solved to the residual tolerance (default
+    1e-6) from rest and from the prediction."""
     from thesis_gb300 import build as native_build
     from thesis_gb300 import warmstart as ws
     native_build.build()
-    n, m = 256, 64
+    n, m = args.ws_n, args.ws_m
+    re_range = (20.0, args.ws_re_max)
     t0 = time.perf_counter()
-    X, Y, Wt, dsteps, dres, dsecs = ws.dataset(range(args.ws_train), n, m)
-    conv = dres <= ws.TOL
+    X, Y, Wt, dsteps, dres, dsecs = ws.dataset(range(args.ws_train), n, m, re_range=re_range, tol=args.ws_train_tol,
+                                               max_steps=args.ws_max_steps)
+    conv = dres <= args.ws_train_tol
     t_data = time.perf_counter() - t0
-    net = ws.UNet(m, n, max_batch=32, seed=1, levels=args.ws_levels)
+    net = ws.UNet(m, n, max_batch=16, seed=1, levels=args.ws_levels, base_channels=args.ws_base)
     net.set_dataset(X[conv], Y[conv], Wt[conv])
+    del X, Y, Wt
     batch = 16
     t0 = time.perf_counter()
     hist = net.train(epochs=args.ws_epochs, batch=batch, lr=2e-3, lr_final=5e-5)
     t_train = time.perf_counter() - t0
     step_ms = float(np.median(net.step_ms[len(net.step_ms) // 2:]))
-    train_flops = 3.0 * ws.forward_flops(m, n, args.ws_levels) * batch  # forward + data and weight gradients
+    # forward + data and weight gradients
+    train_flops = 3.0 * ws.forward_flops(m, n, args.ws_levels, args.ws_base) * batch
     achieved = train_flops / (step_ms / 1e3) / 1e12
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -819,18 +832,20 @@ def run_warmstart(args):
     seeds = range(100000, 100000 + args.ws_eval)
     clocks = ClockSampler(0)
     clocks.start()
-    warm_cap = int(2 * dsteps[conv].max())  # warm runs beyond it fall back to the cold start
-    r = ws.compare(net, seeds, n, m, warm_max_steps=warm_cap)
+    tol = args.ws_tol
+    r = ws.compare(net, seeds, n, m, tol=tol, max_steps=args.ws_max_steps, warm_max_steps=args.ws_max_steps,
+                   re_range=re_range)
+    warm_cap = args.ws_max_steps
     clk = clocks.stop()
-    ok = (r["cold_res"] <= ws.TOL) & (r["warm_res"] <= ws.TOL)
+    ok = (r["cold_res"] <= tol) & (r["warm_res"] <= tol)
     perr = []
     for d, lat in enumerate(r["lats"]):
         fl = lat.node_type == 1
         ur = r["cold_fields"][d][1][fl]
         perr.append(float(np.linalg.norm(r["init"][d][1][fl] - ur) / np.linalg.norm(ur)))
-    # converged-field error of both starts against 300k-step runs of 16 channels
+    # converged-field error of both starts against long runs of 16 channels
     k = min(16, len(r["lats"]))
-    ref = ws.solve_batch(r["lats"][:k], r["re"][:k], None, tol=1e-12, max_steps=300_000)[4]
+    ref = ws.solve_batch(r["lats"][:k], r["re"][:k], None, tol=1e-12, max_steps=args.ws_ref_steps)[4]
     ec, ew = [], []
     for d in range(k):
         fl = r["lats"][d].node_type == 1
@@ -858,22 +873,25 @@ def run_warmstart(args):
         assert res_c.rc == 0
         glups = int((lat.node_type == 1).sum()) * steps / dt / 1e9
         cpu = {"value": cold_updates / (glups * 1e9), "unit": "s", "cores": L.orc_threads(), "kind": "port",
-               "sample": "oracle restatement (FP32, OpenMP) of one 256x64 TRT channel from rest, %d steps in "
+               "sample": "oracle restatement (FP32, OpenMP) of one %dx%d TRT channel from rest, %d steps in "
                          "%.1f s = %.4f GLUPS; value = the cold solves' %d fluid-node updates at that rate"
-                         % (steps, dt, glups, int(cold_updates))}
-    line = {"metric": "wall time to a 1e-5 steady-state residual, %d held-out 256x64 D2Q9 TRT channels "
-                      "(Re 20-100), U-Net warm start including its prediction" % len(r["lats"]),
+                         % (n, m, steps, dt, glups, int(cold_updates))}
+    line = {"metric": "wall time to a %g steady-state residual, %d held-out %dx%d D2Q9 TRT channels "
+                      "(Re %g-%g), U-Net warm start including its prediction"
+                      % (tol, len(r["lats"]), n, m, re_range[0], re_range[1]),
             "value": r["warm_total_seconds"], "unit": "s", "n_gpus": 1, "steps": int(r["warm_steps"].sum()),
             "warmup": 0, "ms_per_step": None, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 solver, bf16 network",
             "data": "synthetic (seeded channel geometries and Reynolds numbers)",
-            "config": {"workload": "256x64 D2Q9 TRT channels, 1-6 obstacles, parabolic inlet u_max 0.05, "
-                                   "pressure outlet, Re uniform in [20, 100], residual every 100 steps, "
-                                   "tolerance 1e-5, one batch of all channels per start",
-                       "unet": {"levels": args.ws_levels, "params": net.num_params, "train_channels": int(conv.sum()),
+            "config": {"workload": "%dx%d D2Q9 TRT channels, 1-6 obstacles, parabolic inlet u_max 0.05, "
+                                   "pressure outlet, Re uniform in [%g, %g], residual every 100 steps, "
+                                   "tolerance %g (training targets %g), one batch of all channels per start"
+                                   % (n, m, re_range[0], re_range[1], tol, args.ws_train_tol),
+                       "unet": {"levels": args.ws_levels, "base_channels": args.ws_base, "params": net.num_params,
+                                "train_channels": int(conv.sum()), "data_channels": args.ws_train,
                                 "epochs": args.ws_epochs, "batch": batch},
-                       "l2_policy": "batch working set (%d x 16k nodes) below L2; timing is wall time "
-                                    "of whole solves" % len(r["lats"])},
+                       "l2_policy": "batch working set %d x %d nodes; timing is wall time of whole solves"
+                                    % (len(r["lats"]), n * m)},
             "cold_seconds": r["cold_total_seconds"], "warm_seconds": r["warm_total_seconds"],
             "speedup": r["cold_total_seconds"] / r["warm_total_seconds"],
             "iteration_seconds": {"cold": r["cold_seconds"], "warm": r["warm_seconds"],
@@ -884,10 +902,10 @@ def run_warmstart(args):
                                    "warm_median": float(np.median(r["warm_steps"])),
                                    "warm_over_cold_sum": float(r["warm_steps"][ok].sum() / r["cold_steps"][ok].sum()),
                                    "warm_with_fallbacks_over_cold_sum": float(
-                                       (r["warm_steps"] + np.where(r["warm_res"] <= ws.TOL, 0, r["cold_steps"])).sum()
+                                       (r["warm_steps"] + np.where(r["warm_res"] <= tol, 0, r["cold_steps"])).sum()
                                        / r["cold_steps"].sum())},
             "prediction_error_u": {"median": float(np.median(perr)), "p90": float(np.percentile(perr, 90))},
-            "converged_field_error_vs_300k_step_runs": {"channels": k, "cold_median": float(np.median(ec)),
+            "converged_field_error_vs_long_runs": {"channels": k, "steps": args.ws_ref_steps, "cold_median": float(np.median(ec)),
                                                         "warm_median": float(np.median(ew)),
                                                         "cold_max": float(max(ec)), "warm_max": float(max(ew))},
             "training": {"data_seconds": t_data, "data_solve_seconds": dsecs, "train_seconds": t_train,

