@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--cpu-sample", default="64,64,128", help="n,m,h of the CPU-baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="target CPU time of one CPU-baseline sample (steps are chosen to fill it)")
-    ap.add_argument("--workload", default="duct", choices=["duct", "cavities", "cg", "cg3d", "warmstart", "precision"],
+    ap.add_argument("--workload", default="duct", choices=["duct", "cavities", "cg", "cg3d", "warmstart", "precision", "unet"],
                     help="duct: the D3Q19 MRT sphere-packed duct (default); cavities: a batch of D2Q9 MRT "
                          "lid-driven cavities of uneven sizes, batched vs one by one; cg: colour-gradient "
                          "static droplets on a periodic 1024^2 lattice (Laplace law); warmstart: time to the "
@@ -117,13 +117,13 @@ def workload_config(args, n, m, h):
             "lattice": [n, m, h], "collision": "MRT", "storage": args.storage,
             "boundaries": "Zou-He pressure z faces, half-way bounce-back",
             "l2_policy": "inputs larger than L2 (population buffers 2 x %.2f GB vs 129 MB L2)"
-                         % (19 * n * m * h * B_LU[STORAGE_NAMES[args.storage]] / 76 * 2 / 2 / 1e9)}
+                         % (19 * n * m * h * (B_LU[STORAGE_NAMES[args.storage]] // 38) / 1e9)}
 
 
 LATTICE_IO = {}
 
 
-def make_lattice(n, m, h, seed):
+def make_lattice(n, m, h, seed, record=True):
     """The duct's lattice as a run reads it: the library's emitter writes the
     sphere packing as reference-format Node and BC files
     (lbm_emit_sphere_duct), the library's readers load them
@@ -145,8 +145,9 @@ def make_lattice(n, m, h, seed):
         t1 = time.perf_counter()
         lat = lattice.from_files_native(node, bc)
         t2 = time.perf_counter()
-        LATTICE_IO.update(emit_seconds=t1 - t0, read_seconds=t2 - t1, spheres=int(k.value),
-                          node_file_bytes=os.path.getsize(node), bc_file_bytes=os.path.getsize(bc))
+        if record:
+            LATTICE_IO.update(emit_seconds=t1 - t0, read_seconds=t2 - t1, spheres=int(k.value),
+                              node_file_bytes=os.path.getsize(node), bc_file_bytes=os.path.getsize(bc))
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
     return lat
@@ -270,7 +271,7 @@ def cpu_baseline_run(sample, seconds, threads=None):
         L.orc_set_threads(int(threads))
     nthreads = L.orc_threads()
     n, m, h = sample
-    lat = make_lattice(n, m, h, 0)
+    lat = make_lattice(n, m, h, 0, record=False)
     kw = dict(viscosity=(WORKLOAD["tau"] - 0.5) / 3.0, collision_model=3, inlet_profile=4, outlet_profile=5)
     nn = lat.num_nodes
     init = (np.ones(nn), np.zeros(nn), np.zeros(nn), np.zeros(nn))
@@ -440,6 +441,65 @@ def run_precision(args):
             "config": dict(workload_config(args, n, m, h), storage="f64 reference vs " + ",".join(stores[1:])),
             "duct": duct, "cavity_centrelines": cavity, "cylinder_drag": cylinder,
             "run_seconds": seconds, "gpu_launches": None}
+    print(json.dumps(line))
+    return 0
+
+
+def run_unet(args):
+    """U-Net training throughput on synthetic channel-sized data: Adam steps
+    of the stated network (levels, base channels) on batches of m x n images,
+    with the 3x3 convolutions of 32+ outputs on tcgen05 and, for comparison,
+    all on mma.sync (THESIS_UNET_TC=0); TFLOP/s of the forward and both
+    gradients against the measured BF16 peak."""
+    from thesis_gb300 import build as native_build
+    from thesis_gb300 import warmstart as ws
+    native_build.build()
+    n, m, B = args.ws_n, args.ws_m, 16
+    rng = np.random.default_rng(0)
+    count = 2 * B
+    x = rng.standard_normal((count, m, n, ws.IN_CHANNELS)).astype(np.float32)
+    t = rng.standard_normal((count, m, n, ws.OUT_CHANNELS)).astype(np.float32)
+    w = np.ones((count, m, n), np.float32)
+    flops = 3.0 * ws.forward_flops(m, n, args.ws_levels, args.ws_base) * B
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak_tf, peak_kind = float(json.load(f)["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        peak_tf, peak_kind = 1900.0, "fallback"
+    out = {}
+    clk = None
+    for tc in ("1", "0"):
+        os.environ["THESIS_UNET_TC"] = tc
+        with ws.UNet(m, n, max_batch=B, seed=1, levels=args.ws_levels, base_channels=args.ws_base) as net:
+            net.set_dataset(x, t, w)
+            idx = np.arange(B)
+            for _ in range(max(args.warmup, 3)):
+                net.train_step(idx, 1e-4)
+            if tc == "1":
+                clocks = ClockSampler(0)
+                clocks.start()
+            ms = []
+            for k in range(args.steps):
+                net.train_step((idx + k * B) % count, 1e-4)
+                ms.append(net.last_ms)
+            if tc == "1":
+                clk = clocks.stop()
+        med = float(np.median(ms))
+        out[tc] = {"step_ms": med, "tflops": flops / (med / 1e3) / 1e12}
+    os.environ.pop("THESIS_UNET_TC", None)
+    a = out["1"]["tflops"]
+    line = {"metric": "U-Net training TFLOP/s (BF16 tensor cores, FP32 accumulate), batch of %d %dx%d images"
+                      % (B, m, n),
+            "value": a, "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": out["1"]["step_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 (fp32 accumulate)", "data": "synthetic (random inputs and targets)",
+            "config": {"workload": "U-Net %d levels, base %d channels (widths min(base 2^l, 64)), %dx%d images, "
+                                   "batch %d, Adam" % (args.ws_levels, args.ws_base, m, n, B),
+                       "flops_per_step": flops, "l2_policy": "activations of a batch (GBs) exceed L2"},
+            "mma_sync_only": out["0"], "tcgen05_over_mma_sync": out["0"]["step_ms"] / out["1"]["step_ms"],
+            "roofline": {"bound": "tensor", "achieved": a, "peak": peak_tf, "unit": "TFLOP/s", "frac": a / peak_tf,
+                         "peak_kind": peak_kind, "traffic": None},
+            "clocks": clk, "gpu_launches": None}
     print(json.dumps(line))
     return 0
 
@@ -909,6 +969,8 @@ def run_warmstart(args):
                                                         "warm_median": float(np.median(ew)),
                                                         "cold_max": float(max(ec)), "warm_max": float(max(ew))},
             "training": {"data_seconds": t_data, "data_solve_seconds": dsecs, "train_seconds": t_train,
+                         "data_steps_median": float(np.median(dsteps)), "data_steps_max": int(np.max(dsteps)),
+                         "data_converged": int(conv.sum()),
                          "step_ms": step_ms, "loss_first": float(hist[0]), "loss_last": float(hist[-1]),
                          "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
                                       "frac": achieved / peak_tf, "peak_kind": peak_kind,
@@ -935,6 +997,8 @@ def main():
         return run_cavities(args)
     if args.workload == "precision" and args.impl != "reference":
         return run_precision(args)
+    if args.workload == "unet" and args.impl != "reference":
+        return run_unet(args)
     rank, world, local = dist_info()
     if args.impl == "reference":
         return run_reference_arm(args, rank, world)
