@@ -72,6 +72,7 @@ def parse():
     ap.add_argument("--ws-n", type=int, default=1024)
     ap.add_argument("--ws-m", type=int, default=256)
     ap.add_argument("--ws-re-max", type=float, default=200.0)
+    ap.add_argument("--unet-batch", type=int, default=16, help="unet: images per training step")
     ap.add_argument("--ws-tol", type=float, default=1e-6, help="residual tolerance of the timed solves")
     ap.add_argument("--ws-train-tol", type=float, default=1e-4, help="residual tolerance of the training fields")
     ap.add_argument("--ws-max-steps", type=int, default=400000)
@@ -454,7 +455,7 @@ def run_unet(args):
     from thesis_gb300 import build as native_build
     from thesis_gb300 import warmstart as ws
     native_build.build()
-    n, m, B = args.ws_n, args.ws_m, 16
+    n, m, B = args.ws_n, args.ws_m, args.unet_batch
     rng = np.random.default_rng(0)
     count = 2 * B
     x = rng.standard_normal((count, m, n, ws.IN_CHANNELS)).astype(np.float32)

@@ -104,7 +104,7 @@ def test_gpu_training_reduces_loss_and_fits_a_field():
 @pytest.mark.gpu
 @pytest.mark.parametrize("levels,base", [(3, 16), (4, 32)])
 def test_gpu_tcgen05_convolutions_match_mma_sync(monkeypatch, levels, base):
-    """The tcgen05 convolutions (32 and 64 output channels: accumulator in
+    """The tcgen05 convolutions (16 to 128 output channels: accumulator in
     tensor memory) against the mma.sync ones (THESIS_UNET_TC=0) on the same
     parameters and inputs: predictions and parameter gradients agree to the
     FP32 accumulation order, far inside the oracle tolerances; and the
@@ -135,3 +135,32 @@ def test_gpu_tcgen05_convolutions_match_mma_sync(monkeypatch, levels, base):
         nb = np.linalg.norm(b)
         if nb > 0:
             assert np.linalg.norm(a - b) <= 3e-2 * nb, (k, np.linalg.norm(a - b) / nb)
+
+
+@pytest.mark.gpu
+def test_gpu_tcgen05_persistent_tiles_match_mma_sync(monkeypatch):
+    """At 4 x 64 x 1024 every level-0 convolution has 2,048 row tiles of 128
+    pixels, so each persistent tcgen05 CTA walks many tiles through both
+    input stages and both tensor-memory accumulators, and the 128-channel
+    decoder inputs take several chunks per tile.  Predictions and every
+    layer's parameter gradient agree with the mma.sync kernels."""
+    from thesis_gb300.warmstart import UNet
+    B, H, W, ic, oc, levels, base = 4, 64, 1024, 4, 3, 4, 32
+    x, t, w = _problem(B, H, W, ic, oc, 17)
+    p = uo.init_params(ic, oc, 19, levels, base)
+    res = {}
+    for tc in ("1", "0"):
+        monkeypatch.setenv("THESIS_UNET_TC", tc)
+        with UNet(H, W, max_batch=B, in_channels=ic, out_channels=oc, levels=levels, base_channels=base) as net:
+            net.set_params(p)
+            net.set_dataset(x, t, w)
+            g, loss = net.gradients(list(range(B)))
+            res[tc] = (net.predict(x), g, loss)
+    (p1, g1, l1), (p0, g0, l0) = res["1"], res["0"]
+    perr = np.abs(p1 - p0).max() / np.abs(p0).max()
+    print("persistent tcgen05 vs mma.sync: prediction %.2e, loss %.4e / %.4e" % (perr, l1, l0))
+    assert perr < 2e-2 and abs(l1 - l0) <= 1e-3 * l0
+    for k, s in enumerate(_layer_slices(levels, base)):
+        a, b = g1[s].astype(np.float64), g0[s].astype(np.float64)
+        nb = np.linalg.norm(b)
+        assert nb > 0 and np.linalg.norm(a - b) <= 3e-2 * nb, (k, np.linalg.norm(a - b) / nb)

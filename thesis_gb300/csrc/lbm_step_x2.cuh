@@ -479,43 +479,46 @@ __device__ __forceinline__ void pair_node(const StepParams &p, const G &g, int x
 // type f1): no decode or encode per population and moments from deviations.
 // The update of one fluid node in storage units: gather (pull or bounce
 // back), boundary conditions, moments, collision; h receives the new state.
-template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC, int HB = 0>
-__device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x, int node, uint32_t w,
-                                         const typename Store<ST>::T *in, f1 (&h)[Q],
-                                         const float (&spec_pull)[SPEC ? Q : 1], const float (&spec_own)[SPEC ? Q : 1],
-                                         int oxm, int oxp, int oym, int oyp, int ozm,
-                                         int ozp) {
+// The node's populations after streaming, in storage units: direction d
+// pulls from the upstream neighbour, or, across a link the flag word marks
+// blocked (bit d), takes the node's own population (its opposite in physics
+// mode: half-way bounce-back).
+template <int Q, int ST, bool PHYS, class G, int HB = 0>
+__device__ __forceinline__ void h_gather(const G &g, uint32_t w, const typename Store<ST>::T *in, f1 (&h)[Q], int oxm,
+                                         int oxp, int oym, int oyp, int ozm, int ozp) {
+    using L = Lat<Q>;
+    using T = typename Store<ST>::T;
+    auto raw = [](const T *q) -> float { return h_raw<ST>(q); };
+    h[0] = raw(in);
+#pragma unroll
+    for (int d = 1; d < Q; ++d) {
+        const int pull = d * g.nx + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
+                         (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
+                         (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
+        const int own = (PHYS ? L::opp(d) : d) * g.nx;
+        if constexpr (HB == 1) {
+            // two exclusive loads at fixed offsets instead of an address
+            // selected per direction
+            float v;
+            if ((w >> d) & 1u) v = raw(in + own);
+            else v = raw(in + pull);
+            h[d] = v;
+        } else {
+            h[d] = raw(in + (((w >> d) & 1u) ? own : pull));
+        }
+    }
+}
+
+// Boundary closures, moments, the macroscopic store and the collision of a
+// fluid node whose streamed populations are in h (storage units).
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G>
+__device__ __forceinline__ void h_finish(const StepParams &p, const G &g, int node, uint32_t w, f1 (&h)[Q]) {
     using L = Lat<Q>;
     using T = typename Store<ST>::T;
     constexpr bool F16 = ST == LBM_STORE_F16S || ST == LBM_STORE_F16C;
     const float sigma = p.sigma;
     const float S = F16 ? p.scale : 1.f;
     const float invS = F16 ? p.inv_scale : 1.f;
-    auto raw = [](const T *q) -> float { return h_raw<ST>(q); };
-    if constexpr (SPEC) {
-        h[0] = spec_pull[0];
-#pragma unroll
-        for (int d = 1; d < Q; ++d) h[d] = ((w >> d) & 1u) ? spec_own[d] : spec_pull[d];
-    } else {
-        h[0] = raw(in);
-#pragma unroll
-        for (int d = 1; d < Q; ++d) {
-            const int pull = d * g.nx + (L::cx(d) == 1 ? oxm : (L::cx(d) == -1 ? oxp : 0)) +
-                             (L::cy(d) == 1 ? oym : (L::cy(d) == -1 ? oyp : 0)) +
-                             (L::cz(d) == 1 ? ozm : (L::cz(d) == -1 ? ozp : 0));
-            const int own = (PHYS ? L::opp(d) : d) * g.nx;
-            if constexpr (HB == 1) {
-                // two exclusive loads at fixed offsets instead of an address
-                // selected per direction
-                float v;
-                if ((w >> d) & 1u) v = raw(in + own);
-                else v = raw(in + pull);
-                h[d] = v;
-            } else {
-                h[d] = raw(in + (((w >> d) & 1u) ? own : pull));
-            }
-        }
-    }
     bool keep = false, zv = false;
     if constexpr (PHYS) {
         // physics-mode faces and moving walls stay in storage units: the
@@ -595,6 +598,22 @@ __device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x,
         p.uz[node] = uz.v;
     }
     collide_x2<Q, COLL, PHYS>(h, rho, rms, ux, uy, uz, p, sigma, S);
+}
+
+template <int Q, int COLL, int ST, bool PHYS, bool WRAP, class G, bool SPEC, int HB = 0>
+__device__ __forceinline__ void h_update(const StepParams &p, const G &g, int x, int node, uint32_t w,
+                                         const typename Store<ST>::T *in, f1 (&h)[Q],
+                                         const float (&spec_pull)[SPEC ? Q : 1], const float (&spec_own)[SPEC ? Q : 1],
+                                         int oxm, int oxp, int oym, int oyp, int ozm,
+                                         int ozp) {
+    if constexpr (SPEC) {
+        h[0] = spec_pull[0];
+#pragma unroll
+        for (int d = 1; d < Q; ++d) h[d] = ((w >> d) & 1u) ? spec_own[d] : spec_pull[d];
+    } else {
+        h_gather<Q, ST, PHYS, G, HB>(g, w, in, h, oxm, oxp, oym, oyp, ozm, ozp);
+    }
+    h_finish<Q, COLL, ST, PHYS, WRAP, G>(p, g, node, w, h);
 }
 
 // SPEC: the pull values (guarded by the node's coordinates, not its flag

@@ -14,8 +14,11 @@
 // gradient is a GEMM over pixels (M = cout, N = cin, K = pixels): each block
 // owns one tap, stages pixel-major tiles of the output gradient and of the
 // shifted input row, and adds its FP32 partial sums atomically.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+#include <stdio.h>
 #include <math.h>
 #include <stdlib.h>
 #include <stdint.h>
@@ -218,83 +221,129 @@ __global__ void __launch_bounds__(128) wgrad_kernel(const bf16 *__restrict__ dpr
     }
 }
 
-// db[co] += sum_p dpre[p][co]
-__global__ void bias_grad_kernel(const bf16 *__restrict__ dpre, int cout, long long npix, float *__restrict__ db) {
-    const int co = threadIdx.x % cout, lane_set = threadIdx.x / cout, sets = blockDim.x / cout;
-    float s = 0.f;
-    for (long long p = (long long)blockIdx.x * sets + lane_set; p < npix; p += (long long)gridDim.x * sets)
-        s += __bfloat162float(dpre[p * cout + co]);
-    if (lane_set < sets) atomicAdd(db + co, s);
+// Elementwise kernels work on 8 channels (16 bytes) per thread: every
+// channel count, channel stride and channel offset of the activations is a
+// multiple of 8, and the index arithmetic stays in 32 bits (a batch holds
+// fewer than 2^31 channel groups; lbm_unet_create checks it).
+struct V8 {
+    float v[8];
+};
+__device__ __forceinline__ V8 ld8(const bf16 *p) {
+    const uint4 r = __ldg((const uint4 *)p);
+    const __nv_bfloat162 *h = (const __nv_bfloat162 *)&r;
+    V8 o;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float2 f = __bfloat1622float2(h[k]);
+        o.v[2 * k] = f.x;
+        o.v[2 * k + 1] = f.y;
+    }
+    return o;
+}
+__device__ __forceinline__ void st8(bf16 *p, const V8 &a) {
+    uint4 r;
+    __nv_bfloat162 *h = (__nv_bfloat162 *)&r;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) h[k] = __floats2bfloat162_rn(a.v[2 * k], a.v[2 * k + 1]);
+    *(uint4 *)p = r;
+}
+
+// db[co] += sum_p dpre[p][co]: thread t sums channel group t % G of pixels
+// t / G, t / G + 256 / G, ...; the block adds its partial sums per channel
+__global__ void __launch_bounds__(256) bias_grad_kernel(const bf16 *__restrict__ dpre, int cout, int npix,
+                                                        float *__restrict__ db) {
+    __shared__ float part[256][9];
+    const int G = cout / 8, t = threadIdx.x, v = t % G, sets = 256 / G;
+    V8 s;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s.v[k] = 0.f;
+    for (int p = blockIdx.x * sets + t / G; p < npix; p += gridDim.x * sets) {
+        const V8 a = ld8(dpre + (size_t)p * cout + 8 * v);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) s.v[k] += a.v[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) part[t][k] = s.v[k];
+    __syncthreads();
+    if (t < cout) {
+        float a = 0.f;
+        for (int q = t / 8; q < 256; q += G) a += part[q][t % 8];
+        atomicAdd(db + t, a);
+    }
 }
 
 // 2x2 average pooling: out[n, y, x, c] = mean of in[n, 2y+i, 2x+j, c]
 __global__ void pool_kernel(const bf16 *in, int in_cs, int in_co, bf16 *out, int C, int B, int Ho, int Wo) {
-    const long long total = (long long)B * Ho * Wo * C;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long p = i / C;
-        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho), n = (int)(p / ((long long)Wo * Ho));
+    const int G = C / 8, total = B * Ho * Wo * G;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int g = i % G, p = i / G, x = p % Wo, ny = p / Wo, y = ny % Ho, n = ny / Ho;
         const int Wi = 2 * Wo;
-        const size_t b = (((size_t)n * 2 * Ho + 2 * y) * Wi + 2 * x) * in_cs + in_co + c;
-        const float s = __bfloat162float(in[b]) + __bfloat162float(in[b + in_cs]) +
-                        __bfloat162float(in[b + (size_t)Wi * in_cs]) + __bfloat162float(in[b + (size_t)Wi * in_cs + in_cs]);
-        out[i] = __float2bfloat16(0.25f * s);
+        const size_t b = (((size_t)n * 2 * Ho + 2 * y) * Wi + 2 * x) * in_cs + in_co + 8 * g;
+        const V8 a = ld8(in + b), c = ld8(in + b + in_cs), d = ld8(in + b + (size_t)Wi * in_cs),
+                 e = ld8(in + b + (size_t)Wi * in_cs + in_cs);
+        V8 o;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) o.v[k] = 0.25f * (a.v[k] + c.v[k] + d.v[k] + e.v[k]);
+        st8(out + (size_t)i * 8, o);
     }
 }
 
 // nearest x2 upsampling into channels [out_co, out_co + C) of out
 __global__ void up_kernel(const bf16 *in, int C, bf16 *out, int out_cs, int out_co, int B, int Ho, int Wo) {
-    const long long total = (long long)B * Ho * Wo * C;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long p = i / C;
-        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho), n = (int)(p / ((long long)Wo * Ho));
+    const int G = C / 8, total = B * Ho * Wo * G;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int g = i % G, p = i / G, x = p % Wo, ny = p / Wo, y = ny % Ho, n = ny / Ho;
         const int Hi = Ho / 2, Wi = Wo / 2;
-        out[p * out_cs + out_co + c] = in[(((size_t)n * Hi + y / 2) * Wi + x / 2) * C + c];
+        *(uint4 *)(out + (size_t)p * out_cs + out_co + 8 * g) =
+            __ldg((const uint4 *)(in + (((size_t)n * Hi + y / 2) * Wi + x / 2) * C + 8 * g));
     }
 }
 
 // dpre[p][c] = g[p][c] * (act[p][c] > 0)
 __global__ void relu_bwd_kernel(const bf16 *g, int g_cs, int g_co, const bf16 *act, int a_cs, int a_co, bf16 *dpre,
-                                int C, long long npix) {
-    const long long total = npix * C;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long p = i / C;
-        const float a = __bfloat162float(act[p * a_cs + a_co + c]);
-        dpre[i] = a > 0.f ? g[p * g_cs + g_co + c] : __float2bfloat16(0.f);
+                                int C, int npix) {
+    const int G = C / 8, total = npix * G;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int v = i % G, p = i / G;
+        const V8 a = ld8(act + (size_t)p * a_cs + a_co + 8 * v);
+        V8 o = ld8(g + (size_t)p * g_cs + g_co + 8 * v);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) o.v[k] = a.v[k] > 0.f ? o.v[k] : 0.f;
+        st8(dpre + (size_t)i * 8, o);
     }
 }
 
 // dpre = (pool gradient + skip gradient) masked by ReLU, at full resolution
 __global__ void pool_skip_bwd_kernel(const bf16 *gpool, const bf16 *gskip, int s_cs, int s_co, const bf16 *act,
                                      int a_cs, int a_co, bf16 *dpre, int C, int B, int H, int W) {
-    const long long total = (long long)B * H * W * C;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long p = i / C;
-        const int x = (int)(p % W), y = (int)((p / W) % H), n = (int)(p / ((long long)W * H));
-        const float gp = __bfloat162float(gpool[(((size_t)n * (H / 2) + y / 2) * (W / 2) + x / 2) * C + c]);
-        const float gs = __bfloat162float(gskip[p * s_cs + s_co + c]);
-        const float a = __bfloat162float(act[p * a_cs + a_co + c]);
-        dpre[i] = __float2bfloat16(a > 0.f ? 0.25f * gp + gs : 0.f);
+    const int G = C / 8, total = B * H * W * G;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int v = i % G, p = i / G, x = p % W, ny = p / W, y = ny % H, n = ny / H;
+        const V8 gp = ld8(gpool + (((size_t)n * (H / 2) + y / 2) * (W / 2) + x / 2) * C + 8 * v);
+        const V8 gs = ld8(gskip + (size_t)p * s_cs + s_co + 8 * v);
+        const V8 a = ld8(act + (size_t)p * a_cs + a_co + 8 * v);
+        V8 o;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) o.v[k] = a.v[k] > 0.f ? 0.25f * gp.v[k] + gs.v[k] : 0.f;
+        st8(dpre + (size_t)i * 8, o);
     }
 }
 
 // dpre at low resolution = sum of the 2x2 upsampled gradient, masked by ReLU
 __global__ void up_bwd_kernel(const bf16 *gup, int g_cs, int g_co, const bf16 *act, bf16 *dpre, int C, int B, int H,
                               int W) {
-    const long long total = (long long)B * H * W * C;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long p = i / C;
-        const int x = (int)(p % W), y = (int)((p / W) % H), n = (int)(p / ((long long)W * H));
+    const int G = C / 8, total = B * H * W * G;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int v = i % G, p = i / G, x = p % W, ny = p / W, y = ny % H, n = ny / H;
         const int W2 = 2 * W;
-        const size_t b = (((size_t)n * 2 * H + 2 * y) * W2 + 2 * x) * g_cs + g_co + c;
-        const float s = __bfloat162float(gup[b]) + __bfloat162float(gup[b + g_cs]) +
-                        __bfloat162float(gup[b + (size_t)W2 * g_cs]) +
-                        __bfloat162float(gup[b + (size_t)W2 * g_cs + g_cs]);
-        dpre[i] = __float2bfloat16(__bfloat162float(act[i]) > 0.f ? s : 0.f);
+        const size_t b = (((size_t)n * 2 * H + 2 * y) * W2 + 2 * x) * g_cs + g_co + 8 * v;
+        const V8 a = ld8(gup + b), c = ld8(gup + b + g_cs), d = ld8(gup + b + (size_t)W2 * g_cs),
+                 e = ld8(gup + b + (size_t)W2 * g_cs + g_cs);
+        const V8 m = ld8(act + (size_t)i * 8);
+        V8 o;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) o.v[k] = m.v[k] > 0.f ? a.v[k] + c.v[k] + d.v[k] + e.v[k] : 0.f;
+        st8(dpre + (size_t)i * 8, o);
     }
 }
 
@@ -324,15 +373,19 @@ __global__ void loss_kernel(const float *pred, int pc, const float *tgt, int oc,
 
 // output gradient of the weighted MSE, BF16, pc channels (the unused ones 0)
 __global__ void loss_grad_kernel(const float *pred, int pc, const float *tgt, int oc, const float *wt,
-                                 long long npix, const double *sums, bf16 *dout) {
-    const double norm = sums[1] > 0 ? 2.0 / (oc * sums[1]) : 0.0;
-    const long long total = npix * pc;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % pc);
-        const long long p = i / pc;
-        float v = 0.f;
-        if (c < oc) v = (float)(norm * wt[p] * (pred[i] - tgt[p * oc + c]));
-        dout[i] = __float2bfloat16(v);
+                                 int npix, const double *sums, bf16 *dout) {
+    const float norm = sums[1] > 0 ? (float)(2.0 / (oc * sums[1])) : 0.f;
+    const int G = pc / 8, total = npix * G;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int v = i % G, p = i / G;
+        const float wp = norm * wt[p];
+        V8 o;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int c = 8 * v + k;
+            o.v[k] = c < oc ? wp * (pred[(size_t)i * 8 + k] - tgt[(size_t)p * oc + c]) : 0.f;
+        }
+        st8(dout + (size_t)i * 8, o);
     }
 }
 
@@ -400,7 +453,8 @@ struct lbm_unet_s {
     lbm_unet_config cfg;
     int levels = 3;
     int base = 16, cap = 64;   // channel widths c_l = min(base * 2^l, cap)
-    bool tc = true;            // 3x3 convolutions with 32..256 outputs on tcgen05 (unet_tc.cuh)
+    bool tc = true;            // 3x3 convolutions with 16..128 outputs on tcgen05 (unet_tc.cuh)
+    int sms = 1, smem_optin = 0;  // the device's SM count and opt-in shared memory per block
     int *tc_err = nullptr;     // set by a tensor-core kernel whose bounded wait gave up
     cudaStream_t stream = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -471,6 +525,45 @@ Act view(const Act &a, int co, int C) {
     return v;
 }
 
+// The driver's tensor-map encoder, through the runtime (no -lcuda).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        cudaDriverEntryPointQueryResult q;
+        void *p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+// Tensor map of C channels of an NHWC BF16 tensor (channel stride cs, base
+// at its first channel): dims (channel, x, y, image), boxes of box_c
+// channels x box_x pixels x box_y rows, swizzled by the box's row bytes
+// (128, 64 or 32: 64, 32 or 16 channels); out-of-image elements read zero.
+bool nhwc_tensor_map(CUtensorMap *m, const bf16 *p, int C, int cs, int H, int W, int B, int box_c, int box_x,
+                     int box_y) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t pcs = (cuuint64_t)cs * sizeof(bf16);
+    const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    const cuuint64_t strides[3] = {pcs, pcs * W, pcs * W * H};
+    const cuuint32_t box[4] = {(cuuint32_t)box_c, (cuuint32_t)box_x, (cuuint32_t)box_y, 1}, es[4] = {1, 1, 1, 1};
+    const CUtensorMapSwizzle sw = box_c == 64 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                              : (box_c == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)p, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// the convolution's input rows: chunk channels x TC_BOX pixels x 3 rows
+bool act_tensor_map(CUtensorMap *m, const Act &a, int cin, int chunk, int H, int W, int B) {
+    return nhwc_tensor_map(m, a.p + a.co, cin, a.cs, H, W, B, chunk, unet_tc::TC_BOX, 3);
+}
+
 void conv(lbm_unet_s *u, const Layer &l, const Act &in, const Act &out, const float *bias, float *out32, int B,
           int level, bool transposed) {
     const int H = H_of(u, level), W = W_of(u, level);
@@ -479,30 +572,39 @@ void conv(lbm_unet_s *u, const Layer &l, const Act &in, const Act &out, const fl
     const int cin = transposed ? l.cout : l.cin, cout = transposed ? l.cin : l.cout;
     const int relu = transposed ? 0 : l.relu;
     bf16 *op = out.p;
-    if (u->tc && (cout == 32 || cout == 64 || cout == 128 || cout == 256)) {
-        const dim3 tg((W + unet_tc::TC_M - 1) / unet_tc::TC_M, H, B);
-#define TC_CASE(CO, CH)                                                                                       \
-    case CO: {                                                                                                \
-        constexpr int bytes = unet_tc::TcSmem<CO, CH>::BYTES;                                                 \
-        static bool attr = false;                                                                             \
-        if (!attr) {                                                                                          \
-            cudaFuncSetAttribute(unet_tc::conv3x3_tc_kernel<CO, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                 bytes);                                                                      \
-            attr = true;                                                                                      \
-        }                                                                                                     \
-        unet_tc::conv3x3_tc_kernel<CO, CH><<<tg, 128, bytes, u->stream>>>(in.p, in.cs, in.co, cin, w, bias, op,  \
-                                                                         out.cs, out.co, out32, H, W, relu,  \
-                                                                         u->tc_err);                          \
-        return;                                                                                               \
+    if (u->tc && (cout == 16 || cout == 32 || cout == 64 || cout == 128) && cin % 16 == 0) {
+        // persistent tensor-core kernel, the layer's weights resident in
+        // shared memory, input rows by tensor copies: the widest chunk of
+        // input channels (and the most stages) that fits
+        const long long tiles = (long long)B * H * ((W + unet_tc::TC_M - 1) / unet_tc::TC_M);
+        int launched = 0;
+#define TC_TRY(CO, CH, NS)                                                                                      \
+    if (!launched && cout == CO && cin % CH == 0 &&                                                              \
+        unet_tc::TcSmem<CO, CH, NS>::bytes(cin) <= (size_t)u->smem_optin) {                                      \
+        CUtensorMap map;                                                                                        \
+        if (!act_tensor_map(&map, in, cin, CH, H, W, B)) {                                                       \
+            fprintf(stderr, "thesis_unet: tensor map encoding failed; convolutions fall back to mma.sync\n");   \
+            u->tc = false;                                                                                      \
+            launched = -1;                                                                                      \
+        } else {                                                                                                \
+            auto kern = unet_tc::conv3x3_tc_kernel<CO, CH, NS>;                                                 \
+            const int bytes = (int)unet_tc::TcSmem<CO, CH, NS>::bytes(cin);                                     \
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);                     \
+            int per_sm = 1;                                                                                     \
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 160, bytes);                           \
+            const int tmem_cap = 512 / (2 * CO < 32 ? 32 : 2 * CO);                                             \
+            per_sm = per_sm < 1 ? 1 : (per_sm > tmem_cap ? tmem_cap : per_sm);                                  \
+            const long long g = (long long)u->sms * per_sm < tiles ? (long long)u->sms * per_sm : tiles;         \
+            kern<<<(unsigned)g, 160, bytes, u->stream>>>(map, cin, w, bias, op, out.cs, out.co, out32, B, H, W,  \
+                                                         relu, u->tc_err);                                      \
+            launched = 1;                                                                                       \
+        }                                                                                                       \
     }
-        switch (cout) {
-            TC_CASE(32, 64)
-            TC_CASE(64, 64)
-            TC_CASE(128, 64)
-            TC_CASE(256, 32)
-        default: break;
-        }
-#undef TC_CASE
+#define TC_SHAPES(CO) TC_TRY(CO, 64, 3) TC_TRY(CO, 32, 3) TC_TRY(CO, 32, 2) TC_TRY(CO, 16, 4) TC_TRY(CO, 16, 2)
+        TC_SHAPES(16) TC_SHAPES(32) TC_SHAPES(64) TC_SHAPES(128)
+#undef TC_SHAPES
+#undef TC_TRY
+        if (launched == 1) return;
     }
     switch (cout) {
     case 16: conv3x3_kernel<16><<<grid, 128, 0, u->stream>>>(in.p, in.cs, in.co, cin, w, bias, op, out.cs, out.co, out32, H, W, relu); break;
@@ -513,11 +615,56 @@ void conv(lbm_unet_s *u, const Layer &l, const Act &in, const Act &out, const fl
     }
 }
 
+// persistent tensor-core weight gradient (unet_tc.cuh); false when the
+// layer's shape has no instance
+bool wgrad_tc(lbm_unet_s *u, const Layer &l, const Act &in, int B, int H, int W, float *dw) {
+    const int nc = l.cin < 64 ? l.cin : 64;
+    if (l.cin % nc) return false;
+    const long long units = (long long)B * H * ((W + unet_tc::TC_M - 1) / unet_tc::TC_M);
+    CUtensorMap tdp, tin;
+    if (!nhwc_tensor_map(&tdp, u->dpre, l.cout, l.cout, H, W, B, l.cout, unet_tc::TC_M, 3) ||
+        !nhwc_tensor_map(&tin, in.p + in.co, l.cin, in.cs, H, W, B, nc, unet_tc::TC_BOX, 1)) {
+        fprintf(stderr, "thesis_unet: tensor map encoding failed; weight gradients fall back to mma.sync\n");
+        u->tc = false;
+        return false;
+    }
+    bool done = false;
+#define WG_TC(CO, NC, NS)                                                                                      \
+    if (!done && l.cout == CO && nc == NC && unet_tc::WgSmem<CO, NC, NS>::BYTES <= u->smem_optin) {            \
+        using SM = unet_tc::WgSmem<CO, NC, NS>;                                                                \
+        auto kern = unet_tc::wgrad_tc_kernel<CO, NC, NS>;                                                      \
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SM::BYTES);                     \
+        int per_sm = 1;                                                                                        \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, SM::BYTES);                          \
+        const int tmem_cap = 512 / (int)SM::COLS;                                                              \
+        per_sm = per_sm < 1 ? 1 : (per_sm > tmem_cap ? tmem_cap : per_sm);                                     \
+        const int split = l.cin / NC;                                                                          \
+        long long g = ((long long)u->sms * per_sm + split - 1) / split;                                        \
+        /* at least 8 rows per CTA: each CTA ends with 9 x CO x NC reductions */                               \
+        g = g < (units + 7) / 8 ? g : (units + 7) / 8;                                                         \
+        kern<<<dim3((unsigned)g, split), 128, SM::BYTES, u->stream>>>(tdp, tin, l.cin, dw, B, H, W, u->tc_err); \
+        done = true;                                                                                           \
+    }
+#define WG_SHAPES(CO, NC) WG_TC(CO, NC, 4) WG_TC(CO, NC, 3) WG_TC(CO, NC, 2)
+    WG_SHAPES(16, 16) WG_SHAPES(16, 32) WG_SHAPES(16, 64)
+    WG_SHAPES(32, 16) WG_SHAPES(32, 32) WG_SHAPES(32, 64)
+    WG_SHAPES(64, 16) WG_SHAPES(64, 32) WG_SHAPES(64, 64)
+#undef WG_SHAPES
+#undef WG_TC
+    return done;
+}
+
 void wgrad(lbm_unet_s *u, const Layer &l, const Act &in, int B, int level) {
     const int H = H_of(u, level), W = W_of(u, level);
     const long long rows = (long long)B * H * ((W + TILE_X - 1) / TILE_X);
     dim3 grid((unsigned)(rows < 64 ? rows : 64), 9);
     float *dw = u->grad + l.w_off;
+    const long long npix = (long long)B * H * W;
+    if (u->tc && l.cin % 16 == 0 && wgrad_tc(u, l, in, B, H, W, dw)) {
+        bias_grad_kernel<<<grid_for(npix * (l.cout / 8), 256), 256, 0, u->stream>>>(u->dpre, l.cout, (int)npix,
+                                                                                 u->grad + l.b_off);
+        return;
+    }
 #define WG(CO, CI)                                                                                            \
     if (l.cout == CO && l.cin == CI) {                                                                        \
         wgrad_kernel<CO, CI><<<grid, 128, 0, u->stream>>>(u->dpre, in.p, in.cs, in.co, dw, B, H, W);         \
@@ -526,8 +673,8 @@ void wgrad(lbm_unet_s *u, const Layer &l, const Act &in, int B, int level) {
         ufail(LBM_ERR_INVALID, "no weight-gradient kernel for this layer shape");
     }
 #undef WG
-    const long long npix = (long long)B * H * W;
-    bias_grad_kernel<<<grid_for(npix, 256), 256, 0, u->stream>>>(u->dpre, l.cout, npix, u->grad + l.b_off);
+    bias_grad_kernel<<<grid_for(npix * (l.cout / 8), 256), 256, 0, u->stream>>>(u->dpre, l.cout, (int)npix,
+                                                                                 u->grad + l.b_off);
 }
 
 void refresh_weights(lbm_unet_s *u) {
@@ -550,7 +697,7 @@ void forward(lbm_unet_s *u, int B) {
         const Act skip = view(u->cat[l], ch_up(u, l), ch(u, l));
         cv(enc_b(l), u->e_a[l], skip, l);
         const long long n = (long long)B * H_of(u, l + 1) * W_of(u, l + 1) * ch(u, l);
-        pool_kernel<<<grid_for(n), 256, 0, u->stream>>>(skip.p, skip.cs, skip.co, u->p[l].p, ch(u, l), B,
+        pool_kernel<<<grid_for(n / 8), 256, 0, u->stream>>>(skip.p, skip.cs, skip.co, u->p[l].p, ch(u, l), B,
                                                           H_of(u, l + 1), W_of(u, l + 1));
         x = u->p[l];
     }
@@ -559,7 +706,7 @@ void forward(lbm_unet_s *u, int B) {
     Act prev = u->bb;
     for (int l = NL - 1; l >= 0; --l) {
         const long long n = (long long)B * H_of(u, l) * W_of(u, l) * prev.C;
-        up_kernel<<<grid_for(n), 256, 0, u->stream>>>(prev.p, prev.C, u->cat[l].p, u->cat[l].cs, 0, B, H_of(u, l),
+        up_kernel<<<grid_for(n / 8), 256, 0, u->stream>>>(prev.p, prev.C, u->cat[l].p, u->cat[l].cs, 0, B, H_of(u, l),
                                                         W_of(u, l));
         cv(dec_a(u, l), u->cat[l], u->d_a[l], l);
         cv(dec_b(u, l), u->d_a[l], u->d_b[l], l);
@@ -584,18 +731,18 @@ void backward(lbm_unet_s *u, int B) {
     };
     auto relu_bwd = [&](const Act &g, const Act &act, int C, int lev) {
         const long long n = npix(lev) * C;
-        relu_bwd_kernel<<<grid_for(n), 256, 0, u->stream>>>(g.p, g.cs, g.co, act.p, act.cs, act.co, u->dpre, C,
-                                                              npix(lev));
+        relu_bwd_kernel<<<grid_for(n / 8), 256, 0, u->stream>>>(g.p, g.cs, g.co, act.p, act.cs, act.co, u->dpre, C,
+                                                                  (int)npix(lev));
     };
     auto pool_skip = [&](const Act &gpool, const Act &gskip, const Act &act, int C, int lev) {
         const long long n = npix(lev) * C;
-        pool_skip_bwd_kernel<<<grid_for(n), 256, 0, u->stream>>>(gpool.p, gskip.p, gskip.cs, gskip.co, act.p,
+        pool_skip_bwd_kernel<<<grid_for(n / 8), 256, 0, u->stream>>>(gpool.p, gskip.p, gskip.cs, gskip.co, act.p,
                                                                    act.cs, act.co, u->dpre, C, B, H_of(u, lev),
                                                                    W_of(u, lev));
     };
     auto up_bwd = [&](const Act &gup, const Act &act, int C, int lev) {
         const long long n = npix(lev) * C;
-        up_bwd_kernel<<<grid_for(n), 256, 0, u->stream>>>(gup.p, gup.cs, gup.co, act.p, u->dpre, C, B, H_of(u, lev),
+        up_bwd_kernel<<<grid_for(n / 8), 256, 0, u->stream>>>(gup.p, gup.cs, gup.co, act.p, u->dpre, C, B, H_of(u, lev),
                                                             W_of(u, lev));
     };
     // output layer: dpre = dout
@@ -637,8 +784,8 @@ void loss(lbm_unet_s *u, int B) {
     const long long np = (long long)B * u->cfg.height * u->cfg.width;
     cudaMemsetAsync(u->sums, 0, 2 * sizeof(double), u->stream);
     loss_kernel<<<grid_for(np), 256, 0, u->stream>>>(u->out32, 16, u->tgt, u->cfg.out_channels, u->wt, np, u->sums);
-    loss_grad_kernel<<<grid_for(np * 16), 256, 0, u->stream>>>(u->out32, 16, u->tgt, u->cfg.out_channels, u->wt, np,
-                                                                u->sums, u->dout);
+    loss_grad_kernel<<<grid_for(np * 2), 256, 0, u->stream>>>(u->out32, 16, u->tgt, u->cfg.out_channels, u->wt,
+                                                               (int)np, u->sums, u->dout);
 }
 
 int gather_batch(lbm_unet_s *u, int batch, const int *idx) {
@@ -696,6 +843,9 @@ int lbm_unet_create(const lbm_unet_config *cfg, lbm_unet *out) {
     if (cfg->in_channels < 1 || cfg->in_channels > 16 || cfg->out_channels < 1 || cfg->out_channels > 16)
         return ufail(LBM_ERR_INVALID, "in_channels and out_channels must be 1..16");
     if (cfg->max_batch < 1) return ufail(LBM_ERR_INVALID, "max_batch must be positive");
+    // the elementwise kernels index 8-channel groups of a batch in 32 bits
+    if ((long long)cfg->max_batch * cfg->height * cfg->width * 16 >= (1ll << 31))
+        return ufail(LBM_ERR_INVALID, "max_batch x height x width must stay below 2^27 pixels");
     const int base = cfg->base_channels ? cfg->base_channels : 16, cap = cfg->max_channels ? cfg->max_channels : 64;
     if ((base != 16 && base != 32) || cap != 64)
         return ufail(LBM_ERR_INVALID, "base_channels must be 16 or 32 and max_channels 64");
@@ -706,6 +856,13 @@ int lbm_unet_create(const lbm_unet_config *cfg, lbm_unet *out) {
     u->cap = cap;
     const char *tce = getenv("THESIS_UNET_TC");
     u->tc = !(tce && strcmp(tce, "0") == 0);
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&u->sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&u->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (u->sms < 1) u->sms = 1;
+    }
     if (cudaStreamCreateWithFlags(&u->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&u->e0) != cudaSuccess || cudaEventCreate(&u->e1) != cudaSuccess) {
         lbm_unet_destroy(u);
