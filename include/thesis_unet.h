@@ -17,10 +17,10 @@
  * channels of which the first out_channels are used (4L + 3 convolutions).
  * Activations are NHWC BF16 with channels padded to multiples of 16, weights
  * BF16 copies of FP32 master weights, accumulation FP32 on the tensor cores:
- * hand-written tcgen05.mma kernels with the accumulator in tensor memory for
- * the forward and data-gradient convolutions with 32..256 outputs
- * (THESIS_UNET_TC=0 selects the mma.sync form instead), mma.sync.m16n8k16
- * for 16-output convolutions and the weight gradients; Adam in FP32.
+ * hand-written tcgen05.mma kernels with the accumulators in tensor memory and
+ * the input rows staged by tensor copies (cp.async.bulk.tensor) for every
+ * forward, data-gradient and weight-gradient convolution (THESIS_UNET_TC=0
+ * selects the mma.sync.m16n8k16 kernels instead); Adam in FP32.
  *
  * Conventions as in thesis_lbm.h: status codes (LBM_OK ...), caller-owned
  * host buffers, device buffers owned by the handle, one handle per thread.

@@ -592,7 +592,8 @@ void conv(lbm_unet_s *u, const Layer &l, const Act &in, const Act &out, const fl
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);                     \
             int per_sm = 1;                                                                                     \
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 160, bytes);                           \
-            const int tmem_cap = 512 / (2 * CO < 32 ? 32 : 2 * CO);                                             \
+            constexpr int cols = unet_tc::TcSmem<CO, CH, NS>::NA * CO;                                          \
+            const int tmem_cap = 512 / (cols < 32 ? 32 : cols);                                                 \
             per_sm = per_sm < 1 ? 1 : (per_sm > tmem_cap ? tmem_cap : per_sm);                                  \
             const long long g = (long long)u->sms * per_sm < tiles ? (long long)u->sms * per_sm : tiles;         \
             kern<<<(unsigned)g, 160, bytes, u->stream>>>(map, cin, w, bias, op, out.cs, out.co, out32, B, H, W,  \

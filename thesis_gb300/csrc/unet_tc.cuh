@@ -1,38 +1,38 @@
-// 3x3 convolution as an implicit GEMM on the fifth-generation tensor cores
-// (tcgen05.mma, accumulator in tensor memory), for sm_100-class GPUs.
+// 3x3 convolutions of the warm-start U-Net on the fifth-generation tensor
+// cores (tcgen05.mma, accumulators in tensor memory, operands staged by
+// tensor copies), for sm_100-class GPUs.
+//
+// Forward and data gradient (conv3x3_tc_kernel):
 //
 //   out[n, y, x0+m, co] = act(bias[co] + sum_{tap, ci} w[tap][co][ci] in[n, y+ky-1, x0+m+kx-1, ci])
 //
 // A tile is TC_M = 128 consecutive pixels of one image row: the GEMM's M.
 // N = COUT output channels (16, 32, 64 or 128), K = 9 taps x cin, taken CHUNK
-// input channels at a time.  The kernel is persistent: each CTA (4 warps)
-// walks tiles blockIdx.x, blockIdx.x + gridDim.x, ... and keeps in shared
-// memory
-//   B  every weight of the layer (9 taps x cin x COUT), loaded once, and
-//   A  two stages of input rows: the three rows a tile's taps read, 130
-//      pixels (one-pixel halo) x CHUNK channels,
-// both in the K-major "no swizzle" layout of the tensor cores' shared-memory
-// descriptors: core matrices of 8 rows x 16 bytes (8 BF16 along K) stored as
-// 128 contiguous bytes.  Rows (pixels, output channels) are 16 bytes apart,
-// and the 8-channel groups of K are whole planes apart:
-//   A byte (row r, group j, pixel p) = ((r * KG + j) * NP + p) * 16
-//   B byte (tap t, group j, chan co) = ((t * KGall + j) * COUT + co) * 16
-// so a core matrix starts at any pixel, and the tap's x shift kx is a start
-// address kx * 16 bytes further: one A stage serves all nine taps.  The
-// descriptor's leading byte offset (between the two 8-channel groups of one
-// K = 16 instruction) is a plane, NP * 16 or COUT * 16 bytes; its stride
-// byte offset (between 8-row groups along M or N) is 128 bytes.
+// (16, 32 or 64) input channels at a time; a job is one (tile, chunk).  The
+// kernel is persistent: CTA b walks tiles b, b + gridDim.x, ...  Shared
+// memory holds
+//   B  every weight of the layer (9 taps x cin x COUT), loaded once, in the
+//      K-major no-swizzle layout: core matrices of 8 rows x 16 bytes stored
+//      as 128 contiguous bytes, byte ((t * KGall + j) * COUT + co) * 16 for
+//      tap t, 8-channel group j, output channel co;
+//   A  NS stages of input rows: one tensor copy per job brings the three
+//      rows the taps read, TC_BOX = 136 pixels from x0 - 1 (zero fill outside
+//      the image) x CHUNK channels, as K-major rows of 2 x CHUNK bytes with
+//      the tensor copy's 128-, 64- or 32-byte swizzle.
+// The tap's x shift kx is a start address kx rows further inside the same
+// staged row: the hardware applies the swizzle to absolute shared-memory
+// address bits, so a start moved by whole rows (or by 32 bytes for the next
+// K = 16) reads the right elements with the descriptor's base offset 0.
 //
-// A job is one (tile, chunk).  All 128 threads copy job j + 1's rows with
-// cp.async (zero fill at the image edges) while the tensor cores run job j;
-// one thread issues a job's 9 x CHUNK/16 MMAs (M = 128, N = COUT, K = 16,
-// BF16 in, FP32 accumulate) and commits them to the stage's mbarrier.  Tiles
-// alternate between two TMEM accumulators, so the epilogue of tile k (each
-// warp reads its 32 TMEM lanes = 32 pixels, adds the bias, applies ReLU and
-// stores BF16, and FP32 if asked) runs while tile k + 1's MMAs do.  Every
-// wait is bounded: a wait that gives up sets *err, the CTA stops issuing,
-// waits (bounded) for its MMAs and copies in flight, frees its tensor memory
-// and returns.
+// Warp 4 (one thread) issues the copies and each job's 9 x CHUNK/16 MMAs
+// (M = 128, N = COUT, K = 16, BF16 in, FP32 accumulate); warps 0-3 read
+// finished tiles from NA tensor-memory accumulators (each warp its 32 lanes =
+// 32 pixels), add the bias, apply ReLU and store BF16 (and FP32 if asked),
+// while the next tiles accumulate.  Every wait is bounded: a wait that gives
+// up sets *err, both roles stop, the copies and MMAs in flight finish, the
+// tensor memory is freed and the kernel returns.
+//
+// Weight gradient (wgrad_tc_kernel): see its comment below.
 #pragma once
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -158,10 +158,14 @@ constexpr int TC_BOX = 136;  // staged pixels per row: x0 - 1 .. x0 + 134, a who
 
 template <int COUT, int CHUNK, int NS>
 struct TcSmem {
+    // tensor-memory accumulators: a tile's MMAs wait for the epilogue of the
+    // tile NA before it, so NA tiles overlap one accumulator round trip
+    // (commit, epilogue, release); NA x COUT columns
+    static constexpr int NA = 4 * COUT <= 512 ? 4 : 2;
     static constexpr int ROWB = CHUNK * 2;
     static constexpr int A_STAGE = 3 * TC_BOX * ROWB;
     static constexpr size_t bytes(int cin) {
-        return 1024 + NS * (size_t)A_STAGE + 18 * (size_t)cin * COUT + 4 * COUT + 8 * (2 * NS + 4) + 16;
+        return 1024 + NS * (size_t)A_STAGE + 18 * (size_t)cin * COUT + 4 * COUT + 8 * (2 * NS + 2 * NA) + 16;
     }
 };
 
@@ -182,7 +186,8 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tin, int cin, const __nv_b
     using SM = TcSmem<COUT, CHUNK, NS>;
     constexpr int ROWB = SM::ROWB, KG = CHUNK / 8;
     constexpr uint32_t A_STAGE = SM::A_STAGE;
-    constexpr uint32_t COLS = 2 * COUT < 32 ? 32 : 2 * COUT;  // two accumulators (a power of two >= 32)
+    constexpr int NA = SM::NA;
+    constexpr uint32_t COLS = NA * COUT < 32 ? 32 : NA * COUT;  // a power of two >= 32
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw), base = (raw + 1023u) & ~1023u;
     unsigned char *smem = smem_raw + (base - raw);
@@ -191,8 +196,8 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tin, int cin, const __nv_b
     const uint32_t b_base = base + NS * A_STAGE;
     float *sbias = (float *)(smem + NS * A_STAGE + (size_t)18 * cin * COUT);
     uint64_t *bars = (uint64_t *)(sbias + COUT);
-    const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * NS, accf0 = empty0 + 8 * NS, acce0 = accf0 + 16;
-    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * NS + 4);
+    const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * NS, accf0 = empty0 + 8 * NS, acce0 = accf0 + 8 * NA;
+    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * NS + 2 * NA);
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
     const int xt = (W + TC_M - 1) / TC_M;
     const long long ntiles = (long long)B * H * xt;
@@ -210,7 +215,7 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tin, int cin, const __nv_b
             mbar_init(full0 + 8 * k, 1);
             mbar_init(empty0 + 8 * k, 1);
         }
-        for (int a = 0; a < 2; ++a) {
+        for (int a = 0; a < NA; ++a) {
             mbar_init(accf0 + 8 * a, 1);
             mbar_init(acce0 + 8 * a, 4);
         }
@@ -249,10 +254,10 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tin, int cin, const __nv_b
             for (; issued < jobs && issued < NS; ++issued) load(issued);
             for (long long j = 0; j < jobs && ok; ++j) {
                 const long long k = j / nch;
-                const int c = (int)(j % nch), s = (int)(j % NS), a = (int)(k & 1);
+                const int c = (int)(j % nch), s = (int)(j % NS), a = (int)(k % NA);
                 if (!mbar_wait(full0 + 8 * s, (uint32_t)((j / NS) & 1), abort_flag)) ok = false;
-                // the epilogue of tile k - 2 has read accumulator a
-                if (ok && c == 0 && k >= 2 && !mbar_wait(acce0 + 8 * a, (uint32_t)(((k >> 1) - 1) & 1), abort_flag))
+                // the epilogue of tile k - NA has read accumulator a
+                if (ok && c == 0 && k >= NA && !mbar_wait(acce0 + 8 * a, (uint32_t)((k / NA - 1) & 1), abort_flag))
                     ok = false;
                 if (!ok || *abort_flag) {
                     ok = false;
@@ -297,10 +302,10 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tin, int cin, const __nv_b
         }
         __syncwarp();
     } else {
-        // epilogue warps: tile k from accumulator k & 1
+        // epilogue warps: tile k from accumulator k % NA
         for (long long k = 0; k < my_tiles; ++k) {
-            const int a = (int)(k & 1);
-            const bool got = mbar_wait(accf0 + 8 * a, (uint32_t)((k >> 1) & 1), abort_flag);
+            const int a = (int)(k % NA);
+            const bool got = mbar_wait(accf0 + 8 * a, (uint32_t)((k / NA) & 1), abort_flag);
             if (!__all_sync(0xffffffffu, got)) {
                 ok = false;
                 break;

@@ -7,18 +7,16 @@ the plain LBM iterates them to the same residual tolerance as a cold start.
 The network's kernels (BF16 tensor cores) and the solver run in the CUDA
 library; this module builds features and targets and drives the two.
 
-Workload (a 256 x 64 version of the 1024 x 256 channel with the same
-proportions): D2Q9 TRT, walls at y = 0 and y = m-1 (half-way bounce-back),
-1-6 circles and rectangles, parabolic velocity inlet at x = 0 with centre-line
-velocity 0.05, pressure outlet rho = 1 at x = n-1, Re = 0.05 m / nu uniform
-in [20, 100], FP32 storage.  Residual: sqrt(sum |u - u_prev|^2) /
+Workload: n x m = 1024 x 256 channels (any size with the same proportions
+through size_scale), D2Q9 TRT, walls at y = 0 and y = m-1 (half-way
+bounce-back), 1-6 circles and rectangles, parabolic velocity inlet at x = 0
+with centre-line velocity 0.05, pressure outlet rho = 1 at x = n-1,
+Re = 0.05 m / nu uniform in [20, 200], FP32 storage with the collision in
+storage units (deviations from the rest state keep their digits, so a
+steady run reaches a 1e-6 residual).  Residual: sqrt(sum |u - u_prev|^2) /
 sqrt(sum |u|^2) over fluid nodes every 100 steps (lbm_batch_residuals),
-tolerance 1e-5.  Measured on this family: above Re ~ 110 the flows develop
-growing unsteady modes (the residual rises again after 100k steps), and with
-FP32 storage the steady flows settle at a residual of 1.5-3.5e-6 (rounding
-keeps the weakly damped acoustic modes between the velocity inlet and the
-pressure outlet excited; FP64 storage settles near 2e-7), so 1e-6 is out of
-reach in FP32 and 1e-5 is the tolerance every steady FP32 run meets.
+tolerance 1e-6; a run that has not met it after max_steps keeps its last
+residual (the warm-start bench lists such runs' Reynolds numbers).
 """
 import ctypes as C
 import time
