@@ -24,7 +24,9 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <algorithm>
 #include <array>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -455,6 +457,10 @@ struct lbm_unet_s {
     int base = 16, cap = 64;   // channel widths c_l = min(base * 2^l, cap)
     bool tc = true;            // 3x3 convolutions with 16..128 outputs on tcgen05 (unet_tc.cuh)
     int sms = 1, smem_optin = 0;  // the device's SM count and opt-in shared memory per block
+    size_t smem_per_sm = 0;       // shared memory per SM
+    // tensor-core configuration per layer shape (+-(cout * 4096 + cin) for
+    // convolutions / weight gradients): instance index and CTAs per SM
+    std::map<int, std::pair<int, int>> tc_choice;
     int *tc_err = nullptr;     // set by a tensor-core kernel whose bounded wait gave up
     cudaStream_t stream = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -525,6 +531,17 @@ Act view(const Act &a, int co, int C) {
     return v;
 }
 
+// Blocks of `threads` threads of a kernel that fit an SM by registers
+// (65,536 per SM, allocated per thread in multiples of 8) and by threads;
+// 1 when the attributes cannot be read.
+int resident_by_registers(const void *kern, int threads) {
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, kern) != cudaSuccess || a.numRegs <= 0) return 1;
+    const int regs = (a.numRegs + 7) / 8 * 8;
+    const int by_regs = 65536 / (regs * ((threads + 31) / 32 * 32));
+    return std::max(1, std::min(by_regs, 2048 / threads));
+}
+
 // The driver's tensor-map encoder, through the runtime (no -lcuda).
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -574,38 +591,92 @@ void conv(lbm_unet_s *u, const Layer &l, const Act &in, const Act &out, const fl
     bf16 *op = out.p;
     if (u->tc && (cout == 16 || cout == 32 || cout == 64 || cout == 128) && cin % 16 == 0) {
         // persistent tensor-core kernel, the layer's weights resident in
-        // shared memory, input rows by tensor copies: the widest chunk of
-        // input channels (and the most stages) that fits
+        // shared memory, input rows by tensor copies.  Each CTA is one
+        // pipeline whose jobs cost about the same whatever their size, and
+        // which needs two copies in flight to hide their latency, so the
+        // configuration (chunk of input channels, stages) maximises resident
+        // CTAs x chunk x min(stages - 1, 2), then resident CTAs, chunk and
+        // stages.  Measured on a
+        // 16 x 256 x 1024 batch: for 16 input channels three CTAs of 4 stages
+        // beat four of 2 stages 1.8x; for 32, three CTAs of 16-channel chunks
+        // beat one CTA of 32-channel chunks 1.6x, and with 64 outputs two
+        // CTAs of 2 stages beat one of 4 stages 1.3x; for 64, one CTA of one
+        // 64-channel chunk beat two CTAs of four 16-channel chunks 1.1x
         const long long tiles = (long long)B * H * ((W + unet_tc::TC_M - 1) / unet_tc::TC_M);
-        int launched = 0;
-#define TC_TRY(CO, CH, NS)                                                                                      \
-    if (!launched && cout == CO && cin % CH == 0 &&                                                              \
-        unet_tc::TcSmem<CO, CH, NS>::bytes(cin) <= (size_t)u->smem_optin) {                                      \
-        CUtensorMap map;                                                                                        \
-        if (!act_tensor_map(&map, in, cin, CH, H, W, B)) {                                                       \
-            fprintf(stderr, "thesis_unet: tensor map encoding failed; convolutions fall back to mma.sync\n");   \
-            u->tc = false;                                                                                      \
-            launched = -1;                                                                                      \
-        } else {                                                                                                \
+        int best = -1, best_occ = 1, idx = 0;
+        long long best_score = -1;
+        const int key = cout * 4096 + cin;
+        const bool cached = u->tc_choice.count(key) != 0;
+        if (cached) {
+            best = u->tc_choice[key].first;
+            best_occ = u->tc_choice[key].second;
+        }
+#define TC_LIST(X)                                                                                              \
+    X(16, 64, 3) X(16, 32, 3) X(16, 32, 2) X(16, 16, 4) X(16, 16, 2)                                            \
+    X(32, 64, 3) X(32, 32, 4) X(32, 32, 3) X(32, 32, 2) X(32, 16, 4) X(32, 16, 2)                               \
+    X(64, 64, 3) X(64, 64, 2) X(64, 32, 4) X(64, 32, 3) X(64, 32, 2) X(64, 16, 4) X(64, 16, 2)                  \
+    X(128, 64, 3) X(128, 32, 3) X(128, 32, 2) X(128, 16, 4) X(128, 16, 2)
+#define TC_EVAL(CO, CH, NS)                                                                                     \
+    {                                                                                                           \
+        using SM = unet_tc::TcSmem<CO, CH, NS>;                                                                 \
+        const size_t bytes = SM::bytes(cin);                                                                    \
+        if (cout == CO && cin % CH == 0 && bytes <= (size_t)u->smem_optin) {                                    \
+            auto kern = unet_tc::conv3x3_tc_kernel<CO, CH, NS>;                                                 \
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);                \
+            cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,                          \
+                                 cudaSharedmemCarveoutMaxShared);                                               \
+            const int occ = std::min(std::min((int)(u->smem_per_sm / (bytes + 1024)),                           \
+                                              512 / std::max(32, SM::NA * CO)),                                 \
+                                     resident_by_registers((const void *)kern, 160));                          \
+            const long long score = (long long)occ * CH * std::min(NS - 1, 2) * 1024 + occ * 128 + CH + NS;   \
+            if (occ >= 1 && score > best_score) {                                                               \
+                best_score = score;                                                                             \
+                best = idx;                                                                                     \
+                best_occ = occ;                                                                                 \
+            }                                                                                                   \
+        }                                                                                                       \
+        ++idx;                                                                                                  \
+    }
+#define TC_RUN(CO, CH, NS)                                                                                      \
+    {                                                                                                           \
+        if (idx == best) {                                                                                      \
             auto kern = unet_tc::conv3x3_tc_kernel<CO, CH, NS>;                                                 \
             const int bytes = (int)unet_tc::TcSmem<CO, CH, NS>::bytes(cin);                                     \
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);                     \
-            int per_sm = 1;                                                                                     \
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 160, bytes);                           \
-            constexpr int cols = unet_tc::TcSmem<CO, CH, NS>::NA * CO;                                          \
-            const int tmem_cap = 512 / (cols < 32 ? 32 : cols);                                                 \
-            per_sm = per_sm < 1 ? 1 : (per_sm > tmem_cap ? tmem_cap : per_sm);                                  \
-            const long long g = (long long)u->sms * per_sm < tiles ? (long long)u->sms * per_sm : tiles;         \
+            cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,                          \
+                                 cudaSharedmemCarveoutMaxShared);                                               \
+            const long long g = (long long)u->sms * best_occ < tiles ? (long long)u->sms * best_occ : tiles;    \
             kern<<<(unsigned)g, 160, bytes, u->stream>>>(map, cin, w, bias, op, out.cs, out.co, out32, B, H, W,  \
                                                          relu, u->tc_err);                                      \
-            launched = 1;                                                                                       \
         }                                                                                                       \
+        ++idx;                                                                                                  \
     }
-#define TC_SHAPES(CO) TC_TRY(CO, 64, 3) TC_TRY(CO, 32, 3) TC_TRY(CO, 32, 2) TC_TRY(CO, 16, 4) TC_TRY(CO, 16, 2)
-        TC_SHAPES(16) TC_SHAPES(32) TC_SHAPES(64) TC_SHAPES(128)
-#undef TC_SHAPES
-#undef TC_TRY
-        if (launched == 1) return;
+        if (!cached) {
+            TC_LIST(TC_EVAL)
+            u->tc_choice[key] = std::make_pair(best, best_occ);
+        }
+        if (best >= 0) {
+            int chunk = 0;
+            idx = 0;
+#define TC_CHUNK(CO, CH, NS)                                                                                    \
+    {                                                                                                           \
+        if (idx == best) chunk = CH;                                                                            \
+        ++idx;                                                                                                  \
+    }
+            TC_LIST(TC_CHUNK)
+            CUtensorMap map;
+            if (act_tensor_map(&map, in, cin, chunk, H, W, B)) {
+                idx = 0;
+                TC_LIST(TC_RUN)
+                return;
+            }
+            fprintf(stderr, "thesis_unet: tensor map encoding failed; convolutions fall back to mma.sync\n");
+            u->tc = false;
+        }
+#undef TC_CHUNK
+#undef TC_RUN
+#undef TC_EVAL
+#undef TC_LIST
     }
     switch (cout) {
     case 16: conv3x3_kernel<16><<<grid, 128, 0, u->stream>>>(in.p, in.cs, in.co, cin, w, bias, op, out.cs, out.co, out32, H, W, relu); break;
@@ -629,30 +700,67 @@ bool wgrad_tc(lbm_unet_s *u, const Layer &l, const Act &in, int B, int H, int W,
         u->tc = false;
         return false;
     }
-    bool done = false;
-#define WG_TC(CO, NC, NS)                                                                                      \
-    if (!done && l.cout == CO && nc == NC && unet_tc::WgSmem<CO, NC, NS>::BYTES <= u->smem_optin) {            \
-        using SM = unet_tc::WgSmem<CO, NC, NS>;                                                                \
-        auto kern = unet_tc::wgrad_tc_kernel<CO, NC, NS>;                                                      \
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SM::BYTES);                     \
-        int per_sm = 1;                                                                                        \
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, SM::BYTES);                          \
-        const int tmem_cap = 512 / (int)SM::COLS;                                                              \
-        per_sm = per_sm < 1 ? 1 : (per_sm > tmem_cap ? tmem_cap : per_sm);                                     \
-        const int split = l.cin / NC;                                                                          \
-        long long g = ((long long)u->sms * per_sm + split - 1) / split;                                        \
-        /* at least 8 rows per CTA: each CTA ends with 9 x CO x NC reductions */                               \
-        g = g < (units + 7) / 8 ? g : (units + 7) / 8;                                                         \
-        kern<<<dim3((unsigned)g, split), 128, SM::BYTES, u->stream>>>(tdp, tin, l.cin, dw, B, H, W, u->tc_err); \
-        done = true;                                                                                           \
+    // the most resident CTAs, then the most stages
+    int best = -1, best_occ = 1, idx = 0;
+    long long best_score = -1;
+    const int key = -(l.cout * 4096 + l.cin);
+    const bool cached = u->tc_choice.count(key) != 0;
+    if (cached) {
+        best = u->tc_choice[key].first;
+        best_occ = u->tc_choice[key].second;
     }
-#define WG_SHAPES(CO, NC) WG_TC(CO, NC, 4) WG_TC(CO, NC, 3) WG_TC(CO, NC, 2)
-    WG_SHAPES(16, 16) WG_SHAPES(16, 32) WG_SHAPES(16, 64)
-    WG_SHAPES(32, 16) WG_SHAPES(32, 32) WG_SHAPES(32, 64)
-    WG_SHAPES(64, 16) WG_SHAPES(64, 32) WG_SHAPES(64, 64)
-#undef WG_SHAPES
-#undef WG_TC
-    return done;
+#define WG_LIST(X)                                                                                              \
+    X(16, 16, 4) X(16, 16, 3) X(16, 16, 2) X(16, 32, 4) X(16, 32, 3) X(16, 32, 2) X(16, 64, 4) X(16, 64, 3)     \
+    X(16, 64, 2) X(32, 16, 4) X(32, 16, 3) X(32, 16, 2) X(32, 32, 4) X(32, 32, 3) X(32, 32, 2) X(32, 64, 4)     \
+    X(32, 64, 3) X(32, 64, 2) X(64, 16, 4) X(64, 16, 3) X(64, 16, 2) X(64, 32, 4) X(64, 32, 3) X(64, 32, 2)     \
+    X(64, 64, 4) X(64, 64, 3) X(64, 64, 2)
+#define WG_EVAL(CO, NC, NS)                                                                                     \
+    {                                                                                                           \
+        using SM = unet_tc::WgSmem<CO, NC, NS>;                                                                 \
+        if (l.cout == CO && nc == NC && SM::BYTES <= u->smem_optin) {                                           \
+            auto kern = unet_tc::wgrad_tc_kernel<CO, NC, NS>;                                                   \
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SM::BYTES);                  \
+            cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,                          \
+                                 cudaSharedmemCarveoutMaxShared);                                               \
+            const int occ = std::min(std::min((int)(u->smem_per_sm / (SM::BYTES + 1024)), 512 / (int)SM::COLS),  \
+                                     resident_by_registers((const void *)kern, 128));                          \
+            const long long score = (long long)occ * 16 + NS;                                                  \
+            if (occ >= 1 && score > best_score) {                                                               \
+                best_score = score;                                                                             \
+                best = idx;                                                                                     \
+                best_occ = occ;                                                                                 \
+            }                                                                                                   \
+        }                                                                                                       \
+        ++idx;                                                                                                  \
+    }
+#define WG_RUN(CO, NC, NS)                                                                                      \
+    {                                                                                                           \
+        if (idx == best) {                                                                                      \
+            using SM = unet_tc::WgSmem<CO, NC, NS>;                                                             \
+            auto kern = unet_tc::wgrad_tc_kernel<CO, NC, NS>;                                                   \
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SM::BYTES);                  \
+            cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,                          \
+                                 cudaSharedmemCarveoutMaxShared);                                               \
+            const int split = l.cin / NC;                                                                       \
+            long long g = ((long long)u->sms * best_occ + split - 1) / split;                                   \
+            /* at least 8 rows per CTA: each CTA ends with 9 x CO x NC reductions */                            \
+            g = g < (units + 7) / 8 ? g : (units + 7) / 8;                                                      \
+            kern<<<dim3((unsigned)g, split), 128, SM::BYTES, u->stream>>>(tdp, tin, l.cin, dw, B, H, W,          \
+                                                                          u->tc_err);                           \
+        }                                                                                                       \
+        ++idx;                                                                                                  \
+    }
+    if (!cached) {
+        WG_LIST(WG_EVAL)
+        u->tc_choice[key] = std::make_pair(best, best_occ);
+    }
+    if (best < 0) return false;
+    idx = 0;
+    WG_LIST(WG_RUN)
+#undef WG_RUN
+#undef WG_EVAL
+#undef WG_LIST
+    return true;
 }
 
 void wgrad(lbm_unet_s *u, const Layer &l, const Act &in, int B, int level) {
@@ -862,6 +970,9 @@ int lbm_unet_create(const lbm_unet_config *cfg, lbm_unet *out) {
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&u->sms, cudaDevAttrMultiProcessorCount, dev);
         cudaDeviceGetAttribute(&u->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        int per_sm = 0;
+        cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        u->smem_per_sm = per_sm > 0 ? (size_t)per_sm : (size_t)u->smem_optin;
         if (u->sms < 1) u->sms = 1;
     }
     if (cudaStreamCreateWithFlags(&u->stream, cudaStreamNonBlocking) != cudaSuccess ||
