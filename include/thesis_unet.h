@@ -38,7 +38,8 @@ typedef struct lbm_unet_config {
     int height, width;        /* image = lattice m x n */
     int in_channels;          /* input features per pixel, 1..16 */
     int out_channels;         /* predicted fields per pixel, 1..16 */
-    int max_batch;            /* largest training / prediction batch */
+    int max_batch;            /* largest training / prediction batch;
+                                 max_batch x height x width < 2^27 */
     unsigned long long seed;  /* weight initialisation (He normal) */
     int levels;               /* pooling levels L, 3..5 (0 selects 3); height and
                                  width must be multiples of 2^L */

@@ -164,3 +164,29 @@ def test_gpu_tcgen05_persistent_tiles_match_mma_sync(monkeypatch):
         a, b = g1[s].astype(np.float64), g0[s].astype(np.float64)
         nb = np.linalg.norm(b)
         assert nb > 0 and np.linalg.norm(a - b) <= 3e-2 * nb, (k, np.linalg.norm(a - b) / nb)
+
+
+@pytest.mark.gpu
+def test_gpu_tcgen05_ragged_rows_match_mma_sync(monkeypatch):
+    """Widths that are not multiples of the 128-pixel tile: at 3 x 16 x 384
+    the level-1 rows are 192 pixels (a full and a half tile) and level 2 and 3
+    rows are shorter than one tile, so the tensor copies read past the image
+    edge (zero fill) and the epilogues store only the pixels inside it."""
+    from thesis_gb300.warmstart import UNet
+    B, H, W, ic, oc, levels, base = 3, 16, 384, 4, 3, 3, 32
+    x, t, w = _problem(B, H, W, ic, oc, 23)
+    p = uo.init_params(ic, oc, 29, levels, base)
+    res = {}
+    for tc in ("1", "0"):
+        monkeypatch.setenv("THESIS_UNET_TC", tc)
+        with UNet(H, W, max_batch=B, in_channels=ic, out_channels=oc, levels=levels, base_channels=base) as net:
+            net.set_params(p)
+            net.set_dataset(x, t, w)
+            g, loss = net.gradients(list(range(B)))
+            res[tc] = (net.predict(x), g, loss)
+    (p1, g1, l1), (p0, g0, l0) = res["1"], res["0"]
+    assert np.abs(p1 - p0).max() < 2e-2 * np.abs(p0).max() and abs(l1 - l0) <= 1e-3 * l0
+    for k, s in enumerate(_layer_slices(levels, base)):
+        a, b = g1[s].astype(np.float64), g0[s].astype(np.float64)
+        nb = np.linalg.norm(b)
+        assert nb > 0 and np.linalg.norm(a - b) <= 3e-2 * nb, (k, np.linalg.norm(a - b) / nb)

@@ -1039,8 +1039,13 @@ int lbm_unet_create(const lbm_unet_config *cfg, lbm_unet *out) {
     const size_t np = (size_t)cfg->max_batch * cfg->height * cfg->width;
     rc = rc ? rc : alloc(u, (void **)&u->out32, np * 16 * sizeof(float));
     rc = rc ? rc : alloc(u, (void **)&u->dout, np * 16 * sizeof(bf16));
-    // largest pre-activation gradient: level 0 x 16 channels (level l holds 16 * 2^l channels on 4^-l pixels)
-    rc = rc ? rc : alloc(u, (void **)&u->dpre, np * 16 * sizeof(bf16));
+    // largest pre-activation gradient: the output layer's 16 channels at level
+    // 0, or the widest level's channels (ch(l) on 4^-l of the pixels; base 32
+    // puts 32 channels on level 0)
+    size_t dpre_elems = np * 16;
+    for (int l = 0; l <= NL; ++l)
+        dpre_elems = std::max(dpre_elems, (size_t)ch(u, l) * cfg->max_batch * H_of(u, l) * W_of(u, l));
+    rc = rc ? rc : alloc(u, (void **)&u->dpre, dpre_elems * sizeof(bf16));
     rc = rc ? rc : alloc(u, (void **)&u->fin, np * 16 * sizeof(float));
     rc = rc ? rc : alloc(u, (void **)&u->fout, np * 16 * sizeof(float));
     rc = rc ? rc : alloc(u, (void **)&u->tgt, np * 16 * sizeof(float));
