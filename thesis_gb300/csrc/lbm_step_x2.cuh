@@ -239,37 +239,36 @@ __device__ __forceinline__ void collide_mrt9_x2(V (&h)[9], V rho, V rms, V ux, V
     E[6] = -E[5];
     E[7] = Sv * (rho * (ux * ux - uy * uy));
     E[8] = Sv * (rho * (ux * uy));
-    const float s[9] = {0.f, 1.4f, 1.4f, 0.f, 1.2f, 0.f, 1.2f, omega, omega};
-    V dm[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-        if (s[k] == 0.f) {
-            dm[k] = 0.f;
-            continue;
-        }
-        V m = 0.f;
-#pragma unroll
-        for (int i = 0; i < 9; ++i) {
-            const int c = mrt2(k, i);
-            if (c == 1) m += h[i];
-            else if (c == -1) m -= h[i];
-            else if (c != 0) m = fma2(V((float)c), h[i], m);
-        }
-        dm[k] = V(s[k] / (float)mrt2_norm(k)) * (m - E[k]);
-    }
-#pragma unroll
-    for (int i = 0; i < 9; ++i) {
-        V c = 0.f;
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            const int mk = mrt2(k, i);
-            if (s[k] == 0.f || mk == 0) continue;
-            if (mk == 1) c += dm[k];
-            else if (mk == -1) c -= dm[k];
-            else c = fma2(V((float)mk), dm[k], c);
-        }
-        h[i] -= c;
-    }
+    // The moment transform of the D2Q9 matrix (mrt2) in pair form: with
+    // opposite pairs (1,3), (2,4), (5,7), (6,8), the even moments (e, eps,
+    // pxx, pxy) take the pair sums and the odd ones (qx, qy) the pair
+    // differences; the back-transform adds a part S shared by a pair and a
+    // part O with opposite signs.  Same operator as the 9 x 9 form, about
+    // 40 % fewer instructions.
+    const V A = h[1] + h[3], B = h[2] + h[4], C = h[5] + h[7], D = h[6] + h[8];
+    const V a = h[1] - h[3], b = h[2] - h[4], c = h[5] - h[7], d = h[6] - h[8];
+    const V AB = A + B, CD = C + D;
+    const V m1 = fma2(V(2.f), CD, fma2(V(-4.f), h[0], -AB));   // e
+    const V m2 = fma2(V(-2.f), AB, fma2(V(4.f), h[0], CD));    // eps
+    const V m4 = fma2(V(-2.f), a, c - d);                      // qx
+    const V m6 = fma2(V(-2.f), b, c + d);                      // qy
+    const V m7 = A - B;                                        // pxx
+    const V m8 = C - D;                                        // pxy
+    const V dm1 = V(1.4f / 36.f) * (m1 - E[1]), dm2 = V(1.4f / 36.f) * (m2 - E[2]);
+    const V dm4 = V(1.2f / 12.f) * (m4 - E[4]), dm6 = V(1.2f / 12.f) * (m6 - E[6]);
+    const V dm7 = V(omega / 4.f) * (m7 - E[7]), dm8 = V(omega / 4.f) * (m8 - E[8]);
+    const V t1 = fma2(V(-2.f), dm2, -dm1), t2 = fma2(V(2.f), dm1, dm2);
+    const V S13 = t1 + dm7, S24 = t1 - dm7, S57 = t2 + dm8, S68 = t2 - dm8;
+    const V O13 = V(-2.f) * dm4, O24 = V(-2.f) * dm6, O57 = dm4 + dm6, O68 = dm6 - dm4;
+    h[0] -= V(4.f) * (dm2 - dm1);
+    h[1] -= S13 + O13;
+    h[3] -= S13 - O13;
+    h[2] -= S24 + O24;
+    h[4] -= S24 - O24;
+    h[5] -= S57 + O57;
+    h[7] -= S57 - O57;
+    h[6] -= S68 + O68;
+    h[8] -= S68 - O68;
 }
 
 // rms = rho - sigma, the density's deviation from the shift's density,
