@@ -378,8 +378,9 @@ __device__ __forceinline__ void red_add4(float *dst, float a, float b, float c, 
 // CO channels each); the A operand stacks them along M as (row, co), so M
 // row m holds channel m % CO of row y - 1 + m / CO, i.e. tap row
 // ky = 2 - m / CO, in M_BLOCKS blocks of 128 (rows past 3 x CO read staging
-// memory no result uses).  A second copy stages the input row (TC_BOX
-// pixels from x0 - 1) for NC input channels: the B operand, whose tap shift
+// memory no result uses: the input row or the next stage).  A second copy
+// stages the input row (TC_BOX pixels from x0 - 1) right after the three
+// rows, for NC input channels: the B operand, whose tap shift
 // kx is a start address kx pixel rows further.  Both operands are
 // channel-contiguous per pixel, "MN-major" (the instruction descriptor's
 // transpose bits), swizzled by their row bytes (2 x CO and 2 x NC): the
@@ -395,11 +396,19 @@ template <int CO, int NC, int NS>
 struct WgSmem {
     static constexpr int ROWB_A = CO * 2, ROWB_B = NC * 2;
     static constexpr int M_BLOCKS = 3 * CO > 128 ? 2 : 1;
-    static constexpr int A_ROWS = 3 * TC_M * ROWB_A;              // bytes the copy writes
-    static constexpr int A_STAGE = M_BLOCKS * 128 * TC_M * 2;     // bytes the MMAs may read
+    // The copy writes the three rows (A_ROWS bytes, a whole number of 1 KB
+    // swizzle atoms) and B right after them; the MMAs of an M block read
+    // 128 rows of CO channels from the stage start (A_SPAN bytes), so the
+    // rows past 3 x CO fall on B or the next stage: in bounds, and they only
+    // feed accumulator rows no result uses.  TAIL keeps the last stage's
+    // span inside the allocation.
+    static constexpr int A_ROWS = 3 * TC_M * ROWB_A;
+    static constexpr int A_STAGE = A_ROWS;                        // offset of B in a stage
+    static constexpr int A_SPAN = M_BLOCKS * 128 * TC_M * 2;
     static constexpr int B_STAGE = TC_BOX * ROWB_B;
     static constexpr int STAGE = (A_STAGE + B_STAGE + 1023) / 1024 * 1024;
-    static constexpr int BYTES = 1024 + NS * STAGE + 16 * NS + 16;
+    static constexpr int TAIL = A_SPAN > STAGE ? A_SPAN - STAGE : 0;
+    static constexpr int BYTES = 1024 + NS * STAGE + TAIL + 16 * NS + 16;
     static constexpr int USED = M_BLOCKS * 3 * NC;
     static constexpr uint32_t COLS = USED <= 32 ? 32 : USED <= 64 ? 64 : USED <= 128 ? 128 : USED <= 256 ? 256 : 512;
 };
@@ -428,7 +437,7 @@ wgrad_tc_kernel(const __grid_constant__ CUtensorMap tdp, const __grid_constant__
     unsigned char *smem = smem_raw + (base - raw);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ci0 = blockIdx.y * NC;
-    uint64_t *bars = (uint64_t *)(smem + NS * STAGE);
+    uint64_t *bars = (uint64_t *)(smem + NS * STAGE + SM::TAIL);
     const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * NS;
     uint32_t *tmem_slot = (uint32_t *)(bars + 2 * NS);
     const int xt = (W + TC_M - 1) / TC_M;
