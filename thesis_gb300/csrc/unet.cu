@@ -542,19 +542,18 @@ int resident_by_registers(const void *kern, int threads) {
     return std::max(1, std::min(by_regs, 2048 / threads));
 }
 
-// The driver's tensor-map encoder, through the runtime (no -lcuda).
+// The driver's tensor-map encoder, through the runtime (no -lcuda); looked
+// up once per process (a function-local static is initialised thread-safely).
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
         cudaDriverEntryPointQueryResult q;
         void *p = nullptr;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    }
+            return (PFN_cuTensorMapEncodeTiled_v12000)p;
+        return nullptr;
+    }();
     return fn;
 }
 
